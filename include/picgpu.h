@@ -1,0 +1,324 @@
+/*
+ * picgpu.h -- C ABI of the GB300-native picFoam particle hot path.
+ *
+ * One context (picgpu_ctx) owns a device-resident PIC/MCC case: a hex mesh,
+ * structure-of-arrays particle storage per species, the electric potential
+ * and field, and the sub-model selection.  Every entry point takes plain
+ * pointers and sizes, returns a picgpu_status and never aborts or traps.
+ *
+ * Each entry point replaces a run-time-selected picFoam sub-model call or a
+ * whole-population loop of the PICCloud evolve step (paths are relative to
+ * the picFoam source tree):
+ *
+ *   picgpu_create            PICCloud constructor + sub-model selection
+ *                            (PICMCCFVM/clouds/Templates/PICCloud/PICCloud.C:378-518)
+ *   picgpu_set_particles     picInitialise parcel creation / PICCloud::addNewParcel
+ *                            (PICCloud.C:707-723)
+ *   picgpu_step              PICCloud::evolve (PICCloud.C:1426-1471): move (push,
+ *                            track, patch interaction), collisions, calculateFields,
+ *                            boundary pre/post updates, Maxwell solve
+ *   picgpu_solve_poisson     ElectroStaticSolver::solveFields
+ *                            (submodels/MaxwellSolver/ElectroStatic/ElectroStaticSolver.C:52-71)
+ *   picgpu_get_particles     parcel write-out (PICParcelIO.C:83-166)
+ *   picgpu_get_field         field access (phiE, E, rhoCharge)
+ *
+ * Threading: one context per host thread; calls on one context are not
+ * re-entrant.  The library owns all device memory; caller buffers are copied.
+ */
+#ifndef PICGPU_H
+#define PICGPU_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef enum {
+    PICGPU_OK = 0,
+    PICGPU_INVALID_ARG = 1,
+    PICGPU_OOM = 2,
+    PICGPU_TRACK_LOOP_CAP = 3,      /* a particle exceeded the tet-step cap   */
+    PICGPU_PCG_NOT_CONVERGED = 4,   /* Poisson PCG hit its iteration cap      */
+    PICGPU_NAN_DETECTED = 5,
+    PICGPU_CUDA_ERROR = 6,
+    PICGPU_SPEED_OF_LIGHT = 7,      /* |U| >= c after a push (PICParcel.C:61-66) */
+    PICGPU_CAPACITY = 8,            /* particle storage capacity exceeded     */
+    PICGPU_NOT_SUPPORTED = 9
+} picgpu_status;
+
+/* ParticlePusher TypeNames: "none", "Boris", "BorisNR", "Vay", "HigueraCary" */
+enum {
+    PICGPU_PUSHER_NONE = 0,
+    PICGPU_PUSHER_BORIS = 1,
+    PICGPU_PUSHER_BORIS_NR = 2,
+    PICGPU_PUSHER_VAY = 3,
+    PICGPU_PUSHER_HIGUERA_CARY = 4
+};
+
+/* FieldWeigthing / ChargeDistribution TypeNames: "CellAverage", "VolumeWeighting" */
+enum {
+    PICGPU_WEIGHTING_CELL_AVERAGE = 0,
+    PICGPU_WEIGHTING_VOLUME = 1
+};
+
+/* MaxwellSolver TypeNames: "none", "ElectroStatic" */
+enum {
+    PICGPU_MAXWELL_NONE = 0,
+    PICGPU_MAXWELL_ELECTROSTATIC = 1
+};
+
+/* Arithmetic form of push + track. */
+enum {
+    PICGPU_PREC_FP64 = 0,   /* FP64 barycentric + velocity (exact form)            */
+    PICGPU_PREC_MIXED = 1   /* FP32 barycentric + velocity, FP64 charge and Poisson */
+};
+
+/* Charge accumulation. */
+enum {
+    PICGPU_DEPOSIT_ATOMIC_FP64 = 0,  /* FP64 atomics: order-dependent round-off     */
+    PICGPU_DEPOSIT_FIXED_POINT = 1   /* 64-bit fixed point: order-independent sums  */
+};
+
+/* Particle-side behaviour of a boundary patch. */
+enum {
+    PICGPU_PATCH_CYCLIC = 0,    /* periodic pair (OpenFOAM cyclic)                    */
+    PICGPU_PATCH_EMPTY = 1,     /* reduced-D direction (OpenFOAM empty)               */
+    PICGPU_PATCH_ABSORB = 2,    /* patch + BoundaryModel "none" (NoInflow.C:56-61)    */
+    PICGPU_PATCH_WALL = 3,      /* wall + WallReflectionModel SpecularReflection      */
+    PICGPU_PATCH_FLOATING = 4   /* BoundaryModel FloatingPotential + circuitBoundary  */
+};
+
+/* Potential boundary condition of an ABSORB or WALL patch. */
+enum {
+    PICGPU_PHI_FIXED_VALUE = 0,
+    PICGPU_PHI_ZERO_GRADIENT = 1
+};
+
+typedef struct {
+    int32_t kind;     /* PICGPU_PATCH_* */
+    int32_t phi_bc;   /* PICGPU_PHI_* (ABSORB / WALL only) */
+    double  phi;      /* fixedValue of the potential [V] */
+} picgpu_patch;
+
+/* A box of cells [lo, hi) removed from the block; its surface is one patch
+ * (an embedded electrode). */
+typedef struct {
+    int32_t lo[3];
+    int32_t hi[3];
+    picgpu_patch patch;
+} picgpu_box;
+
+#define PICGPU_MAX_BOXES 8
+
+/* blockMesh-style hexahedral block: n[0] x n[1] x n[2] uniform cells. */
+typedef struct {
+    int32_t n[3];
+    double  origin[3];
+    double  length[3];
+    picgpu_patch side[6];          /* -x, +x, -y, +y, -z, +z */
+    int32_t n_boxes;
+    picgpu_box box[PICGPU_MAX_BOXES];
+} picgpu_mesh_desc;
+
+#define PICGPU_MAX_SPECIES 4
+
+/* moleculeProperties entry (PICParcel.H:81-138). */
+typedef struct {
+    double  mass;           /* [kg] */
+    double  charge;         /* [C] per real particle */
+    double  weight;         /* nEquivalentParticles */
+    int32_t solve_movement; /* solveMovement */
+    int32_t capacity_hint;  /* optional storage capacity (0: automatic) */
+} picgpu_species;
+
+/* Background gas (uniformBackground.C:36-127) and null-collision MCC
+ * (ElectronNeutralCollisionModel.C:703-829) with List cross sections. */
+#define PICGPU_MAX_XS_POINTS 1024
+typedef struct {
+    int32_t enabled;           /* ElectronNeutralCollisionModel != none */
+    int32_t scatter;           /* 0: NanbuElectronNeutral, 1: RelativisticElectronNeutral */
+    int32_t create_electron;   /* createElectron */
+    int32_t create_ion;        /* createIon */
+    int32_t ion_species;       /* species index of the created ion (-1: none) */
+    int32_t n_xs;              /* cross-section table length */
+    double  gas_density;       /* [m^-3] */
+    double  gas_temperature;   /* [K] */
+    double  gas_mass;          /* [kg] */
+    double  gas_velocity[3];   /* drift [m/s] */
+    double  gas_weight;        /* background nEquivalentParticles */
+    double  ex_threshold;      /* [eV] */
+    double  iz_threshold;      /* [eV] */
+    double  sigma_v_max_init;  /* initial (sigma v)_max per cell [m^3/s]; 0: FindMaximum */
+    double  find_max_energy;   /* FindMaximum search: maximumEnergy [eV] */
+    double  find_energy_step;  /* FindMaximum search: energyStep [eV] */
+    const double* xs_energy;   /* [n_xs] eV, ascending */
+    const double* xs_elastic;  /* [n_xs] m^2 */
+    const double* xs_excitation;
+    const double* xs_ionization;
+} picgpu_mcc;
+
+/* Binary Coulomb collisions (CoulombCollisionModel.C:241-309). */
+typedef struct {
+    int32_t enabled;
+    int32_t pairing;           /* 0: NanbuYonemura, 1: TakizukaAbe */
+    int32_t collide;           /* 0: Nanbu */
+    int32_t allow_intra;       /* allowIntraCollision */
+    double  coulomb_log;       /* fixed coulombLog (> 0); 0 not supported yet */
+} picgpu_coulomb;
+
+typedef struct {
+    int32_t pusher;               /* PICGPU_PUSHER_* */
+    int32_t field_weighting;      /* PICGPU_WEIGHTING_* */
+    int32_t charge_distribution;  /* PICGPU_WEIGHTING_* */
+    int32_t maxwell_solver;       /* PICGPU_MAXWELL_* */
+    int32_t precision;            /* PICGPU_PREC_* */
+    int32_t deposit_mode;         /* PICGPU_DEPOSIT_* */
+    int32_t n_species;
+    int32_t electron_species;     /* SpeciesRelations electronTypeId (-1: none) */
+    picgpu_species species[PICGPU_MAX_SPECIES];
+    double  dt;                   /* deltaT [s] */
+    double  B[3];                 /* uniform magnetic field [T] */
+    double  E_applied[3];         /* uniform field used when maxwell_solver is NONE [V/m] */
+    double  space_charge;         /* SolverSettings spaceCharge [C/m^3] */
+    int32_t sync_velocity_at_boundary;
+    int32_t track_max_steps;      /* tet steps per particle per time step (0: 4096) */
+    double  pcg_tol;              /* relative residual target */
+    int32_t pcg_max_iter;
+    int32_t pcg_norm;             /* 0: ||r||2/||b||2, 1: OpenFOAM-normalised L1 residual */
+    int32_t sort_interval;        /* cell re-sort every N steps (0: never unless needed) */
+    int32_t pad0;
+    uint64_t seed;
+    picgpu_mcc mcc;
+    picgpu_coulomb coulomb;
+} picgpu_config;
+
+typedef struct {
+    int64_t n_particles[PICGPU_MAX_SPECIES];
+    int64_t n_absorbed[PICGPU_MAX_SPECIES];    /* removed at patches this call */
+    int64_t tet_steps;                          /* tet-to-tet moves this call */
+    int64_t face_crossings;                     /* cell-face crossings this call */
+    int64_t wall_hits;
+    int32_t pcg_iterations;                     /* last solve */
+    int32_t pcg_iterations_total;               /* summed over the call */
+    double  pcg_residual_l2;                    /* last solve ||b-Ax||2/||b||2 */
+    double  pcg_residual_of;                    /* last solve OpenFOAM-normalised */
+    int64_t mcc_candidates;
+    int64_t mcc_elastic;
+    int64_t mcc_excitation;
+    int64_t mcc_ionization;
+    int64_t coulomb_pairs;
+    double  floating_charge[PICGPU_MAX_BOXES + 6]; /* accumulated surface charge per patch [C] */
+} picgpu_step_stats;
+
+typedef struct picgpu_ctx picgpu_ctx;
+
+/* Field selectors for picgpu_get_field. */
+enum {
+    PICGPU_FIELD_PHI = 0,        /* n_cells          */
+    PICGPU_FIELD_E_CELL = 1,     /* n_cells x 3      */
+    PICGPU_FIELD_RHO = 2,        /* n_cells          */
+    PICGPU_FIELD_E_POINT = 3,    /* n_points x 3 (cyclic-merged point numbering) */
+    PICGPU_FIELD_SIGMA_V_MAX = 4 /* n_cells          */
+};
+
+/* Size queries. */
+typedef struct {
+    int64_t n_cells;
+    int64_t n_points;        /* cyclic-merged points */
+    int64_t n_tets;          /* 12 per cell */
+    int64_t n_patches;
+} picgpu_mesh_info;
+
+/* Build the context: mesh, sub-models, device buffers. */
+picgpu_status picgpu_create(const picgpu_mesh_desc* mesh, const picgpu_config* cfg,
+                            picgpu_ctx** out);
+void          picgpu_destroy(picgpu_ctx* ctx);
+const char*   picgpu_last_error(const picgpu_ctx* ctx);
+picgpu_status picgpu_mesh_query(const picgpu_ctx* ctx, picgpu_mesh_info* info);
+
+/* Host-only mesh handle (no GPU needed): the blockMesh + tet decomposition
+ * the context builds, for placing particles (picInitialise,
+ * preProcess/picInitialise/picInitialise.C:30-319) and reading positions. */
+typedef struct picgpu_mesh picgpu_mesh;
+picgpu_status picgpu_mesh_create(const picgpu_mesh_desc* desc, picgpu_mesh** out);
+void          picgpu_mesh_destroy(picgpu_mesh* mesh);
+picgpu_status picgpu_mesh_info_get(const picgpu_mesh* mesh, picgpu_mesh_info* info);
+/* Locate Cartesian positions: tet index (cell*12 + local tet) and the three
+ * barycentric coordinates on the tet's face triangle (row-major n x 3); the
+ * cell-centre coordinate is 1 - sum.  Unlocated points get tet = -1. */
+picgpu_status picgpu_mesh_locate(const picgpu_mesh* mesh, size_t n, const double* xyz,
+                                 int32_t* tet, double* bary);
+/* Cartesian position of (tet, bary). */
+picgpu_status picgpu_mesh_position(const picgpu_mesh* mesh, size_t n, const int32_t* tet,
+                                   const double* bary, double* xyz);
+/* Cell centres (n_cells x 3) and volumes (n_cells). */
+picgpu_status picgpu_mesh_cells(const picgpu_mesh* mesh, double* centres, double* volumes);
+
+/* Replace the particles of one species (host buffers, row-major n x 3). */
+picgpu_status picgpu_set_particles(picgpu_ctx* ctx, int species, size_t n,
+                                   const int32_t* tet, const double* bary,
+                                   const double* U);
+picgpu_status picgpu_count_particles(picgpu_ctx* ctx, int species, size_t* n);
+/* Copy one species out, compacted (removed particles dropped), in storage order. */
+picgpu_status picgpu_get_particles(picgpu_ctx* ctx, int species, size_t cap,
+                                   int32_t* tet, double* bary, double* U, size_t* n);
+
+/* Deposit the current particles and solve the fields (what picInitialise does
+ * before the first step: calculateFields + solveFields). */
+picgpu_status picgpu_initialise_fields(picgpu_ctx* ctx);
+
+/* Advance nsteps time steps. */
+picgpu_status picgpu_step(picgpu_ctx* ctx, int nsteps, picgpu_step_stats* stats);
+
+/* One pass of push + track + deposit over all particles (no collisions, no
+ * field solve): the particle hot path alone. */
+picgpu_status picgpu_move(picgpu_ctx* ctx, picgpu_step_stats* stats);
+
+/* ElectroStatic solve on a caller charge density (n_cells); writes the
+ * potential (n_cells) and updates E. phi_inout is the initial guess. */
+picgpu_status picgpu_solve_poisson(picgpu_ctx* ctx, const double* rho,
+                                   double* phi_inout, picgpu_step_stats* stats);
+
+picgpu_status picgpu_get_field(picgpu_ctx* ctx, int which, double* out, size_t n);
+picgpu_status picgpu_set_field(picgpu_ctx* ctx, int which, const double* in, size_t n);
+
+/* Diagnostics (KineticEnergyInfo, FieldEnergyInfo, TemperatureInfo). */
+typedef struct {
+    double kinetic_energy[PICGPU_MAX_SPECIES];       /* sum 0.5 w m |U|^2 [J] */
+    double kinetic_energy_rel[PICGPU_MAX_SPECIES];   /* sum (gamma-1) m c^2 (no weight, KineticEnergyInfo.C:75-77) */
+    double momentum[PICGPU_MAX_SPECIES][3];          /* sum w m U */
+    double velocity_sq[PICGPU_MAX_SPECIES][3];       /* sum w U_i^2 */
+    double weight_sum[PICGPU_MAX_SPECIES];           /* sum w */
+    double field_energy;                              /* 0.5 eps0 sum |E|^2 V [J] */
+} picgpu_diagnostics;
+picgpu_status picgpu_diagnostics_compute(picgpu_ctx* ctx, picgpu_diagnostics* out);
+
+/* Phase timing with CUDA events on the context stream. */
+enum {
+    PICGPU_PHASE_MOVE = 0,       /* push + track + deposit kernel */
+    PICGPU_PHASE_CHARGE = 1,     /* point -> cell charge           */
+    PICGPU_PHASE_POISSON = 2,    /* PCG                            */
+    PICGPU_PHASE_EFIELD = 3,     /* gradient + cell -> point       */
+    PICGPU_PHASE_SORT = 4,
+    PICGPU_PHASE_MCC = 5,
+    PICGPU_PHASE_COULOMB = 6,
+    PICGPU_PHASE_COUNT = 7
+};
+picgpu_status picgpu_set_profiling(picgpu_ctx* ctx, int enabled);
+/* Per phase: summed milliseconds and launch counts since the last reset. */
+picgpu_status picgpu_phase_times(picgpu_ctx* ctx, double* ms, int64_t* launches,
+                                 int nphase, int reset);
+/* Kernels launched by the library since creation (all phases). */
+int64_t       picgpu_kernel_launches(const picgpu_ctx* ctx);
+picgpu_status picgpu_synchronize(picgpu_ctx* ctx);
+/* Device-time region on the context stream: start records an event, stop
+ * records a second one, synchronises and returns the elapsed milliseconds. */
+picgpu_status picgpu_timer_start(picgpu_ctx* ctx);
+picgpu_status picgpu_timer_stop(picgpu_ctx* ctx, double* ms);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* PICGPU_H */

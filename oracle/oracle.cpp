@@ -1,0 +1,1314 @@
+// oracle.cpp -- CPU restatement of the picFoam per-time-step hot path.
+//
+// TEST INFRASTRUCTURE ONLY (the checker for the CUDA library and the timed
+// CPU baseline); nothing in the product links it.  Parity against picFoam
+// binaries is unpinned: picFoam needs OpenFOAM-9 to build and ships no test
+// vectors, so this restatement is pinned by analytic known-answer tests.
+//
+// Structure follows the reference: parcels are records kept in insertion
+// order (PICParcel in an IDLList), each time step runs PICCloud::evolve
+// (PICMCCFVM/clouds/Templates/PICCloud/PICCloud.C:1426-1471) as a sequence
+// of whole-cloud passes.  File:line citations below are relative to the
+// picFoam source tree (PICMCCFVM/ abbreviated as PIC/, PIC/submodels as SM/).
+//
+// The OpenFOAM-9 pieces picFoam calls into (barycentric tet tracking,
+// interpolationCellPoint, fvm::laplacian + PCG, fvc::grad) are restated from
+// their published descriptions, not from OpenFOAM source.
+//
+// Floating point: compiled with -ffp-contract=off; every expression below is
+// written in the evaluation order the CUDA kernels use so that the FP64 form
+// agrees bit for bit.
+
+#include "oracle.h"
+#include "collisions.hpp"
+#include "../picfoam_gb300/csrc/hexmesh.hpp"
+
+#include <algorithm>
+#include <chrono>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <string>
+#include <thread>
+#include <vector>
+
+namespace {
+
+using pg::HexMesh;
+
+// CODATA constants (values used throughout the project).
+constexpr double kC = 299792458.0;
+constexpr double kPi = 3.14159265358979323846;
+constexpr double kMu0 = 4.0 * kPi * 1e-7;
+const double kEps0 = 1.0 / (kMu0 * kC * kC);
+
+struct V3 { double x, y, z; };
+inline V3 v3(double a, double b, double c) { return V3{a, b, c}; }
+inline V3 add(V3 a, V3 b) { return v3(a.x + b.x, a.y + b.y, a.z + b.z); }
+inline V3 sub(V3 a, V3 b) { return v3(a.x - b.x, a.y - b.y, a.z - b.z); }
+inline V3 smul(double s, V3 a) { return v3(s * a.x, s * a.y, s * a.z); }
+inline V3 sdiv(V3 a, double s) { return v3(a.x / s, a.y / s, a.z / s); }
+inline double dotv(V3 a, V3 b) { return a.x * b.x + a.y * b.y + a.z * b.z; }
+inline double magv(V3 a) { return std::sqrt(dotv(a, a)); }
+inline V3 crossv(V3 a, V3 b) {
+    return v3(a.y * b.z - a.z * b.y, a.z * b.x - a.x * b.z, a.x * b.y - a.y * b.x);
+}
+
+struct Parcel {
+    int cell = 0;
+    int tet = 0;         // local tet 0..11
+    double y[4] = {1, 0, 0, 0};
+    V3 U{0, 0, 0};
+    bool alive = true;
+};
+
+// Deterministic reduction: the fixed order the CUDA kernels reduce in
+// (256 threads, 8 strided items per thread, warp xor-tree, 8-warp tree).
+double tree_block(const double* acc /*256*/) {
+    double w[8];
+    for (int wi = 0; wi < 8; ++wi) {
+        double a[32];
+        for (int l = 0; l < 32; ++l) a[l] = acc[32 * wi + l];
+        for (int off = 16; off >= 1; off >>= 1)
+            for (int l = 0; l < off; ++l) a[l] = a[l] + a[l + off];
+        w[wi] = a[0];
+    }
+    for (int off = 4; off >= 1; off >>= 1)
+        for (int l = 0; l < off; ++l) w[l] = w[l] + w[l + off];
+    return w[0];
+}
+
+template <class F>
+double det_sum(long n, F term) {
+    const long chunk = 2048;
+    const long nb = (n + chunk - 1) / chunk;
+    std::vector<double> part(std::max<long>(nb, 1), 0.0);
+    double acc[256];
+    for (long b = 0; b < nb; ++b) {
+        for (int t = 0; t < 256; ++t) {
+            double s = 0.0;
+            for (int j = 0; j < 8; ++j) {
+                const long i = b * chunk + long(j) * 256 + t;
+                if (i < n) s = s + term(i);
+            }
+            acc[t] = s;
+        }
+        part[b] = tree_block(acc);
+    }
+    for (int t = 0; t < 256; ++t) {
+        double s = 0.0;
+        for (long i = t; i < nb; i += 256) s = s + part[i];
+        acc[t] = s;
+    }
+    return tree_block(acc);
+}
+
+struct Oracle {
+    picgpu_config cfg{};
+    HexMesh m;
+    int nthreads = 1;
+    int precond = ORACLE_PRECOND_JACOBI;
+    std::string err;
+    std::vector<std::vector<Parcel>> cloud;  // per species, insertion order
+    // fields
+    std::vector<double> phi, rho, E, Ept, Eb;
+    std::vector<double> ccData, vtxData;     // VolumeWeighting accumulators
+    std::vector<long long> ccFix, vtxFix;    // fixed-point accumulators
+    double fixScale = 1.0;
+    std::vector<double> Mdiag, Moff, dinv;   // SPD Poisson operator -laplacian
+    std::vector<double> sigma, gradBC, Qconv; // per patch floating state
+    bool rotation = false;
+    double move_seconds = 0;
+    long long step_index = 0;
+    // collision state
+    std::vector<double> svmax, remainder;
+    int last_pcg_iter = 0;
+    double last_res_l2 = 0, last_res_of = 0;
+    picgpu_step_stats acc{};
+    ocoll::Tables xs;
+};
+
+// ------------------------------------------------------------ pushers -----
+// E at the particle: FieldWeigthing (SM/FieldWeigthing).
+// VolumeWeighting (VolumeWeightingFW.C:60-67 -> interpolationCellPoint):
+//   E = y0 E_cell + y1 E_pt[tri0] + y2 E_pt[tri1] + y3 E_pt[tri2].
+// CellAverage (CellAverageFW.C:58-65): E = E_cell.
+V3 field_at(const Oracle& o, const Parcel& p) {
+    const HexMesh& m = o.m;
+    const double* Ec = &o.E[3 * size_t(p.cell)];
+    if (o.cfg.field_weighting == PICGPU_WEIGHTING_CELL_AVERAGE) return v3(Ec[0], Ec[1], Ec[2]);
+    const int* cp = &m.cell_pt[8 * size_t(p.cell)];
+    const double* e1 = &o.Ept[3 * size_t(cp[m.tt.tri[p.tet][0]])];
+    const double* e2 = &o.Ept[3 * size_t(cp[m.tt.tri[p.tet][1]])];
+    const double* e3 = &o.Ept[3 * size_t(cp[m.tt.tri[p.tet][2]])];
+    double r[3];
+    for (int a = 0; a < 3; ++a)
+        r[a] = Ec[a] * p.y[0] + e1[a] * p.y[1] + e2[a] * p.y[2] + e3[a] * p.y[3];
+    return v3(r[0], r[1], r[2]);
+}
+
+// BorisPusher::updateVelocity (SM/ParticlePusher/BorisPusher/BorisPusher.C:69-112)
+void push_boris(const Oracle& o, Parcel& p, double q, double mass, double trackTime) {
+    const V3 E = field_at(o, p);
+    const V3 B = v3(o.cfg.B[0], o.cfg.B[1], o.cfg.B[2]);  // B[celli], uniform
+    const double dt2 = 0.5 * trackTime;
+    const double mU = magv(p.U) / kC;
+    V3 rU = sdiv(p.U, std::sqrt(1.0 - mU * mU));
+    const V3 oldrU = rU;
+    const double qdm = q * dt2 / mass;
+    const V3 rUsm = smul(qdm, E);
+    rU = add(rU, rUsm);
+    if (o.rotation) {
+        const double a0 = magv(oldrU) / kC, a1 = magv(rU) / kC;
+        const double lF = (std::sqrt(1.0 + a0 * a0) + std::sqrt(1.0 + a1 * a1)) / 2.0;
+        const V3 t = sdiv(smul(qdm, B), lF);
+        const V3 Udash = add(rU, crossv(rU, t));
+        const double den = 1.0 + dotv(t, t);
+        const V3 s = sdiv(smul(2.0, t), den);
+        rU = add(rU, crossv(Udash, s));
+    }
+    rU = add(rU, rUsm);
+    const double mr = magv(rU) / kC;
+    p.U = sdiv(rU, std::sqrt(1.0 + mr * mr));
+}
+
+// BorisNRPusher::updateVelocity (SM/ParticlePusher/BorisNRPusher/BorisNRPusher.C:69-99)
+void push_boris_nr(const Oracle& o, Parcel& p, double q, double mass, double trackTime) {
+    const V3 E = field_at(o, p);
+    const V3 B = v3(o.cfg.B[0], o.cfg.B[1], o.cfg.B[2]);
+    const double dt2 = 0.5 * trackTime;
+    const double alpha = q * dt2 / mass;
+    V3 U = add(p.U, smul(alpha, E));
+    if (o.rotation) {
+        const V3 t = smul(alpha, B);
+        const V3 Udash = add(U, crossv(U, t));
+        const double den = 1.0 + dotv(t, t);
+        U = add(U, crossv(Udash, sdiv(smul(2.0, t), den)));
+    }
+    p.U = add(U, smul(alpha, E));
+}
+
+// VayPusher::updateVelocity (SM/ParticlePusher/VayPusher/VayPusher.C:54-100);
+// the rotation term uses the velocity v, not u (VayPusher.C:81).
+void push_vay(const Oracle& o, Parcel& p, double q, double mass, double trackTime) {
+    const V3 E = field_at(o, p);
+    const V3 B = v3(o.cfg.B[0], o.cfg.B[1], o.cfg.B[2]);
+    const double dt2 = 0.5 * trackTime;
+    const double mU = magv(p.U) / kC;
+    const double lF = 1.0 / std::sqrt(1.0 - mU * mU);
+    V3 rU = smul(lF, p.U);
+    V3 Ud = add(rU, smul(q * trackTime / mass, E));
+    V3 T = smul(q * dt2 / mass, B);
+    Ud = add(Ud, crossv(p.U, T));
+    const double mUd = magv(Ud) / kC;
+    double alpha = 1.0 + mUd * mUd;
+    const double T2 = dotv(T, T);
+    double s = alpha - T2;
+    const double udt = dotv(Ud, T) / kC;
+    const double us2 = udt * udt;
+    alpha = 1.0 / std::sqrt(0.5 * (s + std::sqrt(s * s + 4.0 * (T2 + us2))));
+    T = smul(alpha, T);
+    s = 1.0 / (1.0 + dotv(T, T));
+    alpha = dotv(Ud, T);
+    rU = smul(s, add(add(Ud, smul(alpha, T)), crossv(Ud, T)));
+    const double mr = magv(rU) / kC;
+    p.U = sdiv(rU, std::sqrt(1.0 + mr * mr));
+}
+
+// HigueraCaryPusher::updateVelocity (SM/ParticlePusher/HigueraCary/HigueraCary.C:69-115)
+void push_hc(const Oracle& o, Parcel& p, double q, double mass, double trackTime) {
+    const V3 E = field_at(o, p);
+    const V3 B = v3(o.cfg.B[0], o.cfg.B[1], o.cfg.B[2]);
+    const double dt2 = 0.5 * trackTime;
+    const double mU = magv(p.U) / kC;
+    V3 rU = sdiv(p.U, std::sqrt(1.0 - mU * mU));
+    const double qdm = q * dt2 / mass;
+    const V3 rUsm = smul(qdm, E);
+    rU = add(rU, rUsm);
+    if (o.rotation) {
+        const double mr0 = magv(rU) / kC;
+        const double gfm2 = 1.0 + mr0 * mr0;
+        V3 t = smul(qdm, B);
+        const double beta2 = dotv(t, t);
+        const double gb = gfm2 - beta2;
+        const double tr = dotv(t, rU);
+        const double iG = 1.0 / std::sqrt(0.5 * (gb + std::sqrt(gb * gb + 4.0 * (beta2 + tr * tr))));
+        t = smul(iG, t);
+        const V3 Udash = add(rU, crossv(rU, t));
+        const double den = 1.0 + dotv(t, t);
+        rU = add(rU, crossv(Udash, sdiv(smul(2.0, t), den)));
+    }
+    rU = add(rU, rUsm);
+    const double mr = magv(rU) / kC;
+    p.U = sdiv(rU, std::sqrt(1.0 + mr * mr));
+}
+
+// ParticlePusher::updateVelocity dispatch (ParticlePusher.H:131-134)
+void push(const Oracle& o, Parcel& p, int species, double trackTime) {
+    const double q = o.cfg.species[species].charge, mass = o.cfg.species[species].mass;
+    switch (o.cfg.pusher) {
+        case PICGPU_PUSHER_BORIS: push_boris(o, p, q, mass, trackTime); break;
+        case PICGPU_PUSHER_BORIS_NR: push_boris_nr(o, p, q, mass, trackTime); break;
+        case PICGPU_PUSHER_VAY: push_vay(o, p, q, mass, trackTime); break;
+        case PICGPU_PUSHER_HIGUERA_CARY: push_hc(o, p, q, mass, trackTime); break;
+        default: break;  // "none" (NoPush)
+    }
+}
+
+// ------------------------------------------------------------ tracking ----
+struct TrackData {
+    bool keep = true;
+    bool requireResync = false;
+    long long tet_steps = 0, faces = 0, walls = 0;
+    bool capped = false;
+    bool superluminal = false;
+    double* qconv = nullptr;   // floating-patch charge accumulator of this thread
+};
+
+V3 position_of(const Oracle& o, const Parcel& p) {
+    double x[3];
+    pg::position(o.m, 12LL * p.cell + p.tet, &p.y[1], x);
+    return v3(x[0], x[1], x[2]);
+}
+
+// One tet step of barycentric tracking (the OpenFOAM-5+ algorithm: map the
+// displacement into barycentric space, take the first coordinate to reach
+// zero, clamp round-off, renormalise).  Returns the hit tet face (-1: the
+// displacement is used up) and the fraction lambda of the displacement moved.
+int tet_step(const Oracle& o, Parcel& p, const double* dx, double* lambda) {
+    const double* inv = &o.m.cls_tetinv[(size_t(o.m.cell_class[p.cell]) * 12 + p.tet) * 9];
+    double dy[4];
+    dy[1] = inv[0] * dx[0] + inv[1] * dx[1] + inv[2] * dx[2];
+    dy[2] = inv[3] * dx[0] + inv[4] * dx[1] + inv[5] * dx[2];
+    dy[3] = inv[6] * dx[0] + inv[7] * dx[1] + inv[8] * dx[2];
+    dy[0] = -(dy[1] + dy[2] + dy[3]);
+    const double S = std::fabs(dy[0]) + std::fabs(dy[1]) + std::fabs(dy[2]) + std::fabs(dy[3]);
+    const double thr = -1e-12 * S;
+    double lam = 1.0;
+    int hit = -1;
+    for (int i = 0; i < 4; ++i) {
+        if (dy[i] < thr) {
+            const double l = -p.y[i] / dy[i];
+            if (l < lam) { lam = l; hit = i; }
+        }
+    }
+    double y[4];
+    for (int i = 0; i < 4; ++i) y[i] = p.y[i] + lam * dy[i];
+    if (hit >= 0) y[hit] = 0.0;
+    for (int i = 0; i < 4; ++i) y[i] = std::fmax(y[i], 0.0);
+    const double r = 1.0 / (y[0] + y[1] + y[2] + y[3]);
+    for (int i = 0; i < 4; ++i) p.y[i] = y[i] * r;
+    *lambda = lam;
+    return hit;
+}
+
+// PICParcel::syncVelocityAtBoundary (PIC/parcels/Templates/PICParcel/PICParcel.C:220-227)
+void sync_velocity(const Oracle& o, Parcel& p, int species, double fraction) {
+    if (o.cfg.sync_velocity_at_boundary && o.cfg.species[species].charge != 0.0)
+        push(o, p, species, fraction * o.cfg.dt);
+}
+
+// PICParcel::hitPatch (PICParcel.C:153-184) with the patch models in scope:
+// NoInflow (SM/BoundaryModel/NoInflow/NoInflow.C:56-61) and FloatingPotential
+// (SM/BoundaryModel/FloatingPotential/FloatingPotential.C:119-127) delete the
+// parcel; a wall without a model reflects (SpecularReflection.C:53-67) and
+// asks for a velocity resync.
+void hit_patch(Oracle& o, Parcel& p, int species, int patch, double sf, TrackData& td) {
+    const picgpu_patch& P = o.m.patches[patch].p;
+    if (P.kind == PICGPU_PATCH_ABSORB) {
+        td.keep = false;
+        return;
+    }
+    if (P.kind == PICGPU_PATCH_FLOATING) {
+        td.keep = false;
+        td.qconv[patch] += o.cfg.species[species].weight * o.cfg.species[species].charge;
+        return;
+    }
+    const int f = p.tet / 2;
+    const double* n = &o.m.cls_fnormal[size_t(o.m.cell_class[p.cell]) * 18 + 3 * f];
+    if (P.kind == PICGPU_PATCH_WALL) {
+        sync_velocity(o, p, species, sf - 0.5);
+        td.walls++;
+        td.requireResync = true;
+    }
+    // specular reflection (also used for a stray hit of an empty patch)
+    const double Un = p.U.x * n[0] + p.U.y * n[1] + p.U.z * n[2];
+    if (Un > 0.0) {
+        const double t = 2.0 * Un;
+        p.U = v3(p.U.x - t * n[0], p.U.y - t * n[1], p.U.z - t * n[2]);
+    }
+}
+
+// trackToAndHitFace: tet steps inside the cell until the displacement is used
+// up or a cell face is reached; then cross into the neighbour (internal or
+// cyclic face) or interact with the patch.
+void track_to_and_hit_face(Oracle& o, Parcel& p, int species, const double* disp, double f,
+                           double& sf, TrackData& td, int& budget) {
+    const HexMesh& m = o.m;
+    double rem = 1.0;
+    for (;;) {
+        if (--budget < 0) { td.capped = true; sf = 1.0; return; }
+        double dx[3] = {rem * disp[0], rem * disp[1], rem * disp[2]};
+        double lam;
+        const int hit = tet_step(o, p, dx, &lam);
+        td.tet_steps++;
+        if (hit < 0) { sf = 1.0; return; }
+        sf += (f * rem) * lam;
+        if (hit > 0) {
+            const int nt = m.tt.inner_next[p.tet][hit];
+            double y[4];
+            for (int j = 0; j < 4; ++j) {
+                const int s = m.tt.inner_src[p.tet][hit][j];
+                y[j] = s < 0 ? 0.0 : p.y[s];
+            }
+            std::memcpy(p.y, y, sizeof y);
+            p.tet = nt;
+            rem = rem * (1.0 - lam);
+            continue;
+        }
+        // cell face
+        const int face = p.tet / 2;
+        const int nb = m.nbr[6 * size_t(p.cell) + face];
+        td.faces++;
+        if (nb >= 0) {
+            const int nt = m.tt.cross_next[p.tet];
+            double y[4];
+            y[0] = 0.0;
+            for (int j = 1; j < 4; ++j) y[j] = p.y[m.tt.cross_src[p.tet][j]];
+            std::memcpy(p.y, y, sizeof y);
+            p.tet = nt;
+            p.cell = nb;
+            return;
+        }
+        hit_patch(o, p, species, -nb - 1, sf, td);
+        return;
+    }
+}
+
+// PICParcel::move + moveForward (PICParcel.C:38-144)
+void move_parcel(Oracle& o, Parcel& p, int species, TrackData& td) {
+    const picgpu_species& sp = o.cfg.species[species];
+    if (!sp.solve_movement) return;
+    // the particle store holds three barycentric coordinates; the centre one
+    // is re-derived at the start of every step
+    p.y[0] = 1.0 - p.y[1] - p.y[2] - p.y[3];
+    if (sp.charge != 0.0) push(o, p, species, o.cfg.dt);
+    if (!(magv(p.U) < kC)) { td.keep = false; td.superluminal = true; return; }
+    const HexMesh& m = o.m;
+    double sf = 0.0;
+    int resync = 0;
+    int budget = o.cfg.track_max_steps > 0 ? o.cfg.track_max_steps : 4096;
+    const double dt = o.cfg.dt;
+    while (td.keep && sf < 1.0) {
+        // Utracking constrained to the solution directions and the deviation
+        // from the mesh centre in the empty ones (PICParcel.C:119-126)
+        double Ut[3] = {p.U.x, p.U.y, p.U.z};
+        double dev[3] = {0, 0, 0};
+        bool reduced = false;
+        for (int a = 0; a < 3; ++a) if (m.empty[a]) { Ut[a] = 0.0; reduced = true; }
+        if (reduced) {
+            const V3 x = position_of(o, p);
+            const double xa[3] = {x.x, x.y, x.z};
+            for (int a = 0; a < 3; ++a) if (m.empty[a]) dev[a] = xa[a] - m.mesh_centre[a];
+        }
+        const double f = 1.0 - sf;
+        const double fdt = f * dt;
+        const double disp[3] = {fdt * Ut[0] - dev[0], fdt * Ut[1] - dev[1], fdt * Ut[2] - dev[2]};
+        td.requireResync = false;
+        track_to_and_hit_face(o, p, species, disp, f, sf, td, budget);
+        if (td.capped) return;
+        if (td.requireResync && td.keep) {
+            resync++;
+            if (resync > 1) { td.requireResync = false; continue; }
+            sync_velocity(o, p, species, 0.5 - sf);
+            td.requireResync = false;
+        }
+    }
+}
+
+// ----------------------------------------------------- charge and fields --
+void reset_charge(Oracle& o) {
+    std::fill(o.ccData.begin(), o.ccData.end(), 0.0);
+    std::fill(o.vtxData.begin(), o.vtxData.end(), 0.0);
+    std::fill(o.ccFix.begin(), o.ccFix.end(), 0LL);
+    std::fill(o.vtxFix.begin(), o.vtxFix.end(), 0LL);
+}
+
+// ChargeDistribution::add: VolumeWeighting (VolumeWeighting.C:105-124),
+// CellAverage (CellAverage.C:53-60).
+void deposit(Oracle& o, const Parcel& p, int species) {
+    const double value = o.cfg.species[species].charge * o.cfg.species[species].weight;
+    if (value == 0.0) return;
+    const HexMesh& m = o.m;
+    const bool fixed = o.cfg.deposit_mode == PICGPU_DEPOSIT_FIXED_POINT;
+    if (o.cfg.charge_distribution == PICGPU_WEIGHTING_CELL_AVERAGE) {
+        if (fixed) o.ccFix[p.cell] += std::llrint(value * o.fixScale);
+        else o.ccData[p.cell] += value;
+        return;
+    }
+    const int* cp = &m.cell_pt[8 * size_t(p.cell)];
+    if (fixed) {
+        o.ccFix[p.cell] += std::llrint((p.y[0] * value) * o.fixScale);
+        for (int i = 0; i < 3; ++i)
+            o.vtxFix[cp[m.tt.tri[p.tet][i]]] += std::llrint((p.y[i + 1] * value) * o.fixScale);
+    } else {
+        o.ccData[p.cell] += p.y[0] * value;
+        for (int i = 0; i < 3; ++i) o.vtxData[cp[m.tt.tri[p.tet][i]]] += p.y[i + 1] * value;
+    }
+}
+
+// ChargeDistribution::update (VolumeWeighting.C:138-164, CellAverage.C:63-68)
+// and the spaceCharge addition (PICCloud.C:687-690).
+void update_charge(Oracle& o) {
+    const HexMesh& m = o.m;
+    const bool fixed = o.cfg.deposit_mode == PICGPU_DEPOSIT_FIXED_POINT;
+    for (int c = 0; c < m.n_cells; ++c) {
+        const double V = m.vol[c];
+        const double ccv = fixed ? double(o.ccFix[c]) / o.fixScale : o.ccData[c];
+        double r = 0.0;
+        if (o.cfg.charge_distribution == PICGPU_WEIGHTING_CELL_AVERAGE) {
+            r = ccv / V;
+        } else {
+            r = r + ccv / V;
+            for (int q = 0; q < 8; ++q) {
+                const int pt = m.cell_pt[8 * size_t(c) + q];
+                const double vv = fixed ? double(o.vtxFix[pt]) / o.fixScale : o.vtxData[pt];
+                r = r + (m.vw_weight[8 * size_t(c) + q] * vv) / V;
+            }
+        }
+        o.rho[c] = r + o.cfg.space_charge;
+    }
+}
+
+// FloatingPotential::preUpdate_Boundary (FloatingPotential.C:89-100)
+void floating_pre_update(Oracle& o) {
+    for (size_t pa = 0; pa < o.m.patches.size(); ++pa) {
+        if (o.m.patches[pa].p.kind != PICGPU_PATCH_FLOATING) continue;
+        o.sigma[pa] += o.Qconv[pa] / o.m.patches[pa].area;
+        o.gradBC[pa] = o.sigma[pa] / kEps0;
+        o.Qconv[pa] = 0.0;
+    }
+}
+
+// Right-hand side of -laplacian(phi) = rho/eps0 in integral form (the
+// fvm::laplacian(phiE) + rhoCharge/epsilon0 system of ElectroStaticSolver.C:61-64):
+// Dirichlet faces add a |S|/delta phi_b, circuitBoundary faces add |S| g
+// (circuitBoundaryFvPatchField.C:157-175).
+void assemble_rhs(const Oracle& o, const double* rho, std::vector<double>& b) {
+    const HexMesh& m = o.m;
+    b.resize(m.n_cells);
+    for (int c = 0; c < m.n_cells; ++c) {
+        double t = (rho[c] / kEps0) * m.vol[c];
+        for (int f = 0; f < 6; ++f) {
+            const int bf = m.cell_bface[6 * size_t(c) + f];
+            if (bf < 0) continue;
+            const pg::BFace& B = m.bfaces[bf];
+            const picgpu_patch& P = m.patches[B.patch].p;
+            if (P.kind == PICGPU_PATCH_FLOATING) {
+                t = t + B.area * o.gradBC[B.patch];
+            } else if (P.phi_bc == PICGPU_PHI_FIXED_VALUE) {
+                t = t + (B.area / B.delta) * P.phi;
+            }
+        }
+        b[c] = t;
+    }
+    if (!m.has_dirichlet) {
+        // singular (fully periodic / Neumann) system: project out the mean
+        const double mean = det_sum(m.n_cells, [&](long i) { return b[i]; }) / double(m.n_cells);
+        for (int c = 0; c < m.n_cells; ++c) b[c] = b[c] - mean;
+    }
+}
+
+void apply_M(const Oracle& o, const std::vector<double>& x, std::vector<double>& y) {
+    const HexMesh& m = o.m;
+    for (int c = 0; c < m.n_cells; ++c) {
+        double s = o.Mdiag[c] * x[c];
+        for (int f = 0; f < 6; ++f) {
+            const int nb = m.nbr[6 * size_t(c) + f];
+            if (nb >= 0) s = s + o.Moff[6 * size_t(c) + f] * x[nb];
+        }
+        y[c] = s;
+    }
+}
+
+// OpenFOAM-normalised residual: sum|b - Ax| / (sum(|Ax - A xRef| + |b - A xRef|) + 1e-20)
+// with xRef the mean of x.
+double of_residual(const Oracle& o, const std::vector<double>& b, const std::vector<double>& x) {
+    const HexMesh& m = o.m;
+    std::vector<double> Ax(m.n_cells);
+    apply_M(o, x, Ax);
+    double mean = 0;
+    for (int c = 0; c < m.n_cells; ++c) mean += x[c];
+    mean /= m.n_cells;
+    double num = 0, den = 0;
+    for (int c = 0; c < m.n_cells; ++c) {
+        double rowsum = o.Mdiag[c];
+        for (int f = 0; f < 6; ++f)
+            if (m.nbr[6 * size_t(c) + f] >= 0) rowsum += o.Moff[6 * size_t(c) + f];
+        const double Axr = rowsum * mean;
+        num += std::fabs(b[c] - Ax[c]);
+        den += std::fabs(Ax[c] - Axr) + std::fabs(b[c] - Axr);
+    }
+    return num / (den + 1e-20);
+}
+
+// PCG with the Jacobi preconditioner, reductions in the GPU's fixed order.
+int pcg_jacobi(Oracle& o, const std::vector<double>& b, std::vector<double>& x, double tol,
+               int maxit, double* res) {
+    const long n = o.m.n_cells;
+    std::vector<double> r(n), z(n), p(n), q(n);
+    apply_M(o, x, q);
+    for (long i = 0; i < n; ++i) r[i] = b[i] - q[i];
+    for (long i = 0; i < n; ++i) z[i] = o.dinv[i] * r[i];
+    double rz = det_sum(n, [&](long i) { return r[i] * z[i]; });
+    double rr = det_sum(n, [&](long i) { return r[i] * r[i]; });
+    const double bb = det_sum(n, [&](long i) { return b[i] * b[i]; });
+    const double lim = (tol * tol) * bb;
+    int it = 0;
+    if (!(rr <= lim)) {
+        p = z;
+        for (it = 1; it <= maxit; ++it) {
+            apply_M(o, p, q);
+            const double pq = det_sum(n, [&](long i) { return p[i] * q[i]; });
+            const double alpha = rz / pq;
+            for (long i = 0; i < n; ++i) {
+                x[i] = x[i] + alpha * p[i];
+                r[i] = r[i] - alpha * q[i];
+                z[i] = o.dinv[i] * r[i];
+            }
+            const double rzn = det_sum(n, [&](long i) { return r[i] * z[i]; });
+            rr = det_sum(n, [&](long i) { return r[i] * r[i]; });
+            if (rr <= lim) break;
+            const double beta = rzn / rz;
+            rz = rzn;
+            for (long i = 0; i < n; ++i) p[i] = z[i] + beta * p[i];
+        }
+        if (it > maxit) it = -maxit;
+    }
+    *res = bb > 0 ? std::sqrt(rr / bb) : 0.0;
+    return it;
+}
+
+// OpenFOAM PCG with the DIC preconditioner (tutorial system/fvSolution) on
+// the internal faces in upper-triangular order; coupled cyclic faces are
+// interfaces the preconditioner leaves out.
+int pcg_dic(Oracle& o, const std::vector<double>& b, std::vector<double>& x, double tol,
+            int maxit, double* res) {
+    const HexMesh& m = o.m;
+    const long n = m.n_cells;
+    struct F { int l, u; double a; };
+    std::vector<F> faces;
+    for (int c = 0; c < n; ++c)
+        for (int f = 1; f < 6; f += 2) {  // + faces: owner c, neighbour higher
+            const int nb = m.nbr[6 * size_t(c) + f];
+            if (nb > c && !(m.cell_ijk[3 * size_t(c) + f / 2] == m.n[f / 2] - 1))
+                faces.push_back({c, nb, o.Moff[6 * size_t(c) + f]});
+        }
+    std::sort(faces.begin(), faces.end(), [](const F& a, const F& b2) {
+        return a.l != b2.l ? a.l < b2.l : a.u < b2.u;
+    });
+    std::vector<double> rD(o.Mdiag);
+    for (const F& f : faces) rD[f.u] -= f.a * f.a / rD[f.l];
+    for (long i = 0; i < n; ++i) rD[i] = 1.0 / rD[i];
+    auto prec = [&](const std::vector<double>& r, std::vector<double>& w) {
+        for (long i = 0; i < n; ++i) w[i] = rD[i] * r[i];
+        for (const F& f : faces) w[f.u] -= rD[f.u] * f.a * w[f.l];
+        for (auto it = faces.rbegin(); it != faces.rend(); ++it) w[it->l] -= rD[it->l] * it->a * w[it->u];
+    };
+    std::vector<double> r(n), z(n), p(n), q(n);
+    apply_M(o, x, q);
+    double rr = 0, bb = 0;
+    for (long i = 0; i < n; ++i) { r[i] = b[i] - q[i]; rr += r[i] * r[i]; bb += b[i] * b[i]; }
+    const double lim = tol * tol * bb;
+    int it = 0;
+    if (!(rr <= lim)) {
+        prec(r, z);
+        double rz = 0;
+        for (long i = 0; i < n; ++i) rz += r[i] * z[i];
+        p = z;
+        for (it = 1; it <= maxit; ++it) {
+            apply_M(o, p, q);
+            double pq = 0;
+            for (long i = 0; i < n; ++i) pq += p[i] * q[i];
+            const double alpha = rz / pq;
+            rr = 0;
+            for (long i = 0; i < n; ++i) {
+                x[i] += alpha * p[i];
+                r[i] -= alpha * q[i];
+                rr += r[i] * r[i];
+            }
+            if (rr <= lim) break;
+            prec(r, z);
+            double rzn = 0;
+            for (long i = 0; i < n; ++i) rzn += r[i] * z[i];
+            const double beta = rzn / rz;
+            rz = rzn;
+            for (long i = 0; i < n; ++i) p[i] = z[i] + beta * p[i];
+        }
+        if (it > maxit) it = -maxit;
+    }
+    *res = bb > 0 ? std::sqrt(rr / bb) : 0.0;
+    return it;
+}
+
+// E = -fvc::grad(phi) (Gauss linear) with corrected boundary values, then the
+// point field (FieldWeigthing::update, VolumeWeightingFW.C:70-75).
+void compute_E(Oracle& o) {
+    const HexMesh& m = o.m;
+    for (int c = 0; c < m.n_cells; ++c) {
+        const int cl = m.cell_class[c];
+        double g[3] = {0, 0, 0};
+        for (int f = 0; f < 6; ++f) {
+            const int nb = m.nbr[6 * size_t(c) + f];
+            double pf;
+            if (nb >= 0) {
+                const double w = m.ip_weight[6 * size_t(c) + f];
+                pf = w * o.phi[c] + (1.0 - w) * o.phi[nb];
+            } else {
+                const int bf = m.cell_bface[6 * size_t(c) + f];
+                if (bf < 0) continue;  // empty
+                const pg::BFace& B = m.bfaces[bf];
+                const picgpu_patch& P = m.patches[B.patch].p;
+                if (P.kind == PICGPU_PATCH_FLOATING) pf = o.phi[c] + o.gradBC[B.patch] * B.delta;
+                else if (P.phi_bc == PICGPU_PHI_FIXED_VALUE) pf = P.phi;
+                else pf = o.phi[c];
+            }
+            const double area = m.cls_farea[size_t(cl) * 6 + f];
+            const double* n = &m.cls_fnormal[size_t(cl) * 18 + 3 * f];
+            for (int a = 0; a < 3; ++a) g[a] = g[a] + pf * (n[a] * area);
+        }
+        for (int a = 0; a < 3; ++a) o.E[3 * size_t(c) + a] = -(g[a] / m.vol[c]);
+    }
+    for (size_t b = 0; b < m.bfaces.size(); ++b) {
+        const pg::BFace& B = m.bfaces[b];
+        const picgpu_patch& P = m.patches[B.patch].p;
+        const double* Ec = &o.E[3 * size_t(B.cell)];
+        double sn = 0.0;
+        if (P.kind == PICGPU_PATCH_FLOATING) sn = o.gradBC[B.patch];
+        else if (P.phi_bc == PICGPU_PHI_FIXED_VALUE) sn = (P.phi - o.phi[B.cell]) / B.delta;
+        const double En = Ec[0] * B.normal[0] + Ec[1] * B.normal[1] + Ec[2] * B.normal[2];
+        for (int a = 0; a < 3; ++a)
+            o.Eb[3 * b + a] = (Ec[a] - En * B.normal[a]) - sn * B.normal[a];
+    }
+    for (int p = 0; p < m.n_points; ++p) {
+        double e[3] = {0, 0, 0};
+        for (int k = m.pi_start[p]; k < m.pi_start[p + 1]; ++k) {
+            const int s = m.pi_src[k];
+            const double* src = s >= 0 ? &o.E[3 * size_t(s)] : &o.Eb[3 * size_t(-s - 1)];
+            for (int a = 0; a < 3; ++a) e[a] = e[a] + m.pi_w[k] * src[a];
+        }
+        for (int a = 0; a < 3; ++a) o.Ept[3 * size_t(p) + a] = e[a];
+    }
+}
+
+void set_applied_field(Oracle& o) {
+    for (int c = 0; c < o.m.n_cells; ++c)
+        for (int a = 0; a < 3; ++a) o.E[3 * size_t(c) + a] = o.cfg.E_applied[a];
+    for (int p = 0; p < o.m.n_points; ++p)
+        for (int a = 0; a < 3; ++a) o.Ept[3 * size_t(p) + a] = o.cfg.E_applied[a];
+}
+
+int solve_fields(Oracle& o, picgpu_step_stats* st) {
+    if (o.cfg.maxwell_solver != PICGPU_MAXWELL_ELECTROSTATIC) { set_applied_field(o); return 0; }
+    std::vector<double> b;
+    assemble_rhs(o, o.rho.data(), b);
+    double res = 0;
+    const int maxit = o.cfg.pcg_max_iter > 0 ? o.cfg.pcg_max_iter : 10000;
+    const double tol = o.cfg.pcg_tol > 0 ? o.cfg.pcg_tol : 1e-10;
+    int it = o.precond == ORACLE_PRECOND_DIC ? pcg_dic(o, b, o.phi, tol, maxit, &res)
+                                              : pcg_jacobi(o, b, o.phi, tol, maxit, &res);
+    o.last_pcg_iter = it < 0 ? -it : it;
+    o.last_res_l2 = res;
+    o.last_res_of = of_residual(o, b, o.phi);
+    if (st) {
+        st->pcg_iterations = o.last_pcg_iter;
+        st->pcg_iterations_total += o.last_pcg_iter;
+        st->pcg_residual_l2 = res;
+        st->pcg_residual_of = o.last_res_of;
+    }
+    compute_E(o);
+    return it < 0 ? PICGPU_PCG_NOT_CONVERGED : 0;
+}
+
+void calculate_fields(Oracle& o) {
+    reset_charge(o);
+    for (size_t s = 0; s < o.cloud.size(); ++s)
+        for (const Parcel& p : o.cloud[s]) deposit(o, p, int(s));
+    update_charge(o);
+}
+
+// Cloud::move over all parcels; parcels are independent, so threads take
+// contiguous ranges (the oracle's host-thread decomposition mode).
+int move_all(Oracle& o, picgpu_step_stats* st) {
+    const auto t0 = std::chrono::steady_clock::now();
+    int status = 0;
+    for (size_t s = 0; s < o.cloud.size(); ++s) {
+        auto& cl = o.cloud[s];
+        const size_t n = cl.size();
+        const int nt = std::max(1, std::min<int>(o.nthreads, int(n / 1024) + 1));
+        std::vector<TrackData> tds(nt);
+        std::vector<std::vector<double>> qconv(nt, std::vector<double>(o.Qconv.size(), 0.0));
+        auto work = [&](int ti) {
+            const size_t lo = n * ti / nt, hi = n * (ti + 1) / nt;
+            for (size_t i = lo; i < hi; ++i) {
+                TrackData td;
+                td.qconv = qconv[ti].data();
+                move_parcel(o, cl[i], int(s), td);
+                cl[i].alive = td.keep && !td.capped && !td.superluminal;
+                tds[ti].tet_steps += td.tet_steps;
+                tds[ti].faces += td.faces;
+                tds[ti].walls += td.walls;
+                tds[ti].capped |= td.capped;
+                tds[ti].superluminal |= td.superluminal;
+            }
+        };
+        if (nt == 1) {
+            work(0);
+        } else {
+            std::vector<std::thread> th;
+            for (int ti = 0; ti < nt; ++ti) th.emplace_back(work, ti);
+            for (auto& t : th) t.join();
+        }
+        // floating-patch charge, summed in thread order
+        for (int ti = 0; ti < nt; ++ti)
+            for (size_t pa = 0; pa < o.Qconv.size(); ++pa) o.Qconv[pa] += qconv[ti][pa];
+        size_t w = 0;
+        long long absorbed = 0;
+        for (size_t i = 0; i < n; ++i) {
+            if (cl[i].alive) cl[w++] = cl[i];
+            else absorbed++;
+        }
+        cl.resize(w);
+        for (auto& td : tds) {
+            if (td.capped) status = PICGPU_TRACK_LOOP_CAP;
+            if (td.superluminal) status = PICGPU_SPEED_OF_LIGHT;
+            if (st) {
+                st->tet_steps += td.tet_steps;
+                st->face_crossings += td.faces;
+                st->wall_hits += td.walls;
+            }
+        }
+        if (st) st->n_absorbed[s] += absorbed;
+    }
+    o.move_seconds += std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
+    return status;
+}
+
+// ------------------------------------------------------------ collisions --
+constexpr double kBoltzmann = 1.380649e-23;
+
+V3 normal3(ocoll::Philox& r) {
+    const double a = r.normal(), b = r.normal(), c = r.normal();
+    return v3(a, b, c);
+}
+
+// Nanbu scattering against a partner of mass mN (NanbuElectronNeutralCollision.C:97-131):
+// cos(chi) = (eV + 2 - 2 (1 + eV)^R) / eV, azimuth 2 pi R.
+void nanbu_scatter(double eV, V3& Ue, V3& Un, double mE, double mN, ocoll::Philox& r) {
+    const double phi = 2.0 * kPi * r.uniform();
+    double cosChi;
+    if (eV < 1e-30) cosChi = 1.0;
+    else cosChi = 1.0 / eV * (eV + 2.0 - 2.0 * std::pow(1.0 + eV, r.uniform()));
+    double sinChi;
+    if (cosChi * cosChi > 1.0) { cosChi = 1.0; sinChi = 0.0; }
+    else sinChi = std::sqrt(1.0 - cosChi * cosChi);
+    const V3 g = sub(Ue, Un);
+    const double gm = magv(g);
+    const double gp = std::sqrt(g.y * g.y + g.z * g.z);
+    const double cp = std::cos(phi), sp = std::sin(phi);
+    const V3 h = v3(gp * cp, -1.0 * (g.y * g.x * cp + gm * g.z * sp) / gp,
+                    -1.0 * (g.z * g.x * cp - gm * g.y * sp) / gp);
+    const V3 d = add(smul(1.0 - cosChi, g), smul(sinChi, h));
+    Ue = sub(Ue, smul(mN / (mN + mE), d));
+    Un = add(Un, smul(mE / (mN + mE), d));
+}
+
+// ElectronNeutralCollisionModel::performBackgroundCollisions
+// (ElectronNeutralCollisionModel.C:703-829) with the event kinematics of
+// :532-544 (elastic), :567-585 (excitation), :645-700 (ionisation).
+void mcc_background(Oracle& o, std::vector<std::vector<int>>& occ, picgpu_step_stats* st) {
+    const picgpu_mcc& mc = o.cfg.mcc;
+    const int es = o.cfg.electron_species;
+    const double me = o.cfg.species[es].mass;
+    const double mg = mc.gas_mass;
+    const double dt = o.cfg.dt;
+    const double vth = std::sqrt(kBoltzmann * mc.gas_temperature / mg);
+    auto& el = o.cloud[es];
+    std::vector<Parcel> new_e, new_i;
+    long long cand = 0, nel = 0, nex = 0, niz = 0;
+    for (int c = 0; c < o.m.n_cells; ++c) {
+        const std::vector<int>& list = occ[c];
+        const long eC = long(list.size());
+        const double sv = o.svmax[c];
+        const double coll = o.remainder[c] + double(eC) * mc.gas_density * sv * dt;
+        const long nC = long(coll);
+        o.remainder[c] = coll - double(nC);
+        if (nC == 0 || eC == 0) continue;
+        ocoll::Philox r(o.cfg.seed, ocoll::kStreamMcc, uint32_t(c), uint32_t(o.step_index));
+        cand += nC;
+        for (long i = 0; i < nC; ++i) {
+            long j = long(r.uniform() * double(eC));
+            if (j >= eC) j = eC - 1;
+            Parcel& e = el[list[j]];
+            const V3 nrm = normal3(r);
+            V3 Un = v3(vth * nrm.x + mc.gas_velocity[0], vth * nrm.y + mc.gas_velocity[1],
+                       vth * nrm.z + mc.gas_velocity[2]);
+            const double cR = magv(sub(e.U, Un));
+            const double gamma = 1.0 / std::sqrt(1.0 - (cR * cR) / (kC * kC));
+            double eV = (gamma - 1.0) * me * kC * kC / ocoll::kEcharge;
+            const double sigmaT = sv / cR;
+            const double Qel = ocoll::interp_xs(eV, o.xs.e, o.xs.el);
+            const double Qex = ocoll::interp_xs(eV, o.xs.e, o.xs.ex);
+            const double Qiz = ocoll::interp_xs(eV, o.xs.e, o.xs.iz);
+            const double Qt = Qel + Qex + Qiz;
+            if (Qt * cR > o.svmax[c]) o.svmax[c] = Qt * cR;
+            const double R = r.uniform();
+            if (R <= Qel / sigmaT) {
+                nel++;
+                nanbu_scatter(eV, e.U, Un, me, mg, r);
+            } else if (eV >= mc.ex_threshold && R <= (Qel + Qex) / sigmaT) {
+                nex++;
+                e.U = smul(std::sqrt(1.0 - mc.ex_threshold / eV), e.U);
+                eV -= mc.ex_threshold;
+                nanbu_scatter(eV, e.U, Un, me, mg, r);
+            } else if (eV >= mc.iz_threshold && R <= Qt / sigmaT) {
+                const double th = mc.iz_threshold;
+                const double E0 = 2.0 - 100.0 / (eV + 10.0);
+                const double E1 = (eV - th) / 2.0 - E0;
+                const double alpha = 10.3;
+                const double Ep = E0 + alpha * std::tan(r.uniform() * (std::atan(E1 / alpha) + std::atan(E0 / alpha)) -
+                                                        std::atan(E0 / alpha));
+                const V3 preUe = e.U;
+                const V3 preUn = Un;
+                e.U = smul(std::sqrt(1.0 - (th + Ep) / eV), e.U);
+                eV -= (th + Ep);
+                const double wE = o.cfg.species[es].weight, wN = mc.gas_weight;
+                const double wEwN = wE / wN, wNwE = 1.0 / wEwN;
+                nanbu_scatter(eV, e.U, Un, me, mg, r);
+                const double rndU = r.uniform();
+                bool created = false;
+                if (rndU <= wEwN && mc.create_ion && mc.ion_species >= 0) {
+                    Parcel ion = e;
+                    ion.U = Un;
+                    new_i.push_back(ion);
+                    created = true;
+                }
+                if (rndU > wNwE) e.U = preUe;
+                if (rndU <= wEwN && mc.create_electron) {
+                    Parcel ne = e;
+                    const double sp = std::sqrt(2.0 * Ep * ocoll::kEcharge / me);
+                    ne.U = smul(sp, sdiv(preUe, magv(preUe)));
+                    V3 un2 = preUn;
+                    nanbu_scatter(Ep, ne.U, un2, me, mg, r);
+                    new_e.push_back(ne);
+                }
+                if (created) niz++;
+            }
+        }
+    }
+    for (auto& p : new_e) el.push_back(p);
+    if (mc.ion_species >= 0)
+        for (auto& p : new_i) o.cloud[mc.ion_species].push_back(p);
+    if (st) {
+        st->mcc_candidates += cand;
+        st->mcc_elastic += nel;
+        st->mcc_excitation += nex;
+        st->mcc_ionization += niz;
+    }
+}
+
+// NanbuCollision::calculate_cosChi (NanbuCollision.C:137-161)
+double nanbu_cos_chi(double s, ocoll::Philox& r) {
+    double U = r.uniform();
+    if (s < 0.1) {
+        if (U < 0.0001) U = 0.0001;
+        return 1.0 + s * std::log(U);
+    }
+    if (s < 3.0) {
+        const double invA = 0.00569578 + (0.95602 + (-0.508139 + (0.479139 + (-0.12789 + 0.0238957 * s) * s) * s) * s) * s;
+        const double A = 1.0 / invA;
+        return invA * std::log(std::exp(-A) + 2.0 * U * std::sinh(A));
+    }
+    if (s < 6.0) {
+        const double A = 3.0 * std::exp(-s);
+        return (1.0 / A) * std::log(std::exp(-A) + 2.0 * U * std::sinh(A));
+    }
+    return 2.0 * U - 1.0;
+}
+
+// NanbuCollision::collide (NanbuCollision.C:60-135), fixed coulombLog.
+void nanbu_collide(Oracle& o, Parcel& P, int sp, Parcel& Q, int sq, double nP, double nQ,
+                   double nPQ, ocoll::Philox& r) {
+    const double mP = o.cfg.species[sp].mass, qP = o.cfg.species[sp].charge;
+    const double mQ = o.cfg.species[sq].mass, qQ = o.cfg.species[sq].charge;
+    const double reMass = mP * mQ / (mP + mQ);
+    const V3 g = sub(P.U, Q.U);
+    const double gm = magv(g);
+    const double cl = o.cfg.coulomb.coulomb_log;
+    const double A = qP * qQ / (kEps0 * reMass);
+    const double s = cl / (4.0 * kPi) * (A * A) * (nQ * nP / nPQ) * (1.0 / (gm * gm * gm)) * o.cfg.dt;
+    const double cosChi = nanbu_cos_chi(s, r);
+    const double sinChi = std::sqrt(1.0 - cosChi * cosChi);
+    const double gp = std::sqrt(g.y * g.y + g.z * g.z);
+    const double eps = 2.0 * kPi * r.uniform();
+    const double ce = std::cos(eps), se = std::sin(eps);
+    const V3 h = v3(gp * ce, -1.0 * (g.y * g.x * ce + gm * g.z * se) / gp,
+                    -1.0 * (g.z * g.x * ce - gm * g.y * se) / gp);
+    const V3 d = add(smul(1.0 - cosChi, g), smul(sinChi, h));
+    P.U = sub(P.U, smul(mQ / (mP + mQ), d));
+    Q.U = add(Q.U, smul(mP / (mP + mQ), d));
+}
+
+void shuffle(std::vector<int>& a, ocoll::Philox& r) {
+    for (long k = long(a.size()) - 1; k > 0; --k) {
+        long j = long(r.uniform() * double(k + 1));
+        if (j > k) j = k;
+        std::swap(a[k], a[j]);
+    }
+}
+
+// NanbuYonemuraPairing::pairANDcollide (NanbuYonemuraPairing.C:56-325)
+void coulomb_ny(Oracle& o, std::vector<std::vector<std::vector<int>>>& occ, picgpu_step_stats* st) {
+    std::vector<int> charged;
+    for (int s = 0; s < o.cfg.n_species; ++s)
+        if (o.cfg.species[s].charge != 0.0 && o.cfg.species[s].solve_movement) charged.push_back(s);
+    long long pairs = 0;
+    for (int c = 0; c < o.m.n_cells; ++c) {
+        const double V = o.m.vol[c];
+        ocoll::Philox r(o.cfg.seed, ocoll::kStreamCoulomb, uint32_t(c), uint32_t(o.step_index));
+        for (size_t i = 0; i < charged.size(); ++i) {
+            for (size_t jj = charged.size(); jj-- > 0;) {
+                if (jj < i) break;
+                const int a = charged[i], b = charged[jj];
+                std::vector<int>& LA = occ[a][c];
+                std::vector<int>& LB = occ[b][c];
+                const long nA = long(LA.size()), nB = long(LB.size());
+                const double wA = o.cfg.species[a].weight, wB = o.cfg.species[b].weight;
+                const double sA = double(nA) * wA;
+                const double sB = a != b ? double(nB) * wB : 0.0;
+                if (a == b && nA > 1) {
+                    if (!o.cfg.coulomb.allow_intra) continue;
+                    std::vector<int> sel(nA);
+                    for (long k = 0; k < nA; ++k) sel[k] = int(k);
+                    shuffle(sel, r);
+                    const double n = sA / V;
+                    auto& cl = o.cloud[a];
+                    if (nA % 2 != 0) {
+                        double nAA = 2.0 * wA;  // the extra (last, first) pair
+                        for (long x = 0; x < nA - 2; x += 2) nAA += 2.0 * wA;
+                        const double n12 = nAA / V;
+                        for (long x = 0; x < nA - 2; x += 2)
+                            nanbu_collide(o, cl[LA[sel[x]]], a, cl[LA[sel[x + 1]]], a, n, n, n12, r);
+                        nanbu_collide(o, cl[LA[sel[nA - 1]]], a, cl[LA[sel[0]]], a, n, n, n12, r);
+                        pairs += 1 + nA / 2;
+                    } else {
+                        double nAA = 0.0;
+                        for (long x = 0; x < nA - 1; x += 2) nAA += 2.0 * wA;
+                        const double n12 = nAA / V;
+                        for (long x = 0; x < nA - 1; x += 2)
+                            nanbu_collide(o, cl[LA[sel[x]]], a, cl[LA[sel[x + 1]]], a, n, n, n12, r);
+                        pairs += nA / 2;
+                    }
+                } else if (a != b && std::min(nA, nB) != 0) {
+                    auto& ca = o.cloud[a];
+                    auto& cb = o.cloud[b];
+                    const double wmin = std::fmin(wA, wB);
+                    if (nA == nB) {
+                        const double nP = sA / V, nQ = sB / V;
+                        std::vector<int> sel(nA);
+                        for (long k = 0; k < nA; ++k) sel[k] = int(k);
+                        shuffle(sel, r);
+                        double nAB = 0.0;
+                        for (long k = 0; k < nA; ++k) nAB += wmin;
+                        const double nPQ = nAB / V;
+                        for (long k = 0; k < nA; ++k)
+                            nanbu_collide(o, ca[LA[sel[k]]], a, cb[LB[sel[nA - k - 1]]], b, nP, nQ, nPQ, r);
+                        pairs += nA;
+                    } else {
+                        const int minS = nA < nB ? a : b, maxS = nA > nB ? a : b;
+                        std::vector<int>& Lmin = nA < nB ? LA : LB;
+                        std::vector<int>& Lmax = nA < nB ? LB : LA;
+                        const long nMax = std::max(nA, nB), nMin = std::min(nA, nB);
+                        std::vector<int> smin(nMin), smax(nMax);
+                        for (long k = 0; k < nMax; ++k) { smax[k] = int(k); if (k < nMin) smin[k] = int(k); }
+                        shuffle(smin, r);
+                        shuffle(smax, r);
+                        const double nMaxS = (maxS == a ? sA : sB) / V;
+                        const double nMinS = (maxS == a ? sB : sA) / V;
+                        double nAB = 0.0;
+                        for (long l = 0; l < nMax; ++l) nAB += wmin;
+                        const double n12 = nAB / V;
+                        long k = 0;
+                        auto& cmin = o.cloud[minS];
+                        auto& cmax = o.cloud[maxS];
+                        for (long l = 0; l < nMax; ++l) {
+                            if (k >= nMin) k = 0;
+                            nanbu_collide(o, cmax[Lmax[smax[l]]], maxS, cmin[Lmin[smin[k]]], minS, nMaxS, nMinS, n12, r);
+                            ++k;
+                        }
+                        pairs += nMax;
+                    }
+                }
+            }
+        }
+    }
+    if (st) st->coulomb_pairs += pairs;
+}
+
+// PICCloud::buildCellOccupancy (PICCloud.C:327-354) + collisions() (PICCloud.C:526-539):
+// Coulomb first, then electron-neutral.
+void collisions(Oracle& o, picgpu_step_stats* st) {
+    if (!o.cfg.mcc.enabled && !o.cfg.coulomb.enabled) return;
+    std::vector<std::vector<std::vector<int>>> occ(o.cfg.n_species,
+                                                   std::vector<std::vector<int>>(o.m.n_cells));
+    for (int s = 0; s < o.cfg.n_species; ++s)
+        for (size_t i = 0; i < o.cloud[s].size(); ++i) occ[s][o.cloud[s][i].cell].push_back(int(i));
+    if (o.cfg.coulomb.enabled) coulomb_ny(o, occ, st);
+    if (o.cfg.mcc.enabled) mcc_background(o, occ[o.cfg.electron_species], st);
+}
+
+void fill_counts(const Oracle& o, picgpu_step_stats* st) {
+    if (!st) return;
+    for (size_t s = 0; s < o.cloud.size(); ++s) st->n_particles[s] = (long long)o.cloud[s].size();
+    for (size_t pa = 0; pa < o.m.patches.size() && pa < PICGPU_MAX_BOXES + 6; ++pa)
+        st->floating_charge[pa] = o.sigma[pa] * o.m.patches[pa].area;
+}
+
+}  // namespace
+
+struct oracle_ctx {
+    Oracle o;
+};
+
+extern "C" {
+
+int oracle_create(const picgpu_mesh_desc* mesh, const picgpu_config* cfg, int nthreads,
+                  oracle_ctx** out) {
+    if (!mesh || !cfg || !out) return PICGPU_INVALID_ARG;
+    *out = nullptr;
+    auto* c = new oracle_ctx();
+    Oracle& o = c->o;
+    try {
+        o.m = pg::build_hex_mesh(*mesh);
+    } catch (const std::exception& e) {
+        o.err = e.what();
+        *out = c;
+        return PICGPU_INVALID_ARG;
+    }
+    o.cfg = *cfg;
+    if (cfg->n_species < 1 || cfg->n_species > PICGPU_MAX_SPECIES || !(cfg->dt > 0)) {
+        o.err = "config: bad species count or dt";
+        *out = c;
+        return PICGPU_INVALID_ARG;
+    }
+    o.nthreads = nthreads > 0 ? nthreads : 1;
+    const HexMesh& m = o.m;
+    o.cloud.resize(cfg->n_species);
+    o.phi.assign(m.n_cells, 0.0);
+    o.rho.assign(m.n_cells, 0.0);
+    o.E.assign(3 * size_t(m.n_cells), 0.0);
+    o.Ept.assign(3 * size_t(m.n_points), 0.0);
+    o.Eb.assign(3 * m.bfaces.size(), 0.0);
+    o.ccData.assign(m.n_cells, 0.0);
+    o.vtxData.assign(m.n_points, 0.0);
+    o.ccFix.assign(m.n_cells, 0);
+    o.vtxFix.assign(m.n_points, 0);
+    o.sigma.assign(m.patches.size(), 0.0);
+    o.gradBC.assign(m.patches.size(), 0.0);
+    o.Qconv.assign(m.patches.size(), 0.0);
+    o.Mdiag.resize(m.n_cells);
+    o.dinv.resize(m.n_cells);
+    o.Moff.resize(6 * size_t(m.n_cells));
+    for (int i = 0; i < m.n_cells; ++i) {
+        o.Mdiag[i] = -m.lap_diag[i];
+        o.dinv[i] = 1.0 / o.Mdiag[i];
+    }
+    for (size_t i = 0; i < o.Moff.size(); ++i) o.Moff[i] = -m.lap_off[i];
+    double qmax = 0;
+    for (int s = 0; s < cfg->n_species; ++s)
+        qmax = std::fmax(qmax, std::fabs(cfg->species[s].charge * cfg->species[s].weight));
+    o.fixScale = qmax > 0 ? std::ldexp(1.0, 39 - std::ilogb(qmax)) : 1.0;
+    o.rotation = cfg->B[0] != 0.0 || cfg->B[1] != 0.0 || cfg->B[2] != 0.0;
+    if (cfg->maxwell_solver != PICGPU_MAXWELL_ELECTROSTATIC) set_applied_field(o);
+    o.svmax.assign(m.n_cells, 0.0);
+    o.remainder.assign(m.n_cells, 0.0);
+    if (cfg->mcc.enabled) {
+        std::string e = ocoll::init_mcc(o.cfg, o.xs, m.n_cells, o.svmax, o.remainder);
+        if (!e.empty()) { o.err = e; *out = c; return PICGPU_INVALID_ARG; }
+    }
+    *out = c;
+    return 0;
+}
+
+void oracle_destroy(oracle_ctx* ctx) { delete ctx; }
+
+const char* oracle_last_error(const oracle_ctx* ctx) { return ctx ? ctx->o.err.c_str() : "null"; }
+
+int oracle_set_precond(oracle_ctx* ctx, int precond) {
+    ctx->o.precond = precond;
+    return 0;
+}
+
+int oracle_mesh_query(const oracle_ctx* ctx, picgpu_mesh_info* info) {
+    info->n_cells = ctx->o.m.n_cells;
+    info->n_points = ctx->o.m.n_points;
+    info->n_tets = 12LL * ctx->o.m.n_cells;
+    info->n_patches = (long long)ctx->o.m.patches.size();
+    return 0;
+}
+
+int oracle_set_particles(oracle_ctx* ctx, int species, size_t n, const int32_t* tet,
+                         const double* bary, const double* U) {
+    Oracle& o = ctx->o;
+    if (species < 0 || species >= o.cfg.n_species) return PICGPU_INVALID_ARG;
+    auto& cl = o.cloud[species];
+    cl.assign(n, Parcel{});
+    const long long ntet = 12LL * o.m.n_cells;
+    for (size_t i = 0; i < n; ++i) {
+        if (tet[i] < 0 || tet[i] >= ntet) { o.err = "particles: tet index out of range"; cl.clear(); return PICGPU_INVALID_ARG; }
+        Parcel& p = cl[i];
+        p.cell = tet[i] / 12;
+        p.tet = tet[i] % 12;
+        p.y[1] = bary[3 * i];
+        p.y[2] = bary[3 * i + 1];
+        p.y[3] = bary[3 * i + 2];
+        p.y[0] = 1.0 - p.y[1] - p.y[2] - p.y[3];
+        p.U = v3(U[3 * i], U[3 * i + 1], U[3 * i + 2]);
+    }
+    return 0;
+}
+
+int oracle_count_particles(oracle_ctx* ctx, int species, size_t* n) {
+    if (species < 0 || species >= ctx->o.cfg.n_species) return PICGPU_INVALID_ARG;
+    *n = ctx->o.cloud[species].size();
+    return 0;
+}
+
+int oracle_get_particles(oracle_ctx* ctx, int species, size_t cap, int32_t* tet, double* bary,
+                         double* U, size_t* n) {
+    Oracle& o = ctx->o;
+    if (species < 0 || species >= o.cfg.n_species) return PICGPU_INVALID_ARG;
+    const auto& cl = o.cloud[species];
+    *n = cl.size();
+    if (cap < cl.size()) return PICGPU_INVALID_ARG;
+    for (size_t i = 0; i < cl.size(); ++i) {
+        tet[i] = cl[i].cell * 12 + cl[i].tet;
+        for (int a = 0; a < 3; ++a) bary[3 * i + a] = cl[i].y[a + 1];
+        U[3 * i] = cl[i].U.x;
+        U[3 * i + 1] = cl[i].U.y;
+        U[3 * i + 2] = cl[i].U.z;
+    }
+    return 0;
+}
+
+int oracle_initialise_fields(oracle_ctx* ctx) {
+    Oracle& o = ctx->o;
+    calculate_fields(o);
+    return solve_fields(o, nullptr);
+}
+
+int oracle_move(oracle_ctx* ctx, picgpu_step_stats* st) {
+    Oracle& o = ctx->o;
+    if (st) std::memset(st, 0, sizeof *st);
+    int s = move_all(o, st);
+    calculate_fields(o);
+    fill_counts(o, st);
+    return s;
+}
+
+// PICCloud::evolve (PICCloud.C:1426-1471)
+int oracle_step(oracle_ctx* ctx, int nsteps, picgpu_step_stats* st) {
+    Oracle& o = ctx->o;
+    if (st) std::memset(st, 0, sizeof *st);
+    int status = 0;
+    for (int k = 0; k < nsteps; ++k) {
+        int s = move_all(o, st);
+        if (s) return s;
+        collisions(o, st);
+        calculate_fields(o);
+        floating_pre_update(o);
+        s = solve_fields(o, st);
+        if (s) status = s;
+        o.step_index++;
+    }
+    fill_counts(o, st);
+    return status;
+}
+
+int oracle_solve_poisson(oracle_ctx* ctx, const double* rho, double* phi_inout,
+                         picgpu_step_stats* st) {
+    Oracle& o = ctx->o;
+    if (st) std::memset(st, 0, sizeof *st);
+    std::copy(rho, rho + o.m.n_cells, o.rho.begin());
+    std::copy(phi_inout, phi_inout + o.m.n_cells, o.phi.begin());
+    const int saved = o.cfg.maxwell_solver;
+    o.cfg.maxwell_solver = PICGPU_MAXWELL_ELECTROSTATIC;
+    int s = solve_fields(o, st);
+    o.cfg.maxwell_solver = saved;
+    std::copy(o.phi.begin(), o.phi.end(), phi_inout);
+    return s;
+}
+
+int oracle_get_field(oracle_ctx* ctx, int which, double* out, size_t n) {
+    Oracle& o = ctx->o;
+    const std::vector<double>* v = nullptr;
+    switch (which) {
+        case PICGPU_FIELD_PHI: v = &o.phi; break;
+        case PICGPU_FIELD_E_CELL: v = &o.E; break;
+        case PICGPU_FIELD_RHO: v = &o.rho; break;
+        case PICGPU_FIELD_E_POINT: v = &o.Ept; break;
+        case PICGPU_FIELD_SIGMA_V_MAX: v = &o.svmax; break;
+        default: return PICGPU_INVALID_ARG;
+    }
+    if (n < v->size()) return PICGPU_INVALID_ARG;
+    std::copy(v->begin(), v->end(), out);
+    return 0;
+}
+
+int oracle_set_field(oracle_ctx* ctx, int which, const double* in, size_t n) {
+    Oracle& o = ctx->o;
+    std::vector<double>* v = nullptr;
+    switch (which) {
+        case PICGPU_FIELD_PHI: v = &o.phi; break;
+        case PICGPU_FIELD_E_CELL: v = &o.E; break;
+        case PICGPU_FIELD_RHO: v = &o.rho; break;
+        case PICGPU_FIELD_E_POINT: v = &o.Ept; break;
+        default: return PICGPU_INVALID_ARG;
+    }
+    if (n < v->size()) return PICGPU_INVALID_ARG;
+    std::copy(in, in + v->size(), v->begin());
+    return 0;
+}
+
+// KineticEnergyInfo.C:72-81, TemperatureInfo.C:71-76, FieldEnergyInfo.C:107-115
+int oracle_diagnostics(oracle_ctx* ctx, picgpu_diagnostics* out) {
+    Oracle& o = ctx->o;
+    std::memset(out, 0, sizeof *out);
+    for (size_t s = 0; s < o.cloud.size(); ++s) {
+        const double m = o.cfg.species[s].mass, w = o.cfg.species[s].weight;
+        for (const Parcel& p : o.cloud[s]) {
+            const double u2 = dotv(p.U, p.U);
+            out->kinetic_energy[s] += 0.5 * m * u2 * w;
+            const double b = magv(p.U) / kC;
+            out->kinetic_energy_rel[s] += (1.0 / std::sqrt(1.0 - b * b) - 1.0) * m * kC * kC;
+            out->momentum[s][0] += w * m * p.U.x;
+            out->momentum[s][1] += w * m * p.U.y;
+            out->momentum[s][2] += w * m * p.U.z;
+            out->velocity_sq[s][0] += w * p.U.x * p.U.x;
+            out->velocity_sq[s][1] += w * p.U.y * p.U.y;
+            out->velocity_sq[s][2] += w * p.U.z * p.U.z;
+            out->weight_sum[s] += w;
+        }
+    }
+    double fe = 0;
+    for (int c = 0; c < o.m.n_cells; ++c) {
+        const double* e = &o.E[3 * size_t(c)];
+        fe += (e[0] * e[0] + e[1] * e[1] + e[2] * e[2]) * o.m.vol[c];
+    }
+    out->field_energy = 0.5 * kEps0 * fe;
+    return 0;
+}
+
+double oracle_move_seconds(const oracle_ctx* ctx) { return ctx->o.move_seconds; }
+
+}  // extern "C"

@@ -1,0 +1,59 @@
+/*
+ * oracle.h -- CPU oracle of the picFoam particle hot path.
+ *
+ * TEST INFRASTRUCTURE ONLY.  This library is a plain C++ restatement of the
+ * picFoam algorithms (push, barycentric tracking with patch interaction,
+ * charge and field weighting, the electrostatic Poisson solve, null-collision
+ * MCC, binary Coulomb collisions) used as the checker for the CUDA library
+ * and as the timed CPU baseline.  Nothing in the product links or loads it.
+ *
+ * The API mirrors include/picgpu.h so one test can drive both sides with the
+ * same inputs.  Parity status: the picFoam source cannot be built here (it
+ * needs OpenFOAM-9, wmake and MPI) and ships no test vectors, so the oracle
+ * is pinned by analytic known-answer tests (gyration radius, E x B drift,
+ * plasma frequency, manufactured Poisson solutions, collision rates) rather
+ * than by reference outputs: "parity unpinned" against picFoam binaries.
+ */
+#ifndef PICGPU_ORACLE_H
+#define PICGPU_ORACLE_H
+
+#include "picgpu.h"
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef struct oracle_ctx oracle_ctx;
+
+/* Preconditioner of the oracle's PCG. */
+enum {
+    ORACLE_PRECOND_JACOBI = 0,  /* same arithmetic and reduction order as the GPU */
+    ORACLE_PRECOND_DIC = 1      /* OpenFOAM PCG/DIC (tutorial fvSolution), sequential sums */
+};
+
+int  oracle_create(const picgpu_mesh_desc* mesh, const picgpu_config* cfg, int nthreads,
+                   oracle_ctx** out);
+void oracle_destroy(oracle_ctx* ctx);
+const char* oracle_last_error(const oracle_ctx* ctx);
+int  oracle_set_precond(oracle_ctx* ctx, int precond);
+int  oracle_mesh_query(const oracle_ctx* ctx, picgpu_mesh_info* info);
+int  oracle_set_particles(oracle_ctx* ctx, int species, size_t n, const int32_t* tet,
+                          const double* bary, const double* U);
+int  oracle_count_particles(oracle_ctx* ctx, int species, size_t* n);
+int  oracle_get_particles(oracle_ctx* ctx, int species, size_t cap, int32_t* tet,
+                          double* bary, double* U, size_t* n);
+int  oracle_initialise_fields(oracle_ctx* ctx);
+int  oracle_step(oracle_ctx* ctx, int nsteps, picgpu_step_stats* stats);
+int  oracle_move(oracle_ctx* ctx, picgpu_step_stats* stats);
+int  oracle_solve_poisson(oracle_ctx* ctx, const double* rho, double* phi_inout,
+                          picgpu_step_stats* stats);
+int  oracle_get_field(oracle_ctx* ctx, int which, double* out, size_t n);
+int  oracle_set_field(oracle_ctx* ctx, int which, const double* in, size_t n);
+int  oracle_diagnostics(oracle_ctx* ctx, picgpu_diagnostics* out);
+/* Wall-clock seconds spent in push + track + deposit since creation. */
+double oracle_move_seconds(const oracle_ctx* ctx);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

@@ -1,0 +1,141 @@
+"""ctypes mirror of include/picgpu.h (the C ABI of the particle hot path).
+
+Every structure here has the exact field order and types of its C
+counterpart; the library and the CPU oracle share the same structures.
+"""
+import ctypes as C
+
+# status codes
+OK = 0
+INVALID_ARG = 1
+OOM = 2
+TRACK_LOOP_CAP = 3
+PCG_NOT_CONVERGED = 4
+NAN_DETECTED = 5
+CUDA_ERROR = 6
+SPEED_OF_LIGHT = 7
+CAPACITY = 8
+NOT_SUPPORTED = 9
+
+STATUS_NAMES = {
+    OK: "OK", INVALID_ARG: "INVALID_ARG", OOM: "OOM", TRACK_LOOP_CAP: "TRACK_LOOP_CAP",
+    PCG_NOT_CONVERGED: "PCG_NOT_CONVERGED", NAN_DETECTED: "NAN_DETECTED",
+    CUDA_ERROR: "CUDA_ERROR", SPEED_OF_LIGHT: "SPEED_OF_LIGHT", CAPACITY: "CAPACITY",
+    NOT_SUPPORTED: "NOT_SUPPORTED",
+}
+
+PUSHER_NONE, PUSHER_BORIS, PUSHER_BORIS_NR, PUSHER_VAY, PUSHER_HIGUERA_CARY = range(5)
+WEIGHTING_CELL_AVERAGE, WEIGHTING_VOLUME = range(2)
+MAXWELL_NONE, MAXWELL_ELECTROSTATIC = range(2)
+PREC_FP64, PREC_MIXED = range(2)
+DEPOSIT_ATOMIC_FP64, DEPOSIT_FIXED_POINT = range(2)
+PATCH_CYCLIC, PATCH_EMPTY, PATCH_ABSORB, PATCH_WALL, PATCH_FLOATING = range(5)
+PHI_FIXED_VALUE, PHI_ZERO_GRADIENT = range(2)
+FIELD_PHI, FIELD_E_CELL, FIELD_RHO, FIELD_E_POINT, FIELD_SIGMA_V_MAX = range(5)
+(PHASE_MOVE, PHASE_CHARGE, PHASE_POISSON, PHASE_EFIELD, PHASE_SORT, PHASE_MCC,
+ PHASE_COULOMB, PHASE_COUNT) = range(8)
+PHASE_NAMES = ["move", "charge", "poisson", "efield", "sort", "mcc", "coulomb"]
+
+MAX_BOXES = 8
+MAX_SPECIES = 4
+
+
+class Patch(C.Structure):
+    _fields_ = [("kind", C.c_int32), ("phi_bc", C.c_int32), ("phi", C.c_double)]
+
+
+class Box(C.Structure):
+    _fields_ = [("lo", C.c_int32 * 3), ("hi", C.c_int32 * 3), ("patch", Patch)]
+
+
+class MeshDesc(C.Structure):
+    _fields_ = [
+        ("n", C.c_int32 * 3),
+        ("origin", C.c_double * 3),
+        ("length", C.c_double * 3),
+        ("side", Patch * 6),
+        ("n_boxes", C.c_int32),
+        ("box", Box * MAX_BOXES),
+    ]
+
+
+class Species(C.Structure):
+    _fields_ = [
+        ("mass", C.c_double), ("charge", C.c_double), ("weight", C.c_double),
+        ("solve_movement", C.c_int32), ("capacity_hint", C.c_int32),
+    ]
+
+
+class Mcc(C.Structure):
+    _fields_ = [
+        ("enabled", C.c_int32), ("scatter", C.c_int32), ("create_electron", C.c_int32),
+        ("create_ion", C.c_int32), ("ion_species", C.c_int32), ("n_xs", C.c_int32),
+        ("gas_density", C.c_double), ("gas_temperature", C.c_double), ("gas_mass", C.c_double),
+        ("gas_velocity", C.c_double * 3), ("gas_weight", C.c_double),
+        ("ex_threshold", C.c_double), ("iz_threshold", C.c_double),
+        ("sigma_v_max_init", C.c_double), ("find_max_energy", C.c_double),
+        ("find_energy_step", C.c_double),
+        ("xs_energy", C.POINTER(C.c_double)), ("xs_elastic", C.POINTER(C.c_double)),
+        ("xs_excitation", C.POINTER(C.c_double)), ("xs_ionization", C.POINTER(C.c_double)),
+    ]
+
+
+class Coulomb(C.Structure):
+    _fields_ = [
+        ("enabled", C.c_int32), ("pairing", C.c_int32), ("collide", C.c_int32),
+        ("allow_intra", C.c_int32), ("coulomb_log", C.c_double),
+    ]
+
+
+class Config(C.Structure):
+    _fields_ = [
+        ("pusher", C.c_int32), ("field_weighting", C.c_int32),
+        ("charge_distribution", C.c_int32), ("maxwell_solver", C.c_int32),
+        ("precision", C.c_int32), ("deposit_mode", C.c_int32),
+        ("n_species", C.c_int32), ("electron_species", C.c_int32),
+        ("species", Species * MAX_SPECIES),
+        ("dt", C.c_double), ("B", C.c_double * 3), ("E_applied", C.c_double * 3),
+        ("space_charge", C.c_double),
+        ("sync_velocity_at_boundary", C.c_int32), ("track_max_steps", C.c_int32),
+        ("pcg_tol", C.c_double), ("pcg_max_iter", C.c_int32), ("pcg_norm", C.c_int32),
+        ("sort_interval", C.c_int32), ("pad0", C.c_int32),
+        ("seed", C.c_uint64),
+        ("mcc", Mcc), ("coulomb", Coulomb),
+    ]
+
+
+class StepStats(C.Structure):
+    _fields_ = [
+        ("n_particles", C.c_int64 * MAX_SPECIES),
+        ("n_absorbed", C.c_int64 * MAX_SPECIES),
+        ("tet_steps", C.c_int64), ("face_crossings", C.c_int64), ("wall_hits", C.c_int64),
+        ("pcg_iterations", C.c_int32), ("pcg_iterations_total", C.c_int32),
+        ("pcg_residual_l2", C.c_double), ("pcg_residual_of", C.c_double),
+        ("mcc_candidates", C.c_int64), ("mcc_elastic", C.c_int64),
+        ("mcc_excitation", C.c_int64), ("mcc_ionization", C.c_int64),
+        ("coulomb_pairs", C.c_int64),
+        ("floating_charge", C.c_double * (MAX_BOXES + 6)),
+    ]
+
+    def as_dict(self):
+        d = {}
+        for name, _ in self._fields_:
+            v = getattr(self, name)
+            d[name] = list(v) if hasattr(v, "__len__") else v
+        return d
+
+
+class MeshInfo(C.Structure):
+    _fields_ = [("n_cells", C.c_int64), ("n_points", C.c_int64), ("n_tets", C.c_int64),
+                ("n_patches", C.c_int64)]
+
+
+class Diagnostics(C.Structure):
+    _fields_ = [
+        ("kinetic_energy", C.c_double * MAX_SPECIES),
+        ("kinetic_energy_rel", C.c_double * MAX_SPECIES),
+        ("momentum", (C.c_double * 3) * MAX_SPECIES),
+        ("velocity_sq", (C.c_double * 3) * MAX_SPECIES),
+        ("weight_sum", C.c_double * MAX_SPECIES),
+        ("field_energy", C.c_double),
+    ]

@@ -1,0 +1,328 @@
+"""Case builders: mesh, sub-model selection and initial particles.
+
+Each builder stands in for a picFoam case directory (blockMeshDict,
+constant/picProperties, system/picInitialiseDict) and the picInitialise
+run that fills it: particles are placed uniformly in tets
+(UniformInitialization.C:51-127, MaxwellianInitialization.C) with Maxwellian
+velocities drawn from numpy's Philox generator.  The workloads are the
+benchmark configurations of the particle hot path (seeded synthetic inputs):
+
+  plasma_oscillation_1d   periodic 0.1 m box, 128 cells, 200 e-/cell
+  two_species_3d          0.05 m cube, 64^3 cells, e- and Ar+ at 50/cell, B = 0.01 T
+  electron_swarm          32x32x256 cells, 10M e-, E = 1e4 V/m, argon-like gas
+  coulomb_thermalisation  16^3 cells, 400 e-/cell, T_x = 2 eV, T_yz = 1 eV
+  electrode_box           128^3 cells, two floating boxes, one 100 V box
+"""
+import dataclasses
+import math
+
+import numpy as np
+
+from . import abi
+
+C_LIGHT = 299792458.0
+MU0 = 4.0 * math.pi * 1e-7
+EPS0 = 1.0 / (MU0 * C_LIGHT * C_LIGHT)
+E_CHARGE = 1.602176634e-19
+K_B = 1.380649e-23
+M_E = 9.1093837015e-31
+M_AR = 6.6335209e-26
+
+
+@dataclasses.dataclass
+class Case:
+    name: str
+    mesh: abi.MeshDesc
+    cfg: abi.Config
+    particles: dict
+    keepalive: list
+    meta: dict
+
+
+def patch(kind, phi=0.0, phi_bc=abi.PHI_FIXED_VALUE):
+    p = abi.Patch()
+    p.kind = kind
+    p.phi_bc = phi_bc
+    p.phi = phi
+    return p
+
+
+def block_mesh(n, length, sides, origin=(0.0, 0.0, 0.0), boxes=()):
+    m = abi.MeshDesc()
+    for a in range(3):
+        m.n[a] = n[a]
+        m.length[a] = length[a]
+        m.origin[a] = origin[a]
+    for s in range(6):
+        m.side[s] = sides[s]
+    m.n_boxes = len(boxes)
+    for i, (lo, hi, p) in enumerate(boxes):
+        for a in range(3):
+            m.box[i].lo[a] = lo[a]
+            m.box[i].hi[a] = hi[a]
+        m.box[i].patch = p
+    return m
+
+
+def base_config(dt, species, pusher=abi.PUSHER_BORIS, precision=abi.PREC_FP64,
+                deposit=abi.DEPOSIT_ATOMIC_FP64, maxwell=abi.MAXWELL_ELECTROSTATIC,
+                weighting=abi.WEIGHTING_VOLUME, B=(0.0, 0.0, 0.0), E_applied=(0.0, 0.0, 0.0),
+                pcg_tol=1e-10, seed=1234, electron_species=0):
+    c = abi.Config()
+    c.pusher = pusher
+    c.field_weighting = weighting
+    c.charge_distribution = weighting
+    c.maxwell_solver = maxwell
+    c.precision = precision
+    c.deposit_mode = deposit
+    c.n_species = len(species)
+    c.electron_species = electron_species
+    for i, (mass, charge, weight, move) in enumerate(species):
+        c.species[i].mass = mass
+        c.species[i].charge = charge
+        c.species[i].weight = weight
+        c.species[i].solve_movement = 1 if move else 0
+    c.dt = dt
+    for a in range(3):
+        c.B[a] = B[a]
+        c.E_applied[a] = E_applied[a]
+    c.sync_velocity_at_boundary = 1
+    c.track_max_steps = 4096
+    c.pcg_tol = pcg_tol
+    c.pcg_max_iter = 20000
+    c.seed = seed
+    return c
+
+
+def plasma_frequency(n, mass=M_E, charge=E_CHARGE):
+    return math.sqrt(n * charge * charge / (EPS0 * mass))
+
+
+def thermal_speed(T_eV, mass):
+    return math.sqrt(T_eV * E_CHARGE / mass)
+
+
+def uniform_in_cells(rng, cells, per_cell):
+    """per_cell particles in each listed cell: random tet, uniform barycentric."""
+    cells = np.repeat(np.asarray(cells, dtype=np.int64), per_cell)
+    n = cells.size
+    tet = (cells * 12 + rng.integers(0, 12, n)).astype(np.int32)
+    u = np.sort(rng.random((n, 3)), axis=1)
+    bary = np.stack([u[:, 0], u[:, 1] - u[:, 0], u[:, 2] - u[:, 1]], axis=1)
+    return tet, bary
+
+
+def maxwellian(rng, n, T_eV, mass):
+    return rng.standard_normal((n, 3)) * thermal_speed(T_eV, mass)
+
+
+def plasma_oscillation_1d(mesh_api, n_cells=128, per_cell=200, seed=1234, dt_factor=0.05,
+                          perturbation=0.01, precision=abi.PREC_FP64,
+                          deposit=abi.DEPOSIT_ATOMIC_FP64, pusher=abi.PUSHER_BORIS, pcg_tol=1e-10,
+                          T_eV=1.0, n_e=1e14):
+    """Periodic 0.1 m box, n_cells x 1 x 1 hexes (thickness = dx, empty y/z),
+    electrons over an immobile neutralising background (spaceCharge)."""
+    L = 0.1
+    dx = L / n_cells
+    sides = [patch(abi.PATCH_CYCLIC), patch(abi.PATCH_CYCLIC),
+             patch(abi.PATCH_EMPTY), patch(abi.PATCH_EMPTY),
+             patch(abi.PATCH_EMPTY), patch(abi.PATCH_EMPTY)]
+    mesh = block_mesh((n_cells, 1, 1), (L, dx, dx), sides)
+    N = n_cells * per_cell
+    w = n_e * L * dx * dx / N
+    wpe = plasma_frequency(n_e)
+    dt = dt_factor / wpe
+    cfg = base_config(dt, [(M_E, -E_CHARGE, w, True)], pusher=pusher, precision=precision,
+                      deposit=deposit, pcg_tol=pcg_tol, seed=seed)
+    cfg.space_charge = E_CHARGE * n_e
+    rng = np.random.Generator(np.random.Philox(seed))
+    x = rng.random(N) * L
+    xyz = np.stack([x, np.full(N, 0.5 * dx), np.full(N, 0.5 * dx)], axis=1)
+    m = mesh_api(mesh)
+    tet, bary = m.locate(xyz)
+    vth = thermal_speed(T_eV, M_E)
+    U = rng.standard_normal((N, 3)) * vth
+    U[:, 0] += perturbation * vth * np.sin(2 * math.pi * x / L)
+    return Case("plasma_oscillation_1d", mesh, cfg, {0: (tet, bary, U)}, [],
+                dict(wpe=wpe, dt=dt, n_e=n_e, L=L, vth=vth, N=N, weight=w))
+
+
+def two_species_3d(n_cells=64, per_cell=50, seed=1234, precision=abi.PREC_MIXED,
+                   pusher=abi.PUSHER_BORIS, deposit=abi.DEPOSIT_ATOMIC_FP64, Bz=0.01, n=1e15,
+                   T_e=2.0, T_i=0.03, dt_factor=0.1, pcg_tol=1e-10, L=0.05):
+    """Cube with grounded absorbing walls, electrons + Ar+, uniform B_z."""
+    sides = [patch(abi.PATCH_ABSORB, 0.0) for _ in range(6)]
+    mesh = block_mesh((n_cells,) * 3, (L,) * 3, sides)
+    n_c = n_cells ** 3
+    N = n_c * per_cell
+    w = n * L ** 3 / N
+    wpe = plasma_frequency(n)
+    dt = dt_factor / wpe
+    cfg = base_config(dt, [(M_E, -E_CHARGE, w, True), (M_AR, E_CHARGE, w, True)], pusher=pusher,
+                      precision=precision, deposit=deposit, B=(0.0, 0.0, Bz), pcg_tol=pcg_tol,
+                      seed=seed)
+    cfg.sort_interval = 0
+    rng = np.random.Generator(np.random.Philox(seed))
+    parts = {}
+    for s, (T, mass) in enumerate([(T_e, M_E), (T_i, M_AR)]):
+        tet, bary = uniform_in_cells(rng, np.arange(n_c), per_cell)
+        U = maxwellian(rng, N, T, mass)
+        parts[s] = (tet, bary, U)
+    return Case("two_species_3d", mesh, cfg, parts, [],
+                dict(wpe=wpe, dt=dt, n=n, N=2 * N, weight=w, n_cells=n_c))
+
+
+def magnetic_rotation(pusher=abi.PUSHER_HIGUERA_CARY, precision=abi.PREC_FP64, beta=0.1, B=1.0,
+                      steps_per_orbit=200, n_cells=40):
+    """Single electron gyrating in B_z (tutorial magneticRotation): 40x1x40
+    cells, empty y, MaxwellSolver none.  Returns the case and the expected
+    gyration radius gamma m v / (e B)."""
+    L = 2e-3
+    sides = [patch(abi.PATCH_ABSORB), patch(abi.PATCH_ABSORB), patch(abi.PATCH_EMPTY),
+             patch(abi.PATCH_EMPTY), patch(abi.PATCH_ABSORB), patch(abi.PATCH_ABSORB)]
+    mesh = block_mesh((n_cells, 1, n_cells), (L, L / n_cells, L), sides)
+    v = beta * C_LIGHT
+    gamma = 1.0 / math.sqrt(1.0 - beta * beta)
+    r = gamma * M_E * v / (E_CHARGE * B)
+    wc = E_CHARGE * B / (gamma * M_E)
+    dt = 2 * math.pi / wc / steps_per_orbit
+    cfg = base_config(dt, [(M_E, -E_CHARGE, 1.0, True)], pusher=pusher, precision=precision,
+                      maxwell=abi.MAXWELL_NONE, B=(0.0, 0.0, B))
+    return Case("magnetic_rotation", mesh, cfg, {}, [],
+                dict(radius=r, v=v, gamma=gamma, wc=wc, dt=dt, L=L))
+
+
+def xs_tables(n=256, emin=0.01, emax=1000.0, el0=1e-19, ex_th=11.5, ex0=5e-21, iz_th=15.8, iz0=3e-20):
+    """Argon-like cross sections tabulated at n log-spaced energies."""
+    e = np.logspace(math.log10(emin), math.log10(emax), n)
+    el = el0 * (1.0 + e / 10.0) ** -0.5
+    ex = np.where(e > ex_th, ex0 * np.log(np.maximum(e / ex_th, 1.0)) / (e / ex_th), 0.0)
+    iz = np.where(e > iz_th, iz0 * np.log(np.maximum(e / iz_th, 1.0)) / (e / iz_th), 0.0)
+    return e, el, ex, iz
+
+
+def electron_swarm(nx=32, ny=32, nz=256, N=10_000_000, Ez=1e4, gas_density=1e21, T_gas=300.0,
+                   T_e=1.0, seed=1234, precision=abi.PREC_MIXED, dt=None, ion_species=True,
+                   size=(0.02, 0.02, 0.16), weight=1.0):
+    """Electron swarm in an argon-like background gas, fixed E along z,
+    absorbing walls, null-collision MCC with ionisation."""
+    sides = [patch(abi.PATCH_ABSORB) for _ in range(6)]
+    mesh = block_mesh((nx, ny, nz), size, sides)
+    e, el, ex, iz = xs_tables()
+    if dt is None:
+        # max(nu) dt <= 0.1 at the table maximum of sigma v; v dt <= 0.5 dx
+        sv = np.max(np.sqrt(2 * E_CHARGE * e / M_E) * (el + ex + iz))
+        dt = min(0.1 / (gas_density * sv), 0.5 * (size[0] / nx) / math.sqrt(2 * E_CHARGE * 200.0 / M_E))
+    species = [(M_E, -E_CHARGE, weight, True)]
+    if ion_species:
+        species.append((M_AR, E_CHARGE, weight, True))
+    cfg = base_config(dt, species, precision=precision, maxwell=abi.MAXWELL_NONE,
+                      E_applied=(0.0, 0.0, Ez), seed=seed)
+    arrs = [np.ascontiguousarray(a, dtype=np.float64) for a in (e, el, ex, iz)]
+    import ctypes as C
+    mc = cfg.mcc
+    mc.enabled = 1
+    mc.scatter = 0
+    mc.create_electron = 1
+    mc.create_ion = 1 if ion_species else 0
+    mc.ion_species = 1 if ion_species else -1
+    mc.n_xs = len(e)
+    mc.gas_density = gas_density
+    mc.gas_temperature = T_gas
+    mc.gas_mass = M_AR
+    mc.gas_weight = weight
+    mc.ex_threshold = 11.5
+    mc.iz_threshold = 15.8
+    mc.find_max_energy = 1000.0
+    mc.find_energy_step = 0.01
+    mc.xs_energy = arrs[0].ctypes.data_as(C.POINTER(C.c_double))
+    mc.xs_elastic = arrs[1].ctypes.data_as(C.POINTER(C.c_double))
+    mc.xs_excitation = arrs[2].ctypes.data_as(C.POINTER(C.c_double))
+    mc.xs_ionization = arrs[3].ctypes.data_as(C.POINTER(C.c_double))
+    rng = np.random.Generator(np.random.Philox(seed))
+    n_c = nx * ny * nz
+    cells = rng.integers(0, n_c, N)
+    tet = (cells * 12 + rng.integers(0, 12, N)).astype(np.int32)
+    u = np.sort(rng.random((N, 3)), axis=1)
+    bary = np.stack([u[:, 0], u[:, 1] - u[:, 0], u[:, 2] - u[:, 1]], axis=1)
+    U = maxwellian(rng, N, T_e, M_E)
+    parts = {0: (tet, bary, U)}
+    if ion_species:
+        parts[1] = (np.zeros(0, np.int32), np.zeros((0, 3)), np.zeros((0, 3)))
+    return Case("electron_swarm", mesh, cfg, parts, arrs,
+                dict(dt=dt, E_over_N_Td=Ez / gas_density * 1e21, N=N))
+
+
+def coulomb_thermalisation(n_cells=16, per_cell=400, n=1e18, T=4.0 / 3.0, ratio=0.5, seed=1234,
+                           coulomb_log=15.0, precision=abi.PREC_FP64, dt_factor=None, L=None):
+    """Electrons with T_x = 2 eV, T_y = T_z = 1 eV (Isotropization initial
+    condition), periodic box, no field solve, Nanbu/NanbuYonemura Coulomb."""
+    if L is None:
+        L = 1e-4
+    sides = [patch(abi.PATCH_CYCLIC) for _ in range(6)]
+    mesh = block_mesh((n_cells,) * 3, (L,) * 3, sides)
+    n_c = n_cells ** 3
+    N = n_c * per_cell
+    w = n * L ** 3 / N
+    # T_para = T * 3 / (1 + 2 ratio), T_perp = ratio * T_para
+    T_x = 3.0 * T / (1.0 + 2.0 * ratio)
+    T_yz = ratio * T_x
+    ve = thermal_speed(T_x, M_E)
+    nu = n * E_CHARGE ** 4 * coulomb_log / (4 * math.pi * EPS0 ** 2 * M_E ** 2 * ve ** 3)
+    dt = (dt_factor if dt_factor else 0.02) / nu
+    cfg = base_config(dt, [(M_E, -E_CHARGE, w, True)], maxwell=abi.MAXWELL_NONE, precision=precision,
+                      seed=seed)
+    cfg.coulomb.enabled = 1
+    cfg.coulomb.pairing = 0
+    cfg.coulomb.collide = 0
+    cfg.coulomb.allow_intra = 1
+    cfg.coulomb.coulomb_log = coulomb_log
+    rng = np.random.Generator(np.random.Philox(seed))
+    tet, bary = uniform_in_cells(rng, np.arange(n_c), per_cell)
+    U = rng.standard_normal((N, 3))
+    U[:, 0] *= thermal_speed(T_x, M_E)
+    U[:, 1:] *= thermal_speed(T_yz, M_E)
+    return Case("coulomb_thermalisation", mesh, cfg, {0: (tet, bary, U)}, [],
+                dict(dt=dt, T_x=T_x, T_yz=T_yz, nu=nu, N=N))
+
+
+def electrode_box(n_cells=128, per_cell=30, n=1e15, T_e=2.0, T_i=0.03, seed=1234,
+                  precision=abi.PREC_MIXED, dt_factor=0.1, pcg_tol=1e-8, L=0.1):
+    """Cube with grounded absorbing walls, two floating 8^3-cell box
+    electrodes and one 100 V box electrode."""
+    sides = [patch(abi.PATCH_ABSORB, 0.0) for _ in range(6)]
+    k = n_cells // 4
+    e = max(n_cells // 16, 1)
+    boxes = [((k, k, k), (k + e, k + e, k + e), patch(abi.PATCH_FLOATING)),
+             ((3 * k - e, k, k), (3 * k, k + e, k + e), patch(abi.PATCH_FLOATING)),
+             ((2 * k - e // 2, 3 * k - e, 2 * k - e // 2), (2 * k + e - e // 2, 3 * k, 2 * k + e - e // 2),
+              patch(abi.PATCH_ABSORB, 100.0))]
+    mesh = block_mesh((n_cells,) * 3, (L,) * 3, sides, boxes=boxes)
+    removed = set()
+    for lo, hi, _ in boxes:
+        for kk in range(lo[2], hi[2]):
+            for j in range(lo[1], hi[1]):
+                for i in range(lo[0], hi[0]):
+                    removed.add(i + n_cells * (j + n_cells * kk))
+    n_c = n_cells ** 3 - len(removed)
+    N = n_c * per_cell
+    w = n * (L ** 3) / (n_cells ** 3 * per_cell)
+    wpe = plasma_frequency(n)
+    dt = dt_factor / wpe
+    cfg = base_config(dt, [(M_E, -E_CHARGE, w, True), (M_AR, E_CHARGE, w, True)], precision=precision,
+                      pcg_tol=pcg_tol, seed=seed)
+    rng = np.random.Generator(np.random.Philox(seed))
+    parts = {}
+    for s, (T, mass) in enumerate([(T_e, M_E), (T_i, M_AR)]):
+        tet, bary = uniform_in_cells(rng, np.arange(n_c), per_cell)
+        parts[s] = (tet, bary, maxwellian(rng, N, T, mass))
+    return Case("electrode_box", mesh, cfg, parts, [], dict(dt=dt, N=2 * N, n_cells=n_c))
+
+
+def build(case, backend=None):
+    """Create a Simulation for the case and upload its particles."""
+    from .simulation import Simulation
+    sim = Simulation(case.mesh, case.cfg, backend=backend, keepalive=case.keepalive)
+    for s, (tet, bary, U) in case.particles.items():
+        sim.set_particles(s, tet, bary, U)
+    return sim

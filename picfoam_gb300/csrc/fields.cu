@@ -1,0 +1,525 @@
+// fields.cu -- charge density, electrostatic Poisson PCG and the E field.
+//
+// Built with --fmad=false: each kernel evaluates in the order of the CPU
+// oracle, and every reduction runs in one fixed tree order (256 threads, 8
+// strided items per thread, warp xor-tree, 8-warp tree; the last block of a
+// launch combines the block partials in the same order), so the FP64 Poisson
+// solve is bit-reproducible and matches the oracle bit for bit.
+//
+//   charge_update   ChargeDistribution::update (VolumeWeighting.C:138-164,
+//                   CellAverage.C:63-68) + spaceCharge (PICCloud.C:687-690)
+//   rhs + pcg_*     solve(fvm::laplacian(phiE) + rhoCharge/epsilon0)
+//                   (ElectroStaticSolver.C:61-64), PCG with a Jacobi
+//                   preconditioner on the SPD operator -laplacian
+//   grad_E          E = -fvc::grad(phiE), Gauss linear (ElectroStaticSolver.C:68)
+//   boundary_E      corrected boundary values of E
+//   point_E         cell -> point interpolation (VolumeWeightingFW.C:70-75)
+#include "fields.h"
+
+#include <algorithm>
+
+namespace pgd {
+
+__constant__ PatchConst c_patchF;
+
+constexpr double kMu0 = 4.0 * kPi * 1e-7;
+__device__ __forceinline__ double eps0() { return 1.0 / (kMu0 * kC * kC); }
+
+// ------------------------------------------------------- reductions ------
+// Sum over the block in the fixed tree order; the result is valid in every
+// lane of warp 0.
+__device__ __forceinline__ double block_tree(double v, double* ws) {
+#pragma unroll
+    for (int off = 16; off >= 1; off >>= 1) v = v + __shfl_xor_sync(0xffffffffu, v, off);
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    if (lane == 0) ws[warp] = v;
+    __syncthreads();
+    double r = 0.0;
+    if (warp == 0) {
+        r = lane < 8 ? ws[lane] : 0.0;
+#pragma unroll
+        for (int off = 4; off >= 1; off >>= 1) r = r + __shfl_xor_sync(0xffffffffu, r, off);
+    }
+    __syncthreads();
+    return r;
+}
+
+// Last-block finalisation: returns true in the block that arrives last; the
+// block partials are then visible to it.
+__device__ __forceinline__ bool arrive_last(unsigned int* ticket) {
+    __shared__ bool last;
+    __threadfence();
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        const unsigned int t = atomicAdd(ticket, 1u);
+        last = (t == gridDim.x - 1);
+        if (last) *ticket = 0u;
+    }
+    __syncthreads();
+    return last;
+}
+
+__device__ __forceinline__ double final_sum(const double* part, int nb, double* ws) {
+    double s = 0.0;
+    for (int i = threadIdx.x; i < nb; i += 256) s = s + __ldcg(part + i);
+    return block_tree(s, ws);
+}
+
+// ------------------------------------------------------------ charge -----
+__global__ void charge_update_kernel(DMesh m, int volume_weighting, int fixed, double fix_scale,
+                                     const double* __restrict__ ccd, const double* __restrict__ vtxd,
+                                     const long long* __restrict__ ccf,
+                                     const long long* __restrict__ vtxf, double space_charge,
+                                     double* __restrict__ rho) {
+    const int c = blockIdx.x * blockDim.x + threadIdx.x;
+    if (c >= m.n_cells) return;
+    const double V = m.vol[c];
+    const double ccv = fixed ? double(ccf[c]) / fix_scale : ccd[c];
+    double r = 0.0;
+    if (!volume_weighting) {
+        r = ccv / V;
+    } else {
+        r = r + ccv / V;
+        for (int q = 0; q < 8; ++q) {
+            const int pt = m.cell_pt[8 * size_t(c) + q];
+            const double vv = fixed ? double(vtxf[pt]) / fix_scale : vtxd[pt];
+            r = r + (m.vw_weight[8 * size_t(c) + q] * vv) / V;
+        }
+    }
+    rho[c] = r + space_charge;
+}
+
+// FloatingPotential::preUpdate_Boundary (FloatingPotential.C:89-100)
+__global__ void floating_update_kernel(double* qconv, double* sigma, double* grad_bc) {
+    const int p = threadIdx.x;
+    if (p >= c_patchF.n || c_patchF.kind[p] != PICGPU_PATCH_FLOATING) return;
+    sigma[p] += qconv[p] / c_patchF.area[p];
+    grad_bc[p] = sigma[p] / eps0();
+    qconv[p] = 0.0;
+}
+
+// ----------------------------------------------------------- Poisson -----
+__global__ void rhs_kernel(DMesh m, const double* __restrict__ rho, const double* __restrict__ grad_bc,
+                           double* __restrict__ b) {
+    const int c = blockIdx.x * blockDim.x + threadIdx.x;
+    if (c >= m.n_cells) return;
+    double t = (rho[c] / eps0()) * m.vol[c];
+    for (int f = 0; f < 6; ++f) {
+        const int bf = m.cell_bface[6 * size_t(c) + f];
+        if (bf < 0) continue;
+        const int pa = m.bf_patch[bf];
+        if (c_patchF.kind[pa] == PICGPU_PATCH_FLOATING) t = t + m.bf_area[bf] * grad_bc[pa];
+        else if (c_patchF.phi_bc[pa] == PICGPU_PHI_FIXED_VALUE)
+            t = t + (m.bf_area[bf] / m.bf_delta[bf]) * c_patchF.phi[pa];
+    }
+    b[c] = t;
+}
+
+__global__ void __launch_bounds__(256) sum_kernel(const double* __restrict__ v, int n,
+                                                  double* part, PcgState* st) {
+    __shared__ double ws[8];
+    double s = 0.0;
+    const long base = long(blockIdx.x) * 2048 + threadIdx.x;
+#pragma unroll
+    for (int j = 0; j < 8; ++j) {
+        const long i = base + j * 256;
+        if (i < n) s = s + v[i];
+    }
+    const double bs = block_tree(s, ws);
+    if (threadIdx.x == 0) part[blockIdx.x] = bs;
+    if (arrive_last(&st->ticket)) {
+        const double tot = final_sum(part, gridDim.x, ws);
+        if (threadIdx.x == 0) st->mean = tot / double(n);
+    }
+}
+
+__global__ void sub_mean_kernel(double* b, int n, const PcgState* st) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) b[i] = b[i] - st->mean;
+}
+
+__device__ __forceinline__ double apply_M(const DMesh& m, const double* x, int c) {
+    double s = m.Mdiag[c] * x[c];
+#pragma unroll
+    for (int f = 0; f < 6; ++f) {
+        const int nb = m.nbr[6 * size_t(c) + f];
+        if (nb >= 0) s = s + m.Moff[6 * size_t(c) + f] * x[nb];
+    }
+    return s;
+}
+
+__global__ void __launch_bounds__(256) pcg_init_kernel(DMesh m, const double* __restrict__ b,
+                                                       const double* __restrict__ x,
+                                                       double* __restrict__ r, double* __restrict__ z,
+                                                       double* part, PcgState* st, double tol) {
+    __shared__ double ws[8];
+    const int n = m.n_cells;
+    const int nb = gridDim.x;
+    double srz = 0.0, srr = 0.0, sbb = 0.0;
+    const long base = long(blockIdx.x) * 2048 + threadIdx.x;
+#pragma unroll
+    for (int j = 0; j < 8; ++j) {
+        const long i = base + j * 256;
+        if (i < n) {
+            const double mx = apply_M(m, x, int(i));
+            const double ri = b[i] - mx;
+            const double zi = m.dinv[i] * ri;
+            r[i] = ri;
+            z[i] = zi;
+            srz = srz + ri * zi;
+            srr = srr + ri * ri;
+            sbb = sbb + b[i] * b[i];
+        }
+    }
+    const double b0 = block_tree(srz, ws);
+    const double b1 = block_tree(srr, ws);
+    const double b2 = block_tree(sbb, ws);
+    if (threadIdx.x == 0) {
+        part[blockIdx.x] = b0;
+        part[nb + blockIdx.x] = b1;
+        part[2 * nb + blockIdx.x] = b2;
+    }
+    if (arrive_last(&st->ticket)) {
+        const double rz = final_sum(part, nb, ws);
+        const double rr = final_sum(part + nb, nb, ws);
+        const double bb = final_sum(part + 2 * nb, nb, ws);
+        if (threadIdx.x == 0) {
+            st->rz = rz;
+            st->rr = rr;
+            st->bb = bb;
+            st->lim = (tol * tol) * bb;
+            st->iters = 0;
+            st->done = rr <= st->lim ? 1 : 0;
+            st->converged = st->done;
+        }
+    }
+}
+
+// q = M p_new with p_new = z + beta p_old (p_new = z on the first iteration),
+// partial sums of p_new . q.
+__global__ void __launch_bounds__(256) pcg_spmv_kernel(DMesh m, const double* __restrict__ z,
+                                                       const double* __restrict__ p_old,
+                                                       double* __restrict__ p_new,
+                                                       double* __restrict__ q, double* part,
+                                                       PcgState* st, int first) {
+    if (st->done) return;
+    __shared__ double ws[8];
+    const int n = m.n_cells;
+    const double beta = st->beta;
+    double acc = 0.0;
+    const long base = long(blockIdx.x) * 2048 + threadIdx.x;
+#pragma unroll 1
+    for (int j = 0; j < 8; ++j) {
+        const long i = base + j * 256;
+        if (i < n) {
+            const double pi = first ? z[i] : z[i] + beta * p_old[i];
+            double s = m.Mdiag[i] * pi;
+#pragma unroll
+            for (int f = 0; f < 6; ++f) {
+                const int nb = m.nbr[6 * size_t(i) + f];
+                if (nb >= 0) {
+                    const double pn = first ? z[nb] : z[nb] + beta * p_old[nb];
+                    s = s + m.Moff[6 * size_t(i) + f] * pn;
+                }
+            }
+            p_new[i] = pi;
+            q[i] = s;
+            acc = acc + pi * s;
+        }
+    }
+    const double bs = block_tree(acc, ws);
+    if (threadIdx.x == 0) part[blockIdx.x] = bs;
+    if (arrive_last(&st->ticket)) {
+        const double pq = final_sum(part, gridDim.x, ws);
+        if (threadIdx.x == 0) st->pq = pq;
+    }
+}
+
+__global__ void __launch_bounds__(256) pcg_update_kernel(DMesh m, double* __restrict__ x,
+                                                         double* __restrict__ r, double* __restrict__ z,
+                                                         const double* __restrict__ p,
+                                                         const double* __restrict__ q, double* part,
+                                                         PcgState* st, int k, int maxit) {
+    if (st->done) return;
+    __shared__ double ws[8];
+    const int n = m.n_cells;
+    const int nb = gridDim.x;
+    const double alpha = st->rz / st->pq;
+    double srz = 0.0, srr = 0.0;
+    const long base = long(blockIdx.x) * 2048 + threadIdx.x;
+#pragma unroll
+    for (int j = 0; j < 8; ++j) {
+        const long i = base + j * 256;
+        if (i < n) {
+            x[i] = x[i] + alpha * p[i];
+            const double ri = r[i] - alpha * q[i];
+            const double zi = m.dinv[i] * ri;
+            r[i] = ri;
+            z[i] = zi;
+            srz = srz + ri * zi;
+            srr = srr + ri * ri;
+        }
+    }
+    const double b0 = block_tree(srz, ws);
+    const double b1 = block_tree(srr, ws);
+    if (threadIdx.x == 0) {
+        part[blockIdx.x] = b0;
+        part[nb + blockIdx.x] = b1;
+    }
+    if (arrive_last(&st->ticket)) {
+        const double rzn = final_sum(part, nb, ws);
+        const double rr = final_sum(part + nb, nb, ws);
+        if (threadIdx.x == 0) {
+            st->rr = rr;
+            if (rr <= st->lim) {
+                st->done = 1;
+                st->converged = 1;
+                st->iters = k;
+            } else if (k >= maxit) {
+                st->done = 1;
+                st->converged = 0;
+                st->iters = k;
+            } else {
+                st->beta = rzn / st->rz;
+                st->rz = rzn;
+                st->iters = k;
+            }
+        }
+    }
+}
+
+// OpenFOAM-normalised residual terms (reported, not used for convergence).
+__global__ void __launch_bounds__(256) of_residual_kernel(DMesh m, const double* __restrict__ b,
+                                                          const double* __restrict__ x, double* part,
+                                                          PcgState* st) {
+    __shared__ double ws[8];
+    const double mean = st->mean;
+    const int n = m.n_cells;
+    const int nb = gridDim.x;
+    double sn = 0.0, sd = 0.0;
+    const long base = long(blockIdx.x) * 2048 + threadIdx.x;
+    for (int j = 0; j < 8; ++j) {
+        const long i = base + j * 256;
+        if (i < n) {
+            const double ax = apply_M(m, x, int(i));
+            double rowsum = m.Mdiag[i];
+            for (int f = 0; f < 6; ++f)
+                if (m.nbr[6 * size_t(i) + f] >= 0) rowsum += m.Moff[6 * size_t(i) + f];
+            const double axr = rowsum * mean;
+            sn += fabs(b[i] - ax);
+            sd += fabs(ax - axr) + fabs(b[i] - axr);
+        }
+    }
+    const double b0 = block_tree(sn, ws);
+    const double b1 = block_tree(sd, ws);
+    if (threadIdx.x == 0) {
+        part[blockIdx.x] = b0;
+        part[nb + blockIdx.x] = b1;
+    }
+    if (arrive_last(&st->ticket)) {
+        const double num = final_sum(part, nb, ws);
+        const double den = final_sum(part + nb, nb, ws);
+        if (threadIdx.x == 0) st->of_residual = num / (den + 1e-20);
+    }
+}
+
+// ------------------------------------------------------------ E field ----
+__global__ void grad_E_kernel(DMesh m, const double* __restrict__ phi,
+                              const double* __restrict__ grad_bc, double* __restrict__ E) {
+    const int c = blockIdx.x * blockDim.x + threadIdx.x;
+    if (c >= m.n_cells) return;
+    const int cl = m.cell_class[c];
+    double g0 = 0.0, g1 = 0.0, g2 = 0.0;
+    for (int f = 0; f < 6; ++f) {
+        const int nb = m.nbr[6 * size_t(c) + f];
+        double pf;
+        if (nb >= 0) {
+            const double w = m.ip_weight[6 * size_t(c) + f];
+            pf = w * phi[c] + (1.0 - w) * phi[nb];
+        } else {
+            const int bf = m.cell_bface[6 * size_t(c) + f];
+            if (bf < 0) continue;
+            const int pa = m.bf_patch[bf];
+            if (c_patchF.kind[pa] == PICGPU_PATCH_FLOATING) pf = phi[c] + grad_bc[pa] * m.bf_delta[bf];
+            else if (c_patchF.phi_bc[pa] == PICGPU_PHI_FIXED_VALUE) pf = c_patchF.phi[pa];
+            else pf = phi[c];
+        }
+        const double area = m.farea[size_t(cl) * 6 + f];
+        const double* n = m.fnormal + size_t(cl) * 18 + 3 * f;
+        g0 = g0 + pf * (n[0] * area);
+        g1 = g1 + pf * (n[1] * area);
+        g2 = g2 + pf * (n[2] * area);
+    }
+    const double V = m.vol[c];
+    E[3 * size_t(c)] = -(g0 / V);
+    E[3 * size_t(c) + 1] = -(g1 / V);
+    E[3 * size_t(c) + 2] = -(g2 / V);
+}
+
+__global__ void boundary_E_kernel(DMesh m, const double* __restrict__ phi,
+                                  const double* __restrict__ grad_bc, const double* __restrict__ E,
+                                  double* __restrict__ Eb) {
+    const int b = blockIdx.x * blockDim.x + threadIdx.x;
+    if (b >= m.n_bfaces) return;
+    const int c = m.bf_cell[b];
+    const int pa = m.bf_patch[b];
+    const double* Ec = E + 3 * size_t(c);
+    const double* n = m.bf_normal + 3 * size_t(b);
+    double sn = 0.0;
+    if (c_patchF.kind[pa] == PICGPU_PATCH_FLOATING) sn = grad_bc[pa];
+    else if (c_patchF.phi_bc[pa] == PICGPU_PHI_FIXED_VALUE) sn = (c_patchF.phi[pa] - phi[c]) / m.bf_delta[b];
+    const double En = Ec[0] * n[0] + Ec[1] * n[1] + Ec[2] * n[2];
+    for (int a = 0; a < 3; ++a) Eb[3 * size_t(b) + a] = (Ec[a] - En * n[a]) - sn * n[a];
+}
+
+__global__ void point_E_kernel(DMesh m, const double* __restrict__ E, const double* __restrict__ Eb,
+                               double* __restrict__ Ept, float* __restrict__ Ept32) {
+    const int p = blockIdx.x * blockDim.x + threadIdx.x;
+    if (p >= m.n_points) return;
+    double e0 = 0.0, e1 = 0.0, e2 = 0.0;
+    for (int k = m.pi_start[p]; k < m.pi_start[p + 1]; ++k) {
+        const int s = m.pi_src[k];
+        const double* src = s >= 0 ? E + 3 * size_t(s) : Eb + 3 * size_t(-s - 1);
+        const double w = m.pi_w[k];
+        e0 = e0 + w * src[0];
+        e1 = e1 + w * src[1];
+        e2 = e2 + w * src[2];
+    }
+    Ept[3 * size_t(p)] = e0;
+    Ept[3 * size_t(p) + 1] = e1;
+    Ept[3 * size_t(p) + 2] = e2;
+    Ept32[3 * size_t(p)] = float(e0);
+    Ept32[3 * size_t(p) + 1] = float(e1);
+    Ept32[3 * size_t(p) + 2] = float(e2);
+}
+
+__global__ void to_float_kernel(const double* __restrict__ a, float* __restrict__ b, long n) {
+    const long i = long(blockIdx.x) * blockDim.x + threadIdx.x;
+    if (i < n) b[i] = float(a[i]);
+}
+
+__global__ void fill_kernel(double* a, long n, double v) {
+    const long i = long(blockIdx.x) * blockDim.x + threadIdx.x;
+    if (i < n) a[i] = v;
+}
+
+// ------------------------------------------------------- diagnostics -----
+__global__ void diagnostics_kernel(const int32_t* __restrict__ tet, const double* __restrict__ u0,
+                                   const double* __restrict__ u1, const double* __restrict__ u2,
+                                   const float* __restrict__ f0, const float* __restrict__ f1,
+                                   const float* __restrict__ f2, int n, double mass, double weight,
+                                   double* out /* 10 */) {
+    double ke = 0, ker = 0, mx = 0, my = 0, mz = 0, vx = 0, vy = 0, vz = 0, w = 0;
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        if (tet[i] < 0) continue;
+        const double a = u0 ? u0[i] : double(f0[i]);
+        const double b = u0 ? u1[i] : double(f1[i]);
+        const double c = u0 ? u2[i] : double(f2[i]);
+        const double uu = a * a + b * b + c * c;
+        ke += 0.5 * mass * uu * weight;
+        const double be = sqrt(uu) / kC;
+        ker += (1.0 / sqrt(1.0 - be * be) - 1.0) * mass * kC * kC;
+        mx += weight * mass * a;
+        my += weight * mass * b;
+        mz += weight * mass * c;
+        vx += weight * a * a;
+        vy += weight * b * b;
+        vz += weight * c * c;
+        w += weight;
+    }
+    double vals[9] = {ke, ker, mx, my, mz, vx, vy, vz, w};
+    for (int k = 0; k < 9; ++k) {
+        double v = vals[k];
+        for (int off = 16; off >= 1; off >>= 1) v += __shfl_xor_sync(0xffffffffu, v, off);
+        if ((threadIdx.x & 31) == 0 && v != 0.0) atomicAdd(out + k, v);
+    }
+}
+
+__global__ void field_energy_kernel(const double* __restrict__ E, const double* __restrict__ vol, int n,
+                                    double* out) {
+    double s = 0;
+    for (int c = blockIdx.x * blockDim.x + threadIdx.x; c < n; c += gridDim.x * blockDim.x) {
+        const double* e = E + 3 * size_t(c);
+        s += (e[0] * e[0] + e[1] * e[1] + e[2] * e[2]) * vol[c];
+    }
+    for (int off = 16; off >= 1; off >>= 1) s += __shfl_xor_sync(0xffffffffu, s, off);
+    if ((threadIdx.x & 31) == 0 && s != 0.0) atomicAdd(out, s);
+}
+
+// ------------------------------------------------------------ launchers --
+static inline int blocks(long n, int bs) { return int((n + bs - 1) / bs); }
+
+cudaError_t fields_set_patches(const PatchConst& p) {
+    return cudaMemcpyToSymbol(c_patchF, &p, sizeof p);
+}
+
+void launch_charge_update(const DMesh& m, int vw, int fixed, double fix_scale, const double* ccd,
+                          const double* vtxd, const long long* ccf, const long long* vtxf,
+                          double space_charge, double* rho, cudaStream_t s) {
+    charge_update_kernel<<<blocks(m.n_cells, 256), 256, 0, s>>>(m, vw, fixed, fix_scale, ccd, vtxd, ccf,
+                                                                vtxf, space_charge, rho);
+}
+
+void launch_floating_update(double* qconv, double* sigma, double* grad_bc, cudaStream_t s) {
+    floating_update_kernel<<<1, 32, 0, s>>>(qconv, sigma, grad_bc);
+}
+
+int pcg_blocks(int n) { return (n + 2047) / 2048; }
+
+void launch_rhs(const DMesh& m, const double* rho, const double* grad_bc, double* b, int singular,
+                double* part, PcgState* st, cudaStream_t s) {
+    rhs_kernel<<<blocks(m.n_cells, 256), 256, 0, s>>>(m, rho, grad_bc, b);
+    if (singular) {
+        sum_kernel<<<pcg_blocks(m.n_cells), 256, 0, s>>>(b, m.n_cells, part, st);
+        sub_mean_kernel<<<blocks(m.n_cells, 256), 256, 0, s>>>(b, m.n_cells, st);
+    }
+}
+
+void launch_pcg_init(const DMesh& m, const double* b, const double* x, double* r, double* z,
+                     double* part, PcgState* st, double tol, cudaStream_t s) {
+    pcg_init_kernel<<<pcg_blocks(m.n_cells), 256, 0, s>>>(m, b, x, r, z, part, st, tol);
+}
+
+void launch_pcg_iteration(const DMesh& m, double* x, double* r, double* z, const double* p_old,
+                          double* p_new, double* q, double* part, PcgState* st, int k, int maxit,
+                          cudaStream_t s) {
+    const int nb = pcg_blocks(m.n_cells);
+    pcg_spmv_kernel<<<nb, 256, 0, s>>>(m, z, p_old, p_new, q, part, st, k == 1);
+    pcg_update_kernel<<<nb, 256, 0, s>>>(m, x, r, z, p_new, q, part, st, k, maxit);
+}
+
+void launch_of_residual(const DMesh& m, const double* b, const double* x, double* part, PcgState* st,
+                        cudaStream_t s) {
+    sum_kernel<<<pcg_blocks(m.n_cells), 256, 0, s>>>(x, m.n_cells, part, st);
+    of_residual_kernel<<<pcg_blocks(m.n_cells), 256, 0, s>>>(m, b, x, part, st);
+}
+
+void launch_efield(const DMesh& m, const double* phi, const double* grad_bc, double* E, double* Eb,
+                   double* Ept, float* E32, float* Ept32, cudaStream_t s) {
+    grad_E_kernel<<<blocks(m.n_cells, 256), 256, 0, s>>>(m, phi, grad_bc, E);
+    if (m.n_bfaces > 0) boundary_E_kernel<<<blocks(m.n_bfaces, 256), 256, 0, s>>>(m, phi, grad_bc, E, Eb);
+    point_E_kernel<<<blocks(m.n_points, 256), 256, 0, s>>>(m, E, Eb, Ept, Ept32);
+    to_float_kernel<<<blocks(3L * m.n_cells, 256), 256, 0, s>>>(E, E32, 3L * m.n_cells);
+}
+
+void launch_to_float(const double* a, float* b, long n, cudaStream_t s) {
+    to_float_kernel<<<blocks(n, 256), 256, 0, s>>>(a, b, n);
+}
+
+void launch_fill(double* a, long n, double v, cudaStream_t s) {
+    if (n > 0) fill_kernel<<<blocks(n, 256), 256, 0, s>>>(a, n, v);
+}
+
+void launch_diagnostics(const int32_t* tet, const double* u0, const double* u1, const double* u2,
+                        const float* f0, const float* f1, const float* f2, int n, double mass,
+                        double weight, double* out, cudaStream_t s) {
+    if (n <= 0) return;
+    diagnostics_kernel<<<std::min(blocks(n, 256), 1216), 256, 0, s>>>(tet, u0, u1, u2, f0, f1, f2, n, mass,
+                                                                       weight, out);
+}
+
+void launch_field_energy(const double* E, const double* vol, int n, double* out, cudaStream_t s) {
+    field_energy_kernel<<<std::min(blocks(n, 256), 1216), 256, 0, s>>>(E, vol, n, out);
+}
+
+}  // namespace pgd

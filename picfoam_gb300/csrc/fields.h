@@ -1,0 +1,42 @@
+// fields.h -- field and Poisson kernel launchers (host declarations).
+#pragma once
+
+#include <algorithm>
+
+#include "common.cuh"
+
+namespace pgd {
+
+// Device-resident PCG scalars; every kernel of one solve reads and writes it.
+struct PcgState {
+    double rz, rr, bb, pq, beta, lim, mean, of_residual;
+    int done, iters, converged, pad;
+    unsigned int ticket;
+    unsigned int pad2[3];
+};
+
+cudaError_t fields_set_patches(const PatchConst& p);
+int pcg_blocks(int n);
+void launch_charge_update(const DMesh& m, int vw, int fixed, double fix_scale, const double* ccd,
+                          const double* vtxd, const long long* ccf, const long long* vtxf,
+                          double space_charge, double* rho, cudaStream_t s);
+void launch_floating_update(double* qconv, double* sigma, double* grad_bc, cudaStream_t s);
+void launch_rhs(const DMesh& m, const double* rho, const double* grad_bc, double* b, int singular,
+                double* part, PcgState* st, cudaStream_t s);
+void launch_pcg_init(const DMesh& m, const double* b, const double* x, double* r, double* z,
+                     double* part, PcgState* st, double tol, cudaStream_t s);
+void launch_pcg_iteration(const DMesh& m, double* x, double* r, double* z, const double* p_old,
+                          double* p_new, double* q, double* part, PcgState* st, int k, int maxit,
+                          cudaStream_t s);
+void launch_of_residual(const DMesh& m, const double* b, const double* x, double* part, PcgState* st,
+                        cudaStream_t s);
+void launch_efield(const DMesh& m, const double* phi, const double* grad_bc, double* E, double* Eb,
+                   double* Ept, float* E32, float* Ept32, cudaStream_t s);
+void launch_to_float(const double* a, float* b, long n, cudaStream_t s);
+void launch_fill(double* a, long n, double v, cudaStream_t s);
+void launch_diagnostics(const int32_t* tet, const double* u0, const double* u1, const double* u2,
+                        const float* f0, const float* f1, const float* f2, int n, double mass,
+                        double weight, double* out, cudaStream_t s);
+void launch_field_energy(const double* E, const double* vol, int n, double* out, cudaStream_t s);
+
+}  // namespace pgd

@@ -1,0 +1,13 @@
+// kernels.h -- host-side declarations of the kernel launchers.
+#pragma once
+
+#include "common.cuh"
+
+namespace pgd {
+
+cudaError_t move_fp64_set_tables(const TetConst& t, const PatchConst& p);
+cudaError_t move_fp32_set_tables(const TetConst& t, const PatchConst& p);
+void launch_move_fp64(const MoveParams& P, int grid, cudaStream_t s);
+void launch_move_fp32(const MoveParams& P, int grid, cudaStream_t s);
+
+}  // namespace pgd

@@ -1,0 +1,1006 @@
+// library.cu -- the picgpu C ABI: context, device memory, step orchestration.
+//
+// A context holds one PIC/MCC case resident on the current CUDA device.
+// picgpu_step runs the PICCloud::evolve sequence
+// (PICMCCFVM/clouds/Templates/PICCloud/PICCloud.C:1426-1471) as a chain of
+// kernels on the context's stream:
+//
+//   zero charge accumulators
+//   move (push + track + patch + deposit), one launch per species
+//   collisions (Coulomb, electron-neutral MCC) on the cell-sorted store
+//   charge update -> rho            (calculateFields, PICCloud.C:587-695)
+//   floating patches: sigma, g      (preUpdate_Boundary)
+//   Poisson PCG, E, point E         (ElectroStaticSolver::solveFields)
+//
+// Nothing returns to the host inside a step except the PCG convergence flag
+// and the per-step counters.
+#include <cuda_runtime.h>
+
+#include <cstdio>
+#include <cstring>
+#include <memory>
+#include <string>
+#include <vector>
+
+#include "collide.h"
+#include "fields.h"
+#include "hexmesh.hpp"
+#include "kernels.h"
+#include "particles.h"
+#include "picgpu.h"
+
+using pgd::DMesh;
+
+struct picgpu_mesh {
+    pg::HexMesh m;
+};
+
+namespace {
+
+constexpr double kMu0 = 4.0 * 3.14159265358979323846 * 1e-7;
+constexpr double kCl = 299792458.0;
+
+struct SpeciesBuf {
+    long n = 0;      // used slots (removed particles keep tet = -1 until compaction)
+    long cap = 0;
+    int cur = 0;     // active buffer of the double-buffered store
+    int32_t* tet[2] = {nullptr, nullptr};
+    double* y64[2][3] = {};
+    double* u64[2][3] = {};
+    float* y32[2][3] = {};
+    float* u32[2][3] = {};
+};
+
+struct EventPair {
+    cudaEvent_t a, b;
+    int phase;
+};
+
+}  // namespace
+
+struct picgpu_ctx {
+    std::string err;
+    picgpu_config cfg{};
+    pg::HexMesh m;
+    cudaStream_t stream = nullptr;
+    int device = 0, sm_count = 148;
+    std::vector<void*> allocs;
+    DMesh dm{};
+    pgd::TetConst tc{};
+    pgd::PatchConst pc{};
+    SpeciesBuf sp[PICGPU_MAX_SPECIES];
+    bool mixed = false;
+    double *phi = nullptr, *rho = nullptr, *E = nullptr, *Ept = nullptr, *Eb = nullptr;
+    float *E32 = nullptr, *Ept32 = nullptr;
+    double *cc_data = nullptr, *vtx_data = nullptr;
+    long long *cc_fix = nullptr, *vtx_fix = nullptr;
+    double *qconv = nullptr, *sigma = nullptr, *grad_bc = nullptr;
+    double *b = nullptr, *r = nullptr, *z = nullptr, *p[2] = {nullptr, nullptr}, *q = nullptr,
+           *part = nullptr;
+    pgd::PcgState* st = nullptr;
+    pgd::PcgState* st_host = nullptr;
+    pgd::MoveCounters* counters = nullptr;
+    pgd::MoveCounters* counters_host = nullptr;
+    double* diag = nullptr;
+    double fix_scale = 1.0;
+    bool rotation = false;
+    long long step_index = 0;
+    // compaction / sort scratch
+    int* scan_buf = nullptr;
+    long scan_cap = 0;
+    pgd::CollideState coll{};
+    // profiling
+    bool profiling = false;
+    std::vector<EventPair> pending;
+    std::vector<cudaEvent_t> free_events;
+    double phase_ms[PICGPU_PHASE_COUNT] = {};
+    int64_t phase_launches[PICGPU_PHASE_COUNT] = {};
+    int64_t launches = 0;
+    picgpu_step_stats acc{};
+    cudaEvent_t timer[2] = {nullptr, nullptr};
+};
+
+picgpu_status pgd_collisions(picgpu_ctx* c, picgpu_step_stats* stats);
+
+namespace {
+
+picgpu_status fail(picgpu_ctx* c, cudaError_t e, const char* what, int line) {
+    char buf[512];
+    std::snprintf(buf, sizeof buf, "CUDA error %s (%s) at library.cu:%d: %s", cudaGetErrorName(e),
+                  cudaGetErrorString(e), line, what);
+    c->err = buf;
+    return PICGPU_CUDA_ERROR;
+}
+
+#define CK(call)                                               \
+    do {                                                       \
+        cudaError_t e_ = (call);                               \
+        if (e_ != cudaSuccess) return fail(c, e_, #call, __LINE__); \
+    } while (0)
+
+picgpu_status bad(picgpu_ctx* c, picgpu_status s, const std::string& msg) {
+    c->err = msg;
+    return s;
+}
+
+template <class T>
+picgpu_status dalloc(picgpu_ctx* c, T** out, size_t count) {
+    void* ptr = nullptr;
+    const size_t bytes = std::max<size_t>(count, 1) * sizeof(T);
+    cudaError_t e = cudaMalloc(&ptr, bytes);
+    if (e != cudaSuccess) {
+        cudaGetLastError();
+        c->err = "device allocation of " + std::to_string(bytes) + " bytes failed";
+        return PICGPU_OOM;
+    }
+    c->allocs.push_back(ptr);
+    *out = static_cast<T*>(ptr);
+    return PICGPU_OK;
+}
+
+template <class T>
+picgpu_status upload(picgpu_ctx* c, T** out, const std::vector<T>& v) {
+    picgpu_status s = dalloc(c, out, v.size());
+    if (s) return s;
+    if (!v.empty()) CK(cudaMemcpy(*out, v.data(), v.size() * sizeof(T), cudaMemcpyHostToDevice));
+    return PICGPU_OK;
+}
+
+void dfree(picgpu_ctx* c, void* ptr) {
+    if (!ptr) return;
+    for (auto& a : c->allocs)
+        if (a == ptr) { cudaFree(a); a = nullptr; }
+}
+
+// ------------------------------------------------------------ profiling --
+struct PhaseScope {
+    picgpu_ctx* c;
+    int phase;
+    cudaEvent_t a = nullptr, b = nullptr;
+    PhaseScope(picgpu_ctx* c_, int ph) : c(c_), phase(ph) {
+        if (!c->profiling) return;
+        a = get();
+        b = get();
+        cudaEventRecord(a, c->stream);
+    }
+    cudaEvent_t get() {
+        if (!c->free_events.empty()) {
+            cudaEvent_t e = c->free_events.back();
+            c->free_events.pop_back();
+            return e;
+        }
+        cudaEvent_t e;
+        cudaEventCreate(&e);
+        return e;
+    }
+    ~PhaseScope() {
+        if (!c->profiling) return;
+        cudaEventRecord(b, c->stream);
+        c->pending.push_back({a, b, phase});
+    }
+};
+
+void harvest_events(picgpu_ctx* c) {
+    for (auto& ep : c->pending) {
+        float ms = 0.f;
+        if (cudaEventSynchronize(ep.b) == cudaSuccess && cudaEventElapsedTime(&ms, ep.a, ep.b) == cudaSuccess) {
+            c->phase_ms[ep.phase] += ms;
+            c->phase_launches[ep.phase] += 1;
+        }
+        c->free_events.push_back(ep.a);
+        c->free_events.push_back(ep.b);
+    }
+    c->pending.clear();
+}
+
+// --------------------------------------------------------- species store --
+picgpu_status alloc_species(picgpu_ctx* c, int s, long cap) {
+    SpeciesBuf& b = c->sp[s];
+    for (int k = 0; k < 2; ++k) {
+        dfree(c, b.tet[k]);
+        for (int a = 0; a < 3; ++a) {
+            dfree(c, b.y64[k][a]); dfree(c, b.u64[k][a]); dfree(c, b.y32[k][a]); dfree(c, b.u32[k][a]);
+            b.y64[k][a] = b.u64[k][a] = nullptr;
+            b.y32[k][a] = b.u32[k][a] = nullptr;
+        }
+        b.tet[k] = nullptr;
+    }
+    b.cap = cap;
+    b.cur = 0;
+    for (int k = 0; k < 2; ++k) {
+        picgpu_status st = dalloc(c, &b.tet[k], cap);
+        if (st) return st;
+        for (int a = 0; a < 3; ++a) {
+            if (c->mixed) {
+                if ((st = dalloc(c, &b.y32[k][a], cap))) return st;
+                if ((st = dalloc(c, &b.u32[k][a], cap))) return st;
+            } else {
+                if ((st = dalloc(c, &b.y64[k][a], cap))) return st;
+                if ((st = dalloc(c, &b.u64[k][a], cap))) return st;
+            }
+        }
+    }
+    return PICGPU_OK;
+}
+
+pgd::DSpecies view(const picgpu_ctx* c, int s, int k) {
+    const SpeciesBuf& b = c->sp[s];
+    pgd::DSpecies v{};
+    v.tet = b.tet[k];
+    for (int a = 0; a < 3; ++a) {
+        v.y64[a] = b.y64[k][a];
+        v.u64[a] = b.u64[k][a];
+        v.y32[a] = b.y32[k][a];
+        v.u32[a] = b.u32[k][a];
+    }
+    return v;
+}
+
+int grid_for(const picgpu_ctx* c, long n, int per_thread_block = 256) {
+    const long want = (n + per_thread_block - 1) / per_thread_block;
+    const long cap = long(c->sm_count) * 8;
+    return int(std::max<long>(1, std::min(want, cap)));
+}
+
+pgd::MoveParams move_params(picgpu_ctx* c, int s, bool deposit_only) {
+    const picgpu_species& S = c->cfg.species[s];
+    pgd::MoveParams P{};
+    P.m = c->dm;
+    P.n = int(c->sp[s].n);
+    P.species = s;
+    P.pusher = c->cfg.pusher;
+    P.field_weighting = c->cfg.field_weighting;
+    P.charge_distribution = c->cfg.charge_distribution;
+    P.deposit_mode = c->cfg.deposit_mode;
+    P.rotation = c->rotation;
+    P.solve_movement = deposit_only ? 0 : S.solve_movement;
+    P.sync = c->cfg.sync_velocity_at_boundary;
+    P.max_steps = c->cfg.track_max_steps > 0 ? c->cfg.track_max_steps : 4096;
+    P.q = S.charge;
+    P.mass = S.mass;
+    P.value = S.charge * S.weight;
+    P.weight = S.weight;
+    P.dt = c->cfg.dt;
+    for (int a = 0; a < 3; ++a) P.B[a] = c->cfg.B[a];
+    P.fix_scale = c->fix_scale;
+    P.E = c->E;
+    P.Ept = c->Ept;
+    P.E32 = c->E32;
+    P.Ept32 = c->Ept32;
+    P.cc_data = c->cc_data;
+    P.vtx_data = c->vtx_data;
+    P.cc_fix = c->cc_fix;
+    P.vtx_fix = c->vtx_fix;
+    P.qconv = c->qconv;
+    P.p = view(c, s, c->sp[s].cur);
+    P.counters = c->counters;
+    return P;
+}
+
+picgpu_status zero_accumulators(picgpu_ctx* c) {
+    CK(cudaMemsetAsync(c->cc_data, 0, sizeof(double) * c->m.n_cells, c->stream));
+    CK(cudaMemsetAsync(c->vtx_data, 0, sizeof(double) * c->m.n_points, c->stream));
+    CK(cudaMemsetAsync(c->cc_fix, 0, sizeof(long long) * c->m.n_cells, c->stream));
+    CK(cudaMemsetAsync(c->vtx_fix, 0, sizeof(long long) * c->m.n_points, c->stream));
+    return PICGPU_OK;
+}
+
+// Move (or deposit only) every species; counters land in c->counters.
+picgpu_status move_species(picgpu_ctx* c, bool deposit_only) {
+    CK(cudaMemsetAsync(c->counters, 0, sizeof(pgd::MoveCounters), c->stream));
+    for (int s = 0; s < c->cfg.n_species; ++s) {
+        if (c->sp[s].n == 0) continue;
+        const pgd::MoveParams P = move_params(c, s, deposit_only);
+        const int grid = grid_for(c, c->sp[s].n);
+        {
+            PhaseScope ps(c, PICGPU_PHASE_MOVE);
+            if (c->mixed) pgd::launch_move_fp32(P, grid, c->stream);
+            else pgd::launch_move_fp64(P, grid, c->stream);
+        }
+        c->launches++;
+    }
+    CK(cudaGetLastError());
+    return PICGPU_OK;
+}
+
+picgpu_status charge_update(picgpu_ctx* c) {
+    PhaseScope ps(c, PICGPU_PHASE_CHARGE);
+    pgd::launch_charge_update(c->dm, c->cfg.charge_distribution == PICGPU_WEIGHTING_VOLUME,
+                              c->cfg.deposit_mode == PICGPU_DEPOSIT_FIXED_POINT, c->fix_scale, c->cc_data,
+                              c->vtx_data, c->cc_fix, c->vtx_fix, c->cfg.space_charge, c->rho, c->stream);
+    c->launches++;
+    CK(cudaGetLastError());
+    return PICGPU_OK;
+}
+
+picgpu_status efield(picgpu_ctx* c) {
+    PhaseScope ps(c, PICGPU_PHASE_EFIELD);
+    pgd::launch_efield(c->dm, c->phi, c->grad_bc, c->E, c->Eb, c->Ept, c->E32, c->Ept32, c->stream);
+    c->launches += c->dm.n_bfaces > 0 ? 4 : 3;
+    CK(cudaGetLastError());
+    return PICGPU_OK;
+}
+
+picgpu_status set_applied_field(picgpu_ctx* c) {
+    std::vector<double> e(3 * size_t(c->m.n_cells)), ep(3 * size_t(c->m.n_points));
+    for (size_t i = 0; i < e.size(); ++i) e[i] = c->cfg.E_applied[i % 3];
+    for (size_t i = 0; i < ep.size(); ++i) ep[i] = c->cfg.E_applied[i % 3];
+    CK(cudaMemcpyAsync(c->E, e.data(), e.size() * sizeof(double), cudaMemcpyHostToDevice, c->stream));
+    CK(cudaMemcpyAsync(c->Ept, ep.data(), ep.size() * sizeof(double), cudaMemcpyHostToDevice, c->stream));
+    pgd::launch_to_float(c->E, c->E32, long(e.size()), c->stream);
+    pgd::launch_to_float(c->Ept, c->Ept32, long(ep.size()), c->stream);
+    c->launches += 2;
+    CK(cudaStreamSynchronize(c->stream));
+    return PICGPU_OK;
+}
+
+// Poisson PCG from the current phi; fills stats.
+picgpu_status poisson(picgpu_ctx* c, picgpu_step_stats* stats) {
+    const int n = c->m.n_cells;
+    const double tol = c->cfg.pcg_tol > 0 ? c->cfg.pcg_tol : 1e-10;
+    const int maxit = c->cfg.pcg_max_iter > 0 ? c->cfg.pcg_max_iter : 10000;
+    {
+        PhaseScope ps(c, PICGPU_PHASE_POISSON);
+        pgd::launch_rhs(c->dm, c->rho, c->grad_bc, c->b, !c->m.has_dirichlet, c->part, c->st, c->stream);
+        pgd::launch_pcg_init(c->dm, c->b, c->phi, c->r, c->z, c->part, c->st, tol, c->stream);
+        c->launches += c->m.has_dirichlet ? 2 : 4;
+        CK(cudaMemcpyAsync(c->st_host, c->st, sizeof(pgd::PcgState), cudaMemcpyDeviceToHost, c->stream));
+        CK(cudaStreamSynchronize(c->stream));
+        int k = 1;
+        int batch = 4;
+        while (!c->st_host->done && k <= maxit) {
+            for (int j = 0; j < batch && k <= maxit; ++j, ++k) {
+                pgd::launch_pcg_iteration(c->dm, c->phi, c->r, c->z, c->p[(k + 1) & 1], c->p[k & 1], c->q,
+                                          c->part, c->st, k, maxit, c->stream);
+                c->launches += 2;
+            }
+            CK(cudaGetLastError());
+            CK(cudaMemcpyAsync(c->st_host, c->st, sizeof(pgd::PcgState), cudaMemcpyDeviceToHost, c->stream));
+            CK(cudaStreamSynchronize(c->stream));
+            batch = std::min(batch * 2, 32);
+        }
+        pgd::launch_of_residual(c->dm, c->b, c->phi, c->part, c->st, c->stream);
+        c->launches += 2;
+        CK(cudaMemcpyAsync(c->st_host, c->st, sizeof(pgd::PcgState), cudaMemcpyDeviceToHost, c->stream));
+    }
+    picgpu_status s = efield(c);
+    if (s) return s;
+    CK(cudaStreamSynchronize(c->stream));
+    (void)n;
+    const pgd::PcgState& S = *c->st_host;
+    if (stats) {
+        stats->pcg_iterations = S.iters;
+        stats->pcg_iterations_total += S.iters;
+        stats->pcg_residual_l2 = S.bb > 0 ? std::sqrt(S.rr / S.bb) : 0.0;
+        stats->pcg_residual_of = S.of_residual;
+    }
+    if (!S.converged) return bad(c, PICGPU_PCG_NOT_CONVERGED, "PCG did not converge within pcg_max_iter");
+    return PICGPU_OK;
+}
+
+picgpu_status solve_fields(picgpu_ctx* c, picgpu_step_stats* stats) {
+    if (c->cfg.maxwell_solver != PICGPU_MAXWELL_ELECTROSTATIC) return PICGPU_OK;
+    return poisson(c, stats);
+}
+
+picgpu_status ensure_scan(picgpu_ctx* c, long n) {
+    if (c->scan_cap >= n) return PICGPU_OK;
+    dfree(c, c->scan_buf);
+    c->scan_cap = std::max<long>(n, 1024);
+    return dalloc(c, &c->scan_buf, c->scan_cap);
+}
+
+// Drop removed particles (stable) in every species that lost some.
+picgpu_status compact(picgpu_ctx* c, bool force) {
+    for (int s = 0; s < c->cfg.n_species; ++s) {
+        SpeciesBuf& B = c->sp[s];
+        if (B.n == 0) continue;
+        if (!force && c->counters_host->absorbed == 0) continue;
+        const long nblk = pgd::compact_blocks(B.n);
+        picgpu_status st = ensure_scan(c, nblk + 1);
+        if (st) return st;
+        const pgd::DSpecies src = view(c, s, B.cur), dst = view(c, s, B.cur ^ 1);
+        long kept = 0;
+        CK(pgd::compact_species(src, dst, B.n, c->mixed, c->scan_buf, &kept, c->stream));
+        c->launches += 3;
+        B.n = kept;
+        B.cur ^= 1;
+    }
+    return PICGPU_OK;
+}
+
+picgpu_status read_counters(picgpu_ctx* c) {
+    CK(cudaMemcpyAsync(c->counters_host, c->counters, sizeof(pgd::MoveCounters), cudaMemcpyDeviceToHost,
+                       c->stream));
+    CK(cudaStreamSynchronize(c->stream));
+    if (c->profiling) harvest_events(c);
+    return PICGPU_OK;
+}
+
+void add_counters(picgpu_ctx* c, picgpu_step_stats* stats) {
+    if (!stats) return;
+    stats->tet_steps += (int64_t)c->counters_host->tet_steps;
+    stats->face_crossings += (int64_t)c->counters_host->faces;
+    stats->wall_hits += (int64_t)c->counters_host->walls;
+}
+
+void fill_counts(picgpu_ctx* c, picgpu_step_stats* stats) {
+    if (!stats) return;
+    for (int s = 0; s < c->cfg.n_species; ++s) stats->n_particles[s] = c->sp[s].n;
+}
+
+// One PICCloud::evolve.
+picgpu_status one_step(picgpu_ctx* c, picgpu_step_stats* stats, bool fields) {
+    picgpu_status s;
+    if ((s = zero_accumulators(c))) return s;
+    // count removals per species: run species one at a time for the tally
+    std::vector<long> before(c->cfg.n_species);
+    for (int k = 0; k < c->cfg.n_species; ++k) before[k] = c->sp[k].n;
+    if ((s = move_species(c, false))) return s;
+    if ((s = read_counters(c))) return s;
+    if (c->counters_host->error) {
+        const int e = c->counters_host->error;
+        return bad(c, picgpu_status(e), e == PICGPU_SPEED_OF_LIGHT
+                                            ? "particle velocity reached the speed of light"
+                                            : "tracking exceeded track_max_steps for a particle");
+    }
+    add_counters(c, stats);
+    if (c->counters_host->absorbed) {
+        std::vector<long> alive_before(c->cfg.n_species);
+        if ((s = compact(c, false))) return s;
+        if (stats)
+            for (int k = 0; k < c->cfg.n_species; ++k) stats->n_absorbed[k] += before[k] - c->sp[k].n;
+    }
+    if (c->cfg.mcc.enabled || c->cfg.coulomb.enabled) {
+        if ((s = pgd_collisions(c, stats))) return s;
+    }
+    if ((s = charge_update(c))) return s;
+    if (!fields) return PICGPU_OK;
+    pgd::launch_floating_update(c->qconv, c->sigma, c->grad_bc, c->stream);
+    c->launches++;
+    if ((s = solve_fields(c, stats))) return s;
+    c->step_index++;
+    return PICGPU_OK;
+}
+
+}  // namespace
+
+// Collisions live in collide.cu; this bridge keeps the context private.
+picgpu_status pgd_collisions(picgpu_ctx* c, picgpu_step_stats* stats) {
+    pgd::CollideArgs a{};
+    a.m = c->dm;
+    a.cfg = &c->cfg;
+    a.step = c->step_index;
+    a.n_species = c->cfg.n_species;
+    a.mixed = c->mixed;
+    for (int s = 0; s < c->cfg.n_species; ++s) {
+        a.sp[s] = view(c, s, c->sp[s].cur);
+        a.alt[s] = view(c, s, c->sp[s].cur ^ 1);
+        a.n[s] = c->sp[s].n;
+        a.cap[s] = c->sp[s].cap;
+    }
+    a.cc_data = c->cc_data;
+    a.vtx_data = c->vtx_data;
+    a.cc_fix = c->cc_fix;
+    a.vtx_fix = c->vtx_fix;
+    a.fix_scale = c->fix_scale;
+    a.stream = c->stream;
+    int64_t counts[8] = {};
+    long newn[PICGPU_MAX_SPECIES] = {};
+    int swapped[PICGPU_MAX_SPECIES] = {};
+    std::string msg;
+    const int st = pgd::run_collisions(c->coll, a, counts, newn, swapped, &msg, &c->launches, nullptr);
+    if (st) return bad(c, picgpu_status(st), msg);
+    for (int s = 0; s < c->cfg.n_species; ++s) {
+        c->sp[s].n = newn[s];
+        if (swapped[s]) c->sp[s].cur ^= 1;
+    }
+    if (stats) {
+        stats->mcc_candidates += counts[0];
+        stats->mcc_elastic += counts[1];
+        stats->mcc_excitation += counts[2];
+        stats->mcc_ionization += counts[3];
+        stats->coulomb_pairs += counts[4];
+    }
+    return PICGPU_OK;
+}
+
+extern "C" {
+
+picgpu_status picgpu_mesh_create(const picgpu_mesh_desc* desc, picgpu_mesh** out) {
+    if (!desc || !out) return PICGPU_INVALID_ARG;
+    *out = nullptr;
+    try {
+        auto* m = new picgpu_mesh();
+        m->m = pg::build_hex_mesh(*desc);
+        *out = m;
+    } catch (const std::exception&) {
+        return PICGPU_INVALID_ARG;
+    }
+    return PICGPU_OK;
+}
+
+void picgpu_mesh_destroy(picgpu_mesh* mesh) { delete mesh; }
+
+picgpu_status picgpu_mesh_info_get(const picgpu_mesh* mesh, picgpu_mesh_info* info) {
+    if (!mesh || !info) return PICGPU_INVALID_ARG;
+    info->n_cells = mesh->m.n_cells;
+    info->n_points = mesh->m.n_points;
+    info->n_tets = 12LL * mesh->m.n_cells;
+    info->n_patches = (int64_t)mesh->m.patches.size();
+    return PICGPU_OK;
+}
+
+picgpu_status picgpu_mesh_locate(const picgpu_mesh* mesh, size_t n, const double* xyz, int32_t* tet,
+                                 double* bary) {
+    if (!mesh || (n && (!xyz || !tet || !bary))) return PICGPU_INVALID_ARG;
+    for (size_t i = 0; i < n; ++i) tet[i] = int32_t(pg::locate(mesh->m, xyz + 3 * i, bary + 3 * i));
+    return PICGPU_OK;
+}
+
+picgpu_status picgpu_mesh_position(const picgpu_mesh* mesh, size_t n, const int32_t* tet, const double* bary,
+                                   double* xyz) {
+    if (!mesh || (n && (!xyz || !tet || !bary))) return PICGPU_INVALID_ARG;
+    const long long nt = 12LL * mesh->m.n_cells;
+    for (size_t i = 0; i < n; ++i) {
+        if (tet[i] < 0 || tet[i] >= nt) return PICGPU_INVALID_ARG;
+        pg::position(mesh->m, tet[i], bary + 3 * i, xyz + 3 * i);
+    }
+    return PICGPU_OK;
+}
+
+picgpu_status picgpu_mesh_cells(const picgpu_mesh* mesh, double* centres, double* volumes) {
+    if (!mesh) return PICGPU_INVALID_ARG;
+    if (centres) std::memcpy(centres, mesh->m.cc.data(), mesh->m.cc.size() * sizeof(double));
+    if (volumes) std::memcpy(volumes, mesh->m.vol.data(), mesh->m.vol.size() * sizeof(double));
+    return PICGPU_OK;
+}
+
+picgpu_status picgpu_create(const picgpu_mesh_desc* mesh, const picgpu_config* cfg, picgpu_ctx** out) {
+    if (!mesh || !cfg || !out) return PICGPU_INVALID_ARG;
+    auto* c = new picgpu_ctx();
+    *out = c;
+    try {
+        c->m = pg::build_hex_mesh(*mesh);
+    } catch (const std::exception& e) {
+        return bad(c, PICGPU_INVALID_ARG, e.what());
+    }
+    if (cfg->n_species < 1 || cfg->n_species > PICGPU_MAX_SPECIES)
+        return bad(c, PICGPU_INVALID_ARG, "config: n_species must be 1..4");
+    if (!(cfg->dt > 0)) return bad(c, PICGPU_INVALID_ARG, "config: dt must be > 0");
+    if (cfg->pusher < PICGPU_PUSHER_NONE || cfg->pusher > PICGPU_PUSHER_HIGUERA_CARY)
+        return bad(c, PICGPU_INVALID_ARG, "config: unknown ParticlePusher");
+    if (cfg->precision != PICGPU_PREC_FP64 && cfg->precision != PICGPU_PREC_MIXED)
+        return bad(c, PICGPU_INVALID_ARG, "config: unknown precision");
+    if (cfg->coulomb.enabled && !(cfg->coulomb.coulomb_log > 0))
+        return bad(c, PICGPU_NOT_SUPPORTED, "Coulomb: only a fixed coulombLog is supported");
+    c->cfg = *cfg;
+    c->mixed = cfg->precision == PICGPU_PREC_MIXED;
+    c->rotation = cfg->B[0] != 0.0 || cfg->B[1] != 0.0 || cfg->B[2] != 0.0;
+    double qmax = 0;
+    for (int s = 0; s < cfg->n_species; ++s)
+        qmax = std::fmax(qmax, std::fabs(cfg->species[s].charge * cfg->species[s].weight));
+    c->fix_scale = qmax > 0 ? std::ldexp(1.0, 39 - std::ilogb(qmax)) : 1.0;
+
+    CK(cudaGetDevice(&c->device));
+    CK(cudaDeviceGetAttribute(&c->sm_count, cudaDevAttrMultiProcessorCount, c->device));
+    CK(cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking));
+
+    const pg::HexMesh& m = c->m;
+    // tables
+    for (int t = 0; t < 12; ++t) {
+        for (int j = 0; j < 3; ++j) c->tc.tri[t][j] = int8_t(m.tt.tri[t][j]);
+        for (int i = 0; i < 4; ++i) {
+            c->tc.inner_next[t][i] = int8_t(m.tt.inner_next[t][i]);
+            for (int j = 0; j < 4; ++j) c->tc.inner_src[t][i][j] = int8_t(m.tt.inner_src[t][i][j]);
+        }
+        c->tc.cross_next[t] = int8_t(m.tt.cross_next[t]);
+        for (int j = 0; j < 4; ++j) c->tc.cross_src[t][j] = int8_t(m.tt.cross_src[t][j]);
+    }
+    if (m.patches.size() > size_t(pgd::kMaxPatches)) return bad(c, PICGPU_INVALID_ARG, "too many patches");
+    c->pc.n = int(m.patches.size());
+    for (size_t p = 0; p < m.patches.size(); ++p) {
+        c->pc.kind[p] = m.patches[p].p.kind;
+        c->pc.phi_bc[p] = m.patches[p].p.phi_bc;
+        c->pc.phi[p] = m.patches[p].p.phi;
+        c->pc.area[p] = m.patches[p].area;
+    }
+    CK(pgd::move_fp64_set_tables(c->tc, c->pc));
+    CK(pgd::move_fp32_set_tables(c->tc, c->pc));
+    CK(pgd::fields_set_patches(c->pc));
+    CK(pgd::collide_set_tables(c->tc));
+
+    // mesh arrays
+    picgpu_status s;
+    DMesh& d = c->dm;
+    d.n_cells = m.n_cells;
+    d.n_points = m.n_points;
+    d.n_bfaces = int(m.bfaces.size());
+    d.n_classes = m.n_classes;
+    for (int a = 0; a < 3; ++a) {
+        d.empty[a] = m.empty[a];
+        d.mesh_centre[a] = m.mesh_centre[a];
+    }
+    d.any_empty = m.empty[0] || m.empty[1] || m.empty[2];
+    std::vector<float> inv32(m.cls_tetinv.begin(), m.cls_tetinv.end());
+    std::vector<float> off32(m.cls_offset.begin(), m.cls_offset.end());
+    std::vector<float> fn32(m.cls_fnormal.begin(), m.cls_fnormal.end());
+    std::vector<int> bf_cell, bf_patch;
+    std::vector<double> bf_normal, bf_area, bf_delta;
+    for (const auto& bf : m.bfaces) {
+        bf_cell.push_back(bf.cell);
+        bf_patch.push_back(bf.patch);
+        for (int a = 0; a < 3; ++a) bf_normal.push_back(bf.normal[a]);
+        bf_area.push_back(bf.area);
+        bf_delta.push_back(bf.delta);
+    }
+    std::vector<double> Mdiag(m.n_cells), Moff(m.lap_off.size()), dinv(m.n_cells);
+    for (int i = 0; i < m.n_cells; ++i) {
+        Mdiag[i] = -m.lap_diag[i];
+        dinv[i] = 1.0 / Mdiag[i];
+    }
+    for (size_t i = 0; i < Moff.size(); ++i) Moff[i] = -m.lap_off[i];
+    int* ip;
+    double* dp;
+    float* fp;
+#define UP(field, vec, T)                              \
+    {                                                  \
+        T* ptr_;                                       \
+        if ((s = upload(c, &ptr_, vec))) return s;     \
+        d.field = ptr_;                                \
+    }
+    UP(cell_class, m.cell_class, int);
+    UP(nbr, m.nbr, int);
+    UP(cell_pt, m.cell_pt, int);
+    UP(cc, m.cc, double);
+    UP(vol, m.vol, double);
+    UP(tetinv, m.cls_tetinv, double);
+    UP(tetinv32, inv32, float);
+    UP(offset, m.cls_offset, double);
+    UP(offset32, off32, float);
+    UP(fnormal, m.cls_fnormal, double);
+    UP(fnormal32, fn32, float);
+    UP(farea, m.cls_farea, double);
+    UP(ip_weight, m.ip_weight, double);
+    UP(cell_bface, m.cell_bface, int);
+    UP(bf_cell, bf_cell, int);
+    UP(bf_patch, bf_patch, int);
+    UP(bf_normal, bf_normal, double);
+    UP(bf_area, bf_area, double);
+    UP(bf_delta, bf_delta, double);
+    UP(vw_weight, m.vw_weight, double);
+    UP(pi_start, m.pi_start, int);
+    UP(pi_src, m.pi_src, int);
+    UP(pi_w, m.pi_w, double);
+    UP(Mdiag, Mdiag, double);
+    UP(Moff, Moff, double);
+    UP(dinv, dinv, double);
+#undef UP
+    (void)ip; (void)dp; (void)fp;
+
+    // fields
+    const size_t nc = m.n_cells, np = m.n_points, nbf = m.bfaces.size(), npa = m.patches.size();
+    if ((s = dalloc(c, &c->phi, nc)) || (s = dalloc(c, &c->rho, nc)) || (s = dalloc(c, &c->E, 3 * nc)) ||
+        (s = dalloc(c, &c->Ept, 3 * np)) || (s = dalloc(c, &c->Eb, 3 * nbf)) ||
+        (s = dalloc(c, &c->E32, 3 * nc)) || (s = dalloc(c, &c->Ept32, 3 * np)) ||
+        (s = dalloc(c, &c->cc_data, nc)) || (s = dalloc(c, &c->vtx_data, np)) ||
+        (s = dalloc(c, &c->cc_fix, nc)) || (s = dalloc(c, &c->vtx_fix, np)) ||
+        (s = dalloc(c, &c->qconv, npa)) || (s = dalloc(c, &c->sigma, npa)) ||
+        (s = dalloc(c, &c->grad_bc, npa)) || (s = dalloc(c, &c->b, nc)) || (s = dalloc(c, &c->r, nc)) ||
+        (s = dalloc(c, &c->z, nc)) || (s = dalloc(c, &c->p[0], nc)) || (s = dalloc(c, &c->p[1], nc)) ||
+        (s = dalloc(c, &c->q, nc)) || (s = dalloc(c, &c->part, 3 * size_t(pgd::pcg_blocks(int(nc))) + 8)) ||
+        (s = dalloc(c, &c->st, 1)) || (s = dalloc(c, &c->counters, 1)) || (s = dalloc(c, &c->diag, 64)))
+        return s;
+    CK(cudaMemset(c->phi, 0, nc * sizeof(double)));
+    CK(cudaMemset(c->E, 0, 3 * nc * sizeof(double)));
+    CK(cudaMemset(c->Ept, 0, 3 * np * sizeof(double)));
+    CK(cudaMemset(c->E32, 0, 3 * nc * sizeof(float)));
+    CK(cudaMemset(c->Ept32, 0, 3 * np * sizeof(float)));
+    CK(cudaMemset(c->qconv, 0, npa * sizeof(double)));
+    CK(cudaMemset(c->sigma, 0, npa * sizeof(double)));
+    CK(cudaMemset(c->grad_bc, 0, npa * sizeof(double)));
+    CK(cudaMemset(c->st, 0, sizeof(pgd::PcgState)));
+    CK(cudaMallocHost(&c->st_host, sizeof(pgd::PcgState)));
+    CK(cudaMallocHost(&c->counters_host, sizeof(pgd::MoveCounters)));
+    std::memset(c->st_host, 0, sizeof(pgd::PcgState));
+    std::memset(c->counters_host, 0, sizeof(pgd::MoveCounters));
+    for (int sp = 0; sp < cfg->n_species; ++sp) {
+        const long cap = std::max<long>(cfg->species[sp].capacity_hint, 1024);
+        if ((s = alloc_species(c, sp, cap))) return s;
+    }
+    if (cfg->maxwell_solver != PICGPU_MAXWELL_ELECTROSTATIC)
+        if ((s = set_applied_field(c))) return s;
+    std::string msg;
+    const int cs = pgd::collide_init(c->coll, c->cfg, c->dm, c->stream, &msg);
+    if (cs) return bad(c, picgpu_status(cs), msg);
+    CK(cudaStreamSynchronize(c->stream));
+    c->err.clear();
+    return PICGPU_OK;
+}
+
+void picgpu_destroy(picgpu_ctx* c) {
+    if (!c) return;
+    if (c->stream) cudaStreamSynchronize(c->stream);
+    pgd::collide_free(c->coll);
+    for (void* a : c->allocs)
+        if (a) cudaFree(a);
+    for (auto& ep : c->pending) { cudaEventDestroy(ep.a); cudaEventDestroy(ep.b); }
+    for (auto e : c->free_events) cudaEventDestroy(e);
+    if (c->timer[0]) { cudaEventDestroy(c->timer[0]); cudaEventDestroy(c->timer[1]); }
+    if (c->st_host) cudaFreeHost(c->st_host);
+    if (c->counters_host) cudaFreeHost(c->counters_host);
+    if (c->stream) cudaStreamDestroy(c->stream);
+    delete c;
+}
+
+const char* picgpu_last_error(const picgpu_ctx* c) { return c ? c->err.c_str() : "null context"; }
+
+picgpu_status picgpu_mesh_query(const picgpu_ctx* c, picgpu_mesh_info* info) {
+    if (!c || !info) return PICGPU_INVALID_ARG;
+    info->n_cells = c->m.n_cells;
+    info->n_points = c->m.n_points;
+    info->n_tets = 12LL * c->m.n_cells;
+    info->n_patches = (int64_t)c->m.patches.size();
+    return PICGPU_OK;
+}
+
+picgpu_status picgpu_set_particles(picgpu_ctx* c, int species, size_t n, const int32_t* tet,
+                                   const double* bary, const double* U) {
+    if (!c || species < 0 || species >= c->cfg.n_species) return PICGPU_INVALID_ARG;
+    if (n && (!tet || !bary || !U)) return PICGPU_INVALID_ARG;
+    if (n > size_t(1) << 31) return bad(c, PICGPU_INVALID_ARG, "at most 2^31 particles per species");
+    const long long ntet = 12LL * c->m.n_cells;
+    for (size_t i = 0; i < n; ++i)
+        if (tet[i] < 0 || tet[i] >= ntet) return bad(c, PICGPU_INVALID_ARG, "particles: tet index out of range");
+    SpeciesBuf& B = c->sp[species];
+    picgpu_status s;
+    if (long(n) > B.cap) {
+        const long cap = std::max<long>(long(n) + long(n) / 4, c->cfg.species[species].capacity_hint);
+        if ((s = alloc_species(c, species, cap))) return s;
+    }
+    B.cur = 0;
+    B.n = long(n);
+    CK(cudaMemcpy(B.tet[0], tet, n * sizeof(int32_t), cudaMemcpyHostToDevice));
+    std::vector<double> col(n);
+    std::vector<float> colf(n);
+    for (int a = 0; a < 3; ++a) {
+        for (int which = 0; which < 2; ++which) {
+            const double* src = which == 0 ? bary : U;
+            for (size_t i = 0; i < n; ++i) col[i] = src[3 * i + a];
+            if (c->mixed) {
+                for (size_t i = 0; i < n; ++i) colf[i] = float(col[i]);
+                CK(cudaMemcpy(which == 0 ? B.y32[0][a] : B.u32[0][a], colf.data(), n * sizeof(float),
+                              cudaMemcpyHostToDevice));
+            } else {
+                CK(cudaMemcpy(which == 0 ? B.y64[0][a] : B.u64[0][a], col.data(), n * sizeof(double),
+                              cudaMemcpyHostToDevice));
+            }
+        }
+    }
+    return PICGPU_OK;
+}
+
+picgpu_status picgpu_count_particles(picgpu_ctx* c, int species, size_t* n) {
+    if (!c || !n || species < 0 || species >= c->cfg.n_species) return PICGPU_INVALID_ARG;
+    *n = size_t(c->sp[species].n);
+    return PICGPU_OK;
+}
+
+picgpu_status picgpu_get_particles(picgpu_ctx* c, int species, size_t cap, int32_t* tet, double* bary,
+                                   double* U, size_t* nout) {
+    if (!c || !nout || species < 0 || species >= c->cfg.n_species) return PICGPU_INVALID_ARG;
+    CK(cudaStreamSynchronize(c->stream));
+    SpeciesBuf& B = c->sp[species];
+    const size_t n = size_t(B.n);
+    std::vector<int32_t> t(n);
+    CK(cudaMemcpy(t.data(), B.tet[B.cur], n * sizeof(int32_t), cudaMemcpyDeviceToHost));
+    size_t alive = 0;
+    for (size_t i = 0; i < n; ++i) alive += t[i] >= 0;
+    *nout = alive;
+    if (!tet) return PICGPU_OK;
+    if (cap < alive || !bary || !U) return PICGPU_INVALID_ARG;
+    std::vector<double> col[6];
+    for (int k = 0; k < 6; ++k) {
+        col[k].resize(n);
+        const int a = k % 3;
+        if (c->mixed) {
+            std::vector<float> f(n);
+            CK(cudaMemcpy(f.data(), k < 3 ? B.y32[B.cur][a] : B.u32[B.cur][a], n * sizeof(float),
+                          cudaMemcpyDeviceToHost));
+            for (size_t i = 0; i < n; ++i) col[k][i] = f[i];
+        } else {
+            CK(cudaMemcpy(col[k].data(), k < 3 ? B.y64[B.cur][a] : B.u64[B.cur][a], n * sizeof(double),
+                          cudaMemcpyDeviceToHost));
+        }
+    }
+    size_t w = 0;
+    for (size_t i = 0; i < n; ++i) {
+        if (t[i] < 0) continue;
+        tet[w] = t[i];
+        for (int a = 0; a < 3; ++a) {
+            bary[3 * w + a] = col[a][i];
+            U[3 * w + a] = col[3 + a][i];
+        }
+        ++w;
+    }
+    return PICGPU_OK;
+}
+
+picgpu_status picgpu_initialise_fields(picgpu_ctx* c) {
+    if (!c) return PICGPU_INVALID_ARG;
+    picgpu_status s;
+    if ((s = zero_accumulators(c))) return s;
+    if ((s = move_species(c, true))) return s;
+    if ((s = charge_update(c))) return s;
+    if ((s = solve_fields(c, nullptr))) return s;
+    CK(cudaStreamSynchronize(c->stream));
+    if (c->profiling) harvest_events(c);
+    return PICGPU_OK;
+}
+
+picgpu_status picgpu_step(picgpu_ctx* c, int nsteps, picgpu_step_stats* stats) {
+    if (!c || nsteps < 0) return PICGPU_INVALID_ARG;
+    if (stats) std::memset(stats, 0, sizeof *stats);
+    for (int k = 0; k < nsteps; ++k) {
+        picgpu_status s = one_step(c, stats, true);
+        if (s) return s;
+    }
+    if (c->profiling) harvest_events(c);
+    fill_counts(c, stats);
+    if (stats) {
+        std::vector<double> sg(c->m.patches.size());
+        CK(cudaMemcpy(sg.data(), c->sigma, sg.size() * sizeof(double), cudaMemcpyDeviceToHost));
+        for (size_t p = 0; p < sg.size() && p < PICGPU_MAX_BOXES + 6; ++p)
+            stats->floating_charge[p] = sg[p] * c->m.patches[p].area;
+    }
+    return PICGPU_OK;
+}
+
+picgpu_status picgpu_move(picgpu_ctx* c, picgpu_step_stats* stats) {
+    if (!c) return PICGPU_INVALID_ARG;
+    if (stats) std::memset(stats, 0, sizeof *stats);
+    picgpu_status s = one_step(c, stats, false);
+    if (s) return s;
+    CK(cudaStreamSynchronize(c->stream));
+    if (c->profiling) harvest_events(c);
+    fill_counts(c, stats);
+    return PICGPU_OK;
+}
+
+picgpu_status picgpu_solve_poisson(picgpu_ctx* c, const double* rho, double* phi_inout,
+                                   picgpu_step_stats* stats) {
+    if (!c || !rho || !phi_inout) return PICGPU_INVALID_ARG;
+    if (stats) std::memset(stats, 0, sizeof *stats);
+    const size_t n = c->m.n_cells;
+    CK(cudaMemcpyAsync(c->rho, rho, n * sizeof(double), cudaMemcpyHostToDevice, c->stream));
+    CK(cudaMemcpyAsync(c->phi, phi_inout, n * sizeof(double), cudaMemcpyHostToDevice, c->stream));
+    picgpu_status s = poisson(c, stats);
+    CK(cudaMemcpyAsync(phi_inout, c->phi, n * sizeof(double), cudaMemcpyDeviceToHost, c->stream));
+    CK(cudaStreamSynchronize(c->stream));
+    if (c->profiling) harvest_events(c);
+    return s;
+}
+
+picgpu_status picgpu_get_field(picgpu_ctx* c, int which, double* out, size_t n) {
+    if (!c || !out) return PICGPU_INVALID_ARG;
+    const double* src = nullptr;
+    size_t cnt = 0;
+    switch (which) {
+        case PICGPU_FIELD_PHI: src = c->phi; cnt = c->m.n_cells; break;
+        case PICGPU_FIELD_E_CELL: src = c->E; cnt = 3 * size_t(c->m.n_cells); break;
+        case PICGPU_FIELD_RHO: src = c->rho; cnt = c->m.n_cells; break;
+        case PICGPU_FIELD_E_POINT: src = c->Ept; cnt = 3 * size_t(c->m.n_points); break;
+        case PICGPU_FIELD_SIGMA_V_MAX:
+            src = c->coll.svmax;
+            cnt = c->m.n_cells;
+            if (!src) return bad(c, PICGPU_INVALID_ARG, "no MCC state");
+            break;
+        default: return PICGPU_INVALID_ARG;
+    }
+    if (n < cnt) return bad(c, PICGPU_INVALID_ARG, "output buffer too small");
+    CK(cudaStreamSynchronize(c->stream));
+    CK(cudaMemcpy(out, src, cnt * sizeof(double), cudaMemcpyDeviceToHost));
+    return PICGPU_OK;
+}
+
+picgpu_status picgpu_set_field(picgpu_ctx* c, int which, const double* in, size_t n) {
+    if (!c || !in) return PICGPU_INVALID_ARG;
+    double* dst = nullptr;
+    size_t cnt = 0;
+    switch (which) {
+        case PICGPU_FIELD_PHI: dst = c->phi; cnt = c->m.n_cells; break;
+        case PICGPU_FIELD_E_CELL: dst = c->E; cnt = 3 * size_t(c->m.n_cells); break;
+        case PICGPU_FIELD_RHO: dst = c->rho; cnt = c->m.n_cells; break;
+        case PICGPU_FIELD_E_POINT: dst = c->Ept; cnt = 3 * size_t(c->m.n_points); break;
+        default: return PICGPU_INVALID_ARG;
+    }
+    if (n < cnt) return bad(c, PICGPU_INVALID_ARG, "input buffer too small");
+    CK(cudaStreamSynchronize(c->stream));
+    CK(cudaMemcpy(dst, in, cnt * sizeof(double), cudaMemcpyHostToDevice));
+    pgd::launch_to_float(c->E, c->E32, 3L * c->m.n_cells, c->stream);
+    pgd::launch_to_float(c->Ept, c->Ept32, 3L * c->m.n_points, c->stream);
+    c->launches += 2;
+    CK(cudaStreamSynchronize(c->stream));
+    return PICGPU_OK;
+}
+
+picgpu_status picgpu_diagnostics_compute(picgpu_ctx* c, picgpu_diagnostics* out) {
+    if (!c || !out) return PICGPU_INVALID_ARG;
+    std::memset(out, 0, sizeof *out);
+    CK(cudaMemsetAsync(c->diag, 0, 64 * sizeof(double), c->stream));
+    for (int s = 0; s < c->cfg.n_species; ++s) {
+        const SpeciesBuf& B = c->sp[s];
+        pgd::launch_diagnostics(B.tet[B.cur], c->mixed ? nullptr : B.u64[B.cur][0],
+                                c->mixed ? nullptr : B.u64[B.cur][1], c->mixed ? nullptr : B.u64[B.cur][2],
+                                B.u32[B.cur][0], B.u32[B.cur][1], B.u32[B.cur][2], int(B.n),
+                                c->cfg.species[s].mass, c->cfg.species[s].weight, c->diag + 10 * s, c->stream);
+        c->launches++;
+    }
+    pgd::launch_field_energy(c->E, c->dm.vol, c->m.n_cells, c->diag + 60, c->stream);
+    c->launches++;
+    double h[64];
+    CK(cudaMemcpyAsync(h, c->diag, sizeof h, cudaMemcpyDeviceToHost, c->stream));
+    CK(cudaStreamSynchronize(c->stream));
+    for (int s = 0; s < c->cfg.n_species; ++s) {
+        const double* v = h + 10 * s;
+        out->kinetic_energy[s] = v[0];
+        out->kinetic_energy_rel[s] = v[1];
+        for (int a = 0; a < 3; ++a) {
+            out->momentum[s][a] = v[2 + a];
+            out->velocity_sq[s][a] = v[5 + a];
+        }
+        out->weight_sum[s] = v[8];
+    }
+    const double eps0 = 1.0 / (kMu0 * kCl * kCl);
+    out->field_energy = 0.5 * eps0 * h[60];
+    return PICGPU_OK;
+}
+
+picgpu_status picgpu_set_profiling(picgpu_ctx* c, int enabled) {
+    if (!c) return PICGPU_INVALID_ARG;
+    c->profiling = enabled != 0;
+    return PICGPU_OK;
+}
+
+picgpu_status picgpu_phase_times(picgpu_ctx* c, double* ms, int64_t* launches, int nphase, int reset) {
+    if (!c) return PICGPU_INVALID_ARG;
+    CK(cudaStreamSynchronize(c->stream));
+    harvest_events(c);
+    for (int i = 0; i < nphase && i < PICGPU_PHASE_COUNT; ++i) {
+        if (ms) ms[i] = c->phase_ms[i];
+        if (launches) launches[i] = c->phase_launches[i];
+    }
+    if (reset)
+        for (int i = 0; i < PICGPU_PHASE_COUNT; ++i) { c->phase_ms[i] = 0; c->phase_launches[i] = 0; }
+    return PICGPU_OK;
+}
+
+int64_t picgpu_kernel_launches(const picgpu_ctx* c) { return c ? c->launches : 0; }
+
+picgpu_status picgpu_synchronize(picgpu_ctx* c) {
+    if (!c) return PICGPU_INVALID_ARG;
+    CK(cudaStreamSynchronize(c->stream));
+    return PICGPU_OK;
+}
+
+picgpu_status picgpu_timer_start(picgpu_ctx* c) {
+    if (!c) return PICGPU_INVALID_ARG;
+    if (!c->timer[0]) {
+        CK(cudaEventCreate(&c->timer[0]));
+        CK(cudaEventCreate(&c->timer[1]));
+    }
+    CK(cudaEventRecord(c->timer[0], c->stream));
+    return PICGPU_OK;
+}
+
+picgpu_status picgpu_timer_stop(picgpu_ctx* c, double* ms) {
+    if (!c || !ms || !c->timer[0]) return PICGPU_INVALID_ARG;
+    CK(cudaEventRecord(c->timer[1], c->stream));
+    CK(cudaEventSynchronize(c->timer[1]));
+    float f = 0.f;
+    CK(cudaEventElapsedTime(&f, c->timer[0], c->timer[1]));
+    *ms = f;
+    return PICGPU_OK;
+}
+
+}  // extern "C"

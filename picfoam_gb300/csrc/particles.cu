@@ -1,0 +1,132 @@
+// particles.cu -- particle store maintenance: stable removal of absorbed
+// particles (the parcels Cloud::move deletes when keepParticle is false,
+// PICParcel.C:70) from the structure-of-arrays store.
+#include "particles.h"
+
+namespace pgd {
+
+namespace {
+
+constexpr int kItems = 4;
+constexpr int kBlock = 256;
+constexpr int kTile = kItems * kBlock;  // 1024 particles per block
+
+__global__ void count_alive_kernel(const int32_t* __restrict__ tet, long n, int* __restrict__ counts) {
+    __shared__ int ws[kBlock / 32];
+    const long base = long(blockIdx.x) * kTile + long(threadIdx.x) * kItems;
+    int c = 0;
+#pragma unroll
+    for (int k = 0; k < kItems; ++k)
+        if (base + k < n && tet[base + k] >= 0) ++c;
+    for (int off = 16; off >= 1; off >>= 1) c += __shfl_xor_sync(0xffffffffu, c, off);
+    if ((threadIdx.x & 31) == 0) ws[threadIdx.x >> 5] = c;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        int t = 0;
+        for (int w = 0; w < kBlock / 32; ++w) t += ws[w];
+        counts[blockIdx.x] = t;
+    }
+}
+
+// Exclusive scan of counts[0..n) in place; counts[n] receives the total.
+__global__ void scan_single_kernel(int* counts, long n) {
+    __shared__ int ws[32];
+    __shared__ long long carry_s;
+    if (threadIdx.x == 0) carry_s = 0;
+    __syncthreads();
+    for (long base = 0; base < n; base += blockDim.x) {
+        const long i = base + threadIdx.x;
+        const int v = i < n ? counts[i] : 0;
+        int x = v;
+        const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+        for (int off = 1; off < 32; off <<= 1) {
+            const int y = __shfl_up_sync(0xffffffffu, x, off);
+            if (lane >= off) x += y;
+        }
+        if (lane == 31) ws[warp] = x;
+        __syncthreads();
+        if (warp == 0) {
+            int w = lane < int(blockDim.x >> 5) ? ws[lane] : 0;
+            for (int off = 1; off < 32; off <<= 1) {
+                const int y = __shfl_up_sync(0xffffffffu, w, off);
+                if (lane >= off) w += y;
+            }
+            ws[lane] = w;
+        }
+        __syncthreads();
+        const int incl = x + (warp > 0 ? ws[warp - 1] : 0);
+        const long long carry = carry_s;
+        if (i < n) counts[i] = int(carry + incl - v);
+        __syncthreads();
+        if (threadIdx.x == blockDim.x - 1) carry_s = carry + incl;
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) counts[n] = int(carry_s);
+}
+
+template <class R>
+__global__ void scatter_kernel(const int32_t* __restrict__ tet, const R* __restrict__ y0,
+                               const R* __restrict__ y1, const R* __restrict__ y2, const R* __restrict__ u0,
+                               const R* __restrict__ u1, const R* __restrict__ u2, int32_t* __restrict__ otet,
+                               R* __restrict__ oy0, R* __restrict__ oy1, R* __restrict__ oy2,
+                               R* __restrict__ ou0, R* __restrict__ ou1, R* __restrict__ ou2, long n,
+                               const int* __restrict__ offsets) {
+    __shared__ int ws[kBlock / 32];
+    const long base = long(blockIdx.x) * kTile + long(threadIdx.x) * kItems;
+    bool f[kItems];
+    int c = 0;
+#pragma unroll
+    for (int k = 0; k < kItems; ++k) {
+        f[k] = base + k < n && tet[base + k] >= 0;
+        c += f[k];
+    }
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    int x = c;
+    for (int off = 1; off < 32; off <<= 1) {
+        const int y = __shfl_up_sync(0xffffffffu, x, off);
+        if (lane >= off) x += y;
+    }
+    if (lane == 31) ws[warp] = x;
+    __syncthreads();
+    int woff = 0;
+    for (int w = 0; w < warp; ++w) woff += ws[w];
+    long pos = long(offsets[blockIdx.x]) + woff + x - c;
+#pragma unroll
+    for (int k = 0; k < kItems; ++k) {
+        if (!f[k]) continue;
+        const long i = base + k;
+        otet[pos] = tet[i];
+        oy0[pos] = y0[i]; oy1[pos] = y1[i]; oy2[pos] = y2[i];
+        ou0[pos] = u0[i]; ou1[pos] = u1[i]; ou2[pos] = u2[i];
+        ++pos;
+    }
+}
+
+}  // namespace
+
+long compact_blocks(long n) { return (n + kTile - 1) / kTile; }
+
+cudaError_t compact_species(const DSpecies& src, const DSpecies& dst, long n, bool mixed, int* scan,
+                            long* kept, cudaStream_t s) {
+    const long nblk = compact_blocks(n);
+    if (nblk == 0) { *kept = 0; return cudaSuccess; }
+    count_alive_kernel<<<unsigned(nblk), kBlock, 0, s>>>(src.tet, n, scan);
+    scan_single_kernel<<<1, 1024, 0, s>>>(scan, nblk);
+    if (mixed)
+        scatter_kernel<float><<<unsigned(nblk), kBlock, 0, s>>>(
+            src.tet, src.y32[0], src.y32[1], src.y32[2], src.u32[0], src.u32[1], src.u32[2], dst.tet, dst.y32[0],
+            dst.y32[1], dst.y32[2], dst.u32[0], dst.u32[1], dst.u32[2], n, scan);
+    else
+        scatter_kernel<double><<<unsigned(nblk), kBlock, 0, s>>>(
+            src.tet, src.y64[0], src.y64[1], src.y64[2], src.u64[0], src.u64[1], src.u64[2], dst.tet, dst.y64[0],
+            dst.y64[1], dst.y64[2], dst.u64[0], dst.u64[1], dst.u64[2], n, scan);
+    int total = 0;
+    cudaError_t e = cudaMemcpyAsync(&total, scan + nblk, sizeof(int), cudaMemcpyDeviceToHost, s);
+    if (e != cudaSuccess) return e;
+    e = cudaStreamSynchronize(s);
+    if (e != cudaSuccess) return e;
+    *kept = total;
+    return cudaGetLastError();
+}
+
+}  // namespace pgd

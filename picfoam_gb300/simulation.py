@@ -1,0 +1,248 @@
+"""Host-side mirror of the picFoam cloud interface over the picgpu C ABI.
+
+Simulation plays the role of PICCloud for the caller: it owns one device
+case (mesh, sub-models, particles, fields) and exposes the calls the picFoam
+time loop makes (evolve -> step, info -> diagnostics) plus field and
+particle access.  It talks to a backend: the CUDA library by default; the
+test suite plugs the CPU oracle in through the same interface.
+"""
+import ctypes as C
+
+import numpy as np
+
+from . import abi, native
+
+
+class PicError(RuntimeError):
+    def __init__(self, status, message):
+        super().__init__(f"{abi.STATUS_NAMES.get(status, status)}: {message}")
+        self.status = status
+
+
+class GpuBackend:
+    """libpicgpu.so (CUDA, sm_103a)."""
+    prefix = "picgpu_"
+    name = "gpu"
+
+    def __init__(self):
+        self.lib = native.load()
+
+    def create(self, mesh, cfg):
+        h = C.c_void_p()
+        st = self.lib.picgpu_create(C.byref(mesh), C.byref(cfg), C.byref(h))
+        return st, h
+
+
+def _f64(a):
+    a = np.ascontiguousarray(a, dtype=np.float64)
+    return a, a.ctypes.data_as(C.POINTER(C.c_double))
+
+
+def _i32(a):
+    a = np.ascontiguousarray(a, dtype=np.int32)
+    return a, a.ctypes.data_as(C.POINTER(C.c_int32))
+
+
+class Simulation:
+    def __init__(self, mesh, cfg, backend=None, keepalive=()):
+        self.backend = backend if backend is not None else GpuBackend()
+        self.lib = self.backend.lib
+        self.mesh_desc = mesh
+        self.cfg = cfg
+        self._keep = list(keepalive)
+        self._h = None
+        st, h = self.backend.create(mesh, cfg)
+        self._h = h
+        if st != abi.OK:
+            msg = self._err()
+            self.close()
+            raise PicError(st, msg)
+
+    # ---------------------------------------------------------------- util
+    def _fn(self, name):
+        return getattr(self.lib, self.backend.prefix + name)
+
+    def _err(self):
+        if not self._h:
+            return ""
+        e = self._fn("last_error")(self._h)
+        return e.decode() if e else ""
+
+    def _check(self, st):
+        if st != abi.OK:
+            raise PicError(st, self._err())
+
+    def close(self):
+        if self._h:
+            self._fn("destroy")(self._h)
+            self._h = None
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    # ----------------------------------------------------------- particles
+    def set_particles(self, species, tet, bary, U):
+        tet, tp = _i32(tet)
+        bary, bp = _f64(np.reshape(bary, (-1, 3)))
+        U, up = _f64(np.reshape(U, (-1, 3)))
+        n = tet.shape[0]
+        assert bary.shape[0] == n and U.shape[0] == n
+        self._check(self._fn("set_particles")(self._h, species, n, tp, bp, up))
+
+    def count(self, species):
+        n = C.c_size_t()
+        self._check(self._fn("count_particles")(self._h, species, C.byref(n)))
+        return n.value
+
+    def get_particles(self, species):
+        cap = self.count(species)
+        tet = np.zeros(cap, np.int32)
+        bary = np.zeros((cap, 3))
+        U = np.zeros((cap, 3))
+        n = C.c_size_t()
+        self._check(self._fn("get_particles")(
+            self._h, species, cap, tet.ctypes.data_as(C.POINTER(C.c_int32)),
+            bary.ctypes.data_as(C.POINTER(C.c_double)), U.ctypes.data_as(C.POINTER(C.c_double)),
+            C.byref(n)))
+        k = n.value
+        return tet[:k], bary[:k], U[:k]
+
+    # ---------------------------------------------------------------- step
+    def initialise_fields(self):
+        self._check(self._fn("initialise_fields")(self._h))
+
+    def step(self, n=1):
+        s = abi.StepStats()
+        self._check(self._fn("step")(self._h, n, C.byref(s)))
+        return s
+
+    def move(self):
+        s = abi.StepStats()
+        self._check(self._fn("move")(self._h, C.byref(s)))
+        return s
+
+    def solve_poisson(self, rho, phi0=None):
+        rho, rp = _f64(rho)
+        phi = np.zeros_like(rho) if phi0 is None else np.array(phi0, dtype=np.float64, copy=True)
+        s = abi.StepStats()
+        self._check(self._fn("solve_poisson")(self._h, rp, phi.ctypes.data_as(C.POINTER(C.c_double)),
+                                              C.byref(s)))
+        return phi, s
+
+    # -------------------------------------------------------------- fields
+    def _field_len(self, which, n_cells, n_points):
+        return {abi.FIELD_PHI: n_cells, abi.FIELD_E_CELL: 3 * n_cells, abi.FIELD_RHO: n_cells,
+                abi.FIELD_E_POINT: 3 * n_points, abi.FIELD_SIGMA_V_MAX: n_cells}[which]
+
+    def sizes(self):
+        """(n_cells, n_points) of the mesh."""
+        if hasattr(self.backend, "sizes"):
+            return self.backend.sizes(self._h)
+        info = abi.MeshInfo()
+        self._check(self.lib.picgpu_mesh_query(self._h, C.byref(info)))
+        return info.n_cells, info.n_points
+
+    def field(self, which):
+        nc, npnt = self.sizes()
+        n = self._field_len(which, nc, npnt)
+        out = np.zeros(n)
+        self._check(self._fn("get_field")(self._h, which, out.ctypes.data_as(C.POINTER(C.c_double)), n))
+        if which in (abi.FIELD_E_CELL, abi.FIELD_E_POINT):
+            out = out.reshape(-1, 3)
+        return out
+
+    def set_field(self, which, values):
+        v, vp = _f64(np.ravel(values))
+        self._check(self._fn("set_field")(self._h, which, vp, v.size))
+
+    def diagnostics(self):
+        d = abi.Diagnostics()
+        fn = self._fn("diagnostics") if hasattr(self.lib, self.backend.prefix + "diagnostics") \
+            else self._fn("diagnostics_compute")
+        self._check(fn(self._h, C.byref(d)))
+        return d
+
+    # ------------------------------------------------------------ profiling
+    def set_profiling(self, on=True):
+        self._check(self.lib.picgpu_set_profiling(self._h, 1 if on else 0))
+
+    def phase_times(self, reset=False):
+        ms = (C.c_double * abi.PHASE_COUNT)()
+        cnt = (C.c_int64 * abi.PHASE_COUNT)()
+        self._check(self.lib.picgpu_phase_times(self._h, ms, cnt, abi.PHASE_COUNT, 1 if reset else 0))
+        return {abi.PHASE_NAMES[i]: (ms[i], cnt[i]) for i in range(abi.PHASE_COUNT)}
+
+    def kernel_launches(self):
+        return int(self.lib.picgpu_kernel_launches(self._h))
+
+    def synchronize(self):
+        self._check(self.lib.picgpu_synchronize(self._h))
+
+    def timer_start(self):
+        self._check(self.lib.picgpu_timer_start(self._h))
+
+    def timer_stop(self):
+        ms = C.c_double()
+        self._check(self.lib.picgpu_timer_stop(self._h, C.byref(ms)))
+        return ms.value
+
+
+class Mesh:
+    """Host-only mesh handle (tet decomposition, locate, positions); no GPU needed."""
+
+    def __init__(self, desc):
+        self.lib = native.load()
+        self._h = C.c_void_p()
+        st = self.lib.picgpu_mesh_create(C.byref(desc), C.byref(self._h))
+        if st != abi.OK:
+            raise PicError(st, "invalid mesh description")
+        info = abi.MeshInfo()
+        self.lib.picgpu_mesh_info_get(self._h, C.byref(info))
+        self.n_cells = info.n_cells
+        self.n_points = info.n_points
+
+    def close(self):
+        if self._h:
+            self.lib.picgpu_mesh_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def locate(self, xyz):
+        xyz, xp = _f64(np.reshape(xyz, (-1, 3)))
+        n = xyz.shape[0]
+        tet = np.zeros(n, np.int32)
+        bary = np.zeros((n, 3))
+        self.lib.picgpu_mesh_locate(self._h, n, xp, tet.ctypes.data_as(C.POINTER(C.c_int32)),
+                                    bary.ctypes.data_as(C.POINTER(C.c_double)))
+        return tet, bary
+
+    def position(self, tet, bary):
+        tet, tp = _i32(tet)
+        bary, bp = _f64(np.reshape(bary, (-1, 3)))
+        out = np.zeros((tet.shape[0], 3))
+        st = self.lib.picgpu_mesh_position(self._h, tet.shape[0], tp, bp,
+                                           out.ctypes.data_as(C.POINTER(C.c_double)))
+        if st != abi.OK:
+            raise PicError(st, "tet index out of range")
+        return out
+
+    def cells(self):
+        cc = np.zeros((self.n_cells, 3))
+        vol = np.zeros(self.n_cells)
+        self.lib.picgpu_mesh_cells(self._h, cc.ctypes.data_as(C.POINTER(C.c_double)),
+                                   vol.ctypes.data_as(C.POINTER(C.c_double)))
+        return cc, vol

@@ -1,0 +1,141 @@
+"""Parity of the CUDA path against the CPU oracle (through the C ABI).
+
+FP64 form with the 64-bit fixed-point deposit: particle records, charge
+density, potential and field are compared bit for bit over many steps.
+FP64 atomics: within 1e-10 relative.  Mixed FP32 form: within the stated
+tolerances of the FP64 oracle.
+"""
+import numpy as np
+import pytest
+
+from picfoam_gb300 import abi, cases
+from picfoam_gb300.simulation import Mesh
+
+pytestmark = pytest.mark.gpu
+
+
+def pair(case, gpu, oracle_backend, nthreads=1):
+    g = cases.build(case, backend=gpu)
+    o = cases.build(case, backend=oracle_backend.OracleBackend(nthreads))
+    return g, o
+
+
+def assert_particles_equal(g, o, n_species, exact=True, rtol=0.0, atol_u=0.0):
+    for s in range(n_species):
+        tg, bg, ug = g.get_particles(s)
+        to, bo, uo = o.get_particles(s)
+        assert tg.shape == to.shape, f"species {s}: {tg.shape} vs {to.shape}"
+        if exact:
+            np.testing.assert_array_equal(tg, to)
+            np.testing.assert_array_equal(bg, bo)
+            np.testing.assert_array_equal(ug, uo)
+        else:
+            np.testing.assert_array_equal(tg, to)
+            np.testing.assert_allclose(bg, bo, rtol=0, atol=rtol)
+            np.testing.assert_allclose(ug, uo, rtol=rtol, atol=atol_u)
+
+
+def assert_fields_equal(g, o):
+    for f in (abi.FIELD_RHO, abi.FIELD_PHI, abi.FIELD_E_CELL, abi.FIELD_E_POINT):
+        np.testing.assert_array_equal(g.field(f), o.field(f), err_msg=f"field {f}")
+
+
+def test_plasma_oscillation_fp64_bit_exact(gpu, oracle_backend):
+    case = cases.plasma_oscillation_1d(Mesh, n_cells=32, per_cell=40, deposit=abi.DEPOSIT_FIXED_POINT)
+    g, o = pair(case, gpu, oracle_backend)
+    g.initialise_fields()
+    o.initialise_fields()
+    assert_fields_equal(g, o)
+    for _ in range(5):
+        sg = g.step(4)
+        so = o.step(4)
+        assert sg.tet_steps == so.tet_steps and sg.face_crossings == so.face_crossings
+        assert sg.pcg_iterations == so.pcg_iterations
+        assert_particles_equal(g, o, 1)
+        assert_fields_equal(g, o)
+
+
+@pytest.mark.parametrize("pusher", [abi.PUSHER_BORIS, abi.PUSHER_BORIS_NR, abi.PUSHER_VAY,
+                                    abi.PUSHER_HIGUERA_CARY])
+def test_two_species_walls_fp64_bit_exact(gpu, oracle_backend, pusher):
+    case = cases.two_species_3d(n_cells=8, per_cell=12, precision=abi.PREC_FP64, pusher=pusher,
+                                deposit=abi.DEPOSIT_FIXED_POINT, dt_factor=0.5, L=0.004)
+    g, o = pair(case, gpu, oracle_backend)
+    g.initialise_fields()
+    o.initialise_fields()
+    assert_fields_equal(g, o)
+    tot_abs = 0
+    for _ in range(4):
+        sg = g.step(3)
+        so = o.step(3)
+        assert list(sg.n_absorbed) == list(so.n_absorbed)
+        assert sg.tet_steps == so.tet_steps and sg.face_crossings == so.face_crossings
+        tot_abs += sum(sg.n_absorbed)
+        assert_particles_equal(g, o, 2)
+        assert_fields_equal(g, o)
+    assert tot_abs > 0, "the case must exercise the absorbing walls"
+
+
+def test_atomic_deposit_within_1e10(gpu, oracle_backend):
+    case = cases.two_species_3d(n_cells=8, per_cell=20, precision=abi.PREC_FP64,
+                                deposit=abi.DEPOSIT_ATOMIC_FP64, L=0.004)
+    g, o = pair(case, gpu, oracle_backend)
+    g.initialise_fields()
+    o.initialise_fields()
+    rg, ro = g.field(abi.FIELD_RHO), o.field(abi.FIELD_RHO)
+    np.testing.assert_allclose(rg, ro, rtol=1e-10, atol=1e-10 * np.abs(ro).max())
+    g.move()
+    o.move()
+    assert_particles_equal(g, o, 2)
+    rg, ro = g.field(abi.FIELD_RHO), o.field(abi.FIELD_RHO)
+    np.testing.assert_allclose(rg, ro, rtol=1e-10, atol=1e-10 * np.abs(ro).max())
+
+
+def test_poisson_bit_exact(gpu, oracle_backend):
+    case = cases.electrode_box(n_cells=32, per_cell=1, precision=abi.PREC_FP64, pcg_tol=1e-10)
+    g, o = pair(case, gpu, oracle_backend)
+    rng = np.random.default_rng(3)
+    n_cells = g.sizes()[0]
+    rho = rng.standard_normal(n_cells) * 1e-6
+    pg, sg = g.solve_poisson(rho)
+    po, so = o.solve_poisson(rho)
+    assert sg.pcg_iterations == so.pcg_iterations > 0
+    np.testing.assert_array_equal(pg, po)
+    np.testing.assert_array_equal(g.field(abi.FIELD_E_POINT), o.field(abi.FIELD_E_POINT))
+    assert so.pcg_residual_l2 <= 1e-10
+
+
+def test_floating_electrodes_fp64_bit_exact(gpu, oracle_backend):
+    case = cases.electrode_box(n_cells=16, per_cell=6, precision=abi.PREC_FP64, dt_factor=0.5, L=0.004)
+    case.cfg.deposit_mode = abi.DEPOSIT_FIXED_POINT
+    g, o = pair(case, gpu, oracle_backend)
+    g.initialise_fields()
+    o.initialise_fields()
+    for _ in range(3):
+        sg = g.step(3)
+        so = o.step(3)
+        assert_particles_equal(g, o, 2)
+        assert_fields_equal(g, o)
+    np.testing.assert_allclose(list(sg.floating_charge), list(so.floating_charge), rtol=1e-12)
+
+
+def test_mixed_precision_against_fp64_oracle(gpu, oracle_backend):
+    case = cases.two_species_3d(n_cells=8, per_cell=20, precision=abi.PREC_MIXED, L=0.004)
+    g = cases.build(case, backend=gpu)
+    case.cfg.precision = abi.PREC_FP64
+    o = cases.build(case, backend=oracle_backend.OracleBackend(1))
+    g.initialise_fields()
+    o.initialise_fields()
+    g.move()
+    o.move()
+    # the FP32 particle store: coordinates to ~1e-6 of a cell, velocities to 1e-5 relative
+    tg, bg, ug = g.get_particles(0)
+    to, bo, uo = o.get_particles(0)
+    assert abs(len(tg) - len(to)) <= max(2, len(to) // 1000)
+    if len(tg) == len(to):
+        same = tg == to
+        assert same.mean() > 0.999
+        np.testing.assert_allclose(bg[same], bo[same], atol=2e-5)
+        np.testing.assert_allclose(ug[same], uo[same], rtol=2e-5, atol=2e-5 * np.abs(uo).max())
+    rg, ro = g.field(abi.FIELD_RHO), o.field(abi.FIELD_RHO)
+    assert np.abs(rg - ro).max() <= 1e-3 * np.abs(ro).max()
