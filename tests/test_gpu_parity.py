@@ -86,7 +86,9 @@ def test_atomic_deposit_within_1e10(gpu, oracle_backend):
     np.testing.assert_allclose(rg, ro, rtol=1e-10, atol=1e-10 * np.abs(ro).max())
     g.move()
     o.move()
-    assert_particles_equal(g, o, 2)
+    # the potential differs in the last bits (summation order of the
+    # deposit), so positions and velocities agree to 1e-10 relative
+    assert_particles_equal(g, o, 2, exact=False, rtol=1e-10, atol_u=1e-10 * 6e5)
     rg, ro = g.field(abi.FIELD_RHO), o.field(abi.FIELD_RHO)
     np.testing.assert_allclose(rg, ro, rtol=1e-10, atol=1e-10 * np.abs(ro).max())
 
