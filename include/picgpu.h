@@ -318,6 +318,38 @@ picgpu_status picgpu_synchronize(picgpu_ctx* ctx);
 picgpu_status picgpu_timer_start(picgpu_ctx* ctx);
 picgpu_status picgpu_timer_stop(picgpu_ctx* ctx, double* ms);
 
+/* Allocation-free PCG solve.  This entry point has no counterpart in picFoam.
+ *
+ * For callers that cannot call cudaMalloc -- a solver plugin hosted by a
+ * framework whose memory pool owns all device memory, or a time-critical
+ * loop where cudaMalloc's implicit device-wide synchronisation is not
+ * acceptable -- it solves M x = b with the same Jacobi-preconditioned PCG
+ * kernels as picgpu_solve_poisson, without allocating anything.  All
+ * pointers are DEVICE pointers owned by the caller:
+ *   diag[n_cells]   M's diagonal (positive: M is -laplacian, SPD)
+ *   off[6*n_cells]  M's off-diagonal coefficient per cell face (-|S|/|d|)
+ *   nbr[6*n_cells]  neighbour cell per face, or -1 where there is none
+ *   b[n_cells]      right-hand side
+ *   x[n_cells]      initial guess in, solution out
+ * Stops when ||b - M x||2 <= tol ||b||2 or after max_iter iterations;
+ * iterations and residual (relative L2) are written to host memory.
+ * Work runs on `stream` (a cudaStream_t; NULL = default stream) of the
+ * current device and the call returns when it has finished.
+ *
+ * Limit: n_cells <= PICGPU_NOALLOC_MAX_CELLS; larger problems are rejected
+ * with PICGPU_CAPACITY.  The working vectors live in a fixed __device__
+ * array (about 3.2 MB) that every device using the library holds until the
+ * process exits.  The first call on a device looks up that array's device
+ * address; make that first call before any stream capture.  All calls on a
+ * device share the array, so calls whose GPU work overlaps race: serialise
+ * them.  Status: PICGPU_OK, PICGPU_INVALID_ARG, PICGPU_CAPACITY,
+ * PICGPU_PCG_NOT_CONVERGED or PICGPU_CUDA_ERROR. */
+#define PICGPU_NOALLOC_MAX_CELLS 65536
+picgpu_status picgpu_solve_ldu_noalloc(int n_cells, const double* diag, const double* off,
+                                       const int32_t* nbr, const double* b, double* x,
+                                       double tol, int max_iter, int* iterations,
+                                       double* residual, void* stream);
+
 #ifdef __cplusplus
 }
 #endif

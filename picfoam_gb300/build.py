@@ -30,6 +30,7 @@ UNITS = {
     "particles.cu": [],
     "collide.cu": [],
     "library.cu": [],
+    "pcg_static.cu": ["--fmad=false"],
 }
 HEADERS = [os.path.join(SRC, f) for f in os.listdir(SRC) if f.endswith((".h", ".cuh", ".hpp"))] + [
     os.path.join(INCLUDE, "picgpu.h")]

@@ -86,5 +86,8 @@ def load():
     lib.picgpu_timer_start.argtypes = [P]
     lib.picgpu_timer_stop.restype = i
     lib.picgpu_timer_stop.argtypes = [P, F64P]
+    lib.picgpu_solve_ldu_noalloc.restype = i
+    lib.picgpu_solve_ldu_noalloc.argtypes = [i, P, P, P, P, P, C.c_double, i, C.POINTER(C.c_int),
+                                             F64P, P]
     _lib = lib
     return lib
