@@ -63,7 +63,7 @@ struct Parcel {
 };
 
 // Deterministic reduction: the fixed order the CUDA kernels reduce in
-// (256 threads, 8 strided items per thread, warp xor-tree, 8-warp tree).
+// (256 threads, 2 strided items per thread, warp xor-tree, 8-warp tree).
 double tree_block(const double* acc /*256*/) {
     double w[8];
     for (int wi = 0; wi < 8; ++wi) {
@@ -80,14 +80,15 @@ double tree_block(const double* acc /*256*/) {
 
 template <class F>
 double det_sum(long n, F term) {
-    const long chunk = 2048;
+    const int items = 2;
+    const long chunk = 256 * items;
     const long nb = (n + chunk - 1) / chunk;
     std::vector<double> part(std::max<long>(nb, 1), 0.0);
     double acc[256];
     for (long b = 0; b < nb; ++b) {
         for (int t = 0; t < 256; ++t) {
             double s = 0.0;
-            for (int j = 0; j < 8; ++j) {
+            for (int j = 0; j < items; ++j) {
                 const long i = b * chunk + long(j) * 256 + t;
                 if (i < n) s = s + term(i);
             }

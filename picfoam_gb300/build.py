@@ -25,7 +25,7 @@ COMMON = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC,-ffp-contract=o
 # translation unit -> extra flags
 UNITS = {
     "move_fp64.cu": ["--fmad=false"],
-    "move_fp32.cu": [],
+    "move_fp32.cu": ["--use_fast_math"],
     "fields.cu": ["--fmad=false"],
     "particles.cu": [],
     "collide.cu": [],

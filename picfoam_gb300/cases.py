@@ -119,9 +119,10 @@ def maxwellian(rng, n, T_eV, mass):
 def plasma_oscillation_1d(mesh_api, n_cells=128, per_cell=200, seed=1234, dt_factor=0.05,
                           perturbation=0.01, precision=abi.PREC_FP64,
                           deposit=abi.DEPOSIT_ATOMIC_FP64, pusher=abi.PUSHER_BORIS, pcg_tol=1e-10,
-                          T_eV=1.0, n_e=1e14):
+                          T_eV=1.0, n_e=1e14, quiet=False):
     """Periodic 0.1 m box, n_cells x 1 x 1 hexes (thickness = dx, empty y/z),
-    electrons over an immobile neutralising background (spaceCharge)."""
+    electrons over an immobile neutralising background (spaceCharge).
+    quiet=True places the electrons evenly (a quiet start)."""
     L = 0.1
     dx = L / n_cells
     sides = [patch(abi.PATCH_CYCLIC), patch(abi.PATCH_CYCLIC),
@@ -136,7 +137,7 @@ def plasma_oscillation_1d(mesh_api, n_cells=128, per_cell=200, seed=1234, dt_fac
                       deposit=deposit, pcg_tol=pcg_tol, seed=seed)
     cfg.space_charge = E_CHARGE * n_e
     rng = np.random.Generator(np.random.Philox(seed))
-    x = rng.random(N) * L
+    x = (np.arange(N) + 0.5) * (L / N) if quiet else rng.random(N) * L
     xyz = np.stack([x, np.full(N, 0.5 * dx), np.full(N, 0.5 * dx)], axis=1)
     m = mesh_api(mesh)
     tet, bary = m.locate(xyz)
@@ -172,23 +173,28 @@ def two_species_3d(n_cells=64, per_cell=50, seed=1234, precision=abi.PREC_MIXED,
                 dict(wpe=wpe, dt=dt, n=n, N=2 * N, weight=w, n_cells=n_c))
 
 
-def magnetic_rotation(pusher=abi.PUSHER_HIGUERA_CARY, precision=abi.PREC_FP64, beta=0.1, B=1.0,
-                      steps_per_orbit=200, n_cells=40):
-    """Single electron gyrating in B_z (tutorial magneticRotation): 40x1x40
-    cells, empty y, MaxwellSolver none.  Returns the case and the expected
+def magnetic_rotation(mesh_api, pusher=abi.PUSHER_HIGUERA_CARY, precision=abi.PREC_FP64, beta=0.1, B=1.0,
+                      steps_per_orbit=200, n_cells=40, E=(0.0, 0.0, 0.0)):
+    """Single electron gyrating in B_z (tutorial magneticRotation: 0.4 mm
+    square, 40 x 40 cells, one cell thick and empty along the field, electron
+    at (0, -r, 0) with v = 0.1 c along x, MaxwellSolver none).  meta holds the
     gyration radius gamma m v / (e B)."""
-    L = 2e-3
-    sides = [patch(abi.PATCH_ABSORB), patch(abi.PATCH_ABSORB), patch(abi.PATCH_EMPTY),
-             patch(abi.PATCH_EMPTY), patch(abi.PATCH_ABSORB), patch(abi.PATCH_ABSORB)]
-    mesh = block_mesh((n_cells, 1, n_cells), (L, L / n_cells, L), sides)
+    L = 4e-4
+    sides = [patch(abi.PATCH_ABSORB), patch(abi.PATCH_ABSORB), patch(abi.PATCH_ABSORB),
+             patch(abi.PATCH_ABSORB), patch(abi.PATCH_EMPTY), patch(abi.PATCH_EMPTY)]
+    mesh = block_mesh((n_cells, n_cells, 1), (L, L, L / n_cells), sides,
+                      origin=(-L / 2, -L / 2, -L / (2 * n_cells)))
     v = beta * C_LIGHT
     gamma = 1.0 / math.sqrt(1.0 - beta * beta)
     r = gamma * M_E * v / (E_CHARGE * B)
     wc = E_CHARGE * B / (gamma * M_E)
     dt = 2 * math.pi / wc / steps_per_orbit
     cfg = base_config(dt, [(M_E, -E_CHARGE, 1.0, True)], pusher=pusher, precision=precision,
-                      maxwell=abi.MAXWELL_NONE, B=(0.0, 0.0, B))
-    return Case("magnetic_rotation", mesh, cfg, {}, [],
+                      maxwell=abi.MAXWELL_NONE, B=(0.0, 0.0, B), E_applied=E)
+    m = mesh_api(mesh)
+    tet, bary = m.locate(np.array([[0.0, -r, 0.0]]))
+    U = np.array([[v, 0.0, 0.0]])
+    return Case("magnetic_rotation", mesh, cfg, {0: (tet, bary, U)}, [],
                 dict(radius=r, v=v, gamma=gamma, wc=wc, dt=dt, L=L))
 
 

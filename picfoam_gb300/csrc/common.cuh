@@ -40,6 +40,7 @@ struct DMesh {
     const int* nbr;          // 6 n_cells
     const int* cell_pt;      // 8 n_cells (cyclic-merged points)
     const double* cc;        // 3 n_cells
+    const float* cc32;       // 3 n_cells
     const double* vol;       // n_cells
     const double* tetinv;    // 108 per class
     const float* tetinv32;   // 108 per class
@@ -100,6 +101,16 @@ struct MoveParams {
     double dt;
     double B[3];
     double fix_scale;
+    // FP32 form: the same constants pre-rounded on the host, so the kernel
+    // never converts a double (GB300 issues FP64 at a small fraction of FP32)
+    int charged;             // q != 0
+    int has_value;           // q * weight != 0
+    float qm_f;              // q / m
+    float dt_f;
+    float B_f[3];
+    float centre_f[3];
+    unsigned long long* acc_cc;   // this species' fixed-point (2^-30) deposit, cells
+    unsigned long long* acc_vtx;  // ... and points
     const double* E;         // 3 n_cells
     const double* Ept;       // 3 n_points
     const float* E32;

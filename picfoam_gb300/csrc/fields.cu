@@ -1,7 +1,7 @@
 // fields.cu -- charge density, electrostatic Poisson PCG and the E field.
 //
 // Built with --fmad=false: each kernel evaluates in the order of the CPU
-// oracle, and every reduction runs in one fixed tree order (256 threads, 8
+// oracle, and every reduction runs in one fixed tree order (256 threads, 2
 // strided items per thread, warp xor-tree, 8-warp tree; the last block of a
 // launch combines the block partials in the same order), so the FP64 Poisson
 // solve is bit-reproducible and matches the oracle bit for bit.
@@ -89,6 +89,33 @@ __global__ void charge_update_kernel(DMesh m, int volume_weighting, int fixed, d
     rho[c] = r + space_charge;
 }
 
+// Charge update of the FP32 form: per-species fixed-point weights times q w.
+__global__ void charge_update_mixed_kernel(DMesh m, int volume_weighting, SpeciesValues sv,
+                                           const unsigned long long* __restrict__ acc, double space_charge,
+                                           double* __restrict__ rho) {
+    const int c = blockIdx.x * blockDim.x + threadIdx.x;
+    if (c >= m.n_cells) return;
+    const size_t stride = size_t(m.n_cells) + size_t(m.n_points);
+    const double V = m.vol[c];
+    double ccv = 0.0;
+    for (int s = 0; s < sv.n; ++s) ccv += sv.v[s] * double(acc[s * stride + c]);
+    double r = ccv / V;
+    if (volume_weighting) {
+        for (int q = 0; q < 8; ++q) {
+            const size_t pt = size_t(m.n_cells) + m.cell_pt[8 * size_t(c) + q];
+            double vv = 0.0;
+            for (int s = 0; s < sv.n; ++s) vv += sv.v[s] * double(acc[s * stride + pt]);
+            r += (m.vw_weight[8 * size_t(c) + q] * vv) / V;
+        }
+    }
+    rho[c] = r + space_charge;
+}
+
+void launch_charge_update_mixed(const DMesh& m, int vw, const SpeciesValues& sv, const unsigned long long* acc,
+                                double space_charge, double* rho, cudaStream_t s) {
+    charge_update_mixed_kernel<<<(m.n_cells + 255) / 256, 256, 0, s>>>(m, vw, sv, acc, space_charge, rho);
+}
+
 // FloatingPotential::preUpdate_Boundary (FloatingPotential.C:89-100)
 __global__ void floating_update_kernel(double* qconv, double* sigma, double* grad_bc) {
     const int p = threadIdx.x;
@@ -119,9 +146,9 @@ __global__ void __launch_bounds__(256) sum_kernel(const double* __restrict__ v, 
                                                   double* part, PcgState* st) {
     __shared__ double ws[8];
     double s = 0.0;
-    const long base = long(blockIdx.x) * 2048 + threadIdx.x;
+    const long base = long(blockIdx.x) * kChunk + threadIdx.x;
 #pragma unroll
-    for (int j = 0; j < 8; ++j) {
+    for (int j = 0; j < kItems; ++j) {
         const long i = base + j * 256;
         if (i < n) s = s + v[i];
     }
@@ -156,9 +183,9 @@ __global__ void __launch_bounds__(256) pcg_init_kernel(DMesh m, const double* __
     const int n = m.n_cells;
     const int nb = gridDim.x;
     double srz = 0.0, srr = 0.0, sbb = 0.0;
-    const long base = long(blockIdx.x) * 2048 + threadIdx.x;
+    const long base = long(blockIdx.x) * kChunk + threadIdx.x;
 #pragma unroll
-    for (int j = 0; j < 8; ++j) {
+    for (int j = 0; j < kItems; ++j) {
         const long i = base + j * 256;
         if (i < n) {
             const double mx = apply_M(m, x, int(i));
@@ -189,6 +216,7 @@ __global__ void __launch_bounds__(256) pcg_init_kernel(DMesh m, const double* __
             st->bb = bb;
             st->lim = (tol * tol) * bb;
             st->iters = 0;
+            st->k = 0;
             st->done = rr <= st->lim ? 1 : 0;
             st->converged = st->done;
         }
@@ -201,15 +229,16 @@ __global__ void __launch_bounds__(256) pcg_spmv_kernel(DMesh m, const double* __
                                                        const double* __restrict__ p_old,
                                                        double* __restrict__ p_new,
                                                        double* __restrict__ q, double* part,
-                                                       PcgState* st, int first) {
+                                                       PcgState* st) {
     if (st->done) return;
     __shared__ double ws[8];
     const int n = m.n_cells;
+    const int first = st->k == 0;
     const double beta = st->beta;
     double acc = 0.0;
-    const long base = long(blockIdx.x) * 2048 + threadIdx.x;
+    const long base = long(blockIdx.x) * kChunk + threadIdx.x;
 #pragma unroll 1
-    for (int j = 0; j < 8; ++j) {
+    for (int j = 0; j < kItems; ++j) {
         const long i = base + j * 256;
         if (i < n) {
             const double pi = first ? z[i] : z[i] + beta * p_old[i];
@@ -239,16 +268,17 @@ __global__ void __launch_bounds__(256) pcg_update_kernel(DMesh m, double* __rest
                                                          double* __restrict__ r, double* __restrict__ z,
                                                          const double* __restrict__ p,
                                                          const double* __restrict__ q, double* part,
-                                                         PcgState* st, int k, int maxit) {
+                                                         PcgState* st, int maxit) {
     if (st->done) return;
     __shared__ double ws[8];
     const int n = m.n_cells;
     const int nb = gridDim.x;
+    const int k = st->k + 1;
     const double alpha = st->rz / st->pq;
     double srz = 0.0, srr = 0.0;
-    const long base = long(blockIdx.x) * 2048 + threadIdx.x;
+    const long base = long(blockIdx.x) * kChunk + threadIdx.x;
 #pragma unroll
-    for (int j = 0; j < 8; ++j) {
+    for (int j = 0; j < kItems; ++j) {
         const long i = base + j * 256;
         if (i < n) {
             x[i] = x[i] + alpha * p[i];
@@ -271,6 +301,7 @@ __global__ void __launch_bounds__(256) pcg_update_kernel(DMesh m, double* __rest
         const double rr = final_sum(part + nb, nb, ws);
         if (threadIdx.x == 0) {
             st->rr = rr;
+            st->k = k;
             if (rr <= st->lim) {
                 st->done = 1;
                 st->converged = 1;
@@ -297,8 +328,8 @@ __global__ void __launch_bounds__(256) of_residual_kernel(DMesh m, const double*
     const int n = m.n_cells;
     const int nb = gridDim.x;
     double sn = 0.0, sd = 0.0;
-    const long base = long(blockIdx.x) * 2048 + threadIdx.x;
-    for (int j = 0; j < 8; ++j) {
+    const long base = long(blockIdx.x) * kChunk + threadIdx.x;
+    for (int j = 0; j < kItems; ++j) {
         const long i = base + j * 256;
         if (i < n) {
             const double ax = apply_M(m, x, int(i));
@@ -464,7 +495,7 @@ void launch_floating_update(double* qconv, double* sigma, double* grad_bc, cudaS
     floating_update_kernel<<<1, 32, 0, s>>>(qconv, sigma, grad_bc);
 }
 
-int pcg_blocks(int n) { return (n + 2047) / 2048; }
+int pcg_blocks(int n) { return (n + kChunk - 1) / kChunk; }
 
 void launch_rhs(const DMesh& m, const double* rho, const double* grad_bc, double* b, int singular,
                 double* part, PcgState* st, cudaStream_t s) {
@@ -481,11 +512,11 @@ void launch_pcg_init(const DMesh& m, const double* b, const double* x, double* r
 }
 
 void launch_pcg_iteration(const DMesh& m, double* x, double* r, double* z, const double* p_old,
-                          double* p_new, double* q, double* part, PcgState* st, int k, int maxit,
+                          double* p_new, double* q, double* part, PcgState* st, int maxit,
                           cudaStream_t s) {
     const int nb = pcg_blocks(m.n_cells);
-    pcg_spmv_kernel<<<nb, 256, 0, s>>>(m, z, p_old, p_new, q, part, st, k == 1);
-    pcg_update_kernel<<<nb, 256, 0, s>>>(m, x, r, z, p_new, q, part, st, k, maxit);
+    pcg_spmv_kernel<<<nb, 256, 0, s>>>(m, z, p_old, p_new, q, part, st);
+    pcg_update_kernel<<<nb, 256, 0, s>>>(m, x, r, z, p_new, q, part, st, maxit);
 }
 
 void launch_of_residual(const DMesh& m, const double* b, const double* x, double* part, PcgState* st,

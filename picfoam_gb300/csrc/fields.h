@@ -7,15 +7,28 @@
 
 namespace pgd {
 
+// Reduction layout shared by every deterministic sum: a block of 256 threads
+// owns kChunk consecutive cells, thread t adds cells t, t+256, ... in order.
+constexpr int kItems = 2;
+constexpr int kChunk = 256 * kItems;
+
 // Device-resident PCG scalars; every kernel of one solve reads and writes it.
 struct PcgState {
     double rz, rr, bb, pq, beta, lim, mean, of_residual;
-    int done, iters, converged, pad;
+    int done, iters, converged, k;
     unsigned int ticket;
     unsigned int pad2[3];
 };
 
+// q * weight * 2^-30 per species (the FP32 form's fixed-point deposit).
+struct SpeciesValues {
+    int n;
+    double v[PICGPU_MAX_SPECIES];
+};
+
 cudaError_t fields_set_patches(const PatchConst& p);
+void launch_charge_update_mixed(const DMesh& m, int vw, const SpeciesValues& sv, const unsigned long long* acc,
+                                double space_charge, double* rho, cudaStream_t s);
 int pcg_blocks(int n);
 void launch_charge_update(const DMesh& m, int vw, int fixed, double fix_scale, const double* ccd,
                           const double* vtxd, const long long* ccf, const long long* vtxf,
@@ -26,7 +39,7 @@ void launch_rhs(const DMesh& m, const double* rho, const double* grad_bc, double
 void launch_pcg_init(const DMesh& m, const double* b, const double* x, double* r, double* z,
                      double* part, PcgState* st, double tol, cudaStream_t s);
 void launch_pcg_iteration(const DMesh& m, double* x, double* r, double* z, const double* p_old,
-                          double* p_new, double* q, double* part, PcgState* st, int k, int maxit,
+                          double* p_new, double* q, double* part, PcgState* st, int maxit,
                           cudaStream_t s);
 void launch_of_residual(const DMesh& m, const double* b, const double* x, double* part, PcgState* st,
                         cudaStream_t s);

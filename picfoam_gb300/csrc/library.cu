@@ -38,6 +38,7 @@ struct picgpu_mesh {
 namespace {
 
 constexpr double kMu0 = 4.0 * 3.14159265358979323846 * 1e-7;
+constexpr int kGraphIters = 8;  // PCG iterations per graph replay (even: p buffers alternate)
 constexpr double kCl = 299792458.0;
 
 struct SpeciesBuf {
@@ -74,6 +75,7 @@ struct picgpu_ctx {
     float *E32 = nullptr, *Ept32 = nullptr;
     double *cc_data = nullptr, *vtx_data = nullptr;
     long long *cc_fix = nullptr, *vtx_fix = nullptr;
+    unsigned long long* acc32 = nullptr;  // FP32 form: per-species fixed-point deposit
     double *qconv = nullptr, *sigma = nullptr, *grad_bc = nullptr;
     double *b = nullptr, *r = nullptr, *z = nullptr, *p[2] = {nullptr, nullptr}, *q = nullptr,
            *part = nullptr;
@@ -98,6 +100,7 @@ struct picgpu_ctx {
     int64_t launches = 0;
     picgpu_step_stats acc{};
     cudaEvent_t timer[2] = {nullptr, nullptr};
+    cudaGraphExec_t pcg_graph = nullptr;
 };
 
 picgpu_status pgd_collisions(picgpu_ctx* c, picgpu_step_stats* stats);
@@ -274,6 +277,17 @@ pgd::MoveParams move_params(picgpu_ctx* c, int s, bool deposit_only) {
     P.qconv = c->qconv;
     P.p = view(c, s, c->sp[s].cur);
     P.counters = c->counters;
+    P.charged = S.charge != 0.0;
+    P.has_value = S.charge * S.weight != 0.0;
+    P.qm_f = float(S.charge / S.mass);
+    P.dt_f = float(c->cfg.dt);
+    for (int a = 0; a < 3; ++a) {
+        P.B_f[a] = float(c->cfg.B[a]);
+        P.centre_f[a] = float(c->m.mesh_centre[a]);
+    }
+    const size_t stride = size_t(c->m.n_cells) + c->m.n_points;
+    P.acc_cc = c->acc32 ? c->acc32 + s * stride : nullptr;
+    P.acc_vtx = c->acc32 ? c->acc32 + s * stride + c->m.n_cells : nullptr;
     return P;
 }
 
@@ -282,6 +296,10 @@ picgpu_status zero_accumulators(picgpu_ctx* c) {
     CK(cudaMemsetAsync(c->vtx_data, 0, sizeof(double) * c->m.n_points, c->stream));
     CK(cudaMemsetAsync(c->cc_fix, 0, sizeof(long long) * c->m.n_cells, c->stream));
     CK(cudaMemsetAsync(c->vtx_fix, 0, sizeof(long long) * c->m.n_points, c->stream));
+    if (c->mixed)
+        CK(cudaMemsetAsync(c->acc32, 0,
+                           sizeof(unsigned long long) * c->cfg.n_species * (size_t(c->m.n_cells) + c->m.n_points),
+                           c->stream));
     return PICGPU_OK;
 }
 
@@ -305,6 +323,17 @@ picgpu_status move_species(picgpu_ctx* c, bool deposit_only) {
 
 picgpu_status charge_update(picgpu_ctx* c) {
     PhaseScope ps(c, PICGPU_PHASE_CHARGE);
+    if (c->mixed) {
+        pgd::SpeciesValues sv{};
+        sv.n = c->cfg.n_species;
+        for (int s = 0; s < sv.n; ++s)
+            sv.v[s] = std::ldexp(c->cfg.species[s].charge * c->cfg.species[s].weight, -30);
+        pgd::launch_charge_update_mixed(c->dm, c->cfg.charge_distribution == PICGPU_WEIGHTING_VOLUME, sv, c->acc32,
+                                        c->cfg.space_charge, c->rho, c->stream);
+        c->launches++;
+        CK(cudaGetLastError());
+        return PICGPU_OK;
+    }
     pgd::launch_charge_update(c->dm, c->cfg.charge_distribution == PICGPU_WEIGHTING_VOLUME,
                               c->cfg.deposit_mode == PICGPU_DEPOSIT_FIXED_POINT, c->fix_scale, c->cc_data,
                               c->vtx_data, c->cc_fix, c->vtx_fix, c->cfg.space_charge, c->rho, c->stream);
@@ -341,23 +370,32 @@ picgpu_status poisson(picgpu_ctx* c, picgpu_step_stats* stats) {
     const int maxit = c->cfg.pcg_max_iter > 0 ? c->cfg.pcg_max_iter : 10000;
     {
         PhaseScope ps(c, PICGPU_PHASE_POISSON);
+        // PCG iterations run as a CUDA graph of kGraphIters iterations
+        // (2 kernels each); iterations after convergence return at once, so
+        // the iteration count stays exact.  The host checks the done flag
+        // after each replay.
+        if (!c->pcg_graph) {
+            cudaGraph_t g;
+            CK(cudaStreamBeginCapture(c->stream, cudaStreamCaptureModeThreadLocal));
+            for (int j = 0; j < kGraphIters; ++j)
+                pgd::launch_pcg_iteration(c->dm, c->phi, c->r, c->z, c->p[j & 1], c->p[(j + 1) & 1], c->q, c->part,
+                                          c->st, maxit, c->stream);
+            CK(cudaStreamEndCapture(c->stream, &g));
+            CK(cudaGraphInstantiate(&c->pcg_graph, g, 0));
+            CK(cudaGraphDestroy(g));
+        }
         pgd::launch_rhs(c->dm, c->rho, c->grad_bc, c->b, !c->m.has_dirichlet, c->part, c->st, c->stream);
         pgd::launch_pcg_init(c->dm, c->b, c->phi, c->r, c->z, c->part, c->st, tol, c->stream);
         c->launches += c->m.has_dirichlet ? 2 : 4;
         CK(cudaMemcpyAsync(c->st_host, c->st, sizeof(pgd::PcgState), cudaMemcpyDeviceToHost, c->stream));
         CK(cudaStreamSynchronize(c->stream));
-        int k = 1;
-        int batch = 4;
-        while (!c->st_host->done && k <= maxit) {
-            for (int j = 0; j < batch && k <= maxit; ++j, ++k) {
-                pgd::launch_pcg_iteration(c->dm, c->phi, c->r, c->z, c->p[(k + 1) & 1], c->p[k & 1], c->q,
-                                          c->part, c->st, k, maxit, c->stream);
-                c->launches += 2;
-            }
-            CK(cudaGetLastError());
+        int launched = 0;
+        while (!c->st_host->done && launched < maxit) {
+            CK(cudaGraphLaunch(c->pcg_graph, c->stream));
+            launched += kGraphIters;
+            c->launches += 2 * kGraphIters;
             CK(cudaMemcpyAsync(c->st_host, c->st, sizeof(pgd::PcgState), cudaMemcpyDeviceToHost, c->stream));
             CK(cudaStreamSynchronize(c->stream));
-            batch = std::min(batch * 2, 32);
         }
         pgd::launch_of_residual(c->dm, c->b, c->phi, c->part, c->st, c->stream);
         c->launches += 2;
@@ -653,6 +691,8 @@ picgpu_status picgpu_create(const picgpu_mesh_desc* mesh, const picgpu_config* c
     UP(nbr, m.nbr, int);
     UP(cell_pt, m.cell_pt, int);
     UP(cc, m.cc, double);
+    std::vector<float> cc32(m.cc.begin(), m.cc.end());
+    UP(cc32, cc32, float);
     UP(vol, m.vol, double);
     UP(tetinv, m.cls_tetinv, double);
     UP(tetinv32, inv32, float);
@@ -691,6 +731,7 @@ picgpu_status picgpu_create(const picgpu_mesh_desc* mesh, const picgpu_config* c
         (s = dalloc(c, &c->q, nc)) || (s = dalloc(c, &c->part, 3 * size_t(pgd::pcg_blocks(int(nc))) + 8)) ||
         (s = dalloc(c, &c->st, 1)) || (s = dalloc(c, &c->counters, 1)) || (s = dalloc(c, &c->diag, 64)))
         return s;
+    if (c->mixed && (s = dalloc(c, &c->acc32, size_t(cfg->n_species) * (nc + np)))) return s;
     CK(cudaMemset(c->phi, 0, nc * sizeof(double)));
     CK(cudaMemset(c->E, 0, 3 * nc * sizeof(double)));
     CK(cudaMemset(c->Ept, 0, 3 * np * sizeof(double)));
@@ -727,6 +768,7 @@ void picgpu_destroy(picgpu_ctx* c) {
     for (auto& ep : c->pending) { cudaEventDestroy(ep.a); cudaEventDestroy(ep.b); }
     for (auto e : c->free_events) cudaEventDestroy(e);
     if (c->timer[0]) { cudaEventDestroy(c->timer[0]); cudaEventDestroy(c->timer[1]); }
+    if (c->pcg_graph) cudaGraphExecDestroy(c->pcg_graph);
     if (c->st_host) cudaFreeHost(c->st_host);
     if (c->counters_host) cudaFreeHost(c->counters_host);
     if (c->stream) cudaStreamDestroy(c->stream);

@@ -24,7 +24,30 @@ template <> struct RealTraits<float> {
     static __device__ __forceinline__ float thr() { return 1e-6f; }
 };
 
-template <class Real> struct V { Real x, y, z; };
+// Per-precision access to the species and field constants.  The FP64 form
+// evaluates q dt/2 / m exactly as the oracle does; the FP32 form uses the
+// host-rounded float copies.
+template <class Real> struct PC;
+template <> struct PC<double> {
+    static __device__ __forceinline__ double dt(const MoveParams& P) { return P.dt; }
+    static __device__ __forceinline__ double B(const MoveParams& P, int a) { return P.B[a]; }
+    static __device__ __forceinline__ double qdm(const MoveParams& P, double half_dt) {
+        return P.q * half_dt / P.mass;
+    }
+    static __device__ __forceinline__ double centre(const MoveParams& P, int a) { return P.m.mesh_centre[a]; }
+    static __device__ __forceinline__ double cc(const MoveParams& P, int c, int a) {
+        return P.m.cc[3 * size_t(c) + a];
+    }
+};
+template <> struct PC<float> {
+    static __device__ __forceinline__ float dt(const MoveParams& P) { return P.dt_f; }
+    static __device__ __forceinline__ float B(const MoveParams& P, int a) { return P.B_f[a]; }
+    static __device__ __forceinline__ float qdm(const MoveParams& P, float half_dt) { return P.qm_f * half_dt; }
+    static __device__ __forceinline__ float centre(const MoveParams& P, int a) { return P.centre_f[a]; }
+    static __device__ __forceinline__ float cc(const MoveParams& P, int c, int a) {
+        return P.m.cc32[3 * size_t(c) + a];
+    }
+};
 
 template <class Real>
 __device__ __forceinline__ Real dot3(const Real* a, const Real* b) {
@@ -90,13 +113,13 @@ __device__ __forceinline__ void push_boris(const MoveParams& P, const Real* E, R
     const Real g0 = sqrt(Real(1) - mU * mU);
     Real rU[3] = {U[0] / g0, U[1] / g0, U[2] / g0};
     const Real oldrU[3] = {rU[0], rU[1], rU[2]};
-    const Real qdm = Real(P.q) * dt2 / Real(P.mass);
+    const Real qdm = PC<Real>::qdm(P, dt2);
     const Real rUsm[3] = {qdm * E[0], qdm * E[1], qdm * E[2]};
     rU[0] = rU[0] + rUsm[0]; rU[1] = rU[1] + rUsm[1]; rU[2] = rU[2] + rUsm[2];
     if (P.rotation) {
         const Real a0 = sqrt(dot3(oldrU, oldrU)) / c, a1 = sqrt(dot3(rU, rU)) / c;
         const Real lF = (sqrt(Real(1) + a0 * a0) + sqrt(Real(1) + a1 * a1)) / Real(2);
-        const Real t[3] = {qdm * Real(P.B[0]) / lF, qdm * Real(P.B[1]) / lF, qdm * Real(P.B[2]) / lF};
+        const Real t[3] = {qdm * PC<Real>::B(P, 0) / lF, qdm * PC<Real>::B(P, 1) / lF, qdm * PC<Real>::B(P, 2) / lF};
         Real cr[3];
         cross3(rU, t, cr);
         const Real Ud[3] = {rU[0] + cr[0], rU[1] + cr[1], rU[2] + cr[2]};
@@ -115,10 +138,10 @@ __device__ __forceinline__ void push_boris(const MoveParams& P, const Real* E, R
 template <class Real>
 __device__ __forceinline__ void push_boris_nr(const MoveParams& P, const Real* E, Real* U, Real tt) {
     const Real dt2 = Real(0.5) * tt;
-    const Real alpha = Real(P.q) * dt2 / Real(P.mass);
+    const Real alpha = PC<Real>::qdm(P, dt2);
     Real W[3] = {U[0] + alpha * E[0], U[1] + alpha * E[1], U[2] + alpha * E[2]};
     if (P.rotation) {
-        const Real t[3] = {alpha * Real(P.B[0]), alpha * Real(P.B[1]), alpha * Real(P.B[2])};
+        const Real t[3] = {alpha * PC<Real>::B(P, 0), alpha * PC<Real>::B(P, 1), alpha * PC<Real>::B(P, 2)};
         Real cr[3];
         cross3(W, t, cr);
         const Real Ud[3] = {W[0] + cr[0], W[1] + cr[1], W[2] + cr[2]};
@@ -138,10 +161,10 @@ __device__ __forceinline__ void push_vay(const MoveParams& P, const Real* E, Rea
     const Real mU = sqrt(dot3(U, U)) / c;
     const Real lF = Real(1) / sqrt(Real(1) - mU * mU);
     const Real rU0[3] = {lF * U[0], lF * U[1], lF * U[2]};
-    const Real qe = Real(P.q) * tt / Real(P.mass);
+    const Real qe = PC<Real>::qdm(P, tt);
     Real Ud[3] = {rU0[0] + qe * E[0], rU0[1] + qe * E[1], rU0[2] + qe * E[2]};
-    const Real qb = Real(P.q) * dt2 / Real(P.mass);
-    Real T[3] = {qb * Real(P.B[0]), qb * Real(P.B[1]), qb * Real(P.B[2])};
+    const Real qb = PC<Real>::qdm(P, dt2);
+    Real T[3] = {qb * PC<Real>::B(P, 0), qb * PC<Real>::B(P, 1), qb * PC<Real>::B(P, 2)};
     Real cr[3];
     cross3(U, T, cr);
     Ud[0] = Ud[0] + cr[0]; Ud[1] = Ud[1] + cr[1]; Ud[2] = Ud[2] + cr[2];
@@ -172,13 +195,13 @@ __device__ __forceinline__ void push_hc(const MoveParams& P, const Real* E, Real
     const Real mU = sqrt(dot3(U, U)) / c;
     const Real g0 = sqrt(Real(1) - mU * mU);
     Real rU[3] = {U[0] / g0, U[1] / g0, U[2] / g0};
-    const Real qdm = Real(P.q) * dt2 / Real(P.mass);
+    const Real qdm = PC<Real>::qdm(P, dt2);
     const Real rUsm[3] = {qdm * E[0], qdm * E[1], qdm * E[2]};
     rU[0] = rU[0] + rUsm[0]; rU[1] = rU[1] + rUsm[1]; rU[2] = rU[2] + rUsm[2];
     if (P.rotation) {
         const Real mr0 = sqrt(dot3(rU, rU)) / c;
         const Real gfm2 = Real(1) + mr0 * mr0;
-        Real t[3] = {qdm * Real(P.B[0]), qdm * Real(P.B[1]), qdm * Real(P.B[2])};
+        Real t[3] = {qdm * PC<Real>::B(P, 0), qdm * PC<Real>::B(P, 1), qdm * PC<Real>::B(P, 2)};
         const Real beta2 = dot3(t, t);
         const Real gb = gfm2 - beta2;
         const Real tr = dot3(t, rU);
@@ -250,7 +273,7 @@ __device__ __forceinline__ int tet_step(const MoveParams& P, PState<Real>& s, co
 template <class Real>
 __device__ __forceinline__ void sync_velocity(const MoveParams& P, const TetConst& T, PState<Real>& s,
                                               Real fraction) {
-    if (P.sync && P.q != 0.0) push(P, T, s, fraction * Real(P.dt));
+    if (P.sync && P.charged) push(P, T, s, fraction * PC<Real>::dt(P));
 }
 
 struct TrackTally {
@@ -260,9 +283,9 @@ struct TrackTally {
 
 // PICParcel::hitPatch (PICParcel.C:153-184) for the patch models in scope.
 template <class Real>
-__device__ __forceinline__ void hit_patch(const MoveParams& P, const TetConst& T, const PatchConst& PC,
+__device__ __forceinline__ void hit_patch(const MoveParams& P, const TetConst& T, const PatchConst& PCs,
                                           PState<Real>& s, int patch, Real sf, TrackTally& td) {
-    const int kind = PC.kind[patch];
+    const int kind = PCs.kind[patch];
     if (kind == PICGPU_PATCH_ABSORB) { td.keep = false; return; }
     if (kind == PICGPU_PATCH_FLOATING) {
         td.keep = false;
@@ -287,7 +310,7 @@ __device__ __forceinline__ void hit_patch(const MoveParams& P, const TetConst& T
 
 template <class Real>
 __device__ __forceinline__ void track_to_and_hit_face(const MoveParams& P, const TetConst& T,
-                                                      const PatchConst& PC, PState<Real>& s,
+                                                      const PatchConst& PCs, PState<Real>& s,
                                                       const Real* disp, Real f, Real& sf,
                                                       TrackTally& td, int& budget) {
     Real rem = Real(1);
@@ -337,7 +360,7 @@ __device__ __forceinline__ void track_to_and_hit_face(const MoveParams& P, const
             for (int j = 0; j < 4; ++j) s.y[j] = y[j];
             return;
         }
-        hit_patch(P, T, PC, s, -nb - 1, sf, td);
+        hit_patch(P, T, PCs, s, -nb - 1, sf, td);
         return;
     }
 }
@@ -360,8 +383,25 @@ __device__ __forceinline__ void deposit_add(const MoveParams& P, double* dst64, 
 }
 
 // ChargeDistribution::add for one particle at its end-of-step position.
-template <class Real>
-__device__ __forceinline__ void deposit(const MoveParams& P, const TetConst& T, const PState<Real>& s) {
+// FP32 form: the dimensionless weights y go to this species' 64-bit
+// fixed-point accumulators (2^-30 resolution); the charge update multiplies
+// by q w per species.  Integer sums are order-independent, so the FP32 form's
+// charge density is deterministic.
+__device__ __forceinline__ void deposit(const MoveParams& P, const TetConst& T, const PState<float>& s) {
+    if (!P.has_value) return;
+    constexpr float kScale = 1073741824.0f;
+    if (P.charge_distribution == PICGPU_WEIGHTING_CELL_AVERAGE) {
+        atomicAdd(P.acc_cc + s.cell, 1ull << 30);
+        return;
+    }
+    const int* cp = P.m.cell_pt + 8 * size_t(s.cell);
+    atomicAdd(P.acc_cc + s.cell, (unsigned long long)__float2uint_rn(s.y[0] * kScale));
+#pragma unroll
+    for (int i = 0; i < 3; ++i)
+        atomicAdd(P.acc_vtx + cp[T.tri[s.tet][i]], (unsigned long long)__float2uint_rn(s.y[i + 1] * kScale));
+}
+
+__device__ __forceinline__ void deposit(const MoveParams& P, const TetConst& T, const PState<double>& s) {
     const double value = P.value;
     if (value == 0.0) return;
     if (P.charge_distribution == PICGPU_WEIGHTING_CELL_AVERAGE) {
@@ -386,7 +426,7 @@ __device__ __forceinline__ void warp_add_counter(unsigned long long* dst, unsign
 // The per-particle step.  Returns through the tally; the particle record is
 // written back in place (tet = -1 once removed).
 template <class Real>
-__device__ __forceinline__ void move_one(const MoveParams& P, const TetConst& T, const PatchConst& PC,
+__device__ __forceinline__ void move_one(const MoveParams& P, const TetConst& T, const PatchConst& PCs,
                                          int i, TrackTally& td) {
     int32_t tetg = P.p.tet[i];
     if (tetg < 0) return;
@@ -401,8 +441,8 @@ __device__ __forceinline__ void move_one(const MoveParams& P, const TetConst& T,
     s.U[1] = ubuf<Real>(P.p, 1)[i];
     s.U[2] = ubuf<Real>(P.p, 2)[i];
     if (P.solve_movement) {
-        const Real dt = Real(P.dt);
-        if (P.q != 0.0) push(P, T, s, dt);
+        const Real dt = PC<Real>::dt(P);
+        if (P.charged) push(P, T, s, dt);
         const Real c = Real(kC);
         if (!(sqrt(dot3(s.U, s.U)) < c)) {
             td.keep = false;
@@ -416,22 +456,21 @@ __device__ __forceinline__ void move_one(const MoveParams& P, const TetConst& T,
                 Real dev[3] = {Real(0), Real(0), Real(0)};
                 if (P.m.any_empty) {
                     const Real* off = offsets<Real>(P.m) + size_t(P.m.cell_class[s.cell]) * 24;
-                    const double* ccp = P.m.cc + 3 * size_t(s.cell);
 #pragma unroll
                     for (int a = 0; a < 3; ++a) {
                         if (!P.m.empty[a]) continue;
                         Ut[a] = Real(0);
-                        const Real x = Real(ccp[a]) + s.y[1] * off[3 * T.tri[s.tet][0] + a] +
+                        const Real x = PC<Real>::cc(P, s.cell, a) + s.y[1] * off[3 * T.tri[s.tet][0] + a] +
                                        s.y[2] * off[3 * T.tri[s.tet][1] + a] +
                                        s.y[3] * off[3 * T.tri[s.tet][2] + a];
-                        dev[a] = x - Real(P.m.mesh_centre[a]);
+                        dev[a] = x - PC<Real>::centre(P, a);
                     }
                 }
                 const Real f = Real(1) - sf;
                 const Real fdt = f * dt;
                 const Real disp[3] = {fdt * Ut[0] - dev[0], fdt * Ut[1] - dev[1], fdt * Ut[2] - dev[2]};
                 td.resync = false;
-                track_to_and_hit_face(P, T, PC, s, disp, f, sf, td, budget);
+                track_to_and_hit_face(P, T, PCs, s, disp, f, sf, td, budget);
                 if (td.capped) break;
                 if (td.resync && td.keep) {
                     resync++;

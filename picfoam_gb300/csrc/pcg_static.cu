@@ -24,7 +24,7 @@
 namespace {
 
 constexpr long kMaxCells = PICGPU_NOALLOC_MAX_CELLS;
-constexpr long kMaxBlocks = (kMaxCells + 2047) / 2048;
+constexpr long kMaxBlocks = (kMaxCells + pgd::kChunk - 1) / pgd::kChunk;
 constexpr long kPartDoubles = 3 * kMaxBlocks + 8;
 constexpr long kStateDoubles = 32;  // holds one pgd::PcgState (rounded up)
 constexpr long kNoallocScratchDoubles = 6 * kMaxCells + kPartDoubles + kStateDoubles;
@@ -95,7 +95,7 @@ extern "C" picgpu_status picgpu_solve_ldu_noalloc(int n_cells, const double* dia
     int k = 1, batch = 4;
     while (!h.done && k <= max_iter) {
         for (int j = 0; j < batch && k <= max_iter; ++j, ++k)
-            pgd::launch_pcg_iteration(m, x, r, z, p[(k + 1) & 1], p[k & 1], q, part, st, k, max_iter, s);
+            pgd::launch_pcg_iteration(m, x, r, z, p[(k + 1) & 1], p[k & 1], q, part, st, max_iter, s);
         if (cudaGetLastError() != cudaSuccess ||
             cudaMemcpyAsync(&h, st, sizeof h, cudaMemcpyDeviceToHost, s) != cudaSuccess ||
             cudaStreamSynchronize(s) != cudaSuccess)

@@ -1,0 +1,68 @@
+"""The C ABI library: loads without a GPU, exports every declared symbol,
+and its host-only mesh calls work."""
+import ctypes as C
+import os
+import re
+
+import numpy as np
+import pytest
+
+from picfoam_gb300 import abi, build, cases, native
+from picfoam_gb300.simulation import Mesh, PicError
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+
+
+@pytest.fixture(scope="module")
+def lib():
+    build.build()
+    return native.load()
+
+
+def declared_symbols():
+    src = open(os.path.join(ROOT, "include", "picgpu.h")).read()
+    src = re.sub(r"/\*.*?\*/", "", src, flags=re.S)
+    return sorted(set(re.findall(r"\b(picgpu_[a-z0-9_]+)\s*\(", src)))
+
+
+def test_every_declared_symbol_is_exported(lib):
+    syms = declared_symbols()
+    assert len(syms) >= 25
+    missing = [s for s in syms if not hasattr(lib, s)]
+    assert not missing, missing
+
+
+def test_struct_sizes_match_header_layout():
+    # the ctypes mirror must have the C layout (natural alignment, no packing)
+    assert C.sizeof(abi.Patch) == 16
+    assert C.sizeof(abi.MeshDesc) == 12 + 4 + 24 + 24 + 6 * 16 + 8 + abi.MAX_BOXES * 40
+    assert C.sizeof(abi.Species) == 32
+    assert C.sizeof(abi.StepStats) % 8 == 0
+
+
+def test_mesh_handle_without_gpu(lib):
+    case = cases.two_species_3d(n_cells=6, per_cell=3, L=0.003)
+    m = Mesh(case.mesh)
+    assert m.n_cells == 216 and m.n_points == 343
+    tet, bary, _ = case.particles[0]
+    x = m.position(tet, bary)
+    t2, b2 = m.locate(x)
+    np.testing.assert_array_equal(t2, tet)
+    np.testing.assert_allclose(b2, bary, atol=1e-12)
+    cc, vol = m.cells()
+    np.testing.assert_allclose(vol, (0.003 / 6) ** 3, rtol=1e-12)
+    assert np.all((cc > 0) & (cc < 0.003))
+
+
+def test_invalid_mesh_rejected(lib):
+    case = cases.two_species_3d(n_cells=4, per_cell=1)
+    case.mesh.side[0].kind = abi.PATCH_CYCLIC  # cyclic without its pair
+    with pytest.raises(PicError):
+        Mesh(case.mesh)
+
+
+def test_position_rejects_bad_tet(lib):
+    case = cases.two_species_3d(n_cells=2, per_cell=1)
+    m = Mesh(case.mesh)
+    with pytest.raises(PicError):
+        m.position(np.array([8 * 12]), np.zeros((1, 3)))
