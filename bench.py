@@ -47,6 +47,8 @@ def parse():
     p.add_argument("--no-cpu-baseline", action="store_true")
     p.add_argument("--no-e2e", action="store_true")
     p.add_argument("--poisson-steps", type=int, default=3)
+    p.add_argument("--sort-interval", type=int, default=10,
+                   help="re-sort the particle store into cell order every N steps (0: never)")
     return p.parse_args()
 
 
@@ -223,6 +225,7 @@ def run_ours(args, rank, ws):
     local = int(os.environ.get("LOCAL_RANK", "0"))
     prec = abi.PREC_MIXED if args.precision == "mixed" else abi.PREC_FP64
     case = cases.two_species_3d(n_cells=args.cells, per_cell=args.ppc, precision=prec, seed=1234 + rank)
+    case.cfg.sort_interval = args.sort_interval
     sim = cases.build(case)
     sim.initialise_fields()
     sim.set_profiling(True)

@@ -1,4 +1,4 @@
-// collide.h -- collision step (cell sort, null-collision MCC, Coulomb).
+// collide.h -- collision step (cell occupancy, null-collision MCC, Coulomb).
 #pragma once
 
 #include <string>
@@ -7,6 +7,16 @@
 
 namespace pgd {
 
+// A secondary staged by the MCC kernel: the ionising electron's position and
+// the velocities of the new electron and ion.
+struct Secondary {
+    int32_t tet;
+    int32_t flag;         // bit 0: electron, bit 1: ion
+    double y[3];
+    double ue[3];
+    double ui[3];
+};
+
 // Device state owned by the collision step.
 struct CollideState {
     int enabled = 0;
@@ -14,13 +24,22 @@ struct CollideState {
     double* remainder = nullptr;  // collision remainder per cell
     double* xs = nullptr;         // 4 x n_xs: energy, elastic, excitation, ionisation
     int n_xs = 0;
-    int* cell_start = nullptr;    // per species: n_cells + 1 offsets of the sorted store
+    int* cell_start = nullptr;    // per species: n_cells + 1 offsets into idx
     int* cell_count = nullptr;
     int* cell_cursor = nullptr;
-    int* perm = nullptr;          // sorted slot -> old slot
-    long perm_cap = 0;
-    unsigned long long* counts = nullptr;  // 8 counters
-    int* new_count = nullptr;              // appended particles per species
+    int* scan_tmp = nullptr;
+    unsigned long long* counts = nullptr;  // candidates, elastic, excitation, ionisation, coulomb pairs
+    int* idx[PICGPU_MAX_SPECIES] = {};     // particle indices grouped by cell
+    int* sel[PICGPU_MAX_SPECIES] = {};     // pairing permutations (scratch)
+    int* sel2[PICGPU_MAX_SPECIES] = {};
+    long idx_cap[PICGPU_MAX_SPECIES] = {};
+    int* ncand = nullptr;                  // MCC candidates per cell
+    int* cand_off = nullptr;               // their staging offsets
+    Secondary* stage = nullptr;
+    int* flags = nullptr;
+    int* pos = nullptr;
+    int* stage_tmp = nullptr;
+    long stage_cap = 0;
 };
 
 struct CollideArgs {
@@ -30,14 +49,8 @@ struct CollideArgs {
     int n_species;
     bool mixed;
     DSpecies sp[PICGPU_MAX_SPECIES];
-    DSpecies alt[PICGPU_MAX_SPECIES];
     long n[PICGPU_MAX_SPECIES];
     long cap[PICGPU_MAX_SPECIES];
-    double* cc_data;
-    double* vtx_data;
-    long long* cc_fix;
-    long long* vtx_fix;
-    double fix_scale;
     cudaStream_t stream;
 };
 
@@ -45,8 +58,13 @@ cudaError_t collide_set_tables(const TetConst& t);
 // Returns a picgpu_status; msg describes a failure.
 int collide_init(CollideState& st, const picgpu_config& cfg, const DMesh& m, cudaStream_t s, std::string* msg);
 void collide_free(CollideState& st);
-// counts: candidates, elastic, excitation, ionisation, coulomb pairs.
-int run_collisions(CollideState& st, const CollideArgs& a, int64_t counts[8], long newn[],
-                   int swapped[], std::string* msg, int64_t* launches, double* phase_ms);
+// Reorder species s into cell order (stable within a cell), dropping removed
+// particles: src -> dst, *kept = particles written.
+int sort_species(CollideState& st, const DMesh& m, int s, const DSpecies& src, const DSpecies& dst, long n,
+                 bool mixed, long* kept, cudaStream_t stream, std::string* msg, int64_t* launches);
+// counts: candidates, elastic, excitation, ionisation, coulomb pairs; newn
+// receives the species counts after MCC secondaries were appended.
+int run_collisions(CollideState& st, const CollideArgs& a, int64_t counts[8], long newn[], int swapped[],
+                   std::string* msg, int64_t* launches, double* phase_ms);
 
 }  // namespace pgd

@@ -11,6 +11,9 @@ namespace pgd {
 constexpr double kC = 299792458.0;
 constexpr double kPi = 3.14159265358979323846;
 constexpr int kMaxPatches = PICGPU_MAX_BOXES + 6;
+// FP32 form: barycentric charge weights are accumulated as integers in units
+// of 2^-kDepositBits (32 lanes x 2^25 still fits a 32-bit warp sum).
+constexpr int kDepositBits = 25;
 
 // Tet tables of the canonical hex (see hexmesh.hpp), in constant memory.
 struct TetConst {
@@ -28,6 +31,19 @@ struct PatchConst {
     int phi_bc[kMaxPatches];
     double phi[kMaxPatches];
     double area[kMaxPatches];
+};
+
+// Shared-memory tables of the FP32 move kernel: the geometry of a uniform
+// block mesh and the tet-crossing tables packed as
+//   bits 0-3 new local tet, bits 4+3j..6+3j source of coordinate j (7: zero).
+struct Tables32 {
+    float inv[108];
+    float normal[18];
+    float off[24];
+    unsigned inner[48];
+    unsigned cross[12];
+    unsigned tri[12];            // corners of the face triangle, 4 bits each
+    int kind[kMaxPatches];
 };
 
 // Read-only mesh arrays on the device.
@@ -63,6 +79,9 @@ struct DMesh {
     const double* Mdiag;     // SPD operator -laplacian
     const double* Moff;      // 6 n_cells
     const double* dinv;
+    const int* pc_start;     // n_points + 1: point -> cell-corner slots
+    const int* pc_slot;
+    int uniform;             // one geometry class (block mesh of equal cells)
 };
 
 // Per-species particle storage (structure of arrays).
@@ -87,6 +106,7 @@ struct MoveCounters {
 struct MoveParams {
     DMesh m;
     int n;                   // particles in this species (including removed slots)
+    int first;               // first slot to process
     int species;
     int pusher;
     int field_weighting;
@@ -109,8 +129,8 @@ struct MoveParams {
     float dt_f;
     float B_f[3];
     float centre_f[3];
-    unsigned long long* acc_cc;   // this species' fixed-point (2^-30) deposit, cells
-    unsigned long long* acc_vtx;  // ... and points
+    unsigned long long* acc9;     // this species' 2^-kDepositBits fixed-point deposit per cell: centre + 8 corners
+    const float4* Ec4;            // E per cell: centre + 8 corners (FP32 form)
     const double* E;         // 3 n_cells
     const double* Ept;       // 3 n_points
     const float* E32;

@@ -89,31 +89,63 @@ __global__ void charge_update_kernel(DMesh m, int volume_weighting, int fixed, d
     rho[c] = r + space_charge;
 }
 
-// Charge update of the FP32 form: per-species fixed-point weights times q w.
+// Charge update of the FP32 form.  The move kernel leaves per species and
+// cell 9 fixed-point slots (centre + 8 corners); a point's charge is the
+// integer sum of the corner slots of every cell around it (syncPointData of
+// VolumeWeighting.C:141-146, cyclic images included), times q w 2^-kDepositBits.
+__global__ void point_charge_kernel(DMesh m, SpeciesValues sv, const unsigned long long* __restrict__ acc9,
+                                    double* __restrict__ vtx) {
+    const int p = blockIdx.x * blockDim.x + threadIdx.x;
+    if (p >= m.n_points) return;
+    const size_t stride = 9 * size_t(m.n_cells);
+    double v = 0.0;
+    for (int s = 0; s < sv.n; ++s) {
+        unsigned long long sum = 0;
+        for (int k = m.pc_start[p]; k < m.pc_start[p + 1]; ++k) sum += acc9[s * stride + m.pc_slot[k]];
+        v += sv.v[s] * double(sum);
+    }
+    vtx[p] = v;
+}
+
 __global__ void charge_update_mixed_kernel(DMesh m, int volume_weighting, SpeciesValues sv,
-                                           const unsigned long long* __restrict__ acc, double space_charge,
+                                           const unsigned long long* __restrict__ acc9,
+                                           const double* __restrict__ vtx, double space_charge,
                                            double* __restrict__ rho) {
     const int c = blockIdx.x * blockDim.x + threadIdx.x;
     if (c >= m.n_cells) return;
-    const size_t stride = size_t(m.n_cells) + size_t(m.n_points);
+    const size_t stride = 9 * size_t(m.n_cells);
     const double V = m.vol[c];
     double ccv = 0.0;
-    for (int s = 0; s < sv.n; ++s) ccv += sv.v[s] * double(acc[s * stride + c]);
+    for (int s = 0; s < sv.n; ++s) ccv += sv.v[s] * double(acc9[s * stride + 9 * size_t(c)]);
     double r = ccv / V;
-    if (volume_weighting) {
-        for (int q = 0; q < 8; ++q) {
-            const size_t pt = size_t(m.n_cells) + m.cell_pt[8 * size_t(c) + q];
-            double vv = 0.0;
-            for (int s = 0; s < sv.n; ++s) vv += sv.v[s] * double(acc[s * stride + pt]);
-            r += (m.vw_weight[8 * size_t(c) + q] * vv) / V;
-        }
-    }
+    if (volume_weighting)
+        for (int q = 0; q < 8; ++q)
+            r += (m.vw_weight[8 * size_t(c) + q] * vtx[m.cell_pt[8 * size_t(c) + q]]) / V;
     rho[c] = r + space_charge;
 }
 
-void launch_charge_update_mixed(const DMesh& m, int vw, const SpeciesValues& sv, const unsigned long long* acc,
-                                double space_charge, double* rho, cudaStream_t s) {
-    charge_update_mixed_kernel<<<(m.n_cells + 255) / 256, 256, 0, s>>>(m, vw, sv, acc, space_charge, rho);
+void launch_charge_update_mixed(const DMesh& m, int vw, const SpeciesValues& sv, const unsigned long long* acc9,
+                                double* vtx, double space_charge, double* rho, cudaStream_t s) {
+    if (vw) point_charge_kernel<<<(m.n_points + 255) / 256, 256, 0, s>>>(m, sv, acc9, vtx);
+    charge_update_mixed_kernel<<<(m.n_cells + 255) / 256, 256, 0, s>>>(m, vw, sv, acc9, vtx, space_charge, rho);
+}
+
+// E per cell for the FP32 move kernel: centre value + the 8 corner (point)
+// values as float4, so a particle's field gather reads one cell block.
+__global__ void corner_E_kernel(DMesh m, const double* __restrict__ E, const double* __restrict__ Ept,
+                                float4* __restrict__ Ec4) {
+    const int c = blockIdx.x * blockDim.x + threadIdx.x;
+    if (c >= m.n_cells) return;
+    const double* e = E + 3 * size_t(c);
+    Ec4[9 * size_t(c)] = make_float4(float(e[0]), float(e[1]), float(e[2]), 0.f);
+    for (int q = 0; q < 8; ++q) {
+        const double* p = Ept + 3 * size_t(m.cell_pt[8 * size_t(c) + q]);
+        Ec4[9 * size_t(c) + 1 + q] = make_float4(float(p[0]), float(p[1]), float(p[2]), 0.f);
+    }
+}
+
+void launch_corner_E(const DMesh& m, const double* E, const double* Ept, float4* Ec4, cudaStream_t s) {
+    corner_E_kernel<<<(m.n_cells + 255) / 256, 256, 0, s>>>(m, E, Ept, Ec4);
 }
 
 // FloatingPotential::preUpdate_Boundary (FloatingPotential.C:89-100)

@@ -20,15 +20,16 @@ struct PcgState {
     unsigned int pad2[3];
 };
 
-// q * weight * 2^-30 per species (the FP32 form's fixed-point deposit).
+// q * weight * 2^-kDepositBits per species (the FP32 form's fixed-point deposit).
 struct SpeciesValues {
     int n;
     double v[PICGPU_MAX_SPECIES];
 };
 
 cudaError_t fields_set_patches(const PatchConst& p);
-void launch_charge_update_mixed(const DMesh& m, int vw, const SpeciesValues& sv, const unsigned long long* acc,
-                                double space_charge, double* rho, cudaStream_t s);
+void launch_charge_update_mixed(const DMesh& m, int vw, const SpeciesValues& sv, const unsigned long long* acc9,
+                                double* vtx, double space_charge, double* rho, cudaStream_t s);
+void launch_corner_E(const DMesh& m, const double* E, const double* Ept, float4* Ec4, cudaStream_t s);
 int pcg_blocks(int n);
 void launch_charge_update(const DMesh& m, int vw, int fixed, double fix_scale, const double* ccd,
                           const double* vtxd, const long long* ccf, const long long* vtxf,

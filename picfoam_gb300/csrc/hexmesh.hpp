@@ -184,6 +184,10 @@ struct HexMesh {
     std::vector<int> pi_src;        // >= 0 cell, < 0: -(bface + 1)
     std::vector<double> pi_w;
 
+    // merged point -> the cell-corner slots (9 c + 1 + corner) that touch it
+    std::vector<int> pc_start;      // n_points + 1
+    std::vector<int> pc_slot;
+
     TetTables tt;
 };
 
@@ -521,6 +525,15 @@ inline HexMesh build_hex_mesh(const picgpu_mesh_desc& d) {
         for (auto& e : src[p]) s += e.second;
         int o = m.pi_start[p];
         for (auto& e : src[p]) { m.pi_src[o] = e.first; m.pi_w[o] = e.second / s; ++o; }
+    }
+    m.pc_start.assign(m.n_points + 1, 0);
+    for (size_t k = 0; k < m.cell_pt.size(); ++k) m.pc_start[m.cell_pt[k] + 1]++;
+    for (int p = 0; p < m.n_points; ++p) m.pc_start[p + 1] += m.pc_start[p];
+    m.pc_slot.resize(m.cell_pt.size());
+    {
+        std::vector<int> fill(m.pc_start.begin(), m.pc_start.end() - 1);
+        for (int c = 0; c < nc; ++c)
+            for (int q = 0; q < 8; ++q) m.pc_slot[fill[m.cell_pt[8 * size_t(c) + q]]++] = 9 * c + 1 + q;
     }
     return m;
 }

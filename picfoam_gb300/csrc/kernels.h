@@ -6,7 +6,7 @@
 namespace pgd {
 
 cudaError_t move_fp64_set_tables(const TetConst& t, const PatchConst& p);
-cudaError_t move_fp32_set_tables(const TetConst& t, const PatchConst& p);
+cudaError_t move_fp32_set_tables(const Tables32& t);
 void launch_move_fp64(const MoveParams& P, int grid, cudaStream_t s);
 void launch_move_fp32(const MoveParams& P, int grid, cudaStream_t s);
 

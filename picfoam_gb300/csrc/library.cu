@@ -43,6 +43,7 @@ constexpr double kCl = 299792458.0;
 
 struct SpeciesBuf {
     long n = 0;      // used slots (removed particles keep tet = -1 until compaction)
+    long alive = 0;  // particles in the used slots that are not removed
     long cap = 0;
     int cur = 0;     // active buffer of the double-buffered store
     int32_t* tet[2] = {nullptr, nullptr};
@@ -75,7 +76,8 @@ struct picgpu_ctx {
     float *E32 = nullptr, *Ept32 = nullptr;
     double *cc_data = nullptr, *vtx_data = nullptr;
     long long *cc_fix = nullptr, *vtx_fix = nullptr;
-    unsigned long long* acc32 = nullptr;  // FP32 form: per-species fixed-point deposit
+    unsigned long long* acc9 = nullptr;   // FP32 form: per-species fixed-point deposit, 9 slots per cell
+    float4* Ec4 = nullptr;                // FP32 form: E per cell, centre + 8 corners
     double *qconv = nullptr, *sigma = nullptr, *grad_bc = nullptr;
     double *b = nullptr, *r = nullptr, *z = nullptr, *p[2] = {nullptr, nullptr}, *q = nullptr,
            *part = nullptr;
@@ -226,6 +228,49 @@ picgpu_status alloc_species(picgpu_ctx* c, int s, long cap) {
     return PICGPU_OK;
 }
 
+// Enlarge a species store, keeping its particles (in slot 0 of the new store).
+picgpu_status grow_species(picgpu_ctx* c, int s, long cap) {
+    SpeciesBuf& b = c->sp[s];
+    SpeciesBuf old = b;
+    const int k = old.cur;
+    SpeciesBuf nb;
+    nb.n = old.n;
+    nb.alive = old.alive;
+    nb.cap = cap;
+    picgpu_status st;
+    for (int q = 0; q < 2; ++q) {
+        if ((st = dalloc(c, &nb.tet[q], cap))) return st;
+        for (int a = 0; a < 3; ++a) {
+            if (c->mixed) {
+                if ((st = dalloc(c, &nb.y32[q][a], cap)) || (st = dalloc(c, &nb.u32[q][a], cap))) return st;
+            } else {
+                if ((st = dalloc(c, &nb.y64[q][a], cap)) || (st = dalloc(c, &nb.u64[q][a], cap))) return st;
+            }
+        }
+    }
+    const size_t n = size_t(old.n);
+    CK(cudaMemcpyAsync(nb.tet[0], old.tet[k], n * sizeof(int32_t), cudaMemcpyDeviceToDevice, c->stream));
+    for (int a = 0; a < 3; ++a) {
+        if (c->mixed) {
+            CK(cudaMemcpyAsync(nb.y32[0][a], old.y32[k][a], n * sizeof(float), cudaMemcpyDeviceToDevice, c->stream));
+            CK(cudaMemcpyAsync(nb.u32[0][a], old.u32[k][a], n * sizeof(float), cudaMemcpyDeviceToDevice, c->stream));
+        } else {
+            CK(cudaMemcpyAsync(nb.y64[0][a], old.y64[k][a], n * sizeof(double), cudaMemcpyDeviceToDevice, c->stream));
+            CK(cudaMemcpyAsync(nb.u64[0][a], old.u64[k][a], n * sizeof(double), cudaMemcpyDeviceToDevice, c->stream));
+        }
+    }
+    CK(cudaStreamSynchronize(c->stream));
+    for (int q = 0; q < 2; ++q) {
+        dfree(c, old.tet[q]);
+        for (int a = 0; a < 3; ++a) {
+            dfree(c, old.y64[q][a]); dfree(c, old.u64[q][a]); dfree(c, old.y32[q][a]); dfree(c, old.u32[q][a]);
+        }
+    }
+    b = nb;
+    b.cur = 0;
+    return PICGPU_OK;
+}
+
 pgd::DSpecies view(const picgpu_ctx* c, int s, int k) {
     const SpeciesBuf& b = c->sp[s];
     pgd::DSpecies v{};
@@ -276,7 +321,7 @@ pgd::MoveParams move_params(picgpu_ctx* c, int s, bool deposit_only) {
     P.vtx_fix = c->vtx_fix;
     P.qconv = c->qconv;
     P.p = view(c, s, c->sp[s].cur);
-    P.counters = c->counters;
+    P.counters = c->counters + s;
     P.charged = S.charge != 0.0;
     P.has_value = S.charge * S.weight != 0.0;
     P.qm_f = float(S.charge / S.mass);
@@ -285,9 +330,8 @@ pgd::MoveParams move_params(picgpu_ctx* c, int s, bool deposit_only) {
         P.B_f[a] = float(c->cfg.B[a]);
         P.centre_f[a] = float(c->m.mesh_centre[a]);
     }
-    const size_t stride = size_t(c->m.n_cells) + c->m.n_points;
-    P.acc_cc = c->acc32 ? c->acc32 + s * stride : nullptr;
-    P.acc_vtx = c->acc32 ? c->acc32 + s * stride + c->m.n_cells : nullptr;
+    P.acc9 = c->acc9 ? c->acc9 + size_t(s) * 9 * c->m.n_cells : nullptr;
+    P.Ec4 = c->Ec4;
     return P;
 }
 
@@ -297,22 +341,21 @@ picgpu_status zero_accumulators(picgpu_ctx* c) {
     CK(cudaMemsetAsync(c->cc_fix, 0, sizeof(long long) * c->m.n_cells, c->stream));
     CK(cudaMemsetAsync(c->vtx_fix, 0, sizeof(long long) * c->m.n_points, c->stream));
     if (c->mixed)
-        CK(cudaMemsetAsync(c->acc32, 0,
-                           sizeof(unsigned long long) * c->cfg.n_species * (size_t(c->m.n_cells) + c->m.n_points),
+        CK(cudaMemsetAsync(c->acc9, 0, sizeof(unsigned long long) * c->cfg.n_species * 9 * size_t(c->m.n_cells),
                            c->stream));
     return PICGPU_OK;
 }
 
 // Move (or deposit only) every species; counters land in c->counters.
 picgpu_status move_species(picgpu_ctx* c, bool deposit_only) {
-    CK(cudaMemsetAsync(c->counters, 0, sizeof(pgd::MoveCounters), c->stream));
+    CK(cudaMemsetAsync(c->counters, 0, sizeof(pgd::MoveCounters) * PICGPU_MAX_SPECIES, c->stream));
     for (int s = 0; s < c->cfg.n_species; ++s) {
         if (c->sp[s].n == 0) continue;
         const pgd::MoveParams P = move_params(c, s, deposit_only);
         const int grid = grid_for(c, c->sp[s].n);
         {
             PhaseScope ps(c, PICGPU_PHASE_MOVE);
-            if (c->mixed) pgd::launch_move_fp32(P, grid, c->stream);
+            if (c->mixed) pgd::launch_move_fp32(P, 5 * c->sm_count, c->stream);
             else pgd::launch_move_fp64(P, grid, c->stream);
         }
         c->launches++;
@@ -327,10 +370,11 @@ picgpu_status charge_update(picgpu_ctx* c) {
         pgd::SpeciesValues sv{};
         sv.n = c->cfg.n_species;
         for (int s = 0; s < sv.n; ++s)
-            sv.v[s] = std::ldexp(c->cfg.species[s].charge * c->cfg.species[s].weight, -30);
-        pgd::launch_charge_update_mixed(c->dm, c->cfg.charge_distribution == PICGPU_WEIGHTING_VOLUME, sv, c->acc32,
-                                        c->cfg.space_charge, c->rho, c->stream);
-        c->launches++;
+            sv.v[s] = std::ldexp(c->cfg.species[s].charge * c->cfg.species[s].weight, -pgd::kDepositBits);
+        const int vw = c->cfg.charge_distribution == PICGPU_WEIGHTING_VOLUME;
+        pgd::launch_charge_update_mixed(c->dm, vw, sv, c->acc9, c->vtx_data, c->cfg.space_charge, c->rho,
+                                        c->stream);
+        c->launches += vw ? 2 : 1;
         CK(cudaGetLastError());
         return PICGPU_OK;
     }
@@ -346,6 +390,10 @@ picgpu_status efield(picgpu_ctx* c) {
     PhaseScope ps(c, PICGPU_PHASE_EFIELD);
     pgd::launch_efield(c->dm, c->phi, c->grad_bc, c->E, c->Eb, c->Ept, c->E32, c->Ept32, c->stream);
     c->launches += c->dm.n_bfaces > 0 ? 4 : 3;
+    if (c->Ec4) {
+        pgd::launch_corner_E(c->dm, c->E, c->Ept, c->Ec4, c->stream);
+        c->launches++;
+    }
     CK(cudaGetLastError());
     return PICGPU_OK;
 }
@@ -359,6 +407,10 @@ picgpu_status set_applied_field(picgpu_ctx* c) {
     pgd::launch_to_float(c->E, c->E32, long(e.size()), c->stream);
     pgd::launch_to_float(c->Ept, c->Ept32, long(ep.size()), c->stream);
     c->launches += 2;
+    if (c->Ec4) {
+        pgd::launch_corner_E(c->dm, c->E, c->Ept, c->Ec4, c->stream);
+        c->launches++;
+    }
     CK(cudaStreamSynchronize(c->stream));
     return PICGPU_OK;
 }
@@ -428,12 +480,15 @@ picgpu_status ensure_scan(picgpu_ctx* c, long n) {
     return dalloc(c, &c->scan_buf, c->scan_cap);
 }
 
-// Drop removed particles (stable) in every species that lost some.
+// Drop removed particles (stable).  Removed slots (tet = -1) are skipped by
+// every kernel, so the store is compacted only once they exceed 1/64 of it
+// (or when forced).
 picgpu_status compact(picgpu_ctx* c, bool force) {
     for (int s = 0; s < c->cfg.n_species; ++s) {
         SpeciesBuf& B = c->sp[s];
         if (B.n == 0) continue;
-        if (!force && c->counters_host->absorbed == 0) continue;
+        const long dead = B.n - B.alive;
+        if (dead == 0 || (!force && dead < std::max<long>(B.n / 64, 4096))) continue;
         const long nblk = pgd::compact_blocks(B.n);
         picgpu_status st = ensure_scan(c, nblk + 1);
         if (st) return st;
@@ -442,52 +497,67 @@ picgpu_status compact(picgpu_ctx* c, bool force) {
         CK(pgd::compact_species(src, dst, B.n, c->mixed, c->scan_buf, &kept, c->stream));
         c->launches += 3;
         B.n = kept;
+        B.alive = kept;
         B.cur ^= 1;
     }
     return PICGPU_OK;
 }
 
 picgpu_status read_counters(picgpu_ctx* c) {
-    CK(cudaMemcpyAsync(c->counters_host, c->counters, sizeof(pgd::MoveCounters), cudaMemcpyDeviceToHost,
-                       c->stream));
+    CK(cudaMemcpyAsync(c->counters_host, c->counters, sizeof(pgd::MoveCounters) * c->cfg.n_species,
+                       cudaMemcpyDeviceToHost, c->stream));
     CK(cudaStreamSynchronize(c->stream));
     if (c->profiling) harvest_events(c);
     return PICGPU_OK;
 }
 
 void add_counters(picgpu_ctx* c, picgpu_step_stats* stats) {
-    if (!stats) return;
-    stats->tet_steps += (int64_t)c->counters_host->tet_steps;
-    stats->face_crossings += (int64_t)c->counters_host->faces;
-    stats->wall_hits += (int64_t)c->counters_host->walls;
+    for (int k = 0; k < c->cfg.n_species; ++k) {
+        const pgd::MoveCounters& m = c->counters_host[k];
+        c->sp[k].alive -= long(m.absorbed);
+        if (!stats) continue;
+        stats->tet_steps += (int64_t)m.tet_steps;
+        stats->face_crossings += (int64_t)m.faces;
+        stats->wall_hits += (int64_t)m.walls;
+        stats->n_absorbed[k] += (int64_t)m.absorbed;
+    }
 }
 
 void fill_counts(picgpu_ctx* c, picgpu_step_stats* stats) {
     if (!stats) return;
-    for (int s = 0; s < c->cfg.n_species; ++s) stats->n_particles[s] = c->sp[s].n;
+    for (int s = 0; s < c->cfg.n_species; ++s) stats->n_particles[s] = c->sp[s].alive;
 }
 
 // One PICCloud::evolve.
 picgpu_status one_step(picgpu_ctx* c, picgpu_step_stats* stats, bool fields) {
     picgpu_status s;
     if ((s = zero_accumulators(c))) return s;
-    // count removals per species: run species one at a time for the tally
-    std::vector<long> before(c->cfg.n_species);
-    for (int k = 0; k < c->cfg.n_species; ++k) before[k] = c->sp[k].n;
     if ((s = move_species(c, false))) return s;
     if ((s = read_counters(c))) return s;
-    if (c->counters_host->error) {
-        const int e = c->counters_host->error;
-        return bad(c, picgpu_status(e), e == PICGPU_SPEED_OF_LIGHT
-                                            ? "particle velocity reached the speed of light"
-                                            : "tracking exceeded track_max_steps for a particle");
-    }
+    int err = 0;
+    for (int k = 0; k < c->cfg.n_species; ++k) err = std::max(err, c->counters_host[k].error);
+    if (err)
+        return bad(c, picgpu_status(err), err == PICGPU_SPEED_OF_LIGHT
+                                              ? "particle velocity reached the speed of light"
+                                              : "tracking exceeded track_max_steps for a particle");
     add_counters(c, stats);
-    if (c->counters_host->absorbed) {
-        std::vector<long> alive_before(c->cfg.n_species);
-        if ((s = compact(c, false))) return s;
-        if (stats)
-            for (int k = 0; k < c->cfg.n_species; ++k) stats->n_absorbed[k] += before[k] - c->sp[k].n;
+    if (c->cfg.sort_interval > 0 && (c->step_index + 1) % c->cfg.sort_interval == 0) {
+        // cell re-sort (keeps each block's particles in a short cell range)
+        PhaseScope ps(c, PICGPU_PHASE_SORT);
+        for (int k = 0; k < c->cfg.n_species; ++k) {
+            SpeciesBuf& B = c->sp[k];
+            if (B.n == 0) continue;
+            long kept = 0;
+            std::string msg;
+            const int e = pgd::sort_species(c->coll, c->dm, k, view(c, k, B.cur), view(c, k, B.cur ^ 1), B.n,
+                                            c->mixed, &kept, c->stream, &msg, &c->launches);
+            if (e) return bad(c, picgpu_status(e), msg);
+            B.n = kept;
+            B.alive = kept;
+            B.cur ^= 1;
+        }
+    } else if ((s = compact(c, false))) {
+        return s;
     }
     if (c->cfg.mcc.enabled || c->cfg.coulomb.enabled) {
         if ((s = pgd_collisions(c, stats))) return s;
@@ -505,6 +575,14 @@ picgpu_status one_step(picgpu_ctx* c, picgpu_step_stats* stats, bool fields) {
 
 // Collisions live in collide.cu; this bridge keeps the context private.
 picgpu_status pgd_collisions(picgpu_ctx* c, picgpu_step_stats* stats) {
+    // room for MCC secondaries: at least an eighth of the population free
+    for (int s = 0; s < c->cfg.n_species; ++s) {
+        const long need = c->sp[s].n + std::max<long>(c->sp[s].n / 8, 4096);
+        if (need > c->sp[s].cap) {
+            const picgpu_status g = grow_species(c, s, need + need / 2);
+            if (g) return g;
+        }
+    }
     pgd::CollideArgs a{};
     a.m = c->dm;
     a.cfg = &c->cfg;
@@ -513,26 +591,35 @@ picgpu_status pgd_collisions(picgpu_ctx* c, picgpu_step_stats* stats) {
     a.mixed = c->mixed;
     for (int s = 0; s < c->cfg.n_species; ++s) {
         a.sp[s] = view(c, s, c->sp[s].cur);
-        a.alt[s] = view(c, s, c->sp[s].cur ^ 1);
         a.n[s] = c->sp[s].n;
         a.cap[s] = c->sp[s].cap;
     }
-    a.cc_data = c->cc_data;
-    a.vtx_data = c->vtx_data;
-    a.cc_fix = c->cc_fix;
-    a.vtx_fix = c->vtx_fix;
-    a.fix_scale = c->fix_scale;
     a.stream = c->stream;
     int64_t counts[8] = {};
     long newn[PICGPU_MAX_SPECIES] = {};
     int swapped[PICGPU_MAX_SPECIES] = {};
     std::string msg;
-    const int st = pgd::run_collisions(c->coll, a, counts, newn, swapped, &msg, &c->launches, nullptr);
-    if (st) return bad(c, picgpu_status(st), msg);
-    for (int s = 0; s < c->cfg.n_species; ++s) {
-        c->sp[s].n = newn[s];
-        if (swapped[s]) c->sp[s].cur ^= 1;
+    picgpu_status st;
+    {
+        PhaseScope ps(c, c->cfg.mcc.enabled ? PICGPU_PHASE_MCC : PICGPU_PHASE_COULOMB);
+        st = picgpu_status(pgd::run_collisions(c->coll, a, counts, newn, swapped, &msg, &c->launches, nullptr));
     }
+    if (st) return bad(c, st, msg);
+    for (int s = 0; s < c->cfg.n_species; ++s) {
+        const long old = c->sp[s].n;
+        c->sp[s].n = newn[s];
+        c->sp[s].alive += newn[s] - old;
+        if (newn[s] > old) {
+            // deposit the secondaries created this step (calculateFields sees
+            // every parcel, PICCloud.C:616-660)
+            pgd::MoveParams P = move_params(c, s, true);
+            P.first = int(old);
+            if (c->mixed) pgd::launch_move_fp32(P, 5 * c->sm_count, c->stream);
+            else pgd::launch_move_fp64(P, grid_for(c, newn[s] - old), c->stream);
+            c->launches++;
+        }
+    }
+    CK(cudaGetLastError());
     if (stats) {
         stats->mcc_candidates += counts[0];
         stats->mcc_elastic += counts[1];
@@ -644,7 +731,26 @@ picgpu_status picgpu_create(const picgpu_mesh_desc* mesh, const picgpu_config* c
         c->pc.area[p] = m.patches[p].area;
     }
     CK(pgd::move_fp64_set_tables(c->tc, c->pc));
-    CK(pgd::move_fp32_set_tables(c->tc, c->pc));
+    {
+        // FP32 kernel tables: class-0 geometry (used when the mesh has one
+        // class) and the packed crossing codes
+        pgd::Tables32 t{};
+        for (int k = 0; k < 108; ++k) t.inv[k] = float(m.cls_tetinv[k]);
+        for (int k = 0; k < 18; ++k) t.normal[k] = float(m.cls_fnormal[k]);
+        for (int k = 0; k < 24; ++k) t.off[k] = float(m.cls_offset[k]);
+        auto enc = [](int nt, const int* src) {
+            unsigned code = unsigned(nt);
+            for (int j = 0; j < 4; ++j) code |= unsigned(src[j] < 0 ? 7 : src[j]) << (4 + 3 * j);
+            return code;
+        };
+        for (int tt = 0; tt < 12; ++tt) {
+            for (int i = 1; i < 4; ++i) t.inner[4 * tt + i] = enc(m.tt.inner_next[tt][i], m.tt.inner_src[tt][i]);
+            t.cross[tt] = enc(m.tt.cross_next[tt], m.tt.cross_src[tt]);
+            t.tri[tt] = unsigned(m.tt.tri[tt][0]) | unsigned(m.tt.tri[tt][1]) << 4 | unsigned(m.tt.tri[tt][2]) << 8;
+        }
+        for (size_t p = 0; p < m.patches.size(); ++p) t.kind[p] = m.patches[p].p.kind;
+        CK(pgd::move_fp32_set_tables(t));
+    }
     CK(pgd::fields_set_patches(c->pc));
     CK(pgd::collide_set_tables(c->tc));
 
@@ -715,6 +821,9 @@ picgpu_status picgpu_create(const picgpu_mesh_desc* mesh, const picgpu_config* c
     UP(Mdiag, Mdiag, double);
     UP(Moff, Moff, double);
     UP(dinv, dinv, double);
+    UP(pc_start, m.pc_start, int);
+    UP(pc_slot, m.pc_slot, int);
+    d.uniform = m.n_classes == 1;
 #undef UP
     (void)ip; (void)dp; (void)fp;
 
@@ -729,9 +838,13 @@ picgpu_status picgpu_create(const picgpu_mesh_desc* mesh, const picgpu_config* c
         (s = dalloc(c, &c->grad_bc, npa)) || (s = dalloc(c, &c->b, nc)) || (s = dalloc(c, &c->r, nc)) ||
         (s = dalloc(c, &c->z, nc)) || (s = dalloc(c, &c->p[0], nc)) || (s = dalloc(c, &c->p[1], nc)) ||
         (s = dalloc(c, &c->q, nc)) || (s = dalloc(c, &c->part, 3 * size_t(pgd::pcg_blocks(int(nc))) + 8)) ||
-        (s = dalloc(c, &c->st, 1)) || (s = dalloc(c, &c->counters, 1)) || (s = dalloc(c, &c->diag, 64)))
+        (s = dalloc(c, &c->st, 1)) || (s = dalloc(c, &c->counters, PICGPU_MAX_SPECIES)) ||
+        (s = dalloc(c, &c->diag, 64)))
         return s;
-    if (c->mixed && (s = dalloc(c, &c->acc32, size_t(cfg->n_species) * (nc + np)))) return s;
+    if (c->mixed && ((s = dalloc(c, &c->acc9, size_t(cfg->n_species) * 9 * nc)) ||
+                     (s = dalloc(c, &c->Ec4, 9 * nc))))
+        return s;
+    if (c->Ec4) CK(cudaMemset(c->Ec4, 0, 9 * nc * sizeof(float4)));
     CK(cudaMemset(c->phi, 0, nc * sizeof(double)));
     CK(cudaMemset(c->E, 0, 3 * nc * sizeof(double)));
     CK(cudaMemset(c->Ept, 0, 3 * np * sizeof(double)));
@@ -742,9 +855,9 @@ picgpu_status picgpu_create(const picgpu_mesh_desc* mesh, const picgpu_config* c
     CK(cudaMemset(c->grad_bc, 0, npa * sizeof(double)));
     CK(cudaMemset(c->st, 0, sizeof(pgd::PcgState)));
     CK(cudaMallocHost(&c->st_host, sizeof(pgd::PcgState)));
-    CK(cudaMallocHost(&c->counters_host, sizeof(pgd::MoveCounters)));
+    CK(cudaMallocHost(&c->counters_host, sizeof(pgd::MoveCounters) * PICGPU_MAX_SPECIES));
     std::memset(c->st_host, 0, sizeof(pgd::PcgState));
-    std::memset(c->counters_host, 0, sizeof(pgd::MoveCounters));
+    std::memset(c->counters_host, 0, sizeof(pgd::MoveCounters) * PICGPU_MAX_SPECIES);
     for (int sp = 0; sp < cfg->n_species; ++sp) {
         const long cap = std::max<long>(cfg->species[sp].capacity_hint, 1024);
         if ((s = alloc_species(c, sp, cap))) return s;
@@ -802,6 +915,7 @@ picgpu_status picgpu_set_particles(picgpu_ctx* c, int species, size_t n, const i
     }
     B.cur = 0;
     B.n = long(n);
+    B.alive = long(n);
     CK(cudaMemcpy(B.tet[0], tet, n * sizeof(int32_t), cudaMemcpyHostToDevice));
     std::vector<double> col(n);
     std::vector<float> colf(n);
@@ -824,7 +938,7 @@ picgpu_status picgpu_set_particles(picgpu_ctx* c, int species, size_t n, const i
 
 picgpu_status picgpu_count_particles(picgpu_ctx* c, int species, size_t* n) {
     if (!c || !n || species < 0 || species >= c->cfg.n_species) return PICGPU_INVALID_ARG;
-    *n = size_t(c->sp[species].n);
+    *n = size_t(c->sp[species].alive);
     return PICGPU_OK;
 }
 
@@ -962,6 +1076,10 @@ picgpu_status picgpu_set_field(picgpu_ctx* c, int which, const double* in, size_
     pgd::launch_to_float(c->E, c->E32, 3L * c->m.n_cells, c->stream);
     pgd::launch_to_float(c->Ept, c->Ept32, 3L * c->m.n_points, c->stream);
     c->launches += 2;
+    if (c->Ec4) {
+        pgd::launch_corner_E(c->dm, c->E, c->Ept, c->Ec4, c->stream);
+        c->launches++;
+    }
     CK(cudaStreamSynchronize(c->stream));
     return PICGPU_OK;
 }

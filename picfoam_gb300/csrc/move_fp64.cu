@@ -11,7 +11,7 @@ __constant__ PatchConst c_patch64;
 
 __global__ void __launch_bounds__(256) move_kernel_fp64(MoveParams P) {
     unsigned ts = 0, fc = 0, wl = 0, ab = 0;
-    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < P.n; i += gridDim.x * blockDim.x) {
+    for (int i = P.first + blockIdx.x * blockDim.x + threadIdx.x; i < P.n; i += gridDim.x * blockDim.x) {
         TrackTally td{0u, 0u, 0u, true, false, false};
         const bool alive = P.p.tet[i] >= 0;
         move_one<double>(P, c_tet64, c_patch64, i, td);

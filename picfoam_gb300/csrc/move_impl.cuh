@@ -383,24 +383,6 @@ __device__ __forceinline__ void deposit_add(const MoveParams& P, double* dst64, 
 }
 
 // ChargeDistribution::add for one particle at its end-of-step position.
-// FP32 form: the dimensionless weights y go to this species' 64-bit
-// fixed-point accumulators (2^-30 resolution); the charge update multiplies
-// by q w per species.  Integer sums are order-independent, so the FP32 form's
-// charge density is deterministic.
-__device__ __forceinline__ void deposit(const MoveParams& P, const TetConst& T, const PState<float>& s) {
-    if (!P.has_value) return;
-    constexpr float kScale = 1073741824.0f;
-    if (P.charge_distribution == PICGPU_WEIGHTING_CELL_AVERAGE) {
-        atomicAdd(P.acc_cc + s.cell, 1ull << 30);
-        return;
-    }
-    const int* cp = P.m.cell_pt + 8 * size_t(s.cell);
-    atomicAdd(P.acc_cc + s.cell, (unsigned long long)__float2uint_rn(s.y[0] * kScale));
-#pragma unroll
-    for (int i = 0; i < 3; ++i)
-        atomicAdd(P.acc_vtx + cp[T.tri[s.tet][i]], (unsigned long long)__float2uint_rn(s.y[i + 1] * kScale));
-}
-
 __device__ __forceinline__ void deposit(const MoveParams& P, const TetConst& T, const PState<double>& s) {
     const double value = P.value;
     if (value == 0.0) return;

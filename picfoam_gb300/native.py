@@ -10,7 +10,8 @@ import os
 from . import abi
 
 _HERE = os.path.dirname(os.path.abspath(__file__))
-LIB_PATH = os.path.join(_HERE, "_build", "libpicgpu.so")
+# PICGPU_LIB selects another build of the library (e.g. a variant build).
+LIB_PATH = os.environ.get("PICGPU_LIB") or os.path.join(_HERE, "_build", "libpicgpu.so")
 
 _lib = None
 
