@@ -134,7 +134,9 @@ typedef struct {
 } picgpu_species;
 
 /* Background gas (uniformBackground.C:36-127) and null-collision MCC
- * (ElectronNeutralCollisionModel.C:703-829) with List cross sections. */
+ * (ElectronNeutralCollisionModel.C:703-829) with List cross sections.  The
+ * gas_* fields describe the background gas of both the electron-neutral and
+ * the ion-neutral model. */
 #define PICGPU_MAX_XS_POINTS 1024
 typedef struct {
     int32_t enabled;           /* ElectronNeutralCollisionModel != none */
@@ -159,13 +161,36 @@ typedef struct {
     const double* xs_ionization;
 } picgpu_mcc;
 
+/* Null-collision MCC of ions against the background gas
+ * (IonNeutralCollisionModel.C:453-577): IsotropicScattering elastic
+ * (IonIsotropicScattering.C:103-143) and charge exchange (:419-426). */
+typedef struct {
+    int32_t enabled;           /* IonNeutralCollisionModel IsotropicScattering */
+    int32_t ion_species;       /* the ion of the background gas */
+    int32_t n_xs;
+    int32_t pad;
+    double  cx_threshold;      /* charge-exchange threshold [eV] */
+    double  sigma_v_max_init;  /* 0: FindMaximum */
+    double  find_max_energy;
+    double  find_energy_step;
+    const double* xs_energy;   /* [n_xs] eV, ascending */
+    const double* xs_elastic;  /* [n_xs] m^2 */
+    const double* xs_charge_exchange;
+} picgpu_ion_mcc;
+
 /* Binary Coulomb collisions (CoulombCollisionModel.C:241-309). */
+enum { PICGPU_PAIRING_NANBU_YONEMURA = 0, PICGPU_PAIRING_TAKIZUKA_ABE = 1 };
+enum { PICGPU_COLLIDE_NANBU = 0, PICGPU_COLLIDE_PEREZ = 1 };
 typedef struct {
     int32_t enabled;
-    int32_t pairing;           /* 0: NanbuYonemura, 1: TakizukaAbe */
-    int32_t collide;           /* 0: Nanbu */
+    int32_t pairing;           /* PICGPU_PAIRING_*; TakizukaAbe needs equal species weights */
+    int32_t collide;           /* PICGPU_COLLIDE_*: Nanbu, Perez (relativistic, s_max cap) */
     int32_t allow_intra;       /* allowIntraCollision */
-    double  coulomb_log;       /* fixed coulombLog (> 0); 0 not supported yet */
+    double  coulomb_log;       /* fixed coulombLog (> 0); 0: from the cell Debye length */
+    int32_t calculate_bmin;    /* calculateBmin: de Broglie floor of the impact parameter */
+    int32_t debye_drift;       /* Debye length: subtract the drift velocity */
+    int32_t weight_correction; /* 0: none, 1: Nanbu (NanbuCorrection.C:50-66) */
+    int32_t pad;
 } picgpu_coulomb;
 
 typedef struct {
@@ -191,6 +216,7 @@ typedef struct {
     int32_t pad0;
     uint64_t seed;
     picgpu_mcc mcc;
+    picgpu_ion_mcc ion_mcc;
     picgpu_coulomb coulomb;
 } picgpu_config;
 
@@ -209,6 +235,9 @@ typedef struct {
     int64_t mcc_excitation;
     int64_t mcc_ionization;
     int64_t coulomb_pairs;
+    int64_t ion_mcc_candidates;
+    int64_t ion_mcc_elastic;
+    int64_t ion_mcc_charge_exchange;
     double  floating_charge[PICGPU_MAX_BOXES + 6]; /* accumulated surface charge per patch [C] */
 } picgpu_step_stats;
 

@@ -73,7 +73,13 @@ struct Philox {
     }
 };
 
-enum : uint32_t { kStreamMcc = 1u << 28, kStreamCoulomb = 2u << 28, kStreamRemainder = 3u << 28 };
+enum : uint32_t {
+    kStreamMcc = 1u << 28,
+    kStreamCoulomb = 2u << 28,
+    kStreamRemainder = 3u << 28,
+    kStreamIonMcc = 4u << 28,
+    kStreamIonRemainder = 5u << 28,
+};
 
 // List cross section: interpolateXY (ListCrossSection.C:33-88): linear in
 // energy between the bracketing nodes, end values held outside the table.
@@ -129,6 +135,43 @@ inline std::string init_mcc(const picgpu_config& cfg, Tables& t, int n_cells,
     rem.resize(n_cells);
     for (int c = 0; c < n_cells; ++c) {
         Philox r(cfg.seed, kStreamRemainder, uint32_t(c), 0u);
+        rem[c] = r.uniform();
+    }
+    return "";
+}
+
+// Ion-neutral tables (elastic in el, charge exchange in ex) and the
+// FindMaximum search with the ion mass (IonNeutralCollisionModel.C:284-333);
+// remainders seeded U(0,1) (IonNeutralCollisionModel.C:199).
+inline std::string init_ion_mcc(const picgpu_config& cfg, Tables& t, int n_cells,
+                                std::vector<double>& svmax, std::vector<double>& rem) {
+    const picgpu_ion_mcc& m = cfg.ion_mcc;
+    if (m.n_xs < 2 || m.n_xs > PICGPU_MAX_XS_POINTS || !m.xs_energy || !m.xs_elastic || !m.xs_charge_exchange)
+        return "ion_mcc: cross-section tables missing";
+    if (m.ion_species < 0 || m.ion_species >= cfg.n_species) return "ion_mcc: ion species not set";
+    if (!(cfg.mcc.gas_density > 0) || !(cfg.mcc.gas_mass > 0))
+        return "ion_mcc: background gas (mcc.gas_*) not set";
+    t.e.assign(m.xs_energy, m.xs_energy + m.n_xs);
+    t.el.assign(m.xs_elastic, m.xs_elastic + m.n_xs);
+    t.ex.assign(m.xs_charge_exchange, m.xs_charge_exchange + m.n_xs);
+    t.iz.clear();
+    for (int i = 1; i < m.n_xs; ++i)
+        if (!(t.e[i] > t.e[i - 1])) return "ion_mcc: energies must ascend";
+    double sv = m.sigma_v_max_init;
+    if (!(sv > 0)) {
+        const double mi = cfg.species[m.ion_species].mass;
+        const double emax = m.find_max_energy > 0 ? m.find_max_energy : t.e.back();
+        const double step = m.find_energy_step > 0 ? m.find_energy_step : emax / 100000.0;
+        sv = 0.0;
+        for (double eV = 0.0; eV < emax; eV += step) {
+            const double q = interp_xs(eV, t.e, t.el) + interp_xs(eV, t.e, t.ex);
+            sv = std::fmax(sv, std::sqrt(2.0 * kEcharge * eV / mi) * q);
+        }
+    }
+    svmax.assign(n_cells, sv);
+    rem.resize(n_cells);
+    for (int c = 0; c < n_cells; ++c) {
+        Philox r(cfg.seed, kStreamIonRemainder, uint32_t(c), 0u);
         rem[c] = r.uniform();
     }
     return "";

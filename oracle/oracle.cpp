@@ -123,10 +123,11 @@ struct Oracle {
     long long step_index = 0;
     // collision state
     std::vector<double> svmax, remainder;
+    std::vector<double> isvmax, iremainder;  // ion-neutral
     int last_pcg_iter = 0;
     double last_res_l2 = 0, last_res_of = 0;
     picgpu_step_stats acc{};
-    ocoll::Tables xs;
+    ocoll::Tables xs, ixs;
 };
 
 // ------------------------------------------------------------ pushers -----
@@ -797,6 +798,7 @@ int move_all(Oracle& o, picgpu_step_stats* st) {
 
 // ------------------------------------------------------------ collisions --
 constexpr double kBoltzmann = 1.380649e-23;
+constexpr double kPlanck = 6.62607015e-34;
 
 V3 normal3(ocoll::Philox& r) {
     const double a = r.normal(), b = r.normal(), c = r.normal();
@@ -822,6 +824,80 @@ void nanbu_scatter(double eV, V3& Ue, V3& Un, double mE, double mN, ocoll::Philo
     const V3 d = add(smul(1.0 - cosChi, g), smul(sinChi, h));
     Ue = sub(Ue, smul(mN / (mN + mE), d));
     Un = add(Un, smul(mE / (mN + mE), d));
+}
+
+// Relativistic centre-of-momentum frame of two particles and the rotation of
+// the momentum in it by (chi, eps), shared by
+// RelativisticElectronNeutralCollision.C:161-242 and PerezRelativisticCollision.C:60-192.
+struct CoM {
+    double gP, gQ, gc, gcv, gPc, gQc, mag_pc;
+    V3 vc, pc;
+};
+
+bool com_frame(const V3& UP, const V3& UQ, double mP, double mQ, CoM& f) {
+    const double aP = magv(UP) / kC, aQ = magv(UQ) / kC;
+    f.gP = 1.0 / std::sqrt(1.0 - aP * aP);
+    f.gQ = 1.0 / std::sqrt(1.0 - aQ * aQ);
+    const V3 pP = smul(mP * f.gP, UP);
+    const V3 pQ = smul(mQ * f.gQ, UQ);
+    f.vc = sdiv(add(pP, pQ), mP * f.gP + mQ * f.gQ);
+    const double vc2 = dotv(f.vc, f.vc);
+    if (vc2 == 0.0) {
+        f.gc = 1.0;
+        f.gcv = 0.5;
+        f.pc = pP;
+        f.gPc = f.gP;
+        f.gQc = f.gQ;
+    } else {
+        f.gc = 1.0 / std::sqrt(1.0 - vc2 / (kC * kC));
+        f.gcv = (f.gc - 1.0) / vc2;
+        f.pc = add(pP, smul((f.gcv * dotv(f.vc, UP) - f.gc) * mP * f.gP, f.vc));
+        f.gPc = (1.0 - dotv(f.vc, UP) / (kC * kC)) * f.gP * f.gc;
+        f.gQc = (1.0 - dotv(f.vc, UQ) / (kC * kC)) * f.gQ * f.gc;
+    }
+    f.mag_pc = magv(f.pc);
+    return f.mag_pc != 0.0;
+}
+
+void com_rotate(const CoM& f, double cosChi, double sinChi, double eps, double mP, double mQ, V3& UP, V3& UQ) {
+    const double sce = sinChi * std::cos(eps), sse = sinChi * std::sin(eps);
+    const V3& p = f.pc;
+    const double pperp = std::sqrt(p.x * p.x + p.y * p.y);
+    V3 np;
+    if (pperp > 1.e-10 * f.mag_pc) {
+        const double ip = 1.0 / pperp;
+        np = v3((p.x * p.z * sce - p.y * f.mag_pc * sse) * ip + p.x * cosChi,
+                (p.y * p.z * sce + p.x * f.mag_pc * sse) * ip + p.y * cosChi, -pperp * sce + p.z * cosChi);
+    } else {
+        np = v3(f.mag_pc * sce, f.mag_pc * sse, f.mag_pc * cosChi);
+    }
+    const V3 npP = add(np, smul(f.gcv * dotv(f.vc, np) + mP * f.gPc * f.gc, f.vc));
+    const double aP = magv(npP) / (mP * kC);
+    const double ngP = std::sqrt(1.0 + aP * aP);
+    const V3 mnp = smul(-1.0, np);
+    const V3 npQ = add(mnp, smul(f.gcv * dotv(f.vc, mnp) + mQ * f.gQc * f.gc, f.vc));
+    const double aQ = magv(npQ) / (mQ * kC);
+    const double ngQ = std::sqrt(1.0 + aQ * aQ);
+    UP = sdiv(npP, mP * ngP);
+    UQ = sdiv(npQ, mQ * ngQ);
+}
+
+// RelativisticElectronNeutralCollision::updateVelocity (:161-242): draws
+// cos(chi) first, then the azimuth.
+void relativistic_scatter(double eV, V3& Ue, V3& Un, double mE, double mN, ocoll::Philox& r) {
+    CoM f;
+    if (!com_frame(Ue, Un, mE, mN, f)) return;
+    double cosChi;
+    if (eV < 1e-30) cosChi = 1.0;
+    else cosChi = 1.0 / eV * (eV + 2.0 - 2.0 * std::pow(1.0 + eV, r.uniform()));
+    const double sinChi = std::sqrt(1.0 - cosChi * cosChi);
+    const double eps = 2.0 * kPi * r.uniform();
+    com_rotate(f, cosChi, sinChi, eps, mE, mN, Ue, Un);
+}
+
+void electron_scatter(const Oracle& o, double eV, V3& Ue, V3& Un, double mE, double mN, ocoll::Philox& r) {
+    if (o.cfg.mcc.scatter == 1) relativistic_scatter(eV, Ue, Un, mE, mN, r);
+    else nanbu_scatter(eV, Ue, Un, mE, mN, r);
 }
 
 // ElectronNeutralCollisionModel::performBackgroundCollisions
@@ -866,12 +942,12 @@ void mcc_background(Oracle& o, std::vector<std::vector<int>>& occ, picgpu_step_s
             const double R = r.uniform();
             if (R <= Qel / sigmaT) {
                 nel++;
-                nanbu_scatter(eV, e.U, Un, me, mg, r);
+                electron_scatter(o, eV, e.U, Un, me, mg, r);
             } else if (eV >= mc.ex_threshold && R <= (Qel + Qex) / sigmaT) {
                 nex++;
                 e.U = smul(std::sqrt(1.0 - mc.ex_threshold / eV), e.U);
                 eV -= mc.ex_threshold;
-                nanbu_scatter(eV, e.U, Un, me, mg, r);
+                electron_scatter(o, eV, e.U, Un, me, mg, r);
             } else if (eV >= mc.iz_threshold && R <= Qt / sigmaT) {
                 const double th = mc.iz_threshold;
                 const double E0 = 2.0 - 100.0 / (eV + 10.0);
@@ -885,7 +961,7 @@ void mcc_background(Oracle& o, std::vector<std::vector<int>>& occ, picgpu_step_s
                 eV -= (th + Ep);
                 const double wE = o.cfg.species[es].weight, wN = mc.gas_weight;
                 const double wEwN = wE / wN, wNwE = 1.0 / wEwN;
-                nanbu_scatter(eV, e.U, Un, me, mg, r);
+                electron_scatter(o, eV, e.U, Un, me, mg, r);
                 const double rndU = r.uniform();
                 bool created = false;
                 if (rndU <= wEwN && mc.create_ion && mc.ion_species >= 0) {
@@ -900,7 +976,7 @@ void mcc_background(Oracle& o, std::vector<std::vector<int>>& occ, picgpu_step_s
                     const double sp = std::sqrt(2.0 * Ep * ocoll::kEcharge / me);
                     ne.U = smul(sp, sdiv(preUe, magv(preUe)));
                     V3 un2 = preUn;
-                    nanbu_scatter(Ep, ne.U, un2, me, mg, r);
+                    electron_scatter(o, Ep, ne.U, un2, me, mg, r);
                     new_e.push_back(ne);
                 }
                 if (created) niz++;
@@ -918,7 +994,69 @@ void mcc_background(Oracle& o, std::vector<std::vector<int>>& occ, picgpu_step_s
     }
 }
 
-// NanbuCollision::calculate_cosChi (NanbuCollision.C:137-161)
+// IonNeutralCollisionModel::performBackgroundCollisions
+// (IonNeutralCollisionModel.C:453-577): IsotropicScattering elastic
+// (IonIsotropicScattering.C:103-143) or charge exchange (:419-426).
+void ion_mcc_background(Oracle& o, std::vector<std::vector<int>>& occ, picgpu_step_stats* st) {
+    const picgpu_ion_mcc& im = o.cfg.ion_mcc;
+    const picgpu_mcc& gas = o.cfg.mcc;
+    const int is = im.ion_species;
+    const double mi = o.cfg.species[is].mass;
+    const double mg = gas.gas_mass;
+    const double dt = o.cfg.dt;
+    const double vth = std::sqrt(kBoltzmann * gas.gas_temperature / mg);
+    auto& ions = o.cloud[is];
+    long long cand = 0, nel = 0, ncx = 0;
+    for (int c = 0; c < o.m.n_cells; ++c) {
+        const std::vector<int>& list = occ[c];
+        const long nI = long(list.size());
+        const double sv = o.isvmax[c];
+        const double coll = o.iremainder[c] + double(nI) * gas.gas_density * sv * dt;
+        const long nC = long(coll);
+        o.iremainder[c] = coll - double(nC);
+        if (nC == 0 || nI == 0) continue;
+        ocoll::Philox r(o.cfg.seed, ocoll::kStreamIonMcc, uint32_t(c), uint32_t(o.step_index));
+        cand += nC;
+        for (long i = 0; i < nC; ++i) {
+            long j = long(r.uniform() * double(nI));
+            if (j >= nI) j = nI - 1;
+            Parcel& p = ions[list[j]];
+            const V3 nrm = normal3(r);
+            V3 Un = v3(vth * nrm.x + gas.gas_velocity[0], vth * nrm.y + gas.gas_velocity[1],
+                       vth * nrm.z + gas.gas_velocity[2]);
+            const double cR = magv(sub(p.U, Un));
+            const double gamma = 1.0 / std::sqrt(1.0 - (cR * cR) / (kC * kC));
+            const double eV = (gamma - 1.0) * mi * kC * kC / ocoll::kEcharge;
+            const double sigmaT = sv / cR;
+            const double Qel = ocoll::interp_xs(eV, o.ixs.e, o.ixs.el);
+            const double Qcx = ocoll::interp_xs(eV, o.ixs.e, o.ixs.ex);
+            const double Qt = Qel + Qcx;
+            if (Qt * cR > o.isvmax[c]) o.isvmax[c] = Qt * cR;
+            const double R = r.uniform();
+            if (R <= Qel / sigmaT) {
+                nel++;
+                // isotropic scattering in the centre-of-mass frame
+                const V3 Ucm = sdiv(add(smul(mi, p.U), smul(mg, Un)), mi + mg);
+                const double cosT = 2.0 * r.uniform() - 1.0;
+                const double sinT = std::sqrt(1.0 - cosT * cosT);
+                const double phi = 2.0 * kPi * r.uniform();
+                const V3 rel = smul(cR, v3(cosT, sinT * std::cos(phi), sinT * std::sin(phi)));
+                p.U = add(Ucm, sdiv(smul(mg, rel), mi + mg));
+            } else if (eV >= im.cx_threshold && R <= Qt / sigmaT) {
+                ncx++;
+                p.U = Un;  // identity swap with the background neutral
+            }
+        }
+    }
+    if (st) {
+        st->ion_mcc_candidates += cand;
+        st->ion_mcc_elastic += nel;
+        st->ion_mcc_charge_exchange += ncx;
+    }
+}
+
+// NanbuCollision::calculate_cosChi (NanbuCollision.C:137-161), also
+// PerezRelativisticCollision::calculate_cosChi.
 double nanbu_cos_chi(double s, ocoll::Philox& r) {
     double U = r.uniform();
     if (s < 0.1) {
@@ -937,15 +1075,31 @@ double nanbu_cos_chi(double s, ocoll::Philox& r) {
     return 2.0 * U - 1.0;
 }
 
-// NanbuCollision::collide (NanbuCollision.C:60-135), fixed coulombLog.
-void nanbu_collide(Oracle& o, Parcel& P, int sp, Parcel& Q, int sq, double nP, double nQ,
+// NanbuWeightCorrectionModel::correctVelocity (NanbuCorrection.C:50-66): one
+// draw; each partner keeps its new velocity with probability w_other/w_self.
+void weight_correct(Oracle& o, Parcel& P, int sp, Parcel& Q, int sq, const V3& preP, const V3& preQ,
+                    ocoll::Philox& r) {
+    if (o.cfg.coulomb.weight_correction != 1) return;
+    const double wP = o.cfg.species[sp].weight, wQ = o.cfg.species[sq].weight;
+    const double u = r.uniform();
+    if (u > wP / wQ) Q.U = preQ;
+    if (u > wQ / wP) P.U = preP;
+}
+
+// NanbuCollision::collide (NanbuCollision.C:60-135).
+void nanbu_collide(Oracle& o, Parcel& P, int sp, Parcel& Q, int sq, double lD, double nP, double nQ,
                    double nPQ, ocoll::Philox& r) {
     const double mP = o.cfg.species[sp].mass, qP = o.cfg.species[sp].charge;
     const double mQ = o.cfg.species[sq].mass, qQ = o.cfg.species[sq].charge;
     const double reMass = mP * mQ / (mP + mQ);
     const V3 g = sub(P.U, Q.U);
     const double gm = magv(g);
-    const double cl = o.cfg.coulomb.coulomb_log;
+    double cl = o.cfg.coulomb.coulomb_log;
+    if (cl == 0.0) {
+        double b0 = qP * qQ / (2.0 * kPi * kEps0 * reMass * gm * gm);
+        if (o.cfg.coulomb.calculate_bmin) b0 = std::fmax(kPlanck / (2.0 * (gm * reMass)), std::fabs(b0));
+        cl = std::fmax(2.0, 0.5 * std::log(1.0 + (lD * lD) / (b0 * b0)));
+    }
     const double A = qP * qQ / (kEps0 * reMass);
     const double s = cl / (4.0 * kPi) * (A * A) * (nQ * nP / nPQ) * (1.0 / (gm * gm * gm)) * o.cfg.dt;
     const double cosChi = nanbu_cos_chi(s, r);
@@ -956,8 +1110,50 @@ void nanbu_collide(Oracle& o, Parcel& P, int sp, Parcel& Q, int sq, double nP, d
     const V3 h = v3(gp * ce, -1.0 * (g.y * g.x * ce + gm * g.z * se) / gp,
                     -1.0 * (g.z * g.x * ce - gm * g.y * se) / gp);
     const V3 d = add(smul(1.0 - cosChi, g), smul(sinChi, h));
+    const V3 preP = P.U, preQ = Q.U;
     P.U = sub(P.U, smul(mQ / (mP + mQ), d));
     Q.U = add(Q.U, smul(mP / (mP + mQ), d));
+    weight_correct(o, P, sp, Q, sq, preP, preQ, r);
+}
+
+// PerezRelativisticCollision::collide (PerezRelativisticCollision.C:60-192).
+void perez_collide(Oracle& o, Parcel& P, int sp, Parcel& Q, int sq, double lD, double nP, double nQ,
+                   double nPQ, ocoll::Philox& r) {
+    const double mP = o.cfg.species[sp].mass, qP = o.cfg.species[sp].charge;
+    const double mQ = o.cfg.species[sq].mass, qQ = o.cfg.species[sq].charge;
+    CoM f;
+    if (!com_frame(P.U, Q.U, mP, mQ, f)) return;
+    const double mgsum = mP * f.gP + mQ * f.gQ;
+    const double c2 = kC * kC;
+    const double pc2 = f.mag_pc * f.mag_pc;
+    double cl = o.cfg.coulomb.coulomb_log;
+    if (cl == 0.0) {
+        double b0 = qP * qQ / (4.0 * kPi * kEps0 * c2) * f.gc / mgsum * (1.0 + mP * f.gPc * mQ * f.gQc * c2 / pc2);
+        if (o.cfg.coulomb.calculate_bmin) b0 = std::fmax(kPlanck / (2 * f.mag_pc), std::fabs(b0));
+        cl = std::fmax(2.0, 0.5 * std::log(1.0 + (lD * lD) / (b0 * b0)));
+    }
+    const double t1 = f.gc * f.mag_pc / mgsum;
+    const double t2b = 1.0 + mP * f.gPc * mQ * f.gQc * c2 / pc2;
+    const double t2 = t2b * t2b;
+    const double qq = qP * qQ;
+    double s = (nP * nQ / nPQ) * o.cfg.dt * cl * (qq * qq) /
+               (4.0 * kPi * (kEps0 * kEps0) * (c2 * c2) * mP * f.gP * mQ * f.gQ) * t1 * t2;
+    const double v_rel = f.mag_pc * mgsum / (mP * f.gPc * mQ * f.gQc * f.gc);
+    const double s_max = std::pow(4.0 * kPi / 3.0, 1.0 / 3.0) * (nP * nQ / nPQ) * o.cfg.dt * (mP + mQ) /
+                         std::fmax(mP * std::pow(nP, 2.0 / 3.0), mQ * std::pow(nQ, 2.0 / 3.0)) * v_rel;
+    s = std::fmin(s_max, s);
+    const double cosChi = nanbu_cos_chi(s, r);
+    const double sinChi = std::sqrt(1.0 - cosChi * cosChi);
+    const double eps = 2.0 * kPi * r.uniform();
+    const V3 preP = P.U, preQ = Q.U;
+    com_rotate(f, cosChi, sinChi, eps, mP, mQ, P.U, Q.U);
+    weight_correct(o, P, sp, Q, sq, preP, preQ, r);
+}
+
+void coulomb_collide(Oracle& o, Parcel& P, int sp, Parcel& Q, int sq, double lD, double nP, double nQ,
+                     double nPQ, ocoll::Philox& r) {
+    if (o.cfg.coulomb.collide == 1) perez_collide(o, P, sp, Q, sq, lD, nP, nQ, nPQ, r);
+    else nanbu_collide(o, P, sp, Q, sq, lD, nP, nQ, nPQ, r);
 }
 
 void shuffle(std::vector<int>& a, ocoll::Philox& r) {
@@ -968,15 +1164,51 @@ void shuffle(std::vector<int>& a, ocoll::Philox& r) {
     }
 }
 
-// NanbuYonemuraPairing::pairANDcollide (NanbuYonemuraPairing.C:56-325)
-void coulomb_ny(Oracle& o, std::vector<std::vector<std::vector<int>>>& occ, picgpu_step_stats* st) {
+// CoulombCollisionModel::debyeLength (CoulombCollisionModel.C:249-309) over
+// the colliding species.
+double debye_length(const Oracle& o, const std::vector<int>& charged,
+                    std::vector<std::vector<std::vector<int>>>& occ, int c) {
+    double debye = 0.0, n_max = 0.0;
+    for (int s : charged) {
+        const double mass = o.cfg.species[s].mass, w = o.cfg.species[s].weight, q = o.cfg.species[s].charge;
+        double vSqr = 0.0, n = 0.0, charge = 0.0;
+        V3 v = v3(0, 0, 0);
+        for (int idx : occ[s][c]) {
+            const Parcel& p = o.cloud[s][idx];
+            vSqr += dotv(p.U, p.U) * w;
+            charge += q * w;
+            v = add(v, smul(w, p.U));
+            n += w;
+        }
+        if (n <= 0.0) continue;
+        v = sdiv(v, n);
+        charge /= n;
+        vSqr /= n;
+        n /= o.m.vol[c];
+        if (n > n_max) n_max = n;
+        const double vd2 = o.cfg.coulomb.debye_drift ? dotv(v, v) : 0.0;
+        const double T = mass / (3.0 * kBoltzmann) * (vSqr - vd2);
+        if (T <= 0.0) continue;
+        debye += n * charge * charge / kEps0 * 1.0 / (T * kBoltzmann);
+    }
+    if (debye <= 0.0) return 0.0;
+    const double r_min = std::pow(4.0 * kPi * n_max / 3.0, -1.0 / 3.0);
+    return std::fmax(r_min, std::sqrt(1 / debye));
+}
+
+// NanbuYonemuraPairing::pairANDcollide (NanbuYonemuraPairing.C:56-325) and
+// TakizukaAbePairing::pairANDcollide (TakizukaAbePairing.C:60-341).
+void coulomb_pairs(Oracle& o, std::vector<std::vector<std::vector<int>>>& occ, picgpu_step_stats* st) {
     std::vector<int> charged;
     for (int s = 0; s < o.cfg.n_species; ++s)
         if (o.cfg.species[s].charge != 0.0 && o.cfg.species[s].solve_movement) charged.push_back(s);
+    const bool ta = o.cfg.coulomb.pairing == 1;
+    const bool need_debye = o.cfg.coulomb.coulomb_log == 0.0;
     long long pairs = 0;
     for (int c = 0; c < o.m.n_cells; ++c) {
         const double V = o.m.vol[c];
         ocoll::Philox r(o.cfg.seed, ocoll::kStreamCoulomb, uint32_t(c), uint32_t(o.step_index));
+        const double lD = need_debye ? debye_length(o, charged, occ, c) : 0.0;
         for (size_t i = 0; i < charged.size(); ++i) {
             for (size_t jj = charged.size(); jj-- > 0;) {
                 if (jj < i) break;
@@ -987,43 +1219,70 @@ void coulomb_ny(Oracle& o, std::vector<std::vector<std::vector<int>>>& occ, picg
                 const double wA = o.cfg.species[a].weight, wB = o.cfg.species[b].weight;
                 const double sA = double(nA) * wA;
                 const double sB = a != b ? double(nB) * wB : 0.0;
+                auto& ca = o.cloud[a];
+                auto& cb = o.cloud[b];
                 if (a == b && nA > 1) {
                     if (!o.cfg.coulomb.allow_intra) continue;
                     std::vector<int> sel(nA);
                     for (long k = 0; k < nA; ++k) sel[k] = int(k);
                     shuffle(sel, r);
+                    if (ta) {
+                        const double n = double(nA) * wA / V;
+                        if (nA % 2 != 0) {
+                            const double n12 = (double(nA) + 3.0) * wA / V;
+                            Parcel& P = ca[LA[sel[0]]];
+                            Parcel& Q = ca[LA[sel[1]]];
+                            Parcel& R = ca[LA[sel[2]]];
+                            coulomb_collide(o, P, a, Q, a, lD, n, n, n12, r);
+                            coulomb_collide(o, Q, a, R, a, lD, n, n, n12, r);
+                            coulomb_collide(o, P, a, R, a, lD, n, n, n12, r);
+                            for (long x = 3; x < nA - 1; x += 2)
+                                coulomb_collide(o, ca[LA[sel[x]]], a, ca[LA[sel[x + 1]]], a, lD, n, n, n12, r);
+                            pairs += 2 + nA / 2;
+                        } else {
+                            for (long x = 0; x < nA - 1; x += 2)
+                                coulomb_collide(o, ca[LA[sel[x]]], a, ca[LA[sel[x + 1]]], a, lD, n, n, n, r);
+                            pairs += nA / 2;
+                        }
+                        continue;
+                    }
                     const double n = sA / V;
-                    auto& cl = o.cloud[a];
                     if (nA % 2 != 0) {
                         double nAA = 2.0 * wA;  // the extra (last, first) pair
                         for (long x = 0; x < nA - 2; x += 2) nAA += 2.0 * wA;
                         const double n12 = nAA / V;
                         for (long x = 0; x < nA - 2; x += 2)
-                            nanbu_collide(o, cl[LA[sel[x]]], a, cl[LA[sel[x + 1]]], a, n, n, n12, r);
-                        nanbu_collide(o, cl[LA[sel[nA - 1]]], a, cl[LA[sel[0]]], a, n, n, n12, r);
+                            coulomb_collide(o, ca[LA[sel[x]]], a, ca[LA[sel[x + 1]]], a, lD, n, n, n12, r);
+                        coulomb_collide(o, ca[LA[sel[nA - 1]]], a, ca[LA[sel[0]]], a, lD, n, n, n12, r);
                         pairs += 1 + nA / 2;
                     } else {
                         double nAA = 0.0;
                         for (long x = 0; x < nA - 1; x += 2) nAA += 2.0 * wA;
                         const double n12 = nAA / V;
                         for (long x = 0; x < nA - 1; x += 2)
-                            nanbu_collide(o, cl[LA[sel[x]]], a, cl[LA[sel[x + 1]]], a, n, n, n12, r);
+                            coulomb_collide(o, ca[LA[sel[x]]], a, ca[LA[sel[x + 1]]], a, lD, n, n, n12, r);
                         pairs += nA / 2;
                     }
                 } else if (a != b && std::min(nA, nB) != 0) {
-                    auto& ca = o.cloud[a];
-                    auto& cb = o.cloud[b];
                     const double wmin = std::fmin(wA, wB);
                     if (nA == nB) {
-                        const double nP = sA / V, nQ = sB / V;
                         std::vector<int> sel(nA);
                         for (long k = 0; k < nA; ++k) sel[k] = int(k);
                         shuffle(sel, r);
-                        double nAB = 0.0;
-                        for (long k = 0; k < nA; ++k) nAB += wmin;
-                        const double nPQ = nAB / V;
+                        double nP, nQ, nPQ;
+                        if (ta) {
+                            nP = double(nA) * wA / V;
+                            nQ = double(nB) * wA / V;
+                            nPQ = nP;
+                        } else {
+                            nP = sA / V;
+                            nQ = sB / V;
+                            double nAB = 0.0;
+                            for (long k = 0; k < nA; ++k) nAB += wmin;
+                            nPQ = nAB / V;
+                        }
                         for (long k = 0; k < nA; ++k)
-                            nanbu_collide(o, ca[LA[sel[k]]], a, cb[LB[sel[nA - k - 1]]], b, nP, nQ, nPQ, r);
+                            coulomb_collide(o, ca[LA[sel[k]]], a, cb[LB[sel[nA - k - 1]]], b, lD, nP, nQ, nPQ, r);
                         pairs += nA;
                     } else {
                         const int minS = nA < nB ? a : b, maxS = nA > nB ? a : b;
@@ -1034,17 +1293,48 @@ void coulomb_ny(Oracle& o, std::vector<std::vector<std::vector<int>>>& occ, picg
                         for (long k = 0; k < nMax; ++k) { smax[k] = int(k); if (k < nMin) smin[k] = int(k); }
                         shuffle(smin, r);
                         shuffle(smax, r);
+                        auto& cmin = o.cloud[minS];
+                        auto& cmax = o.cloud[maxS];
+                        if (ta) {
+                            const double nMinS = double(nMin) * wA / V, nMaxS = double(nMax) * wA / V;
+                            const long delta = nMax / nMin;
+                            const double delta_r = double(nMax % nMin) / double(nMin);
+                            const long g1min = long(delta_r * double(nMin));
+                            const long g1max = long(double(delta + 1) * delta_r * double(nMin));
+                            const long g2min = long((1.0 - delta_r) * double(nMin));
+                            const long g2max = long(double(delta) * (1.0 - delta_r) * double(nMin));
+                            long s1 = 0, s2 = 0;
+                            if (g1min > 0) {
+                                for (long g = 0; g < g1max; ++g) {
+                                    if (s1 >= g1min) s1 = 0;
+                                    coulomb_collide(o, cmax[Lmax[smax[s2]]], maxS, cmin[Lmin[smin[s1]]], minS, lD, nMaxS,
+                                                    nMinS, nMaxS, r);
+                                    ++s1;
+                                    ++s2;
+                                }
+                            }
+                            s1 = g1min;
+                            s2 = g1max;
+                            for (long g = 0; g < g2max; ++g) {
+                                if (s1 >= g2min + g1min) s1 = g1min;
+                                coulomb_collide(o, cmax[Lmax[smax[s2]]], maxS, cmin[Lmin[smin[s1]]], minS, lD, nMaxS,
+                                                nMinS, nMaxS, r);
+                                ++s1;
+                                ++s2;
+                            }
+                            pairs += g1max + g2max;
+                            continue;
+                        }
                         const double nMaxS = (maxS == a ? sA : sB) / V;
                         const double nMinS = (maxS == a ? sB : sA) / V;
                         double nAB = 0.0;
                         for (long l = 0; l < nMax; ++l) nAB += wmin;
                         const double n12 = nAB / V;
                         long k = 0;
-                        auto& cmin = o.cloud[minS];
-                        auto& cmax = o.cloud[maxS];
                         for (long l = 0; l < nMax; ++l) {
                             if (k >= nMin) k = 0;
-                            nanbu_collide(o, cmax[Lmax[smax[l]]], maxS, cmin[Lmin[smin[k]]], minS, nMaxS, nMinS, n12, r);
+                            coulomb_collide(o, cmax[Lmax[smax[l]]], maxS, cmin[Lmin[smin[k]]], minS, lD, nMaxS, nMinS,
+                                            n12, r);
                             ++k;
                         }
                         pairs += nMax;
@@ -1057,15 +1347,16 @@ void coulomb_ny(Oracle& o, std::vector<std::vector<std::vector<int>>>& occ, picg
 }
 
 // PICCloud::buildCellOccupancy (PICCloud.C:327-354) + collisions() (PICCloud.C:526-539):
-// Coulomb first, then electron-neutral.
+// Coulomb, then electron-neutral, then ion-neutral.
 void collisions(Oracle& o, picgpu_step_stats* st) {
-    if (!o.cfg.mcc.enabled && !o.cfg.coulomb.enabled) return;
+    if (!o.cfg.mcc.enabled && !o.cfg.coulomb.enabled && !o.cfg.ion_mcc.enabled) return;
     std::vector<std::vector<std::vector<int>>> occ(o.cfg.n_species,
                                                    std::vector<std::vector<int>>(o.m.n_cells));
     for (int s = 0; s < o.cfg.n_species; ++s)
         for (size_t i = 0; i < o.cloud[s].size(); ++i) occ[s][o.cloud[s][i].cell].push_back(int(i));
-    if (o.cfg.coulomb.enabled) coulomb_ny(o, occ, st);
+    if (o.cfg.coulomb.enabled) coulomb_pairs(o, occ, st);
     if (o.cfg.mcc.enabled) mcc_background(o, occ[o.cfg.electron_species], st);
+    if (o.cfg.ion_mcc.enabled) ion_mcc_background(o, occ[o.cfg.ion_mcc.ion_species], st);
 }
 
 void fill_counts(const Oracle& o, picgpu_step_stats* st) {
@@ -1136,6 +1427,24 @@ int oracle_create(const picgpu_mesh_desc* mesh, const picgpu_config* cfg, int nt
     if (cfg->mcc.enabled) {
         std::string e = ocoll::init_mcc(o.cfg, o.xs, m.n_cells, o.svmax, o.remainder);
         if (!e.empty()) { o.err = e; *out = c; return PICGPU_INVALID_ARG; }
+    }
+    o.isvmax.assign(m.n_cells, 0.0);
+    o.iremainder.assign(m.n_cells, 0.0);
+    if (cfg->ion_mcc.enabled) {
+        std::string e = ocoll::init_ion_mcc(o.cfg, o.ixs, m.n_cells, o.isvmax, o.iremainder);
+        if (!e.empty()) { o.err = e; *out = c; return PICGPU_INVALID_ARG; }
+    }
+    if (cfg->coulomb.enabled && cfg->coulomb.pairing == 1) {
+        double w = -1.0;
+        for (int s = 0; s < cfg->n_species; ++s) {
+            if (cfg->species[s].charge == 0.0 || !cfg->species[s].solve_movement) continue;
+            if (w < 0) w = cfg->species[s].weight;
+            else if (cfg->species[s].weight != w) {
+                o.err = "coulomb: TakizukaAbe pairing needs equal species weights";
+                *out = c;
+                return PICGPU_INVALID_ARG;
+            }
+        }
     }
     *out = c;
     return 0;
@@ -1311,5 +1620,25 @@ int oracle_diagnostics(oracle_ctx* ctx, picgpu_diagnostics* out) {
 }
 
 double oracle_move_seconds(const oracle_ctx* ctx) { return ctx->o.move_seconds; }
+
+void oracle_philox4x32(const uint32_t ctr[4], const uint32_t key[2], uint32_t out[4]) {
+    ocoll::Philox r(uint64_t(key[0]) | (uint64_t(key[1]) << 32), ctr[1], ctr[2], ctr[3]);
+    r.ctr[0] = ctr[0];
+    r.block();
+    for (int k = 0; k < 4; ++k) out[k] = r.buf[k];
+}
+
+double oracle_debye_length(oracle_ctx* ctx, int cell) {
+    Oracle& o = ctx->o;
+    if (cell < 0 || cell >= o.m.n_cells) return 0.0;
+    std::vector<int> charged;
+    for (int s = 0; s < o.cfg.n_species; ++s)
+        if (o.cfg.species[s].charge != 0.0 && o.cfg.species[s].solve_movement) charged.push_back(s);
+    std::vector<std::vector<std::vector<int>>> occ(o.cfg.n_species, std::vector<std::vector<int>>(o.m.n_cells));
+    for (int s = 0; s < o.cfg.n_species; ++s)
+        for (size_t i = 0; i < o.cloud[s].size(); ++i)
+            if (o.cloud[s][i].cell == cell) occ[s][cell].push_back(int(i));
+    return debye_length(o, charged, occ, cell);
+}
 
 }  // extern "C"

@@ -52,6 +52,11 @@ int  oracle_set_field(oracle_ctx* ctx, int which, const double* in, size_t n);
 int  oracle_diagnostics(oracle_ctx* ctx, picgpu_diagnostics* out);
 /* Wall-clock seconds spent in push + track + deposit since creation. */
 double oracle_move_seconds(const oracle_ctx* ctx);
+/* One Philox4x32-10 block of the collision generator (known-answer checks). */
+void oracle_philox4x32(const uint32_t ctr[4], const uint32_t key[2], uint32_t out[4]);
+/* Debye length of a cell over the Coulomb-colliding species for the current
+ * particles (CoulombCollisionModel.C:249-309); 0 when undefined. */
+double oracle_debye_length(oracle_ctx* ctx, int cell);
 
 #ifdef __cplusplus
 }

@@ -51,6 +51,10 @@ def load():
         lib.oracle_mesh_query.argtypes = [P, C.POINTER(abi.MeshInfo)]
         lib.oracle_move_seconds.restype = C.c_double
         lib.oracle_move_seconds.argtypes = [P]
+        lib.oracle_philox4x32.restype = None
+        lib.oracle_philox4x32.argtypes = [C.POINTER(C.c_uint32), C.POINTER(C.c_uint32), C.POINTER(C.c_uint32)]
+        lib.oracle_debye_length.restype = C.c_double
+        lib.oracle_debye_length.argtypes = [P, C.c_int]
         _lib = lib
     return _lib
 

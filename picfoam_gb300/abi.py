@@ -80,10 +80,26 @@ class Mcc(C.Structure):
     ]
 
 
+class IonMcc(C.Structure):
+    _fields_ = [
+        ("enabled", C.c_int32), ("ion_species", C.c_int32), ("n_xs", C.c_int32), ("pad", C.c_int32),
+        ("cx_threshold", C.c_double), ("sigma_v_max_init", C.c_double),
+        ("find_max_energy", C.c_double), ("find_energy_step", C.c_double),
+        ("xs_energy", C.POINTER(C.c_double)), ("xs_elastic", C.POINTER(C.c_double)),
+        ("xs_charge_exchange", C.POINTER(C.c_double)),
+    ]
+
+
+PAIRING_NANBU_YONEMURA, PAIRING_TAKIZUKA_ABE = range(2)
+COLLIDE_NANBU, COLLIDE_PEREZ = range(2)
+
+
 class Coulomb(C.Structure):
     _fields_ = [
         ("enabled", C.c_int32), ("pairing", C.c_int32), ("collide", C.c_int32),
         ("allow_intra", C.c_int32), ("coulomb_log", C.c_double),
+        ("calculate_bmin", C.c_int32), ("debye_drift", C.c_int32),
+        ("weight_correction", C.c_int32), ("pad", C.c_int32),
     ]
 
 
@@ -100,7 +116,7 @@ class Config(C.Structure):
         ("pcg_tol", C.c_double), ("pcg_max_iter", C.c_int32), ("pcg_norm", C.c_int32),
         ("sort_interval", C.c_int32), ("pad0", C.c_int32),
         ("seed", C.c_uint64),
-        ("mcc", Mcc), ("coulomb", Coulomb),
+        ("mcc", Mcc), ("ion_mcc", IonMcc), ("coulomb", Coulomb),
     ]
 
 
@@ -114,6 +130,8 @@ class StepStats(C.Structure):
         ("mcc_candidates", C.c_int64), ("mcc_elastic", C.c_int64),
         ("mcc_excitation", C.c_int64), ("mcc_ionization", C.c_int64),
         ("coulomb_pairs", C.c_int64),
+        ("ion_mcc_candidates", C.c_int64), ("ion_mcc_elastic", C.c_int64),
+        ("ion_mcc_charge_exchange", C.c_int64),
         ("floating_charge", C.c_double * (MAX_BOXES + 6)),
     ]
 

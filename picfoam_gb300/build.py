@@ -28,7 +28,7 @@ UNITS = {
     "move_fp32.cu": ["--use_fast_math"],
     "fields.cu": ["--fmad=false"],
     "particles.cu": [],
-    "collide.cu": [],
+    "collide.cu": ["--fmad=false"],
     "library.cu": [],
     "pcg_static.cu": ["--fmad=false"],
 }

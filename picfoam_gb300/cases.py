@@ -11,6 +11,8 @@ benchmark configurations of the particle hot path (seeded synthetic inputs):
   two_species_3d          0.05 m cube, 64^3 cells, e- and Ar+ at 50/cell, B = 0.01 T
   electron_swarm          32x32x256 cells, 10M e-, E = 1e4 V/m, argon-like gas
   coulomb_thermalisation  16^3 cells, 400 e-/cell, T_x = 2 eV, T_yz = 1 eV
+  coulomb_relaxation      e- and heavy ions at different temperatures (e-i exchange)
+  ion_swarm               Ar+ in argon: isotropic elastic + charge exchange MCC
   electrode_box           128^3 cells, two floating boxes, one 100 V box
 """
 import dataclasses
@@ -259,10 +261,29 @@ def electron_swarm(nx=32, ny=32, nz=256, N=10_000_000, Ez=1e4, gas_density=1e21,
                 dict(dt=dt, E_over_N_Td=Ez / gas_density * 1e21, N=N))
 
 
+def set_coulomb(cfg, pairing=abi.PAIRING_NANBU_YONEMURA, collide=abi.COLLIDE_NANBU, coulomb_log=15.0,
+                calculate_bmin=True, debye_drift=True, weight_correction=0, allow_intra=True):
+    """CoulombCollisionModel dictionary: coulomb_log 0 computes the logarithm
+    from the cell Debye length (calculate_bmin / accountForDrift default on,
+    CoulombCollisionModel.C:128-140)."""
+    co = cfg.coulomb
+    co.enabled = 1
+    co.pairing = pairing
+    co.collide = collide
+    co.allow_intra = 1 if allow_intra else 0
+    co.coulomb_log = coulomb_log
+    co.calculate_bmin = 1 if calculate_bmin else 0
+    co.debye_drift = 1 if debye_drift else 0
+    co.weight_correction = weight_correction
+
+
 def coulomb_thermalisation(n_cells=16, per_cell=400, n=1e18, T=4.0 / 3.0, ratio=0.5, seed=1234,
-                           coulomb_log=15.0, precision=abi.PREC_FP64, dt_factor=None, L=None):
+                           coulomb_log=15.0, precision=abi.PREC_FP64, dt_factor=None, L=None,
+                           pairing=abi.PAIRING_NANBU_YONEMURA, collide=abi.COLLIDE_NANBU):
     """Electrons with T_x = 2 eV, T_y = T_z = 1 eV (Isotropization initial
-    condition), periodic box, no field solve, Nanbu/NanbuYonemura Coulomb."""
+    condition), periodic box, no field solve, intra-species Coulomb
+    collisions (NanbuYonemura or TakizukaAbe pairing, Nanbu or Perez
+    collide; coulomb_log 0 = from the Debye length)."""
     if L is None:
         L = 1e-4
     sides = [patch(abi.PATCH_CYCLIC) for _ in range(6)]
@@ -274,15 +295,12 @@ def coulomb_thermalisation(n_cells=16, per_cell=400, n=1e18, T=4.0 / 3.0, ratio=
     T_x = 3.0 * T / (1.0 + 2.0 * ratio)
     T_yz = ratio * T_x
     ve = thermal_speed(T_x, M_E)
-    nu = n * E_CHARGE ** 4 * coulomb_log / (4 * math.pi * EPS0 ** 2 * M_E ** 2 * ve ** 3)
+    # the time step is set by a logarithm of 15 whether or not it is computed
+    nu = n * E_CHARGE ** 4 * (coulomb_log or 15.0) / (4 * math.pi * EPS0 ** 2 * M_E ** 2 * ve ** 3)
     dt = (dt_factor if dt_factor else 0.02) / nu
     cfg = base_config(dt, [(M_E, -E_CHARGE, w, True)], maxwell=abi.MAXWELL_NONE, precision=precision,
                       seed=seed)
-    cfg.coulomb.enabled = 1
-    cfg.coulomb.pairing = 0
-    cfg.coulomb.collide = 0
-    cfg.coulomb.allow_intra = 1
-    cfg.coulomb.coulomb_log = coulomb_log
+    set_coulomb(cfg, pairing=pairing, collide=collide, coulomb_log=coulomb_log)
     rng = np.random.Generator(np.random.Philox(seed))
     tet, bary = uniform_in_cells(rng, np.arange(n_c), per_cell)
     U = rng.standard_normal((N, 3))
@@ -290,6 +308,96 @@ def coulomb_thermalisation(n_cells=16, per_cell=400, n=1e18, T=4.0 / 3.0, ratio=
     U[:, 1:] *= thermal_speed(T_yz, M_E)
     return Case("coulomb_thermalisation", mesh, cfg, {0: (tet, bary, U)}, [],
                 dict(dt=dt, T_x=T_x, T_yz=T_yz, nu=nu, N=N))
+
+
+def coulomb_relaxation(n_cells=4, e_per_cell=60, i_per_cell=45, n=1e18, T_e=2.0, T_i=0.5, m_i=100.0 * M_E,
+                       seed=1234, coulomb_log=10.0, precision=abi.PREC_FP64, L=2e-5,
+                       pairing=abi.PAIRING_NANBU_YONEMURA, collide=abi.COLLIDE_NANBU, w_i_factor=1.0,
+                       weight_correction=0, dt_factor=0.02, ragged=False):
+    """Electrons (T_e) and ions of mass m_i (T_i) in a periodic box, no
+    field solve: inter- and intra-species Coulomb collisions relax the two
+    temperatures.  Unequal per-cell counts exercise the unequal-group
+    pairing; w_i_factor != 1 gives the ions another parcel weight (with
+    weight_correction 1 the Nanbu correction applies); ragged draws the
+    per-cell counts at random (0..2x the mean) so that empty, single and odd
+    cells occur."""
+    sides = [patch(abi.PATCH_CYCLIC) for _ in range(6)]
+    mesh = block_mesh((n_cells,) * 3, (L,) * 3, sides)
+    n_c = n_cells ** 3
+    V = L ** 3
+    rng = np.random.Generator(np.random.Philox(seed))
+    if ragged:
+        ce = rng.integers(0, 2 * e_per_cell + 1, n_c)
+        ci = rng.integers(0, 2 * i_per_cell + 1, n_c)
+    else:
+        ce = np.full(n_c, e_per_cell)
+        ci = np.full(n_c, i_per_cell)
+    Ne, Ni = int(ce.sum()), int(ci.sum())
+    w_e = n * V / max(Ne, 1)
+    w_i = w_e * w_i_factor
+    ve = thermal_speed(T_e, M_E)
+    nu = n * E_CHARGE ** 4 * (coulomb_log or 10.0) / (4 * math.pi * EPS0 ** 2 * M_E ** 2 * ve ** 3)
+    dt = dt_factor / nu
+    cfg = base_config(dt, [(M_E, -E_CHARGE, w_e, True), (m_i, E_CHARGE, w_i, True)], maxwell=abi.MAXWELL_NONE,
+                      precision=precision, seed=seed)
+    set_coulomb(cfg, pairing=pairing, collide=collide, coulomb_log=coulomb_log,
+                weight_correction=weight_correction)
+
+    def place(counts):
+        cells = np.repeat(np.arange(n_c), counts)
+        m = cells.size
+        tet = (cells * 12 + rng.integers(0, 12, m)).astype(np.int32)
+        u = np.sort(rng.random((m, 3)), axis=1)
+        return tet, np.stack([u[:, 0], u[:, 1] - u[:, 0], u[:, 2] - u[:, 1]], axis=1)
+
+    te, be = place(ce)
+    ti, bi = place(ci)
+    Ue = maxwellian(rng, Ne, T_e, M_E)
+    Ui = maxwellian(rng, Ni, T_i, m_i)
+    return Case("coulomb_relaxation", mesh, cfg, {0: (te, be, Ue), 1: (ti, bi, Ui)}, [],
+                dict(dt=dt, nu=nu, Ne=Ne, Ni=Ni, counts_e=ce, counts_i=ci))
+
+
+def ion_swarm(n_cells=(8, 8, 8), N=20000, T_i=1.0, gas_density=1e21, T_gas=300.0, sigma_el=5e-19,
+              sigma_cx=5e-19, cx_threshold=0.0, seed=1234, precision=abi.PREC_FP64, size=(0.01, 0.01, 0.01),
+              steps_dt=0.01, gas_drift=(0.0, 0.0, 0.0)):
+    """Ar+ ions in argon, periodic box, no field: IonNeutralCollisionModel
+    with isotropic elastic scattering and charge exchange (constant cross
+    sections, List tables of two nodes)."""
+    import ctypes as C
+    sides = [patch(abi.PATCH_CYCLIC) for _ in range(6)]
+    mesh = block_mesh(n_cells, size, sides)
+    n_c = n_cells[0] * n_cells[1] * n_cells[2]
+    vmax = math.sqrt(2 * E_CHARGE * 30.0 * T_i / M_AR) + 4 * math.sqrt(K_B * T_gas / M_AR)
+    sv = (sigma_el + sigma_cx) * vmax
+    dt = steps_dt / (gas_density * sv)
+    cfg = base_config(dt, [(M_AR, E_CHARGE, 1.0, True)], maxwell=abi.MAXWELL_NONE, precision=precision,
+                      seed=seed, electron_species=-1)
+    mc = cfg.mcc
+    mc.gas_density = gas_density
+    mc.gas_temperature = T_gas
+    mc.gas_mass = M_AR
+    mc.gas_weight = 1.0
+    for a in range(3):
+        mc.gas_velocity[a] = gas_drift[a]
+    arrs = [np.ascontiguousarray(a, dtype=np.float64)
+            for a in ([0.0, 1e4], [sigma_el, sigma_el], [sigma_cx, sigma_cx])]
+    im = cfg.ion_mcc
+    im.enabled = 1
+    im.ion_species = 0
+    im.n_xs = 2
+    im.cx_threshold = cx_threshold
+    im.sigma_v_max_init = sv
+    im.xs_energy, im.xs_elastic, im.xs_charge_exchange = [
+        a.ctypes.data_as(C.POINTER(C.c_double)) for a in arrs]
+    rng = np.random.Generator(np.random.Philox(seed))
+    cells = rng.integers(0, n_c, N)
+    tet = (cells * 12 + rng.integers(0, 12, N)).astype(np.int32)
+    u = np.sort(rng.random((N, 3)), axis=1)
+    bary = np.stack([u[:, 0], u[:, 1] - u[:, 0], u[:, 2] - u[:, 1]], axis=1)
+    U = maxwellian(rng, N, T_i, M_AR)
+    return Case("ion_swarm", mesh, cfg, {0: (tet, bary, U)}, arrs,
+                dict(dt=dt, N=N, sv=sv))
 
 
 def electrode_box(n_cells=128, per_cell=30, n=1e15, T_e=2.0, T_i=0.03, seed=1234,

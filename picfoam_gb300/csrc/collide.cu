@@ -10,10 +10,17 @@
 //                    one thread per cell, candidates drawn sequentially from a
 //                    Philox stream keyed by (seed, cell, step); secondaries go
 //                    to a staging slot per candidate and are appended in
-//                    (cell, candidate) order
+//                    (cell, candidate) order; Nanbu or relativistic
+//                    (RelativisticElectronNeutralCollision.C:161-242) scattering
+//   ion_mcc_*        IonNeutralCollisionModel::performBackgroundCollisions
+//                    (IonNeutralCollisionModel.C:453-577): isotropic elastic
+//                    scattering or charge exchange, one thread per cell
 //   coulomb_*        NanbuYonemuraPairing::pairANDcollide (NanbuYonemuraPairing.C:56-325)
-//                    with NanbuCollision::collide (NanbuCollision.C:60-161),
-//                    one thread per cell
+//                    or TakizukaAbePairing::pairANDcollide (TakizukaAbePairing.C:60-341)
+//                    with NanbuCollision::collide (NanbuCollision.C:60-161) or
+//                    PerezRelativisticCollision::collide (PerezRelativisticCollision.C:60-220),
+//                    fixed or Debye-length Coulomb logarithm
+//                    (CoulombCollisionModel.C:249-309), one thread per cell
 // The collision arithmetic is FP64 for both particle forms.
 #include <algorithm>
 #include <vector>
@@ -28,6 +35,7 @@ namespace {
 
 constexpr double kEch = 1.602176634e-19;
 constexpr double kKb = 1.380649e-23;
+constexpr double kPlanck = 6.62607015e-34;
 constexpr double kMu0c = 4.0 * kPi * 1e-7;
 __device__ __forceinline__ double eps0c() { return 1.0 / (kMu0c * kC * kC); }
 
@@ -201,6 +209,90 @@ __device__ void nanbu_scatter(double eV, V3d& Ue, V3d& Un, double mE, double mN,
     Un = {Un.x + kn * d.x, Un.y + kn * d.y, Un.z + kn * d.z};
 }
 
+__device__ __forceinline__ double dotd(V3d a, V3d b) { return a.x * b.x + a.y * b.y + a.z * b.z; }
+
+// Centre-of-momentum frame of two particles and the rotation of the momentum
+// in it (RelativisticElectronNeutralCollision.C:161-242,
+// PerezRelativisticCollision.C:90-187).
+struct CoM {
+    double gP, gQ, gc, gcv, gPc, gQc, mag_pc;
+    V3d vc, pc;
+};
+
+__device__ bool com_frame(V3d UP, V3d UQ, double mP, double mQ, CoM& f) {
+    const double aP = magd(UP) / kC, aQ = magd(UQ) / kC;
+    f.gP = 1.0 / sqrt(1.0 - aP * aP);
+    f.gQ = 1.0 / sqrt(1.0 - aQ * aQ);
+    const double kp = mP * f.gP, kq = mQ * f.gQ;
+    const V3d pP = {kp * UP.x, kp * UP.y, kp * UP.z};
+    const V3d pQ = {kq * UQ.x, kq * UQ.y, kq * UQ.z};
+    const double den = mP * f.gP + mQ * f.gQ;
+    f.vc = {(pP.x + pQ.x) / den, (pP.y + pQ.y) / den, (pP.z + pQ.z) / den};
+    const double vc2 = dotd(f.vc, f.vc);
+    if (vc2 == 0.0) {
+        f.gc = 1.0;
+        f.gcv = 0.5;
+        f.pc = pP;
+        f.gPc = f.gP;
+        f.gQc = f.gQ;
+    } else {
+        f.gc = 1.0 / sqrt(1.0 - vc2 / (kC * kC));
+        f.gcv = (f.gc - 1.0) / vc2;
+        const double k = (f.gcv * dotd(f.vc, UP) - f.gc) * mP * f.gP;
+        f.pc = {pP.x + k * f.vc.x, pP.y + k * f.vc.y, pP.z + k * f.vc.z};
+        f.gPc = (1.0 - dotd(f.vc, UP) / (kC * kC)) * f.gP * f.gc;
+        f.gQc = (1.0 - dotd(f.vc, UQ) / (kC * kC)) * f.gQ * f.gc;
+    }
+    f.mag_pc = magd(f.pc);
+    return f.mag_pc != 0.0;
+}
+
+__device__ void com_rotate(const CoM& f, double cosChi, double sinChi, double eps, double mP, double mQ, V3d& UP,
+                           V3d& UQ) {
+    const double sce = sinChi * cos(eps), sse = sinChi * sin(eps);
+    const V3d p = f.pc;
+    const double pperp = sqrt(p.x * p.x + p.y * p.y);
+    V3d np;
+    if (pperp > 1.e-10 * f.mag_pc) {
+        const double ip = 1.0 / pperp;
+        np = {(p.x * p.z * sce - p.y * f.mag_pc * sse) * ip + p.x * cosChi,
+              (p.y * p.z * sce + p.x * f.mag_pc * sse) * ip + p.y * cosChi, -pperp * sce + p.z * cosChi};
+    } else {
+        np = {f.mag_pc * sce, f.mag_pc * sse, f.mag_pc * cosChi};
+    }
+    const double kP = f.gcv * dotd(f.vc, np) + mP * f.gPc * f.gc;
+    const V3d npP = {np.x + kP * f.vc.x, np.y + kP * f.vc.y, np.z + kP * f.vc.z};
+    const double aP = magd(npP) / (mP * kC);
+    const double ngP = sqrt(1.0 + aP * aP);
+    const V3d mnp = {-1.0 * np.x, -1.0 * np.y, -1.0 * np.z};
+    const double kQ = f.gcv * dotd(f.vc, mnp) + mQ * f.gQc * f.gc;
+    const V3d npQ = {mnp.x + kQ * f.vc.x, mnp.y + kQ * f.vc.y, mnp.z + kQ * f.vc.z};
+    const double aQ = magd(npQ) / (mQ * kC);
+    const double ngQ = sqrt(1.0 + aQ * aQ);
+    const double dP = mP * ngP, dQ = mQ * ngQ;
+    UP = {npP.x / dP, npP.y / dP, npP.z / dP};
+    UQ = {npQ.x / dQ, npQ.y / dQ, npQ.z / dQ};
+}
+
+// RelativisticElectronNeutralCollision::updateVelocity: cos(chi) is drawn
+// before the azimuth.
+__device__ void relativistic_scatter(double eV, V3d& Ue, V3d& Un, double mE, double mN, Rng& r) {
+    CoM f;
+    if (!com_frame(Ue, Un, mE, mN, f)) return;
+    double cosChi;
+    if (eV < 1e-30) cosChi = 1.0;
+    else cosChi = 1.0 / eV * (eV + 2.0 - 2.0 * pow(1.0 + eV, r.uniform()));
+    const double sinChi = sqrt(1.0 - cosChi * cosChi);
+    const double eps = 2.0 * kPi * r.uniform();
+    com_rotate(f, cosChi, sinChi, eps, mE, mN, Ue, Un);
+}
+
+__device__ __forceinline__ void electron_scatter(int relativistic, double eV, V3d& Ue, V3d& Un, double mE,
+                                                 double mN, Rng& r) {
+    if (relativistic) relativistic_scatter(eV, Ue, Un, mE, mN, r);
+    else nanbu_scatter(eV, Ue, Un, mE, mN, r);
+}
+
 // List cross section, linear between bracketing nodes, end values held
 // (ListCrossSection.C:33-88).
 __device__ double interp_xs(double x, const double* e, const double* v, int n) {
@@ -228,6 +320,7 @@ struct MccParams {
     double ex_th, iz_th;
     double wEwN, wNwE;
     int create_e, create_i;
+    int relativistic;     // RelativisticElectronNeutral scattering
     uint64_t seed;
     uint32_t step;
     const int* cand_off;  // n_cells + 1
@@ -286,14 +379,14 @@ __global__ void mcc_kernel(MccParams M, DSpecies el, Secondary* __restrict__ sta
         const double Ru = r.uniform();
         if (Ru <= Qel / sigmaT) {
             nel++;
-            nanbu_scatter(eV, Ue, Un, M.me, M.mg, r);
+            electron_scatter(M.relativistic, eV, Ue, Un, M.me, M.mg, r);
             Vel<R>::put(el, pi, Ue);
         } else if (eV >= M.ex_th && Ru <= (Qel + Qex) / sigmaT) {
             nex++;
             const double f = sqrt(1.0 - M.ex_th / eV);
             Ue = {f * Ue.x, f * Ue.y, f * Ue.z};
             eV -= M.ex_th;
-            nanbu_scatter(eV, Ue, Un, M.me, M.mg, r);
+            electron_scatter(M.relativistic, eV, Ue, Un, M.me, M.mg, r);
             Vel<R>::put(el, pi, Ue);
         } else if (eV >= M.iz_th && Ru <= Qt / sigmaT) {
             const double th = M.iz_th;
@@ -306,7 +399,7 @@ __global__ void mcc_kernel(MccParams M, DSpecies el, Secondary* __restrict__ sta
             const double f = sqrt(1.0 - (th + Ep) / eV);
             Ue = {f * Ue.x, f * Ue.y, f * Ue.z};
             eV -= (th + Ep);
-            nanbu_scatter(eV, Ue, Un, M.me, M.mg, r);
+            electron_scatter(M.relativistic, eV, Ue, Un, M.me, M.mg, r);
             const double rndU = r.uniform();
             Secondary sc{};
             const bool make = rndU <= M.wEwN;
@@ -322,7 +415,7 @@ __global__ void mcc_kernel(MccParams M, DSpecies el, Secondary* __restrict__ sta
                 const double mp = magd(preUe);
                 V3d ne = {sp * (preUe.x / mp), sp * (preUe.y / mp), sp * (preUe.z / mp)};
                 V3d un2 = preUn;
-                nanbu_scatter(Ep, ne, un2, M.me, M.mg, r);
+                electron_scatter(M.relativistic, Ep, ne, un2, M.me, M.mg, r);
                 sc.flag |= 1;
                 sc.ue[0] = ne.x; sc.ue[1] = ne.y; sc.ue[2] = ne.z;
             }
@@ -363,6 +456,80 @@ __global__ void stage_append_kernel(const Secondary* __restrict__ stage, int n, 
     }
 }
 
+// --------------------------------------------------------- ion-neutral ---
+struct IonMccParams {
+    int n_cells;
+    const int* i_start;   // n_cells + 1
+    const int* i_idx;
+    double* svmax;
+    double* rem;
+    const double* xs;     // 3 x n_xs: energy, elastic, charge exchange
+    int n_xs;
+    double n_gas, vth_gas, mg, mi, dt;
+    double drift[3];
+    double cx_th;
+    uint64_t seed;
+    uint32_t step;
+    unsigned long long* counts;
+};
+
+// IonNeutralCollisionModel::performBackgroundCollisions: elastic scattering
+// isotropic in the centre-of-mass frame (IonIsotropicScattering.C:103-143) or
+// charge exchange, the ion taking the neutral's velocity (:419-426).
+template <class R>
+__global__ void ion_mcc_kernel(IonMccParams M, DSpecies ions) {
+    const int c = blockIdx.x * blockDim.x + threadIdx.x;
+    if (c >= M.n_cells) return;
+    const int nI = M.i_start[c + 1] - M.i_start[c];
+    const double sv = M.svmax[c];
+    const double coll = M.rem[c] + double(nI) * M.n_gas * sv * M.dt;
+    const long nC = long(coll);
+    M.rem[c] = coll - double(nC);
+    if (nC == 0 || nI == 0) return;
+    const int* list = M.i_idx + M.i_start[c];
+    const double* E = M.xs;
+    const double* EL = M.xs + M.n_xs;
+    const double* CX = M.xs + 2 * M.n_xs;
+    Rng r(M.seed, kStreamIonMcc, uint32_t(c), M.step);
+    unsigned long long nel = 0, ncx = 0;
+    const double mt = M.mi + M.mg;
+    for (long i = 0; i < nC; ++i) {
+        long j = long(r.uniform() * double(nI));
+        if (j >= nI) j = nI - 1;
+        const int pi = list[j];
+        const V3d U = Vel<R>::get(ions, pi);
+        const double n0 = r.normal(), n1 = r.normal(), n2 = r.normal();
+        const V3d Un = {M.vth_gas * n0 + M.drift[0], M.vth_gas * n1 + M.drift[1], M.vth_gas * n2 + M.drift[2]};
+        const V3d d = {U.x - Un.x, U.y - Un.y, U.z - Un.z};
+        const double cR = magd(d);
+        const double gamma = 1.0 / sqrt(1.0 - (cR * cR) / (kC * kC));
+        const double eV = (gamma - 1.0) * M.mi * kC * kC / kEch;
+        const double sigmaT = sv / cR;
+        const double Qel = interp_xs(eV, E, EL, M.n_xs);
+        const double Qcx = interp_xs(eV, E, CX, M.n_xs);
+        const double Qt = Qel + Qcx;
+        if (Qt * cR > M.svmax[c]) M.svmax[c] = Qt * cR;
+        const double Ru = r.uniform();
+        if (Ru <= Qel / sigmaT) {
+            nel++;
+            const V3d Ucm = {(M.mi * U.x + M.mg * Un.x) / mt, (M.mi * U.y + M.mg * Un.y) / mt,
+                             (M.mi * U.z + M.mg * Un.z) / mt};
+            const double cosT = 2.0 * r.uniform() - 1.0;
+            const double sinT = sqrt(1.0 - cosT * cosT);
+            const double phi = 2.0 * kPi * r.uniform();
+            const V3d rel = {cR * cosT, cR * (sinT * cos(phi)), cR * (sinT * sin(phi))};
+            Vel<R>::put(ions, pi,
+                        V3d{Ucm.x + (M.mg * rel.x) / mt, Ucm.y + (M.mg * rel.y) / mt, Ucm.z + (M.mg * rel.z) / mt});
+        } else if (eV >= M.cx_th && Ru <= Qt / sigmaT) {
+            ncx++;
+            Vel<R>::put(ions, pi, Un);
+        }
+    }
+    atomicAdd(M.counts + 5, (unsigned long long)nC);
+    if (nel) atomicAdd(M.counts + 6, nel);
+    if (ncx) atomicAdd(M.counts + 7, ncx);
+}
+
 // ------------------------------------------------------------ Coulomb ---
 struct CoulombSpecies {
     int n;                // charged species taking part
@@ -393,16 +560,45 @@ __device__ double cos_chi(double s, Rng& r) {
     return 2.0 * U - 1.0;
 }
 
+struct CoulombParams {
+    int n_cells;
+    const double* vol;
+    double cl;            // fixed coulombLog; 0: from the cell Debye length
+    int takizuka_abe;     // pairing: 0 NanbuYonemura, 1 TakizukaAbe
+    int perez;            // collide: 0 Nanbu, 1 PerezRelativistic
+    int allow_intra, calc_bmin, debye_drift, weight_corr;
+    double dt;
+    uint64_t seed;
+    uint32_t step;
+    unsigned long long* counts;
+};
+
+// NanbuWeightCorrectionModel::correctVelocity (NanbuCorrection.C:50-66).
+__device__ __forceinline__ void weight_correct(const CoulombSpecies& C, const CoulombParams& K, int a, int b,
+                                               V3d preP, V3d preQ, V3d& UP, V3d& UQ, Rng& r) {
+    if (K.weight_corr != 1) return;
+    const double u = r.uniform();
+    if (u > C.w[a] / C.w[b]) UQ = preQ;
+    if (u > C.w[b] / C.w[a]) UP = preP;
+}
+
+// NanbuCollision::collide (NanbuCollision.C:60-135).
 template <class R>
-__device__ void collide(const CoulombSpecies& C, int a, int ia, int b, int ib, double nP, double nQ, double nPQ,
-                        double cl, double dt, Rng& r) {
+__device__ void nanbu_collide(const CoulombSpecies& C, const CoulombParams& K, int a, int ia, int b, int ib,
+                              double lD, double nP, double nQ, double nPQ, Rng& r) {
     const double mP = C.m[a], qP = C.q[a], mQ = C.m[b], qQ = C.q[b];
     V3d UP = Vel<R>::get(C.p[a], ia), UQ = Vel<R>::get(C.p[b], ib);
     const double reMass = mP * mQ / (mP + mQ);
     const V3d g = {UP.x - UQ.x, UP.y - UQ.y, UP.z - UQ.z};
     const double gm = magd(g);
+    double cl = K.cl;
+    if (cl == 0.0) {
+        double b0 = qP * qQ / (2.0 * kPi * eps0c() * reMass * gm * gm);
+        if (K.calc_bmin) b0 = fmax(kPlanck / (2.0 * (gm * reMass)), fabs(b0));
+        cl = fmax(2.0, 0.5 * log(1.0 + (lD * lD) / (b0 * b0)));
+    }
     const double A = qP * qQ / (eps0c() * reMass);
-    const double s = cl / (4.0 * kPi) * (A * A) * (nQ * nP / nPQ) * (1.0 / (gm * gm * gm)) * dt;
+    const double s = cl / (4.0 * kPi) * (A * A) * (nQ * nP / nPQ) * (1.0 / (gm * gm * gm)) * K.dt;
     const double cosChi = cos_chi(s, r);
     const double sinChi = sqrt(1.0 - cosChi * cosChi);
     const double gp = sqrt(g.y * g.y + g.z * g.z);
@@ -412,8 +608,89 @@ __device__ void collide(const CoulombSpecies& C, int a, int ia, int b, int ib, d
     const V3d d = {(1.0 - cosChi) * g.x + sinChi * h.x, (1.0 - cosChi) * g.y + sinChi * h.y,
                    (1.0 - cosChi) * g.z + sinChi * h.z};
     const double kp = mQ / (mP + mQ), kq = mP / (mP + mQ);
-    Vel<R>::put(C.p[a], ia, V3d{UP.x - kp * d.x, UP.y - kp * d.y, UP.z - kp * d.z});
-    Vel<R>::put(C.p[b], ib, V3d{UQ.x + kq * d.x, UQ.y + kq * d.y, UQ.z + kq * d.z});
+    V3d nUP = {UP.x - kp * d.x, UP.y - kp * d.y, UP.z - kp * d.z};
+    V3d nUQ = {UQ.x + kq * d.x, UQ.y + kq * d.y, UQ.z + kq * d.z};
+    weight_correct(C, K, a, b, UP, UQ, nUP, nUQ, r);
+    Vel<R>::put(C.p[a], ia, nUP);
+    Vel<R>::put(C.p[b], ib, nUQ);
+}
+
+// PerezRelativisticCollision::collide (PerezRelativisticCollision.C:60-192),
+// with the low-temperature cap s_max.
+template <class R>
+__device__ void perez_collide(const CoulombSpecies& C, const CoulombParams& K, int a, int ia, int b, int ib,
+                              double lD, double nP, double nQ, double nPQ, Rng& r) {
+    const double mP = C.m[a], qP = C.q[a], mQ = C.m[b], qQ = C.q[b];
+    const V3d UP = Vel<R>::get(C.p[a], ia), UQ = Vel<R>::get(C.p[b], ib);
+    CoM f;
+    if (!com_frame(UP, UQ, mP, mQ, f)) return;
+    const double mgsum = mP * f.gP + mQ * f.gQ;
+    const double c2 = kC * kC;
+    const double pc2 = f.mag_pc * f.mag_pc;
+    const double e0 = eps0c();
+    double cl = K.cl;
+    if (cl == 0.0) {
+        double b0 = qP * qQ / (4.0 * kPi * e0 * c2) * f.gc / mgsum * (1.0 + mP * f.gPc * mQ * f.gQc * c2 / pc2);
+        if (K.calc_bmin) b0 = fmax(kPlanck / (2 * f.mag_pc), fabs(b0));
+        cl = fmax(2.0, 0.5 * log(1.0 + (lD * lD) / (b0 * b0)));
+    }
+    const double t1 = f.gc * f.mag_pc / mgsum;
+    const double t2b = 1.0 + mP * f.gPc * mQ * f.gQc * c2 / pc2;
+    const double t2 = t2b * t2b;
+    const double qq = qP * qQ;
+    double s = (nP * nQ / nPQ) * K.dt * cl * (qq * qq) / (4.0 * kPi * (e0 * e0) * (c2 * c2) * mP * f.gP * mQ * f.gQ) *
+               t1 * t2;
+    const double v_rel = f.mag_pc * mgsum / (mP * f.gPc * mQ * f.gQc * f.gc);
+    const double s_max = pow(4.0 * kPi / 3.0, 1.0 / 3.0) * (nP * nQ / nPQ) * K.dt * (mP + mQ) /
+                         fmax(mP * pow(nP, 2.0 / 3.0), mQ * pow(nQ, 2.0 / 3.0)) * v_rel;
+    s = fmin(s_max, s);
+    const double cosChi = cos_chi(s, r);
+    const double sinChi = sqrt(1.0 - cosChi * cosChi);
+    const double eps = 2.0 * kPi * r.uniform();
+    V3d nUP = UP, nUQ = UQ;
+    com_rotate(f, cosChi, sinChi, eps, mP, mQ, nUP, nUQ);
+    weight_correct(C, K, a, b, UP, UQ, nUP, nUQ, r);
+    Vel<R>::put(C.p[a], ia, nUP);
+    Vel<R>::put(C.p[b], ib, nUQ);
+}
+
+template <class R>
+__device__ __forceinline__ void collide(const CoulombSpecies& C, const CoulombParams& K, int a, int ia, int b,
+                                        int ib, double lD, double nP, double nQ, double nPQ, Rng& r) {
+    if (K.perez) perez_collide<R>(C, K, a, ia, b, ib, lD, nP, nQ, nPQ, r);
+    else nanbu_collide<R>(C, K, a, ia, b, ib, lD, nP, nQ, nPQ, r);
+}
+
+// CoulombCollisionModel::debyeLength (CoulombCollisionModel.C:249-309) over
+// the colliding species of cell c, before any of its pairs collide.
+template <class R>
+__device__ double debye_length(const CoulombSpecies& C, const CoulombParams& K, int c) {
+    double debye = 0.0, n_max = 0.0;
+    for (int k = 0; k < C.n; ++k) {
+        const double w = C.w[k], q = C.q[k];
+        double vSqr = 0.0, n = 0.0, charge = 0.0;
+        V3d v = {0.0, 0.0, 0.0};
+        for (int t = C.start[k][c]; t < C.start[k][c + 1]; ++t) {
+            const V3d U = Vel<R>::get(C.p[k], C.idx[k][t]);
+            vSqr += dotd(U, U) * w;
+            charge += q * w;
+            v = {v.x + w * U.x, v.y + w * U.y, v.z + w * U.z};
+            n += w;
+        }
+        if (n <= 0.0) continue;
+        v = {v.x / n, v.y / n, v.z / n};
+        charge /= n;
+        vSqr /= n;
+        n /= K.vol[c];
+        if (n > n_max) n_max = n;
+        const double vd2 = K.debye_drift ? dotd(v, v) : 0.0;
+        const double T = C.m[k] / (3.0 * kKb) * (vSqr - vd2);
+        if (T <= 0.0) continue;
+        debye += n * charge * charge / eps0c() * 1.0 / (T * kKb);
+    }
+    if (debye <= 0.0) return 0.0;
+    const double r_min = pow(4.0 * kPi * n_max / 3.0, -1.0 / 3.0);
+    return fmax(r_min, sqrt(1 / debye));
 }
 
 __device__ void shuffle(int* a, int n, Rng& r) {
@@ -425,13 +702,12 @@ __device__ void shuffle(int* a, int n, Rng& r) {
 }
 
 template <class R>
-__global__ void coulomb_kernel(CoulombSpecies C, int n_cells, const double* __restrict__ vol, double cl,
-                               int allow_intra, double dt, uint64_t seed, uint32_t step,
-                               unsigned long long* counts) {
+__global__ void coulomb_kernel(CoulombSpecies C, CoulombParams K) {
     const int c = blockIdx.x * blockDim.x + threadIdx.x;
-    if (c >= n_cells) return;
-    const double V = vol[c];
-    Rng r(seed, kStreamCoulomb, uint32_t(c), step);
+    if (c >= K.n_cells) return;
+    const double V = K.vol[c];
+    Rng r(K.seed, kStreamCoulomb, uint32_t(c), K.step);
+    const double lD = K.cl == 0.0 ? debye_length<R>(C, K, c) : 0.0;
     unsigned long long pairs = 0;
     for (int i = 0; i < C.n; ++i) {
         for (int jj = C.n - 1; jj >= i; --jj) {
@@ -443,39 +719,67 @@ __global__ void coulomb_kernel(CoulombSpecies C, int n_cells, const double* __re
             const double sA = double(nA) * C.w[a];
             const double sB = a != b ? double(nB) * C.w[b] : 0.0;
             if (a == b && nA > 1) {
-                if (!allow_intra) continue;
+                if (!K.allow_intra) continue;
                 int* sel = C.sel[a] + sa;
                 for (int k = 0; k < nA; ++k) sel[k] = k;
                 shuffle(sel, nA, r);
+                if (K.takizuka_abe) {
+                    // TakizukaAbePairing.C:108-153: an odd count collides
+                    // P-Q, Q-R and P-R, then pairs from the fourth parcel on
+                    const double n = double(nA) * C.w[a] / V;
+                    if (nA % 2 != 0) {
+                        const double n12 = (double(nA) + 3.0) * C.w[a] / V;
+                        const int P = LA[sel[0]], Q = LA[sel[1]], Rr = LA[sel[2]];
+                        collide<R>(C, K, a, P, a, Q, lD, n, n, n12, r);
+                        collide<R>(C, K, a, Q, a, Rr, lD, n, n, n12, r);
+                        collide<R>(C, K, a, P, a, Rr, lD, n, n, n12, r);
+                        for (int x = 3; x < nA - 1; x += 2)
+                            collide<R>(C, K, a, LA[sel[x]], a, LA[sel[x + 1]], lD, n, n, n12, r);
+                        pairs += 2 + nA / 2;
+                    } else {
+                        for (int x = 0; x < nA - 1; x += 2)
+                            collide<R>(C, K, a, LA[sel[x]], a, LA[sel[x + 1]], lD, n, n, n, r);
+                        pairs += nA / 2;
+                    }
+                    continue;
+                }
                 const double n = sA / V;
                 if (nA % 2 != 0) {
                     double nAA = 2.0 * C.w[a];
                     for (int x = 0; x < nA - 2; x += 2) nAA += 2.0 * C.w[a];
                     const double n12 = nAA / V;
                     for (int x = 0; x < nA - 2; x += 2)
-                        collide<R>(C, a, LA[sel[x]], a, LA[sel[x + 1]], n, n, n12, cl, dt, r);
-                    collide<R>(C, a, LA[sel[nA - 1]], a, LA[sel[0]], n, n, n12, cl, dt, r);
+                        collide<R>(C, K, a, LA[sel[x]], a, LA[sel[x + 1]], lD, n, n, n12, r);
+                    collide<R>(C, K, a, LA[sel[nA - 1]], a, LA[sel[0]], lD, n, n, n12, r);
                     pairs += 1 + nA / 2;
                 } else {
                     double nAA = 0.0;
                     for (int x = 0; x < nA - 1; x += 2) nAA += 2.0 * C.w[a];
                     const double n12 = nAA / V;
                     for (int x = 0; x < nA - 1; x += 2)
-                        collide<R>(C, a, LA[sel[x]], a, LA[sel[x + 1]], n, n, n12, cl, dt, r);
+                        collide<R>(C, K, a, LA[sel[x]], a, LA[sel[x + 1]], lD, n, n, n12, r);
                     pairs += nA / 2;
                 }
             } else if (a != b && min(nA, nB) != 0) {
                 const double wmin = fmin(C.w[a], C.w[b]);
                 if (nA == nB) {
-                    const double nP = sA / V, nQ = sB / V;
                     int* sel = C.sel[a] + sa;
                     for (int k = 0; k < nA; ++k) sel[k] = k;
                     shuffle(sel, nA, r);
-                    double nAB = 0.0;
-                    for (int k = 0; k < nA; ++k) nAB += wmin;
-                    const double nPQ = nAB / V;
+                    double nP, nQ, nPQ;
+                    if (K.takizuka_abe) {
+                        nP = double(nA) * C.w[a] / V;
+                        nQ = double(nB) * C.w[a] / V;
+                        nPQ = nP;
+                    } else {
+                        nP = sA / V;
+                        nQ = sB / V;
+                        double nAB = 0.0;
+                        for (int k = 0; k < nA; ++k) nAB += wmin;
+                        nPQ = nAB / V;
+                    }
                     for (int k = 0; k < nA; ++k)
-                        collide<R>(C, a, LA[sel[k]], b, LB[sel[nA - k - 1]], nP, nQ, nPQ, cl, dt, r);
+                        collide<R>(C, K, a, LA[sel[k]], b, LB[sel[nA - k - 1]], lD, nP, nQ, nPQ, r);
                     pairs += nA;
                 } else {
                     const bool aMin = nA < nB;
@@ -488,6 +792,38 @@ __global__ void coulomb_kernel(CoulombSpecies C, int n_cells, const double* __re
                     for (int k = 0; k < nMax; ++k) { smax[k] = k; if (k < nMin) smin[k] = k; }
                     shuffle(smin, nMin, r);
                     shuffle(smax, nMax, r);
+                    if (K.takizuka_abe) {
+                        // TakizukaAbePairing.C:197-314: group 1 spreads the
+                        // remainder nMax % nMin over delta + 1 partners each,
+                        // group 2 gives the other minority parcels delta each
+                        const double nMinS = double(nMin) * C.w[a] / V, nMaxS = double(nMax) * C.w[a] / V;
+                        const int delta = nMax / nMin;
+                        const double delta_r = double(nMax % nMin) / double(nMin);
+                        const int g1min = int(delta_r * double(nMin));
+                        const int g1max = int(double(delta + 1) * delta_r * double(nMin));
+                        const int g2min = int((1.0 - delta_r) * double(nMin));
+                        const int g2max = int(double(delta) * (1.0 - delta_r) * double(nMin));
+                        int s1 = 0, s2 = 0;
+                        if (g1min > 0) {
+                            for (int g = 0; g < g1max; ++g) {
+                                if (s1 >= g1min) s1 = 0;
+                                collide<R>(C, K, maxS, Lmax[smax[s2]], minS, Lmin[smin[s1]], lD, nMaxS, nMinS, nMaxS,
+                                           r);
+                                ++s1;
+                                ++s2;
+                            }
+                        }
+                        s1 = g1min;
+                        s2 = g1max;
+                        for (int g = 0; g < g2max; ++g) {
+                            if (s1 >= g2min + g1min) s1 = g1min;
+                            collide<R>(C, K, maxS, Lmax[smax[s2]], minS, Lmin[smin[s1]], lD, nMaxS, nMinS, nMaxS, r);
+                            ++s1;
+                            ++s2;
+                        }
+                        pairs += g1max + g2max;
+                        continue;
+                    }
                     const double nMaxS = (maxS == a ? sA : sB) / V;
                     const double nMinS = (maxS == a ? sB : sA) / V;
                     double nAB = 0.0;
@@ -496,7 +832,7 @@ __global__ void coulomb_kernel(CoulombSpecies C, int n_cells, const double* __re
                     int k = 0;
                     for (int l = 0; l < nMax; ++l) {
                         if (k >= nMin) k = 0;
-                        collide<R>(C, maxS, Lmax[smax[l]], minS, Lmin[smin[k]], nMaxS, nMinS, n12, cl, dt, r);
+                        collide<R>(C, K, maxS, Lmax[smax[l]], minS, Lmin[smin[k]], lD, nMaxS, nMinS, n12, r);
                         ++k;
                     }
                     pairs += nMax;
@@ -504,7 +840,7 @@ __global__ void coulomb_kernel(CoulombSpecies C, int n_cells, const double* __re
             }
         }
     }
-    if (pairs) atomicAdd(counts + 4, pairs);
+    if (pairs) atomicAdd(K.counts + 4, pairs);
 }
 
 template <class T>
@@ -518,8 +854,82 @@ int grid_of(long n, int bs) { return int(std::max<long>(1, std::min<long>((n + b
 
 cudaError_t collide_set_tables(const TetConst& t) { return cudaMemcpyToSymbol(c_tetC, &t, sizeof t); }
 
+namespace {
+
+// Philox4x32-10 of the device generator, first uniform of stream (stream, cell, 0).
+double host_uniform(uint64_t seed, uint32_t stream, uint32_t cell) {
+    uint32_t key0 = uint32_t(seed), key1 = uint32_t(seed >> 32);
+    uint32_t x0 = 0, x1 = stream, x2 = cell, x3 = 0;
+    for (int rr = 0; rr < 10; ++rr) {
+        const uint64_t p0 = uint64_t(0xD2511F53u) * x0, p1 = uint64_t(0xCD9E8D57u) * x2;
+        const uint32_t n0 = uint32_t(p1 >> 32) ^ x1 ^ key0, n2 = uint32_t(p0 >> 32) ^ x3 ^ key1;
+        x1 = uint32_t(p1); x3 = uint32_t(p0); x0 = n0; x2 = n2;
+        key0 += 0x9E3779B9u; key1 += 0xBB67AE85u;
+    }
+    const uint32_t a = x0 >> 5, b = x1 >> 6;
+    return (double(a) * 67108864.0 + double(b)) * (1.0 / 9007199254740992.0);
+}
+
+// Table k of a packed cross-section block (energies first), linear between
+// the bracketing nodes (ListCrossSection.C:33-88).
+double host_xs(const std::vector<double>& xs, int n, int k, double x) {
+    const double* e = xs.data();
+    const double* v = xs.data() + size_t(k) * n;
+    if (x <= e[0]) return v[0];
+    if (x >= e[n - 1]) return v[n - 1];
+    int lo = 0, hi = n - 1;
+    while (hi - lo > 1) {
+        const int mid = (lo + hi) / 2;
+        if (e[mid] <= x) lo = mid; else hi = mid;
+    }
+    if (e[lo] == x) return v[lo];
+    return v[lo] + ((x - e[lo]) / (e[hi] - e[lo])) * (v[hi] - v[lo]);
+}
+
+// FindMaximum (sigma v)_max over [0, emax) of the summed tables 1..n_tables-1
+// (ElectronNeutralCollisionModel.C:383-424, IonNeutralCollisionModel.C:284-333).
+double find_maximum(const std::vector<double>& xs, int n, int n_tables, double mass, double emax, double step) {
+    if (!(emax > 0)) emax = xs[n - 1];
+    if (!(step > 0)) step = emax / 100000.0;
+    double sv = 0.0;
+    for (double eV = 0.0; eV < emax; eV += step) {
+        double q = 0.0;
+        for (int k = 1; k < n_tables; ++k) q += host_xs(xs, n, k, eV);
+        sv = std::fmax(sv, std::sqrt(2.0 * kEch * eV / mass) * q);
+    }
+    return sv;
+}
+
+// Uploads (sigma v)_max, remainders seeded U(0,1) from one Philox stream per
+// cell, and the packed tables.
+int upload_mcc(double** svmax, double** rem, double** xs_d, const std::vector<double>& xs, double sv,
+               uint64_t seed, uint32_t stream, int nc, cudaStream_t s, std::string* msg) {
+    std::vector<double> svm(nc, sv), r(nc);
+    for (int c = 0; c < nc; ++c) r[c] = host_uniform(seed, stream, uint32_t(c));
+    if (dmalloc(svmax, nc) || dmalloc(rem, nc) || dmalloc(xs_d, xs.size())) {
+        *msg = "MCC state: device allocation failed";
+        return PICGPU_OOM;
+    }
+    cudaMemcpyAsync(*svmax, svm.data(), nc * sizeof(double), cudaMemcpyHostToDevice, s);
+    cudaMemcpyAsync(*rem, r.data(), nc * sizeof(double), cudaMemcpyHostToDevice, s);
+    cudaMemcpyAsync(*xs_d, xs.data(), xs.size() * sizeof(double), cudaMemcpyHostToDevice, s);
+    if (cudaStreamSynchronize(s) != cudaSuccess) {
+        *msg = "MCC state: upload failed";
+        return PICGPU_CUDA_ERROR;
+    }
+    return PICGPU_OK;
+}
+
+bool ascending(const double* e, int n) {
+    for (int i = 1; i < n; ++i)
+        if (!(e[i] > e[i - 1])) return false;
+    return true;
+}
+
+}  // namespace
+
 int collide_init(CollideState& st, const picgpu_config& cfg, const DMesh& m, cudaStream_t s, std::string* msg) {
-    st.enabled = cfg.mcc.enabled || cfg.coulomb.enabled;
+    st.enabled = cfg.mcc.enabled || cfg.coulomb.enabled || cfg.ion_mcc.enabled;
     if (!st.enabled) return PICGPU_OK;
     const int nc = m.n_cells;
     if (dmalloc(&st.cell_start, size_t(PICGPU_MAX_SPECIES) * (nc + 1)) ||
@@ -527,6 +937,26 @@ int collide_init(CollideState& st, const picgpu_config& cfg, const DMesh& m, cud
         dmalloc(&st.counts, 8) || dmalloc(&st.scan_tmp, (nc + 1) / 1024 + 8)) {
         *msg = "collision state: device allocation failed";
         return PICGPU_OOM;
+    }
+    if (cfg.coulomb.enabled) {
+        const picgpu_coulomb& co = cfg.coulomb;
+        if (co.pairing < 0 || co.pairing > 1 || co.collide < 0 || co.collide > 1 || co.coulomb_log < 0 ||
+            co.weight_correction < 0 || co.weight_correction > 1) {
+            *msg = "Coulomb: unknown pairing, collide or weight-correction model";
+            return PICGPU_INVALID_ARG;
+        }
+        if (co.pairing == 1) {
+            // TakizukaAbePairing.C:45-46: equal parcel weights only
+            double w = -1.0;
+            for (int k = 0; k < cfg.n_species; ++k) {
+                if (cfg.species[k].charge == 0.0 || !cfg.species[k].solve_movement) continue;
+                if (w < 0) w = cfg.species[k].weight;
+                else if (cfg.species[k].weight != w) {
+                    *msg = "Coulomb: TakizukaAbe pairing needs equal species weights";
+                    return PICGPU_INVALID_ARG;
+                }
+            }
+        }
     }
     if (cfg.mcc.enabled) {
         const picgpu_mcc& mc = cfg.mcc;
@@ -543,11 +973,10 @@ int collide_init(CollideState& st, const picgpu_config& cfg, const DMesh& m, cud
             *msg = "MCC: createIon needs an ion species";
             return PICGPU_INVALID_ARG;
         }
-        for (int i = 1; i < mc.n_xs; ++i)
-            if (!(mc.xs_energy[i] > mc.xs_energy[i - 1])) {
-                *msg = "MCC: cross-section energies must ascend";
-                return PICGPU_INVALID_ARG;
-            }
+        if (!ascending(mc.xs_energy, mc.n_xs)) {
+            *msg = "MCC: cross-section energies must ascend";
+            return PICGPU_INVALID_ARG;
+        }
         // the parcel weights of the store are per species: secondaries carry the
         // background weight, so it must equal the species weights
         if (mc.gas_weight != cfg.species[cfg.electron_species].weight ||
@@ -563,66 +992,60 @@ int collide_init(CollideState& st, const picgpu_config& cfg, const DMesh& m, cud
             xs[2 * mc.n_xs + i] = mc.xs_excitation[i];
             xs[3 * mc.n_xs + i] = mc.xs_ionization[i];
         }
-        // (sigma v)_max initialisation: FindMaximum (ElectronNeutralCollisionModel.C:383-424)
         double sv = mc.sigma_v_max_init;
-        if (!(sv > 0)) {
-            const double me = cfg.species[cfg.electron_species].mass;
-            const double emax = mc.find_max_energy > 0 ? mc.find_max_energy : xs[mc.n_xs - 1];
-            const double step = mc.find_energy_step > 0 ? mc.find_energy_step : emax / 100000.0;
-            auto lin = [&](double x, int k) {
-                const double* e = xs.data();
-                const double* v = xs.data() + size_t(k) * mc.n_xs;
-                const int n = mc.n_xs;
-                if (x <= e[0]) return v[0];
-                if (x >= e[n - 1]) return v[n - 1];
-                int lo = 0, hi = n - 1;
-                while (hi - lo > 1) {
-                    const int mid = (lo + hi) / 2;
-                    if (e[mid] <= x) lo = mid; else hi = mid;
-                }
-                if (e[lo] == x) return v[lo];
-                return v[lo] + ((x - e[lo]) / (e[hi] - e[lo])) * (v[hi] - v[lo]);
-            };
-            sv = 0.0;
-            for (double eV = 0.0; eV < emax; eV += step) {
-                const double q = lin(eV, 1) + lin(eV, 2) + lin(eV, 3);
-                sv = std::fmax(sv, std::sqrt(2.0 * kEch * eV / me) * q);
-            }
-        }
-        std::vector<double> svm(nc, sv), rem(nc);
-        // remainders seeded U(0,1) (ElectronNeutralCollisionModel.C:286-296),
-        // one Philox stream per cell (host copy of the device generator)
-        for (int c = 0; c < nc; ++c) {
-            uint32_t key0 = uint32_t(cfg.seed), key1 = uint32_t(cfg.seed >> 32);
-            uint32_t x0 = 0, x1 = kStreamRemainder, x2 = uint32_t(c), x3 = 0;
-            for (int rr = 0; rr < 10; ++rr) {
-                const uint64_t p0 = uint64_t(0xD2511F53u) * x0, p1 = uint64_t(0xCD9E8D57u) * x2;
-                const uint32_t n0 = uint32_t(p1 >> 32) ^ x1 ^ key0, n2 = uint32_t(p0 >> 32) ^ x3 ^ key1;
-                x1 = uint32_t(p1); x3 = uint32_t(p0); x0 = n0; x2 = n2;
-                key0 += 0x9E3779B9u; key1 += 0xBB67AE85u;
-            }
-            const uint32_t a = x0 >> 5, b = x1 >> 6;
-            rem[c] = (double(a) * 67108864.0 + double(b)) * (1.0 / 9007199254740992.0);
-        }
-        if (dmalloc(&st.svmax, nc) || dmalloc(&st.remainder, nc) || dmalloc(&st.xs, xs.size()) ||
-            dmalloc(&st.ncand, nc + 1) || dmalloc(&st.cand_off, nc + 2)) {
+        if (!(sv > 0))
+            sv = find_maximum(xs, mc.n_xs, 4, cfg.species[cfg.electron_species].mass, mc.find_max_energy,
+                              mc.find_energy_step);
+        // remainders seeded U(0,1) (ElectronNeutralCollisionModel.C:286-296)
+        const int e = upload_mcc(&st.svmax, &st.remainder, &st.xs, xs, sv, cfg.seed, kStreamRemainder, nc, s, msg);
+        if (e) return e;
+        if (dmalloc(&st.ncand, nc + 1) || dmalloc(&st.cand_off, nc + 2)) {
             *msg = "MCC state: device allocation failed";
             return PICGPU_OOM;
         }
-        cudaMemcpyAsync(st.svmax, svm.data(), nc * sizeof(double), cudaMemcpyHostToDevice, s);
-        cudaMemcpyAsync(st.remainder, rem.data(), nc * sizeof(double), cudaMemcpyHostToDevice, s);
-        cudaMemcpyAsync(st.xs, xs.data(), xs.size() * sizeof(double), cudaMemcpyHostToDevice, s);
-        if (cudaStreamSynchronize(s) != cudaSuccess) {
-            *msg = "MCC state: upload failed";
-            return PICGPU_CUDA_ERROR;
+    }
+    if (cfg.ion_mcc.enabled) {
+        const picgpu_ion_mcc& im = cfg.ion_mcc;
+        if (im.n_xs < 2 || im.n_xs > PICGPU_MAX_XS_POINTS || !im.xs_energy || !im.xs_elastic ||
+            !im.xs_charge_exchange) {
+            *msg = "ion MCC: cross-section tables missing";
+            return PICGPU_INVALID_ARG;
         }
+        if (im.ion_species < 0 || im.ion_species >= cfg.n_species) {
+            *msg = "ion MCC: ion species not set";
+            return PICGPU_INVALID_ARG;
+        }
+        if (!(cfg.mcc.gas_density > 0) || !(cfg.mcc.gas_mass > 0)) {
+            *msg = "ion MCC: background gas (mcc.gas_*) not set";
+            return PICGPU_INVALID_ARG;
+        }
+        if (!ascending(im.xs_energy, im.n_xs)) {
+            *msg = "ion MCC: cross-section energies must ascend";
+            return PICGPU_INVALID_ARG;
+        }
+        st.n_ixs = im.n_xs;
+        std::vector<double> xs(3 * size_t(im.n_xs));
+        for (int i = 0; i < im.n_xs; ++i) {
+            xs[i] = im.xs_energy[i];
+            xs[im.n_xs + i] = im.xs_elastic[i];
+            xs[2 * im.n_xs + i] = im.xs_charge_exchange[i];
+        }
+        double sv = im.sigma_v_max_init;
+        if (!(sv > 0))
+            sv = find_maximum(xs, im.n_xs, 3, cfg.species[im.ion_species].mass, im.find_max_energy,
+                              im.find_energy_step);
+        // remainders seeded U(0,1) (IonNeutralCollisionModel.C:199)
+        const int e =
+            upload_mcc(&st.isvmax, &st.iremainder, &st.ixs, xs, sv, cfg.seed, kStreamIonRemainder, nc, s, msg);
+        if (e) return e;
     }
     return PICGPU_OK;
 }
 
 void collide_free(CollideState& st) {
-    void* ptrs[] = {st.svmax, st.remainder, st.xs, st.cell_start, st.cell_count, st.cell_cursor, st.counts,
-                    st.scan_tmp, st.ncand, st.cand_off, st.stage, st.flags, st.pos, st.stage_tmp};
+    void* ptrs[] = {st.svmax,      st.remainder, st.xs,     st.isvmax, st.iremainder, st.ixs,   st.cell_start,
+                    st.cell_count, st.cell_cursor, st.counts, st.scan_tmp, st.ncand,  st.cand_off, st.stage,
+                    st.flags,      st.pos,       st.stage_tmp};
     for (void* p : ptrs)
         if (p) cudaFree(p);
     for (int s = 0; s < PICGPU_MAX_SPECIES; ++s) {
@@ -737,7 +1160,9 @@ int run_collisions(CollideState& st, const CollideArgs& a, int64_t counts[8], lo
         const int e = occupancy(st, a, s, msg, launches);
         if (e) return e;
     }
-    // Coulomb first, then electron-neutral (PICCloud::collisions, PICCloud.C:526-539)
+    // Coulomb, electron-neutral, then ion-neutral (PICCloud::collisions,
+    // PICCloud.C:526-539); parcels created on the way do not join the lists
+    // (PICCloud::addNewParcel adds to the cloud only)
     if (cfg.coulomb.enabled) {
         CoulombSpecies C{};
         for (int s = 0; s < a.n_species; ++s) {
@@ -753,14 +1178,22 @@ int run_collisions(CollideState& st, const CollideArgs& a, int64_t counts[8], lo
             C.sel2[k] = st.sel2[s];
             C.p[k] = a.sp[s];
         }
-        if (a.mixed)
-            coulomb_kernel<float><<<(nc + 63) / 64, 64, 0, a.stream>>>(
-                C, nc, a.m.vol, cfg.coulomb.coulomb_log, cfg.coulomb.allow_intra, cfg.dt, cfg.seed, uint32_t(a.step),
-                st.counts);
-        else
-            coulomb_kernel<double><<<(nc + 63) / 64, 64, 0, a.stream>>>(
-                C, nc, a.m.vol, cfg.coulomb.coulomb_log, cfg.coulomb.allow_intra, cfg.dt, cfg.seed, uint32_t(a.step),
-                st.counts);
+        CoulombParams K{};
+        K.n_cells = nc;
+        K.vol = a.m.vol;
+        K.cl = cfg.coulomb.coulomb_log;
+        K.takizuka_abe = cfg.coulomb.pairing == PICGPU_PAIRING_TAKIZUKA_ABE;
+        K.perez = cfg.coulomb.collide == PICGPU_COLLIDE_PEREZ;
+        K.allow_intra = cfg.coulomb.allow_intra;
+        K.calc_bmin = cfg.coulomb.calculate_bmin;
+        K.debye_drift = cfg.coulomb.debye_drift;
+        K.weight_corr = cfg.coulomb.weight_correction;
+        K.dt = cfg.dt;
+        K.seed = cfg.seed;
+        K.step = uint32_t(a.step);
+        K.counts = st.counts;
+        if (a.mixed) coulomb_kernel<float><<<(nc + 63) / 64, 64, 0, a.stream>>>(C, K);
+        else coulomb_kernel<double><<<(nc + 63) / 64, 64, 0, a.stream>>>(C, K);
         *launches += 1;
     }
     if (cfg.mcc.enabled) {
@@ -786,6 +1219,7 @@ int run_collisions(CollideState& st, const CollideArgs& a, int64_t counts[8], lo
         M.wNwE = 1.0 / M.wEwN;
         M.create_e = mc.create_electron;
         M.create_i = mc.create_ion;
+        M.relativistic = mc.scatter == 1;
         M.seed = cfg.seed;
         M.step = uint32_t(a.step);
         M.counts = st.counts;
@@ -839,6 +1273,32 @@ int run_collisions(CollideState& st, const CollideArgs& a, int64_t counts[8], lo
                 newn[s] += add;
             }
         }
+    }
+    // ion-neutral last, over the ions present before this step's secondaries
+    if (cfg.ion_mcc.enabled) {
+        const picgpu_mcc& gas = cfg.mcc;
+        const int is = cfg.ion_mcc.ion_species;
+        IonMccParams M{};
+        M.n_cells = nc;
+        M.i_start = st.cell_start + size_t(is) * (nc + 1);
+        M.i_idx = st.idx[is];
+        M.svmax = st.isvmax;
+        M.rem = st.iremainder;
+        M.xs = st.ixs;
+        M.n_xs = st.n_ixs;
+        M.n_gas = gas.gas_density;
+        M.mg = gas.gas_mass;
+        M.vth_gas = std::sqrt(kKb * gas.gas_temperature / gas.gas_mass);
+        M.mi = cfg.species[is].mass;
+        M.dt = cfg.dt;
+        for (int k = 0; k < 3; ++k) M.drift[k] = gas.gas_velocity[k];
+        M.cx_th = cfg.ion_mcc.cx_threshold;
+        M.seed = cfg.seed;
+        M.step = uint32_t(a.step);
+        M.counts = st.counts;
+        if (a.mixed) ion_mcc_kernel<float><<<(nc + 127) / 128, 128, 0, a.stream>>>(M, a.sp[is]);
+        else ion_mcc_kernel<double><<<(nc + 127) / 128, 128, 0, a.stream>>>(M, a.sp[is]);
+        *launches += 1;
     }
     unsigned long long h[8];
     cudaMemcpyAsync(h, st.counts, sizeof h, cudaMemcpyDeviceToHost, a.stream);

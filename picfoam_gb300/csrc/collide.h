@@ -1,4 +1,5 @@
-// collide.h -- collision step (cell occupancy, null-collision MCC, Coulomb).
+// collide.h -- collision step (cell occupancy, electron- and ion-neutral
+// null-collision MCC, binary Coulomb collisions).
 #pragma once
 
 #include <string>
@@ -24,11 +25,17 @@ struct CollideState {
     double* remainder = nullptr;  // collision remainder per cell
     double* xs = nullptr;         // 4 x n_xs: energy, elastic, excitation, ionisation
     int n_xs = 0;
+    double* isvmax = nullptr;     // ion-neutral (sigma v)_max per cell
+    double* iremainder = nullptr; // ion-neutral collision remainder per cell
+    double* ixs = nullptr;        // 3 x n_ixs: energy, elastic, charge exchange
+    int n_ixs = 0;
     int* cell_start = nullptr;    // per species: n_cells + 1 offsets into idx
     int* cell_count = nullptr;
     int* cell_cursor = nullptr;
     int* scan_tmp = nullptr;
-    unsigned long long* counts = nullptr;  // candidates, elastic, excitation, ionisation, coulomb pairs
+    // candidates, elastic, excitation, ionisation, coulomb pairs,
+    // ion candidates, ion elastic, ion charge exchange
+    unsigned long long* counts = nullptr;
     int* idx[PICGPU_MAX_SPECIES] = {};     // particle indices grouped by cell
     int* sel[PICGPU_MAX_SPECIES] = {};     // pairing permutations (scratch)
     int* sel2[PICGPU_MAX_SPECIES] = {};
@@ -62,7 +69,8 @@ void collide_free(CollideState& st);
 // particles: src -> dst, *kept = particles written.
 int sort_species(CollideState& st, const DMesh& m, int s, const DSpecies& src, const DSpecies& dst, long n,
                  bool mixed, long* kept, cudaStream_t stream, std::string* msg, int64_t* launches);
-// counts: candidates, elastic, excitation, ionisation, coulomb pairs; newn
+// counts: candidates, elastic, excitation, ionisation, coulomb pairs, ion
+// candidates, ion elastic, ion charge exchange; newn
 // receives the species counts after MCC secondaries were appended.
 int run_collisions(CollideState& st, const CollideArgs& a, int64_t counts[8], long newn[], int swapped[],
                    std::string* msg, int64_t* launches, double* phase_ms);

@@ -182,7 +182,13 @@ struct Philox {
     }
 };
 
-enum : uint32_t { kStreamMcc = 1u << 28, kStreamCoulomb = 2u << 28, kStreamRemainder = 3u << 28 };
+enum : uint32_t {
+    kStreamMcc = 1u << 28,
+    kStreamCoulomb = 2u << 28,
+    kStreamRemainder = 3u << 28,
+    kStreamIonMcc = 4u << 28,
+    kStreamIonRemainder = 5u << 28,
+};
 
 }  // namespace pgd
 

@@ -559,7 +559,7 @@ picgpu_status one_step(picgpu_ctx* c, picgpu_step_stats* stats, bool fields) {
     } else if ((s = compact(c, false))) {
         return s;
     }
-    if (c->cfg.mcc.enabled || c->cfg.coulomb.enabled) {
+    if (c->cfg.mcc.enabled || c->cfg.coulomb.enabled || c->cfg.ion_mcc.enabled) {
         if ((s = pgd_collisions(c, stats))) return s;
     }
     if ((s = charge_update(c))) return s;
@@ -626,6 +626,9 @@ picgpu_status pgd_collisions(picgpu_ctx* c, picgpu_step_stats* stats) {
         stats->mcc_excitation += counts[2];
         stats->mcc_ionization += counts[3];
         stats->coulomb_pairs += counts[4];
+        stats->ion_mcc_candidates += counts[5];
+        stats->ion_mcc_elastic += counts[6];
+        stats->ion_mcc_charge_exchange += counts[7];
     }
     return PICGPU_OK;
 }
@@ -697,8 +700,6 @@ picgpu_status picgpu_create(const picgpu_mesh_desc* mesh, const picgpu_config* c
         return bad(c, PICGPU_INVALID_ARG, "config: unknown ParticlePusher");
     if (cfg->precision != PICGPU_PREC_FP64 && cfg->precision != PICGPU_PREC_MIXED)
         return bad(c, PICGPU_INVALID_ARG, "config: unknown precision");
-    if (cfg->coulomb.enabled && !(cfg->coulomb.coulomb_log > 0))
-        return bad(c, PICGPU_NOT_SUPPORTED, "Coulomb: only a fixed coulombLog is supported");
     c->cfg = *cfg;
     c->mixed = cfg->precision == PICGPU_PREC_MIXED;
     c->rotation = cfg->B[0] != 0.0 || cfg->B[1] != 0.0 || cfg->B[2] != 0.0;

@@ -97,3 +97,266 @@ def test_coulomb_isotropises(oracle_backend):
     a2 = anis()
     # T_x / T_yz relaxes towards 1 monotonically (dt = 0.02 / nu, 50 steps ~ 1 relaxation time)
     assert a0 > a1 > a2 > 1.0
+
+
+# ------------------------------------------------------------------ Philox
+# Philox4x32-10 known-answer vectors published with the algorithm (Salmon,
+# Moraes, Dror & Shaw, SC'11; the Random123 kat_vectors file): counter,
+# key -> output block.
+PHILOX_KAT = [
+    ((0, 0, 0, 0), (0, 0), (0x6627E8D5, 0xE169C58D, 0xBC57AC4C, 0x9B00DBD8)),
+    ((0xFFFFFFFF,) * 4, (0xFFFFFFFF,) * 2, (0x408F276D, 0x41C83B0E, 0xA20BC7C6, 0x6D5451FD)),
+    ((0x243F6A88, 0x85A308D3, 0x13198A2E, 0x03707344), (0xA4093822, 0x299F31D0),
+     (0xD16CFE09, 0x94FDCCEB, 0x5001E420, 0x24126EA1)),
+]
+
+
+@pytest.mark.parametrize("ctr,key,expect", PHILOX_KAT)
+def test_philox_known_answers(oracle_backend, ctr, key, expect):
+    lib = oracle_backend.load()
+    c = (C.c_uint32 * 4)(*ctr)
+    k = (C.c_uint32 * 2)(*key)
+    out = (C.c_uint32 * 4)()
+    lib.oracle_philox4x32(c, k, out)
+    assert tuple(out) == expect
+
+
+# --------------------------------------------------------------- ion MCC
+def ion_speeds(sim):
+    _, _, U = sim.get_particles(0)
+    return U
+
+
+def test_ion_mcc_rates_match_n_sigma_v(oracle_backend):
+    # cold gas: the relative speed is the ion speed
+    case = cases.ion_swarm(N=20000, T_gas=1e-3, sigma_el=5e-19, sigma_cx=2.5e-19)
+    sim = cases.build(case, backend=oracle_backend.OracleBackend(4))
+    n_gas, dt = case.cfg.mcc.gas_density, case.cfg.dt
+    exp_el = exp_cx = 0.0
+    got_el = got_cx = 0
+    for _ in range(10):
+        v = np.linalg.norm(ion_speeds(sim), axis=1).sum()
+        exp_el += n_gas * 5e-19 * dt * v
+        exp_cx += n_gas * 2.5e-19 * dt * v
+        st = sim.step(1)
+        got_el += st.ion_mcc_elastic
+        got_cx += st.ion_mcc_charge_exchange
+        assert st.mcc_candidates == 0 and st.ion_mcc_candidates > 0
+    assert abs(got_el - exp_el) < 4 * math.sqrt(exp_el)
+    assert abs(got_cx - exp_cx) < 4 * math.sqrt(exp_cx)
+
+
+def test_ion_charge_exchange_thermalises_to_gas(oracle_backend):
+    # charge exchange alone hands every ion a gas velocity: the ion mean
+    # energy relaxes from 1.5 eV to 1.5 k T_gas
+    case = cases.ion_swarm(N=4000, n_cells=(4, 4, 4), T_i=1.0, T_gas=300.0, sigma_el=0.0, sigma_cx=5e-19,
+                           steps_dt=0.2)
+    sim = cases.build(case, backend=oracle_backend.OracleBackend(4))
+    sim.step(200)
+    U = ion_speeds(sim)
+    e_mean = 0.5 * cases.M_AR * (U * U).sum(axis=1).mean()
+    assert abs(e_mean / (1.5 * cases.K_B * 300.0) - 1.0) < 0.08
+
+
+def test_ion_charge_exchange_threshold(oracle_backend):
+    # a threshold above every ion energy turns charge exchange off
+    case = cases.ion_swarm(N=4000, n_cells=(4, 4, 4), T_i=0.01, sigma_el=0.0, sigma_cx=5e-19, cx_threshold=10.0)
+    sim = cases.build(case, backend=oracle_backend.OracleBackend(2))
+    st = sim.step(5)
+    assert st.ion_mcc_candidates > 0 and st.ion_mcc_charge_exchange == 0 and st.ion_mcc_elastic == 0
+
+
+def test_ion_isotropic_scattering_equal_mass_energy(oracle_backend):
+    # equal masses, cold gas: an isotropic CoM scatter leaves the ion half its
+    # energy on average, so the mean energy of the population after one step
+    # is E0 (1 - f/2) with f the fraction of ions hit (no repeats at f << 1)
+    case = cases.ion_swarm(N=40000, T_gas=1e-3, sigma_el=5e-19, sigma_cx=0.0, steps_dt=0.05)
+    sim = cases.build(case, backend=oracle_backend.OracleBackend(4))
+    U0 = ion_speeds(sim)
+    st = sim.step(1)
+    U1 = ion_speeds(sim)
+    # the relativistic push round-trips u = gamma v to within ulps: a hit
+    # changes the velocity by far more
+    hit = np.linalg.norm(U1 - U0, axis=1) > 1e-9 * np.linalg.norm(U0, axis=1)
+    assert hit.sum() == st.ion_mcc_elastic
+    e0 = (U0[hit] ** 2).sum(axis=1)
+    e1 = (U1[hit] ** 2).sum(axis=1)
+    assert abs(e1.sum() / e0.sum() - 0.5) < 0.05
+
+
+# ------------------------------------------------- relativistic scattering
+def test_relativistic_electron_neutral_scatter(oracle_backend):
+    case = constant_xs_swarm()
+    case.cfg.mcc.scatter = 1
+    sim = cases.build(case, backend=oracle_backend.OracleBackend(4))
+    n_gas, sigma, dt = case.cfg.mcc.gas_density, 1e-19, case.cfg.dt
+    d0 = sim.diagnostics()
+    expected = 0.0
+    got = 0
+    for _ in range(10):
+        _, _, U = sim.get_particles(0)
+        expected += n_gas * sigma * dt * np.linalg.norm(U, axis=1).sum()
+        got += sim.step(1).mcc_elastic
+    assert abs(got - expected) < 4 * math.sqrt(expected)
+    # a cold heavy partner takes ~2 m/M of the energy per collision
+    d1 = sim.diagnostics()
+    assert abs(d1.kinetic_energy[0] / d0.kinetic_energy[0] - 1.0) < 1e-3
+
+
+# ------------------------------------------------------------- Coulomb
+def cell_counts(sim, species, n_cells):
+    tet, _, _ = sim.get_particles(species)
+    return np.bincount(tet // 12, minlength=n_cells)
+
+
+def ta_pairs(nA, nB):
+    """Pairs the TakizukaAbe algorithm collides in one cell (intra-species
+    for both species, then inter-species; TakizukaAbePairing.C:101-314)."""
+    p = 0
+    for n in (nA, nB):
+        if n > 1:
+            p += 2 + n // 2 if n % 2 else n // 2
+    if min(nA, nB) > 0:
+        if nA == nB:
+            p += nA
+        else:
+            nMax, nMin = max(nA, nB), min(nA, nB)
+            delta = nMax // nMin
+            dr = (nMax % nMin) / nMin
+            p += int((delta + 1) * dr * nMin) + int(delta * (1.0 - dr) * nMin)
+    return p
+
+
+def relativistic_totals(sim, case):
+    P = np.zeros(3)
+    E = 0.0
+    for s in range(case.cfg.n_species):
+        _, _, U = sim.get_particles(s)
+        m, w = case.cfg.species[s].mass, case.cfg.species[s].weight
+        a = np.linalg.norm(U, axis=1) / cases.C_LIGHT
+        g = 1.0 / np.sqrt(1.0 - a * a)
+        P += (m * w * g[:, None] * U).sum(axis=0)
+        E += (m * w * cases.C_LIGHT ** 2 * (a * a) * g * g / (g + 1.0)).sum()  # (g - 1) m c^2
+    return P, E
+
+
+def momentum_energy(sim, case):
+    """Non-relativistic totals sum(w m U), sum(w m U^2 / 2): the invariants of
+    the Nanbu collide."""
+    P = np.zeros(3)
+    E = 0.0
+    for s in range(case.cfg.n_species):
+        _, _, U = sim.get_particles(s)
+        m, w = case.cfg.species[s].mass, case.cfg.species[s].weight
+        P += (m * w * U).sum(axis=0)
+        E += 0.5 * m * w * (U * U).sum()
+    return P, E
+
+
+def temperatures(sim, case):
+    T = []
+    for s in range(case.cfg.n_species):
+        _, _, U = sim.get_particles(s)
+        T.append(case.cfg.species[s].mass * (U * U).sum(axis=1).mean() / (3 * cases.E_CHARGE))
+    return T
+
+
+def test_takizuka_abe_pair_count_and_conservation(oracle_backend):
+    case = cases.coulomb_relaxation(ragged=True, pairing=abi.PAIRING_TAKIZUKA_ABE)
+    sim = cases.build(case, backend=oracle_backend.OracleBackend(2))
+    n_c = 4 ** 3
+    P0, E0 = momentum_energy(sim, case)
+    T0 = temperatures(sim, case)
+    for _ in range(3):
+        st = sim.step(1)
+        ce, ci = cell_counts(sim, 0, n_c), cell_counts(sim, 1, n_c)
+        assert st.coulomb_pairs == sum(ta_pairs(int(a), int(b)) for a, b in zip(ce, ci))
+    P1, E1 = momentum_energy(sim, case)
+    # thermal momentum of the whole electron population
+    pscale = np.sqrt(2 * cases.M_E * E0 * case.cfg.species[0].weight * case.meta["Ne"])
+    assert np.abs(P1 - P0).max() < 1e-9 * pscale
+    # the relativistic push with E = 0 round-trips U to within ulps
+    assert abs(E1 / E0 - 1.0) < 1e-11
+    T1 = temperatures(sim, case)
+    assert T1[0] < T0[0] and T1[1] > T0[1]
+
+
+def test_takizuka_abe_needs_equal_weights(oracle_backend):
+    from picfoam_gb300.simulation import PicError
+    case = cases.coulomb_relaxation(pairing=abi.PAIRING_TAKIZUKA_ABE, w_i_factor=2.0)
+    with pytest.raises(PicError):
+        cases.build(case, backend=oracle_backend.OracleBackend(1))
+
+
+def test_perez_conserves_relativistic_momentum_and_energy(oracle_backend):
+    case = cases.coulomb_relaxation(collide=abi.COLLIDE_PEREZ, T_e=2000.0, T_i=500.0, m_i=4.0 * cases.M_E)
+    case.cfg.dt = 1e-13  # under a cell crossing at 2 keV
+    sim = cases.build(case, backend=oracle_backend.OracleBackend(2))
+    P0, E0 = relativistic_totals(sim, case)
+    st = sim.step(3)
+    assert st.coulomb_pairs > 0
+    P1, E1 = relativistic_totals(sim, case)
+    pscale = np.sqrt(2 * cases.M_E * E0 * case.cfg.species[0].weight * case.meta["Ne"])
+    assert np.abs(P1 - P0).max() < 1e-9 * pscale
+    assert abs(E1 / E0 - 1.0) < 1e-10
+
+
+def test_perez_matches_nanbu_at_low_temperature(oracle_backend):
+    # the Perez scattering parameter reduces to Nanbu's when v << c, and both
+    # draw cos(chi) then the azimuth from the same streams
+    out = []
+    for col in (abi.COLLIDE_NANBU, abi.COLLIDE_PEREZ):
+        case = cases.coulomb_thermalisation(n_cells=4, per_cell=200, L=2e-5, collide=col)
+        sim = cases.build(case, backend=oracle_backend.OracleBackend(2))
+        sim.step(25)
+        d = sim.diagnostics()
+        v = np.array(d.velocity_sq[0]) / d.weight_sum[0]
+        out.append(v[0] / (0.5 * (v[1] + v[2])))
+    assert out[0] < 1.9 and abs(out[0] - out[1]) < 1e-2
+
+
+def test_debye_length_matches_formula(oracle_backend):
+    case = cases.coulomb_relaxation(coulomb_log=0.0, ragged=True)
+    sim = cases.build(case, backend=oracle_backend.OracleBackend(1))
+    lib = oracle_backend.load()
+    V = (2e-5 / 4) ** 3
+    parts = [sim.get_particles(s) for s in range(2)]
+    for cell in (0, 5, 17, 63):
+        debye, n_max = 0.0, 0.0
+        for s, (tet, _, U) in enumerate(parts):
+            sel = tet // 12 == cell
+            if not sel.any():
+                continue
+            sp = case.cfg.species[s]
+            n = sel.sum() * sp.weight / V
+            n_max = max(n_max, n)
+            u = U[sel]
+            T = sp.mass / (3 * cases.K_B) * ((u * u).sum(axis=1).mean() - (u.mean(axis=0) ** 2).sum())
+            debye += n * sp.charge ** 2 / cases.EPS0 / (T * cases.K_B)
+        expect = max((4 * math.pi * n_max / 3) ** (-1 / 3), math.sqrt(1 / debye)) if debye > 0 else 0.0
+        got = lib.oracle_debye_length(sim._h, cell)
+        assert got == pytest.approx(expect, rel=1e-9)
+
+
+def test_computed_coulomb_log_slows_relaxation(oracle_backend):
+    # for n = 1e18 m^-3 and ~1.3 eV the logarithm from the Debye length is
+    # near 9-10, so the anisotropy relaxes more slowly than with 15
+    out = []
+    for cl in (15.0, 0.0):
+        case = cases.coulomb_thermalisation(n_cells=4, per_cell=200, L=2e-5, coulomb_log=cl)
+        sim = cases.build(case, backend=oracle_backend.OracleBackend(2))
+        sim.step(25)
+        d = sim.diagnostics()
+        v = np.array(d.velocity_sq[0]) / d.weight_sum[0]
+        out.append(v[0] / (0.5 * (v[1] + v[2])))
+    assert 1.0 < out[0] < out[1] < 2.0
+
+
+def test_nanbu_weight_correction_unequal_weights(oracle_backend):
+    case = cases.coulomb_relaxation(w_i_factor=2.0, weight_correction=1)
+    sim = cases.build(case, backend=oracle_backend.OracleBackend(2))
+    T0 = temperatures(sim, case)
+    st = sim.step(10)
+    assert st.coulomb_pairs > 0
+    T1 = temperatures(sim, case)
+    assert T1[0] < T0[0] and T1[1] > T0[1]

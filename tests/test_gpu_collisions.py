@@ -78,3 +78,69 @@ def test_coulomb_mixed_isotropisation_rate(gpu, oracle_backend):
         o.step(25)
         # 12800 electrons: the anisotropy agrees to a few percent
         assert abs(anis(g) - anis(o)) < 0.05
+
+
+def close_fraction(g, o, species, rtol):
+    tg, _, ug = g.get_particles(species)
+    to, _, uo = o.get_particles(species)
+    np.testing.assert_array_equal(tg, to)
+    return np.isclose(ug, uo, rtol=rtol, atol=rtol * np.abs(uo).max()).all(axis=1).mean()
+
+
+def test_ion_mcc_fp64_matches_oracle(gpu, oracle_backend):
+    case = cases.ion_swarm(N=20000, T_gas=300.0, sigma_el=5e-19, sigma_cx=2.5e-19, steps_dt=0.05)
+    g, o, sg, so = run_pair(case, gpu, oracle_backend, 4)
+    for a, b in zip(sg, so):
+        assert a.ion_mcc_candidates == b.ion_mcc_candidates > 0
+        assert abs(a.ion_mcc_elastic - b.ion_mcc_elastic) <= 2
+        assert abs(a.ion_mcc_charge_exchange - b.ion_mcc_charge_exchange) <= 2
+    assert close_fraction(g, o, 0, 1e-9) > 0.999
+
+
+def test_ion_charge_exchange_mixed_thermalises(gpu):
+    case = cases.ion_swarm(N=4000, n_cells=(4, 4, 4), T_i=1.0, T_gas=300.0, sigma_el=0.0, sigma_cx=5e-19,
+                           steps_dt=0.2, precision=abi.PREC_MIXED)
+    sim = cases.build(case, backend=gpu)
+    sim.step(200)
+    _, _, U = sim.get_particles(0)
+    e_mean = 0.5 * cases.M_AR * (U * U).sum(axis=1).mean()
+    assert abs(e_mean / (1.5 * cases.K_B * 300.0) - 1.0) < 0.08
+
+
+def test_relativistic_scatter_fp64_matches_oracle(gpu, oracle_backend):
+    case = constant_xs_swarm(N=20000)
+    case.cfg.mcc.scatter = 1
+    g, o, sg, so = run_pair(case, gpu, oracle_backend, 4)
+    for a, b in zip(sg, so):
+        assert a.mcc_candidates == b.mcc_candidates
+        assert abs(a.mcc_elastic - b.mcc_elastic) <= 2
+    assert close_fraction(g, o, 0, 1e-9) > 0.999
+
+
+@pytest.mark.parametrize("collide", [abi.COLLIDE_NANBU, abi.COLLIDE_PEREZ])
+def test_takizuka_abe_fp64_matches_oracle(gpu, oracle_backend, collide):
+    # ragged per-cell counts: empty, single, odd and unequal cells
+    case = cases.coulomb_relaxation(ragged=True, pairing=abi.PAIRING_TAKIZUKA_ABE, collide=collide)
+    g, o, sg, so = run_pair(case, gpu, oracle_backend, 4)
+    for a, b in zip(sg, so):
+        assert a.coulomb_pairs == b.coulomb_pairs > 0
+    for s in range(2):
+        assert close_fraction(g, o, s, 1e-8) > 0.99
+
+
+def test_computed_coulomb_log_fp64_matches_oracle(gpu, oracle_backend):
+    case = cases.coulomb_relaxation(ragged=True, coulomb_log=0.0, collide=abi.COLLIDE_PEREZ)
+    g, o, sg, so = run_pair(case, gpu, oracle_backend, 4)
+    for a, b in zip(sg, so):
+        assert a.coulomb_pairs == b.coulomb_pairs > 0
+    for s in range(2):
+        assert close_fraction(g, o, s, 1e-8) > 0.99
+
+
+def test_weight_correction_fp64_matches_oracle(gpu, oracle_backend):
+    case = cases.coulomb_relaxation(w_i_factor=2.0, weight_correction=1, coulomb_log=0.0)
+    g, o, sg, so = run_pair(case, gpu, oracle_backend, 4)
+    for a, b in zip(sg, so):
+        assert a.coulomb_pairs == b.coulomb_pairs > 0
+    for s in range(2):
+        assert close_fraction(g, o, s, 1e-8) > 0.99
