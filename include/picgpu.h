@@ -230,6 +230,7 @@ typedef struct {
     int32_t pcg_iterations_total;               /* summed over the call */
     double  pcg_residual_l2;                    /* last solve ||b-Ax||2/||b||2 */
     double  pcg_residual_of;                    /* last solve OpenFOAM-normalised */
+    double  pcg_residual_initial;               /* last solve ||b-Ax0||2/||b||2 of the start guess */
     int64_t mcc_candidates;
     int64_t mcc_elastic;
     int64_t mcc_excitation;

@@ -62,25 +62,49 @@ struct Parcel {
     bool alive = true;
 };
 
-// Deterministic reduction: the fixed order the CUDA kernels reduce in
-// (256 threads, 2 strided items per thread, warp xor-tree, 8-warp tree).
+// Deterministic reduction: the fixed order the CUDA kernels reduce in (256
+// threads, kItems = 4 strided items per thread; lane l adds threads l, l+32,
+// ..., l+224 in turn, then a 32-lane xor-tree).
 double tree_block(const double* acc /*256*/) {
-    double w[8];
-    for (int wi = 0; wi < 8; ++wi) {
-        double a[32];
-        for (int l = 0; l < 32; ++l) a[l] = acc[32 * wi + l];
-        for (int off = 16; off >= 1; off >>= 1)
-            for (int l = 0; l < off; ++l) a[l] = a[l] + a[l + off];
-        w[wi] = a[0];
+    double a[32];
+    for (int l = 0; l < 32; ++l) {
+        a[l] = acc[l];
+        for (int j = 1; j < 8; ++j) a[l] = a[l] + acc[l + 32 * j];
     }
-    for (int off = 4; off >= 1; off >>= 1)
-        for (int l = 0; l < off; ++l) w[l] = w[l] + w[l + off];
-    return w[0];
+    for (int off = 16; off >= 1; off >>= 1)
+        for (int l = 0; l < off; ++l) a[l] = a[l] + a[l + off];
+    return a[0];
+}
+
+// det_sum with the GPU's fused accumulation s = fma(a_i, b_i, s).
+double det_dot(long n, const double* a, const double* b) {
+    const int items = 4;
+    const long chunk = 256 * items;
+    const long nb = (n + chunk - 1) / chunk;
+    std::vector<double> part(std::max<long>(nb, 1), 0.0);
+    double acc[256];
+    for (long blk = 0; blk < nb; ++blk) {
+        for (int t = 0; t < 256; ++t) {
+            double s = 0.0;
+            for (int j = 0; j < items; ++j) {
+                const long i = blk * chunk + long(j) * 256 + t;
+                if (i < n) s = std::fma(a[i], b[i], s);
+            }
+            acc[t] = s;
+        }
+        part[blk] = tree_block(acc);
+    }
+    for (int t = 0; t < 256; ++t) {
+        double s = 0.0;
+        for (long i = t; i < nb; i += 256) s = s + part[i];
+        acc[t] = s;
+    }
+    return tree_block(acc);
 }
 
 template <class F>
 double det_sum(long n, F term) {
-    const int items = 2;
+    const int items = 4;
     const long chunk = 256 * items;
     const long nb = (n + chunk - 1) / chunk;
     std::vector<double> part(std::max<long>(nb, 1), 0.0);
@@ -527,7 +551,7 @@ void apply_M(const Oracle& o, const std::vector<double>& x, std::vector<double>&
         double s = o.Mdiag[c] * x[c];
         for (int f = 0; f < 6; ++f) {
             const int nb = m.nbr[6 * size_t(c) + f];
-            if (nb >= 0) s = s + o.Moff[6 * size_t(c) + f] * x[nb];
+            if (nb >= 0) s = std::fma(o.Moff[6 * size_t(c) + f], x[nb], s);
         }
         y[c] = s;
     }
@@ -555,37 +579,52 @@ double of_residual(const Oracle& o, const std::vector<double>& b, const std::vec
 }
 
 // PCG with the Jacobi preconditioner, reductions in the GPU's fixed order.
+// Jacobi-preconditioned CG in the Chronopoulos-Gear form the GPU runs (one
+// reduction point per iteration), with the GPU's operation order, fused
+// multiply-adds and reduction tree, so both produce the same bits.  The iterates equal those
+// of the textbook PCG of lduMatrix in exact arithmetic.
 int pcg_jacobi(Oracle& o, const std::vector<double>& b, std::vector<double>& x, double tol,
                int maxit, double* res) {
     const long n = o.m.n_cells;
-    std::vector<double> r(n), z(n), p(n), q(n);
-    apply_M(o, x, q);
-    for (long i = 0; i < n; ++i) r[i] = b[i] - q[i];
-    for (long i = 0; i < n; ++i) z[i] = o.dinv[i] * r[i];
-    double rz = det_sum(n, [&](long i) { return r[i] * z[i]; });
-    double rr = det_sum(n, [&](long i) { return r[i] * r[i]; });
-    const double bb = det_sum(n, [&](long i) { return b[i] * b[i]; });
+    std::vector<double> r(n), u(n), w(n), p(n), s(n);
+    apply_M(o, x, w);
+    for (long i = 0; i < n; ++i) {
+        r[i] = b[i] - w[i];
+        u[i] = o.dinv[i] * r[i];
+    }
+    double g = det_dot(n, r.data(), u.data());
+    double rr = det_dot(n, r.data(), r.data());
+    const double bb = det_dot(n, b.data(), b.data());
+    apply_M(o, u, w);
+    double d = det_dot(n, w.data(), u.data());
     const double lim = (tol * tol) * bb;
+    double alpha = g / d, beta = 0.0;
     int it = 0;
     if (!(rr <= lim)) {
-        p = z;
-        for (it = 1; it <= maxit; ++it) {
-            apply_M(o, p, q);
-            const double pq = det_sum(n, [&](long i) { return p[i] * q[i]; });
-            const double alpha = rz / pq;
+        for (int k = 0;;) {
             for (long i = 0; i < n; ++i) {
-                x[i] = x[i] + alpha * p[i];
-                r[i] = r[i] - alpha * q[i];
-                z[i] = o.dinv[i] * r[i];
+                if (k == 0) {
+                    p[i] = u[i];
+                    s[i] = w[i];
+                } else {
+                    p[i] = std::fma(beta, p[i], u[i]);
+                    s[i] = std::fma(beta, s[i], w[i]);
+                }
+                x[i] = std::fma(alpha, p[i], x[i]);
+                r[i] = std::fma(-alpha, s[i], r[i]);
+                u[i] = o.dinv[i] * r[i];
             }
-            const double rzn = det_sum(n, [&](long i) { return r[i] * z[i]; });
-            rr = det_sum(n, [&](long i) { return r[i] * r[i]; });
-            if (rr <= lim) break;
-            const double beta = rzn / rz;
-            rz = rzn;
-            for (long i = 0; i < n; ++i) p[i] = z[i] + beta * p[i];
+            const double gn = det_dot(n, r.data(), u.data());
+            rr = det_dot(n, r.data(), r.data());
+            apply_M(o, u, w);
+            d = det_dot(n, w.data(), u.data());
+            ++k;
+            if (rr <= lim) { it = k; break; }
+            if (k >= maxit) { it = -maxit; break; }
+            beta = gn / g;
+            alpha = gn / (d - beta * gn / alpha);
+            g = gn;
         }
-        if (it > maxit) it = -maxit;
     }
     *res = bb > 0 ? std::sqrt(rr / bb) : 0.0;
     return it;
@@ -715,6 +754,16 @@ int solve_fields(Oracle& o, picgpu_step_stats* st) {
     std::vector<double> b;
     assemble_rhs(o, o.rho.data(), b);
     double res = 0;
+    double r0 = 0, bb = 0;
+    for (int i = 0; i < o.m.n_cells; ++i) {
+        double ax = o.Mdiag[i] * o.phi[i];
+        for (int k = 0; k < 6; ++k) {
+            const int j = o.m.nbr[6 * size_t(i) + k];
+            if (j >= 0) ax += o.Moff[6 * size_t(i) + k] * o.phi[j];
+        }
+        r0 += (b[i] - ax) * (b[i] - ax);
+        bb += b[i] * b[i];
+    }
     const int maxit = o.cfg.pcg_max_iter > 0 ? o.cfg.pcg_max_iter : 10000;
     const double tol = o.cfg.pcg_tol > 0 ? o.cfg.pcg_tol : 1e-10;
     int it = o.precond == ORACLE_PRECOND_DIC ? pcg_dic(o, b, o.phi, tol, maxit, &res)
@@ -727,6 +776,7 @@ int solve_fields(Oracle& o, picgpu_step_stats* st) {
         st->pcg_iterations_total += o.last_pcg_iter;
         st->pcg_residual_l2 = res;
         st->pcg_residual_of = o.last_res_of;
+        st->pcg_residual_initial = bb > 0 ? std::sqrt(r0 / bb) : 0.0;
     }
     compute_E(o);
     return it < 0 ? PICGPU_PCG_NOT_CONVERGED : 0;

@@ -127,6 +127,7 @@ class StepStats(C.Structure):
         ("tet_steps", C.c_int64), ("face_crossings", C.c_int64), ("wall_hits", C.c_int64),
         ("pcg_iterations", C.c_int32), ("pcg_iterations_total", C.c_int32),
         ("pcg_residual_l2", C.c_double), ("pcg_residual_of", C.c_double),
+        ("pcg_residual_initial", C.c_double),
         ("mcc_candidates", C.c_int64), ("mcc_elastic", C.c_int64),
         ("mcc_excitation", C.c_int64), ("mcc_ionization", C.c_int64),
         ("coulomb_pairs", C.c_int64),

@@ -82,6 +82,8 @@ struct DMesh {
     const int* pc_start;     // n_points + 1: point -> cell-corner slots
     const int* pc_slot;
     int uniform;             // one geometry class (block mesh of equal cells)
+    int lap_uniform;         // every coupled face in direction f has M coefficient lap_coef[f]
+    double lap_coef[6];
 };
 
 // Per-species particle storage (structure of arrays).

@@ -1,10 +1,11 @@
 // fields.cu -- charge density, electrostatic Poisson PCG and the E field.
 //
 // Built with --fmad=false: each kernel evaluates in the order of the CPU
-// oracle, and every reduction runs in one fixed tree order (256 threads, 2
-// strided items per thread, warp xor-tree, 8-warp tree; the last block of a
-// launch combines the block partials in the same order), so the FP64 Poisson
-// solve is bit-reproducible and matches the oracle bit for bit.
+// oracle, and every reduction runs in one fixed tree order (256 threads,
+// kItems strided items per thread; lane l of warp 0 adds threads l, l+32, ...,
+// l+224, then a warp xor-tree; the last block of a launch combines the block
+// partials in the same order), so the FP64 Poisson solve is bit-reproducible
+// and matches the oracle bit for bit.
 //
 //   charge_update   ChargeDistribution::update (VolumeWeighting.C:138-164,
 //                   CellAverage.C:63-68) + spaceCharge (PICCloud.C:687-690)
@@ -26,19 +27,21 @@ constexpr double kMu0 = 4.0 * kPi * 1e-7;
 __device__ __forceinline__ double eps0() { return 1.0 / (kMu0 * kC * kC); }
 
 // ------------------------------------------------------- reductions ------
-// Sum over the block in the fixed tree order; the result is valid in every
-// lane of warp 0.
+// Sum over the block in the fixed tree order: lane l of warp 0 adds the
+// values of threads l, l+32, ..., l+224 in turn, then the 32 lanes meet in an
+// xor-tree.  One warp does the FP64 adds (the FP64 pipe is the scarce unit on
+// this part).  ws holds 256 doubles; the result is valid in every lane of
+// warp 0.
 __device__ __forceinline__ double block_tree(double v, double* ws) {
-#pragma unroll
-    for (int off = 16; off >= 1; off >>= 1) v = v + __shfl_xor_sync(0xffffffffu, v, off);
-    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-    if (lane == 0) ws[warp] = v;
+    ws[threadIdx.x] = v;
     __syncthreads();
     double r = 0.0;
-    if (warp == 0) {
-        r = lane < 8 ? ws[lane] : 0.0;
+    if (threadIdx.x < 32) {
+        r = ws[threadIdx.x];
 #pragma unroll
-        for (int off = 4; off >= 1; off >>= 1) r = r + __shfl_xor_sync(0xffffffffu, r, off);
+        for (int j = 1; j < 8; ++j) r = r + ws[threadIdx.x + 32 * j];
+#pragma unroll
+        for (int off = 16; off >= 1; off >>= 1) r = r + __shfl_xor_sync(0xffffffffu, r, off);
     }
     __syncthreads();
     return r;
@@ -176,7 +179,7 @@ __global__ void rhs_kernel(DMesh m, const double* __restrict__ rho, const double
 
 __global__ void __launch_bounds__(256) sum_kernel(const double* __restrict__ v, int n,
                                                   double* part, PcgState* st) {
-    __shared__ double ws[8];
+    __shared__ double ws[256];
     double s = 0.0;
     const long base = long(blockIdx.x) * kChunk + threadIdx.x;
 #pragma unroll
@@ -197,157 +200,174 @@ __global__ void sub_mean_kernel(double* b, int n, const PcgState* st) {
     if (i < n) b[i] = b[i] - st->mean;
 }
 
-__device__ __forceinline__ double apply_M(const DMesh& m, const double* x, int c) {
+// y = M x in the row of cell c.  On a uniform block mesh every coupled face
+// in direction f carries the same coefficient (the mesh builder computes it
+// from the one geometry class; the host checks every face), so the per-face
+// array is not read.
+template <bool Uniform>
+__device__ __forceinline__ double apply_M(const DMesh& m, const double* __restrict__ x, int c) {
     double s = m.Mdiag[c] * x[c];
 #pragma unroll
     for (int f = 0; f < 6; ++f) {
         const int nb = m.nbr[6 * size_t(c) + f];
-        if (nb >= 0) s = s + m.Moff[6 * size_t(c) + f] * x[nb];
+        if (nb >= 0) s = fma(Uniform ? m.lap_coef[f] : m.Moff[6 * size_t(c) + f], x[nb], s);
     }
     return s;
 }
 
+// The PCG runs in the Chronopoulos-Gear form (one reduction point per
+// iteration): with u = D^-1 r, w = M u, s = M p,
+//   p = u + beta p,  s = w + beta s,  x += alpha p,  r -= alpha s,  u = D^-1 r
+//   w = M u,  gamma = r.u,  delta = w.u,  beta = gamma / gamma_old,
+//   alpha = gamma / (delta - beta gamma / alpha_old).
+// It is the same Krylov iteration as the textbook PCG of lduMatrix (the
+// iterates agree in exact arithmetic) with one global synchronisation per
+// iteration instead of two and no per-thread division.  The vector updates,
+// the SpMV and the dot products use explicit fused multiply-adds (the oracle
+// calls std::fma at the same places): FP64 issue is the bound of both kernels
+// on this part, and a fused a*b + c is one FP64 instruction instead of two.
+
+// r = b - M x, u = D^-1 r; partials of gamma = r.u, r.r and b.b.
+template <bool Uniform>
 __global__ void __launch_bounds__(256) pcg_init_kernel(DMesh m, const double* __restrict__ b,
-                                                       const double* __restrict__ x,
-                                                       double* __restrict__ r, double* __restrict__ z,
-                                                       double* part, PcgState* st, double tol) {
-    __shared__ double ws[8];
+                                                       const double* __restrict__ x, double* __restrict__ r,
+                                                       double* __restrict__ u, double* part) {
+    __shared__ double ws[256];
     const int n = m.n_cells;
     const int nb = gridDim.x;
-    double srz = 0.0, srr = 0.0, sbb = 0.0;
+    double sg = 0.0, srr = 0.0, sbb = 0.0;
     const long base = long(blockIdx.x) * kChunk + threadIdx.x;
 #pragma unroll
     for (int j = 0; j < kItems; ++j) {
         const long i = base + j * 256;
         if (i < n) {
-            const double mx = apply_M(m, x, int(i));
+            const double mx = apply_M<Uniform>(m, x, int(i));
             const double ri = b[i] - mx;
-            const double zi = m.dinv[i] * ri;
+            const double ui = m.dinv[i] * ri;
             r[i] = ri;
-            z[i] = zi;
-            srz = srz + ri * zi;
-            srr = srr + ri * ri;
-            sbb = sbb + b[i] * b[i];
+            u[i] = ui;
+            sg = fma(ri, ui, sg);
+            srr = fma(ri, ri, srr);
+            sbb = fma(b[i], b[i], sbb);
         }
     }
-    const double b0 = block_tree(srz, ws);
+    const double b0 = block_tree(sg, ws);
     const double b1 = block_tree(srr, ws);
     const double b2 = block_tree(sbb, ws);
     if (threadIdx.x == 0) {
         part[blockIdx.x] = b0;
         part[nb + blockIdx.x] = b1;
-        part[2 * nb + blockIdx.x] = b2;
-    }
-    if (arrive_last(&st->ticket)) {
-        const double rz = final_sum(part, nb, ws);
-        const double rr = final_sum(part + nb, nb, ws);
-        const double bb = final_sum(part + 2 * nb, nb, ws);
-        if (threadIdx.x == 0) {
-            st->rz = rz;
-            st->rr = rr;
-            st->bb = bb;
-            st->lim = (tol * tol) * bb;
-            st->iters = 0;
-            st->k = 0;
-            st->done = rr <= st->lim ? 1 : 0;
-            st->converged = st->done;
-        }
+        part[3 * nb + blockIdx.x] = b2;
     }
 }
 
-// q = M p_new with p_new = z + beta p_old (p_new = z on the first iteration),
-// partial sums of p_new . q.
-__global__ void __launch_bounds__(256) pcg_spmv_kernel(DMesh m, const double* __restrict__ z,
-                                                       const double* __restrict__ p_old,
-                                                       double* __restrict__ p_new,
-                                                       double* __restrict__ q, double* part,
-                                                       PcgState* st) {
-    if (st->done) return;
-    __shared__ double ws[8];
-    const int n = m.n_cells;
-    const int first = st->k == 0;
-    const double beta = st->beta;
-    double acc = 0.0;
-    const long base = long(blockIdx.x) * kChunk + threadIdx.x;
-#pragma unroll 1
-    for (int j = 0; j < kItems; ++j) {
-        const long i = base + j * 256;
-        if (i < n) {
-            const double pi = first ? z[i] : z[i] + beta * p_old[i];
-            double s = m.Mdiag[i] * pi;
-#pragma unroll
-            for (int f = 0; f < 6; ++f) {
-                const int nb = m.nbr[6 * size_t(i) + f];
-                if (nb >= 0) {
-                    const double pn = first ? z[nb] : z[nb] + beta * p_old[nb];
-                    s = s + m.Moff[6 * size_t(i) + f] * pn;
-                }
-            }
-            p_new[i] = pi;
-            q[i] = s;
-            acc = acc + pi * s;
-        }
-    }
-    const double bs = block_tree(acc, ws);
-    if (threadIdx.x == 0) part[blockIdx.x] = bs;
-    if (arrive_last(&st->ticket)) {
-        const double pq = final_sum(part, gridDim.x, ws);
-        if (threadIdx.x == 0) st->pq = pq;
-    }
-}
-
-__global__ void __launch_bounds__(256) pcg_update_kernel(DMesh m, double* __restrict__ x,
-                                                         double* __restrict__ r, double* __restrict__ z,
-                                                         const double* __restrict__ p,
-                                                         const double* __restrict__ q, double* part,
-                                                         PcgState* st, int maxit) {
-    if (st->done) return;
-    __shared__ double ws[8];
+// w = M u; partial delta = w.u.  The last block finalises: after the
+// initialisation (init = 1) it sets alpha_0, otherwise it closes iteration
+// k + 1 (convergence test on r.r, then beta and alpha).
+template <bool Uniform>
+__global__ void __launch_bounds__(256) pcg_spmv_kernel(DMesh m, const double* __restrict__ u,
+                                                       double* __restrict__ w, double* part, PcgState* st,
+                                                       int init, double tol, int maxit) {
+    if (!init && st->done) return;
+    __shared__ double ws[256];
     const int n = m.n_cells;
     const int nb = gridDim.x;
-    const int k = st->k + 1;
-    const double alpha = st->rz / st->pq;
-    double srz = 0.0, srr = 0.0;
+    double sd = 0.0;
     const long base = long(blockIdx.x) * kChunk + threadIdx.x;
 #pragma unroll
     for (int j = 0; j < kItems; ++j) {
         const long i = base + j * 256;
         if (i < n) {
-            x[i] = x[i] + alpha * p[i];
-            const double ri = r[i] - alpha * q[i];
-            const double zi = m.dinv[i] * ri;
-            r[i] = ri;
-            z[i] = zi;
-            srz = srz + ri * zi;
-            srr = srr + ri * ri;
+            const double wi = apply_M<Uniform>(m, u, int(i));
+            w[i] = wi;
+            sd = fma(wi, u[i], sd);
         }
     }
-    const double b0 = block_tree(srz, ws);
+    const double b2 = block_tree(sd, ws);
+    if (threadIdx.x == 0) part[2 * nb + blockIdx.x] = b2;
+    if (arrive_last(&st->ticket)) {
+        const double g = final_sum(part, nb, ws);
+        const double rr = final_sum(part + nb, nb, ws);
+        const double d = final_sum(part + 2 * nb, nb, ws);
+        const double bb = init ? final_sum(part + 3 * nb, nb, ws) : 0.0;
+        if (threadIdx.x == 0) {
+            if (init) {
+                st->rz = g;
+                st->rr = rr;
+                st->bb = bb;
+                st->pq = d;
+                st->lim = (tol * tol) * bb;
+                st->alpha = g / d;
+                st->beta = 0.0;
+                st->iters = 0;
+                st->k = 0;
+                st->done = rr <= st->lim ? 1 : 0;
+                st->converged = st->done;
+            } else {
+                const int k = st->k + 1;
+                st->rr = rr;
+                st->pq = d;
+                st->k = k;
+                st->iters = k;
+                if (rr <= st->lim) {
+                    st->done = 1;
+                    st->converged = 1;
+                } else if (k >= maxit) {
+                    st->done = 1;
+                    st->converged = 0;
+                } else {
+                    const double beta = g / st->rz;
+                    st->alpha = g / (d - beta * g / st->alpha);
+                    st->beta = beta;
+                    st->rz = g;
+                }
+            }
+        }
+    }
+}
+
+// p = u + beta p, s = w + beta s (p = u, s = w on the first iteration),
+// x += alpha p, r -= alpha s, u = D^-1 r; partials of gamma = r.u and r.r.
+__global__ void __launch_bounds__(256) pcg_update_kernel(DMesh m, double* __restrict__ x, double* __restrict__ r,
+                                                         double* __restrict__ u, const double* __restrict__ w,
+                                                         double* __restrict__ p, double* __restrict__ sv,
+                                                         double* part, PcgState* st) {
+    if (st->done) return;
+    __shared__ double ws[256];
+    const int n = m.n_cells;
+    const int nb = gridDim.x;
+    const int first = st->k == 0;
+    const double alpha = st->alpha, beta = st->beta;
+    double sg = 0.0, srr = 0.0;
+    const long base = long(blockIdx.x) * kChunk + threadIdx.x;
+#pragma unroll
+    for (int j = 0; j < kItems; ++j) {
+        const long i = base + j * 256;
+        if (i < n) {
+            double pi, si;
+            if (first) {
+                pi = u[i];
+                si = w[i];
+            } else {
+                pi = fma(beta, p[i], u[i]);
+                si = fma(beta, sv[i], w[i]);
+            }
+            p[i] = pi;
+            sv[i] = si;
+            x[i] = fma(alpha, pi, x[i]);
+            const double ri = fma(-alpha, si, r[i]);
+            const double ui = m.dinv[i] * ri;
+            r[i] = ri;
+            u[i] = ui;
+            sg = fma(ri, ui, sg);
+            srr = fma(ri, ri, srr);
+        }
+    }
+    const double b0 = block_tree(sg, ws);
     const double b1 = block_tree(srr, ws);
     if (threadIdx.x == 0) {
         part[blockIdx.x] = b0;
         part[nb + blockIdx.x] = b1;
-    }
-    if (arrive_last(&st->ticket)) {
-        const double rzn = final_sum(part, nb, ws);
-        const double rr = final_sum(part + nb, nb, ws);
-        if (threadIdx.x == 0) {
-            st->rr = rr;
-            st->k = k;
-            if (rr <= st->lim) {
-                st->done = 1;
-                st->converged = 1;
-                st->iters = k;
-            } else if (k >= maxit) {
-                st->done = 1;
-                st->converged = 0;
-                st->iters = k;
-            } else {
-                st->beta = rzn / st->rz;
-                st->rz = rzn;
-                st->iters = k;
-            }
-        }
     }
 }
 
@@ -355,7 +375,7 @@ __global__ void __launch_bounds__(256) pcg_update_kernel(DMesh m, double* __rest
 __global__ void __launch_bounds__(256) of_residual_kernel(DMesh m, const double* __restrict__ b,
                                                           const double* __restrict__ x, double* part,
                                                           PcgState* st) {
-    __shared__ double ws[8];
+    __shared__ double ws[256];
     const double mean = st->mean;
     const int n = m.n_cells;
     const int nb = gridDim.x;
@@ -364,7 +384,7 @@ __global__ void __launch_bounds__(256) of_residual_kernel(DMesh m, const double*
     for (int j = 0; j < kItems; ++j) {
         const long i = base + j * 256;
         if (i < n) {
-            const double ax = apply_M(m, x, int(i));
+            const double ax = apply_M<false>(m, x, int(i));
             double rowsum = m.Mdiag[i];
             for (int f = 0; f < 6; ++f)
                 if (m.nbr[6 * size_t(i) + f] >= 0) rowsum += m.Moff[6 * size_t(i) + f];
@@ -538,17 +558,24 @@ void launch_rhs(const DMesh& m, const double* rho, const double* grad_bc, double
     }
 }
 
-void launch_pcg_init(const DMesh& m, const double* b, const double* x, double* r, double* z,
+void launch_pcg_init(const DMesh& m, const double* b, const double* x, double* r, double* u, double* w,
                      double* part, PcgState* st, double tol, cudaStream_t s) {
-    pcg_init_kernel<<<pcg_blocks(m.n_cells), 256, 0, s>>>(m, b, x, r, z, part, st, tol);
+    const int nb = pcg_blocks(m.n_cells);
+    if (m.lap_uniform) {
+        pcg_init_kernel<true><<<nb, 256, 0, s>>>(m, b, x, r, u, part);
+        pcg_spmv_kernel<true><<<nb, 256, 0, s>>>(m, u, w, part, st, 1, tol, 0);
+    } else {
+        pcg_init_kernel<false><<<nb, 256, 0, s>>>(m, b, x, r, u, part);
+        pcg_spmv_kernel<false><<<nb, 256, 0, s>>>(m, u, w, part, st, 1, tol, 0);
+    }
 }
 
-void launch_pcg_iteration(const DMesh& m, double* x, double* r, double* z, const double* p_old,
-                          double* p_new, double* q, double* part, PcgState* st, int maxit,
-                          cudaStream_t s) {
+void launch_pcg_iteration(const DMesh& m, double* x, double* r, double* u, double* w, double* p, double* sv,
+                          double* part, PcgState* st, int maxit, cudaStream_t s) {
     const int nb = pcg_blocks(m.n_cells);
-    pcg_spmv_kernel<<<nb, 256, 0, s>>>(m, z, p_old, p_new, q, part, st);
-    pcg_update_kernel<<<nb, 256, 0, s>>>(m, x, r, z, p_new, q, part, st, maxit);
+    pcg_update_kernel<<<nb, 256, 0, s>>>(m, x, r, u, w, p, sv, part, st);
+    if (m.lap_uniform) pcg_spmv_kernel<true><<<nb, 256, 0, s>>>(m, u, w, part, st, 0, 0.0, maxit);
+    else pcg_spmv_kernel<false><<<nb, 256, 0, s>>>(m, u, w, part, st, 0, 0.0, maxit);
 }
 
 void launch_of_residual(const DMesh& m, const double* b, const double* x, double* part, PcgState* st,

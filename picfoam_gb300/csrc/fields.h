@@ -9,12 +9,13 @@ namespace pgd {
 
 // Reduction layout shared by every deterministic sum: a block of 256 threads
 // owns kChunk consecutive cells, thread t adds cells t, t+256, ... in order.
-constexpr int kItems = 2;
+constexpr int kItems = 4;
 constexpr int kChunk = 256 * kItems;
 
 // Device-resident PCG scalars; every kernel of one solve reads and writes it.
+// Chronopoulos-Gear form: rz = gamma = r.u, pq = delta = w.u.
 struct PcgState {
-    double rz, rr, bb, pq, beta, lim, mean, of_residual;
+    double rz, rr, bb, pq, beta, lim, mean, of_residual, alpha;
     int done, iters, converged, k;
     unsigned int ticket;
     unsigned int pad2[3];
@@ -37,11 +38,12 @@ void launch_charge_update(const DMesh& m, int vw, int fixed, double fix_scale, c
 void launch_floating_update(double* qconv, double* sigma, double* grad_bc, cudaStream_t s);
 void launch_rhs(const DMesh& m, const double* rho, const double* grad_bc, double* b, int singular,
                 double* part, PcgState* st, cudaStream_t s);
-void launch_pcg_init(const DMesh& m, const double* b, const double* x, double* r, double* z,
+// PCG (Chronopoulos-Gear form, Jacobi preconditioner).  part holds 4 x
+// pcg_blocks(n) doubles; the state's ticket must be zero on entry.
+void launch_pcg_init(const DMesh& m, const double* b, const double* x, double* r, double* u, double* w,
                      double* part, PcgState* st, double tol, cudaStream_t s);
-void launch_pcg_iteration(const DMesh& m, double* x, double* r, double* z, const double* p_old,
-                          double* p_new, double* q, double* part, PcgState* st, int maxit,
-                          cudaStream_t s);
+void launch_pcg_iteration(const DMesh& m, double* x, double* r, double* u, double* w, double* p, double* sv,
+                          double* part, PcgState* st, int maxit, cudaStream_t s);
 void launch_of_residual(const DMesh& m, const double* b, const double* x, double* part, PcgState* st,
                         cudaStream_t s);
 void launch_efield(const DMesh& m, const double* phi, const double* grad_bc, double* E, double* Eb,

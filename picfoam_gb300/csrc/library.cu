@@ -38,7 +38,7 @@ struct picgpu_mesh {
 namespace {
 
 constexpr double kMu0 = 4.0 * 3.14159265358979323846 * 1e-7;
-constexpr int kGraphIters = 8;  // PCG iterations per graph replay (even: p buffers alternate)
+constexpr int kGraphIters = 8;  // PCG iterations per graph replay
 constexpr double kCl = 299792458.0;
 
 struct SpeciesBuf {
@@ -103,6 +103,7 @@ struct picgpu_ctx {
     picgpu_step_stats acc{};
     cudaEvent_t timer[2] = {nullptr, nullptr};
     cudaGraphExec_t pcg_graph = nullptr;
+    double pcg_r0 = 0.0;  // ||b - A x0|| / ||b|| of the last solve's start guess
 };
 
 picgpu_status pgd_collisions(picgpu_ctx* c, picgpu_step_stats* stats);
@@ -430,17 +431,18 @@ picgpu_status poisson(picgpu_ctx* c, picgpu_step_stats* stats) {
             cudaGraph_t g;
             CK(cudaStreamBeginCapture(c->stream, cudaStreamCaptureModeThreadLocal));
             for (int j = 0; j < kGraphIters; ++j)
-                pgd::launch_pcg_iteration(c->dm, c->phi, c->r, c->z, c->p[j & 1], c->p[(j + 1) & 1], c->q, c->part,
-                                          c->st, maxit, c->stream);
+                pgd::launch_pcg_iteration(c->dm, c->phi, c->r, c->z, c->q, c->p[0], c->p[1], c->part, c->st, maxit,
+                                          c->stream);
             CK(cudaStreamEndCapture(c->stream, &g));
             CK(cudaGraphInstantiate(&c->pcg_graph, g, 0));
             CK(cudaGraphDestroy(g));
         }
         pgd::launch_rhs(c->dm, c->rho, c->grad_bc, c->b, !c->m.has_dirichlet, c->part, c->st, c->stream);
-        pgd::launch_pcg_init(c->dm, c->b, c->phi, c->r, c->z, c->part, c->st, tol, c->stream);
-        c->launches += c->m.has_dirichlet ? 2 : 4;
+        pgd::launch_pcg_init(c->dm, c->b, c->phi, c->r, c->z, c->q, c->part, c->st, tol, c->stream);
+        c->launches += c->m.has_dirichlet ? 3 : 5;
         CK(cudaMemcpyAsync(c->st_host, c->st, sizeof(pgd::PcgState), cudaMemcpyDeviceToHost, c->stream));
         CK(cudaStreamSynchronize(c->stream));
+        c->pcg_r0 = c->st_host->bb > 0 ? std::sqrt(c->st_host->rr / c->st_host->bb) : 0.0;
         int launched = 0;
         while (!c->st_host->done && launched < maxit) {
             CK(cudaGraphLaunch(c->pcg_graph, c->stream));
@@ -463,6 +465,7 @@ picgpu_status poisson(picgpu_ctx* c, picgpu_step_stats* stats) {
         stats->pcg_iterations_total += S.iters;
         stats->pcg_residual_l2 = S.bb > 0 ? std::sqrt(S.rr / S.bb) : 0.0;
         stats->pcg_residual_of = S.of_residual;
+        stats->pcg_residual_initial = c->pcg_r0;
     }
     if (!S.converged) return bad(c, PICGPU_PCG_NOT_CONVERGED, "PCG did not converge within pcg_max_iter");
     return PICGPU_OK;
@@ -825,6 +828,18 @@ picgpu_status picgpu_create(const picgpu_mesh_desc* mesh, const picgpu_config* c
     UP(pc_start, m.pc_start, int);
     UP(pc_slot, m.pc_slot, int);
     d.uniform = m.n_classes == 1;
+    // one M coefficient per face direction: the SpMV then skips Moff
+    d.lap_uniform = 1;
+    for (int f = 0; f < 6; ++f) d.lap_coef[f] = 0.0;
+    {
+        bool seen[6] = {};
+        for (size_t k = 0; k < Moff.size() && d.lap_uniform; ++k) {
+            if (m.nbr[k] < 0) continue;
+            const int f = int(k % 6);
+            if (!seen[f]) { seen[f] = true; d.lap_coef[f] = Moff[k]; }
+            else if (Moff[k] != d.lap_coef[f]) d.lap_uniform = 0;
+        }
+    }
 #undef UP
     (void)ip; (void)dp; (void)fp;
 
@@ -838,7 +853,7 @@ picgpu_status picgpu_create(const picgpu_mesh_desc* mesh, const picgpu_config* c
         (s = dalloc(c, &c->qconv, npa)) || (s = dalloc(c, &c->sigma, npa)) ||
         (s = dalloc(c, &c->grad_bc, npa)) || (s = dalloc(c, &c->b, nc)) || (s = dalloc(c, &c->r, nc)) ||
         (s = dalloc(c, &c->z, nc)) || (s = dalloc(c, &c->p[0], nc)) || (s = dalloc(c, &c->p[1], nc)) ||
-        (s = dalloc(c, &c->q, nc)) || (s = dalloc(c, &c->part, 3 * size_t(pgd::pcg_blocks(int(nc))) + 8)) ||
+        (s = dalloc(c, &c->q, nc)) || (s = dalloc(c, &c->part, 4 * size_t(pgd::pcg_blocks(int(nc))) + 8)) ||
         (s = dalloc(c, &c->st, 1)) || (s = dalloc(c, &c->counters, PICGPU_MAX_SPECIES)) ||
         (s = dalloc(c, &c->diag, 64)))
         return s;

@@ -25,12 +25,12 @@ namespace {
 
 constexpr long kMaxCells = PICGPU_NOALLOC_MAX_CELLS;
 constexpr long kMaxBlocks = (kMaxCells + pgd::kChunk - 1) / pgd::kChunk;
-constexpr long kPartDoubles = 3 * kMaxBlocks + 8;
+constexpr long kPartDoubles = 4 * kMaxBlocks + 8;
 constexpr long kStateDoubles = 32;  // holds one pgd::PcgState (rounded up)
 constexpr long kNoallocScratchDoubles = 6 * kMaxCells + kPartDoubles + kStateDoubles;
 static_assert(sizeof(pgd::PcgState) <= kStateDoubles * sizeof(double), "state does not fit");
 
-// The scratch: dinv | r | z | p0 | p1 | q | partial sums | PCG state.
+// The scratch: dinv | r | u | p | s | w | partial sums | PCG state.
 static __device__ __align__(256) double g_pcg_scratch[kNoallocScratchDoubles];
 
 // Device address of g_pcg_scratch per device, filled on the first call made
@@ -73,9 +73,10 @@ extern "C" picgpu_status picgpu_solve_ldu_noalloc(int n_cells, const double* dia
     const long n = n_cells;
     double* dinv = scratch;
     double* r = dinv + n;
-    double* z = r + n;
-    double* p[2] = {z + n, z + 2 * n};
-    double* q = z + 3 * n;
+    double* u = r + n;
+    double* p = u + n;
+    double* sv = u + 2 * n;
+    double* w = u + 3 * n;
     double* part = scratch + 6 * kMaxCells;
     auto* st = reinterpret_cast<pgd::PcgState*>(part + kPartDoubles);
     // the state carries the reduction ticket, which must start at zero
@@ -87,7 +88,7 @@ extern "C" picgpu_status picgpu_solve_ldu_noalloc(int n_cells, const double* dia
     m.Moff = off;
     m.nbr = nbr;
     m.dinv = dinv;
-    pgd::launch_pcg_init(m, b, x, r, z, part, st, tol, s);
+    pgd::launch_pcg_init(m, b, x, r, u, w, part, st, tol, s);
     pgd::PcgState h{};
     if (cudaMemcpyAsync(&h, st, sizeof h, cudaMemcpyDeviceToHost, s) != cudaSuccess ||
         cudaStreamSynchronize(s) != cudaSuccess)
@@ -95,7 +96,7 @@ extern "C" picgpu_status picgpu_solve_ldu_noalloc(int n_cells, const double* dia
     int k = 1, batch = 4;
     while (!h.done && k <= max_iter) {
         for (int j = 0; j < batch && k <= max_iter; ++j, ++k)
-            pgd::launch_pcg_iteration(m, x, r, z, p[(k + 1) & 1], p[k & 1], q, part, st, max_iter, s);
+            pgd::launch_pcg_iteration(m, x, r, u, w, p, sv, part, st, max_iter, s);
         if (cudaGetLastError() != cudaSuccess ||
             cudaMemcpyAsync(&h, st, sizeof h, cudaMemcpyDeviceToHost, s) != cudaSuccess ||
             cudaStreamSynchronize(s) != cudaSuccess)
