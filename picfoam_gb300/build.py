@@ -31,9 +31,11 @@ UNITS = {
     "collide.cu": ["--fmad=false"],
     "library.cu": [],
     "pcg_static.cu": ["--fmad=false"],
+    "unet_conv.cu": [],
+    "unet_api.cu": [],
 }
 HEADERS = [os.path.join(SRC, f) for f in os.listdir(SRC) if f.endswith((".h", ".cuh", ".hpp"))] + [
-    os.path.join(INCLUDE, "picgpu.h")]
+    os.path.join(INCLUDE, f) for f in os.listdir(INCLUDE) if f.endswith(".h")]
 
 
 def nvcc():

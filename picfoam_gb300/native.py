@@ -90,5 +90,9 @@ def load():
     lib.picgpu_solve_ldu_noalloc.restype = i
     lib.picgpu_solve_ldu_noalloc.argtypes = [i, P, P, P, P, P, C.c_double, i, C.POINTER(C.c_int),
                                              F64P, P]
+    U16P = C.POINTER(C.c_uint16)
+    F32P = C.POINTER(C.c_float)
+    lib.picgpu_test_conv3d.restype = i
+    lib.picgpu_test_conv3d.argtypes = [i, i, i, i, i, i, i, i, U16P, U16P, U16P, F32P]
     _lib = lib
     return lib

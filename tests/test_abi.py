@@ -20,9 +20,16 @@ def lib():
 
 
 def declared_symbols():
-    src = open(os.path.join(ROOT, "include", "picgpu.h")).read()
-    src = re.sub(r"/\*.*?\*/", "", src, flags=re.S)
-    return sorted(set(re.findall(r"\b(picgpu_[a-z0-9_]+)\s*\(", src)))
+    """Every function declared by a header under include/."""
+    syms = set()
+    inc = os.path.join(ROOT, "include")
+    for name in sorted(os.listdir(inc)):
+        if not name.endswith(".h"):
+            continue
+        src = open(os.path.join(inc, name)).read()
+        src = re.sub(r"/\*.*?\*/", "", src, flags=re.S)
+        syms.update(re.findall(r"\b(picgpu_[a-z0-9_]+)\s*\(", src))
+    return sorted(syms)
 
 
 def test_every_declared_symbol_is_exported(lib):
