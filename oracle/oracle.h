@@ -58,6 +58,14 @@ void oracle_philox4x32(const uint32_t ctr[4], const uint32_t key[2], uint32_t ou
  * particles (CoulombCollisionModel.C:249-309); 0 when undefined. */
 double oracle_debye_length(oracle_ctx* ctx, int cell);
 
+/* CPU reference of the learned warm-start U-Net (unet_ref.cpp), same weight
+ * and tensor layouts as picgpu_unet_* (include/picgpu_learned.h); FP64, and
+ * with emulate = 1 rounded to BF16 wherever the GPU stores BF16. */
+size_t oracle_unet_param_count(void);
+int oracle_unet_forward(int X, int Y, int Z, const float* w, const float* in, int emulate, double* out);
+int oracle_unet_gradients(int X, int Y, int Z, const float* w, const float* in, const float* target,
+                          const float* mask, int emulate, double* grad, double* loss);
+
 #ifdef __cplusplus
 }
 #endif

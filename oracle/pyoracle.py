@@ -55,6 +55,14 @@ def load():
         lib.oracle_philox4x32.argtypes = [C.POINTER(C.c_uint32), C.POINTER(C.c_uint32), C.POINTER(C.c_uint32)]
         lib.oracle_debye_length.restype = C.c_double
         lib.oracle_debye_length.argtypes = [P, C.c_int]
+        F32P, F64P = C.POINTER(C.c_float), C.POINTER(C.c_double)
+        i = C.c_int
+        lib.oracle_unet_param_count.restype = C.c_size_t
+        lib.oracle_unet_param_count.argtypes = []
+        lib.oracle_unet_forward.restype = i
+        lib.oracle_unet_forward.argtypes = [i, i, i, F32P, F32P, i, F64P]
+        lib.oracle_unet_gradients.restype = i
+        lib.oracle_unet_gradients.argtypes = [i, i, i, F32P, F32P, F32P, F32P, i, F64P, F64P]
         _lib = lib
     return _lib
 

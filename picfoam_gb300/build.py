@@ -32,6 +32,7 @@ UNITS = {
     "library.cu": [],
     "pcg_static.cu": ["--fmad=false"],
     "unet_conv.cu": [],
+    "unet.cu": [],
     "unet_api.cu": [],
 }
 HEADERS = [os.path.join(SRC, f) for f in os.listdir(SRC) if f.endswith((".h", ".cuh", ".hpp"))] + [

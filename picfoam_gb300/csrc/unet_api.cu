@@ -73,3 +73,127 @@ extern "C" picgpu_status picgpu_test_conv3d(int X, int Y, int Z, int cin1, int c
     }
     return PICGPU_OK;
 }
+
+// --------------------------------------------------------- the network --
+#include <memory>
+
+#include "unet_net.h"
+
+struct picgpu_unet {
+    pgd::UNet net;
+    cudaStream_t stream = nullptr;
+    float* target = nullptr;
+    float* mask = nullptr;
+};
+
+namespace {
+
+picgpu_status upload_sample(picgpu_unet* u, const float* in, const float* target, const float* mask) {
+    const long V = u->net.voxels();
+    cudaStream_t s = u->stream;
+    if (cudaMemcpyAsync(u->net.input(), in, size_t(V) * 2 * sizeof(float), cudaMemcpyHostToDevice, s) != cudaSuccess)
+        return PICGPU_CUDA_ERROR;
+    if (target && cudaMemcpyAsync(u->target, target, size_t(V) * sizeof(float), cudaMemcpyHostToDevice, s) != cudaSuccess)
+        return PICGPU_CUDA_ERROR;
+    if (mask && cudaMemcpyAsync(u->mask, mask, size_t(V) * sizeof(float), cudaMemcpyHostToDevice, s) != cudaSuccess)
+        return PICGPU_CUDA_ERROR;
+    return PICGPU_OK;
+}
+
+picgpu_status finish(picgpu_unet* u) {
+    bool timed_out = false;
+    if (cudaGetLastError() != cudaSuccess || u->net.check_error(&timed_out, u->stream) != cudaSuccess)
+        return PICGPU_CUDA_ERROR;
+    return timed_out ? PICGPU_CUDA_ERROR : PICGPU_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+size_t picgpu_unet_param_count(void) { return pgd::UNet::param_count(); }
+
+picgpu_status picgpu_unet_create(int X, int Y, int Z, uint64_t seed, picgpu_unet** out) {
+    if (!out) return PICGPU_INVALID_ARG;
+    *out = nullptr;
+    if (!pgd::UNet::grid_supported(X, Y, Z)) return PICGPU_INVALID_ARG;
+    auto u = std::make_unique<picgpu_unet>();
+    std::string msg;
+    if (cudaStreamCreateWithFlags(&u->stream, cudaStreamNonBlocking) != cudaSuccess) return PICGPU_CUDA_ERROR;
+    const int e = u->net.init(X, Y, Z, seed, &msg);
+    if (e) {
+        cudaStreamDestroy(u->stream);
+        return e == 2 ? PICGPU_OOM : PICGPU_CUDA_ERROR;
+    }
+    const long V = long(X) * Y * Z;
+    if (cudaMalloc(&u->target, size_t(V) * sizeof(float)) != cudaSuccess ||
+        cudaMalloc(&u->mask, size_t(V) * sizeof(float)) != cudaSuccess) {
+        cudaFree(u->target);
+        cudaStreamDestroy(u->stream);
+        return PICGPU_OOM;
+    }
+    *out = u.release();
+    return PICGPU_OK;
+}
+
+void picgpu_unet_destroy(picgpu_unet* u) {
+    if (!u) return;
+    cudaStreamSynchronize(u->stream);
+    cudaFree(u->target);
+    cudaFree(u->mask);
+    cudaStreamDestroy(u->stream);
+    delete u;
+}
+
+picgpu_status picgpu_unet_set_weights(picgpu_unet* u, const float* w) {
+    if (!u || !w) return PICGPU_INVALID_ARG;
+    return u->net.set_weights(w, u->stream) == cudaSuccess ? PICGPU_OK : PICGPU_CUDA_ERROR;
+}
+
+picgpu_status picgpu_unet_get_weights(picgpu_unet* u, float* w) {
+    if (!u || !w) return PICGPU_INVALID_ARG;
+    return u->net.get_weights(w, u->stream) == cudaSuccess ? PICGPU_OK : PICGPU_CUDA_ERROR;
+}
+
+picgpu_status picgpu_unet_forward(picgpu_unet* u, const float* in, float* out) {
+    if (!u || !in || !out) return PICGPU_INVALID_ARG;
+    picgpu_status st = upload_sample(u, in, nullptr, nullptr);
+    if (st) return st;
+    if (u->net.forward(u->stream) != cudaSuccess) return PICGPU_CUDA_ERROR;
+    if (cudaMemcpyAsync(out, u->net.output(), size_t(u->net.voxels()) * sizeof(float), cudaMemcpyDeviceToHost,
+                        u->stream) != cudaSuccess)
+        return PICGPU_CUDA_ERROR;
+    return finish(u);
+}
+
+picgpu_status picgpu_unet_gradients(picgpu_unet* u, const float* in, const float* target, const float* mask,
+                                    float* grad, double* loss) {
+    if (!u || !in || !target || !mask || !grad) return PICGPU_INVALID_ARG;
+    picgpu_status st = upload_sample(u, in, target, mask);
+    if (st) return st;
+    if (u->net.forward(u->stream) != cudaSuccess || u->net.loss_and_grad(u->target, u->mask, u->stream) != cudaSuccess ||
+        u->net.backward(u->stream) != cudaSuccess)
+        return PICGPU_CUDA_ERROR;
+    if ((st = finish(u))) return st;
+    if (u->net.get_gradients(grad, u->stream) != cudaSuccess) return PICGPU_CUDA_ERROR;
+    if (loss && u->net.read_loss(loss, u->stream) != cudaSuccess) return PICGPU_CUDA_ERROR;
+    return PICGPU_OK;
+}
+
+picgpu_status picgpu_unet_train(picgpu_unet* u, const float* in, const float* target, const float* mask, int iters,
+                                double lr, double* loss) {
+    if (!u || !in || !target || !mask || iters < 0 || !(lr > 0)) return PICGPU_INVALID_ARG;
+    picgpu_status st = upload_sample(u, in, target, mask);
+    if (st) return st;
+    for (int k = 0; k < iters; ++k) {
+        if (u->net.forward(u->stream) != cudaSuccess ||
+            u->net.loss_and_grad(u->target, u->mask, u->stream) != cudaSuccess ||
+            u->net.backward(u->stream) != cudaSuccess || u->net.adam(float(lr), u->stream) != cudaSuccess)
+            return PICGPU_CUDA_ERROR;
+    }
+    if ((st = finish(u))) return st;
+    if (loss && u->net.read_loss(loss, u->stream) != cudaSuccess) return PICGPU_CUDA_ERROR;
+    return PICGPU_OK;
+}
+
+}  // extern "C"

@@ -94,5 +94,21 @@ def load():
     F32P = C.POINTER(C.c_float)
     lib.picgpu_test_conv3d.restype = i
     lib.picgpu_test_conv3d.argtypes = [i, i, i, i, i, i, i, i, U16P, U16P, U16P, F32P]
+    lib.picgpu_unet_param_count.restype = C.c_size_t
+    lib.picgpu_unet_param_count.argtypes = []
+    lib.picgpu_unet_create.restype = i
+    lib.picgpu_unet_create.argtypes = [i, i, i, C.c_uint64, PP]
+    lib.picgpu_unet_destroy.restype = None
+    lib.picgpu_unet_destroy.argtypes = [P]
+    lib.picgpu_unet_set_weights.restype = i
+    lib.picgpu_unet_set_weights.argtypes = [P, F32P]
+    lib.picgpu_unet_get_weights.restype = i
+    lib.picgpu_unet_get_weights.argtypes = [P, F32P]
+    lib.picgpu_unet_forward.restype = i
+    lib.picgpu_unet_forward.argtypes = [P, F32P, F32P]
+    lib.picgpu_unet_gradients.restype = i
+    lib.picgpu_unet_gradients.argtypes = [P, F32P, F32P, F32P, F32P, F64P]
+    lib.picgpu_unet_train.restype = i
+    lib.picgpu_unet_train.argtypes = [P, F32P, F32P, F32P, i, C.c_double, F64P]
     _lib = lib
     return lib

@@ -69,3 +69,103 @@ def test_conv_tc_concat_upsampled_source(gpu):
     assert st == abi.OK
     ref = conv_ref(x.astype(np.float64), w.astype(np.float64), 0).reshape(-1, cout)
     assert np.abs(out - ref).max() <= 1e-4 * np.abs(ref).max()
+
+
+# ------------------------------------------------------------ the network
+F32P = C.POINTER(C.c_float)
+F64P = C.POINTER(C.c_double)
+
+
+def f32p(a):
+    return a.ctypes.data_as(F32P)
+
+
+def make_net(lib, X, Y, Z, seed=3):
+    h = C.c_void_p()
+    assert lib.picgpu_unet_create(X, Y, Z, seed, C.byref(h)) == abi.OK
+    return h
+
+
+def unet_sample(rng, V):
+    x = np.zeros((V, 2), np.float32)
+    x[:, 0] = rng.standard_normal(V)
+    x[:, 1] = (rng.random(V) > 0.1).astype(np.float32)
+    t = rng.standard_normal(V).astype(np.float32)
+    return x, t, x[:, 1].copy()
+
+
+def test_unet_forward_and_gradients_match_oracle(gpu, oracle_backend):
+    lib = native.load()
+    olib = oracle_backend.load()
+    X, Y, Z = 16, 16, 32
+    V = X * Y * Z
+    h = make_net(lib, X, Y, Z)
+    try:
+        n = lib.picgpu_unet_param_count()
+        assert n == olib.oracle_unet_param_count()
+        w = np.zeros(n, np.float32)
+        assert lib.picgpu_unet_get_weights(h, f32p(w)) == abi.OK
+        rng = np.random.default_rng(1)
+        x, t, m = unet_sample(rng, V)
+        out = np.zeros(V, np.float32)
+        assert lib.picgpu_unet_forward(h, f32p(x), f32p(out)) == abi.OK
+        ref = np.zeros(V)
+        assert olib.oracle_unet_forward(X, Y, Z, f32p(w), f32p(x), 1, ref.ctypes.data_as(F64P)) == 0
+        # BF16 activations: the forward output agrees to a few BF16 roundings
+        assert np.linalg.norm(out - ref) <= 2e-2 * np.linalg.norm(ref)
+        g = np.zeros(n, np.float32)
+        loss = C.c_double()
+        assert lib.picgpu_unet_gradients(h, f32p(x), f32p(t), f32p(m), f32p(g), C.byref(loss)) == abi.OK
+        gref, gexact = np.zeros(n), np.zeros(n)
+        lref = C.c_double()
+        assert olib.oracle_unet_gradients(X, Y, Z, f32p(w), f32p(x), f32p(t), f32p(m), 1, gref.ctypes.data_as(F64P),
+                                          C.byref(lref)) == 0
+        assert olib.oracle_unet_gradients(X, Y, Z, f32p(w), f32p(x), f32p(t), f32p(m), 0,
+                                          gexact.ctypes.data_as(F64P), None) == 0
+        assert loss.value == pytest.approx(lref.value, rel=1e-2)
+        defs = [(2, 16), (16, 16), (16, 32), (32, 32), (32, 64), (64, 64), (96, 32), (32, 32), (48, 16), (16, 16),
+                (16, 1)]
+        off = 0
+        for ci, co in defs:
+            k = 27 * ci * co
+            a, b, e = g[off:off + k], gref[off:off + k], gexact[off:off + k]
+            # The reference rounds to BF16 where the GPU does, but a rounding
+            # that flips (FP32 accumulation order) perturbs ~27*C sums of the
+            # next layer by more than FP32 round-off, so over eleven layers the
+            # two BF16 computations decorrelate.  The check is therefore that
+            # the GPU gradient is as close to the exact FP64 gradient as BF16
+            # storage allows (bf16_effect = emulated vs exact); a wrong
+            # backward pass is off by O(1).
+            bf16_effect = np.linalg.norm(e - b) / np.linalg.norm(e)
+            err_em = np.linalg.norm(a - b) / np.linalg.norm(b)
+            err_exact = np.linalg.norm(a - e) / np.linalg.norm(e)
+            assert err_em <= 1.5 * bf16_effect + 5e-3, (ci, co, err_em, bf16_effect)
+            assert err_exact <= 2.0 * bf16_effect + 5e-3, (ci, co, err_exact, bf16_effect)
+            assert np.dot(a, e) / (np.linalg.norm(a) * np.linalg.norm(e)) > 0.99, (ci, co)
+            off += k
+    finally:
+        lib.picgpu_unet_destroy(h)
+
+
+def test_unet_training_reduces_loss(gpu):
+    lib = native.load()
+    X, Y, Z = 16, 16, 32
+    V = X * Y * Z
+    h = make_net(lib, X, Y, Z)
+    try:
+        rng = np.random.default_rng(2)
+        x, _, m = unet_sample(rng, V)
+        # a smooth target the net can fit: a blurred copy of the input
+        r = x[:, 0].reshape(Z, Y, X)
+        s = r.copy()
+        for ax in range(3):
+            s = 0.25 * np.roll(s, 1, ax) + 0.5 * s + 0.25 * np.roll(s, -1, ax)
+        t = s.reshape(-1).astype(np.float32)
+        l0 = C.c_double()
+        g = np.zeros(lib.picgpu_unet_param_count(), np.float32)
+        assert lib.picgpu_unet_gradients(h, f32p(x), f32p(t), f32p(m), f32p(g), C.byref(l0)) == abi.OK
+        l1 = C.c_double()
+        assert lib.picgpu_unet_train(h, f32p(x), f32p(t), f32p(m), 60, 2e-3, C.byref(l1)) == abi.OK
+        assert l1.value < 0.5 * l0.value
+    finally:
+        lib.picgpu_unet_destroy(h)
