@@ -193,6 +193,24 @@ typedef struct {
     int32_t pad;
 } picgpu_coulomb;
 
+/* Learned warm start of the Poisson PCG (a 3D U-Net on the cell grid, see
+ * picgpu_learned.h; no picFoam counterpart).  The first train_steps solves
+ * start from the previous potential and feed (start residual, potential
+ * increment) pairs to the net, which trains train_iters Adam steps after
+ * each; later solves start from the previous potential plus the net's
+ * predicted increment, scaled by the A-norm line search, then the FP64 PCG
+ * runs to the same tolerance.  Needs a block mesh whose cell counts are
+ * multiples of 4 with n[0]*n[1]*n[2]/64 a multiple of 128. */
+typedef struct {
+    int32_t enabled;
+    int32_t train_steps;      /* solves that feed the training set (0: 500) */
+    int32_t train_iters;      /* Adam steps after each of those solves (0: 4) */
+    int32_t replay;           /* training pairs kept, newest first (0: 16) */
+    double  lr;               /* Adam learning rate (0: 1e-3) */
+    int32_t refine;           /* further net passes on the remaining residual (0..3) */
+    int32_t pad;
+} picgpu_learned;
+
 typedef struct {
     int32_t pusher;               /* PICGPU_PUSHER_* */
     int32_t field_weighting;      /* PICGPU_WEIGHTING_* */
@@ -218,6 +236,7 @@ typedef struct {
     picgpu_mcc mcc;
     picgpu_ion_mcc ion_mcc;
     picgpu_coulomb coulomb;
+    picgpu_learned learned;
 } picgpu_config;
 
 typedef struct {
@@ -240,6 +259,11 @@ typedef struct {
     int64_t ion_mcc_elastic;
     int64_t ion_mcc_charge_exchange;
     double  floating_charge[PICGPU_MAX_BOXES + 6]; /* accumulated surface charge per patch [C] */
+    double  learned_loss;                       /* last training loss of the warm-start net */
+    double  learned_alpha;                      /* line-search factor of the last learned warm start */
+    double  learned_residual;                   /* ||b-Ax||2/||b||2 before the net (the plain guess) */
+    int32_t learned_active;                     /* 1 when the last solve started from the net's guess */
+    int32_t learned_samples;                    /* training pairs collected so far */
 } picgpu_step_stats;
 
 typedef struct picgpu_ctx picgpu_ctx;

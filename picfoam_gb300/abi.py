@@ -103,6 +103,13 @@ class Coulomb(C.Structure):
     ]
 
 
+class Learned(C.Structure):
+    _fields_ = [
+        ("enabled", C.c_int32), ("train_steps", C.c_int32), ("train_iters", C.c_int32),
+        ("replay", C.c_int32), ("lr", C.c_double), ("refine", C.c_int32), ("pad", C.c_int32),
+    ]
+
+
 class Config(C.Structure):
     _fields_ = [
         ("pusher", C.c_int32), ("field_weighting", C.c_int32),
@@ -116,7 +123,7 @@ class Config(C.Structure):
         ("pcg_tol", C.c_double), ("pcg_max_iter", C.c_int32), ("pcg_norm", C.c_int32),
         ("sort_interval", C.c_int32), ("pad0", C.c_int32),
         ("seed", C.c_uint64),
-        ("mcc", Mcc), ("ion_mcc", IonMcc), ("coulomb", Coulomb),
+        ("mcc", Mcc), ("ion_mcc", IonMcc), ("coulomb", Coulomb), ("learned", Learned),
     ]
 
 
@@ -134,6 +141,8 @@ class StepStats(C.Structure):
         ("ion_mcc_candidates", C.c_int64), ("ion_mcc_elastic", C.c_int64),
         ("ion_mcc_charge_exchange", C.c_int64),
         ("floating_charge", C.c_double * (MAX_BOXES + 6)),
+        ("learned_loss", C.c_double), ("learned_alpha", C.c_double), ("learned_residual", C.c_double),
+        ("learned_active", C.c_int32), ("learned_samples", C.c_int32),
     ]
 
     def as_dict(self):

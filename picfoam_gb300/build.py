@@ -33,6 +33,7 @@ UNITS = {
     "pcg_static.cu": ["--fmad=false"],
     "unet_conv.cu": [],
     "unet.cu": [],
+    "learned.cu": [],
     "unet_api.cu": [],
 }
 HEADERS = [os.path.join(SRC, f) for f in os.listdir(SRC) if f.endswith((".h", ".cuh", ".hpp"))] + [

@@ -26,6 +26,7 @@
 #include "fields.h"
 #include "hexmesh.hpp"
 #include "kernels.h"
+#include "learned.h"
 #include "particles.h"
 #include "picgpu.h"
 
@@ -104,6 +105,7 @@ struct picgpu_ctx {
     cudaEvent_t timer[2] = {nullptr, nullptr};
     cudaGraphExec_t pcg_graph = nullptr;
     double pcg_r0 = 0.0;  // ||b - A x0|| / ||b|| of the last solve's start guess
+    std::unique_ptr<pgd::LearnedWarmStart> ws;  // learned warm start (cfg.learned.enabled)
 };
 
 picgpu_status pgd_collisions(picgpu_ctx* c, picgpu_step_stats* stats);
@@ -417,7 +419,7 @@ picgpu_status set_applied_field(picgpu_ctx* c) {
 }
 
 // Poisson PCG from the current phi; fills stats.
-picgpu_status poisson(picgpu_ctx* c, picgpu_step_stats* stats) {
+picgpu_status poisson(picgpu_ctx* c, picgpu_step_stats* stats, bool learned = false) {
     const int n = c->m.n_cells;
     const double tol = c->cfg.pcg_tol > 0 ? c->cfg.pcg_tol : 1e-10;
     const int maxit = c->cfg.pcg_max_iter > 0 ? c->cfg.pcg_max_iter : 10000;
@@ -438,6 +440,9 @@ picgpu_status poisson(picgpu_ctx* c, picgpu_step_stats* stats) {
             CK(cudaGraphDestroy(g));
         }
         pgd::launch_rhs(c->dm, c->rho, c->grad_bc, c->b, !c->m.has_dirichlet, c->part, c->st, c->stream);
+        if (learned && c->ws) {
+            CK(c->ws->before(c->dm, c->b, c->phi, c->stream));
+        }
         pgd::launch_pcg_init(c->dm, c->b, c->phi, c->r, c->z, c->q, c->part, c->st, tol, c->stream);
         c->launches += c->m.has_dirichlet ? 3 : 5;
         CK(cudaMemcpyAsync(c->st_host, c->st, sizeof(pgd::PcgState), cudaMemcpyDeviceToHost, c->stream));
@@ -453,6 +458,11 @@ picgpu_status poisson(picgpu_ctx* c, picgpu_step_stats* stats) {
         }
         pgd::launch_of_residual(c->dm, c->b, c->phi, c->part, c->st, c->stream);
         c->launches += 2;
+        if (learned && c->ws) {
+            const int64_t l0 = c->ws->launches;
+            CK(c->ws->after(c->dm, c->phi, c->stream));
+            (void)l0;
+        }
         CK(cudaMemcpyAsync(c->st_host, c->st, sizeof(pgd::PcgState), cudaMemcpyDeviceToHost, c->stream));
     }
     picgpu_status s = efield(c);
@@ -466,14 +476,21 @@ picgpu_status poisson(picgpu_ctx* c, picgpu_step_stats* stats) {
         stats->pcg_residual_l2 = S.bb > 0 ? std::sqrt(S.rr / S.bb) : 0.0;
         stats->pcg_residual_of = S.of_residual;
         stats->pcg_residual_initial = c->pcg_r0;
+        if (learned && c->ws) {
+            stats->learned_loss = c->ws->loss;
+            stats->learned_alpha = c->ws->alpha;
+            stats->learned_residual = c->ws->plain_residual;
+            stats->learned_active = c->ws->active;
+            stats->learned_samples = c->ws->samples;
+        }
     }
     if (!S.converged) return bad(c, PICGPU_PCG_NOT_CONVERGED, "PCG did not converge within pcg_max_iter");
     return PICGPU_OK;
 }
 
-picgpu_status solve_fields(picgpu_ctx* c, picgpu_step_stats* stats) {
+picgpu_status solve_fields(picgpu_ctx* c, picgpu_step_stats* stats, bool learned = false) {
     if (c->cfg.maxwell_solver != PICGPU_MAXWELL_ELECTROSTATIC) return PICGPU_OK;
-    return poisson(c, stats);
+    return poisson(c, stats, learned);
 }
 
 picgpu_status ensure_scan(picgpu_ctx* c, long n) {
@@ -569,7 +586,7 @@ picgpu_status one_step(picgpu_ctx* c, picgpu_step_stats* stats, bool fields) {
     if (!fields) return PICGPU_OK;
     pgd::launch_floating_update(c->qconv, c->sigma, c->grad_bc, c->stream);
     c->launches++;
-    if ((s = solve_fields(c, stats))) return s;
+    if ((s = solve_fields(c, stats, true))) return s;
     c->step_index++;
     return PICGPU_OK;
 }
@@ -883,6 +900,13 @@ picgpu_status picgpu_create(const picgpu_mesh_desc* mesh, const picgpu_config* c
     std::string msg;
     const int cs = pgd::collide_init(c->coll, c->cfg, c->dm, c->stream, &msg);
     if (cs) return bad(c, picgpu_status(cs), msg);
+    if (cfg->learned.enabled) {
+        if (cfg->maxwell_solver != PICGPU_MAXWELL_ELECTROSTATIC)
+            return bad(c, PICGPU_INVALID_ARG, "learned warm start needs the electrostatic Maxwell solver");
+        c->ws = std::make_unique<pgd::LearnedWarmStart>();
+        const int ls = c->ws->init(cfg->learned, cfg->seed, c->m.n_cells, c->m.n, c->m.cell_ijk, c->stream, &msg);
+        if (ls) return bad(c, picgpu_status(ls), msg);
+    }
     CK(cudaStreamSynchronize(c->stream));
     c->err.clear();
     return PICGPU_OK;
