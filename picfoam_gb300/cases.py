@@ -13,6 +13,7 @@ benchmark configurations of the particle hot path (seeded synthetic inputs):
   coulomb_thermalisation  16^3 cells, 400 e-/cell, T_x = 2 eV, T_yz = 1 eV
   coulomb_relaxation      e- and heavy ions at different temperatures (e-i exchange)
   ion_swarm               Ar+ in argon: isotropic elastic + charge exchange MCC
+  swarm_ensemble          64 swarm cases of 16x16x128 cells, 10-1000 Td, 1e5-4e6 e- each
   electrode_box           128^3 cells, two floating boxes, one 100 V box
 """
 import dataclasses
@@ -431,6 +432,55 @@ def electrode_box(n_cells=128, per_cell=30, n=1e15, T_e=2.0, T_i=0.03, seed=1234
         tet, bary = uniform_in_cells(rng, np.arange(n_c), per_cell)
         parts[s] = (tet, bary, maxwellian(rng, N, T, mass))
     return Case("electrode_box", mesh, cfg, parts, [], dict(dt=dt, N=2 * N, n_cells=n_c))
+
+
+def swarm_ensemble(n_cases=64, n=(16, 16, 128), size=(0.01, 0.01, 0.08), counts=None, EN_Td=None,
+                   count_range=(1e5, 4e6), count_seed=7, gas_density=1e21, T_gas=300.0, T_e=1.0, seed=1234,
+                   ion_species=True, dt=None):
+    """Batched electron swarms: n_cases independent copies of the swarm
+    geometry (config of electron_swarm scaled to n cells), reduced fields
+    E/N log-spaced over 10-1000 Td, particle counts log-uniform over
+    count_range drawn from count_seed.  Returns the single-case mesh, the
+    config, the per-case fields and the combined particle arrays (tet indices
+    of case k offset by k cells_per_case)."""
+    one = electron_swarm(nx=n[0], ny=n[1], nz=n[2], N=1, Ez=0.0, gas_density=gas_density, T_gas=T_gas, T_e=T_e,
+                         seed=seed, precision=abi.PREC_MIXED, ion_species=ion_species, size=size, dt=dt)
+    cfg = one.cfg
+    cpc = n[0] * n[1] * n[2]
+    if counts is None:
+        r = np.random.Generator(np.random.Philox(count_seed))
+        lo, hi = np.log(count_range[0]), np.log(count_range[1])
+        counts = np.exp(r.uniform(lo, hi, n_cases)).astype(np.int64)
+    counts = np.asarray(counts, dtype=np.int64)
+    if EN_Td is None:
+        EN_Td = np.logspace(1.0, 3.0, n_cases)
+    E = np.zeros((n_cases, 3))
+    E[:, 2] = np.asarray(EN_Td) * 1e-21 * gas_density
+    rng = np.random.Generator(np.random.Philox(seed))
+    N = int(counts.sum())
+    case_of = np.repeat(np.arange(n_cases, dtype=np.int64), counts)
+    cells = case_of * cpc + rng.integers(0, cpc, N)
+    tet = (cells * 12 + rng.integers(0, 12, N)).astype(np.int32)
+    u = np.sort(rng.random((N, 3), dtype=np.float32), axis=1)
+    bary = np.stack([u[:, 0], u[:, 1] - u[:, 0], u[:, 2] - u[:, 1]], axis=1)
+    U = maxwellian(rng, N, T_e, M_E).astype(np.float32)
+    parts = {0: (tet, bary, U)}
+    if ion_species:
+        parts[1] = (np.zeros(0, np.int32), np.zeros((0, 3)), np.zeros((0, 3)))
+    return Case("swarm_ensemble", one.mesh, cfg, parts, one.keepalive,
+                dict(dt=cfg.dt, n_cases=n_cases, counts=counts, EN_Td=np.asarray(EN_Td), E=E,
+                     cells_per_case=cpc, N=N))
+
+
+def build_ensemble(case, backend=None):
+    """Create an ensemble Simulation (one context, n_cases mesh copies)."""
+    from .simulation import EnsembleBackend, Simulation
+    be = backend if backend is not None else EnsembleBackend(case.meta["n_cases"])
+    sim = Simulation(case.mesh, case.cfg, backend=be, keepalive=case.keepalive)
+    sim.set_case_efield(case.meta["E"])
+    for s, (tet, bary, U) in case.particles.items():
+        sim.set_particles(s, tet, bary, U)
+    return sim
 
 
 def build(case, backend=None):

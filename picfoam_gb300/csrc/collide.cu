@@ -127,7 +127,9 @@ void exclusive_scan(const int* in, int* out, long n, int* tmp, cudaStream_t s, i
 }
 
 // ---------------------------------------------------- cell occupancy -----
-__global__ void count_cells_kernel(const int32_t* __restrict__ tet, int n, int* __restrict__ count) {
+__global__ void count_cells_kernel(const int32_t* __restrict__ tet, int n, int* __restrict__ count,
+                                   const int* n_dev = nullptr) {
+    if (n_dev) n = *n_dev;
     for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
         const int t = tet[i];
         if (t >= 0) atomicAdd(count + t / 12, 1);
@@ -135,7 +137,8 @@ __global__ void count_cells_kernel(const int32_t* __restrict__ tet, int n, int* 
 }
 
 __global__ void scatter_cells_kernel(const int32_t* __restrict__ tet, int n, const int* __restrict__ start,
-                                     int* __restrict__ cursor, int* __restrict__ idx) {
+                                     int* __restrict__ cursor, int* __restrict__ idx, const int* n_dev = nullptr) {
+    if (n_dev) n = *n_dev;
     for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
         const int t = tet[i];
         if (t >= 0) {
@@ -325,6 +328,10 @@ struct MccParams {
     uint32_t step;
     const int* cand_off;  // n_cells + 1
     unsigned long long* counts;
+    long stage_cap;       // staging slots; a cell whose candidates do not fit drops its secondaries
+    int* overflow;        // raised when that happens
+    unsigned long long* iz_cell;  // optional ionisations per cell
+    const unsigned* step_dev;     // optional: the step index read on the device (graph replays)
 };
 
 __device__ __forceinline__ long mcc_candidates(const MccParams& M, int c, double* coll_out) {
@@ -356,9 +363,16 @@ __global__ void mcc_kernel(MccParams M, DSpecies el, Secondary* __restrict__ sta
     const double* EL = M.xs + M.n_xs;
     const double* EX = M.xs + 2 * M.n_xs;
     const double* IZ = M.xs + 3 * M.n_xs;
-    Rng r(M.seed, kStreamMcc, uint32_t(c), M.step);
+    Rng r(M.seed, kStreamMcc, uint32_t(c), M.step_dev ? *M.step_dev : M.step);
     unsigned long long nel = 0, nex = 0, niz = 0;
     const int base = M.cand_off[c];
+    const bool room = long(base) + nC <= M.stage_cap;
+    if (!room) {
+        // this cell's slots below the capacity stay unused: clear them so
+        // that no stale flag is appended
+        atomicExch(M.overflow, 1);
+        for (long k = base; k < long(base) + nC && k < M.stage_cap; ++k) stage[k].flag = 0;
+    }
     for (long i = 0; i < nC; ++i) {
         long j = long(r.uniform() * double(eC));
         if (j >= eC) j = eC - 1;
@@ -424,28 +438,41 @@ __global__ void mcc_kernel(MccParams M, DSpecies el, Secondary* __restrict__ sta
                 if (el.y64[0]) { sc.y[0] = el.y64[0][pi]; sc.y[1] = el.y64[1][pi]; sc.y[2] = el.y64[2][pi]; }
                 else { sc.y[0] = el.y32[0][pi]; sc.y[1] = el.y32[1][pi]; sc.y[2] = el.y32[2][pi]; }
             }
-            stage[base + i] = sc;
+            if (room) stage[base + i] = sc;
             continue;
         }
-        stage[base + i].flag = 0;
+        if (room) stage[base + i].flag = 0;
     }
+    if (M.iz_cell && niz) M.iz_cell[c] += niz;
     atomicAdd(M.counts + 0, (unsigned long long)nC);
     if (nel) atomicAdd(M.counts + 1, nel);
     if (nex) atomicAdd(M.counts + 2, nex);
     if (niz) atomicAdd(M.counts + 3, niz);
 }
 
-__global__ void stage_flags_kernel(const Secondary* __restrict__ stage, int n, int bit, int* __restrict__ flags) {
+// n_dev (optional): the staged count is read on the device; slots from it
+// to n are flagged 0.
+__global__ void stage_flags_kernel(const Secondary* __restrict__ stage, int n, int bit, int* __restrict__ flags,
+                                   const int* n_dev = nullptr) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i < n) flags[i] = (stage[i].flag & bit) ? 1 : 0;
+    const int used = n_dev ? min(*n_dev, n) : n;
+    if (i < n) flags[i] = (i < used && (stage[i].flag & bit)) ? 1 : 0;
 }
 
+// base_dev (optional): the destination offset is read on the device; slots
+// at or beyond cap are dropped and raise *overflow.
 template <class R>
 __global__ void stage_append_kernel(const Secondary* __restrict__ stage, int n, int bit,
-                                    const int* __restrict__ pos, DSpecies dst, int base) {
+                                    const int* __restrict__ pos, DSpecies dst, int base,
+                                    const int* base_dev = nullptr, long cap = 0, int* overflow = nullptr) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n || !(stage[i].flag & bit)) return;
-    const int k = base + pos[i];
+    const long kk = long(base_dev ? *base_dev : base) + pos[i];
+    if (base_dev && kk >= cap) {
+        atomicExch(overflow, 1);
+        return;
+    }
+    const int k = int(kk);
     const Secondary& s = stage[i];
     dst.tet[k] = s.tet;
     const double* u = bit == 1 ? s.ue : s.ui;
@@ -471,6 +498,7 @@ struct IonMccParams {
     uint64_t seed;
     uint32_t step;
     unsigned long long* counts;
+    const unsigned* step_dev;
 };
 
 // IonNeutralCollisionModel::performBackgroundCollisions: elastic scattering
@@ -490,7 +518,7 @@ __global__ void ion_mcc_kernel(IonMccParams M, DSpecies ions) {
     const double* E = M.xs;
     const double* EL = M.xs + M.n_xs;
     const double* CX = M.xs + 2 * M.n_xs;
-    Rng r(M.seed, kStreamIonMcc, uint32_t(c), M.step);
+    Rng r(M.seed, kStreamIonMcc, uint32_t(c), M.step_dev ? *M.step_dev : M.step);
     unsigned long long nel = 0, ncx = 0;
     const double mt = M.mi + M.mg;
     for (long i = 0; i < nC; ++i) {
@@ -571,6 +599,7 @@ struct CoulombParams {
     uint64_t seed;
     uint32_t step;
     unsigned long long* counts;
+    const unsigned* step_dev;
 };
 
 // NanbuWeightCorrectionModel::correctVelocity (NanbuCorrection.C:50-66).
@@ -706,7 +735,7 @@ __global__ void coulomb_kernel(CoulombSpecies C, CoulombParams K) {
     const int c = blockIdx.x * blockDim.x + threadIdx.x;
     if (c >= K.n_cells) return;
     const double V = K.vol[c];
-    Rng r(K.seed, kStreamCoulomb, uint32_t(c), K.step);
+    Rng r(K.seed, kStreamCoulomb, uint32_t(c), K.step_dev ? *K.step_dev : K.step);
     const double lD = K.cl == 0.0 ? debye_length<R>(C, K, c) : 0.0;
     unsigned long long pairs = 0;
     for (int i = 0; i < C.n; ++i) {
@@ -934,10 +963,14 @@ int collide_init(CollideState& st, const picgpu_config& cfg, const DMesh& m, cud
     const int nc = m.n_cells;
     if (dmalloc(&st.cell_start, size_t(PICGPU_MAX_SPECIES) * (nc + 1)) ||
         dmalloc(&st.cell_count, size_t(PICGPU_MAX_SPECIES) * (nc + 1)) || dmalloc(&st.cell_cursor, nc + 1) ||
-        dmalloc(&st.counts, 8) || dmalloc(&st.scan_tmp, (nc + 1) / 1024 + 8)) {
+        dmalloc(&st.counts, 8) || dmalloc(&st.scan_tmp, (nc + 1) / 1024 + 8) || dmalloc(&st.overflow, 1) ||
+        (cfg.mcc.enabled && dmalloc(&st.iz_cell, nc))) {
         *msg = "collision state: device allocation failed";
         return PICGPU_OOM;
     }
+    cudaMemsetAsync(st.overflow, 0, sizeof(int), s);
+    cudaMemsetAsync(st.counts, 0, 8 * sizeof(unsigned long long), s);
+    if (st.iz_cell) cudaMemsetAsync(st.iz_cell, 0, size_t(nc) * sizeof(unsigned long long), s);
     if (cfg.coulomb.enabled) {
         const picgpu_coulomb& co = cfg.coulomb;
         if (co.pairing < 0 || co.pairing > 1 || co.collide < 0 || co.collide > 1 || co.coulomb_log < 0 ||
@@ -996,6 +1029,7 @@ int collide_init(CollideState& st, const picgpu_config& cfg, const DMesh& m, cud
         if (!(sv > 0))
             sv = find_maximum(xs, mc.n_xs, 4, cfg.species[cfg.electron_species].mass, mc.find_max_energy,
                               mc.find_energy_step);
+        st.svmax_init = sv;
         // remainders seeded U(0,1) (ElectronNeutralCollisionModel.C:286-296)
         const int e = upload_mcc(&st.svmax, &st.remainder, &st.xs, xs, sv, cfg.seed, kStreamRemainder, nc, s, msg);
         if (e) return e;
@@ -1043,9 +1077,10 @@ int collide_init(CollideState& st, const picgpu_config& cfg, const DMesh& m, cud
 }
 
 void collide_free(CollideState& st) {
-    void* ptrs[] = {st.svmax,      st.remainder, st.xs,     st.isvmax, st.iremainder, st.ixs,   st.cell_start,
-                    st.cell_count, st.cell_cursor, st.counts, st.scan_tmp, st.ncand,  st.cand_off, st.stage,
-                    st.flags,      st.pos,       st.stage_tmp};
+    void* ptrs[] = {st.svmax,      st.remainder,   st.xs,     st.isvmax,   st.iremainder, st.ixs,
+                    st.cell_start, st.cell_count,  st.cell_cursor, st.counts, st.scan_tmp, st.ncand,
+                    st.cand_off,   st.stage,       st.flags,  st.pos,      st.stage_tmp, st.overflow,
+                    st.iz_cell};
     for (void* p : ptrs)
         if (p) cudaFree(p);
     for (int s = 0; s < PICGPU_MAX_SPECIES; ++s) {
@@ -1148,6 +1183,120 @@ int sort_species(CollideState& st, const DMesh& m, int s, const DSpecies& src, c
     return cudaGetLastError() == cudaSuccess ? PICGPU_OK : PICGPU_CUDA_ERROR;
 }
 
+namespace {
+
+void coulomb_setup(const CollideState& st, const CollideArgs& a, CoulombSpecies& C, CoulombParams& K) {
+    const picgpu_config& cfg = *a.cfg;
+    const int nc = a.m.n_cells;
+    C = CoulombSpecies{};
+    for (int s = 0; s < a.n_species; ++s) {
+        if (cfg.species[s].charge == 0.0 || !cfg.species[s].solve_movement) continue;
+        const int k = C.n++;
+        C.sp[k] = s;
+        C.m[k] = cfg.species[s].mass;
+        C.q[k] = cfg.species[s].charge;
+        C.w[k] = cfg.species[s].weight;
+        C.start[k] = st.cell_start + size_t(s) * (nc + 1);
+        C.idx[k] = st.idx[s];
+        C.sel[k] = st.sel[s];
+        C.sel2[k] = st.sel2[s];
+        C.p[k] = a.sp[s];
+    }
+    K = CoulombParams{};
+    K.n_cells = nc;
+    K.vol = a.m.vol;
+    K.cl = cfg.coulomb.coulomb_log;
+    K.takizuka_abe = cfg.coulomb.pairing == PICGPU_PAIRING_TAKIZUKA_ABE;
+    K.perez = cfg.coulomb.collide == PICGPU_COLLIDE_PEREZ;
+    K.allow_intra = cfg.coulomb.allow_intra;
+    K.calc_bmin = cfg.coulomb.calculate_bmin;
+    K.debye_drift = cfg.coulomb.debye_drift;
+    K.weight_corr = cfg.coulomb.weight_correction;
+    K.dt = cfg.dt;
+    K.seed = cfg.seed;
+    K.step = uint32_t(a.step);
+    K.counts = st.counts;
+}
+
+MccParams mcc_setup(const CollideState& st, const CollideArgs& a) {
+    const picgpu_config& cfg = *a.cfg;
+    const picgpu_mcc& mc = cfg.mcc;
+    const int nc = a.m.n_cells;
+    const int es = cfg.electron_species;
+    MccParams M{};
+    M.n_cells = nc;
+    M.e_start = st.cell_start + size_t(es) * (nc + 1);
+    M.e_idx = st.idx[es];
+    M.svmax = st.svmax;
+    M.rem = st.remainder;
+    M.xs = st.xs;
+    M.n_xs = st.n_xs;
+    M.n_gas = mc.gas_density;
+    M.mg = mc.gas_mass;
+    M.vth_gas = std::sqrt(kKb * mc.gas_temperature / mc.gas_mass);
+    M.me = cfg.species[es].mass;
+    M.dt = cfg.dt;
+    for (int k = 0; k < 3; ++k) M.drift[k] = mc.gas_velocity[k];
+    M.ex_th = mc.ex_threshold;
+    M.iz_th = mc.iz_threshold;
+    M.wEwN = cfg.species[es].weight / mc.gas_weight;
+    M.wNwE = 1.0 / M.wEwN;
+    M.create_e = mc.create_electron;
+    M.create_i = mc.create_ion;
+    M.relativistic = mc.scatter == 1;
+    M.seed = cfg.seed;
+    M.step = uint32_t(a.step);
+    M.counts = st.counts;
+    M.cand_off = st.cand_off;
+    M.stage_cap = st.stage_cap;
+    M.overflow = st.overflow;
+    M.iz_cell = st.iz_cell;
+    return M;
+}
+
+IonMccParams ion_setup(const CollideState& st, const CollideArgs& a) {
+    const picgpu_config& cfg = *a.cfg;
+    const picgpu_mcc& gas = cfg.mcc;
+    const int nc = a.m.n_cells;
+    const int is = cfg.ion_mcc.ion_species;
+    IonMccParams M{};
+    M.n_cells = nc;
+    M.i_start = st.cell_start + size_t(is) * (nc + 1);
+    M.i_idx = st.idx[is];
+    M.svmax = st.isvmax;
+    M.rem = st.iremainder;
+    M.xs = st.ixs;
+    M.n_xs = st.n_ixs;
+    M.n_gas = gas.gas_density;
+    M.mg = gas.gas_mass;
+    M.vth_gas = std::sqrt(kKb * gas.gas_temperature / gas.gas_mass);
+    M.mi = cfg.species[is].mass;
+    M.dt = cfg.dt;
+    for (int k = 0; k < 3; ++k) M.drift[k] = gas.gas_velocity[k];
+    M.cx_th = cfg.ion_mcc.cx_threshold;
+    M.seed = cfg.seed;
+    M.step = uint32_t(a.step);
+    M.counts = st.counts;
+    return M;
+}
+
+__global__ void set_first_kernel(const int* n_dev, int* first_dev, int ns) {
+    if (threadIdx.x < ns) first_dev[threadIdx.x] = n_dev[threadIdx.x];
+}
+
+// n += the secondaries just appended (clamped at the capacity).
+__global__ void append_commit_kernel(int* n_dev, const int* add, long cap, int* overflow) {
+    const long nn = long(*n_dev) + *add;
+    if (nn > cap) {
+        *overflow = 1;
+        *n_dev = int(cap);
+    } else {
+        *n_dev = int(nn);
+    }
+}
+
+}  // namespace
+
 int run_collisions(CollideState& st, const CollideArgs& a, int64_t counts[8], long newn[], int swapped[],
                    std::string* msg, int64_t* launches, double* phase_ms) {
     (void)phase_ms;
@@ -1164,34 +1313,9 @@ int run_collisions(CollideState& st, const CollideArgs& a, int64_t counts[8], lo
     // PICCloud.C:526-539); parcels created on the way do not join the lists
     // (PICCloud::addNewParcel adds to the cloud only)
     if (cfg.coulomb.enabled) {
-        CoulombSpecies C{};
-        for (int s = 0; s < a.n_species; ++s) {
-            if (cfg.species[s].charge == 0.0 || !cfg.species[s].solve_movement) continue;
-            const int k = C.n++;
-            C.sp[k] = s;
-            C.m[k] = cfg.species[s].mass;
-            C.q[k] = cfg.species[s].charge;
-            C.w[k] = cfg.species[s].weight;
-            C.start[k] = st.cell_start + size_t(s) * (nc + 1);
-            C.idx[k] = st.idx[s];
-            C.sel[k] = st.sel[s];
-            C.sel2[k] = st.sel2[s];
-            C.p[k] = a.sp[s];
-        }
-        CoulombParams K{};
-        K.n_cells = nc;
-        K.vol = a.m.vol;
-        K.cl = cfg.coulomb.coulomb_log;
-        K.takizuka_abe = cfg.coulomb.pairing == PICGPU_PAIRING_TAKIZUKA_ABE;
-        K.perez = cfg.coulomb.collide == PICGPU_COLLIDE_PEREZ;
-        K.allow_intra = cfg.coulomb.allow_intra;
-        K.calc_bmin = cfg.coulomb.calculate_bmin;
-        K.debye_drift = cfg.coulomb.debye_drift;
-        K.weight_corr = cfg.coulomb.weight_correction;
-        K.dt = cfg.dt;
-        K.seed = cfg.seed;
-        K.step = uint32_t(a.step);
-        K.counts = st.counts;
+        CoulombSpecies C;
+        CoulombParams K;
+        coulomb_setup(st, a, C, K);
         if (a.mixed) coulomb_kernel<float><<<(nc + 63) / 64, 64, 0, a.stream>>>(C, K);
         else coulomb_kernel<double><<<(nc + 63) / 64, 64, 0, a.stream>>>(C, K);
         *launches += 1;
@@ -1199,30 +1323,7 @@ int run_collisions(CollideState& st, const CollideArgs& a, int64_t counts[8], lo
     if (cfg.mcc.enabled) {
         const picgpu_mcc& mc = cfg.mcc;
         const int es = cfg.electron_species;
-        MccParams M{};
-        M.n_cells = nc;
-        M.e_start = st.cell_start + size_t(es) * (nc + 1);
-        M.e_idx = st.idx[es];
-        M.svmax = st.svmax;
-        M.rem = st.remainder;
-        M.xs = st.xs;
-        M.n_xs = st.n_xs;
-        M.n_gas = mc.gas_density;
-        M.mg = mc.gas_mass;
-        M.vth_gas = std::sqrt(kKb * mc.gas_temperature / mc.gas_mass);
-        M.me = cfg.species[es].mass;
-        M.dt = cfg.dt;
-        for (int k = 0; k < 3; ++k) M.drift[k] = mc.gas_velocity[k];
-        M.ex_th = mc.ex_threshold;
-        M.iz_th = mc.iz_threshold;
-        M.wEwN = cfg.species[es].weight / mc.gas_weight;
-        M.wNwE = 1.0 / M.wEwN;
-        M.create_e = mc.create_electron;
-        M.create_i = mc.create_ion;
-        M.relativistic = mc.scatter == 1;
-        M.seed = cfg.seed;
-        M.step = uint32_t(a.step);
-        M.counts = st.counts;
+        MccParams M = mcc_setup(st, a);
         // candidates per cell and their staging offsets
         mcc_count_kernel<<<(nc + 255) / 256, 256, 0, a.stream>>>(M, st.ncand);
         exclusive_scan(st.ncand, st.cand_off, nc, st.scan_tmp, a.stream, launches);
@@ -1244,8 +1345,11 @@ int run_collisions(CollideState& st, const CollideArgs& a, int64_t counts[8], lo
             st.stage_cap = cap;
         }
         M.cand_off = st.cand_off;
-        if (a.mixed) mcc_kernel<float><<<(nc + 127) / 128, 128, 0, a.stream>>>(M, a.sp[es], st.stage);
-        else mcc_kernel<double><<<(nc + 127) / 128, 128, 0, a.stream>>>(M, a.sp[es], st.stage);
+        M.stage_cap = st.stage_cap;
+        M.overflow = st.overflow;
+        M.iz_cell = st.iz_cell;
+        if (a.mixed) mcc_kernel<float><<<(nc + st.mcc_block - 1) / st.mcc_block, st.mcc_block, 0, a.stream>>>(M, a.sp[es], st.stage);
+        else mcc_kernel<double><<<(nc + st.mcc_block - 1) / st.mcc_block, st.mcc_block, 0, a.stream>>>(M, a.sp[es], st.stage);
         *launches += 2;
         // append secondaries in (cell, candidate) order
         if (total > 0) {
@@ -1276,28 +1380,10 @@ int run_collisions(CollideState& st, const CollideArgs& a, int64_t counts[8], lo
     }
     // ion-neutral last, over the ions present before this step's secondaries
     if (cfg.ion_mcc.enabled) {
-        const picgpu_mcc& gas = cfg.mcc;
         const int is = cfg.ion_mcc.ion_species;
-        IonMccParams M{};
-        M.n_cells = nc;
-        M.i_start = st.cell_start + size_t(is) * (nc + 1);
-        M.i_idx = st.idx[is];
-        M.svmax = st.isvmax;
-        M.rem = st.iremainder;
-        M.xs = st.ixs;
-        M.n_xs = st.n_ixs;
-        M.n_gas = gas.gas_density;
-        M.mg = gas.gas_mass;
-        M.vth_gas = std::sqrt(kKb * gas.gas_temperature / gas.gas_mass);
-        M.mi = cfg.species[is].mass;
-        M.dt = cfg.dt;
-        for (int k = 0; k < 3; ++k) M.drift[k] = gas.gas_velocity[k];
-        M.cx_th = cfg.ion_mcc.cx_threshold;
-        M.seed = cfg.seed;
-        M.step = uint32_t(a.step);
-        M.counts = st.counts;
-        if (a.mixed) ion_mcc_kernel<float><<<(nc + 127) / 128, 128, 0, a.stream>>>(M, a.sp[is]);
-        else ion_mcc_kernel<double><<<(nc + 127) / 128, 128, 0, a.stream>>>(M, a.sp[is]);
+        const IonMccParams M = ion_setup(st, a);
+        if (a.mixed) ion_mcc_kernel<float><<<(nc + st.mcc_block - 1) / st.mcc_block, st.mcc_block, 0, a.stream>>>(M, a.sp[is]);
+        else ion_mcc_kernel<double><<<(nc + st.mcc_block - 1) / st.mcc_block, st.mcc_block, 0, a.stream>>>(M, a.sp[is]);
         *launches += 1;
     }
     unsigned long long h[8];
@@ -1307,6 +1393,117 @@ int run_collisions(CollideState& st, const CollideArgs& a, int64_t counts[8], lo
         return PICGPU_CUDA_ERROR;
     }
     for (int k = 0; k < 8; ++k) counts[k] = (int64_t)h[k];
+    return cudaGetLastError() == cudaSuccess ? PICGPU_OK : PICGPU_CUDA_ERROR;
+}
+
+int collide_reserve_device(CollideState& st, const CollideArgs& a, std::string* msg) {
+    const picgpu_config& cfg = *a.cfg;
+    const int nc = a.m.n_cells;
+    for (int s = 0; s < a.n_species; ++s) {
+        if (st.idx_cap[s] >= a.cap[s]) continue;
+        if (st.idx[s]) cudaFree(st.idx[s]);
+        if (st.sel[s]) cudaFree(st.sel[s]);
+        if (st.sel2[s]) cudaFree(st.sel2[s]);
+        st.idx[s] = st.sel[s] = st.sel2[s] = nullptr;
+        if (dmalloc(&st.idx[s], a.cap[s]) || dmalloc(&st.sel[s], a.cap[s]) || dmalloc(&st.sel2[s], a.cap[s])) {
+            *msg = "cell occupancy: device allocation failed";
+            return PICGPU_OOM;
+        }
+        st.idx_cap[s] = a.cap[s];
+    }
+    if (cfg.mcc.enabled) {
+        // candidates per step: sum over cells of ceil(R + N_c n (sigma v)_max dt)
+        // <= n_cells + N n (sigma v)_max dt; (sigma v)_max may grow, so twice
+        // the initial bound plus margin
+        const int es = cfg.electron_species;
+        const double per = cfg.mcc.gas_density * st.svmax_init * cfg.dt;
+        const long need = long(nc) + long(2.0 * per * double(a.cap[es])) + 65536;
+        if (st.stage_cap < need) {
+            if (st.stage) cudaFree(st.stage);
+            if (st.flags) cudaFree(st.flags);
+            if (st.pos) cudaFree(st.pos);
+            if (st.stage_tmp) cudaFree(st.stage_tmp);
+            st.stage = nullptr;
+            st.flags = st.pos = st.stage_tmp = nullptr;
+            if (dmalloc(&st.stage, need) || dmalloc(&st.flags, need + 1) || dmalloc(&st.pos, need + 2) ||
+                dmalloc(&st.stage_tmp, need / 1024 + 8)) {
+                *msg = "MCC staging: device allocation failed";
+                return PICGPU_OOM;
+            }
+            st.stage_cap = need;
+        }
+    }
+    return PICGPU_OK;
+}
+
+int run_collisions_device(CollideState& st, const CollideArgs& a, int* n_dev, int* first_dev,
+                          const unsigned* step_dev, std::string* msg, int64_t* launches) {
+    const picgpu_config& cfg = *a.cfg;
+    const int nc = a.m.n_cells;
+    set_first_kernel<<<1, 32, 0, a.stream>>>(n_dev, first_dev, a.n_species);
+    *launches += 1;
+    for (int s = 0; s < a.n_species; ++s) {
+        if (st.idx_cap[s] < a.cap[s]) {
+            *msg = "device-driven collisions: lists not reserved";
+            return PICGPU_INVALID_ARG;
+        }
+        int* cnt = st.cell_count + size_t(s) * (nc + 1);
+        int* start = st.cell_start + size_t(s) * (nc + 1);
+        cudaMemsetAsync(cnt, 0, (nc + 1) * sizeof(int), a.stream);
+        cudaMemsetAsync(st.cell_cursor, 0, (nc + 1) * sizeof(int), a.stream);
+        const long cap = a.cap[s];
+        count_cells_kernel<<<grid_of(cap, 256), 256, 0, a.stream>>>(a.sp[s].tet, int(cap), cnt, n_dev + s);
+        exclusive_scan(cnt, start, nc, st.scan_tmp, a.stream, launches);
+        scatter_cells_kernel<<<grid_of(cap, 256), 256, 0, a.stream>>>(a.sp[s].tet, int(cap), start, st.cell_cursor,
+                                                                      st.idx[s], n_dev + s);
+        order_cells_kernel<<<(nc + 127) / 128, 128, 0, a.stream>>>(nc, start, st.idx[s]);
+        *launches += 3;
+    }
+    if (cfg.coulomb.enabled) {
+        CoulombSpecies C;
+        CoulombParams K;
+        coulomb_setup(st, a, C, K);
+        K.step_dev = step_dev;
+        if (a.mixed) coulomb_kernel<float><<<(nc + 63) / 64, 64, 0, a.stream>>>(C, K);
+        else coulomb_kernel<double><<<(nc + 63) / 64, 64, 0, a.stream>>>(C, K);
+        *launches += 1;
+    }
+    if (cfg.mcc.enabled) {
+        const picgpu_mcc& mc = cfg.mcc;
+        const int es = cfg.electron_species;
+        MccParams M = mcc_setup(st, a);
+        M.step_dev = step_dev;
+        const long scap = st.stage_cap;
+        mcc_count_kernel<<<(nc + 255) / 256, 256, 0, a.stream>>>(M, st.ncand);
+        exclusive_scan(st.ncand, st.cand_off, nc, st.scan_tmp, a.stream, launches);
+        if (a.mixed) mcc_kernel<float><<<(nc + st.mcc_block - 1) / st.mcc_block, st.mcc_block, 0, a.stream>>>(M, a.sp[es], st.stage);
+        else mcc_kernel<double><<<(nc + st.mcc_block - 1) / st.mcc_block, st.mcc_block, 0, a.stream>>>(M, a.sp[es], st.stage);
+        *launches += 2;
+        for (int bit = 1; bit <= 2; bit <<= 1) {
+            const int s = bit == 1 ? es : mc.ion_species;
+            if (s < 0 || (bit == 1 && !mc.create_electron) || (bit == 2 && !mc.create_ion)) continue;
+            // slots past the staged candidates (cand_off[nc]) are flagged 0
+            stage_flags_kernel<<<unsigned((scap + 255) / 256), 256, 0, a.stream>>>(st.stage, int(scap), bit, st.flags,
+                                                                                   st.cand_off + nc);
+            exclusive_scan(st.flags, st.pos, scap, st.stage_tmp, a.stream, launches);
+            if (a.mixed)
+                stage_append_kernel<float><<<unsigned((scap + 255) / 256), 256, 0, a.stream>>>(
+                    st.stage, int(scap), bit, st.pos, a.sp[s], 0, n_dev + s, a.cap[s], st.overflow);
+            else
+                stage_append_kernel<double><<<unsigned((scap + 255) / 256), 256, 0, a.stream>>>(
+                    st.stage, int(scap), bit, st.pos, a.sp[s], 0, n_dev + s, a.cap[s], st.overflow);
+            append_commit_kernel<<<1, 1, 0, a.stream>>>(n_dev + s, st.pos + scap, a.cap[s], st.overflow);
+            *launches += 3;
+        }
+    }
+    if (cfg.ion_mcc.enabled) {
+        const int is = cfg.ion_mcc.ion_species;
+        IonMccParams M = ion_setup(st, a);
+        M.step_dev = step_dev;
+        if (a.mixed) ion_mcc_kernel<float><<<(nc + st.mcc_block - 1) / st.mcc_block, st.mcc_block, 0, a.stream>>>(M, a.sp[is]);
+        else ion_mcc_kernel<double><<<(nc + st.mcc_block - 1) / st.mcc_block, st.mcc_block, 0, a.stream>>>(M, a.sp[is]);
+        *launches += 1;
+    }
     return cudaGetLastError() == cudaSuccess ? PICGPU_OK : PICGPU_CUDA_ERROR;
 }
 

@@ -47,6 +47,10 @@ struct CollideState {
     int* pos = nullptr;
     int* stage_tmp = nullptr;
     long stage_cap = 0;
+    int* overflow = nullptr;                // staging or store overflow (device-driven step)
+    double svmax_init = 0.0;                // initial (sigma v)_max of the electron MCC
+    int mcc_block = 128;                    // threads per block of the MCC kernel (one cell each)
+    unsigned long long* iz_cell = nullptr;  // MCC ionisations per cell (accumulated)
 };
 
 struct CollideArgs {
@@ -74,5 +78,15 @@ int sort_species(CollideState& st, const DMesh& m, int s, const DSpecies& src, c
 // receives the species counts after MCC secondaries were appended.
 int run_collisions(CollideState& st, const CollideArgs& a, int64_t counts[8], long newn[], int swapped[],
                    std::string* msg, int64_t* launches, double* phase_ms);
+
+// Device-driven form of run_collisions for a step captured in a CUDA graph:
+// the species counts n_dev[s] stay on the device (MCC secondaries are
+// appended there, first_dev[s] receiving the count before them), nothing is
+// read back, and the counts in st.counts accumulate over steps.  Staging and
+// lists are sized by collide_reserve_device from the species capacities a.cap;
+// a step that would need more raises st.overflow and drops secondaries.
+int collide_reserve_device(CollideState& st, const CollideArgs& a, std::string* msg);
+int run_collisions_device(CollideState& st, const CollideArgs& a, int* n_dev, int* first_dev,
+                          const unsigned* step_dev, std::string* msg, int64_t* launches);
 
 }  // namespace pgd

@@ -109,6 +109,8 @@ struct MoveParams {
     DMesh m;
     int n;                   // particles in this species (including removed slots)
     int first;               // first slot to process
+    const int* n_dev;        // FP32 form: when set, n (and first, from first_dev) are read on the
+    const int* first_dev;    // device, so the launch can sit in a CUDA graph
     int species;
     int pusher;
     int field_weighting;

@@ -19,6 +19,7 @@
 // coordinates across unchanged up to a fixed permutation.
 #pragma once
 
+#include <algorithm>
 #include <cmath>
 #include <cstdint>
 #include <cstring>
@@ -587,6 +588,90 @@ inline void position(const HexMesh& m, long long tet, const double* bary, double
         x[a] = m.cc[3 * size_t(c) + a] + bary[0] * off[3 * m.tt.tri[t][0] + a] +
                bary[1] * off[3 * m.tt.tri[t][1] + a] + bary[2] * off[3 * m.tt.tri[t][2] + a];
     }
+}
+
+// `copies` topologically disjoint copies of one block mesh: a batched
+// ensemble of independent cases in one store.  Cell, point and boundary-face
+// indices of copy k are those of the single case plus k times the case's
+// counts; geometry classes, patches and coordinates are shared (the copies
+// overlap in space, which only the host-side locate/position calls see: they
+// address copy 0).  Patch areas and face counts are totals over the copies.
+inline HexMesh replicate_mesh(const HexMesh& one, int copies) {
+    if (copies <= 1) return one;
+    HexMesh m = one;
+    const int nc = one.n_cells, np = one.n_points, ngp = one.n_grid_points;
+    const int nbf = int(one.bfaces.size());
+    m.n_cells = nc * copies;
+    m.n_points = np * copies;
+    m.n_grid_points = ngp * copies;
+    auto raw = [copies](std::vector<double>& v) {
+        const size_t n = v.size();
+        v.resize(n * copies);
+        for (int k = 1; k < copies; ++k) std::copy(v.begin(), v.begin() + n, v.begin() + k * n);
+    };
+    auto raw_i = [copies](std::vector<int>& v) {
+        const size_t n = v.size();
+        v.resize(n * copies);
+        for (int k = 1; k < copies; ++k) std::copy(v.begin(), v.begin() + n, v.begin() + k * n);
+    };
+    auto shifted = [copies](const std::vector<int>& src, int step, bool keep_negative) {
+        std::vector<int> v(src.size() * copies);
+        for (int k = 0; k < copies; ++k)
+            for (size_t i = 0; i < src.size(); ++i) {
+                const int x = src[i];
+                v[k * src.size() + i] = (keep_negative && x < 0) ? x : x + k * step;
+            }
+        return v;
+    };
+    raw(m.grid_pts);
+    raw_i(m.cell_ijk);
+    raw(m.cc);
+    raw(m.vol);
+    raw_i(m.cell_class);
+    raw(m.lap_off);
+    raw(m.lap_diag);
+    raw(m.ip_weight);
+    raw(m.vw_weight);
+    m.cell_gpt = shifted(one.cell_gpt, ngp, false);
+    m.cell_pt = shifted(one.cell_pt, np, false);
+    m.nbr = shifted(one.nbr, nc, true);
+    m.cell_bface = shifted(one.cell_bface, nbf, true);
+    m.bfaces.clear();
+    for (int k = 0; k < copies; ++k)
+        for (BFace b : one.bfaces) {
+            b.cell += k * nc;
+            m.bfaces.push_back(b);
+        }
+    for (Patch& p : m.patches) {
+        p.area *= copies;
+        p.n_faces *= copies;
+    }
+    // CSR point interpolation: sources are cells (>= 0) or boundary faces (< 0)
+    m.pi_start.assign(size_t(np) * copies + 1, 0);
+    m.pi_src.clear();
+    m.pi_w.clear();
+    for (int k = 0; k < copies; ++k) {
+        for (int p = 0; p < np; ++p) {
+            m.pi_start[size_t(k) * np + p] = int(m.pi_src.size());
+            for (int q = one.pi_start[p]; q < one.pi_start[p + 1]; ++q) {
+                const int src = one.pi_src[q];
+                m.pi_src.push_back(src >= 0 ? src + k * nc : -(-src - 1 + k * nbf) - 1);
+                m.pi_w.push_back(one.pi_w[q]);
+            }
+        }
+    }
+    m.pi_start[size_t(np) * copies] = int(m.pi_src.size());
+    // point -> cell-corner slots 9 c + 1 + corner
+    m.pc_start.assign(size_t(np) * copies + 1, 0);
+    m.pc_slot.clear();
+    for (int k = 0; k < copies; ++k) {
+        for (int p = 0; p < np; ++p) {
+            m.pc_start[size_t(k) * np + p] = int(m.pc_slot.size());
+            for (int q = one.pc_start[p]; q < one.pc_start[p + 1]; ++q) m.pc_slot.push_back(one.pc_slot[q] + 9 * k * nc);
+        }
+    }
+    m.pc_start[size_t(np) * copies] = int(m.pc_slot.size());
+    return m;
 }
 
 }  // namespace pg

@@ -29,6 +29,7 @@
 #include "learned.h"
 #include "particles.h"
 #include "picgpu.h"
+#include "picgpu_ensemble.h"
 
 using pgd::DMesh;
 
@@ -106,6 +107,21 @@ struct picgpu_ctx {
     cudaGraphExec_t pcg_graph = nullptr;
     double pcg_r0 = 0.0;  // ||b - A x0|| / ||b|| of the last solve's start guess
     std::unique_ptr<pgd::LearnedWarmStart> ws;  // learned warm start (cfg.learned.enabled)
+    // batched ensembles and graph-stepped runs
+    int n_cases = 1;
+    int* n_dev = nullptr;          // species counts on the device (graph steps)
+    int* first_dev = nullptr;      // counts before this step's secondaries
+    unsigned* step_dev = nullptr;  // step index read by the collision kernels
+    struct GraphEntry {
+        uint64_t key;
+        cudaGraphExec_t exec;
+    };
+    std::vector<GraphEntry> graphs;
+    uint64_t graph_sig = 0;        // signature of the buffers the cached graphs address
+    int move_bps = 5;              // FP32 move kernel: blocks per SM
+    bool tuned = false;
+    std::vector<double> tune_ms;
+    long long last_sort = 0;
 };
 
 picgpu_status pgd_collisions(picgpu_ctx* c, picgpu_step_stats* stats);
@@ -653,6 +669,278 @@ picgpu_status pgd_collisions(picgpu_ctx* c, picgpu_step_stats* stats) {
     return PICGPU_OK;
 }
 
+namespace {
+
+// ------------------------------------------------- graph-stepped runs --
+__global__ void step_inc_kernel(unsigned* step) { *step += 1u; }
+
+// Per case and species: count, sum U, sum |U|^2 (shared-memory partials).
+template <class R>
+__global__ void case_stats_kernel(const int32_t* __restrict__ tet, const R* __restrict__ u0,
+                                  const R* __restrict__ u1, const R* __restrict__ u2, long n, int cells_per_case,
+                                  int n_cases, double* __restrict__ out) {
+    extern __shared__ double sh[];  // n_cases * 5
+    for (int k = threadIdx.x; k < n_cases * 5; k += blockDim.x) sh[k] = 0.0;
+    __syncthreads();
+    for (long i = long(blockIdx.x) * blockDim.x + threadIdx.x; i < n; i += long(gridDim.x) * blockDim.x) {
+        const int t = tet[i];
+        if (t < 0) continue;
+        const int k = (t / 12) / cells_per_case;
+        const double a = u0[i], b = u1[i], c = u2[i];
+        atomicAdd(sh + 5 * k, 1.0);
+        atomicAdd(sh + 5 * k + 1, a);
+        atomicAdd(sh + 5 * k + 2, b);
+        atomicAdd(sh + 5 * k + 3, c);
+        atomicAdd(sh + 5 * k + 4, a * a + b * b + c * c);
+    }
+    __syncthreads();
+    for (int k = threadIdx.x; k < n_cases * 5; k += blockDim.x)
+        if (sh[k] != 0.0) atomicAdd(out + k, sh[k]);
+}
+
+__global__ void case_sum_kernel(const unsigned long long* __restrict__ per_cell, int cells_per_case,
+                                unsigned long long* __restrict__ out) {
+    __shared__ unsigned long long s[256];
+    unsigned long long v = 0;
+    const size_t base = size_t(blockIdx.x) * cells_per_case;
+    for (int c = threadIdx.x; c < cells_per_case; c += 256) v += per_cell[base + c];
+    s[threadIdx.x] = v;
+    __syncthreads();
+    for (int o = 128; o > 0; o >>= 1) {
+        if (threadIdx.x < o) s[threadIdx.x] += s[threadIdx.x + o];
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) out[blockIdx.x] = s[0];
+}
+
+bool any_collisions(const picgpu_ctx* c) {
+    return c->cfg.mcc.enabled || c->cfg.coulomb.enabled || c->cfg.ion_mcc.enabled;
+}
+
+pgd::CollideArgs collide_args(picgpu_ctx* c) {
+    pgd::CollideArgs a{};
+    a.m = c->dm;
+    a.cfg = &c->cfg;
+    a.step = c->step_index;
+    a.n_species = c->cfg.n_species;
+    a.mixed = c->mixed;
+    for (int s = 0; s < c->cfg.n_species; ++s) {
+        a.sp[s] = view(c, s, c->sp[s].cur);
+        a.n[s] = c->sp[s].n;
+        a.cap[s] = c->sp[s].cap;
+    }
+    a.stream = c->stream;
+    return a;
+}
+
+// The kernels of one step with every count on the device (captured).
+picgpu_status graph_step_body(picgpu_ctx* c) {
+    picgpu_status s;
+    if ((s = zero_accumulators(c))) return s;
+    const int grid = c->move_bps * c->sm_count;
+    for (int k = 0; k < c->cfg.n_species; ++k) {
+        pgd::MoveParams P = move_params(c, k, false);
+        P.n_dev = c->n_dev + k;
+        P.first_dev = nullptr;
+        pgd::launch_move_fp32(P, grid, c->stream);
+        c->launches++;
+    }
+    if (any_collisions(c)) {
+        std::string msg;
+        const pgd::CollideArgs a = collide_args(c);
+        const int e = pgd::run_collisions_device(c->coll, a, c->n_dev, c->first_dev, c->step_dev, &msg, &c->launches);
+        if (e) return bad(c, picgpu_status(e), msg);
+        // deposit the secondaries of this step (first_dev .. n_dev)
+        for (int k = 0; k < c->cfg.n_species; ++k) {
+            pgd::MoveParams P = move_params(c, k, true);
+            P.n_dev = c->n_dev + k;
+            P.first_dev = c->first_dev + k;
+            pgd::launch_move_fp32(P, grid, c->stream);
+            c->launches++;
+        }
+    }
+    if ((s = charge_update(c))) return s;
+    step_inc_kernel<<<1, 1, 0, c->stream>>>(c->step_dev);
+    c->launches++;
+    CK(cudaGetLastError());
+    return PICGPU_OK;
+}
+
+// The graph for the current buffers and launch shapes, captured on demand.
+picgpu_status graph_for(picgpu_ctx* c, int steps, cudaGraphExec_t* out) {
+    uint64_t key = uint64_t(steps) | (uint64_t(c->move_bps) << 16) | (uint64_t(c->coll.mcc_block) << 24);
+    for (int k = 0; k < c->cfg.n_species; ++k) key |= uint64_t(c->sp[k].cur) << (40 + k);
+    for (const auto& g : c->graphs)
+        if (g.key == key) {
+            *out = g.exec;
+            return PICGPU_OK;
+        }
+    cudaGraph_t g;
+    // phase events are host-side bookkeeping: keep them out of the capture
+    const bool prof = c->profiling;
+    c->profiling = false;
+    CK(cudaStreamBeginCapture(c->stream, cudaStreamCaptureModeThreadLocal));
+    picgpu_status s = PICGPU_OK;
+    for (int j = 0; j < steps && !s; ++j) s = graph_step_body(c);
+    cudaError_t e = cudaStreamEndCapture(c->stream, &g);
+    c->profiling = prof;
+    if (s) {
+        if (e == cudaSuccess) cudaGraphDestroy(g);
+        return s;
+    }
+    CK(e);
+    cudaGraphExec_t exec;
+    e = cudaGraphInstantiate(&exec, g, 0);
+    cudaGraphDestroy(g);
+    CK(e);
+    c->graphs.push_back({key, exec});
+    *out = exec;
+    return PICGPU_OK;
+}
+
+void drop_graphs(picgpu_ctx* c) {
+    for (auto& g : c->graphs) cudaGraphExecDestroy(g.exec);
+    c->graphs.clear();
+}
+
+// FNV-1a over every device pointer a captured step addresses: a graph is
+// reused only while none of them moved.
+uint64_t buffers_signature(const picgpu_ctx* c) {
+    uint64_t h = 1469598103934665603ull;
+    auto mix = [&h](const void* p) {
+        uint64_t v = uint64_t(reinterpret_cast<uintptr_t>(p));
+        for (int i = 0; i < 8; ++i) {
+            h ^= (v >> (8 * i)) & 0xFFu;
+            h *= 1099511628211ull;
+        }
+    };
+    for (int k = 0; k < c->cfg.n_species; ++k) {
+        const SpeciesBuf& B = c->sp[k];
+        for (int q = 0; q < 2; ++q) {
+            mix(B.tet[q]);
+            for (int a = 0; a < 3; ++a) {
+                mix(B.y32[q][a]);
+                mix(B.u32[q][a]);
+            }
+        }
+        mix(c->coll.idx[k]);
+        mix(c->coll.sel[k]);
+        mix(c->coll.sel2[k]);
+    }
+    const void* ps[] = {c->coll.stage, c->coll.flags, c->coll.pos, c->coll.stage_tmp, c->coll.cell_start,
+                        c->coll.cell_count, c->coll.cell_cursor, c->coll.scan_tmp, c->coll.ncand, c->coll.cand_off,
+                        c->acc9, c->Ec4};
+    for (const void* p : ps) mix(p);
+    return h;
+}
+
+// Between replays: re-sort or compact, and reserve room for the next replay.
+picgpu_status graph_maintenance(picgpu_ctx* c, int steps) {
+    picgpu_status s;
+    if (c->cfg.sort_interval > 0 && c->step_index - c->last_sort >= c->cfg.sort_interval) {
+        PhaseScope ps(c, PICGPU_PHASE_SORT);
+        for (int k = 0; k < c->cfg.n_species; ++k) {
+            SpeciesBuf& B = c->sp[k];
+            if (B.n == 0) continue;
+            long kept = 0;
+            std::string msg;
+            const int e = pgd::sort_species(c->coll, c->dm, k, view(c, k, B.cur), view(c, k, B.cur ^ 1), B.n,
+                                            c->mixed, &kept, c->stream, &msg, &c->launches);
+            if (e) return bad(c, picgpu_status(e), msg);
+            B.n = kept;
+            B.alive = kept;
+            B.cur ^= 1;
+        }
+        c->last_sort = c->step_index;
+    } else if ((s = compact(c, false))) {
+        return s;
+    }
+    for (int k = 0; k < c->cfg.n_species; ++k) {
+        // MCC secondaries of the coming replay: keep an eighth (and per step
+        // at least 1/64) of the population free
+        const long n = c->sp[k].n;
+        const long need = n + std::max<long>(n / 8, 4096) + long(steps) * (n / 64 + 1024);
+        if (need > c->sp[k].cap && (s = grow_species(c, k, need + need / 2))) return s;
+    }
+    if (any_collisions(c)) {
+        std::string msg;
+        const pgd::CollideArgs a = collide_args(c);
+        const int e = pgd::collide_reserve_device(c->coll, a, &msg);
+        if (e) return bad(c, picgpu_status(e), msg);
+    }
+    const uint64_t sig = buffers_signature(c);
+    if (sig != c->graph_sig) {
+        drop_graphs(c);
+        c->graph_sig = sig;
+    }
+    return PICGPU_OK;
+}
+
+// One replay of `steps` steps; counters accumulate into stats.
+picgpu_status graph_replay(picgpu_ctx* c, int steps, picgpu_step_stats* stats, float* ms) {
+    picgpu_status s;
+    if ((s = graph_maintenance(c, steps))) return s;
+    int nh[PICGPU_MAX_SPECIES] = {};
+    for (int k = 0; k < c->cfg.n_species; ++k) nh[k] = int(c->sp[k].n);
+    const unsigned step0 = unsigned(c->step_index);
+    CK(cudaMemcpyAsync(c->n_dev, nh, sizeof nh, cudaMemcpyHostToDevice, c->stream));
+    CK(cudaMemcpyAsync(c->step_dev, &step0, sizeof step0, cudaMemcpyHostToDevice, c->stream));
+    CK(cudaMemsetAsync(c->counters, 0, sizeof(pgd::MoveCounters) * PICGPU_MAX_SPECIES, c->stream));
+    if (any_collisions(c)) {
+        CK(cudaMemsetAsync(c->coll.counts, 0, 8 * sizeof(unsigned long long), c->stream));
+        CK(cudaMemsetAsync(c->coll.overflow, 0, sizeof(int), c->stream));
+    }
+    cudaGraphExec_t g;
+    if ((s = graph_for(c, steps, &g))) return s;
+    if (!c->timer[0]) {
+        CK(cudaEventCreate(&c->timer[0]));
+        CK(cudaEventCreate(&c->timer[1]));
+    }
+    {
+        PhaseScope ps(c, PICGPU_PHASE_MOVE);
+        CK(cudaEventRecord(c->timer[0], c->stream));
+        CK(cudaGraphLaunch(g, c->stream));
+        CK(cudaEventRecord(c->timer[1], c->stream));
+    }
+    if ((s = read_counters(c))) return s;
+    int nd[PICGPU_MAX_SPECIES] = {};
+    int ovf = 0;
+    unsigned long long h[8] = {};
+    CK(cudaMemcpyAsync(nd, c->n_dev, sizeof nd, cudaMemcpyDeviceToHost, c->stream));
+    if (any_collisions(c)) {
+        CK(cudaMemcpyAsync(&ovf, c->coll.overflow, sizeof ovf, cudaMemcpyDeviceToHost, c->stream));
+        CK(cudaMemcpyAsync(h, c->coll.counts, sizeof h, cudaMemcpyDeviceToHost, c->stream));
+    }
+    CK(cudaStreamSynchronize(c->stream));
+    if (ms) CK(cudaEventElapsedTime(ms, c->timer[0], c->timer[1]));
+    int err = 0;
+    for (int k = 0; k < c->cfg.n_species; ++k) err = std::max(err, c->counters_host[k].error);
+    if (err)
+        return bad(c, picgpu_status(err), err == PICGPU_SPEED_OF_LIGHT
+                                              ? "particle velocity reached the speed of light"
+                                              : "tracking exceeded track_max_steps for a particle");
+    if (ovf) return bad(c, PICGPU_CAPACITY, "graph step: MCC staging or particle storage ran out of room");
+    add_counters(c, stats);
+    for (int k = 0; k < c->cfg.n_species; ++k) {
+        c->sp[k].alive += long(nd[k]) - c->sp[k].n;
+        c->sp[k].n = nd[k];
+    }
+    if (stats) {
+        stats->mcc_candidates += (int64_t)h[0];
+        stats->mcc_elastic += (int64_t)h[1];
+        stats->mcc_excitation += (int64_t)h[2];
+        stats->mcc_ionization += (int64_t)h[3];
+        stats->coulomb_pairs += (int64_t)h[4];
+        stats->ion_mcc_candidates += (int64_t)h[5];
+        stats->ion_mcc_elastic += (int64_t)h[6];
+        stats->ion_mcc_charge_exchange += (int64_t)h[7];
+    }
+    c->step_index += steps;
+    return PICGPU_OK;
+}
+
+}  // namespace
+
 extern "C" {
 
 picgpu_status picgpu_mesh_create(const picgpu_mesh_desc* desc, picgpu_mesh** out) {
@@ -704,6 +992,8 @@ picgpu_status picgpu_mesh_cells(const picgpu_mesh* mesh, double* centres, double
     return PICGPU_OK;
 }
 
+static picgpu_status create_with_mesh(picgpu_ctx* c, const picgpu_config* cfg);
+
 picgpu_status picgpu_create(const picgpu_mesh_desc* mesh, const picgpu_config* cfg, picgpu_ctx** out) {
     if (!mesh || !cfg || !out) return PICGPU_INVALID_ARG;
     auto* c = new picgpu_ctx();
@@ -713,6 +1003,27 @@ picgpu_status picgpu_create(const picgpu_mesh_desc* mesh, const picgpu_config* c
     } catch (const std::exception& e) {
         return bad(c, PICGPU_INVALID_ARG, e.what());
     }
+    return create_with_mesh(c, cfg);
+}
+
+picgpu_status picgpu_ensemble_create(const picgpu_mesh_desc* one_case, int n_cases, const picgpu_config* cfg,
+                                     picgpu_ctx** out) {
+    if (!one_case || !cfg || !out || n_cases < 1) return PICGPU_INVALID_ARG;
+    auto* c = new picgpu_ctx();
+    *out = c;
+    try {
+        const pg::HexMesh one = pg::build_hex_mesh(*one_case);
+        if (long(one.n_cells) * n_cases > (1L << 31) / 12 - 1)
+            return bad(c, PICGPU_INVALID_ARG, "ensemble: too many cells for 32-bit tet indices");
+        c->m = pg::replicate_mesh(one, n_cases);
+    } catch (const std::exception& e) {
+        return bad(c, PICGPU_INVALID_ARG, e.what());
+    }
+    c->n_cases = n_cases;
+    return create_with_mesh(c, cfg);
+}
+
+static picgpu_status create_with_mesh(picgpu_ctx* c, const picgpu_config* cfg) {
     if (cfg->n_species < 1 || cfg->n_species > PICGPU_MAX_SPECIES)
         return bad(c, PICGPU_INVALID_ARG, "config: n_species must be 1..4");
     if (!(cfg->dt > 0)) return bad(c, PICGPU_INVALID_ARG, "config: dt must be > 0");
@@ -872,7 +1183,8 @@ picgpu_status picgpu_create(const picgpu_mesh_desc* mesh, const picgpu_config* c
         (s = dalloc(c, &c->z, nc)) || (s = dalloc(c, &c->p[0], nc)) || (s = dalloc(c, &c->p[1], nc)) ||
         (s = dalloc(c, &c->q, nc)) || (s = dalloc(c, &c->part, 4 * size_t(pgd::pcg_blocks(int(nc))) + 8)) ||
         (s = dalloc(c, &c->st, 1)) || (s = dalloc(c, &c->counters, PICGPU_MAX_SPECIES)) ||
-        (s = dalloc(c, &c->diag, 64)))
+        (s = dalloc(c, &c->diag, 64)) || (s = dalloc(c, &c->n_dev, PICGPU_MAX_SPECIES)) ||
+        (s = dalloc(c, &c->first_dev, PICGPU_MAX_SPECIES)) || (s = dalloc(c, &c->step_dev, 1)))
         return s;
     if (c->mixed && ((s = dalloc(c, &c->acc9, size_t(cfg->n_species) * 9 * nc)) ||
                      (s = dalloc(c, &c->Ec4, 9 * nc))))
@@ -922,6 +1234,7 @@ void picgpu_destroy(picgpu_ctx* c) {
     for (auto e : c->free_events) cudaEventDestroy(e);
     if (c->timer[0]) { cudaEventDestroy(c->timer[0]); cudaEventDestroy(c->timer[1]); }
     if (c->pcg_graph) cudaGraphExecDestroy(c->pcg_graph);
+    for (auto& g : c->graphs) cudaGraphExecDestroy(g.exec);
     if (c->st_host) cudaFreeHost(c->st_host);
     if (c->counters_host) cudaFreeHost(c->counters_host);
     if (c->stream) cudaStreamDestroy(c->stream);
@@ -1200,6 +1513,134 @@ picgpu_status picgpu_timer_stop(picgpu_ctx* c, double* ms) {
     float f = 0.f;
     CK(cudaEventElapsedTime(&f, c->timer[0], c->timer[1]));
     *ms = f;
+    return PICGPU_OK;
+}
+
+}  // extern "C"
+
+// ------------------------------------------------------------ ensembles --
+extern "C" {
+
+picgpu_status picgpu_ensemble_set_efield(picgpu_ctx* c, const double* E) {
+    if (!c || !E) return PICGPU_INVALID_ARG;
+    if (c->cfg.maxwell_solver != PICGPU_MAXWELL_NONE)
+        return bad(c, PICGPU_INVALID_ARG, "ensemble E field: MaxwellSolver must be none");
+    const long nc = c->m.n_cells / c->n_cases, np = c->m.n_points / c->n_cases;
+    std::vector<double> e(3 * size_t(c->m.n_cells)), ep(3 * size_t(c->m.n_points));
+    for (long i = 0; i < c->m.n_cells; ++i)
+        for (int a = 0; a < 3; ++a) e[3 * i + a] = E[3 * (i / nc) + a];
+    for (long i = 0; i < c->m.n_points; ++i)
+        for (int a = 0; a < 3; ++a) ep[3 * i + a] = E[3 * (i / np) + a];
+    CK(cudaMemcpyAsync(c->E, e.data(), e.size() * sizeof(double), cudaMemcpyHostToDevice, c->stream));
+    CK(cudaMemcpyAsync(c->Ept, ep.data(), ep.size() * sizeof(double), cudaMemcpyHostToDevice, c->stream));
+    pgd::launch_to_float(c->E, c->E32, long(e.size()), c->stream);
+    pgd::launch_to_float(c->Ept, c->Ept32, long(ep.size()), c->stream);
+    c->launches += 2;
+    if (c->Ec4) {
+        pgd::launch_corner_E(c->dm, c->E, c->Ept, c->Ec4, c->stream);
+        c->launches++;
+    }
+    CK(cudaStreamSynchronize(c->stream));
+    return PICGPU_OK;
+}
+
+picgpu_status picgpu_ensemble_case_stats(picgpu_ctx* c, int species, double* out, int64_t* ionisations) {
+    if (!c || !out || species < 0 || species >= c->cfg.n_species) return PICGPU_INVALID_ARG;
+    const int cases = c->n_cases;
+    const int cpc = c->m.n_cells / cases;
+    double* d = nullptr;
+    CK(cudaMalloc(&d, sizeof(double) * 5 * cases));
+    CK(cudaMemsetAsync(d, 0, sizeof(double) * 5 * cases, c->stream));
+    const SpeciesBuf& B = c->sp[species];
+    const pgd::DSpecies v = view(c, species, B.cur);
+    const int grid = std::max(1, std::min<int>(int((B.n + 255) / 256), 4 * c->sm_count));
+    const size_t sm = sizeof(double) * 5 * cases;
+    if (B.n > 0) {
+        if (c->mixed)
+            case_stats_kernel<float><<<grid, 256, sm, c->stream>>>(v.tet, v.u32[0], v.u32[1], v.u32[2], B.n, cpc,
+                                                                    cases, d);
+        else
+            case_stats_kernel<double><<<grid, 256, sm, c->stream>>>(v.tet, v.u64[0], v.u64[1], v.u64[2], B.n, cpc,
+                                                                     cases, d);
+    }
+    cudaError_t e = cudaMemcpyAsync(out, d, sizeof(double) * 5 * cases, cudaMemcpyDeviceToHost, c->stream);
+    if (e == cudaSuccess && ionisations) {
+        if (c->coll.iz_cell) {
+            unsigned long long* di = nullptr;
+            e = cudaMalloc(&di, sizeof(unsigned long long) * cases);
+            if (e == cudaSuccess) {
+                case_sum_kernel<<<cases, 256, 0, c->stream>>>(c->coll.iz_cell, cpc, di);
+                e = cudaMemcpyAsync(ionisations, di, sizeof(int64_t) * cases, cudaMemcpyDeviceToHost, c->stream);
+                cudaStreamSynchronize(c->stream);
+                cudaFree(di);
+            }
+        } else {
+            for (int k = 0; k < cases; ++k) ionisations[k] = 0;
+        }
+    }
+    if (e == cudaSuccess) e = cudaStreamSynchronize(c->stream);
+    cudaFree(d);
+    CK(e);
+    return PICGPU_OK;
+}
+
+picgpu_status picgpu_step_graph(picgpu_ctx* c, int nsteps, int steps_per_graph, picgpu_step_stats* stats) {
+    if (!c || nsteps < 0 || steps_per_graph <= 0 || nsteps % steps_per_graph) return PICGPU_INVALID_ARG;
+    if (!c->mixed || c->cfg.maxwell_solver != PICGPU_MAXWELL_NONE)
+        return bad(c, PICGPU_NOT_SUPPORTED, "graph steps need the FP32 form and MaxwellSolver none");
+    if (stats) *stats = picgpu_step_stats{};
+    int replays = nsteps / steps_per_graph;
+    picgpu_status s;
+    if (!c->tuned && replays > 0) {
+        // autotune on live steps (the physics does not depend on the launch
+        // shape: per-particle moves, integer deposits, per-cell collisions):
+        // two replays per candidate, the second one timed
+        const int bps_cand[] = {3, 4, 5, 6, 8};
+        const int mcc_cand[] = {64, 128, 256};
+        c->tune_ms.clear();
+        int best_bps = c->move_bps, best_mcc = c->coll.mcc_block;
+        double best = 1e30;
+        for (int b : bps_cand) {
+            if (replays < 2) break;
+            c->move_bps = b;
+            float ms = 0.f;
+            if ((s = graph_replay(c, steps_per_graph, stats, nullptr)) || (s = graph_replay(c, steps_per_graph, stats, &ms)))
+                return s;
+            replays -= 2;
+            c->tune_ms.push_back(ms / steps_per_graph);
+            if (ms < best) { best = ms; best_bps = b; }
+        }
+        c->move_bps = best_bps;
+        if (any_collisions(c) && c->cfg.mcc.enabled) {
+            best = 1e30;
+            for (int b : mcc_cand) {
+                if (replays < 2) break;
+                c->coll.mcc_block = b;
+                float ms = 0.f;
+                if ((s = graph_replay(c, steps_per_graph, stats, nullptr)) ||
+                    (s = graph_replay(c, steps_per_graph, stats, &ms)))
+                    return s;
+                replays -= 2;
+                c->tune_ms.push_back(ms / steps_per_graph);
+                if (ms < best) { best = ms; best_mcc = b; }
+            }
+            c->coll.mcc_block = best_mcc;
+        }
+        c->tuned = true;
+    }
+    for (int r = 0; r < replays; ++r)
+        if ((s = graph_replay(c, steps_per_graph, stats, nullptr))) return s;
+    if (c->profiling) harvest_events(c);
+    fill_counts(c, stats);
+    return PICGPU_OK;
+}
+
+picgpu_status picgpu_graph_tuning(picgpu_ctx* c, int* move_blocks_per_sm, int* mcc_block, double* times,
+                                  int n_times) {
+    if (!c) return PICGPU_INVALID_ARG;
+    if (move_blocks_per_sm) *move_blocks_per_sm = c->move_bps;
+    if (mcc_block) *mcc_block = c->coll.mcc_block;
+    for (int k = 0; times && k < n_times; ++k) times[k] = k < int(c->tune_ms.size()) ? c->tune_ms[k] : 0.0;
     return PICGPU_OK;
 }
 

@@ -273,8 +273,17 @@ __global__ void __launch_bounds__(256, 5) move_kernel_fp32(MoveParams P, int chu
         for (int k = threadIdx.x; k < int(sizeof(Tables32) / 4); k += blockDim.x) dst[k] = src[k];
         for (int k = threadIdx.x; k < kWindow * 9; k += blockDim.x) win[k] = 0ull;
     }
-    const int start = P.first + blockIdx.x * chunk;
-    const int end = min(P.n, start + chunk);
+    int n_end = P.n, first = P.first, ch = chunk;
+    if (P.n_dev) {
+        // counts live on the device: split [first, n) over the grid here
+        n_end = *P.n_dev;
+        first = P.first_dev ? *P.first_dev : 0;
+        const long tiles = (long(n_end) - first + 255) / 256;
+        ch = int(((tiles + gridDim.x - 1) / gridDim.x) * 256);
+        if (ch <= 0) ch = 256;
+    }
+    const int start = first + blockIdx.x * ch;
+    const int end = min(n_end, start + ch);
     __shared__ int w0s;
     if (threadIdx.x == 0) {
         int c0 = 0;
@@ -348,14 +357,22 @@ __global__ void __launch_bounds__(256, 5) move_kernel_fp32(MoveParams P, int chu
 cudaError_t move_fp32_set_tables(const Tables32& t) { return cudaMemcpyToSymbol(c_t32, &t, sizeof t); }
 
 // grid: the number of resident blocks to use (5 per SM); each block takes one
-// contiguous chunk (a multiple of 256 particles) of [P.first, P.n).
+// contiguous chunk (a multiple of 256 particles) of [P.first, P.n).  With
+// P.n_dev set the counts are read on the device and all grid blocks launch.
 void launch_move_fp32(const MoveParams& P, int grid, cudaStream_t s) {
-    const long work = long(P.n) - P.first;
-    if (work <= 0) return;
-    const long tiles = (work + 255) / 256;
-    const long per = (tiles + grid - 1) / grid;
-    const int chunk = int(per * 256);
-    const int blocks = int((work + chunk - 1) / chunk);
+    int blocks, chunk;
+    if (P.n_dev) {
+        // device-resident counts: the kernel sizes its chunks; grid fixed
+        blocks = grid;
+        chunk = 0;
+    } else {
+        const long work = long(P.n) - P.first;
+        if (work <= 0) return;
+        const long tiles = (work + 255) / 256;
+        const long per = (tiles + grid - 1) / grid;
+        chunk = int(per * 256);
+        blocks = int((work + chunk - 1) / chunk);
+    }
     const size_t smem = size_t(kWindow) * 9 * sizeof(unsigned long long);
     switch (P.pusher) {
         case PICGPU_PUSHER_BORIS:

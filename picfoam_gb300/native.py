@@ -94,6 +94,16 @@ def load():
     F32P = C.POINTER(C.c_float)
     lib.picgpu_test_conv3d.restype = i
     lib.picgpu_test_conv3d.argtypes = [i, i, i, i, i, i, i, i, U16P, U16P, U16P, F32P]
+    lib.picgpu_ensemble_create.restype = i
+    lib.picgpu_ensemble_create.argtypes = [C.POINTER(abi.MeshDesc), i, C.POINTER(abi.Config), PP]
+    lib.picgpu_ensemble_set_efield.restype = i
+    lib.picgpu_ensemble_set_efield.argtypes = [P, F64P]
+    lib.picgpu_ensemble_case_stats.restype = i
+    lib.picgpu_ensemble_case_stats.argtypes = [P, i, F64P, I64P]
+    lib.picgpu_step_graph.restype = i
+    lib.picgpu_step_graph.argtypes = [P, i, i, C.POINTER(abi.StepStats)]
+    lib.picgpu_graph_tuning.restype = i
+    lib.picgpu_graph_tuning.argtypes = [P, C.POINTER(C.c_int), C.POINTER(C.c_int), F64P, i]
     lib.picgpu_unet_param_count.restype = C.c_size_t
     lib.picgpu_unet_param_count.argtypes = []
     lib.picgpu_unet_create.restype = i

@@ -33,6 +33,21 @@ class GpuBackend:
         return st, h
 
 
+class EnsembleBackend(GpuBackend):
+    """libpicgpu.so with n_cases disjoint copies of the mesh in one context
+    (picgpu_ensemble_create)."""
+    name = "gpu-ensemble"
+
+    def __init__(self, n_cases):
+        super().__init__()
+        self.n_cases = n_cases
+
+    def create(self, mesh, cfg):
+        h = C.c_void_p()
+        st = self.lib.picgpu_ensemble_create(C.byref(mesh), self.n_cases, C.byref(cfg), C.byref(h))
+        return st, h
+
+
 def _f64(a):
     a = np.ascontiguousarray(a, dtype=np.float64)
     return a, a.ctypes.data_as(C.POINTER(C.c_double))
@@ -124,6 +139,33 @@ class Simulation:
         s = abi.StepStats()
         self._check(self._fn("step")(self._h, n, C.byref(s)))
         return s
+
+    def step_graph(self, n, steps_per_graph):
+        """n steps as CUDA-graph replays of steps_per_graph steps (FP32 form,
+        MaxwellSolver none); the first call tunes the launch shapes."""
+        s = abi.StepStats()
+        self._check(self.lib.picgpu_step_graph(self._h, n, steps_per_graph, C.byref(s)))
+        return s
+
+    def graph_tuning(self, n_times=16):
+        bps, blk = C.c_int(), C.c_int()
+        t = np.zeros(n_times)
+        self._check(self.lib.picgpu_graph_tuning(self._h, C.byref(bps), C.byref(blk),
+                                                 t.ctypes.data_as(C.POINTER(C.c_double)), n_times))
+        return bps.value, blk.value, t
+
+    def set_case_efield(self, E):
+        """Applied field per case of an ensemble, E[n_cases][3]."""
+        e, ep = _f64(np.reshape(E, (-1, 3)))
+        self._check(self.lib.picgpu_ensemble_set_efield(self._h, ep))
+
+    def case_stats(self, species, n_cases):
+        """Per case: count, sum U (3), sum |U|^2, and MCC ionisations."""
+        out = np.zeros((n_cases, 5))
+        iz = np.zeros(n_cases, np.int64)
+        self._check(self.lib.picgpu_ensemble_case_stats(self._h, species, out.ctypes.data_as(C.POINTER(C.c_double)),
+                                                        iz.ctypes.data_as(C.POINTER(C.c_int64))))
+        return out, iz
 
     def move(self):
         s = abi.StepStats()
