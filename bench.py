@@ -49,6 +49,18 @@ def parse():
     p.add_argument("--poisson-steps", type=int, default=3)
     p.add_argument("--sort-interval", type=int, default=10,
                    help="re-sort the particle store into cell order every N steps (0: never)")
+    p.add_argument("--no-learned", action="store_true", help="skip the Poisson learned-vs-plain comparison")
+    p.add_argument("--ws-cells", type=int, default=128)
+    p.add_argument("--ws-ppc", type=int, default=4)
+    p.add_argument("--ws-train", type=int, default=100)
+    p.add_argument("--ws-iters", type=int, default=4)
+    p.add_argument("--ws-refine", type=int, default=1)
+    p.add_argument("--ws-measure", type=int, default=10)
+    p.add_argument("--no-ensemble", action="store_true", help="skip the batched-ensemble measurement")
+    p.add_argument("--ens-cases", type=int, default=64)
+    p.add_argument("--ens-steps", type=int, default=100)
+    p.add_argument("--ens-graph", type=int, default=10)
+    p.add_argument("--ens-seq-steps", type=int, default=20)
     return p.parse_args()
 
 
@@ -218,6 +230,120 @@ def run_reference(args, rank, ws):
     return 0
 
 
+def learned_vs_plain(args):
+    """Poisson ms/step and PCG iterations on the electrode geometry (128^3
+    cells, two floating boxes, a 100 V box, PCG to 1e-8): previous-potential
+    start against the learned warm start after its training solves."""
+    import numpy as np
+    from picfoam_gb300 import cases
+    out = {}
+    for mode in ("plain", "learned"):
+        case = cases.electrode_box(n_cells=args.ws_cells, per_cell=args.ws_ppc)
+        if mode == "learned":
+            case.cfg.learned.enabled = 1
+            case.cfg.learned.train_steps = args.ws_train
+            case.cfg.learned.train_iters = args.ws_iters
+            case.cfg.learned.refine = args.ws_refine
+            case.cfg.learned.lr = 2e-3
+        sim = cases.build(case)
+        sim.set_profiling(True)
+        t0 = time.perf_counter()
+        pre = args.ws_train + 2 if mode == "learned" else 3
+        last = None
+        for _ in range(pre):
+            last = sim.step(1)
+        t_train = time.perf_counter() - t0
+        sim.phase_times(reset=True)
+        its, r0, rp, alpha = [], [], [], []
+        for _ in range(args.ws_measure):
+            st = sim.step(1)
+            its.append(st.pcg_iterations)
+            r0.append(st.pcg_residual_initial)
+            rp.append(st.learned_residual)
+            alpha.append(st.learned_alpha)
+        ph = sim.phase_times()
+        d = {"poisson_ms_per_step": ph["poisson"][0] / args.ws_measure,
+             "pcg_iterations_per_step": float(np.mean(its)),
+             "start_residual": float(np.mean(r0))}
+        if mode == "learned":
+            d.update({"previous_potential_residual": float(np.mean(rp)), "line_search_alpha": float(np.mean(alpha)),
+                      "training_solves": args.ws_train, "adam_steps_per_solve": args.ws_iters,
+                      "refine_passes": args.ws_refine, "final_training_loss": last.learned_loss,
+                      "training_wall_s": t_train, "active": bool(st.learned_active)})
+        out[mode] = d
+        sim.close()
+    out["iteration_ratio_plain_over_learned"] = (out["plain"]["pcg_iterations_per_step"] /
+                                                 max(out["learned"]["pcg_iterations_per_step"], 1e-9))
+    out["ms_ratio_plain_over_learned"] = (out["plain"]["poisson_ms_per_step"] /
+                                          max(out["learned"]["poisson_ms_per_step"], 1e-9))
+    out["config"] = (f"{args.ws_cells}^3 cells, 0.1 m cube, two floating 8^3-cell boxes and a 100 V box, "
+                     f"e- + Ar+ at {args.ws_ppc}/cell, FP64 Jacobi PCG (Chronopoulos-Gear) to 1e-8 relative residual, "
+                     f"{args.ws_measure} measured steps")
+    return out
+
+
+def ensemble(args):
+    """Batched swarm ensemble (64 cases of 16x16x128 cells, 10-1000 Td,
+    1e5-4e6 electrons each from seed 7): one context, CUDA-graph steps with
+    tuned launch shapes, against the same cases run one after another."""
+    import numpy as np
+    from picfoam_gb300 import cases
+    case = cases.swarm_ensemble(n_cases=args.ens_cases)
+    sim = cases.build_ensemble(case)
+    S = args.ens_graph
+    # tuning replays (live steps) then warm-up
+    sim.step_graph(32 * S, S)
+    bps, blk, tune = sim.graph_tuning()
+    n0 = sim.count(0) + sim.count(1)
+    sim.synchronize()
+    sim.timer_start()
+    st = sim.step_graph(args.ens_steps, S)
+    ms = sim.timer_stop()
+    n1 = sim.count(0) + sim.count(1)
+    batched = 0.5 * (n0 + n1) * args.ens_steps / (ms * 1e-3)
+    out, iz = sim.case_stats(0, args.ens_cases)
+    dt = case.meta["dt"]
+    steps_total = sim_steps = 32 * S + args.ens_steps
+    drift = out[:, 3] / np.maximum(out[:, 0], 1)
+    sim.close()
+    # the same cases one after another, each in its own context (regular steps)
+    seq_ps, seq_s = 0, 0.0
+    counts = case.meta["counts"]
+    tet, bary, U = case.particles[0]
+    cpc = case.meta["cells_per_case"]
+    case_of = (tet // 12) // cpc
+    from picfoam_gb300.simulation import Simulation
+    for k in range(args.ens_cases):
+        sel = case_of == k
+        cfg = case.cfg
+        cfg.E_applied[2] = case.meta["E"][k, 2]
+        s1 = Simulation(case.mesh, cfg, keepalive=case.keepalive)
+        s1.set_particles(0, tet[sel] - 12 * cpc * k, bary[sel], U[sel])
+        s1.set_particles(1, np.zeros(0, np.int32), np.zeros((0, 3)), np.zeros((0, 3)))
+        s1.step(2)
+        s1.synchronize()
+        s1.timer_start()
+        for _ in range(args.ens_seq_steps):
+            seq_ps += s1.count(0) + s1.count(1)
+            s1.step(1)
+        seq_s += s1.timer_stop() * 1e-3
+        s1.close()
+    sequential = seq_ps / seq_s
+    return {"config": f"{args.ens_cases} cases of 16x16x128 cells (0.01x0.01x0.08 m), E/N 10-1000 Td at 1e21 m^-3, "
+                      f"1e5-4e6 e- per case (seed 7, {int(counts.sum())} total), NanbuElectronNeutral MCC with "
+                      f"ionisation, FP32 push, MaxwellSolver none",
+            "batched_particle_steps_per_s": batched, "sequential_particle_steps_per_s": sequential,
+            "speedup": batched / sequential, "steps_per_graph": S, "timed_steps": args.ens_steps,
+            "ms_per_step": ms / args.ens_steps,
+            "tuning": {"move_blocks_per_sm": bps, "mcc_block": blk,
+                       "candidate_ns_per_particle_step": [float(x) for x in tune if x > 0]},
+            "per_case_drift_velocity_mps": [float(x) for x in drift],
+            "per_case_ionisation_rate_per_s": [float(iz[k]) / max(out[k, 0], 1) / (steps_total * dt)
+                                               for k in range(args.ens_cases)],
+            "per_case_EN_Td": [float(x) for x in case.meta["EN_Td"]],
+            "ionisations": int(st.mcc_ionization)}
+
+
 def run_ours(args, rank, ws):
     import numpy as np
     from picfoam_gb300 import abi, cases
@@ -314,6 +440,16 @@ def run_ours(args, rank, ws):
             "particles": counts}
     if e2e:
         line["e2e"] = e2e
+    if rank == 0 and ws == 1 and not args.no_learned:
+        try:
+            line["poisson_learned_vs_plain"] = learned_vs_plain(args)
+        except Exception as ex:  # reported, not fatal
+            line["poisson_learned_vs_plain"] = {"error": str(ex)}
+    if rank == 0 and ws == 1 and not args.no_ensemble:
+        try:
+            line["ensemble"] = ensemble(args)
+        except Exception as ex:  # reported, not fatal
+            line["ensemble"] = {"error": str(ex)}
     if rank == 0 and ws == 1 and not args.no_cpu_baseline:
         try:
             line["cpu_baseline"] = cpu_baseline(args)

@@ -35,7 +35,7 @@ picgpu_status picgpu_ensemble_case_stats(picgpu_ctx* ctx, int species, double* o
  * picgpu_graph_tuning) on its first replays. */
 picgpu_status picgpu_step_graph(picgpu_ctx* ctx, int nsteps, int steps_per_graph, picgpu_step_stats* stats);
 /* The launch shapes chosen by the tuner: move blocks per SM, MCC threads
- * per block, and the measured ms per step of each candidate tried
+ * per block, and the measured ns per particle-step of each candidate tried
  * (times[n_times], move candidates first). */
 picgpu_status picgpu_graph_tuning(picgpu_ctx* ctx, int* move_blocks_per_sm, int* mcc_block, double* times,
                                   int n_times);

@@ -446,6 +446,7 @@ def swarm_ensemble(n_cases=64, n=(16, 16, 128), size=(0.01, 0.01, 0.08), counts=
     one = electron_swarm(nx=n[0], ny=n[1], nz=n[2], N=1, Ez=0.0, gas_density=gas_density, T_gas=T_gas, T_e=T_e,
                          seed=seed, precision=abi.PREC_MIXED, ion_species=ion_species, size=size, dt=dt)
     cfg = one.cfg
+    cfg.sort_interval = 20  # keep the store in cell order (deposit locality)
     cpc = n[0] * n[1] * n[2]
     if counts is None:
         r = np.random.Generator(np.random.Philox(count_seed))

@@ -118,6 +118,7 @@ struct picgpu_ctx {
     };
     std::vector<GraphEntry> graphs;
     uint64_t graph_sig = 0;        // signature of the buffers the cached graphs address
+    cudaEvent_t replay_ev[2] = {nullptr, nullptr};  // the tuner's replay timing (not the user timer)
     int move_bps = 5;              // FP32 move kernel: blocks per SM
     bool tuned = false;
     std::vector<double> tune_ms;
@@ -713,6 +714,12 @@ __global__ void case_sum_kernel(const unsigned long long* __restrict__ per_cell,
     if (threadIdx.x == 0) out[blockIdx.x] = s[0];
 }
 
+long total_particles(const picgpu_ctx* c) {
+    long n = 0;
+    for (int k = 0; k < c->cfg.n_species; ++k) n += c->sp[k].alive;
+    return n;
+}
+
 bool any_collisions(const picgpu_ctx* c) {
     return c->cfg.mcc.enabled || c->cfg.coulomb.enabled || c->cfg.ion_mcc.enabled;
 }
@@ -892,15 +899,15 @@ picgpu_status graph_replay(picgpu_ctx* c, int steps, picgpu_step_stats* stats, f
     }
     cudaGraphExec_t g;
     if ((s = graph_for(c, steps, &g))) return s;
-    if (!c->timer[0]) {
-        CK(cudaEventCreate(&c->timer[0]));
-        CK(cudaEventCreate(&c->timer[1]));
+    if (!c->replay_ev[0]) {
+        CK(cudaEventCreate(&c->replay_ev[0]));
+        CK(cudaEventCreate(&c->replay_ev[1]));
     }
     {
         PhaseScope ps(c, PICGPU_PHASE_MOVE);
-        CK(cudaEventRecord(c->timer[0], c->stream));
+        CK(cudaEventRecord(c->replay_ev[0], c->stream));
         CK(cudaGraphLaunch(g, c->stream));
-        CK(cudaEventRecord(c->timer[1], c->stream));
+        CK(cudaEventRecord(c->replay_ev[1], c->stream));
     }
     if ((s = read_counters(c))) return s;
     int nd[PICGPU_MAX_SPECIES] = {};
@@ -912,7 +919,7 @@ picgpu_status graph_replay(picgpu_ctx* c, int steps, picgpu_step_stats* stats, f
         CK(cudaMemcpyAsync(h, c->coll.counts, sizeof h, cudaMemcpyDeviceToHost, c->stream));
     }
     CK(cudaStreamSynchronize(c->stream));
-    if (ms) CK(cudaEventElapsedTime(ms, c->timer[0], c->timer[1]));
+    if (ms) CK(cudaEventElapsedTime(ms, c->replay_ev[0], c->replay_ev[1]));
     int err = 0;
     for (int k = 0; k < c->cfg.n_species; ++k) err = std::max(err, c->counters_host[k].error);
     if (err)
@@ -1235,6 +1242,7 @@ void picgpu_destroy(picgpu_ctx* c) {
     if (c->timer[0]) { cudaEventDestroy(c->timer[0]); cudaEventDestroy(c->timer[1]); }
     if (c->pcg_graph) cudaGraphExecDestroy(c->pcg_graph);
     for (auto& g : c->graphs) cudaGraphExecDestroy(g.exec);
+    if (c->replay_ev[0]) { cudaEventDestroy(c->replay_ev[0]); cudaEventDestroy(c->replay_ev[1]); }
     if (c->st_host) cudaFreeHost(c->st_host);
     if (c->counters_host) cudaFreeHost(c->counters_host);
     if (c->stream) cudaStreamDestroy(c->stream);
@@ -1594,7 +1602,8 @@ picgpu_status picgpu_step_graph(picgpu_ctx* c, int nsteps, int steps_per_graph, 
     if (!c->tuned && replays > 0) {
         // autotune on live steps (the physics does not depend on the launch
         // shape: per-particle moves, integer deposits, per-cell collisions):
-        // two replays per candidate, the second one timed
+        // two replays per candidate, the second one timed and normalised by
+        // the particles it moved (the population changes while tuning)
         const int bps_cand[] = {3, 4, 5, 6, 8};
         const int mcc_cand[] = {64, 128, 256};
         c->tune_ms.clear();
@@ -1604,11 +1613,13 @@ picgpu_status picgpu_step_graph(picgpu_ctx* c, int nsteps, int steps_per_graph, 
             if (replays < 2) break;
             c->move_bps = b;
             float ms = 0.f;
-            if ((s = graph_replay(c, steps_per_graph, stats, nullptr)) || (s = graph_replay(c, steps_per_graph, stats, &ms)))
-                return s;
+            if ((s = graph_replay(c, steps_per_graph, stats, nullptr))) return s;
+            const double n0 = double(total_particles(c));
+            if ((s = graph_replay(c, steps_per_graph, stats, &ms))) return s;
+            const double per = ms / (0.5 * (n0 + double(total_particles(c))) * steps_per_graph + 1.0);
             replays -= 2;
-            c->tune_ms.push_back(ms / steps_per_graph);
-            if (ms < best) { best = ms; best_bps = b; }
+            c->tune_ms.push_back(1e6 * per);
+            if (per < best) { best = per; best_bps = b; }
         }
         c->move_bps = best_bps;
         if (any_collisions(c) && c->cfg.mcc.enabled) {
@@ -1617,12 +1628,13 @@ picgpu_status picgpu_step_graph(picgpu_ctx* c, int nsteps, int steps_per_graph, 
                 if (replays < 2) break;
                 c->coll.mcc_block = b;
                 float ms = 0.f;
-                if ((s = graph_replay(c, steps_per_graph, stats, nullptr)) ||
-                    (s = graph_replay(c, steps_per_graph, stats, &ms)))
-                    return s;
+                if ((s = graph_replay(c, steps_per_graph, stats, nullptr))) return s;
+                const double n0 = double(total_particles(c));
+                if ((s = graph_replay(c, steps_per_graph, stats, &ms))) return s;
+                const double per = ms / (0.5 * (n0 + double(total_particles(c))) * steps_per_graph + 1.0);
                 replays -= 2;
-                c->tune_ms.push_back(ms / steps_per_graph);
-                if (ms < best) { best = ms; best_mcc = b; }
+                c->tune_ms.push_back(1e6 * per);
+                if (per < best) { best = per; best_mcc = b; }
             }
             c->coll.mcc_block = best_mcc;
         }
