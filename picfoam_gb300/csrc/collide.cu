@@ -148,22 +148,35 @@ __global__ void scatter_cells_kernel(const int32_t* __restrict__ tet, int n, con
     }
 }
 
-// Order every cell's list by particle index (insertion sort; lists are short).
-__global__ void order_cells_kernel(int n_cells, const int* __restrict__ start, int* __restrict__ idx) {
-    const int c = blockIdx.x * blockDim.x + threadIdx.x;
-    if (c >= n_cells) return;
-    int* a = idx + start[c];
-    const int L = start[c + 1] - start[c];
-    for (int k = 1; k < L; ++k) {
-        const int v = a[k];
-        int j = k - 1;
-        while (j >= 0 && a[j] > v) {
-            a[j + 1] = a[j];
-            --j;
+// Order every cell's list by particle index: one warp per cell; each lane
+// ranks its element against the whole list through shuffles (indices are
+// distinct), writes it to its rank in tmp, and the warp copies the list back.
+__global__ void order_cells_kernel(int n_cells, const int* __restrict__ start, int* __restrict__ idx,
+                                   int* __restrict__ tmp) {
+    const int cell = int((long(blockIdx.x) * blockDim.x + threadIdx.x) >> 5);
+    const int lane = threadIdx.x & 31;
+    if (cell >= n_cells) return;
+    const int s0 = start[cell];
+    const int L = start[cell + 1] - s0;
+    if (L <= 1) return;
+    int* a = idx + s0;
+    int* t = tmp + s0;
+    for (int base = 0; base < L; base += 32) {
+        const int i = base + lane;
+        const int v = i < L ? a[i] : 0x7fffffff;
+        int rank = 0;
+        for (int cb = 0; cb < L; cb += 32) {
+            const int w = cb + lane < L ? a[cb + lane] : 0x7fffffff;
+            const int m = min(32, L - cb);
+            for (int k = 0; k < m; ++k) rank += __shfl_sync(0xffffffffu, w, k) < v ? 1 : 0;
         }
-        a[j + 1] = v;
+        if (i < L) t[rank] = v;
     }
+    __syncwarp();
+    for (int i = lane; i < L; i += 32) a[i] = t[i];
 }
+
+unsigned order_blocks(int n_cells) { return unsigned((long(n_cells) * 32 + 255) / 256); }
 
 // ------------------------------------------------------------- Philox ---
 struct Rng {
@@ -1124,7 +1137,7 @@ int occupancy(CollideState& st, const CollideArgs& a, int s, std::string* msg, i
                                                                     st.idx[s]);
         *launches += 1;
         if (ordered) {
-            order_cells_kernel<<<(nc + 127) / 128, 128, 0, a.stream>>>(nc, start, st.idx[s]);
+            order_cells_kernel<<<order_blocks(nc), 256, 0, a.stream>>>(nc, start, st.idx[s], st.sel[s]);
             *launches += 1;
         }
     }
@@ -1456,7 +1469,7 @@ int run_collisions_device(CollideState& st, const CollideArgs& a, int* n_dev, in
         exclusive_scan(cnt, start, nc, st.scan_tmp, a.stream, launches);
         scatter_cells_kernel<<<grid_of(cap, 256), 256, 0, a.stream>>>(a.sp[s].tet, int(cap), start, st.cell_cursor,
                                                                       st.idx[s], n_dev + s);
-        order_cells_kernel<<<(nc + 127) / 128, 128, 0, a.stream>>>(nc, start, st.idx[s]);
+        order_cells_kernel<<<order_blocks(nc), 256, 0, a.stream>>>(nc, start, st.idx[s], st.sel[s]);
         *launches += 3;
     }
     if (cfg.coulomb.enabled) {

@@ -122,7 +122,7 @@ struct picgpu_ctx {
     int move_bps = 5;              // FP32 move kernel: blocks per SM
     bool tuned = false;
     std::vector<double> tune_ms;
-    long long last_sort = 0;
+    long long last_sort = -(1LL << 40);  // graph steps re-sort on their first replay
 };
 
 picgpu_status pgd_collisions(picgpu_ctx* c, picgpu_step_stats* stats);

@@ -267,12 +267,6 @@ template <int PUSHER>
 __global__ void __launch_bounds__(256, 5) move_kernel_fp32(MoveParams P, int chunk) {
     __shared__ Tables32 T;
     extern __shared__ unsigned long long win[];  // kWindow * 9 slots
-    {
-        const unsigned* src = reinterpret_cast<const unsigned*>(&c_t32);
-        unsigned* dst = reinterpret_cast<unsigned*>(&T);
-        for (int k = threadIdx.x; k < int(sizeof(Tables32) / 4); k += blockDim.x) dst[k] = src[k];
-        for (int k = threadIdx.x; k < kWindow * 9; k += blockDim.x) win[k] = 0ull;
-    }
     int n_end = P.n, first = P.first, ch = chunk;
     if (P.n_dev) {
         // counts live on the device: split [first, n) over the grid here
@@ -284,6 +278,13 @@ __global__ void __launch_bounds__(256, 5) move_kernel_fp32(MoveParams P, int chu
     }
     const int start = first + blockIdx.x * ch;
     const int end = min(n_end, start + ch);
+    if (start >= end) return;  // block-uniform: nothing to move (e.g. no secondaries this step)
+    {
+        const unsigned* src = reinterpret_cast<const unsigned*>(&c_t32);
+        unsigned* dst = reinterpret_cast<unsigned*>(&T);
+        for (int k = threadIdx.x; k < int(sizeof(Tables32) / 4); k += blockDim.x) dst[k] = src[k];
+        for (int k = threadIdx.x; k < kWindow * 9; k += blockDim.x) win[k] = 0ull;
+    }
     __shared__ int w0s;
     if (threadIdx.x == 0) {
         int c0 = 0;
