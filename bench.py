@@ -61,6 +61,11 @@ def parse():
     p.add_argument("--ens-steps", type=int, default=100)
     p.add_argument("--ens-graph", type=int, default=10)
     p.add_argument("--ens-seq-steps", type=int, default=20)
+    p.add_argument("--only", default=None, choices=["electrode", "unet", "ensemble"],
+                   help="profiling drivers: run one workload briefly and print a short summary "
+                        "(electrode: electrode_box steps; unet: one forward + train steps; "
+                        "ensemble: two graph replays)")
+    p.add_argument("--only-steps", type=int, default=2)
     return p.parse_args()
 
 
@@ -460,8 +465,49 @@ def run_ours(args, rank, ws):
     return 0
 
 
+def run_only(args):
+    """Short runs of one workload for ncu captures (no timing claims)."""
+    import ctypes as C
+    import numpy as np
+    from picfoam_gb300 import cases, native
+    if args.only == "electrode":
+        case = cases.electrode_box(n_cells=args.ws_cells, per_cell=args.ws_ppc)
+        sim = cases.build(case)
+        for _ in range(args.only_steps):
+            st = sim.step(1)
+        print(json.dumps({"only": "electrode", "cells": args.ws_cells ** 3, "pcg_iterations": st.pcg_iterations}))
+    elif args.only == "unet":
+        lib = native.load()
+        n = args.ws_cells
+        V = n ** 3
+        h = C.c_void_p()
+        assert lib.picgpu_unet_create(n, n, n, 3, C.byref(h)) == 0
+        rng = np.random.default_rng(0)
+        x = np.zeros((V, 2), np.float32)
+        x[:, 0] = rng.standard_normal(V)
+        x[:, 1] = 1.0
+        t = rng.standard_normal(V).astype(np.float32)
+        m = np.ones(V, np.float32)
+        out = np.zeros(V, np.float32)
+        p = lambda a: a.ctypes.data_as(C.POINTER(C.c_float))
+        assert lib.picgpu_unet_forward(h, p(x), p(out)) == 0
+        loss = C.c_double()
+        assert lib.picgpu_unet_train(h, p(x), p(t), p(m), args.only_steps, 1e-3, C.byref(loss)) == 0
+        lib.picgpu_unet_destroy(h)
+        print(json.dumps({"only": "unet", "grid": n, "loss": loss.value}))
+    else:
+        case = cases.swarm_ensemble(n_cases=args.ens_cases)
+        sim = cases.build_ensemble(case)
+        sim.step_graph(10, 10)
+        sim.step_graph(10, 10)
+        print(json.dumps({"only": "ensemble", "cases": args.ens_cases, "particles": sim.count(0)}))
+    return 0
+
+
 def main():
     args = parse()
+    if args.only:
+        return run_only(args)
     rank, ws = dist()
     if args.impl == "reference":
         return run_reference(args, rank, ws)
