@@ -122,15 +122,32 @@ struct Tally {
     bool keep;
 };
 
+// The push of PICParcel::move (once per step, before tracking); false when
+// the particle reached the speed of light (it is then removed).
 template <int PUSHER>
-__device__ __forceinline__ void move32(const MoveParams& P, const Tables32& T, S32& s, Tally& td) {
-    const float dt = P.dt_f;
-    if (P.charged) push32<PUSHER>(P, T, s, dt);
+__device__ __forceinline__ bool push_phase(const MoveParams& P, const Tables32& T, S32& s, Tally& td) {
+    if (P.charged) push32<PUSHER>(P, T, s, P.dt_f);
     if (!(s.U[0] * s.U[0] + s.U[1] * s.U[1] + s.U[2] * s.U[2] < float(kC) * float(kC))) {
         td.keep = false;
         atomicMax(&P.counters->error, int(PICGPU_SPEED_OF_LIGHT));
-        return;
+        return false;
     }
+    return true;
+}
+
+template <int PUSHER>
+__device__ __forceinline__ void track32(const MoveParams& P, const Tables32& T, S32& s, Tally& td);
+
+template <int PUSHER>
+__device__ __forceinline__ void move32(const MoveParams& P, const Tables32& T, S32& s, Tally& td) {
+    if (!push_phase<PUSHER>(P, T, s, td)) return;
+    track32<PUSHER>(P, T, s, td);
+}
+
+// Tracking of one time step after the push (PICParcel::moveForward).
+template <int PUSHER>
+__device__ __forceinline__ void track32(const MoveParams& P, const Tables32& T, S32& s, Tally& td) {
+    const float dt = P.dt_f;
     float disp[3];
     displacement(P, T, s, dt, disp);
     float rem = 1.f;     // unused fraction of disp
@@ -352,6 +369,8 @@ __global__ void __launch_bounds__(256, 5) move_kernel_fp32(MoveParams P, int chu
     warp_add_counter<float>(&P.counters->walls, wl);
     warp_add_counter<float>(&P.counters->absorbed, ab);
 }
+
+
 
 }  // namespace
 
