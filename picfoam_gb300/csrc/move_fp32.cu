@@ -239,25 +239,40 @@ __device__ __forceinline__ void track32(const MoveParams& P, const Tables32& T, 
 // Deposit into the block's shared-memory window of cells [w0, w0 + kWindow)
 // (the store is kept in cell order, so a block's contiguous chunk of
 // particles covers a short cell range); particles outside the window go
-// straight to the global accumulators.
-constexpr int kWindow = 512;
+// straight to the global accumulators.  Window slots are 32-bit: an add that
+// wraps carries 2^32 into the cell's 64-bit global slot, so the integer sums
+// stay exact.
+constexpr int kWindow = 1024;
+
+__device__ __forceinline__ void win_add(unsigned* slot, unsigned long long* gslot, unsigned v) {
+    const unsigned old = atomicAdd(slot, v);
+    if (old + v < old) atomicAdd(gslot, 1ull << 32);
+}
 
 __device__ __forceinline__ void deposit32(const MoveParams& P, const Tables32& T, const S32& s, int w0,
-                                          unsigned long long* win) {
+                                          unsigned* win) {
     if (!P.has_value) return;
     constexpr float kScale = float(1u << kDepositBits);
     const int rel = s.cell - w0;
-    const bool local = unsigned(rel) < unsigned(kWindow);
-    unsigned long long* a = local ? win + 9 * rel : P.acc9 + 9 * size_t(s.cell);
-    if (P.charge_distribution == PICGPU_WEIGHTING_CELL_AVERAGE) {
-        atomicAdd(a, 1ull << kDepositBits);
+    unsigned long long* g = P.acc9 + 9 * size_t(s.cell);
+    const bool average = P.charge_distribution == PICGPU_WEIGHTING_CELL_AVERAGE;
+    const unsigned tri = T.tri[s.tet];
+    const unsigned w0v = average ? (1u << kDepositBits) : __float2uint_rn(s.y[0] * kScale);
+    if (unsigned(rel) < unsigned(kWindow)) {
+        unsigned* a = win + 9 * rel;
+        win_add(a, g, w0v);
+        if (average) return;
+        const unsigned k1 = 1 + (tri & 15u), k2 = 1 + ((tri >> 4) & 15u), k3 = 1 + ((tri >> 8) & 15u);
+        win_add(a + k1, g + k1, __float2uint_rn(s.y[1] * kScale));
+        win_add(a + k2, g + k2, __float2uint_rn(s.y[2] * kScale));
+        win_add(a + k3, g + k3, __float2uint_rn(s.y[3] * kScale));
         return;
     }
-    const unsigned tri = T.tri[s.tet];
-    atomicAdd(a, (unsigned long long)__float2uint_rn(s.y[0] * kScale));
-    atomicAdd(a + 1 + (tri & 15u), (unsigned long long)__float2uint_rn(s.y[1] * kScale));
-    atomicAdd(a + 1 + ((tri >> 4) & 15u), (unsigned long long)__float2uint_rn(s.y[2] * kScale));
-    atomicAdd(a + 1 + ((tri >> 8) & 15u), (unsigned long long)__float2uint_rn(s.y[3] * kScale));
+    atomicAdd(g, (unsigned long long)w0v);
+    if (average) return;
+    atomicAdd(g + 1 + (tri & 15u), (unsigned long long)__float2uint_rn(s.y[1] * kScale));
+    atomicAdd(g + 1 + ((tri >> 4) & 15u), (unsigned long long)__float2uint_rn(s.y[2] * kScale));
+    atomicAdd(g + 1 + ((tri >> 8) & 15u), (unsigned long long)__float2uint_rn(s.y[3] * kScale));
 }
 
 struct Rec {
@@ -283,7 +298,7 @@ __device__ __forceinline__ Rec load_rec(const DSpecies& p, int i) {
 template <int PUSHER>
 __global__ void __launch_bounds__(256, 5) move_kernel_fp32(MoveParams P, int chunk) {
     __shared__ Tables32 T;
-    extern __shared__ unsigned long long win[];  // kWindow * 9 slots
+    extern __shared__ unsigned win[];  // kWindow * 9 slots (32-bit, carry to global)
     int n_end = P.n, first = P.first, ch = chunk;
     if (P.n_dev) {
         // counts live on the device: split [first, n) over the grid here
@@ -300,7 +315,7 @@ __global__ void __launch_bounds__(256, 5) move_kernel_fp32(MoveParams P, int chu
         const unsigned* src = reinterpret_cast<const unsigned*>(&c_t32);
         unsigned* dst = reinterpret_cast<unsigned*>(&T);
         for (int k = threadIdx.x; k < int(sizeof(Tables32) / 4); k += blockDim.x) dst[k] = src[k];
-        for (int k = threadIdx.x; k < kWindow * 9; k += blockDim.x) win[k] = 0ull;
+        for (int k = threadIdx.x; k < kWindow * 9; k += blockDim.x) win[k] = 0u;
     }
     __shared__ int w0s;
     if (threadIdx.x == 0) {
@@ -360,8 +375,8 @@ __global__ void __launch_bounds__(256, 5) move_kernel_fp32(MoveParams P, int chu
         const int nslot = min(kWindow, P.m.n_cells - w0) * 9;
         unsigned long long* g = P.acc9 + 9 * size_t(w0);
         for (int k = threadIdx.x; k < nslot; k += blockDim.x) {
-            const unsigned long long v = win[k];
-            if (v) atomicAdd(g + k, v);
+            const unsigned v = win[k];
+            if (v) atomicAdd(g + k, (unsigned long long)v);
         }
     }
     warp_add_counter<float>(&P.counters->tet_steps, ts);
@@ -393,7 +408,7 @@ void launch_move_fp32(const MoveParams& P, int grid, cudaStream_t s) {
         chunk = int(per * 256);
         blocks = int((work + chunk - 1) / chunk);
     }
-    const size_t smem = size_t(kWindow) * 9 * sizeof(unsigned long long);
+    const size_t smem = size_t(kWindow) * 9 * sizeof(unsigned);
     switch (P.pusher) {
         case PICGPU_PUSHER_BORIS:
             move_kernel_fp32<PICGPU_PUSHER_BORIS><<<blocks, 256, smem, s>>>(P, chunk);

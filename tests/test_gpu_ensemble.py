@@ -33,6 +33,10 @@ def case_rows(keys, k, cells_per_case):
 
 def test_graph_step_reproduces_regular_step(gpu):
     case = small_ensemble(1, [20000], [3e3])
+    # Re-sorting renumbers particles: two that later meet in one cell can
+    # swap their order in its list, and MCC picks by list position.  The two
+    # paths re-sort at different times, so exact equality needs no re-sort.
+    case.cfg.sort_interval = 0
     # regular context: the same case with a uniform applied field
     case.cfg.E_applied[2] = case.meta["E"][0, 2]
     reg = cases.build(case)
