@@ -192,9 +192,17 @@ def cpu_baseline(args, steps=2):
         sim.move()
     dt = be.move_seconds(sim._h) - t0
     sim.close()
+    # the same sample on one thread (a single picFoam MPI rank's throughput)
+    sim1 = cases.build(case, backend=pyoracle.OracleBackend(1))
+    sim1.initialise_fields()
+    t1 = sim1.backend.move_seconds(sim1._h)
+    sim1.move()
+    dt1 = sim1.backend.move_seconds(sim1._h) - t1
+    sim1.close()
     return {"value": n * steps / dt, "unit": UNIT, "cores": cores, "kind": "port",
-            "sample": f"{args.cells}^3 cells, {ppc}/cell per species ({n} particles), {steps} steps, "
-                      f"FP64 CPU restatement"}
+            "single_thread_value": n / dt1,
+            "sample": f"{args.cells}^3 cells, {ppc}/cell per species ({n} particles), {steps} steps on "
+                      f"{cores} threads (1 step on 1 thread), FP64 CPU restatement"}
 
 
 def run_reference(args, rank, ws):
