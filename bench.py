@@ -283,6 +283,13 @@ def learned_vs_plain(args):
                       "training_solves": args.ws_train, "adam_steps_per_solve": args.ws_iters,
                       "refine_passes": args.ws_refine, "final_training_loss": last.learned_loss,
                       "training_wall_s": t_train, "active": bool(st.learned_active)})
+            # the fallback check closes its first window after 20 net-started solves
+            sim.phase_times(reset=True)
+            for _ in range(max(0, 20 - args.ws_measure) + 10):
+                st = sim.step(1)
+            ph = sim.phase_times()
+            d["fallback_after_20_solves"] = bool(st.learned_fallback)
+            d["poisson_ms_per_step_after_check"] = ph["poisson"][0] / (max(0, 20 - args.ws_measure) + 10)
         out[mode] = d
         sim.close()
     out["iteration_ratio_plain_over_learned"] = (out["plain"]["pcg_iterations_per_step"] /

@@ -199,8 +199,11 @@ typedef struct {
  * increment) pairs to the net, which trains train_iters Adam steps after
  * each; later solves start from the previous potential plus the net's
  * predicted increment, scaled by the A-norm line search, then the FP64 PCG
- * runs to the same tolerance.  Needs a block mesh whose cell counts are
- * multiples of 4 with n[0]*n[1]*n[2]/64 a multiple of 128. */
+ * runs to the same tolerance.  After each window of 20 such solves the mean
+ * PCG iterations are compared with the plain solves of the training phase;
+ * if the net saved less than 2% the solver falls back to the previous
+ * potential for good (learned_fallback).  Needs a block mesh whose cell
+ * counts are multiples of 4 with n[0]*n[1]*n[2]/64 a multiple of 128. */
 typedef struct {
     int32_t enabled;
     int32_t train_steps;      /* solves that feed the training set (0: 500) */
@@ -264,6 +267,8 @@ typedef struct {
     double  learned_residual;                   /* ||b-Ax||2/||b||2 before the net (the plain guess) */
     int32_t learned_active;                     /* 1 when the last solve started from the net's guess */
     int32_t learned_samples;                    /* training pairs collected so far */
+    int32_t learned_fallback;                   /* 1 once the net was switched off: it did not cut iterations */
+    int32_t pad_learned;
 } picgpu_step_stats;
 
 typedef struct picgpu_ctx picgpu_ctx;

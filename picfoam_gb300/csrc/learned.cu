@@ -241,7 +241,7 @@ cudaError_t LearnedWarmStart::before(const DMesh& m, const double* b, double* ph
     dot(b, b, &sc_->bb, s);
     cudaMemcpyAsync(&sc_->plain_rr, &sc_->rr, sizeof(double), cudaMemcpyDeviceToDevice, s);
     active = 0;
-    if (!trained() || !have_c0_) return cudaGetLastError();
+    if (!trained() || !have_c0_ || fallback) return cudaGetLastError();
     for (int pass = 0; pass <= cfg_.refine; ++pass) {
         if (pass > 0) residual(m, b, phi, s);
         if ((e = net_pass(m, b, phi, s)) != cudaSuccess) return e;
@@ -250,9 +250,19 @@ cudaError_t LearnedWarmStart::before(const DMesh& m, const double* b, double* ph
     return cudaGetLastError();
 }
 
-cudaError_t LearnedWarmStart::after(const DMesh& m, const double* phi, cudaStream_t s) {
+cudaError_t LearnedWarmStart::after(const DMesh& m, const double* phi, int iterations, cudaStream_t s) {
     (void)m;
     cudaError_t e;
+    if (active) {
+        // does the net cut iterations?  Window of 20 solves against the
+        // plain solves of the training phase; off for good if not.
+        net_iters_ += iterations;
+        if (++net_n_ == 20) {
+            if (plain_n_ > 0 && net_iters_ / net_n_ > 0.98 * (plain_iters_ / plain_n_)) fallback = 1;
+            net_iters_ = 0.0;
+            net_n_ = 0;
+        }
+    }
     if (!trained()) {
         // the pair (r(phi_prev), phi - phi_prev); r_ still holds r(phi_prev)
         // because a solve in the training phase has no net pass
@@ -297,6 +307,8 @@ cudaError_t LearnedWarmStart::after(const DMesh& m, const double* phi, cudaStrea
                     return e;
             }
             if ((e = net_.read_loss(&loss, s)) != cudaSuccess) return e;
+            plain_iters_ += iterations;
+            ++plain_n_;
             ++solves_;
         }
     }

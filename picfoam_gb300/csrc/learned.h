@@ -33,12 +33,14 @@ class LearnedWarmStart {
     // net's increment(s) added to phi with the A-norm line search.
     cudaError_t before(const DMesh& m, const double* b, double* phi, cudaStream_t s);
     // After the PCG: during training, store (residual, increment) and train.
-    cudaError_t after(const DMesh& m, const double* phi, cudaStream_t s);
+    // iterations: the PCG iterations the solve just took.
+    cudaError_t after(const DMesh& m, const double* phi, int iterations, cudaStream_t s);
     bool trained() const { return solves_ >= cfg_.train_steps; }
 
     double loss = 0.0, alpha = 0.0, plain_residual = 0.0;
     int active = 0;
     int samples = 0;
+    int fallback = 0;  // 1 once the net was switched off for not cutting iterations
     int64_t launches = 0;
 
    private:
@@ -56,6 +58,10 @@ class LearnedWarmStart {
     std::vector<void*> allocs_;
     int solves_ = 0;
     int head_ = 0;
+    double plain_iters_ = 0.0;   // PCG iterations of the warm training solves (previous-potential start)
+    int plain_n_ = 0;
+    double net_iters_ = 0.0;     // of the current window of net-started solves
+    int net_n_ = 0;
     uint64_t rng_ = 0;
     bool have_c0_ = false;
 

@@ -477,7 +477,7 @@ picgpu_status poisson(picgpu_ctx* c, picgpu_step_stats* stats, bool learned = fa
         c->launches += 2;
         if (learned && c->ws) {
             const int64_t l0 = c->ws->launches;
-            CK(c->ws->after(c->dm, c->phi, c->stream));
+            CK(c->ws->after(c->dm, c->phi, c->st_host->iters, c->stream));
             (void)l0;
         }
         CK(cudaMemcpyAsync(c->st_host, c->st, sizeof(pgd::PcgState), cudaMemcpyDeviceToHost, c->stream));
@@ -499,6 +499,7 @@ picgpu_status poisson(picgpu_ctx* c, picgpu_step_stats* stats, bool learned = fa
             stats->learned_residual = c->ws->plain_residual;
             stats->learned_active = c->ws->active;
             stats->learned_samples = c->ws->samples;
+            stats->learned_fallback = c->ws->fallback;
         }
     }
     if (!S.converged) return bad(c, PICGPU_PCG_NOT_CONVERGED, "PCG did not converge within pcg_max_iter");
