@@ -66,6 +66,9 @@ def parse():
                         "(electrode: electrode_box steps; unet: one forward + train steps; "
                         "ensemble: two graph replays)")
     p.add_argument("--only-steps", type=int, default=2)
+    p.add_argument("--only-precond", default="jacobi", choices=["jacobi", "multigrid"],
+                   help="Poisson preconditioner of the electrode driver")
+    p.add_argument("--no-multigrid", action="store_true", help="skip the multigrid-preconditioned Poisson arm")
     return p.parse_args()
 
 
@@ -250,8 +253,12 @@ def learned_vs_plain(args):
     import numpy as np
     from picfoam_gb300 import cases
     out = {}
-    for mode in ("plain", "learned"):
+    from picfoam_gb300 import abi
+    modes = ("plain", "learned") if args.no_multigrid else ("plain", "learned", "multigrid")
+    for mode in modes:
         case = cases.electrode_box(n_cells=args.ws_cells, per_cell=args.ws_ppc)
+        if mode == "multigrid":
+            case.cfg.pcg_precond = abi.PRECOND_MULTIGRID
         if mode == "learned":
             case.cfg.learned.enabled = 1
             case.cfg.learned.train_steps = args.ws_train
@@ -296,8 +303,15 @@ def learned_vs_plain(args):
                                                  max(out["learned"]["pcg_iterations_per_step"], 1e-9))
     out["ms_ratio_plain_over_learned"] = (out["plain"]["poisson_ms_per_step"] /
                                           max(out["learned"]["poisson_ms_per_step"], 1e-9))
+    if "multigrid" in out:
+        out["iteration_ratio_plain_over_multigrid"] = (out["plain"]["pcg_iterations_per_step"] /
+                                                       max(out["multigrid"]["pcg_iterations_per_step"], 1e-9))
+        out["ms_ratio_plain_over_multigrid"] = (out["plain"]["poisson_ms_per_step"] /
+                                                max(out["multigrid"]["poisson_ms_per_step"], 1e-9))
     out["config"] = (f"{args.ws_cells}^3 cells, 0.1 m cube, two floating 8^3-cell boxes and a 100 V box, "
-                     f"e- + Ar+ at {args.ws_ppc}/cell, FP64 Jacobi PCG (Chronopoulos-Gear) to 1e-8 relative residual, "
+                     f"e- + Ar+ at {args.ws_ppc}/cell, FP64 Jacobi PCG (Chronopoulos-Gear) to 1e-8 relative residual; "
+                     f"multigrid: flexible FP64 PCG with an FP32 aggregation V-cycle (2 + 2 Jacobi sweeps), same "
+                     f"tolerance; "
                      f"{args.ws_measure} measured steps")
     return out
 
@@ -487,6 +501,9 @@ def run_only(args):
     from picfoam_gb300 import cases, native
     if args.only == "electrode":
         case = cases.electrode_box(n_cells=args.ws_cells, per_cell=args.ws_ppc)
+        if args.only_precond == "multigrid":
+            from picfoam_gb300 import abi
+            case.cfg.pcg_precond = abi.PRECOND_MULTIGRID
         sim = cases.build(case)
         for _ in range(args.only_steps):
             st = sim.step(1)

@@ -193,6 +193,15 @@ typedef struct {
     int32_t pad;
 } picgpu_coulomb;
 
+/* Preconditioner of the Poisson PCG (fvSolution phiE { preconditioner }).
+ * Jacobi is the default and the form the oracle reproduces bit for bit.
+ * MULTIGRID (the GAMG preconditioner's role) applies one FP32 V-cycle of
+ * aggregation multigrid per iteration -- 2x2x2 cell aggregates on the block
+ * grid, Galerkin coarse operators, weighted-Jacobi smoothing, a dense inverse
+ * on the coarsest level -- inside a flexible FP64 PCG that still decides
+ * convergence at pcg_tol.  It needs a block mesh (picgpu_mesh_desc). */
+enum { PICGPU_PRECOND_JACOBI = 0, PICGPU_PRECOND_MULTIGRID = 1 };
+
 /* Learned warm start of the Poisson PCG (a 3D U-Net on the cell grid, see
  * picgpu_learned.h; no picFoam counterpart).  The first train_steps solves
  * start from the previous potential and feed (start residual, potential
@@ -214,6 +223,17 @@ typedef struct {
     int32_t pad;
 } picgpu_learned;
 
+/* Settings of the multigrid preconditioner (GAMG's nPreSweeps, nPostSweeps,
+ * nCellsInCoarsestLevel, scaleCorrection); 0 selects the default. */
+typedef struct {
+    int32_t pre_sweeps;       /* weighted-Jacobi sweeps before the coarse correction (0: 2) */
+    int32_t post_sweeps;      /* and after it (0: 2) */
+    int32_t coarsest_cells;   /* aggregate until a level has at most this many cells (0: 512, max 4096) */
+    int32_t pad;
+    double  omega;            /* Jacobi relaxation factor (0: 0.8) */
+    double  scale_correction; /* factor on the prolonged coarse correction (0: 1.6) */
+} picgpu_multigrid;
+
 typedef struct {
     int32_t pusher;               /* PICGPU_PUSHER_* */
     int32_t field_weighting;      /* PICGPU_WEIGHTING_* */
@@ -234,12 +254,13 @@ typedef struct {
     int32_t pcg_max_iter;
     int32_t pcg_norm;             /* 0: ||r||2/||b||2, 1: OpenFOAM-normalised L1 residual */
     int32_t sort_interval;        /* cell re-sort every N steps (0: never unless needed) */
-    int32_t pad0;
+    int32_t pcg_precond;          /* PICGPU_PRECOND_*: Jacobi (0) or multigrid (1) */
     uint64_t seed;
     picgpu_mcc mcc;
     picgpu_ion_mcc ion_mcc;
     picgpu_coulomb coulomb;
     picgpu_learned learned;
+    picgpu_multigrid mg;
 } picgpu_config;
 
 typedef struct {

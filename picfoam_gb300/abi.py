@@ -31,6 +31,7 @@ PREC_FP64, PREC_MIXED = range(2)
 DEPOSIT_ATOMIC_FP64, DEPOSIT_FIXED_POINT = range(2)
 PATCH_CYCLIC, PATCH_EMPTY, PATCH_ABSORB, PATCH_WALL, PATCH_FLOATING = range(5)
 PHI_FIXED_VALUE, PHI_ZERO_GRADIENT = range(2)
+PRECOND_JACOBI, PRECOND_MULTIGRID = range(2)
 FIELD_PHI, FIELD_E_CELL, FIELD_RHO, FIELD_E_POINT, FIELD_SIGMA_V_MAX = range(5)
 (PHASE_MOVE, PHASE_CHARGE, PHASE_POISSON, PHASE_EFIELD, PHASE_SORT, PHASE_MCC,
  PHASE_COULOMB, PHASE_COUNT) = range(8)
@@ -110,6 +111,13 @@ class Learned(C.Structure):
     ]
 
 
+class Multigrid(C.Structure):
+    _fields_ = [
+        ("pre_sweeps", C.c_int32), ("post_sweeps", C.c_int32), ("coarsest_cells", C.c_int32),
+        ("pad", C.c_int32), ("omega", C.c_double), ("scale_correction", C.c_double),
+    ]
+
+
 class Config(C.Structure):
     _fields_ = [
         ("pusher", C.c_int32), ("field_weighting", C.c_int32),
@@ -121,9 +129,10 @@ class Config(C.Structure):
         ("space_charge", C.c_double),
         ("sync_velocity_at_boundary", C.c_int32), ("track_max_steps", C.c_int32),
         ("pcg_tol", C.c_double), ("pcg_max_iter", C.c_int32), ("pcg_norm", C.c_int32),
-        ("sort_interval", C.c_int32), ("pad0", C.c_int32),
+        ("sort_interval", C.c_int32), ("pcg_precond", C.c_int32),
         ("seed", C.c_uint64),
         ("mcc", Mcc), ("ion_mcc", IonMcc), ("coulomb", Coulomb), ("learned", Learned),
+        ("mg", Multigrid),
     ]
 
 

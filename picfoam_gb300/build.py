@@ -34,6 +34,7 @@ UNITS = {
     "unet_conv.cu": [],
     "unet.cu": [],
     "learned.cu": [],
+    "mg.cu": [],
     "unet_api.cu": [],
 }
 HEADERS = [os.path.join(SRC, f) for f in os.listdir(SRC) if f.endswith((".h", ".cuh", ".hpp"))] + [

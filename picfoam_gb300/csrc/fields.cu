@@ -16,6 +16,7 @@
 //   boundary_E      corrected boundary values of E
 //   point_E         cell -> point interpolation (VolumeWeightingFW.C:70-75)
 #include "fields.h"
+#include "reduce.cuh"
 
 #include <algorithm>
 
@@ -25,48 +26,6 @@ __constant__ PatchConst c_patchF;
 
 constexpr double kMu0 = 4.0 * kPi * 1e-7;
 __device__ __forceinline__ double eps0() { return 1.0 / (kMu0 * kC * kC); }
-
-// ------------------------------------------------------- reductions ------
-// Sum over the block in the fixed tree order: lane l of warp 0 adds the
-// values of threads l, l+32, ..., l+224 in turn, then the 32 lanes meet in an
-// xor-tree.  One warp does the FP64 adds (the FP64 pipe is the scarce unit on
-// this part).  ws holds 256 doubles; the result is valid in every lane of
-// warp 0.
-__device__ __forceinline__ double block_tree(double v, double* ws) {
-    ws[threadIdx.x] = v;
-    __syncthreads();
-    double r = 0.0;
-    if (threadIdx.x < 32) {
-        r = ws[threadIdx.x];
-#pragma unroll
-        for (int j = 1; j < 8; ++j) r = r + ws[threadIdx.x + 32 * j];
-#pragma unroll
-        for (int off = 16; off >= 1; off >>= 1) r = r + __shfl_xor_sync(0xffffffffu, r, off);
-    }
-    __syncthreads();
-    return r;
-}
-
-// Last-block finalisation: returns true in the block that arrives last; the
-// block partials are then visible to it.
-__device__ __forceinline__ bool arrive_last(unsigned int* ticket) {
-    __shared__ bool last;
-    __threadfence();
-    __syncthreads();
-    if (threadIdx.x == 0) {
-        const unsigned int t = atomicAdd(ticket, 1u);
-        last = (t == gridDim.x - 1);
-        if (last) *ticket = 0u;
-    }
-    __syncthreads();
-    return last;
-}
-
-__device__ __forceinline__ double final_sum(const double* part, int nb, double* ws) {
-    double s = 0.0;
-    for (int i = threadIdx.x; i < nb; i += 256) s = s + __ldcg(part + i);
-    return block_tree(s, ws);
-}
 
 // ------------------------------------------------------------ charge -----
 __global__ void charge_update_kernel(DMesh m, int volume_weighting, int fixed, double fix_scale,

@@ -27,6 +27,7 @@
 #include "hexmesh.hpp"
 #include "kernels.h"
 #include "learned.h"
+#include "mg.h"
 #include "particles.h"
 #include "picgpu.h"
 #include "picgpu_ensemble.h"
@@ -107,6 +108,7 @@ struct picgpu_ctx {
     cudaGraphExec_t pcg_graph = nullptr;
     double pcg_r0 = 0.0;  // ||b - A x0|| / ||b|| of the last solve's start guess
     std::unique_ptr<pgd::LearnedWarmStart> ws;  // learned warm start (cfg.learned.enabled)
+    std::unique_ptr<pgd::MultigridPCG> mg;      // multigrid-preconditioned PCG (cfg.pcg_precond)
     // batched ensembles and graph-stepped runs
     int n_cases = 1;
     int* n_dev = nullptr;          // species counts on the device (graph steps)
@@ -446,7 +448,7 @@ picgpu_status poisson(picgpu_ctx* c, picgpu_step_stats* stats, bool learned = fa
         // (2 kernels each); iterations after convergence return at once, so
         // the iteration count stays exact.  The host checks the done flag
         // after each replay.
-        if (!c->pcg_graph) {
+        if (!c->pcg_graph && !c->mg) {
             cudaGraph_t g;
             CK(cudaStreamBeginCapture(c->stream, cudaStreamCaptureModeThreadLocal));
             for (int j = 0; j < kGraphIters; ++j)
@@ -460,27 +462,44 @@ picgpu_status poisson(picgpu_ctx* c, picgpu_step_stats* stats, bool learned = fa
         if (learned && c->ws) {
             CK(c->ws->before(c->dm, c->b, c->phi, c->stream));
         }
-        pgd::launch_pcg_init(c->dm, c->b, c->phi, c->r, c->z, c->q, c->part, c->st, tol, c->stream);
-        c->launches += c->m.has_dirichlet ? 3 : 5;
-        CK(cudaMemcpyAsync(c->st_host, c->st, sizeof(pgd::PcgState), cudaMemcpyDeviceToHost, c->stream));
-        CK(cudaStreamSynchronize(c->stream));
-        c->pcg_r0 = c->st_host->bb > 0 ? std::sqrt(c->st_host->rr / c->st_host->bb) : 0.0;
-        int launched = 0;
-        while (!c->st_host->done && launched < maxit) {
-            CK(cudaGraphLaunch(c->pcg_graph, c->stream));
-            launched += kGraphIters;
-            c->launches += 2 * kGraphIters;
+        c->launches += c->m.has_dirichlet ? 1 : 3;
+        if (c->mg) {
+            // flexible PCG with the multigrid V-cycle
+            int it = 0;
+            double rr0 = 0, rr = 0, bb = 0;
+            bool conv = false;
+            const int64_t l0 = c->mg->launches;
+            CK(c->mg->solve(c->dm, c->b, c->phi, tol, maxit, c->stream, &it, &rr0, &rr, &bb, &conv));
+            c->launches += c->mg->launches - l0;
+            c->pcg_r0 = bb > 0 ? std::sqrt(rr0 / bb) : 0.0;
+            pgd::launch_of_residual(c->dm, c->b, c->phi, c->part, c->st, c->stream);
+            c->launches += 2;
+            if (learned && c->ws) CK(c->ws->after(c->dm, c->phi, it, c->stream));
             CK(cudaMemcpyAsync(c->st_host, c->st, sizeof(pgd::PcgState), cudaMemcpyDeviceToHost, c->stream));
             CK(cudaStreamSynchronize(c->stream));
+            c->st_host->iters = it;
+            c->st_host->rr = rr;
+            c->st_host->bb = bb;
+            c->st_host->converged = conv ? 1 : 0;
+        } else {
+            pgd::launch_pcg_init(c->dm, c->b, c->phi, c->r, c->z, c->q, c->part, c->st, tol, c->stream);
+            c->launches += 2;
+            CK(cudaMemcpyAsync(c->st_host, c->st, sizeof(pgd::PcgState), cudaMemcpyDeviceToHost, c->stream));
+            CK(cudaStreamSynchronize(c->stream));
+            c->pcg_r0 = c->st_host->bb > 0 ? std::sqrt(c->st_host->rr / c->st_host->bb) : 0.0;
+            int launched = 0;
+            while (!c->st_host->done && launched < maxit) {
+                CK(cudaGraphLaunch(c->pcg_graph, c->stream));
+                launched += kGraphIters;
+                c->launches += 2 * kGraphIters;
+                CK(cudaMemcpyAsync(c->st_host, c->st, sizeof(pgd::PcgState), cudaMemcpyDeviceToHost, c->stream));
+                CK(cudaStreamSynchronize(c->stream));
+            }
+            pgd::launch_of_residual(c->dm, c->b, c->phi, c->part, c->st, c->stream);
+            c->launches += 2;
+            if (learned && c->ws) CK(c->ws->after(c->dm, c->phi, c->st_host->iters, c->stream));
+            CK(cudaMemcpyAsync(c->st_host, c->st, sizeof(pgd::PcgState), cudaMemcpyDeviceToHost, c->stream));
         }
-        pgd::launch_of_residual(c->dm, c->b, c->phi, c->part, c->st, c->stream);
-        c->launches += 2;
-        if (learned && c->ws) {
-            const int64_t l0 = c->ws->launches;
-            CK(c->ws->after(c->dm, c->phi, c->st_host->iters, c->stream));
-            (void)l0;
-        }
-        CK(cudaMemcpyAsync(c->st_host, c->st, sizeof(pgd::PcgState), cudaMemcpyDeviceToHost, c->stream));
     }
     picgpu_status s = efield(c);
     if (s) return s;
@@ -1039,6 +1058,8 @@ static picgpu_status create_with_mesh(picgpu_ctx* c, const picgpu_config* cfg) {
         return bad(c, PICGPU_INVALID_ARG, "config: unknown ParticlePusher");
     if (cfg->precision != PICGPU_PREC_FP64 && cfg->precision != PICGPU_PREC_MIXED)
         return bad(c, PICGPU_INVALID_ARG, "config: unknown precision");
+    if (cfg->pcg_precond != PICGPU_PRECOND_JACOBI && cfg->pcg_precond != PICGPU_PRECOND_MULTIGRID)
+        return bad(c, PICGPU_INVALID_ARG, "config: unknown PCG preconditioner");
     c->cfg = *cfg;
     c->mixed = cfg->precision == PICGPU_PREC_MIXED;
     c->rotation = cfg->B[0] != 0.0 || cfg->B[1] != 0.0 || cfg->B[2] != 0.0;
@@ -1227,6 +1248,21 @@ static picgpu_status create_with_mesh(picgpu_ctx* c, const picgpu_config* cfg) {
         const int ls = c->ws->init(cfg->learned, cfg->seed, c->m.n_cells, c->m.n, c->m.cell_ijk, c->stream, &msg);
         if (ls) return bad(c, picgpu_status(ls), msg);
     }
+    if (cfg->pcg_precond == PICGPU_PRECOND_MULTIGRID && cfg->maxwell_solver == PICGPU_MAXWELL_ELECTROSTATIC) {
+        pgd::MgSettings ms;
+        if (cfg->mg.pre_sweeps > 0) ms.pre = cfg->mg.pre_sweeps;
+        if (cfg->mg.post_sweeps > 0) ms.post = cfg->mg.post_sweeps;
+        if (cfg->mg.coarsest_cells > 0) ms.coarsest = cfg->mg.coarsest_cells;
+        if (cfg->mg.omega > 0) ms.omega = cfg->mg.omega;
+        if (cfg->mg.scale_correction > 0) ms.scale = cfg->mg.scale_correction;
+        if (ms.pre > 8 || ms.post > 8 || ms.coarsest > 4096 || !(ms.omega < 2.0) || !(ms.scale <= 2.0))
+            return bad(c, PICGPU_INVALID_ARG, "config: multigrid settings out of range");
+        std::vector<double> Md(c->m.n_cells), Mo(c->m.lap_off.size());
+        for (int i = 0; i < c->m.n_cells; ++i) Md[i] = -c->m.lap_diag[i];
+        for (size_t i = 0; i < Mo.size(); ++i) Mo[i] = -c->m.lap_off[i];
+        c->mg = std::make_unique<pgd::MultigridPCG>();
+        if (!c->mg->init(c->m, Md, Mo, ms, &msg)) return bad(c, PICGPU_NOT_SUPPORTED, msg);
+    }
     CK(cudaStreamSynchronize(c->stream));
     c->err.clear();
     return PICGPU_OK;
@@ -1235,6 +1271,7 @@ static picgpu_status create_with_mesh(picgpu_ctx* c, const picgpu_config* cfg) {
 void picgpu_destroy(picgpu_ctx* c) {
     if (!c) return;
     if (c->stream) cudaStreamSynchronize(c->stream);
+    c->mg.reset();
     pgd::collide_free(c->coll);
     for (void* a : c->allocs)
         if (a) cudaFree(a);

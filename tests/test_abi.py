@@ -47,6 +47,39 @@ def test_struct_sizes_match_header_layout():
     assert C.sizeof(abi.StepStats) % 8 == 0
 
 
+MIRRORS = {
+    "Patch": "picgpu_patch", "Box": "picgpu_box", "MeshDesc": "picgpu_mesh_desc", "Species": "picgpu_species",
+    "Mcc": "picgpu_mcc", "IonMcc": "picgpu_ion_mcc", "Coulomb": "picgpu_coulomb", "Learned": "picgpu_learned",
+    "Multigrid": "picgpu_multigrid", "Config": "picgpu_config", "StepStats": "picgpu_step_stats",
+    "MeshInfo": "picgpu_mesh_info", "Diagnostics": "picgpu_diagnostics",
+}
+
+
+def test_every_field_offset_matches_the_header(tmp_path):
+    """A C probe compiled against include/picgpu.h prints sizeof and the
+    offset of every field the ctypes mirrors declare."""
+    import shutil
+    import subprocess
+    cc = shutil.which("gcc") or shutil.which("cc")
+    if cc is None:
+        pytest.skip("no C compiler")
+    lines, expect = [], []
+    for py, cname in MIRRORS.items():
+        st = getattr(abi, py)
+        lines.append(f'printf("%zu\\n", sizeof({cname}));')
+        expect.append(C.sizeof(st))
+        for f in st._fields_:
+            lines.append(f'printf("%zu\\n", offsetof({cname}, {f[0]}));')
+            expect.append(getattr(st, f[0]).offset)
+    src = tmp_path / "probe.c"
+    src.write_text("#include <stddef.h>\n#include <stdio.h>\n#include \"picgpu.h\"\nint main(void) {\n"
+                   + "\n".join(lines) + "\nreturn 0;\n}\n")
+    exe = tmp_path / "probe"
+    subprocess.run([cc, "-std=c11", "-I", os.path.join(ROOT, "include"), str(src), "-o", str(exe)], check=True)
+    got = [int(v) for v in subprocess.run([str(exe)], check=True, capture_output=True, text=True).stdout.split()]
+    assert got == expect
+
+
 def test_mesh_handle_without_gpu(lib):
     case = cases.two_species_3d(n_cells=6, per_cell=3, L=0.003)
     m = Mesh(case.mesh)
