@@ -289,7 +289,7 @@ typedef struct {
     int32_t learned_active;                     /* 1 when the last solve started from the net's guess */
     int32_t learned_samples;                    /* training pairs collected so far */
     int32_t learned_fallback;                   /* 1 once the net was switched off: it did not cut iterations */
-    int32_t pad_learned;
+    int32_t pcg_refinements;                    /* last multigrid solve: FP64 refinement steps (0 with Jacobi) */
 } picgpu_step_stats;
 
 typedef struct picgpu_ctx picgpu_ctx;

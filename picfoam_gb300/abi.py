@@ -152,7 +152,7 @@ class StepStats(C.Structure):
         ("floating_charge", C.c_double * (MAX_BOXES + 6)),
         ("learned_loss", C.c_double), ("learned_alpha", C.c_double), ("learned_residual", C.c_double),
         ("learned_active", C.c_int32), ("learned_samples", C.c_int32),
-        ("learned_fallback", C.c_int32), ("pad_learned", C.c_int32),
+        ("learned_fallback", C.c_int32), ("pcg_refinements", C.c_int32),
     ]
 
     def as_dict(self):

@@ -109,6 +109,7 @@ struct picgpu_ctx {
     double pcg_r0 = 0.0;  // ||b - A x0|| / ||b|| of the last solve's start guess
     std::unique_ptr<pgd::LearnedWarmStart> ws;  // learned warm start (cfg.learned.enabled)
     std::unique_ptr<pgd::MultigridPCG> mg;      // multigrid-preconditioned PCG (cfg.pcg_precond)
+    int mg_outer = 0;                           // refinement steps of the last multigrid solve
     // batched ensembles and graph-stepped runs
     int n_cases = 1;
     int* n_dev = nullptr;          // species counts on the device (graph steps)
@@ -464,12 +465,13 @@ picgpu_status poisson(picgpu_ctx* c, picgpu_step_stats* stats, bool learned = fa
         }
         c->launches += c->m.has_dirichlet ? 1 : 3;
         if (c->mg) {
-            // flexible PCG with the multigrid V-cycle
-            int it = 0;
+            // FP64 refinement around the FP32 multigrid-preconditioned CG
+            int it = 0, outer = 0;
             double rr0 = 0, rr = 0, bb = 0;
             bool conv = false;
             const int64_t l0 = c->mg->launches;
-            CK(c->mg->solve(c->dm, c->b, c->phi, tol, maxit, c->stream, &it, &rr0, &rr, &bb, &conv));
+            CK(c->mg->solve(c->dm, c->b, c->phi, tol, maxit, c->stream, &it, &outer, &rr0, &rr, &bb, &conv));
+            c->mg_outer = outer;
             c->launches += c->mg->launches - l0;
             c->pcg_r0 = bb > 0 ? std::sqrt(rr0 / bb) : 0.0;
             pgd::launch_of_residual(c->dm, c->b, c->phi, c->part, c->st, c->stream);
@@ -512,6 +514,7 @@ picgpu_status poisson(picgpu_ctx* c, picgpu_step_stats* stats, bool learned = fa
         stats->pcg_residual_l2 = S.bb > 0 ? std::sqrt(S.rr / S.bb) : 0.0;
         stats->pcg_residual_of = S.of_residual;
         stats->pcg_residual_initial = c->pcg_r0;
+        stats->pcg_refinements = c->mg ? c->mg_outer : 0;
         if (learned && c->ws) {
             stats->learned_loss = c->ws->loss;
             stats->learned_alpha = c->ws->alpha;
@@ -521,7 +524,13 @@ picgpu_status poisson(picgpu_ctx* c, picgpu_step_stats* stats, bool learned = fa
             stats->learned_fallback = c->ws->fallback;
         }
     }
-    if (!S.converged) return bad(c, PICGPU_PCG_NOT_CONVERGED, "PCG did not converge within pcg_max_iter");
+    if (!S.converged) {
+        char msg[160];
+        std::snprintf(msg, sizeof msg, "PCG did not converge within pcg_max_iter (%d iterations, %d refinements, "
+                      "relative residual %.3e)", S.iters, c->mg ? c->mg_outer : 0,
+                      S.bb > 0 ? std::sqrt(S.rr / S.bb) : 0.0);
+        return bad(c, PICGPU_PCG_NOT_CONVERGED, msg);
+    }
     return PICGPU_OK;
 }
 

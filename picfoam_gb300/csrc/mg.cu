@@ -1,24 +1,30 @@
-// mg.cu -- flexible FP64 PCG with an FP32 aggregation-multigrid V-cycle as
-// preconditioner (the role of OpenFOAM's GAMG preconditioner inside PCG; the
-// solver call it replaces is ElectroStaticSolver.C:61-64).
+// mg.cu -- Poisson solve: FP64 iterative refinement around an FP32
+// aggregation-multigrid-preconditioned conjugate gradient (the role of
+// OpenFOAM's PCG + GAMG preconditioner for the solve of
+// ElectroStaticSolver.C:61-64).
 //
-// Kernels, all deterministic (no atomics in any sum):
-//   mg_init      r = b - M x, r.r and b.b; r as FP32 into the level-0 voxels
-//   V-cycle      per level: Jacobi sweeps, residual + restriction to the
-//                aggregates, (coarse level), prolongation, Jacobi sweeps;
-//                dense inverse times vector on the coarsest level
-//   mg_gather    z = V-cycle result, r.z and r.z_old -> beta
-//   mg_direction p = z + beta p
-//   mg_spmv      q = M p, p.q -> alpha
-//   mg_axpy      x += alpha p, r -= alpha q, r.r -> convergence; r into level 0
-// Every kernel after the initialisation returns at once when the solve is
-// done, so a CUDA graph of a fixed number of iterations stops exactly at
-// convergence.
+// Kernels; every sum runs in a fixed order (no atomics), so a solve is
+// bit-reproducible:
+//   mg_residual   FP64 r = b - M x over the cells, r.r (and b.b); closes the
+//                 outer loop (convergence, power-of-two scale, inner eta)
+//   mg_convert    r into the level-0 voxels as FP32 (scaled), d = 0, r.r
+//   V-cycle       per level: two Jacobi sweeps from the zero guess in one
+//                 pass, residual + restriction to the aggregates, coarse
+//                 level, prolongation, Jacobi sweeps; the last level-0 sweep
+//                 also forms r.z and beta; dense inverse times vector on the
+//                 coarsest level
+//   mg_spmv       p = z + beta p (formed at the stencil points) and q = A p
+//                 in one pass, p.q and q.z -> alpha
+//   mg_axpy       d += alpha p, r -= alpha q, r.r; closes the inner loop
+//   mg_update     FP64 x += d / scale
+// Voxel kernels run on 3-D grids (x-y tiles, one grid slice per plane), so a
+// thread's (i, j, k) come without a division.
 #include "mg.h"
 
 #include <algorithm>
 #include <array>
 #include <cmath>
+#include <cstdlib>
 #include <cstring>
 
 #include "fields.h"
@@ -28,12 +34,15 @@ namespace pgd {
 
 namespace {
 
-constexpr int kGraphIters = 8;
+constexpr int kInnerMax = 200;     // inner iterations per outer step
+constexpr int kOuterMax = 64;      // outer steps per solve
+constexpr double kEtaMin = 1e-4;   // deepest relative reduction asked of one FP32 inner solve
 
-// Level description passed by value to the FP32 kernels.
+// Level description passed by value to the FP32 kernels (32-bit indices:
+// a level holds fewer than 2^31 voxels).
 struct Lv {
     int X, Y, Z, cx, cy, cz;
-    long V;
+    int V;
     int uniform;
     float coef[6];
     const float* __restrict__ diag;
@@ -49,7 +58,7 @@ Lv view(const MgLevel& L) {
     v.cx = L.cyc[0];
     v.cy = L.cyc[1];
     v.cz = L.cyc[2];
-    v.V = L.V;
+    v.V = int(L.V);
     v.uniform = L.uniform;
     for (int f = 0; f < 6; ++f) v.coef[f] = L.coef[f];
     v.diag = L.diag;
@@ -58,13 +67,70 @@ Lv view(const MgLevel& L) {
     return v;
 }
 
-// (A x)_v on one level.  A neighbour across a non-periodic edge has no
-// coupling (its coefficient is zero, the index falls back to v itself); a
-// hole neighbour holds zero, so the uniform form may use coef[f] there.
-template <bool Uniform>
-__device__ __forceinline__ float apply_A(const Lv& L, const float* __restrict__ x, long v, int i, int j, int k) {
-    const long X = L.X, XY = long(L.X) * L.Y;
-    long nb[6];
+// Launch shape of a voxel kernel: 256-thread blocks tiling an x-y plane as
+// BX x BY, one grid z-slice per plane, so that a thread's (i, j, k) come
+// from its indices without a division.
+struct Shape {
+    dim3 grid, block;
+    int blocks;
+};
+
+int pow2_at_least(int n, int cap) {
+    int p = 1;
+    while (p < n && p < cap) p <<= 1;
+    return p;
+}
+
+// Rows of up to 32 x-neighbours; thin planes (small Y) get wider x-tiles so
+// that few threads fall outside the grid.
+Shape shape(int X, int Y, int Z) {
+    const int by = std::min(256 / pow2_at_least(X, 32), pow2_at_least(Y, 256));
+    const int bx = 256 / by;
+    Shape s;
+    s.block = dim3(bx, by, 1);
+    s.grid = dim3((X + bx - 1) / bx, (Y + by - 1) / by, Z);
+    s.blocks = int(s.grid.x * s.grid.y * s.grid.z);
+    return s;
+}
+
+Shape shape(const MgLevel& L) { return shape(L.n[0], L.n[1], L.n[2]); }
+
+// The level-0 kernels that end in a grid-wide sum give each thread kZB
+// z-planes, so that the last block combines kZB times fewer partials.
+constexpr int kZB = 4;
+
+Shape shape_sum(const MgLevel& L) {
+    Shape s = shape(L);
+    s.grid.z = (L.n[2] + kZB - 1) / kZB;
+    s.blocks = int(s.grid.x * s.grid.y * s.grid.z);
+    return s;
+}
+
+__device__ __forceinline__ bool coords(const Lv& L, int& i, int& j, int& k, int& v) {
+    i = blockIdx.x * blockDim.x + threadIdx.x;
+    j = blockIdx.y * blockDim.y + threadIdx.y;
+    k = blockIdx.z;
+    v = i + L.X * (j + L.Y * k);
+    return i < L.X && j < L.Y;
+}
+
+// Plane kz of the kZB planes of a shape_sum block.
+__device__ __forceinline__ bool coords_sum(const Lv& L, int kz, int& i, int& j, int& k, int& v) {
+    i = blockIdx.x * blockDim.x + threadIdx.x;
+    j = blockIdx.y * blockDim.y + threadIdx.y;
+    k = blockIdx.z * kZB + kz;
+    v = i + L.X * (j + L.Y * k);
+    return i < L.X && j < L.Y && k < L.Z;
+}
+
+// (A u)_v on one level for a field given by val(w).  A neighbour across a
+// non-periodic edge has no coupling (its coefficient is zero, the index falls
+// back to v itself); a hole neighbour holds zero, so the uniform form may use
+// coef[f] there.
+template <bool Uniform, class Val>
+__device__ __forceinline__ float apply_A(const Lv& L, int i, int j, int k, int v, Val val) {
+    const int X = L.X, XY = L.X * L.Y;
+    int nb[6];
     bool ok[6];
     ok[0] = i > 0 || L.cx;
     nb[0] = i > 0 ? v - 1 : (L.cx ? v + X - 1 : v);
@@ -78,68 +144,124 @@ __device__ __forceinline__ float apply_A(const Lv& L, const float* __restrict__ 
     nb[4] = k > 0 ? v - XY : (L.cz ? v + L.V - XY : v);
     ok[5] = k < L.Z - 1 || L.cz;
     nb[5] = k < L.Z - 1 ? v + XY : (L.cz ? v - (L.V - XY) : v);
-    float s = L.diag[v] * x[v];
+    float s = L.diag[v] * val(v);
 #pragma unroll
     for (int f = 0; f < 6; ++f) {
         const float a = Uniform ? (ok[f] ? L.coef[f] : 0.f) : L.off[f * L.V + v];
-        s = fmaf(a, x[nb[f]], s);
+        s = fmaf(a, val(nb[f]), s);
     }
     return s;
 }
 
-__device__ __forceinline__ void decode(const Lv& L, long v, int& i, int& j, int& k) {
-    i = int(v % L.X);
-    const long r = v / L.X;
-    j = int(r % L.Y);
-    k = int(r / L.Y);
+// ------------------------------------------------------------ V-cycle ----
+// One sweep from a zero guess: y = omega D^-1 b.
+__global__ void __launch_bounds__(256) mg_smooth0_kernel(Lv L, const float* __restrict__ b, float* __restrict__ y,
+                                                         float omega) {
+    int i, j, k, v;
+    if (!coords(L, i, j, k, v)) return;
+    y[v] = (omega * L.inv[v]) * b[v];
 }
 
-// First sweep from a zero guess: y = omega D^-1 b.
-__global__ void __launch_bounds__(256) mg_smooth0_kernel(Lv L, const float* __restrict__ b, float* __restrict__ y,
-                                                         float omega, const MgScalars* sc) {
-    if (sc->done) return;
-    const long v = long(blockIdx.x) * 256 + threadIdx.x;
-    if (v >= L.V) return;
-    y[v] = (omega * L.inv[v]) * b[v];
+// Two sweeps from a zero guess in one pass: x1 = omega D^-1 b is formed on
+// the fly at the seven stencil points, y = x1 + omega D^-1 (b - A x1).
+template <bool Uniform>
+__global__ void __launch_bounds__(256) mg_smooth01_kernel(Lv L, const float* __restrict__ b, float* __restrict__ y,
+                                                          float omega) {
+    int i, j, k, v;
+    if (!coords(L, i, j, k, v)) return;
+    const float* __restrict__ inv = L.inv;
+    auto x1 = [&](int w) { return (omega * inv[w]) * b[w]; };
+    const float ax = apply_A<Uniform>(L, i, j, k, v, x1);
+    y[v] = fmaf(omega * inv[v], b[v] - ax, x1(v));
 }
 
 // One weighted-Jacobi sweep: y = x + omega D^-1 (b - A x).
 template <bool Uniform>
 __global__ void __launch_bounds__(256) mg_smooth_kernel(Lv L, const float* __restrict__ b,
                                                         const float* __restrict__ x, float* __restrict__ y,
-                                                        float omega, const MgScalars* sc) {
-    if (sc->done) return;
-    const long v = long(blockIdx.x) * 256 + threadIdx.x;
-    if (v >= L.V) return;
-    int i, j, k;
-    decode(L, v, i, j, k);
-    const float ax = apply_A<Uniform>(L, x, v, i, j, k);
+                                                        float omega) {
+    int i, j, k, v;
+    if (!coords(L, i, j, k, v)) return;
+    const float ax = apply_A<Uniform>(L, i, j, k, v, [&](int w) { return x[w]; });
     y[v] = fmaf(omega * L.inv[v], b[v] - ax, x[v]);
 }
 
-// Coarse right-hand side: bc[I] = sum over the active children of I of
-// (b - A x), children in x-fastest order.
+// Closes the preconditioner application: rz = r.z, and the flexible
+// (Polak-Ribiere) beta = (r.z - r.z_old) / rz_old with
+// r.z_old = rz_old - alpha q.z_old from the previous iteration.
+__device__ __forceinline__ void finish_rz(float prod, float* wsf, double* ws, double* part, MgScalars* sc) {
+    const float bs = block_tree_f(prod, wsf);
+    if (flat_tid() == 0) part[flat_bid()] = double(bs);
+    if (arrive_last(&sc->ticket)) {
+        const double rz = final_sum(part, int(grid_blocks()), ws);
+        if (flat_tid() == 0) {
+            const double rzo = sc->rz - sc->alpha * sc->qz;
+            sc->beta = sc->k == 0 ? 0.0 : (rz - rzo) / sc->rz;
+            sc->rz = rz;
+        }
+    }
+}
+
+// The last level-0 sweep, which also forms r.z (b is the inner residual r).
 template <bool Uniform>
-__global__ void __launch_bounds__(256) mg_restrict_kernel(Lv F, Lv Cl, int fx, int fy, int fz,
+__global__ void __launch_bounds__(256) mg_smooth_dot_kernel(Lv L, const float* __restrict__ b,
+                                                            const float* __restrict__ x, float* __restrict__ y,
+                                                            float omega, double* part, MgScalars* sc) {
+    __shared__ float wsf[256];
+    __shared__ double ws[256];
+    float prod = 0.f;
+#pragma unroll
+    for (int kz = 0; kz < kZB; ++kz) {
+        int i, j, k, v;
+        if (!coords_sum(L, kz, i, j, k, v)) continue;
+        const float ax = apply_A<Uniform>(L, i, j, k, v, [&](int w) { return x[w]; });
+        const float bv = b[v];
+        const float yv = fmaf(omega * L.inv[v], bv - ax, x[v]);
+        y[v] = yv;
+        prod = fmaf(bv, yv, prod);
+    }
+    finish_rz(prod, wsf, ws, part, sc);
+}
+
+// r.z alone (no post sweeps, or a single-level hierarchy).
+__global__ void __launch_bounds__(256) mg_rz_kernel(Lv L, const float* __restrict__ r, const float* __restrict__ z,
+                                                    double* part, MgScalars* sc) {
+    __shared__ float wsf[256];
+    __shared__ double ws[256];
+    float prod = 0.f;
+#pragma unroll
+    for (int kz = 0; kz < kZB; ++kz) {
+        int i, j, k, v;
+        if (coords_sum(L, kz, i, j, k, v)) prod = fmaf(r[v], z[v], prod);
+    }
+    finish_rz(prod, wsf, ws, part, sc);
+}
+
+// Coarse right-hand side: bc[I] = sum over the active children of I of
+// (b - A x), children in x-fastest order; sx, sy, sz are the aggregation
+// shifts (1: pairs, 0: none) of each axis.
+template <bool Uniform>
+__global__ void __launch_bounds__(256) mg_restrict_kernel(Lv F, Lv Cl, int sx, int sy, int sz,
                                                           const float* __restrict__ b, const float* __restrict__ x,
-                                                          float* __restrict__ bc, const MgScalars* sc) {
-    if (sc->done) return;
-    const long I = long(blockIdx.x) * 256 + threadIdx.x;
-    if (I >= Cl.V) return;
-    int ci, cj, ck;
-    decode(Cl, I, ci, cj, ck);
+                                                          float* __restrict__ bc) {
+    int ci, cj, ck, I;
+    if (!coords(Cl, ci, cj, ck, I)) return;
+    auto xv = [&](int w) { return x[w]; };
     float s = 0.f;
-    for (int dz = 0; dz < fz; ++dz) {
-        const int k = fz * ck + dz;
-        if (k >= F.Z) break;
-        for (int dy = 0; dy < fy; ++dy) {
-            const int j = fy * cj + dy;
-            if (j >= F.Y) break;
-            for (int dx = 0; dx < fx; ++dx) {
-                const int i = fx * ci + dx;
-                if (i >= F.X) break;
-                const long v = i + long(F.X) * (j + long(F.Y) * k);
-                if (F.inv[v] != 0.f) s += b[v] - apply_A<Uniform>(F, x, v, i, j, k);
+#pragma unroll
+    for (int dz = 0; dz < 2; ++dz) {
+        const int k = (ck << sz) + dz;
+        if (dz > sz || k >= F.Z) continue;
+#pragma unroll
+        for (int dy = 0; dy < 2; ++dy) {
+            const int j = (cj << sy) + dy;
+            if (dy > sy || j >= F.Y) continue;
+#pragma unroll
+            for (int dx = 0; dx < 2; ++dx) {
+                const int i = (ci << sx) + dx;
+                if (dx > sx || i >= F.X) continue;
+                const int v = i + F.X * (j + F.Y * k);
+                if (F.inv[v] != 0.f) s += b[v] - apply_A<Uniform>(F, i, j, k, v, xv);
             }
         }
     }
@@ -147,25 +269,20 @@ __global__ void __launch_bounds__(256) mg_restrict_kernel(Lv F, Lv Cl, int fx, i
 }
 
 // x += scale * xc[parent] on the active voxels.
-__global__ void __launch_bounds__(256) mg_prolong_kernel(Lv F, int CX, int CY, int fx, int fy, int fz,
+__global__ void __launch_bounds__(256) mg_prolong_kernel(Lv F, int CX, int CY, int sx, int sy, int sz,
                                                          const float* __restrict__ xc, float* __restrict__ x,
-                                                         float scale, const MgScalars* sc) {
-    if (sc->done) return;
-    const long v = long(blockIdx.x) * 256 + threadIdx.x;
-    if (v >= F.V) return;
+                                                         float scale) {
+    int i, j, k, v;
+    if (!coords(F, i, j, k, v)) return;
     if (F.inv[v] == 0.f) return;
-    int i, j, k;
-    decode(F, v, i, j, k);
-    const long I = i / fx + long(CX) * (j / fy + long(CY) * (k / fz));
+    const int I = (i >> sx) + CX * ((j >> sy) + CY * (k >> sz));
     x[v] = fmaf(scale, xc[I], x[v]);
 }
 
 // Coarsest level: x[idx[r]] = sum_k inv[r][k] b[idx[k]], one warp per row,
 // lane l adds k = l, l + 32, ... then an xor-tree.
 __global__ void __launch_bounds__(256) mg_coarse_kernel(const float* __restrict__ inv, const int* __restrict__ idx,
-                                                        int nc, const float* __restrict__ b, float* __restrict__ x,
-                                                        const MgScalars* sc) {
-    if (sc->done) return;
+                                                        int nc, const float* __restrict__ b, float* __restrict__ x) {
     const int row = int((long(blockIdx.x) * 256 + threadIdx.x) >> 5);
     const int lane = threadIdx.x & 31;
     if (row >= nc) return;
@@ -177,7 +294,99 @@ __global__ void __launch_bounds__(256) mg_coarse_kernel(const float* __restrict_
     if (lane == 0) x[idx[row]] = s;
 }
 
-// ---------------------------------------------------------- FP64 PCG -----
+// ------------------------------------------------------- FP32 inner PCG --
+// New direction and its image in one pass: p = z + beta p_old is formed at
+// the seven stencil points, q = A p on the active voxels (0 on holes); p.q
+// and q.z -> alpha.  p alternates between two buffers by iteration parity
+// (p_old = pb[k & 1], p = pb[(k + 1) & 1]), so a fixed kernel sequence serves
+// every iteration.
+template <bool Uniform>
+__global__ void __launch_bounds__(256) mg_spmv_kernel(Lv L, const float* __restrict__ z, float* __restrict__ pb,
+                                                      float* __restrict__ q, double* part, MgScalars* sc) {
+    __shared__ float wsf[256];
+    __shared__ double ws[256];
+    const int it = sc->k;
+    const float beta = it == 0 ? 0.f : float(sc->beta);
+    const float* __restrict__ pold = pb + size_t(it & 1) * L.V;
+    float* __restrict__ pnew = pb + size_t((it + 1) & 1) * L.V;
+    auto pv = [&](int u) { return fmaf(beta, pold[u], z[u]); };
+    float spq = 0.f, sqz = 0.f;
+#pragma unroll
+    for (int kz = 0; kz < kZB; ++kz) {
+        int i, j, k, v;
+        if (!coords_sum(L, kz, i, j, k, v)) continue;
+        const float pc = pv(v);
+        float qv = 0.f;
+        if (L.inv[v] != 0.f) qv = apply_A<Uniform>(L, i, j, k, v, pv);
+        pnew[v] = pc;
+        q[v] = qv;
+        spq = fmaf(pc, qv, spq);
+        sqz = fmaf(qv, z[v], sqz);
+    }
+    const float b0 = block_tree_f(spq, wsf);
+    const float b1 = block_tree_f(sqz, wsf);
+    const int nb = int(grid_blocks());
+    if (flat_tid() == 0) {
+        part[flat_bid()] = double(b0);
+        part[nb + flat_bid()] = double(b1);
+    }
+    if (arrive_last(&sc->ticket)) {
+        const double pq = final_sum(part, nb, ws);
+        const double qz = final_sum(part + nb, nb, ws);
+        if (flat_tid() == 0) {
+            sc->qz = qz;
+            if (pq > 0.0 && sc->rz > 0.0) {
+                sc->alpha = sc->rz / pq;
+            } else {  // breakdown: the direction carries no energy
+                sc->alpha = 0.0;
+                sc->idone = 1;
+            }
+        }
+    }
+}
+
+// d += alpha p, r -= alpha q, r.r; ends the inner loop on convergence or at
+// the iteration caps (graph: through the loop's condition).
+__global__ void __launch_bounds__(256) mg_axpy_kernel(Lv L, float* __restrict__ d, float* __restrict__ r,
+                                                      const float* __restrict__ pb, const float* __restrict__ q,
+                                                      double* part, MgScalars* sc, unsigned int* guard,
+                                                      int maxit, cudaGraphConditionalHandle inner, int graph) {
+    __shared__ float wsf[256];
+    __shared__ double ws[256];
+    const float alpha = float(sc->alpha);
+    const float* __restrict__ p = pb + size_t((sc->k + 1) & 1) * L.V;
+    float srr = 0.f;
+#pragma unroll
+    for (int kz = 0; kz < kZB; ++kz) {
+        int i, j, k, v;
+        if (!coords_sum(L, kz, i, j, k, v)) continue;
+        d[v] = fmaf(alpha, p[v], d[v]);
+        const float rv = fmaf(-alpha, q[v], r[v]);
+        r[v] = rv;
+        srr = fmaf(rv, rv, srr);
+    }
+    const float bs = block_tree_f(srr, wsf);
+    if (flat_tid() == 0) part[flat_bid()] = double(bs);
+    if (arrive_last(&sc->ticket)) {
+        const double rr = final_sum(part, int(grid_blocks()), ws);
+        if (flat_tid() == 0) {
+            const int kk = sc->k + 1;
+            const int total = sc->total + 1;
+            const unsigned int g = *guard + 1u;
+            *guard = g;
+            sc->k = kk;
+            sc->total = total;
+            sc->irr = rr;
+            // caps written so that out-of-range counters also end the loop
+            const int done = sc->idone || !(rr > sc->ilim) || !(kk > 0 && kk < kInnerMax) ||
+                             !(total > 0 && total < maxit) || g >= unsigned(maxit);
+            sc->idone = done;
+            if (graph) cudaGraphSetConditional(inner, done ? 0u : 1u);
+        }
+    }
+}
+
+// ------------------------------------------------------- FP64 outer loop --
 template <bool Uniform>
 __device__ __forceinline__ double apply_M(const DMesh& m, const double* __restrict__ x, int c) {
     double s = m.Mdiag[c] * x[c];
@@ -189,11 +398,16 @@ __device__ __forceinline__ double apply_M(const DMesh& m, const double* __restri
     return s;
 }
 
+// r = b - M x; r.r (first: and b.b).  The last block closes the outer loop:
+// converged when ||r||2 <= tol ||b||2; otherwise the next inner solve gets
+// the power-of-two scale that brings r to unit RMS and the relative
+// reduction eta it needs (clamped to [kEtaMin, 0.5]).
 template <bool Uniform>
-__global__ void __launch_bounds__(256) mg_init_kernel(DMesh m, const double* __restrict__ b,
-                                                      const double* __restrict__ x, double* __restrict__ r,
-                                                      const int* __restrict__ vox, float* __restrict__ b0,
-                                                      double* part, MgScalars* sc, double tol, int maxit) {
+__global__ void __launch_bounds__(256) mg_residual_kernel(DMesh m, const double* __restrict__ b,
+                                                          const double* __restrict__ x, double* __restrict__ r,
+                                                          double* part, MgScalars* sc, int first, double tol,
+                                                          int maxit, unsigned int* guard,
+                                                          cudaGraphConditionalHandle outer, int graph) {
     __shared__ double ws[256];
     const int n = m.n_cells;
     const int nb = gridDim.x;
@@ -205,151 +419,97 @@ __global__ void __launch_bounds__(256) mg_init_kernel(DMesh m, const double* __r
         if (i < n) {
             const double ri = b[i] - apply_M<Uniform>(m, x, int(i));
             r[i] = ri;
-            b0[vox[i]] = float(ri);
             srr = fma(ri, ri, srr);
-            sbb = fma(b[i], b[i], sbb);
+            if (first) sbb = fma(b[i], b[i], sbb);
         }
     }
     const double b1 = block_tree(srr, ws);
-    const double b2 = block_tree(sbb, ws);
+    const double b2 = first ? block_tree(sbb, ws) : 0.0;
     if (threadIdx.x == 0) {
         part[blockIdx.x] = b1;
         part[nb + blockIdx.x] = b2;
     }
     if (arrive_last(&sc->ticket)) {
         const double rr = final_sum(part, nb, ws);
-        const double bb = final_sum(part + nb, nb, ws);
+        const double bb = first ? final_sum(part + nb, nb, ws) : 0.0;
         if (threadIdx.x == 0) {
+            if (first) {
+                sc->bb = bb;
+                sc->lim = (tol * tol) * bb;
+                sc->rr0 = rr;
+                sc->total = 0;
+                sc->outer = 0;
+                sc->maxit = maxit;
+                sc->rz = 0.0;
+                sc->alpha = 0.0;
+                sc->qz = 0.0;
+            } else {
+                sc->outer = sc->outer + 1;
+            }
             sc->rr = rr;
-            sc->rr0 = rr;
-            sc->bb = bb;
-            sc->lim = (tol * tol) * bb;
-            sc->k = 0;
-            sc->maxit = maxit;
-            sc->done = rr <= sc->lim ? 1 : 0;
-            sc->converged = sc->done;
-            sc->beta = 0.0;
+            const int conv = !(rr > sc->lim);
+            if (first) *guard = 0u;
+            const int t = sc->total, o = sc->outer;
+            const int done = conv || !(t >= 0 && t < maxit) || !(o >= 0 && o < kOuterMax) || !(rr == rr) ||
+                             *guard >= unsigned(maxit);
+            sc->converged = conv;
+            sc->done = done;
+            double scale = 1.0;
+            if (rr > 0.0) scale = ldexp(1.0, -ilogb(sqrt(rr / double(n))));
+            sc->scale = scale;
+            sc->inv_scale = 1.0 / scale;
+            const double need = rr > 0.0 ? 0.5 * sqrt(sc->lim / rr) : 1.0;
+            sc->eta = fmin(fmax(need, kEtaMin), 0.5);
+            if (graph) cudaGraphSetConditional(outer, done ? 0u : 1u);
         }
     }
 }
 
-// z = double(V-cycle result); partials of r.z and r.z_old; beta.
-__global__ void __launch_bounds__(256) mg_gather_kernel(int n, const int* __restrict__ vox,
-                                                        const float* __restrict__ xr, const double* __restrict__ r,
-                                                        double* __restrict__ z, double* part, MgScalars* sc) {
-    if (sc->done) return;
+// Level-0 inner residual r32 = scale * r (cells -> voxels), d = 0; r.r
+// starts the inner loop.
+__global__ void __launch_bounds__(256) mg_convert_kernel(int n, const int* __restrict__ vox,
+                                                         const double* __restrict__ r, float* __restrict__ r32,
+                                                         float* __restrict__ d, double* part, MgScalars* sc,
+                                                         int maxit, cudaGraphConditionalHandle inner, int graph) {
+    __shared__ float wsf[256];
     __shared__ double ws[256];
-    const int nb = gridDim.x;
-    const int first = sc->k == 0;
-    double s0 = 0.0, s1 = 0.0;
+    const double scale = sc->scale;
+    float srr = 0.f;
     const long base = long(blockIdx.x) * kChunk + threadIdx.x;
 #pragma unroll
     for (int j = 0; j < kItems; ++j) {
         const long i = base + j * 256;
         if (i < n) {
-            const double zi = double(xr[vox[i]]);
-            const double ri = r[i];
-            if (!first) s1 = fma(ri, z[i], s1);
-            s0 = fma(ri, zi, s0);
-            z[i] = zi;
+            const int v = vox[i];
+            const float rv = float(r[i] * scale);
+            r32[v] = rv;
+            d[v] = 0.f;
+            srr = fmaf(rv, rv, srr);
         }
     }
-    const double b0 = block_tree(s0, ws);
-    const double b1 = block_tree(s1, ws);
-    if (threadIdx.x == 0) {
-        part[blockIdx.x] = b0;
-        part[nb + blockIdx.x] = b1;
-    }
+    const float bs = block_tree_f(srr, wsf);
+    if (threadIdx.x == 0) part[blockIdx.x] = double(bs);
     if (arrive_last(&sc->ticket)) {
-        const double rz = final_sum(part, nb, ws);
-        const double rzo = final_sum(part + nb, nb, ws);
+        const double rr = final_sum(part, gridDim.x, ws);
         if (threadIdx.x == 0) {
-            sc->beta = first ? 0.0 : (rz - rzo) / sc->rz;
-            sc->rz = rz;
+            sc->irr = rr;
+            sc->ilim = sc->eta * sc->eta * rr;
+            sc->k = 0;
+            const int t = sc->total;
+            const int done = !(rr > 0.0) || !(t >= 0 && t < maxit);
+            sc->idone = done;
+            if (graph) cudaGraphSetConditional(inner, done ? 0u : 1u);
         }
     }
 }
 
-__global__ void __launch_bounds__(256) mg_direction_kernel(int n, const double* __restrict__ z, double* __restrict__ p,
-                                                           const MgScalars* sc) {
-    if (sc->done) return;
+// x += d / scale (FP64).
+__global__ void __launch_bounds__(256) mg_update_kernel(int n, const int* __restrict__ vox,
+                                                        const float* __restrict__ d, double* __restrict__ x,
+                                                        const MgScalars* sc) {
     const long i = long(blockIdx.x) * 256 + threadIdx.x;
     if (i >= n) return;
-    p[i] = sc->k == 0 ? z[i] : fma(sc->beta, p[i], z[i]);
-}
-
-template <bool Uniform>
-__global__ void __launch_bounds__(256) mg_spmv_kernel(DMesh m, const double* __restrict__ p, double* __restrict__ q,
-                                                      double* part, MgScalars* sc) {
-    if (sc->done) return;
-    __shared__ double ws[256];
-    const int n = m.n_cells;
-    const int nb = gridDim.x;
-    double s = 0.0;
-    const long base = long(blockIdx.x) * kChunk + threadIdx.x;
-#pragma unroll
-    for (int j = 0; j < kItems; ++j) {
-        const long i = base + j * 256;
-        if (i < n) {
-            const double qi = apply_M<Uniform>(m, p, int(i));
-            q[i] = qi;
-            s = fma(p[i], qi, s);
-        }
-    }
-    const double bs = block_tree(s, ws);
-    if (threadIdx.x == 0) part[blockIdx.x] = bs;
-    if (arrive_last(&sc->ticket)) {
-        const double pq = final_sum(part, nb, ws);
-        if (threadIdx.x == 0) {
-            if (pq > 0.0) {
-                sc->alpha = sc->rz / pq;
-            } else {  // breakdown: the preconditioned direction has no energy
-                sc->alpha = 0.0;
-                sc->done = 1;
-                sc->converged = 0;
-            }
-        }
-    }
-}
-
-__global__ void __launch_bounds__(256) mg_axpy_kernel(int n, double* __restrict__ x, double* __restrict__ r,
-                                                      const double* __restrict__ p, const double* __restrict__ q,
-                                                      const int* __restrict__ vox, float* __restrict__ b0,
-                                                      double* part, MgScalars* sc) {
-    if (sc->done) return;
-    __shared__ double ws[256];
-    const int nb = gridDim.x;
-    const double alpha = sc->alpha;
-    double s = 0.0;
-    const long base = long(blockIdx.x) * kChunk + threadIdx.x;
-#pragma unroll
-    for (int j = 0; j < kItems; ++j) {
-        const long i = base + j * 256;
-        if (i < n) {
-            x[i] = fma(alpha, p[i], x[i]);
-            const double ri = fma(-alpha, q[i], r[i]);
-            r[i] = ri;
-            b0[vox[i]] = float(ri);
-            s = fma(ri, ri, s);
-        }
-    }
-    const double bs = block_tree(s, ws);
-    if (threadIdx.x == 0) part[blockIdx.x] = bs;
-    if (arrive_last(&sc->ticket)) {
-        const double rr = final_sum(part, nb, ws);
-        if (threadIdx.x == 0) {
-            const int k = sc->k + 1;
-            sc->k = k;
-            sc->rr = rr;
-            if (rr <= sc->lim) {
-                sc->done = 1;
-                sc->converged = 1;
-            } else if (k >= sc->maxit) {
-                sc->done = 1;
-                sc->converged = 0;
-            }
-        }
-    }
+    x[i] = fma(double(d[vox[i]]), sc->inv_scale, x[i]);
 }
 
 inline int nblk(long n, int bs) { return int((n + bs - 1) / bs); }
@@ -421,7 +581,7 @@ T* MultigridPCG::dalloc(size_t n) {
 }
 
 MultigridPCG::~MultigridPCG() {
-    if (graph_) cudaGraphExecDestroy(graph_);
+    if (exec_) cudaGraphExecDestroy(exec_);
     for (void* p : dev_) cudaFree(p);
     if (sc_host_) cudaFreeHost(sc_host_);
 }
@@ -429,11 +589,17 @@ MultigridPCG::~MultigridPCG() {
 bool MultigridPCG::init(const pg::HexMesh& m, const std::vector<double>& Mdiag, const std::vector<double>& Moff,
                         const MgSettings& set, std::string* msg) {
     set_ = set;
+    const char* g = std::getenv("PICGPU_MG_GRAPH");
+    use_graph_ = !(g && g[0] == '0');
     set_.pre = std::max(1, std::min(set_.pre, 8));
     set_.post = std::max(0, std::min(set_.post, 8));
     set_.coarsest = std::max(1, std::min(set_.coarsest, 4096));
-    const long V0 = long(m.n[0]) * m.n[1] * m.n[2];
-    if (V0 <= 0 || long(m.grid_cell.size()) != V0 || long(m.cell_ijk.size()) != 3L * m.n_cells) {
+    const long G0 = long(m.n[0]) * m.n[1] * m.n[2];
+    if (G0 >= (1L << 31) || m.n[2] > 65535) {
+        *msg = "multigrid preconditioner: at most 2^31 block cells and 65535 cells along z";
+        return false;
+    }
+    if (G0 <= 0 || long(m.grid_cell.size()) != G0 || long(m.cell_ijk.size()) != 3L * m.n_cells) {
         *msg = "multigrid preconditioner needs a block mesh";
         return false;
     }
@@ -445,10 +611,10 @@ bool MultigridPCG::init(const pg::HexMesh& m, const std::vector<double>& Mdiag, 
             L.n[a] = m.n[a];
             L.cyc[a] = m.cyclic[a];
         }
-        L.V = V0;
-        L.diag.assign(V0, 1.0);
-        L.off.assign(6 * size_t(V0), 0.0);
-        L.act.assign(V0, 0);
+        L.V = G0;
+        L.diag.assign(G0, 1.0);
+        L.off.assign(6 * size_t(G0), 0.0);
+        L.act.assign(G0, 0);
         for (int c = 0; c < m.n_cells; ++c) {
             const int i = m.cell_ijk[3 * size_t(c)], j = m.cell_ijk[3 * size_t(c) + 1],
                       k = m.cell_ijk[3 * size_t(c) + 2];
@@ -463,7 +629,7 @@ bool MultigridPCG::init(const pg::HexMesh& m, const std::vector<double>& Mdiag, 
                     *msg = "multigrid preconditioner: mesh neighbours do not follow the block grid";
                     return false;
                 }
-                L.off[f * size_t(V0) + v] = Moff[6 * size_t(c) + f];
+                L.off[f * size_t(G0) + v] = Moff[6 * size_t(c) + f];
             }
         }
     }
@@ -614,18 +780,25 @@ bool MultigridPCG::init(const pg::HexMesh& m, const std::vector<double>& Mdiag, 
     for (int c = 0; c < m.n_cells; ++c)
         vox[c] = int(vidx(hl[0], m.cell_ijk[3 * size_t(c)], m.cell_ijk[3 * size_t(c) + 1],
                           m.cell_ijk[3 * size_t(c) + 2]));
-    const int nb = pcg_blocks(m.n_cells);
+    const long V0 = hl[0].V;
+    // block partials: the widest reduction launch (cells, or the level-0 grid)
+    const long nbmax = std::max<long>(pcg_blocks(m.n_cells), shape(lv_[0]).blocks);
+    part_cap_ = 2 * nbmax + 8;
     if (!(cidx_ = dalloc<int>(nc_)) || !(cinv_ = dalloc<float>(size_t(nc_) * nc_)) ||
-        !(vox_ = dalloc<int>(m.n_cells)) || !(r_ = dalloc<double>(m.n_cells)) || !(z_ = dalloc<double>(m.n_cells)) ||
-        !(p_ = dalloc<double>(m.n_cells)) || !(q_ = dalloc<double>(m.n_cells)) ||
-        !(part_ = dalloc<double>(2 * size_t(nb) + 8)) || !(sc_ = dalloc<MgScalars>(1))) {
+        !(vox_ = dalloc<int>(m.n_cells)) || !(r64_ = dalloc<double>(m.n_cells)) || !(d_ = dalloc<float>(V0)) ||
+        !(p_ = dalloc<float>(2 * V0)) || !(q_ = dalloc<float>(V0)) || !(part_ = dalloc<double>(size_t(part_cap_))) ||
+        !(sc_ = dalloc<MgScalars>(1)) || !(guard_ = dalloc<unsigned int>(1))) {
         *msg = "multigrid preconditioner: out of device memory";
         return false;
     }
+    cudaMemset(d_, 0, V0 * sizeof(float));
+    cudaMemset(p_, 0, 2 * V0 * sizeof(float));
+    cudaMemset(q_, 0, V0 * sizeof(float));
     cudaMemcpy(cidx_, cidx.data(), nc_ * sizeof(int), cudaMemcpyHostToDevice);
     cudaMemcpy(cinv_, cinv.data(), cinv.size() * sizeof(float), cudaMemcpyHostToDevice);
     cudaMemcpy(vox_, vox.data(), vox.size() * sizeof(int), cudaMemcpyHostToDevice);
     cudaMemset(sc_, 0, sizeof(MgScalars));
+    cudaMemset(guard_, 0, sizeof(unsigned int));
     if (cudaMallocHost(&sc_host_, sizeof(MgScalars)) != cudaSuccess) {
         *msg = "multigrid preconditioner: out of pinned host memory";
         return false;
@@ -640,105 +813,233 @@ bool MultigridPCG::init(const pg::HexMesh& m, const std::vector<double>& Mdiag, 
 
 float* MultigridPCG::result(int l) const {
     if (l == int(lv_.size()) - 1) return lv_[l].x;
-    // pre sweeps leave the iterate in x (odd count) or t (even count); the
-    // prolongation adds into it; post sweeps alternate from there
-    const bool in_x = (set_.pre % 2 == 1) == (set_.post % 2 == 0);
-    return in_x ? lv_[l].x : lv_[l].t;
+    // the pre sweeps leave the iterate in x: a lone zero-guess sweep or the
+    // fused two-sweep kernel write x, each further sweep swaps x and t; the
+    // prolongation adds into it and each post sweep swaps again
+    const int swaps = std::max(0, set_.pre - 2) + set_.post;
+    return swaps % 2 == 0 ? lv_[l].x : lv_[l].t;
 }
 
 int MultigridPCG::vcycle(int l, cudaStream_t s) {
     const MgLevel& L = lv_[l];
     const Lv v = view(L);
+    const Shape sh = shape(L);
     const float om = float(set_.omega);
     if (l == int(lv_.size()) - 1) {
-        mg_coarse_kernel<<<nblk(32L * nc_, 256), 256, 0, s>>>(cinv_, cidx_, nc_, L.b, L.x, sc_);
-        return 1;
+        mg_coarse_kernel<<<nblk(32L * nc_, 256), 256, 0, s>>>(cinv_, cidx_, nc_, L.b, L.x);
+        if (l > 0) return 1;
+        const Shape ss = shape_sum(L);
+        mg_rz_kernel<<<ss.grid, ss.block, 0, s>>>(v, L.b, L.x, part_, sc_);
+        return 2;
     }
     int launched = 0;
-    const int g = nblk(L.V, 256);
     float* cur = L.x;
     float* oth = L.t;
-    mg_smooth0_kernel<<<g, 256, 0, s>>>(v, L.b, cur, om, sc_);
+    if (set_.pre == 1) {
+        mg_smooth0_kernel<<<sh.grid, sh.block, 0, s>>>(v, L.b, cur, om);
+    } else {
+        if (L.uniform) mg_smooth01_kernel<true><<<sh.grid, sh.block, 0, s>>>(v, L.b, cur, om);
+        else mg_smooth01_kernel<false><<<sh.grid, sh.block, 0, s>>>(v, L.b, cur, om);
+    }
     ++launched;
-    for (int it = 1; it < set_.pre; ++it) {
-        if (L.uniform) mg_smooth_kernel<true><<<g, 256, 0, s>>>(v, L.b, cur, oth, om, sc_);
-        else mg_smooth_kernel<false><<<g, 256, 0, s>>>(v, L.b, cur, oth, om, sc_);
+    for (int it = 2; it < set_.pre; ++it) {
+        if (L.uniform) mg_smooth_kernel<true><<<sh.grid, sh.block, 0, s>>>(v, L.b, cur, oth, om);
+        else mg_smooth_kernel<false><<<sh.grid, sh.block, 0, s>>>(v, L.b, cur, oth, om);
         std::swap(cur, oth);
         ++launched;
     }
     const MgLevel& C = lv_[l + 1];
     const Lv cv = view(C);
+    const Shape cs = shape(C);
+    const int sx = L.fac[0] - 1, sy = L.fac[1] - 1, sz = L.fac[2] - 1;
     if (L.uniform)
-        mg_restrict_kernel<true><<<nblk(C.V, 256), 256, 0, s>>>(v, cv, L.fac[0], L.fac[1], L.fac[2], L.b, cur, C.b,
-                                                                sc_);
+        mg_restrict_kernel<true><<<cs.grid, cs.block, 0, s>>>(v, cv, sx, sy, sz, L.b, cur, C.b);
     else
-        mg_restrict_kernel<false><<<nblk(C.V, 256), 256, 0, s>>>(v, cv, L.fac[0], L.fac[1], L.fac[2], L.b, cur, C.b,
-                                                                 sc_);
+        mg_restrict_kernel<false><<<cs.grid, cs.block, 0, s>>>(v, cv, sx, sy, sz, L.b, cur, C.b);
     ++launched;
     launched += vcycle(l + 1, s);
-    mg_prolong_kernel<<<g, 256, 0, s>>>(v, C.n[0], C.n[1], L.fac[0], L.fac[1], L.fac[2], result(l + 1), cur,
-                                        float(set_.scale), sc_);
+    mg_prolong_kernel<<<sh.grid, sh.block, 0, s>>>(v, C.n[0], C.n[1], sx, sy, sz, result(l + 1), cur,
+                                                  float(set_.scale));
     ++launched;
     for (int it = 0; it < set_.post; ++it) {
-        if (L.uniform) mg_smooth_kernel<true><<<g, 256, 0, s>>>(v, L.b, cur, oth, om, sc_);
-        else mg_smooth_kernel<false><<<g, 256, 0, s>>>(v, L.b, cur, oth, om, sc_);
+        const bool last0 = l == 0 && it == set_.post - 1;
+        if (last0) {
+            const Shape ss = shape_sum(L);
+            if (L.uniform) mg_smooth_dot_kernel<true><<<ss.grid, ss.block, 0, s>>>(v, L.b, cur, oth, om, part_, sc_);
+            else mg_smooth_dot_kernel<false><<<ss.grid, ss.block, 0, s>>>(v, L.b, cur, oth, om, part_, sc_);
+        } else {
+            if (L.uniform) mg_smooth_kernel<true><<<sh.grid, sh.block, 0, s>>>(v, L.b, cur, oth, om);
+            else mg_smooth_kernel<false><<<sh.grid, sh.block, 0, s>>>(v, L.b, cur, oth, om);
+        }
         std::swap(cur, oth);
+        ++launched;
+    }
+    if (l == 0 && set_.post == 0) {
+        const Shape ss = shape_sum(L);
+        mg_rz_kernel<<<ss.grid, ss.block, 0, s>>>(v, L.b, cur, part_, sc_);
         ++launched;
     }
     return launched;
 }
 
-int MultigridPCG::iteration(const DMesh& dm, double* x, cudaStream_t s) {
-    const int n = n_cells_;
-    const int nb = pcg_blocks(n);
+// One inner iteration: V-cycle (ends with r.z and beta), direction + A p,
+// update of d and r.
+int MultigridPCG::inner_iteration(cudaStream_t s, int maxit, cudaGraphConditionalHandle h_inner, int graph) {
+    const MgLevel& L0 = lv_[0];
+    const Lv v0 = view(L0);
+    const Shape sh = shape_sum(L0);
     int launched = vcycle(0, s);
-    mg_gather_kernel<<<nb, 256, 0, s>>>(n, vox_, result(0), r_, z_, part_, sc_);
-    mg_direction_kernel<<<nblk(n, 256), 256, 0, s>>>(n, z_, p_, sc_);
-    if (dm.lap_uniform) mg_spmv_kernel<true><<<nb, 256, 0, s>>>(dm, p_, q_, part_, sc_);
-    else mg_spmv_kernel<false><<<nb, 256, 0, s>>>(dm, p_, q_, part_, sc_);
-    mg_axpy_kernel<<<nb, 256, 0, s>>>(n, x, r_, p_, q_, vox_, lv_[0].b, part_, sc_);
-    return launched + 4;
+    float* z = result(0);
+    if (L0.uniform) mg_spmv_kernel<true><<<sh.grid, sh.block, 0, s>>>(v0, z, p_, q_, part_, sc_);
+    else mg_spmv_kernel<false><<<sh.grid, sh.block, 0, s>>>(v0, z, p_, q_, part_, sc_);
+    mg_axpy_kernel<<<sh.grid, sh.block, 0, s>>>(v0, d_, L0.b, p_, q_, part_, sc_, guard_, maxit, h_inner, graph);
+    return launched + 2;
 }
 
-cudaError_t MultigridPCG::solve(const DMesh& dm, const double* b, double* x, double tol, int maxit,
-                                cudaStream_t s, int* iters, double* rr0, double* rr, double* bb, bool* converged) {
+void MultigridPCG::residual(const DMesh& dm, const double* b, double* x, int first, double tol, int maxit,
+                            cudaStream_t s, cudaGraphConditionalHandle h_outer, int graph) {
+    const int nbc = pcg_blocks(n_cells_);
+    if (dm.lap_uniform)
+        mg_residual_kernel<true><<<nbc, 256, 0, s>>>(dm, b, x, r64_, part_, sc_, first, tol, maxit, guard_, h_outer,
+                                                      graph);
+    else
+        mg_residual_kernel<false><<<nbc, 256, 0, s>>>(dm, b, x, r64_, part_, sc_, first, tol, maxit, guard_, h_outer,
+                                                       graph);
+}
+
+// The solve graph:
+//   residual(first) -> while (outer) { convert -> while (inner) { V-cycle,
+//   direction + A p, axpy } -> update -> residual }
+cudaError_t MultigridPCG::build_graph(const DMesh& dm, const double* b, double* x, double tol, int maxit,
+                                      cudaStream_t s) {
+    if (exec_) {
+        cudaGraphExecDestroy(exec_);
+        exec_ = nullptr;
+    }
     const int n = n_cells_;
-    const int nb = pcg_blocks(n);
-    if (graph_ && (graph_b_ != b || graph_x_ != x)) {
-        cudaGraphExecDestroy(graph_);
-        graph_ = nullptr;
-    }
-    if (!graph_) {
-        cudaGraph_t g;
-        cudaError_t e = cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal);
-        if (e != cudaSuccess) return e;
-        graph_launches_ = 0;
-        for (int it = 0; it < kGraphIters; ++it) graph_launches_ += iteration(dm, x, s);
-        e = cudaStreamEndCapture(s, &g);
-        if (e != cudaSuccess) return e;
-        e = cudaGraphInstantiate(&graph_, g, 0);
-        cudaGraphDestroy(g);
-        if (e != cudaSuccess) return e;
-        graph_b_ = b;
-        graph_x_ = x;
-    }
-    if (dm.lap_uniform) mg_init_kernel<true><<<nb, 256, 0, s>>>(dm, b, x, r_, vox_, lv_[0].b, part_, sc_, tol, maxit);
-    else mg_init_kernel<false><<<nb, 256, 0, s>>>(dm, b, x, r_, vox_, lv_[0].b, part_, sc_, tol, maxit);
-    ++launches;
-    cudaError_t e = cudaMemcpyAsync(sc_host_, sc_, sizeof(MgScalars), cudaMemcpyDeviceToHost, s);
-    if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+    const int nbc = pcg_blocks(n);
+    const cudaStreamCaptureMode mode = cudaStreamCaptureModeThreadLocal;
+    cudaGraph_t main = nullptr;
+    cudaError_t e = cudaGraphCreate(&main, 0);
     if (e != cudaSuccess) return e;
-    int replayed = 0;
-    while (!sc_host_->done && replayed < maxit) {
-        e = cudaGraphLaunch(graph_, s);
-        if (e != cudaSuccess) return e;
-        replayed += kGraphIters;
-        launches += graph_launches_;
-        e = cudaMemcpyAsync(sc_host_, sc_, sizeof(MgScalars), cudaMemcpyDeviceToHost, s);
-        if (e == cudaSuccess) e = cudaStreamSynchronize(s);
-        if (e != cudaSuccess) return e;
+    auto fail = [&](cudaError_t err) {
+        cudaGraphDestroy(main);
+        return err;
+    };
+    cudaGraphConditionalHandle h_outer, h_inner;
+    if ((e = cudaGraphConditionalHandleCreate(&h_outer, main, 0, cudaGraphCondAssignDefault))) return fail(e);
+    // captured kernels go into `g` after `deps`; `tail` receives the last nodes
+    auto capture = [&](cudaGraph_t g, const std::vector<cudaGraphNode_t>& deps, auto&& body,
+                       std::vector<cudaGraphNode_t>* tail) -> cudaError_t {
+        cudaError_t err = cudaStreamBeginCaptureToGraph(s, g, deps.empty() ? nullptr : deps.data(), nullptr,
+                                                        deps.size(), mode);
+        if (err != cudaSuccess) return err;
+        body();
+        if (tail) {
+            cudaStreamCaptureStatus st;
+            const cudaGraphNode_t* d = nullptr;
+            size_t nd = 0;
+            err = cudaStreamGetCaptureInfo(s, &st, nullptr, nullptr, &d, nullptr, &nd);
+            if (err == cudaSuccess) tail->assign(d, d + nd);
+        }
+        cudaGraph_t out = g;
+        const cudaError_t err2 = cudaStreamEndCapture(s, &out);
+        return err != cudaSuccess ? err : err2;
+    };
+    auto add_while = [&](cudaGraph_t g, const std::vector<cudaGraphNode_t>& deps, cudaGraphConditionalHandle h,
+                         cudaGraphNode_t* node, cudaGraph_t* body) -> cudaError_t {
+        cudaGraphNodeParams np{};
+        np.type = cudaGraphNodeTypeConditional;
+        np.conditional.handle = h;
+        np.conditional.type = cudaGraphCondTypeWhile;
+        np.conditional.size = 1;
+        const cudaError_t err = cudaGraphAddNode(node, g, deps.empty() ? nullptr : deps.data(), nullptr,
+                                                 deps.size(), &np);
+        if (err == cudaSuccess) *body = np.conditional.phGraph_out[0];
+        return err;
+    };
+    std::vector<cudaGraphNode_t> tail;
+    e = capture(main, {}, [&] { residual(dm, b, x, 1, tol, maxit, s, h_outer, 1); }, &tail);
+    if (e) return fail(e);
+    cudaGraphNode_t w_outer, w_inner;
+    cudaGraph_t body_outer, body_inner;
+    if ((e = add_while(main, tail, h_outer, &w_outer, &body_outer))) return fail(e);
+    if ((e = cudaGraphConditionalHandleCreate(&h_inner, body_outer, 0, cudaGraphCondAssignDefault))) return fail(e);
+    e = capture(body_outer, {}, [&] {
+        mg_convert_kernel<<<nbc, 256, 0, s>>>(n, vox_, r64_, lv_[0].b, d_, part_, sc_, maxit, h_inner, 1);
+    }, &tail);
+    if (e) return fail(e);
+    if ((e = add_while(body_outer, tail, h_inner, &w_inner, &body_inner))) return fail(e);
+    int inner = 0;
+    e = capture(body_inner, {}, [&] { inner = inner_iteration(s, maxit, h_inner, 1); }, nullptr);
+    if (e) return fail(e);
+    e = capture(body_outer, {w_inner}, [&] {
+        mg_update_kernel<<<nblk(n, 256), 256, 0, s>>>(n, vox_, d_, x, sc_);
+        residual(dm, b, x, 0, tol, maxit, s, h_outer, 1);
+    }, nullptr);
+    if (e) return fail(e);
+    e = cudaGraphInstantiate(&exec_, main, 0);
+    cudaGraphDestroy(main);
+    if (e != cudaSuccess) return e;
+    inner_launches_ = inner;
+    outer_launches_ = 3;
+    graph_b_ = b;
+    graph_x_ = x;
+    graph_tol_ = tol;
+    graph_maxit_ = maxit;
+    return cudaSuccess;
+}
+
+// The same kernel sequence driven from the host, which reads the loop flags
+// after each closing kernel (used when graphs are switched off, e.g. for
+// kernel profilers that cannot see into conditional graph nodes).
+cudaError_t MultigridPCG::solve_eager(const DMesh& dm, const double* b, double* x, double tol, int maxit,
+                                      cudaStream_t s) {
+    const int n = n_cells_;
+    const int nbc = pcg_blocks(n);
+    auto read = [&]() {
+        cudaError_t e = cudaMemcpyAsync(sc_host_, sc_, sizeof(MgScalars), cudaMemcpyDeviceToHost, s);
+        return e == cudaSuccess ? cudaStreamSynchronize(s) : e;
+    };
+    cudaError_t e;
+    residual(dm, b, x, 1, tol, maxit, s, 0, 0);
+    launches += 1;
+    if ((e = read())) return e;
+    while (!sc_host_->done) {
+        mg_convert_kernel<<<nbc, 256, 0, s>>>(n, vox_, r64_, lv_[0].b, d_, part_, sc_, maxit, 0, 0);
+        launches += 1;
+        if ((e = read())) return e;
+        while (!sc_host_->idone) {
+            launches += inner_iteration(s, maxit, 0, 0);
+            if ((e = read())) return e;
+        }
+        mg_update_kernel<<<nblk(n, 256), 256, 0, s>>>(n, vox_, d_, x, sc_);
+        residual(dm, b, x, 0, tol, maxit, s, 0, 0);
+        launches += 2;
+        if ((e = read())) return e;
     }
-    *iters = sc_host_->k;
+    return cudaGetLastError();
+}
+
+cudaError_t MultigridPCG::solve(const DMesh& dm, const double* b, double* x, double tol, int maxit, cudaStream_t s,
+                                int* iters, int* outer, double* rr0, double* rr, double* bb, bool* converged) {
+    cudaError_t e;
+    // every reduction launch must fit the partials buffer
+    if (2L * std::max<long>(pcg_blocks(n_cells_), shape(lv_[0]).blocks) + 8 > part_cap_ || maxit < 1)
+        return cudaErrorInvalidValue;
+    if (use_graph_) {
+        if (!exec_ || graph_b_ != b || graph_x_ != x || graph_tol_ != tol || graph_maxit_ != maxit)
+            if ((e = build_graph(dm, b, x, tol, maxit, s)) != cudaSuccess) return e;
+        if ((e = cudaGraphLaunch(exec_, s)) != cudaSuccess) return e;
+        if ((e = cudaMemcpyAsync(sc_host_, sc_, sizeof(MgScalars), cudaMemcpyDeviceToHost, s)) != cudaSuccess)
+            return e;
+        if ((e = cudaStreamSynchronize(s)) != cudaSuccess) return e;
+        launches += 1 + int64_t(sc_host_->outer) * outer_launches_ + int64_t(sc_host_->total) * inner_launches_;
+    } else if ((e = solve_eager(dm, b, x, tol, maxit, s)) != cudaSuccess) {
+        return e;
+    }
+    *iters = sc_host_->total;
+    *outer = sc_host_->outer;
     *rr0 = sc_host_->rr0;
     *rr = sc_host_->rr;
     *bb = sc_host_->bb;
