@@ -21,6 +21,7 @@
 
 #include "oracle.h"
 #include "collisions.hpp"
+#include "picgpu_init.h"
 #include "../picfoam_gb300/csrc/hexmesh.hpp"
 
 #include <algorithm>
@@ -1418,6 +1419,389 @@ void fill_counts(const Oracle& o, picgpu_step_stats* st) {
 
 }  // namespace
 
+// ------------------------------------------------ initial conditions -----
+// picInitialise (preProcess/picInitialise/picInitialise.C:30-319) with the
+// InitializationModel sub-models Equipartition
+// (EquipartitionInitialization.C:65-141), Maxwellian
+// (MaxwellianInitialization.C:73-126), Isotropization
+// (IsotropizationInitialization.C:52-123), QuasineutralPlasma
+// (QuasineutralPlasmaInitialization.C:38-175) and UniformDisplacement
+// (UniformInitialization.C:51-127).  Within a species the particles are added
+// in picFoam's order (cell, tet, particle; or cell, particle; or the lattice
+// order i, j, k).  picFoam draws every number from one sequential
+// Foam::Random; here each tet (cell, lattice point) of each species has its
+// own Philox stream, so the CUDA kernels can place the particles in parallel
+// and still draw the same numbers.  Normal variates: Marsaglia's polar
+// method; the logarithm and the sine are evaluated in fixed FP64 operations
+// (atanh series after frexp, Taylor series after reduction by pi) so that no
+// math library enters the result.  Points in a tet: the cube-folding method
+// of Rocchini & Cignoni (J. Graphics Tools 5(4), 2000).
+namespace oinit {
+
+double det_log(double x) {
+    int e;
+    double m = std::frexp(x, &e);
+    if (m < 0.70710678118654752440) {
+        m = m * 2.0;
+        e = e - 1;
+    }
+    const double z = (m - 1.0) / (m + 1.0);
+    const double w = z * z;
+    const double inv_odd[11] = {1.0 / 23.0, 1.0 / 21.0, 1.0 / 19.0, 1.0 / 17.0, 1.0 / 15.0, 1.0 / 13.0,
+                                1.0 / 11.0, 1.0 / 9.0,  1.0 / 7.0,  1.0 / 5.0,  1.0 / 3.0};
+    double p = inv_odd[0];
+    for (int i = 1; i < 11; ++i) p = p * w + inv_odd[i];
+    const double lm = 2.0 * z + 2.0 * z * (w * p);
+    return double(e) * 0.69314718055994530942 + lm;
+}
+
+double det_sin(double x) {
+    const double pi_hi = 3.141592653589793116, pi_lo = 1.2246467991473532e-16;
+    const double k = std::rint(x / pi_hi);
+    const double r = (x - k * pi_hi) - k * pi_lo;
+    const double w = r * r;
+    // -1/23!, 1/21!, ..., -1/3!
+    const double c[11] = {-1.0 / 25852016738884976640000.0, 1.0 / 51090942171709440000.0,
+                          -1.0 / 121645100408832000.0,      1.0 / 355687428096000.0,
+                          -1.0 / 1307674368000.0,           1.0 / 6227020800.0,
+                          -1.0 / 39916800.0,                1.0 / 362880.0,
+                          -1.0 / 5040.0,                    1.0 / 120.0,
+                          -1.0 / 6.0};
+    double p = c[0];
+    for (int i = 1; i < 11; ++i) p = p * w + c[i];
+    const double s = r + r * (w * p);
+    return ((long long)k & 1) ? -s : s;
+}
+
+void polar_pair(ocoll::Philox& r, double& n1, double& n2) {
+    for (int a = 0; a < 64; ++a) {
+        const double u1 = 2.0 * r.uniform() - 1.0;
+        const double u2 = 2.0 * r.uniform() - 1.0;
+        const double s = u1 * u1 + u2 * u2;
+        if (s > 0.0 && s < 1.0) {
+            const double f = std::sqrt(-2.0 * det_log(s) / s);
+            n1 = u1 * f;
+            n2 = u2 * f;
+            return;
+        }
+    }
+    n1 = n2 = 0.0;
+}
+
+// sampleNormal<vector>
+V3 normal3(ocoll::Philox& r) {
+    double a, b, c, d;
+    polar_pair(r, a, b);
+    polar_pair(r, c, d);
+    return v3(a, b, c);
+}
+
+// tetPointRef::randomPoint as barycentric coordinates 1..3 of the tet
+void tet_point(ocoll::Philox& r, double* y) {
+    double s = r.uniform(), t = r.uniform(), u = r.uniform();
+    if (s + t > 1.0) {
+        s = 1.0 - s;
+        t = 1.0 - t;
+    }
+    if (t + u > 1.0) {
+        const double tmp = u;
+        u = 1.0 - s - t;
+        t = 1.0 - tmp;
+    } else if (s + t + u > 1.0) {
+        const double tmp = u;
+        u = s + t + u - 1.0;
+        s = 1.0 - t - tmp;
+    }
+    y[0] = s;
+    y[1] = t;
+    y[2] = u;
+}
+
+// The tet of cell c holding x (largest smallest coordinate), clamped and
+// renormalised coordinates; false when x is outside by more than 1e-9.
+bool locate_in_cell(const HexMesh& m, int c, const double* x, int& tet, double* y) {
+    double best_min = -1e300, by[3] = {0, 0, 0};
+    int best = -1;
+    for (int t = 0; t < 12; ++t) {
+        double q[3];
+        tet_coords(m, c, t, x, q);
+        const double q0 = 1.0 - q[0] - q[1] - q[2];
+        const double mn = std::fmin(std::fmin(q0, q[0]), std::fmin(q[1], q[2]));
+        if (mn > best_min) {
+            best_min = mn;
+            best = t;
+            by[0] = q[0];
+            by[1] = q[1];
+            by[2] = q[2];
+        }
+    }
+    if (best_min < -1e-9) return false;
+    const double y0 = 1.0 - by[0] - by[1] - by[2];
+    const double yy[4] = {std::fmax(y0, 0.0), std::fmax(by[0], 0.0), std::fmax(by[1], 0.0), std::fmax(by[2], 0.0)};
+    const double s = yy[0] + yy[1] + yy[2] + yy[3];
+    for (int a = 0; a < 3; ++a) y[a] = yy[a + 1] / s;
+    tet = best;
+    return true;
+}
+
+// meshTools::constrainDirection(mesh, solutionD, p): the point's components
+// along empty axes become zero; the point is then located in its cell again.
+bool constrain(const HexMesh& m, int c, int& t, double* y) {
+    const double* off = &m.cls_offset[size_t(m.cell_class[c]) * 24];
+    double x[3];
+    for (int a = 0; a < 3; ++a)
+        x[a] = m.cc[3 * size_t(c) + a] + y[0] * off[3 * m.tt.tri[t][0] + a] + y[1] * off[3 * m.tt.tri[t][1] + a] +
+               y[2] * off[3 * m.tt.tri[t][2] + a];
+    for (int a = 0; a < 3; ++a)
+        if (m.empty[a]) x[a] = 0.0;
+    return locate_in_cell(m, c, x, t, y);
+}
+
+struct Sampling {
+    double n = 0, w = 1, scale[3] = {0, 0, 0}, drift[3] = {0, 0, 0}, speed = 0, displacement = 0;
+    long long cell_count = 0;
+    bool place = false;
+};
+
+Parcel make_parcel(int c, int t, const double* y, V3 U) {
+    Parcel p;
+    p.cell = c;
+    p.tet = t;
+    p.y[1] = y[0];
+    p.y[2] = y[1];
+    p.y[3] = y[2];
+    p.y[0] = 1.0 - p.y[1] - p.y[2] - p.y[3];
+    p.U = U;
+    return p;
+}
+
+V3 velocity(const Sampling& q, ocoll::Philox& r) {
+    const V3 n = normal3(r);
+    return v3(q.scale[0] * n.x + q.drift[0], q.scale[1] * n.y + q.drift[1], q.scale[2] * n.z + q.drift[2]);
+}
+
+}  // namespace oinit
+
+int oracle_initialise_impl(Oracle& o, const picgpu_init* in, picgpu_init_stats* out) {
+    using namespace oinit;
+    const HexMesh& m = o.m;
+    const int ns = o.cfg.n_species, nc = m.n_cells;
+    if (in->model < PICGPU_INIT_NONE || in->model > PICGPU_INIT_UNIFORM_DISPLACEMENT) {
+        o.err = "initialise: unknown InitializationModel";
+        return PICGPU_INVALID_ARG;
+    }
+    picgpu_init_stats S{};
+    if (in->clear_particles)
+        for (auto& cl : o.cloud) cl.clear();
+    Sampling smp[PICGPU_MAX_SPECIES];
+    bool calc_T = false, calc_n = false;
+    for (int sp = 0; sp < ns; ++sp) {
+        const picgpu_species& P = o.cfg.species[sp];
+        Sampling& q = smp[sp];
+        q.n = in->number_density[sp];
+        q.w = P.weight;
+        // equipartitionLinearVelocity (PICCloud.C:1506-1515): sqrt(kT/m) N(0,1)^3
+        const double th = std::sqrt(kBoltzmann * in->temperature[sp] / P.mass);
+        switch (in->model) {
+            case PICGPU_INIT_EQUIPARTITION:  // EquipartitionInitialization.C:128-135: + velocity
+                for (int a = 0; a < 3; ++a) { q.scale[a] = th; q.drift[a] = in->velocity[a]; }
+                q.place = q.n > 0;
+                break;
+            case PICGPU_INIT_MAXWELLIAN:  // MaxwellianInitialization.C:112-119
+                for (int a = 0; a < 3; ++a) {
+                    q.scale[a] = in->thermal_velocity[sp][a];
+                    q.drift[a] = in->drift_velocity[sp][a];
+                }
+                q.place = q.n > 0;
+                calc_T = true;
+                break;
+            case PICGPU_INIT_ISOTROPIZATION: {  // IsotropizationInitialization.C:95-110
+                const double f = in->tperp_over_tpara;
+                if (!(f > 0)) { o.err = "initialise: Tperp_over_Tpara must be > 0"; return PICGPU_INVALID_ARG; }
+                const double T = in->temperature[sp];
+                q.scale[0] = std::sqrt(kBoltzmann * T / (((2.0 / 3.0) * f + (1.0 / 3.0)) * P.mass));
+                q.scale[1] = std::sqrt(kBoltzmann * T / (((2.0 / 3.0) + (1.0 / (3.0 * f))) * P.mass));
+                q.scale[2] = q.scale[1];
+                q.place = q.n > 0;
+                break;
+            }
+            case PICGPU_INIT_QUASINEUTRAL_PLASMA:
+                for (int a = 0; a < 3; ++a) q.scale[a] = th;
+                q.speed = std::sqrt(in->temperature[sp] * kBoltzmann * 3.0 / P.mass);
+                calc_n = true;
+                break;
+            case PICGPU_INIT_UNIFORM_DISPLACEMENT:
+                for (int a = 0; a < 3; ++a) q.scale[a] = th;
+                q.displacement = in->displacement[sp];
+                q.place = (in->species_mask >> sp) & 1;
+                calc_n = true;
+                break;
+            default:
+                calc_T = calc_n = true;
+                break;
+        }
+    }
+    if (in->model == PICGPU_INIT_QUASINEUTRAL_PLASMA) {
+        // QuasineutralPlasmaInitialization.C:38-80
+        const int ion = in->ion_species, el = o.cfg.electron_species;
+        if (ion < 0 || ion >= ns || el < 0 || el >= ns) { o.err = "initialise: species"; return PICGPU_INVALID_ARG; }
+        if (o.cfg.species[ion].charge + o.cfg.species[el].charge != 0.0) {
+            o.err = "initialise: ion and electron charge must be of same magnitude and opposite signs";
+            return PICGPU_INVALID_ARG;
+        }
+        for (int sp : {ion, el}) {
+            smp[sp].cell_count = (long long)(in->cell_count / o.cfg.species[sp].weight);
+            smp[sp].place = smp[sp].cell_count > 0;
+        }
+    }
+    const bool cons = m.empty[0] || m.empty[1] || m.empty[2];
+    for (int sp = 0; sp < ns && in->model != PICGPU_INIT_NONE; ++sp) {
+        const Sampling& q = smp[sp];
+        if (!q.place) continue;
+        auto& cl = o.cloud[sp];
+        const size_t before = cl.size();
+        if (in->model == PICGPU_INIT_QUASINEUTRAL_PLASMA) {
+            // QuasineutralPlasmaInitialization.C:102-175
+            for (int c = 0; c < nc; ++c)
+                for (long long k = 0; k < q.cell_count; ++k) {
+                    ocoll::Philox r(in->seed, ocoll::kStreamInitParticle | uint32_t(sp), uint32_t(c), uint32_t(k));
+                    int t = int((12.0 - 1.0) * r.uniform());  // label((cellTets.size()-1.0)*scalar01())
+                    double y[3];
+                    tet_point(r, y);
+                    if (cons && !constrain(m, c, t, y)) { o.err = "initialise: point left its cell"; return PICGPU_INVALID_ARG; }
+                    V3 U;
+                    if (in->use_maxwellian) {
+                        U = velocity(q, r);
+                    } else {
+                        const double d0 = r.uniform(), d1 = r.uniform(), d2 = r.uniform();
+                        const double inv = 1.0 / std::sqrt(d0 * d0 + d1 * d1 + d2 * d2);
+                        U = v3((d0 * inv) * q.speed, (d1 * inv) * q.speed, (d2 * inv) * q.speed);
+                    }
+                    cl.push_back(make_parcel(c, t, y, U));
+                }
+        } else if (in->model == PICGPU_INIT_UNIFORM_DISPLACEMENT) {
+            // UniformInitialization.C:60-125
+            double lo[3], hi[3], dir[3], span[3], delta[3];
+            const int gtop = grid_point_id(m, m.n[0], m.n[1], m.n[2]);
+            for (int a = 0; a < 3; ++a) {
+                lo[a] = in->use_bounds ? in->min[a] : m.grid_pts[a];
+                hi[a] = in->use_bounds ? in->max[a] : m.grid_pts[3 * size_t(gtop) + a];
+            }
+            const double dm = std::sqrt(in->displacement_dir[0] * in->displacement_dir[0] +
+                                        in->displacement_dir[1] * in->displacement_dir[1] +
+                                        in->displacement_dir[2] * in->displacement_dir[2]);
+            for (int a = 0; a < 3; ++a) dir[a] = in->displacement_dir[a] / dm;
+            for (int a = 0; a < 3; ++a) span[a] = hi[a] - lo[a];
+            const double span_len = span[0] * dir[0] + span[1] * dir[1] + span[2] * dir[2];
+            for (int a = 0; a < 3; ++a)
+                delta[a] = span[a] / double(std::max<long long>(in->particle_numbers[a] - 1, 2));
+            const long long nx = in->particle_numbers[0], ny = in->particle_numbers[1], nz = in->particle_numbers[2];
+            for (long long i = 0; i < nx; ++i)
+                for (long long j = 0; j < ny; ++j)
+                    for (long long k = 0; k < nz; ++k) {
+                        const long long idx = (i * ny + j) * nz + k;
+                        const double p[3] = {lo[0] + delta[0] * double(i), lo[1] + delta[1] * double(j),
+                                             lo[2] + delta[2] * double(k)};
+                        const double dist = (p[0] - lo[0]) * dir[0] + (p[1] - lo[1]) * dir[1] + (p[2] - lo[2]) * dir[2];
+                        const double cur = q.displacement * det_sin(dist / span_len * in->cycles * 3.141592653589793116);
+                        double x[3];
+                        for (int a = 0; a < 3; ++a) x[a] = p[a] + dir[a] * cur;
+                        double by[3];
+                        const long long tg = locate(m, x, by);  // mesh.findCell
+                        if (tg < 0) { o.err = "initialise: tried to create a particle outside of the mesh"; return PICGPU_INVALID_ARG; }
+                        int t = 0;
+                        double y[3];
+                        if (!locate_in_cell(m, int(tg / 12), x, t, y)) { o.err = "initialise: locate"; return PICGPU_INVALID_ARG; }
+                        ocoll::Philox r(in->seed, ocoll::kStreamInitLattice | uint32_t(sp), uint32_t(idx >> 32), uint32_t(idx));
+                        cl.push_back(make_parcel(int(tg / 12), t, y, velocity(q, r)));
+                    }
+        } else {
+            // per-tet models: particlesRequired = n V / w, floor plus one with
+            // probability of the remainder
+            for (int c = 0; c < nc; ++c)
+                for (int t = 0; t < 12; ++t) {
+                    const double V = tet_volume(m, m.cell_class[c], t);
+                    const double req = (q.n * V) / q.w;
+                    long long cnt = (long long)req;
+                    ocoll::Philox rc(in->seed, ocoll::kStreamInitCount | uint32_t(sp), uint32_t(c), uint32_t(t));
+                    if (req - double(cnt) > rc.uniform()) ++cnt;
+                    if (cnt >= (1LL << 24)) { o.err = "initialise: more than 2^24 particles in one tet"; return PICGPU_CAPACITY; }
+                    for (long long k = 0; k < cnt; ++k) {
+                        ocoll::Philox r(in->seed, ocoll::kStreamInitParticle | uint32_t(sp), uint32_t(c),
+                                        (uint32_t(t) << 24) | uint32_t(k));
+                        double y[3];
+                        tet_point(r, y);
+                        int tt = t;
+                        if (cons && !constrain(m, c, tt, y)) { o.err = "initialise: point left its cell"; return PICGPU_INVALID_ARG; }
+                        cl.push_back(make_parcel(c, tt, y, velocity(q, r)));
+                    }
+                }
+        }
+        S.added[sp] = (long long)(cl.size() - before);
+    }
+
+    // statistics (picInitialise.C:86-188)
+    double vol = 0, lsum = 0;
+    for (int c = 0; c < nc; ++c) {
+        vol += m.vol[c];
+        lsum += std::cbrt(m.vol[c]);
+    }
+    S.mesh_volume = vol;
+    S.average_cell_size = nc > 0 ? lsum / nc : 0.0;
+    for (int sp = 0; sp < ns; ++sp) {
+        const picgpu_species& P = o.cfg.species[sp];
+        std::vector<long long> occ(nc, 0);
+        double N = 0, vs = 0, d[3] = {0, 0, 0};
+        for (const Parcel& p : o.cloud[sp]) {
+            if (!p.alive) continue;
+            occ[p.cell]++;
+            N += P.weight;
+            d[0] += p.U.x * P.weight;
+            d[1] += p.U.y * P.weight;
+            d[2] += p.U.z * P.weight;
+            vs += dotv(p.U, p.U) * P.weight;
+        }
+        long long mn = nc > 0 ? (1LL << 62) : 0, mx = 0, sum = 0;
+        for (long long v : occ) { mn = std::min(mn, v); mx = std::max(mx, v); sum += v; }
+        S.occupancy_min[sp] = mn;
+        S.occupancy_max[sp] = mx;
+        S.occupancy_avg[sp] = nc > 0 ? double(sum) / nc : 0.0;
+        if (N > 0) {
+            double dd = 0;
+            for (int a = 0; a < 3; ++a) { S.drift[sp][a] = d[a] / N; dd += S.drift[sp][a] * S.drift[sp][a]; }
+            S.temperature[sp] = P.mass / (3.0 * kBoltzmann) * (vs / N - dd);
+        }
+        S.number_density[sp] = vol > 0 ? N / vol : 0.0;
+        S.model_temperature[sp] = calc_T ? S.temperature[sp] : in->temperature[sp];
+        S.model_number_density[sp] = calc_n ? S.number_density[sp] : in->number_density[sp];
+    }
+    const double eps0 = 1.0 / (kMu0 * kC * kC);
+    double inv_l2 = 0;
+    for (int sp = 0; sp < ns; ++sp) {
+        const double qq = o.cfg.species[sp].charge, T = S.model_temperature[sp], n = S.model_number_density[sp];
+        if (qq == 0.0 || n <= 0.0 || T <= 0.0) continue;
+        inv_l2 += n * qq * qq / eps0 / (T * kBoltzmann);
+    }
+    S.debye_length = inv_l2 > 0 ? std::sqrt(1.0 / inv_l2) : 0.0;
+    const int el = o.cfg.electron_species;
+    if (el >= 0 && el < ns && S.model_number_density[el] > 0) {
+        const double qq = o.cfg.species[el].charge;
+        S.plasma_frequency_dt = std::sqrt(S.model_number_density[el] * qq * qq / eps0 / o.cfg.species[el].mass) * o.cfg.dt;
+    }
+    // calculateFields, solveMaxwellEquations, initalizeLeapFrog (picInitialise.C:209-227)
+    calculate_fields(o);
+    if (in->solve_fields) {
+        const int r = solve_fields(o, nullptr);
+        if (r) return r;
+    }
+    if (in->leapfrog)
+        for (int sp = 0; sp < ns; ++sp)
+            for (Parcel& p : o.cloud[sp])
+                if (p.alive) push(o, p, sp, -0.5 * o.cfg.dt);
+    if (out) *out = S;
+    return 0;
+}
+
 struct oracle_ctx {
     Oracle o;
 };
@@ -1559,6 +1943,16 @@ int oracle_get_particles(oracle_ctx* ctx, int species, size_t cap, int32_t* tet,
         U[3 * i + 2] = cl[i].U.z;
     }
     return 0;
+}
+
+// The fixed-operation logarithm and sine of the initial-condition sampler
+// (accuracy checks against the C library in the tests).
+double oracle_det_log(double x) { return oinit::det_log(x); }
+double oracle_det_sin(double x) { return oinit::det_sin(x); }
+
+int oracle_initialise(oracle_ctx* ctx, const picgpu_init* init, picgpu_init_stats* stats) {
+    if (!ctx || !init) return PICGPU_INVALID_ARG;
+    return oracle_initialise_impl(ctx->o, init, stats);
 }
 
 int oracle_initialise_fields(oracle_ctx* ctx) {

@@ -18,6 +18,7 @@
 #define PICGPU_ORACLE_H
 
 #include "picgpu.h"
+#include "picgpu_init.h"
 
 #ifdef __cplusplus
 extern "C" {
@@ -43,6 +44,12 @@ int  oracle_count_particles(oracle_ctx* ctx, int species, size_t* n);
 int  oracle_get_particles(oracle_ctx* ctx, int species, size_t cap, int32_t* tet,
                           double* bary, double* U, size_t* n);
 int  oracle_initialise_fields(oracle_ctx* ctx);
+/* picInitialise restated (picgpu_initialise's oracle): places the particles
+ * of `init` in picFoam's order, reports the statistics, computes the fields,
+ * optionally solves them and applies the leapfrog back-step. */
+int  oracle_initialise(oracle_ctx* ctx, const picgpu_init* init, picgpu_init_stats* stats);
+double oracle_det_log(double x);
+double oracle_det_sin(double x);
 int  oracle_step(oracle_ctx* ctx, int nsteps, picgpu_step_stats* stats);
 int  oracle_move(oracle_ctx* ctx, picgpu_step_stats* stats);
 int  oracle_solve_poisson(oracle_ctx* ctx, const double* rho, double* phi_inout,

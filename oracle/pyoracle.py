@@ -53,6 +53,10 @@ def load():
         lib.oracle_move_seconds.argtypes = [P]
         lib.oracle_philox4x32.restype = None
         lib.oracle_philox4x32.argtypes = [C.POINTER(C.c_uint32), C.POINTER(C.c_uint32), C.POINTER(C.c_uint32)]
+        lib.oracle_det_log.restype = C.c_double
+        lib.oracle_det_log.argtypes = [C.c_double]
+        lib.oracle_det_sin.restype = C.c_double
+        lib.oracle_det_sin.argtypes = [C.c_double]
         lib.oracle_debye_length.restype = C.c_double
         lib.oracle_debye_length.argtypes = [P, C.c_int]
         F32P, F64P = C.POINTER(C.c_float), C.POINTER(C.c_double)

@@ -136,6 +136,39 @@ class Config(C.Structure):
     ]
 
 
+# picgpu_init.h
+INIT_NONE, INIT_EQUIPARTITION, INIT_MAXWELLIAN, INIT_ISOTROPIZATION, INIT_QUASINEUTRAL_PLASMA, \
+    INIT_UNIFORM_DISPLACEMENT = range(6)
+
+
+class Init(C.Structure):
+    _fields_ = [
+        ("model", C.c_int32), ("clear_particles", C.c_int32), ("solve_fields", C.c_int32),
+        ("leapfrog", C.c_int32),
+        ("number_density", C.c_double * MAX_SPECIES), ("temperature", C.c_double * MAX_SPECIES),
+        ("velocity", C.c_double * 3),
+        ("drift_velocity", (C.c_double * 3) * MAX_SPECIES), ("thermal_velocity", (C.c_double * 3) * MAX_SPECIES),
+        ("tperp_over_tpara", C.c_double), ("cell_count", C.c_double),
+        ("ion_species", C.c_int32), ("use_maxwellian", C.c_int32),
+        ("species_mask", C.c_int32), ("use_bounds", C.c_int32),
+        ("min", C.c_double * 3), ("max", C.c_double * 3), ("particle_numbers", C.c_int64 * 3),
+        ("displacement_dir", C.c_double * 3), ("displacement", C.c_double * MAX_SPECIES),
+        ("cycles", C.c_double), ("seed", C.c_uint64),
+    ]
+
+
+class InitStats(C.Structure):
+    _fields_ = [
+        ("added", C.c_int64 * MAX_SPECIES), ("occupancy_avg", C.c_double * MAX_SPECIES),
+        ("occupancy_min", C.c_int64 * MAX_SPECIES), ("occupancy_max", C.c_int64 * MAX_SPECIES),
+        ("drift", (C.c_double * 3) * MAX_SPECIES), ("temperature", C.c_double * MAX_SPECIES),
+        ("number_density", C.c_double * MAX_SPECIES), ("model_temperature", C.c_double * MAX_SPECIES),
+        ("model_number_density", C.c_double * MAX_SPECIES),
+        ("mesh_volume", C.c_double), ("debye_length", C.c_double), ("average_cell_size", C.c_double),
+        ("plasma_frequency_dt", C.c_double), ("place_ms", C.c_double),
+    ]
+
+
 class StepStats(C.Structure):
     _fields_ = [
         ("n_particles", C.c_int64 * MAX_SPECIES),

@@ -35,6 +35,7 @@ UNITS = {
     "unet.cu": [],
     "learned.cu": [],
     "mg.cu": [],
+    "init.cu": ["--fmad=false"],
     "unet_api.cu": [],
 }
 HEADERS = [os.path.join(SRC, f) for f in os.listdir(SRC) if f.endswith((".h", ".cuh", ".hpp"))] + [

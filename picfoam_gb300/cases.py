@@ -473,6 +473,62 @@ def swarm_ensemble(n_cases=64, n=(16, 16, 128), size=(0.01, 0.01, 0.08), counts=
                      cells_per_case=cpc, N=N))
 
 
+def init_config(model, seed=1234, number_density=(), temperature=(), clear=True, solve_fields=False,
+                leapfrog=False, electron_volt=False, **kw):
+    """An abi.Init (system/picInitialiseDict): number densities [1/m^3] and
+    temperatures (K, or eV with electron_volt, as picInitialise's
+    electronVolt switch) per species; model coefficients by keyword:
+    velocity, drift_velocity, thermal_velocity, tperp_over_tpara, cell_count,
+    ion_species, use_maxwellian, species (UniformDisplacement list), min, max,
+    particle_numbers, displacement_dir, displacement, cycles."""
+    it = abi.Init()
+    it.model = model
+    it.clear_particles = 1 if clear else 0
+    it.solve_fields = 1 if solve_fields else 0
+    it.leapfrog = 1 if leapfrog else 0
+    it.seed = seed
+    for s, n in enumerate(number_density):
+        it.number_density[s] = n
+    for s, T in enumerate(temperature):
+        it.temperature[s] = T * (E_CHARGE / K_B if electron_volt else 1.0)
+    for k in ("velocity", "min", "max", "displacement_dir"):
+        if k in kw:
+            for a in range(3):
+                getattr(it, k)[a] = kw[k][a]
+    for k in ("drift_velocity", "thermal_velocity"):
+        for s, v in enumerate(kw.get(k, ())):
+            for a in range(3):
+                getattr(it, k)[s][a] = v[a]
+    if "particle_numbers" in kw:
+        for a in range(3):
+            it.particle_numbers[a] = int(kw["particle_numbers"][a])
+    if "min" in kw or "max" in kw:
+        it.use_bounds = 1
+    for s, d in enumerate(kw.get("displacement", ())):
+        it.displacement[s] = d
+    it.species_mask = sum(1 << s for s in kw.get("species", ()))
+    for k in ("tperp_over_tpara", "cell_count", "cycles"):
+        if k in kw:
+            setattr(it, k, kw[k])
+    it.ion_species = kw.get("ion_species", -1)
+    it.use_maxwellian = 1 if kw.get("use_maxwellian", True) else 0
+    return it
+
+
+def empty_case(n_cells=(8, 8, 8), length=(0.01, 0.01, 0.01), sides=None, boxes=(), species=None,
+               precision=abi.PREC_FP64, dt=1e-12, origin=(0.0, 0.0, 0.0), electron_species=0):
+    """A case without particles: block mesh and config for picInitialise runs.
+    species: (mass, charge, weight, solveMovement) tuples (default e-, Ar+)."""
+    if sides is None:
+        sides = [patch(abi.PATCH_ABSORB, 0.0) for _ in range(6)]
+    if species is None:
+        species = [(M_E, -E_CHARGE, 1e4, True), (M_AR, E_CHARGE, 1e4, True)]
+    mesh = block_mesh(n_cells, length, sides, origin=origin, boxes=boxes)
+    cfg = base_config(dt, species, precision=precision, deposit=abi.DEPOSIT_FIXED_POINT,
+                      electron_species=electron_species)
+    return Case("empty", mesh, cfg, {}, [], {})
+
+
 def build_ensemble(case, backend=None):
     """Create an ensemble Simulation (one context, n_cases mesh copies)."""
     from .simulation import EnsembleBackend, Simulation

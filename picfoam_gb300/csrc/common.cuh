@@ -192,6 +192,9 @@ enum : uint32_t {
     kStreamRemainder = 3u << 28,
     kStreamIonMcc = 4u << 28,
     kStreamIonRemainder = 5u << 28,
+    kStreamInitCount = 6u << 28,      // initial conditions: remainder draw per (species, cell, tet)
+    kStreamInitParticle = 7u << 28,   // per (species, cell, tet << 24 | k) or (species, cell, k)
+    kStreamInitLattice = 8u << 28,    // per (species, lattice index)
 };
 
 }  // namespace pgd

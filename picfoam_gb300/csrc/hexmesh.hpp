@@ -581,6 +581,19 @@ inline long long locate(const HexMesh& m, const double* x, double* bary) {
     return 12LL * c + best;
 }
 
+// Volume of tet t of geometry class cls (the cell centre and the three face
+// points of its triangle): |a . (b x c)| / 6 with a, b, c the corner offsets.
+inline double tet_volume(const HexMesh& m, int cls, int t) {
+    const double* off = &m.cls_offset[size_t(cls) * 24];
+    const double* a = off + 3 * m.tt.tri[t][0];
+    const double* b = off + 3 * m.tt.tri[t][1];
+    const double* c = off + 3 * m.tt.tri[t][2];
+    const double x = b[1] * c[2] - b[2] * c[1];
+    const double y = b[2] * c[0] - b[0] * c[2];
+    const double z = b[0] * c[1] - b[1] * c[0];
+    return std::fabs(a[0] * x + a[1] * y + a[2] * z) / 6.0;
+}
+
 inline void position(const HexMesh& m, long long tet, const double* bary, double* x) {
     const int c = int(tet / 12), t = int(tet % 12);
     const double* off = &m.cls_offset[size_t(m.cell_class[c]) * 24];

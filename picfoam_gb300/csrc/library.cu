@@ -24,6 +24,7 @@
 
 #include "collide.h"
 #include "fields.h"
+#include "init.h"
 #include "hexmesh.hpp"
 #include "kernels.h"
 #include "learned.h"
@@ -31,6 +32,7 @@
 #include "particles.h"
 #include "picgpu.h"
 #include "picgpu_ensemble.h"
+#include "picgpu_init.h"
 
 using pgd::DMesh;
 
@@ -110,6 +112,7 @@ struct picgpu_ctx {
     std::unique_ptr<pgd::LearnedWarmStart> ws;  // learned warm start (cfg.learned.enabled)
     std::unique_ptr<pgd::MultigridPCG> mg;      // multigrid-preconditioned PCG (cfg.pcg_precond)
     int mg_outer = 0;                           // refinement steps of the last multigrid solve
+    double* tet_vol = nullptr;                  // 12 tet volumes per geometry class (initial conditions)
     // batched ensembles and graph-stepped runs
     int n_cases = 1;
     int* n_dev = nullptr;          // species counts on the device (graph steps)
@@ -1101,6 +1104,14 @@ static picgpu_status create_with_mesh(picgpu_ctx* c, const picgpu_config* cfg) {
         c->pc.area[p] = m.patches[p].area;
     }
     CK(pgd::move_fp64_set_tables(c->tc, c->pc));
+    CK(pgd::init_set_tables(c->tc));
+    {
+        std::vector<double> tv(12 * size_t(std::max(m.n_classes, 1)), 0.0);
+        for (int k = 0; k < m.n_classes; ++k)
+            for (int t = 0; t < 12; ++t) tv[12 * size_t(k) + t] = pg::tet_volume(m, k, t);
+        const picgpu_status us = upload(c, &c->tet_vol, tv);
+        if (us) return us;
+    }
     {
         // FP32 kernel tables: class-0 geometry (used when the mesh has one
         // class) and the packed crossing codes
@@ -1399,6 +1410,326 @@ picgpu_status picgpu_initialise_fields(picgpu_ctx* c) {
     if ((s = solve_fields(c, nullptr))) return s;
     CK(cudaStreamSynchronize(c->stream));
     if (c->profiling) harvest_events(c);
+    return PICGPU_OK;
+}
+
+// ------------------------------------------------ initial conditions ----
+// picInitialise (preProcess/picInitialise/picInitialise.C:30-319) for a
+// context; the placement runs on the device (csrc/init.cu).
+namespace {
+
+constexpr double kBoltzmann = 1.380649e-23;
+constexpr double kElementary = 1.602176634e-19;
+
+// Makes room for `add` more particles after the n used slots of species s.
+picgpu_status reserve_species(picgpu_ctx* c, int s, long long add) {
+    SpeciesBuf& B = c->sp[s];
+    const long long need = B.n + add;
+    if (need > (1LL << 31)) return bad(c, PICGPU_CAPACITY, "initialise: more than 2^31 particles of one species");
+    if (need <= B.cap) return PICGPU_OK;
+    const long cap = long(std::min<long long>(need + need / 4 + 1024, 1LL << 31));
+    if (B.n == 0) return alloc_species(c, s, cap);
+    return grow_species(c, s, cap);
+}
+
+}  // namespace
+
+picgpu_status picgpu_initialise(picgpu_ctx* c, const picgpu_init* in, picgpu_init_stats* st) {
+    if (!c || !in) return PICGPU_INVALID_ARG;
+    const int ns = c->cfg.n_species;
+    if (in->model < PICGPU_INIT_NONE || in->model > PICGPU_INIT_UNIFORM_DISPLACEMENT)
+        return bad(c, PICGPU_INVALID_ARG, "initialise: unknown InitializationModel");
+    if (c->n_cases != 1) return bad(c, PICGPU_NOT_SUPPORTED, "initialise: not for ensemble contexts");
+    picgpu_init_stats S{};
+    picgpu_status ps;
+    const pg::HexMesh& m = c->m;
+    if (in->clear_particles)
+        for (int sp = 0; sp < ns; ++sp) {
+            c->sp[sp].n = 0;
+            c->sp[sp].alive = 0;
+            c->sp[sp].cur = 0;
+        }
+
+    // per-species sampling (what each model draws)
+    pgd::InitSpecies smp[PICGPU_MAX_SPECIES] = {};
+    bool place[PICGPU_MAX_SPECIES] = {};
+    bool calc_T = false, calc_n = false;
+    for (int sp = 0; sp < ns; ++sp) {
+        const picgpu_species& P = c->cfg.species[sp];
+        pgd::InitSpecies& q = smp[sp];
+        q.n = in->number_density[sp];
+        q.w = P.weight;
+        const double th = std::sqrt(kBoltzmann * in->temperature[sp] / P.mass);  // equipartitionLinearVelocity
+        switch (in->model) {
+            case PICGPU_INIT_EQUIPARTITION:
+                for (int a = 0; a < 3; ++a) { q.scale[a] = th; q.drift[a] = in->velocity[a]; }
+                place[sp] = q.n > 0;
+                break;
+            case PICGPU_INIT_MAXWELLIAN:
+                for (int a = 0; a < 3; ++a) { q.scale[a] = in->thermal_velocity[sp][a]; q.drift[a] = in->drift_velocity[sp][a]; }
+                place[sp] = q.n > 0;
+                calc_T = true;
+                break;
+            case PICGPU_INIT_ISOTROPIZATION: {
+                const double f = in->tperp_over_tpara;
+                if (!(f > 0)) return bad(c, PICGPU_INVALID_ARG, "initialise: Tperp_over_Tpara must be > 0");
+                const double T = in->temperature[sp];
+                const double upara = std::sqrt(kBoltzmann * T / (((2.0 / 3.0) * f + (1.0 / 3.0)) * P.mass));
+                const double uperp = std::sqrt(kBoltzmann * T / (((2.0 / 3.0) + (1.0 / (3.0 * f))) * P.mass));
+                q.scale[0] = upara;
+                q.scale[1] = uperp;
+                q.scale[2] = uperp;
+                place[sp] = q.n > 0;
+                break;
+            }
+            case PICGPU_INIT_QUASINEUTRAL_PLASMA:
+                for (int a = 0; a < 3; ++a) q.scale[a] = th;
+                q.speed = std::sqrt(in->temperature[sp] * kBoltzmann * 3.0 / P.mass);
+                calc_n = true;
+                break;
+            case PICGPU_INIT_UNIFORM_DISPLACEMENT:
+                for (int a = 0; a < 3; ++a) q.scale[a] = th;
+                q.displacement = in->displacement[sp];
+                place[sp] = (in->species_mask >> sp) & 1;
+                calc_n = true;
+                break;
+            default:
+                calc_T = calc_n = true;
+                break;
+        }
+        if (place[sp] && !(P.weight > 0)) return bad(c, PICGPU_INVALID_ARG, "initialise: species weight must be > 0");
+    }
+    if (in->model == PICGPU_INIT_QUASINEUTRAL_PLASMA) {
+        const int ion = in->ion_species, el = c->cfg.electron_species;
+        if (ion < 0 || ion >= ns) return bad(c, PICGPU_INVALID_ARG, "initialise: ionSpecies is not defined");
+        if (el < 0 || el >= ns) return bad(c, PICGPU_INVALID_ARG, "initialise: electron species is not defined");
+        if (c->cfg.species[ion].charge + c->cfg.species[el].charge != 0.0)
+            return bad(c, PICGPU_INVALID_ARG,
+                       "initialise: ion and electron charge must be of same magnitude and opposite signs");
+        for (int sp : {ion, el}) {
+            const double nn = in->cell_count / c->cfg.species[sp].weight;
+            if (!(nn >= 0 && nn < 2147483647.0)) return bad(c, PICGPU_CAPACITY, "initialise: cellCount too large");
+            smp[sp].cell_count = int(nn);
+            place[sp] = smp[sp].cell_count > 0;
+        }
+    }
+
+    // lattice of UniformDisplacement (UniformInitialization.C:60-87)
+    double lo[3], hi[3], glo[3], ghi[3], dir[3], delta[3], span_len = 0;
+    const int gtop = pg::grid_point_id(m, m.n[0], m.n[1], m.n[2]);
+    for (int a = 0; a < 3; ++a) {
+        glo[a] = m.grid_pts[a];
+        ghi[a] = m.grid_pts[3 * size_t(gtop) + a];
+        lo[a] = in->use_bounds ? in->min[a] : glo[a];
+        hi[a] = in->use_bounds ? in->max[a] : ghi[a];
+    }
+    if (in->model == PICGPU_INIT_UNIFORM_DISPLACEMENT) {
+        const double dm = std::sqrt(in->displacement_dir[0] * in->displacement_dir[0] +
+                                    in->displacement_dir[1] * in->displacement_dir[1] +
+                                    in->displacement_dir[2] * in->displacement_dir[2]);
+        if (!(dm > 0)) return bad(c, PICGPU_INVALID_ARG, "initialise: displacementDir must be non-zero");
+        for (int a = 0; a < 3; ++a) dir[a] = in->displacement_dir[a] / dm;
+        double span[3];
+        for (int a = 0; a < 3; ++a) span[a] = hi[a] - lo[a];
+        span_len = span[0] * dir[0] + span[1] * dir[1] + span[2] * dir[2];
+        for (int a = 0; a < 3; ++a) {
+            if (in->particle_numbers[a] < 0) return bad(c, PICGPU_INVALID_ARG, "initialise: particleNumbers < 0");
+            delta[a] = span[a] / double(std::max<long long>(in->particle_numbers[a] - 1, 2));
+        }
+    }
+
+    int* counts = nullptr;
+    long long *offsets = nullptr, *sums = nullptr, *mm = nullptr;
+    int* err = nullptr;
+    const int nc = m.n_cells;
+    auto release = [&]() {
+        dfree(c, counts);
+        dfree(c, offsets);
+        dfree(c, sums);
+        dfree(c, mm);
+        dfree(c, err);
+    };
+    if ((ps = dalloc(c, &counts, size_t(nc))) || (ps = dalloc(c, &offsets, size_t(nc) + 1)) ||
+        (ps = dalloc(c, &sums, size_t(pgd::init_scan_scratch(nc)) + 1)) || (ps = dalloc(c, &mm, 3)) ||
+        (ps = dalloc(c, &err, 1))) {
+        release();
+        return ps;
+    }
+    CK(cudaMemsetAsync(err, 0, sizeof(int), c->stream));
+    cudaEvent_t e0, e1;
+    CK(cudaEventCreate(&e0));
+    CK(cudaEventCreate(&e1));
+    float place_ms = 0;
+    const bool constrain = m.empty[0] || m.empty[1] || m.empty[2];
+    for (int sp = 0; sp < ns && in->model != PICGPU_INIT_NONE; ++sp) {
+        if (!place[sp]) continue;
+        pgd::InitParams P{};
+        P.m = c->dm;
+        P.model = in->model;
+        P.species = sp;
+        P.constrain = constrain && in->model != PICGPU_INIT_UNIFORM_DISPLACEMENT;
+        P.use_maxwellian = in->use_maxwellian;
+        P.seed = in->seed;
+        P.sp = smp[sp];
+        P.tet_vol = c->tet_vol;
+        P.error = err;
+        long long total = 0;
+        CK(cudaEventRecord(e0, c->stream));
+        if (in->model == PICGPU_INIT_QUASINEUTRAL_PLASMA) {
+            total = (long long)smp[sp].cell_count * nc;
+        } else if (in->model == PICGPU_INIT_UNIFORM_DISPLACEMENT) {
+            for (int a = 0; a < 3; ++a) {
+                P.nl[a] = in->particle_numbers[a];
+                P.lo[a] = lo[a];
+                P.delta[a] = delta[a];
+                P.dir[a] = dir[a];
+                P.grid_lo[a] = glo[a];
+                P.grid_hi[a] = ghi[a];
+                P.grid_n[a] = m.n[a];
+            }
+            P.span_len = span_len;
+            P.cycles = in->cycles;
+            if (m.grid_cell.empty()) {
+                release();
+                return bad(c, PICGPU_NOT_SUPPORTED, "initialise: UniformDisplacement needs a block mesh");
+            }
+            total = in->particle_numbers[0] * in->particle_numbers[1] * in->particle_numbers[2];
+        } else {
+            pgd::launch_init_count(P, counts, c->stream);
+            CK(pgd::init_scan(counts, offsets, sums, nc, c->stream));
+            CK(cudaMemcpyAsync(&total, offsets + nc, sizeof(long long), cudaMemcpyDeviceToHost, c->stream));
+            CK(cudaStreamSynchronize(c->stream));
+            c->launches += 4;
+        }
+        if ((ps = reserve_species(c, sp, total))) {
+            release();
+            return ps;
+        }
+        SpeciesBuf& B = c->sp[sp];
+        P.first = B.n;
+        P.tet = B.tet[B.cur];
+        for (int a = 0; a < 3; ++a) {
+            P.y64[a] = B.y64[B.cur][a];
+            P.u64[a] = B.u64[B.cur][a];
+            P.y32[a] = B.y32[B.cur][a];
+            P.u32[a] = B.u32[B.cur][a];
+        }
+        if (in->model == PICGPU_INIT_UNIFORM_DISPLACEMENT) {
+            const int* gc = nullptr;
+            if ((ps = upload(c, const_cast<int**>(&gc), m.grid_cell))) {
+                release();
+                return ps;
+            }
+            P.grid_cell = gc;
+            pgd::launch_init_fill_lattice(P, c->stream);
+            CK(cudaStreamSynchronize(c->stream));
+            dfree(c, const_cast<int*>(gc));
+        } else if (in->model == PICGPU_INIT_QUASINEUTRAL_PLASMA) {
+            pgd::launch_init_fill_cells(P, c->stream);
+        } else {
+            pgd::launch_init_fill_tets(P, offsets, c->stream);
+        }
+        c->launches++;
+        CK(cudaEventRecord(e1, c->stream));
+        int e = 0;
+        CK(cudaMemcpyAsync(&e, err, sizeof(int), cudaMemcpyDeviceToHost, c->stream));
+        CK(cudaStreamSynchronize(c->stream));
+        CK(cudaGetLastError());
+        float ms = 0;
+        CK(cudaEventElapsedTime(&ms, e0, e1));
+        place_ms += ms;
+        if (e) {
+            release();
+            cudaEventDestroy(e0);
+            cudaEventDestroy(e1);
+            return bad(c, e == 2 ? PICGPU_CAPACITY : PICGPU_INVALID_ARG,
+                       e == 2 ? "initialise: more than 2^24 particles in one tet"
+                              : "initialise: tried to create a particle outside of the mesh");
+        }
+        B.n += total;
+        B.alive += total;
+        S.added[sp] = total;
+    }
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    S.place_ms = place_ms;
+
+    // statistics (picInitialise.C:86-188)
+    double vol = 0, lsum = 0;
+    for (int k = 0; k < nc; ++k) {
+        vol += m.vol[k];
+        lsum += std::cbrt(m.vol[k]);
+    }
+    S.mesh_volume = vol;
+    S.average_cell_size = nc > 0 ? lsum / nc : 0.0;
+    for (int sp = 0; sp < ns; ++sp) {
+        const SpeciesBuf& B = c->sp[sp];
+        const picgpu_species& P = c->cfg.species[sp];
+        pgd::launch_init_occupancy(B.tet[B.cur], B.n, nc, counts, c->stream);
+        pgd::launch_init_minmax(counts, nc, mm, c->stream);
+        long long h[3];
+        CK(cudaMemcpyAsync(h, mm, sizeof h, cudaMemcpyDeviceToHost, c->stream));
+        CK(cudaMemsetAsync(c->diag, 0, 10 * sizeof(double), c->stream));
+        const pgd::DSpecies v = view(c, sp, B.cur);
+        pgd::launch_diagnostics(v.tet, v.u64[0], v.u64[1], v.u64[2], v.u32[0], v.u32[1], v.u32[2], int(B.n),
+                                P.mass, P.weight, c->diag, c->stream);
+        double d[10];
+        CK(cudaMemcpyAsync(d, c->diag, sizeof d, cudaMemcpyDeviceToHost, c->stream));
+        CK(cudaStreamSynchronize(c->stream));
+        c->launches += 3;
+        S.occupancy_min[sp] = h[0];
+        S.occupancy_max[sp] = h[1];
+        S.occupancy_avg[sp] = nc > 0 ? double(h[2]) / nc : 0.0;
+        const double N = d[8];  // sum of nParticle
+        if (N > 0) {
+            double v2 = 0, dd = 0;
+            for (int a = 0; a < 3; ++a) {
+                S.drift[sp][a] = d[2 + a] / (P.mass * N);
+                v2 += d[5 + a];
+                dd += S.drift[sp][a] * S.drift[sp][a];
+            }
+            S.temperature[sp] = P.mass / (3.0 * kBoltzmann) * (v2 / N - dd);
+        }
+        S.number_density[sp] = vol > 0 ? N / vol : 0.0;
+        S.model_temperature[sp] = calc_T ? S.temperature[sp] : in->temperature[sp];
+        S.model_number_density[sp] = calc_n ? S.number_density[sp] : in->number_density[sp];
+    }
+    {
+        const double eps0 = 1.0 / (kMu0 * kCl * kCl);
+        double inv_l2 = 0;
+        for (int sp = 0; sp < ns; ++sp) {
+            const double q = c->cfg.species[sp].charge;
+            const double T = S.model_temperature[sp], n = S.model_number_density[sp];
+            if (q == 0.0 || n <= 0.0 || T <= 0.0) continue;
+            inv_l2 += n * q * q / eps0 / (T * kBoltzmann);
+        }
+        S.debye_length = inv_l2 > 0 ? std::sqrt(1.0 / inv_l2) : 0.0;
+        const int el = c->cfg.electron_species;
+        if (el >= 0 && el < ns && S.model_number_density[el] > 0) {
+            const double q = c->cfg.species[el].charge;
+            S.plasma_frequency_dt =
+                std::sqrt(S.model_number_density[el] * q * q / eps0 / c->cfg.species[el].mass) * c->cfg.dt;
+        }
+    }
+    release();
+
+    // calculateFields, solveMaxwellEquations (picInitialise.C:209-217)
+    if ((ps = zero_accumulators(c)) || (ps = move_species(c, true)) || (ps = charge_update(c))) return ps;
+    if (in->solve_fields && (ps = solve_fields(c, nullptr))) return ps;
+    // initalizeLeapFrog (picInitialise.C:219-227)
+    if (in->leapfrog) {
+        for (int sp = 0; sp < ns; ++sp) {
+            if (c->sp[sp].n == 0) continue;
+            pgd::MoveParams P = move_params(c, sp, false);
+            pgd::launch_push_only(P, c->mixed, -0.5 * c->cfg.dt, grid_for(c, c->sp[sp].n), c->stream);
+            c->launches++;
+        }
+    }
+    CK(cudaStreamSynchronize(c->stream));
+    CK(cudaGetLastError());
+    if (c->profiling) harvest_events(c);
+    if (st) *st = S;
+    (void)kElementary;
     return PICGPU_OK;
 }
 

@@ -26,6 +26,35 @@ __global__ void __launch_bounds__(256) move_kernel_fp64(MoveParams P) {
     warp_add_counter<double>(&P.counters->absorbed, ab);
 }
 
+// Push only, no tracking: initalizeLeapFrog (picInitialise.C:219-227) calls
+// the pusher's updateVelocity(p, -dt/2) on every parcel, moving or not.
+template <class Real>
+__global__ void __launch_bounds__(256) push_only_kernel(MoveParams P, Real tt) {
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < P.n; i += gridDim.x * blockDim.x) {
+        const int tetg = P.p.tet[i];
+        if (tetg < 0) continue;
+        PState<Real> s;
+        s.cell = tetg / 12;
+        s.tet = tetg - 12 * s.cell;
+        s.y[1] = ybuf<Real>(P.p, 0)[i];
+        s.y[2] = ybuf<Real>(P.p, 1)[i];
+        s.y[3] = ybuf<Real>(P.p, 2)[i];
+        s.y[0] = Real(1) - s.y[1] - s.y[2] - s.y[3];
+        s.U[0] = ubuf<Real>(P.p, 0)[i];
+        s.U[1] = ubuf<Real>(P.p, 1)[i];
+        s.U[2] = ubuf<Real>(P.p, 2)[i];
+        push<Real>(P, c_tet64, s, tt);
+        ubuf<Real>(P.p, 0)[i] = s.U[0];
+        ubuf<Real>(P.p, 1)[i] = s.U[1];
+        ubuf<Real>(P.p, 2)[i] = s.U[2];
+    }
+}
+
+void launch_push_only(const MoveParams& P, bool fp32, double tt, int grid, cudaStream_t s) {
+    if (fp32) push_only_kernel<float><<<grid, 256, 0, s>>>(P, float(tt));
+    else push_only_kernel<double><<<grid, 256, 0, s>>>(P, tt);
+}
+
 cudaError_t move_fp64_set_tables(const TetConst& t, const PatchConst& p) {
     cudaError_t e = cudaMemcpyToSymbol(c_tet64, &t, sizeof t);
     if (e != cudaSuccess) return e;

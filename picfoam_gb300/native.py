@@ -38,6 +38,7 @@ def declare(lib, prefix, ctx_api=True):
     f("count_particles", i, [P, i, SZP])
     f("get_particles", i, [P, i, C.c_size_t, I32P, F64P, F64P, SZP])
     f("initialise_fields", i, [P])
+    f("initialise", i, [P, C.POINTER(abi.Init), C.POINTER(abi.InitStats)])
     f("step", i, [P, i, C.POINTER(abi.StepStats)])
     f("move", i, [P, C.POINTER(abi.StepStats)])
     f("solve_poisson", i, [P, F64P, F64P, C.POINTER(abi.StepStats)])

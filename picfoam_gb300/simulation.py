@@ -135,6 +135,14 @@ class Simulation:
     def initialise_fields(self):
         self._check(self._fn("initialise_fields")(self._h))
 
+    def initialise(self, init):
+        """picInitialise: place the particles of an abi.Init on the device (or
+        in the oracle), compute the fields, optionally solve them and apply
+        the leapfrog back-step; returns the abi.InitStats."""
+        st = abi.InitStats()
+        self._check(self._fn("initialise")(self._h, C.byref(init), C.byref(st)))
+        return st
+
     def step(self, n=1):
         s = abi.StepStats()
         self._check(self._fn("step")(self._h, n, C.byref(s)))
