@@ -61,7 +61,7 @@ def parse():
     p.add_argument("--ens-steps", type=int, default=100)
     p.add_argument("--ens-graph", type=int, default=10)
     p.add_argument("--ens-seq-steps", type=int, default=20)
-    p.add_argument("--only", default=None, choices=["electrode", "unet", "ensemble"],
+    p.add_argument("--only", default=None, choices=["electrode", "unet", "ensemble", "init"],
                    help="profiling drivers: run one workload briefly and print a short summary "
                         "(electrode: electrode_box steps; unet: one forward + train steps; "
                         "ensemble: two graph replays)")
@@ -69,6 +69,7 @@ def parse():
     p.add_argument("--only-precond", default="jacobi", choices=["jacobi", "multigrid"],
                    help="Poisson preconditioner of the electrode driver")
     p.add_argument("--no-multigrid", action="store_true", help="skip the multigrid-preconditioned Poisson arm")
+    p.add_argument("--no-init", action="store_true", help="skip the device initial-condition measurement")
     return p.parse_args()
 
 
@@ -316,6 +317,61 @@ def learned_vs_plain(args):
     return out
 
 
+def init_conditions(args, reps=3):
+    """picgpu_initialise on the benchmark workload (64^3 cells, 0.05 m, e- and
+    Ar+ at n = 1e15 with the benchmark's weight: 50 per cell and species,
+    Equipartition at 2 eV / 0.03 eV): device placement time (CUDA events) and
+    particles/s, against the oracle's restatement (one thread, a bounded
+    sample of 16^3 cells) and the host path it replaces (numpy sampling of
+    the same population + upload through picgpu_set_particles)."""
+    import numpy as np
+    from picfoam_gb300 import abi, cases
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import pyoracle
+    L, n = 0.05, 1e15
+    w = n * L ** 3 / (args.cells ** 3 * args.ppc)
+    prec = abi.PREC_MIXED if args.precision == "mixed" else abi.PREC_FP64
+    species = [(cases.M_E, -cases.E_CHARGE, w, True), (cases.M_AR, cases.E_CHARGE, w, True)]
+    init = cases.init_config(abi.INIT_EQUIPARTITION, number_density=(n, n), temperature=(2.0, 0.03),
+                             electron_volt=True)
+    case = cases.empty_case(n_cells=(args.cells,) * 3, length=(L,) * 3, species=species, precision=prec)
+    sim = cases.build(case)
+    times, added = [], 0
+    for _ in range(reps + 1):                       # the first call also sizes the store
+        st = sim.initialise(init)
+        times.append(st.place_ms)
+        added = st.added[0] + st.added[1]
+    ms = float(np.median(times[1:]))
+    t0 = time.perf_counter()
+    init.solve_fields = 0
+    sim.initialise(init)
+    wall = time.perf_counter() - t0
+    sim.close()
+    # host path: numpy sampling of the same population and the upload
+    t0 = time.perf_counter()
+    hc = cases.two_species_3d(n_cells=args.cells, per_cell=args.ppc, precision=prec)
+    t1 = time.perf_counter()
+    sim2 = cases.build(hc)
+    t2 = time.perf_counter()
+    sim2.close()
+    # oracle, one thread, 16^3-cell sample at the same density and weight
+    sc = 16
+    ocase = cases.empty_case(n_cells=(sc,) * 3, length=(L * sc / args.cells,) * 3, species=species,
+                             precision=abi.PREC_FP64)
+    osim = cases.build(ocase, backend=pyoracle.OracleBackend(1))
+    t3 = time.perf_counter()
+    ost = osim.initialise(init)
+    t4 = time.perf_counter()
+    osim.close()
+    on = ost.added[0] + ost.added[1]
+    return {"model": "Equipartition", "particles": int(added), "place_ms": ms,
+            "particles_per_s": added / (ms * 1e-3), "initialise_call_wall_s": wall,
+            "host_numpy_sampling_s": t1 - t0, "host_upload_s": t2 - t1,
+            "oracle_single_thread_particles_per_s": on / (t4 - t3), "oracle_sample_particles": int(on),
+            "config": f"{args.cells}^3 cells, 0.05 m, e- + Ar+ at 1e15 m^-3, weight {w:.4g} "
+                      f"({args.ppc}/cell per species), {args.precision} store"}
+
+
 def ensemble(args):
     """Batched swarm ensemble (64 cases of 16x16x128 cells, 10-1000 Td,
     1e5-4e6 electrons each from seed 7): one context, CUDA-graph steps with
@@ -479,6 +535,11 @@ def run_ours(args, rank, ws):
             line["poisson_learned_vs_plain"] = learned_vs_plain(args)
         except Exception as ex:  # reported, not fatal
             line["poisson_learned_vs_plain"] = {"error": str(ex)}
+    if rank == 0 and ws == 1 and not args.no_init:
+        try:
+            line["initial_conditions"] = init_conditions(args)
+        except Exception as ex:  # reported, not fatal
+            line["initial_conditions"] = {"error": str(ex)}
     if rank == 0 and ws == 1 and not args.no_ensemble:
         try:
             line["ensemble"] = ensemble(args)
@@ -527,6 +588,18 @@ def run_only(args):
         assert lib.picgpu_unet_train(h, p(x), p(t), p(m), args.only_steps, 1e-3, C.byref(loss)) == 0
         lib.picgpu_unet_destroy(h)
         print(json.dumps({"only": "unet", "grid": n, "loss": loss.value}))
+    elif args.only == "init":
+        from picfoam_gb300 import abi
+        L, n = 0.05, 1e15
+        w = n * L ** 3 / (args.cells ** 3 * args.ppc)
+        case = cases.empty_case(n_cells=(args.cells,) * 3, length=(L,) * 3, precision=abi.PREC_MIXED,
+                                species=[(cases.M_E, -cases.E_CHARGE, w, True), (cases.M_AR, cases.E_CHARGE, w, True)])
+        sim = cases.build(case)
+        init = cases.init_config(abi.INIT_EQUIPARTITION, number_density=(n, n), temperature=(2.0, 0.03),
+                                 electron_volt=True)
+        for _ in range(args.only_steps):
+            st = sim.initialise(init)
+        print(json.dumps({"only": "init", "particles": st.added[0] + st.added[1], "place_ms": st.place_ms}))
     else:
         case = cases.swarm_ensemble(n_cases=args.ens_cases)
         sim = cases.build_ensemble(case)
