@@ -349,6 +349,40 @@ picgpu_status picgpu_get_particles(picgpu_ctx* ctx, int species, size_t cap,
  * before the first step: calculateFields + solveFields). */
 picgpu_status picgpu_initialise_fields(picgpu_ctx* ctx);
 
+/* SimpleInjection boundary model (SM/BoundaryModel/SimpleInjection/
+ * SimpleInjection.C:197-240, emitter SM/Helper/ParticleEmitter/
+ * ParticleEmitter.C:54-139 and :265-418): every step, before the move, each
+ * listed species gets frequency / weight * dt parcels (the fraction carried
+ * to the next step) at area-weighted random points of the patch's face
+ * triangles, moved 10-50 % of the way towards the owner cell's centre plane,
+ * with a velocity from the model below about the inward normal, then pushed
+ * back by dt/2 (syncVelocityAtBoundary) when the species is charged and
+ * sync_velocity_at_boundary is set.  The particles' later interaction with
+ * the patch is the patch kind's (deletion: ABSORB, reflection: WALL,
+ * floating: FLOATING, where each injected parcel also takes its charge off
+ * the patch, SimpleInjection.C:295-302). */
+enum {
+    PICGPU_EMIT_BIRD_MAXWELLIAN_FLUX = 0,  /* birdMaxwellianFlux (ParticleEmitter.C:420-461) */
+    PICGPU_EMIT_MOST_PROBABLE_SPEED = 1,   /* mostProbableSpeed (:464-481) */
+    PICGPU_EMIT_MAXWELLIAN_FLUX = 2,       /* maxwellianFlux (:503-535) */
+    PICGPU_EMIT_HALF_MAXWELLIAN_FLUX = 3   /* halfMaxwellianFlux (:484-496) */
+};
+#define PICGPU_MAX_INJECTORS 8
+typedef struct {
+    int32_t patch;                          /* side 0..5 or box 6 + b; not cyclic or empty */
+    int32_t velocity_model;                 /* PICGPU_EMIT_* */
+    int32_t n_species;                      /* entries of injectionTypeIds */
+    int32_t pad;
+    int32_t species[PICGPU_MAX_SPECIES];    /* injectionTypeIds */
+    double  frequency[PICGPU_MAX_SPECIES];  /* frequencies: physical particles per second */
+    double  eV[PICGPU_MAX_SPECIES];         /* temperature of the emitted flux [eV] */
+    double  end_time;                       /* injectionEndTime [s]: no injection at t > end_time */
+} picgpu_injection;
+
+/* Replace the context's injectors (n = 0 removes them); remainders restart
+ * at zero.  Not for ensemble contexts or picgpu_step_graph. */
+picgpu_status picgpu_set_injection(picgpu_ctx* ctx, int n, const picgpu_injection* inj);
+
 /* Advance nsteps time steps. */
 picgpu_status picgpu_step(picgpu_ctx* ctx, int nsteps, picgpu_step_stats* stats);
 

@@ -36,6 +36,8 @@
 namespace {
 
 using pg::HexMesh;
+using pg::PatchTriangles;
+using pg::patch_triangles;
 
 // CODATA constants (values used throughout the project).
 constexpr double kC = 299792458.0;
@@ -153,6 +155,13 @@ struct Oracle {
     double last_res_l2 = 0, last_res_of = 0;
     picgpu_step_stats acc{};
     ocoll::Tables xs, ixs;
+    // SimpleInjection boundary models
+    struct Injector {
+        picgpu_injection cfg{};
+        double remainder[PICGPU_MAX_SPECIES] = {};
+        PatchTriangles tri;
+    };
+    std::vector<Injector> injectors;
 };
 
 // ------------------------------------------------------------ pushers -----
@@ -1473,6 +1482,22 @@ double det_sin(double x) {
     return ((long long)k & 1) ? -s : s;
 }
 
+double det_exp(double x) {
+    const double ln2_hi = 0.6931471805599452862, ln2_lo = 2.3190468138462996e-17;
+    const double k = std::rint(x / ln2_hi);
+    const double r = (x - k * ln2_hi) - k * ln2_lo;
+    // 1/17!, 1/16!, ..., 1/2!, 1/1!, 1/0!
+    const double c[18] = {1.0 / 355687428096000.0, 1.0 / 20922789888000.0, 1.0 / 1307674368000.0,
+                          1.0 / 87178291200.0,     1.0 / 6227020800.0,     1.0 / 479001600.0,
+                          1.0 / 39916800.0,        1.0 / 3628800.0,        1.0 / 362880.0,
+                          1.0 / 40320.0,           1.0 / 5040.0,           1.0 / 720.0,
+                          1.0 / 120.0,             1.0 / 24.0,             1.0 / 6.0,
+                          0.5,                     1.0,                    1.0};
+    double p = c[0];
+    for (int i = 1; i < 18; ++i) p = p * r + c[i];
+    return std::ldexp(p, int(k));
+}
+
 void polar_pair(ocoll::Philox& r, double& n1, double& n2) {
     for (int a = 0; a < 64; ++a) {
         const double u1 = 2.0 * r.uniform() - 1.0;
@@ -1802,6 +1827,119 @@ int oracle_initialise_impl(Oracle& o, const picgpu_init* in, picgpu_init_stats* 
     return 0;
 }
 
+// SimpleInjection::injection (SimpleInjection.C:197-240) before the move:
+// frequency / weight * dt parcels per listed species plus the carried
+// remainder, each emitted by ParticleEmitter::emitParticle
+// (ParticleEmitter.C:265-418) -- area-weighted face triangle, uniform point
+// on it, moved U(0.1, 0.5) of the normal distance towards the cell centre,
+// velocity model about the inward normal (:420-535), constrainDirection,
+// syncVelocityAtBoundary(-0.5) (:401) -- and, on a floating patch, its
+// charge taken off the patch (particleEjection, SimpleInjection.C:295-302).
+void inject(Oracle& o) {
+    using namespace oinit;
+    const HexMesh& m = o.m;
+    const double dt = o.cfg.dt;
+    const double t = double(o.step_index + 1) * dt;
+    const bool cons = m.empty[0] || m.empty[1] || m.empty[2];
+    for (size_t i = 0; i < o.injectors.size(); ++i) {
+        Oracle::Injector& I = o.injectors[i];
+        if (t > I.cfg.end_time) continue;
+        const PatchTriangles& T = I.tri;
+        const int ntri = int(T.cell.size());
+        for (int j = 0; j < I.cfg.n_species; ++j) {
+            const int sp = I.cfg.species[j];
+            const picgpu_species& S = o.cfg.species[sp];
+            const double np = I.cfg.frequency[j] / S.weight * dt + I.remainder[j];
+            const long long n = (long long)np;
+            I.remainder[j] = np - double(n);
+            if (n <= 0) continue;
+            if (m.patches[I.cfg.patch].p.kind == PICGPU_PATCH_FLOATING)
+                o.Qconv[I.cfg.patch] = o.Qconv[I.cfg.patch] - double(n) * S.charge * S.weight;
+            const double temperature = I.cfg.eV[j] * 1.602176634e-19 / kBoltzmann;
+            for (long long k = 0; k < n; ++k) {
+                ocoll::Philox r(o.cfg.seed, ocoll::kStreamInject | (uint32_t(i) << 4) | uint32_t(sp),
+                                uint32_t(o.step_index), uint32_t(k));
+                const double af = r.uniform() * T.area;
+                int tri = 0;
+                for (int q = ntri - 1; q >= 0; --q)
+                    if (af > T.cum[q]) { tri = q; break; }
+                const int c = T.cell[tri], tt = T.tet[tri];
+                const double* off = &m.cls_offset[size_t(m.cell_class[c]) * 24];
+                const double* cc = &m.cc[3 * size_t(c)];
+                double A[3], B[3], Cc[3];
+                for (int a = 0; a < 3; ++a) {
+                    A[a] = cc[a] + off[3 * m.tt.tri[tt][0] + a];
+                    B[a] = cc[a] + off[3 * m.tt.tri[tt][1] + a];
+                    Cc[a] = cc[a] + off[3 * m.tt.tri[tt][2] + a];
+                }
+                // triPointRef::randomPoint: (1 - sqrt r1) A + sqrt r1 (1 - r2) B + sqrt r1 r2 C
+                const double r1 = r.uniform(), r2 = r.uniform();
+                const double sr = std::sqrt(r1);
+                double pf[3];
+                for (int a = 0; a < 3; ++a) pf[a] = (1.0 - sr) * A[a] + sr * (1.0 - r2) * B[a] + sr * r2 * Cc[a];
+                const double fa = 0.1 + 0.4 * r.uniform();  // scalarAB(0.1, 0.5)
+                const double* nrm = &T.normal[3 * size_t(tri)];
+                const double dn =
+                    std::fabs((pf[0] - cc[0]) * nrm[0] + (pf[1] - cc[1]) * nrm[1] + (pf[2] - cc[2]) * nrm[2]);
+                double x[3];
+                for (int a = 0; a < 3; ++a) x[a] = pf[a] - fa * (dn * nrm[a]);
+                const double* fc = &T.centre[3 * size_t(tri)];
+                double nn[3], t1[3], t2[3];
+                for (int a = 0; a < 3; ++a) {
+                    nn[a] = -nrm[a];
+                    t1[a] = fc[a] - A[a];
+                }
+                const double m1 = std::sqrt(t1[0] * t1[0] + t1[1] * t1[1] + t1[2] * t1[2]);
+                for (int a = 0; a < 3; ++a) t1[a] = t1[a] / m1;
+                t2[0] = nn[1] * t1[2] - nn[2] * t1[1];
+                t2[1] = nn[2] * t1[0] - nn[0] * t1[2];
+                t2[2] = nn[0] * t1[1] - nn[1] * t1[0];
+                const double m2 = std::sqrt(t2[0] * t2[0] + t2[1] * t2[1] + t2[2] * t2[2]);
+                for (int a = 0; a < 3; ++a) t2[a] = t2[a] / m2;
+                double U[3];
+                const double vt = std::sqrt(kBoltzmann * temperature / S.mass);
+                if (I.cfg.velocity_model == PICGPU_EMIT_MOST_PROBABLE_SPEED) {
+                    const double vmp = std::sqrt(2.0 * kBoltzmann * temperature / S.mass);
+                    for (int a = 0; a < 3; ++a) U[a] = vmp * nn[a];
+                } else {
+                    double n1, n2;
+                    polar_pair(r, n1, n2);
+                    double tg[3];
+                    for (int a = 0; a < 3; ++a) tg[a] = vt * (n1 * t1[a] + n2 * t2[a]);
+                    double un;
+                    if (I.cfg.velocity_model == PICGPU_EMIT_BIRD_MAXWELLIAN_FLUX) {
+                        const double vmp = std::sqrt(2.0 * kBoltzmann * temperature / S.mass);
+                        double u = 0.0;
+                        for (int it = 0; it < 1000; ++it) {  // do { ... } while (P < U01)
+                            u = 3.0 * (2.0 * r.uniform() - 1.0);
+                            const double pr = u < 0.0 ? -1.0 : 2.0 * u / 1.4142135623730951 * det_exp(0.5 - u * u);
+                            if (!(pr < r.uniform())) break;
+                        }
+                        un = vmp * u;
+                    } else if (I.cfg.velocity_model == PICGPU_EMIT_HALF_MAXWELLIAN_FLUX) {
+                        double n3, n4;
+                        polar_pair(r, n3, n4);
+                        un = std::fabs(n3) * vt;
+                    } else {
+                        const double R = r.uniform();
+                        un = vt * std::sqrt(-2.0 * det_log(1.0 - R));
+                    }
+                    for (int a = 0; a < 3; ++a) U[a] = tg[a] + un * nn[a];
+                }
+                for (int a = 0; a < 3; ++a)
+                    if (cons && m.empty[a]) x[a] = 0.0;
+                int tet = 0;
+                double y[3] = {0, 0, 0};
+                locate_in_cell(m, c, x, tet, y);
+                Parcel p = make_parcel(c, tet, y, v3(U[0], U[1], U[2]));
+                if (o.cfg.sync_velocity_at_boundary && S.charge != 0.0 && o.cfg.pusher != PICGPU_PUSHER_NONE)
+                    push(o, p, sp, -0.5 * dt);
+                o.cloud[sp].push_back(p);
+            }
+        }
+    }
+}
+
 struct oracle_ctx {
     Oracle o;
 };
@@ -1950,6 +2088,26 @@ int oracle_get_particles(oracle_ctx* ctx, int species, size_t cap, int32_t* tet,
 double oracle_det_log(double x) { return oinit::det_log(x); }
 double oracle_det_sin(double x) { return oinit::det_sin(x); }
 
+int oracle_set_injection(oracle_ctx* ctx, int n, const picgpu_injection* inj) {
+    Oracle& o = ctx->o;
+    if (n < 0 || n > PICGPU_MAX_INJECTORS || (n > 0 && !inj)) return PICGPU_INVALID_ARG;
+    o.injectors.clear();
+    for (int i = 0; i < n; ++i) {
+        const picgpu_injection& q = inj[i];
+        if (q.patch < 0 || q.patch >= int(o.m.patches.size())) return PICGPU_INVALID_ARG;
+        const int kind = o.m.patches[q.patch].p.kind;
+        if (kind == PICGPU_PATCH_CYCLIC || kind == PICGPU_PATCH_EMPTY) return PICGPU_INVALID_ARG;
+        for (int j = 0; j < q.n_species; ++j)
+            if (q.species[j] < 0 || q.species[j] >= o.cfg.n_species) return PICGPU_INVALID_ARG;
+        Oracle::Injector I;
+        I.cfg = q;
+        I.tri = patch_triangles(o.m, q.patch);
+        if (I.tri.cell.empty()) return PICGPU_INVALID_ARG;
+        o.injectors.push_back(I);
+    }
+    return 0;
+}
+
 int oracle_initialise(oracle_ctx* ctx, const picgpu_init* init, picgpu_init_stats* stats) {
     if (!ctx || !init) return PICGPU_INVALID_ARG;
     return oracle_initialise_impl(ctx->o, init, stats);
@@ -1976,6 +2134,7 @@ int oracle_step(oracle_ctx* ctx, int nsteps, picgpu_step_stats* st) {
     if (st) std::memset(st, 0, sizeof *st);
     int status = 0;
     for (int k = 0; k < nsteps; ++k) {
+        inject(o);
         int s = move_all(o, st);
         if (s) return s;
         collisions(o, st);

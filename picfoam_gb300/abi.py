@@ -136,6 +136,19 @@ class Config(C.Structure):
     ]
 
 
+# SimpleInjection (picgpu.h)
+EMIT_BIRD_MAXWELLIAN_FLUX, EMIT_MOST_PROBABLE_SPEED, EMIT_MAXWELLIAN_FLUX, EMIT_HALF_MAXWELLIAN_FLUX = range(4)
+MAX_INJECTORS = 8
+
+
+class Injection(C.Structure):
+    _fields_ = [
+        ("patch", C.c_int32), ("velocity_model", C.c_int32), ("n_species", C.c_int32), ("pad", C.c_int32),
+        ("species", C.c_int32 * MAX_SPECIES), ("frequency", C.c_double * MAX_SPECIES),
+        ("eV", C.c_double * MAX_SPECIES), ("end_time", C.c_double),
+    ]
+
+
 # picgpu_init.h
 INIT_NONE, INIT_EQUIPARTITION, INIT_MAXWELLIAN, INIT_ISOTROPIZATION, INIT_QUASINEUTRAL_PLASMA, \
     INIT_UNIFORM_DISPLACEMENT = range(6)

@@ -515,6 +515,21 @@ def init_config(model, seed=1234, number_density=(), temperature=(), clear=True,
     return it
 
 
+def injection(patch, species, frequency, eV, model=abi.EMIT_MAXWELLIAN_FLUX, end_time=1.0):
+    """An abi.Injection (SimpleInjectionCoeffs): injectionTypeIds `species`,
+    frequencies [1/s] and eV per species, velocityModel, injectionEndTime."""
+    q = abi.Injection()
+    q.patch = patch
+    q.velocity_model = model
+    q.n_species = len(species)
+    for j, s in enumerate(species):
+        q.species[j] = s
+        q.frequency[j] = frequency[j]
+        q.eV[j] = eV[j]
+    q.end_time = end_time
+    return q
+
+
 def empty_case(n_cells=(8, 8, 8), length=(0.01, 0.01, 0.01), sides=None, boxes=(), species=None,
                precision=abi.PREC_FP64, dt=1e-12, origin=(0.0, 0.0, 0.0), electron_species=0):
     """A case without particles: block mesh and config for picInitialise runs.

@@ -195,6 +195,7 @@ enum : uint32_t {
     kStreamInitCount = 6u << 28,      // initial conditions: remainder draw per (species, cell, tet)
     kStreamInitParticle = 7u << 28,   // per (species, cell, tet << 24 | k) or (species, cell, k)
     kStreamInitLattice = 8u << 28,    // per (species, lattice index)
+    kStreamInject = 9u << 28,         // per (injector << 4 | species, step, parcel)
 };
 
 }  // namespace pgd

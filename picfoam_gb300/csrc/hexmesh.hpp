@@ -581,6 +581,45 @@ inline long long locate(const HexMesh& m, const double* x, double* bary) {
     return 12LL * c + best;
 }
 
+// The emitting triangles of one patch (ParticleEmitter::initilizeParticleEmitter,
+// ParticleEmitter.C:54-139): each boundary face of the patch, in boundary-face
+// order, split into the face triangles of its two tets; cum[0] = 0 and
+// cum[i + 1] = cum[i] + area of triangle i; area = sum of the face areas.
+struct PatchTriangles {
+    std::vector<int> cell, tet;          // owner cell, local tet (2 face + k)
+    std::vector<double> normal, centre;  // 3 per triangle: outward unit face normal, face centre
+    std::vector<double> cum;
+    double area = 0.0;
+};
+
+inline PatchTriangles patch_triangles(const HexMesh& m, int patch) {
+    PatchTriangles T;
+    T.cum.push_back(0.0);
+    for (const BFace& b : m.bfaces) {
+        if (b.patch != patch) continue;
+        T.area += b.area;
+        const double* off = &m.cls_offset[size_t(m.cell_class[b.cell]) * 24];
+        for (int k = 0; k < 2; ++k) {
+            const int t = 2 * b.local_face + k;
+            const double* A = off + 3 * m.tt.tri[t][0];
+            const double* B = off + 3 * m.tt.tri[t][1];
+            const double* C = off + 3 * m.tt.tri[t][2];
+            const double u[3] = {B[0] - A[0], B[1] - A[1], B[2] - A[2]};
+            const double v[3] = {C[0] - A[0], C[1] - A[1], C[2] - A[2]};
+            const double w[3] = {u[1] * v[2] - u[2] * v[1], u[2] * v[0] - u[0] * v[2], u[0] * v[1] - u[1] * v[0]};
+            const double a = 0.5 * std::sqrt(w[0] * w[0] + w[1] * w[1] + w[2] * w[2]);
+            T.cell.push_back(b.cell);
+            T.tet.push_back(t);
+            for (int q = 0; q < 3; ++q) {
+                T.normal.push_back(b.normal[q]);
+                T.centre.push_back(b.centre[q]);
+            }
+            T.cum.push_back(T.cum.back() + a);
+        }
+    }
+    return T;
+}
+
 // Volume of tet t of geometry class cls (the cell centre and the three face
 // points of its triangle): |a . (b x c)| / 6 with a, b, c the corner offsets.
 inline double tet_volume(const HexMesh& m, int cls, int t) {

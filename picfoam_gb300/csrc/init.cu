@@ -1,5 +1,6 @@
-// init.cu -- particle initial conditions on the device: the InitializationModel
-// sub-models of picInitialise (preProcess/picInitialise/InitializationModel).
+// init.cu -- particles created on the device: the InitializationModel
+// sub-models of picInitialise (preProcess/picInitialise/InitializationModel)
+// and the SimpleInjection boundary model's per-step emission.
 //
 // Built with --fmad=false: every product and sum rounds on its own, in the
 // order of the CPU oracle, which places the same particles bit for bit.
@@ -16,6 +17,8 @@
 //                            cellCount parcels per cell in a random tet
 //   init_fill_lattice_kernel UniformDisplacement (UniformInitialization.C:51-127):
 //                            sinusoidally displaced lattice, located in the mesh
+//   inject_kernel            SimpleInjection::injection (SimpleInjection.C:197-240)
+//                            through ParticleEmitter::emitParticle
 #include "init.h"
 
 #include <algorithm>
@@ -77,6 +80,33 @@ __device__ double det_sin(double x) {
     const double s = r + r * (w * p);
     const long long ki = (long long)k;
     return (ki & 1) ? -s : s;
+}
+
+// e^x in fixed FP64 operations for |x| < 700: x = k ln2 + r with ln 2 in two
+// parts, |r| <= ln2 / 2, e^r by its Taylor series to r^17, then 2^k exactly.
+__device__ double det_exp(double x) {
+    const double ln2_hi = 0.6931471805599452862, ln2_lo = 2.3190468138462996e-17;
+    const double k = rint(x / ln2_hi);
+    const double r = (x - k * ln2_hi) - k * ln2_lo;
+    double p = 1.0 / 355687428096000.0;  // 1/17!
+    p = p * r + 1.0 / 20922789888000.0;  // 1/16!
+    p = p * r + 1.0 / 1307674368000.0;
+    p = p * r + 1.0 / 87178291200.0;
+    p = p * r + 1.0 / 6227020800.0;
+    p = p * r + 1.0 / 479001600.0;
+    p = p * r + 1.0 / 39916800.0;
+    p = p * r + 1.0 / 3628800.0;
+    p = p * r + 1.0 / 362880.0;
+    p = p * r + 1.0 / 40320.0;
+    p = p * r + 1.0 / 5040.0;
+    p = p * r + 1.0 / 720.0;
+    p = p * r + 1.0 / 120.0;
+    p = p * r + 1.0 / 24.0;
+    p = p * r + 1.0 / 6.0;
+    p = p * r + 0.5;
+    p = p * r + 1.0;
+    p = p * r + 1.0;
+    return ldexp(p, int(k));
 }
 
 // Two standard normal variates by Marsaglia's polar method (rejection of
@@ -179,6 +209,21 @@ __device__ bool constrain(const InitParams& P, int c, int& t, double* y) {
 }
 
 __device__ void store(const InitParams& P, long long i, int tet, const double* y, const double* U) {
+    P.tet[i] = tet;
+    if (P.y64[0]) {
+        for (int a = 0; a < 3; ++a) {
+            P.y64[a][i] = y[a];
+            P.u64[a][i] = U[a];
+        }
+    } else {
+        for (int a = 0; a < 3; ++a) {
+            P.y32[a][i] = float(y[a]);
+            P.u32[a][i] = float(U[a]);
+        }
+    }
+}
+
+__device__ void store_inject(const InjectParams& P, long long i, int tet, const double* y, const double* U) {
     P.tet[i] = tet;
     if (P.y64[0]) {
         for (int a = 0; a < 3; ++a) {
@@ -365,6 +410,100 @@ __global__ void __launch_bounds__(1024) init_minmax_kernel(const int* __restrict
     }
 }
 
+// ------------------------------------------------------------ injection --
+// ParticleEmitter::emitParticle (ParticleEmitter.C:265-418): area-weighted
+// triangle, uniform point on it (Osada, Funkhouser, Chazelle & Dobkin 2002:
+// (1 - sqrt r1) A + sqrt r1 (1 - r2) B + sqrt r1 r2 C), moved a = U(0.1, 0.5)
+// of the normal distance towards the cell centre, velocity about the inward
+// normal n with tangents t1 = (face centre - first triangle point) / |.|,
+// t2 = n x t1 / |.|, the empty-axis constraint, located in the owner cell.
+__global__ void __launch_bounds__(256) inject_kernel(InjectParams P) {
+    const double kB = 1.380649e-23;
+    if (blockIdx.x == 0 && threadIdx.x == 0 && P.qconv) P.qconv[P.patch] = P.qconv[P.patch] - P.ejected_charge;
+    for (long long k = blockIdx.x * (long long)blockDim.x + threadIdx.x; k < P.n;
+         k += (long long)gridDim.x * blockDim.x) {
+        Philox r(P.seed, kStreamInject | (uint32_t(P.injector) << 4) | uint32_t(P.species), P.step, uint32_t(k));
+        const double af = r.uniform() * P.area;
+        // the largest i with af > cum[i] (cum[0] = 0): the triangle holding af
+        int lo = 0, hi = P.n_tri - 1;
+        while (lo < hi) {
+            const int mid = (lo + hi + 1) >> 1;
+            if (af > P.tri_cum[mid]) lo = mid;
+            else hi = mid - 1;
+        }
+        const int tri = lo;
+        const int c = P.tri_cell[tri], t = P.tri_tet[tri];
+        const double* off = P.m.offset + size_t(P.m.cell_class[c]) * 24;
+        const double* cc = P.m.cc + 3 * size_t(c);
+        double A[3], B[3], C[3];
+        for (int a = 0; a < 3; ++a) {
+            A[a] = cc[a] + off[3 * c_init_tri[t][0] + a];
+            B[a] = cc[a] + off[3 * c_init_tri[t][1] + a];
+            C[a] = cc[a] + off[3 * c_init_tri[t][2] + a];
+        }
+        const double r1 = r.uniform(), r2 = r.uniform();
+        const double sr = sqrt(r1);
+        double pf[3];
+        for (int a = 0; a < 3; ++a) pf[a] = (1.0 - sr) * A[a] + sr * (1.0 - r2) * B[a] + sr * r2 * C[a];
+        const double fa = 0.1 + 0.4 * r.uniform();
+        const double* nrm = P.tri_normal + 3 * size_t(tri);
+        const double dn = fabs((pf[0] - cc[0]) * nrm[0] + (pf[1] - cc[1]) * nrm[1] + (pf[2] - cc[2]) * nrm[2]);
+        double x[3];
+        for (int a = 0; a < 3; ++a) x[a] = pf[a] - fa * (dn * nrm[a]);
+        // tangents and the inward normal
+        const double* fc = P.tri_fc + 3 * size_t(tri);
+        double n[3], t1[3], t2[3];
+        for (int a = 0; a < 3; ++a) {
+            n[a] = -nrm[a];
+            t1[a] = fc[a] - A[a];
+        }
+        const double m1 = sqrt(t1[0] * t1[0] + t1[1] * t1[1] + t1[2] * t1[2]);
+        for (int a = 0; a < 3; ++a) t1[a] = t1[a] / m1;
+        t2[0] = n[1] * t1[2] - n[2] * t1[1];
+        t2[1] = n[2] * t1[0] - n[0] * t1[2];
+        t2[2] = n[0] * t1[1] - n[1] * t1[0];
+        const double m2 = sqrt(t2[0] * t2[0] + t2[1] * t2[1] + t2[2] * t2[2]);
+        for (int a = 0; a < 3; ++a) t2[a] = t2[a] / m2;
+        // velocity models (ParticleEmitter.C:420-535)
+        double U[3];
+        const double vt = sqrt(kB * P.temperature / P.mass);
+        if (P.model == PICGPU_EMIT_MOST_PROBABLE_SPEED) {
+            const double vmp = sqrt(2.0 * kB * P.temperature / P.mass);
+            for (int a = 0; a < 3; ++a) U[a] = vmp * n[a];
+        } else {
+            double n1, n2;
+            polar_pair(r, n1, n2);
+            double tg[3];
+            for (int a = 0; a < 3; ++a) tg[a] = vt * (n1 * t1[a] + n2 * t2[a]);
+            double un;
+            if (P.model == PICGPU_EMIT_BIRD_MAXWELLIAN_FLUX) {
+                const double vmp = sqrt(2.0 * kB * P.temperature / P.mass);
+                double u = 0.0;
+                for (int it = 0; it < 1000; ++it) {
+                    u = 3.0 * (2.0 * r.uniform() - 1.0);
+                    const double pr = u < 0.0 ? -1.0 : 2.0 * u / 1.4142135623730951 * det_exp(0.5 - u * u);
+                    if (!(pr < r.uniform())) break;
+                }
+                un = vmp * u;
+            } else if (P.model == PICGPU_EMIT_HALF_MAXWELLIAN_FLUX) {
+                double n3, n4;
+                polar_pair(r, n3, n4);
+                un = fabs(n3) * vt;
+            } else {  // maxwellianFlux
+                const double R = r.uniform();
+                un = vt * sqrt(-2.0 * det_log(1.0 - R));
+            }
+            for (int a = 0; a < 3; ++a) U[a] = tg[a] + un * n[a];
+        }
+        for (int a = 0; a < 3; ++a)
+            if (P.constrain && P.m.empty[a]) x[a] = 0.0;
+        int tt = 0;
+        double y[3] = {0, 0, 0};
+        if (!locate_in_cell(P.m, c, x, tt, y)) *P.error = 1;
+        store_inject(P, P.first + k, 12 * c + tt, y, U);
+    }
+}
+
 // ------------------------------------------------------------- scan ------
 constexpr int kScanChunk = 1024;  // 256 threads x 4 counts
 
@@ -469,6 +608,10 @@ void launch_init_fill_lattice(const InitParams& P, cudaStream_t s) {
 void launch_init_occupancy(const int32_t* tet, long long n, int n_cells, int* counts, cudaStream_t s) {
     cudaMemsetAsync(counts, 0, size_t(n_cells) * sizeof(int), s);
     if (n > 0) init_occupancy_kernel<<<nblocks(n, 256, 152 * 64), 256, 0, s>>>(tet, n, counts);
+}
+
+void launch_inject(const InjectParams& P, cudaStream_t s) {
+    if (P.n > 0 || P.qconv) inject_kernel<<<std::max(1, nblocks(P.n, 256, 152 * 32)), 256, 0, s>>>(P);
 }
 
 void launch_init_minmax(const int* counts, int n, long long* out, cudaStream_t s) {

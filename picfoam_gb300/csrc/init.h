@@ -58,4 +58,33 @@ void launch_init_occupancy(const int32_t* tet, long long n, int n_cells, int* co
 // min, max and sum of counts[0..n) -> out[0..2].
 void launch_init_minmax(const int* counts, int n, long long* out, cudaStream_t s);
 
+// SimpleInjection through the ParticleEmitter: n parcels of one species on
+// one patch's face triangles.
+struct InjectParams {
+    DMesh m;
+    uint64_t seed;
+    uint32_t step;
+    int injector, species, model, constrain;
+    double mass, temperature;     // [kg], [K]
+    long long n;
+    int n_tri;
+    const double* tri_cum;        // n_tri + 1 cumulative triangle areas, tri_cum[0] = 0
+    const int* tri_cell;          // owner cell of triangle i
+    const int* tri_tet;           // local tet (2 face + k) whose face triangle it is
+    const double* tri_normal;     // 3 per triangle: outward unit face normal
+    const double* tri_fc;         // 3 per triangle: face centre
+    double area;                  // patch area (sum of the face areas)
+    double* qconv;                // floating patch charge (nullptr otherwise)
+    int patch;
+    double ejected_charge;        // n q w, taken off qconv[patch]
+    long long first;
+    int32_t* tet;
+    double* y64[3];
+    double* u64[3];
+    float* y32[3];
+    float* u32[3];
+    int* error;
+};
+void launch_inject(const InjectParams& P, cudaStream_t s);
+
 }  // namespace pgd

@@ -58,6 +58,19 @@ struct SpeciesBuf {
     float* u32[2][3] = {};
 };
 
+// A SimpleInjection boundary model on one patch.
+struct Injector {
+    picgpu_injection cfg{};
+    double remainder[PICGPU_MAX_SPECIES] = {};   // particleRemainder_
+    int n_tri = 0;
+    double area = 0.0;
+    double* tri_cum = nullptr;
+    int* tri_cell = nullptr;
+    int* tri_tet = nullptr;
+    double* tri_normal = nullptr;
+    double* tri_fc = nullptr;
+};
+
 struct EventPair {
     cudaEvent_t a, b;
     int phase;
@@ -113,6 +126,8 @@ struct picgpu_ctx {
     std::unique_ptr<pgd::MultigridPCG> mg;      // multigrid-preconditioned PCG (cfg.pcg_precond)
     int mg_outer = 0;                           // refinement steps of the last multigrid solve
     double* tet_vol = nullptr;                  // 12 tet volumes per geometry class (initial conditions)
+    std::vector<Injector> injectors;            // SimpleInjection boundary models
+    int* inj_err = nullptr;                     // an emitted parcel could not be located
     // batched ensembles and graph-stepped runs
     int n_cases = 1;
     int* n_dev = nullptr;          // species counts on the device (graph steps)
@@ -598,8 +613,89 @@ void fill_counts(picgpu_ctx* c, picgpu_step_stats* stats) {
 }
 
 // One PICCloud::evolve.
+// Makes room for `add` more particles after the n used slots of species s.
+picgpu_status reserve_species(picgpu_ctx* c, int s, long long add) {
+    SpeciesBuf& B = c->sp[s];
+    const long long need = B.n + add;
+    if (need > (1LL << 31)) return bad(c, PICGPU_CAPACITY, "more than 2^31 particles of one species");
+    if (need <= B.cap) return PICGPU_OK;
+    const long cap = long(std::min<long long>(need + need / 4 + 1024, 1LL << 31));
+    if (B.n == 0) return alloc_species(c, s, cap);
+    return grow_species(c, s, cap);
+}
+
+// boundaryModels().injection() (PICCloud.C:1435): SimpleInjection::injection
+// (SimpleInjection.C:197-240) for every injector, before the move.
+picgpu_status inject(picgpu_ctx* c) {
+    const double dt = c->cfg.dt;
+    const double t = double(c->step_index + 1) * dt;  // OpenFOAM advances the time before evolve
+    bool any_empty = c->m.empty[0] || c->m.empty[1] || c->m.empty[2];
+    for (size_t i = 0; i < c->injectors.size(); ++i) {
+        Injector& I = c->injectors[i];
+        if (t > I.cfg.end_time) continue;
+        for (int j = 0; j < I.cfg.n_species; ++j) {
+            const int sp = I.cfg.species[j];
+            const picgpu_species& S = c->cfg.species[sp];
+            const double np = I.cfg.frequency[j] / S.weight * dt + I.remainder[j];
+            const long long n = (long long)np;
+            I.remainder[j] = np - double(n);
+            if (n <= 0) continue;
+            picgpu_status st = reserve_species(c, sp, n);
+            if (st) return st;
+            SpeciesBuf& B = c->sp[sp];
+            pgd::InjectParams P{};
+            P.m = c->dm;
+            P.seed = c->cfg.seed;
+            P.step = uint32_t(c->step_index);
+            P.injector = int(i);
+            P.species = sp;
+            P.model = I.cfg.velocity_model;
+            P.constrain = any_empty;
+            P.mass = S.mass;
+            P.temperature = I.cfg.eV[j] * 1.602176634e-19 / 1.380649e-23;
+            P.n = n;
+            P.n_tri = I.n_tri;
+            P.tri_cum = I.tri_cum;
+            P.tri_cell = I.tri_cell;
+            P.tri_tet = I.tri_tet;
+            P.tri_normal = I.tri_normal;
+            P.tri_fc = I.tri_fc;
+            P.area = I.area;
+            P.patch = I.cfg.patch;
+            if (c->m.patches[I.cfg.patch].p.kind == PICGPU_PATCH_FLOATING) {
+                P.qconv = c->qconv;
+                P.ejected_charge = double(n) * S.charge * S.weight;
+            }
+            P.first = B.n;
+            P.tet = B.tet[B.cur];
+            for (int a = 0; a < 3; ++a) {
+                P.y64[a] = B.y64[B.cur][a];
+                P.u64[a] = B.u64[B.cur][a];
+                P.y32[a] = B.y32[B.cur][a];
+                P.u32[a] = B.u32[B.cur][a];
+            }
+            P.error = c->inj_err;
+            pgd::launch_inject(P, c->stream);
+            c->launches++;
+            // syncVelocityAtBoundary(-0.5) of the new parcels (ParticleEmitter.C:401)
+            if (c->cfg.sync_velocity_at_boundary && S.charge != 0.0 && c->cfg.pusher != PICGPU_PUSHER_NONE) {
+                pgd::MoveParams MP = move_params(c, sp, false);
+                MP.first = int(B.n);
+                MP.n = int(B.n + n);
+                pgd::launch_push_only(MP, c->mixed, -0.5 * dt, grid_for(c, n), c->stream);
+                c->launches++;
+            }
+            B.n += n;
+            B.alive += n;
+        }
+    }
+    CK(cudaGetLastError());
+    return PICGPU_OK;
+}
+
 picgpu_status one_step(picgpu_ctx* c, picgpu_step_stats* stats, bool fields) {
     picgpu_status s;
+    if (!c->injectors.empty() && (s = inject(c))) return s;
     if ((s = zero_accumulators(c))) return s;
     if ((s = move_species(c, false))) return s;
     if ((s = read_counters(c))) return s;
@@ -610,6 +706,11 @@ picgpu_status one_step(picgpu_ctx* c, picgpu_step_stats* stats, bool fields) {
                                               ? "particle velocity reached the speed of light"
                                               : "tracking exceeded track_max_steps for a particle");
     add_counters(c, stats);
+    if (!c->injectors.empty()) {
+        int ie = 0;
+        CK(cudaMemcpy(&ie, c->inj_err, sizeof(int), cudaMemcpyDeviceToHost));
+        if (ie) return bad(c, PICGPU_INVALID_ARG, "injection: an emitted parcel left its owner cell");
+    }
     if (c->cfg.sort_interval > 0 && (c->step_index + 1) % c->cfg.sort_interval == 0) {
         // cell re-sort (keeps each block's particles in a short cell range)
         PhaseScope ps(c, PICGPU_PHASE_SORT);
@@ -1413,6 +1514,57 @@ picgpu_status picgpu_initialise_fields(picgpu_ctx* c) {
     return PICGPU_OK;
 }
 
+// ------------------------------------------------------- injection ------
+picgpu_status picgpu_set_injection(picgpu_ctx* c, int n, const picgpu_injection* inj) {
+    if (!c || n < 0 || n > PICGPU_MAX_INJECTORS || (n > 0 && !inj)) return PICGPU_INVALID_ARG;
+    if (c->n_cases != 1) return bad(c, PICGPU_NOT_SUPPORTED, "injection: not for ensemble contexts");
+    for (Injector& I : c->injectors) {
+        dfree(c, I.tri_cum);
+        dfree(c, I.tri_cell);
+        dfree(c, I.tri_tet);
+        dfree(c, I.tri_normal);
+        dfree(c, I.tri_fc);
+    }
+    c->injectors.clear();
+    for (int i = 0; i < n; ++i) {
+        const picgpu_injection& q = inj[i];
+        if (q.patch < 0 || q.patch >= int(c->m.patches.size()))
+            return bad(c, PICGPU_INVALID_ARG, "injection: no such patch");
+        const int kind = c->m.patches[q.patch].p.kind;
+        if (kind == PICGPU_PATCH_CYCLIC || kind == PICGPU_PATCH_EMPTY)
+            return bad(c, PICGPU_INVALID_ARG, "injection: the patch must not be cyclic or empty");
+        if (q.velocity_model < PICGPU_EMIT_BIRD_MAXWELLIAN_FLUX || q.velocity_model > PICGPU_EMIT_HALF_MAXWELLIAN_FLUX)
+            return bad(c, PICGPU_INVALID_ARG, "injection: unknown velocityModel");
+        if (q.n_species < 0 || q.n_species > PICGPU_MAX_SPECIES)
+            return bad(c, PICGPU_INVALID_ARG, "injection: injectionTypeIds");
+        for (int j = 0; j < q.n_species; ++j) {
+            if (q.species[j] < 0 || q.species[j] >= c->cfg.n_species || !(c->cfg.species[q.species[j]].weight > 0))
+                return bad(c, PICGPU_INVALID_ARG, "injection: species not defined");
+            if (!(q.frequency[j] >= 0) || !(q.eV[j] >= 0))
+                return bad(c, PICGPU_INVALID_ARG, "injection: frequencies and eV must be >= 0");
+        }
+        const pg::PatchTriangles T = pg::patch_triangles(c->m, q.patch);
+        if (T.cell.empty()) return bad(c, PICGPU_INVALID_ARG, "injection: the patch has no boundary faces");
+        Injector I;
+        I.cfg = q;
+        I.n_tri = int(T.cell.size());
+        I.area = T.area;
+        picgpu_status st;
+        c->injectors.push_back(I);
+        Injector& J = c->injectors.back();
+        if ((st = upload(c, &J.tri_cum, T.cum)) || (st = upload(c, &J.tri_cell, T.cell)) ||
+            (st = upload(c, &J.tri_tet, T.tet)) || (st = upload(c, &J.tri_normal, T.normal)) ||
+            (st = upload(c, &J.tri_fc, T.centre)))
+            return st;
+    }
+    if (!c->inj_err) {
+        picgpu_status st = dalloc(c, &c->inj_err, 1);
+        if (st) return st;
+    }
+    CK(cudaMemset(c->inj_err, 0, sizeof(int)));
+    return PICGPU_OK;
+}
+
 // ------------------------------------------------ initial conditions ----
 // picInitialise (preProcess/picInitialise/picInitialise.C:30-319) for a
 // context; the placement runs on the device (csrc/init.cu).
@@ -1420,17 +1572,6 @@ namespace {
 
 constexpr double kBoltzmann = 1.380649e-23;
 constexpr double kElementary = 1.602176634e-19;
-
-// Makes room for `add` more particles after the n used slots of species s.
-picgpu_status reserve_species(picgpu_ctx* c, int s, long long add) {
-    SpeciesBuf& B = c->sp[s];
-    const long long need = B.n + add;
-    if (need > (1LL << 31)) return bad(c, PICGPU_CAPACITY, "initialise: more than 2^31 particles of one species");
-    if (need <= B.cap) return PICGPU_OK;
-    const long cap = long(std::min<long long>(need + need / 4 + 1024, 1LL << 31));
-    if (B.n == 0) return alloc_species(c, s, cap);
-    return grow_species(c, s, cap);
-}
 
 }  // namespace
 
@@ -1971,6 +2112,8 @@ picgpu_status picgpu_ensemble_case_stats(picgpu_ctx* c, int species, double* out
 }
 
 picgpu_status picgpu_step_graph(picgpu_ctx* c, int nsteps, int steps_per_graph, picgpu_step_stats* stats) {
+    if (c && !c->injectors.empty())
+        return bad(c, PICGPU_NOT_SUPPORTED, "step_graph: injection runs only in picgpu_step");
     if (!c || nsteps < 0 || steps_per_graph <= 0 || nsteps % steps_per_graph) return PICGPU_INVALID_ARG;
     if (!c->mixed || c->cfg.maxwell_solver != PICGPU_MAXWELL_NONE)
         return bad(c, PICGPU_NOT_SUPPORTED, "graph steps need the FP32 form and MaxwellSolver none");

@@ -26,11 +26,13 @@ __global__ void __launch_bounds__(256) move_kernel_fp64(MoveParams P) {
     warp_add_counter<double>(&P.counters->absorbed, ab);
 }
 
-// Push only, no tracking: initalizeLeapFrog (picInitialise.C:219-227) calls
-// the pusher's updateVelocity(p, -dt/2) on every parcel, moving or not.
+// Push only, no tracking, of slots [first, n): initalizeLeapFrog
+// (picInitialise.C:219-227) calls the pusher's updateVelocity(p, -dt/2) on
+// every parcel, moving or not; an emitted parcel is synchronised the same way
+// (ParticleEmitter.C:401, PICParcel.C:220-227).
 template <class Real>
 __global__ void __launch_bounds__(256) push_only_kernel(MoveParams P, Real tt) {
-    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < P.n; i += gridDim.x * blockDim.x) {
+    for (int i = P.first + blockIdx.x * blockDim.x + threadIdx.x; i < P.n; i += gridDim.x * blockDim.x) {
         const int tetg = P.p.tet[i];
         if (tetg < 0) continue;
         PState<Real> s;

@@ -39,6 +39,7 @@ def declare(lib, prefix, ctx_api=True):
     f("get_particles", i, [P, i, C.c_size_t, I32P, F64P, F64P, SZP])
     f("initialise_fields", i, [P])
     f("initialise", i, [P, C.POINTER(abi.Init), C.POINTER(abi.InitStats)])
+    f("set_injection", i, [P, i, C.POINTER(abi.Injection)])
     f("step", i, [P, i, C.POINTER(abi.StepStats)])
     f("move", i, [P, C.POINTER(abi.StepStats)])
     f("solve_poisson", i, [P, F64P, F64P, C.POINTER(abi.StepStats)])

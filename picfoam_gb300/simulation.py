@@ -135,6 +135,12 @@ class Simulation:
     def initialise_fields(self):
         self._check(self._fn("initialise_fields")(self._h))
 
+    def set_injection(self, injectors):
+        """SimpleInjection boundary models: a list of abi.Injection (empty
+        removes them)."""
+        arr = (abi.Injection * max(len(injectors), 1))(*injectors)
+        self._check(self._fn("set_injection")(self._h, len(injectors), arr))
+
     def initialise(self, init):
         """picInitialise: place the particles of an abi.Init on the device (or
         in the oracle), compute the fields, optionally solve them and apply
