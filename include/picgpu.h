@@ -181,6 +181,14 @@ typedef struct {
 /* Binary Coulomb collisions (CoulombCollisionModel.C:241-309). */
 enum { PICGPU_PAIRING_NANBU_YONEMURA = 0, PICGPU_PAIRING_TAKIZUKA_ABE = 1 };
 enum { PICGPU_COLLIDE_NANBU = 0, PICGPU_COLLIDE_PEREZ = 1 };
+/* WeightCorrection TypeNames: none, Nanbu (NanbuCorrection.C:50-66), SentokuKempNR
+ * (SentokuKempNonRelCorrection.C:50-125), SentokuKemp (SentokuKempCorrection.C:50-169) */
+enum {
+    PICGPU_WEIGHT_CORRECTION_NONE = 0,
+    PICGPU_WEIGHT_CORRECTION_NANBU = 1,
+    PICGPU_WEIGHT_CORRECTION_SENTOKU_KEMP_NR = 2,
+    PICGPU_WEIGHT_CORRECTION_SENTOKU_KEMP = 3
+};
 typedef struct {
     int32_t enabled;
     int32_t pairing;           /* PICGPU_PAIRING_*; TakizukaAbe needs equal species weights */
@@ -189,7 +197,7 @@ typedef struct {
     double  coulomb_log;       /* fixed coulombLog (> 0); 0: from the cell Debye length */
     int32_t calculate_bmin;    /* calculateBmin: de Broglie floor of the impact parameter */
     int32_t debye_drift;       /* Debye length: subtract the drift velocity */
-    int32_t weight_correction; /* 0: none, 1: Nanbu (NanbuCorrection.C:50-66) */
+    int32_t weight_correction; /* PICGPU_WEIGHT_CORRECTION_*: none, Nanbu, SentokuKempNR, SentokuKemp */
     int32_t pad;
 } picgpu_coulomb;
 

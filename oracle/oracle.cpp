@@ -1137,13 +1137,80 @@ double nanbu_cos_chi(double s, ocoll::Philox& r) {
 
 // NanbuWeightCorrectionModel::correctVelocity (NanbuCorrection.C:50-66): one
 // draw; each partner keeps its new velocity with probability w_other/w_self.
+// Sentoku-Kemp weight corrections (SentokuKempNonRelCorrection.C:50-125,
+// SentokuKempCorrection.C:50-169): the parcel of the larger weight gets the
+// weight-averaged velocity (momentum) plus an orthogonal kick restoring the
+// weight-averaged kinetic (total) energy, at a uniform azimuth.
+void sk_basis(const V3& a, double amag, V3& e2, V3& e3) {
+    e2 = v3(0.0, 1.0, 0.0);
+    e3 = v3(0.0, 0.0, 1.0);
+    const double up = std::sqrt(a.y * a.y + a.z * a.z);
+    if (up > 1.0e-300) {  // VSMALL
+        e2 = v3(0.0, a.z / up, -a.y / up);
+        const double den = amag * up;
+        e3 = v3((up * up) / den, -(a.x * a.y) / den, -(a.x * a.z) / den);
+    }
+}
+
+void sentoku_kemp_nr(double mass, double wr, const V3& pre, V3& U, ocoll::Philox& r) {
+    const V3 after = v3((1.0 - wr) * pre.x + wr * U.x, (1.0 - wr) * pre.y + wr * U.y, (1.0 - wr) * pre.z + wr * U.z);
+    const double afterE = (1.0 - wr) * 0.5 * mass * dotv(pre, pre) + wr * 0.5 * mass * dotv(U, U);
+    const double dE = afterE - 0.5 * mass * dotv(after, after);
+    if (!(dE > 0.0)) return;
+    V3 e2, e3;
+    sk_basis(after, std::sqrt(dotv(after, after)), e2, e3);
+    const double eps = 6.283185307179586 * r.uniform();  // twoPi * scalar01
+    const double sp = std::sqrt(dE * 2.0 / mass), ce = std::cos(eps), se = std::sin(eps);
+    U = v3(after.x + sp * (e2.x * ce + e3.x * se), after.y + sp * (e2.y * ce + e3.y * se),
+           after.z + sp * (e2.z * ce + e3.z * se));
+}
+
+void sentoku_kemp(double mass, double dw, const V3& pre, V3& U, ocoll::Philox& r) {
+    const double c = kC;
+    const double mpre = std::sqrt(dotv(pre, pre)) / c, mpost = std::sqrt(dotv(U, U)) / c;
+    const double g0 = 1.0 / std::sqrt(1.0 - mpre * mpre), g1 = 1.0 / std::sqrt(1.0 - mpost * mpost);
+    const V3 p0 = v3(mass * g0 * pre.x, mass * g0 * pre.y, mass * g0 * pre.z);
+    const V3 p1 = v3(mass * g1 * U.x, mass * g1 * U.y, mass * g1 * U.z);
+    const double mc = mass * c;
+    const double e0 = c * std::sqrt(dotv(p0, p0) + mc * mc), e1 = c * std::sqrt(dotv(p1, p1) + mc * mc);
+    const double aE = (1.0 - dw) * e0 + dw * e1;
+    const V3 aM = v3((1.0 - dw) * p0.x + dw * p1.x, (1.0 - dw) * p0.y + dw * p1.y, (1.0 - dw) * p0.z + dw * p1.z);
+    const double aMm = std::sqrt(dotv(aM, aM));
+    const double ge = aE / (mass * (c * c));
+    const double gq = aMm / mc;
+    const double gp = std::sqrt(1.0 + gq * gq);
+    if (!(gp < ge)) return;
+    const double dp = mass * c * std::sqrt(ge * ge - gp * gp);
+    V3 e2, e3;
+    sk_basis(aM, aMm, e2, e3);
+    const double eps = 6.283185307179586 * r.uniform();
+    const double ce = std::cos(eps), se = std::sin(eps);
+    const V3 ps = v3(aM.x + dp * (e2.x * ce + e3.x * se), aM.y + dp * (e2.y * ce + e3.y * se),
+                     aM.z + dp * (e2.z * ce + e3.z * se));
+    const double gs0 = std::sqrt(dotv(ps, ps)) / mc;
+    const double gs = std::sqrt(1.0 + gs0 * gs0);
+    U = v3(ps.x / (mass * gs), ps.y / (mass * gs), ps.z / (mass * gs));
+}
+
+// WeightCorrection: none, Nanbu (NanbuCorrection.C:50-66), SentokuKempNR,
+// SentokuKemp.
 void weight_correct(Oracle& o, Parcel& P, int sp, Parcel& Q, int sq, const V3& preP, const V3& preQ,
                     ocoll::Philox& r) {
-    if (o.cfg.coulomb.weight_correction != 1) return;
+    const int wc = o.cfg.coulomb.weight_correction;
     const double wP = o.cfg.species[sp].weight, wQ = o.cfg.species[sq].weight;
-    const double u = r.uniform();
-    if (u > wP / wQ) Q.U = preQ;
-    if (u > wQ / wP) P.U = preP;
+    if (wc == 1) {
+        const double u = r.uniform();
+        if (u > wP / wQ) Q.U = preQ;
+        if (u > wQ / wP) P.U = preP;
+    } else if (wc == 2 || wc == 3) {
+        if (wP > wQ) {
+            if (wc == 3) sentoku_kemp(o.cfg.species[sp].mass, wQ / wP, preP, P.U, r);
+            else sentoku_kemp_nr(o.cfg.species[sp].mass, wQ / wP, preP, P.U, r);
+        } else if (wP < wQ) {
+            if (wc == 3) sentoku_kemp(o.cfg.species[sq].mass, wP / wQ, preQ, Q.U, r);
+            else sentoku_kemp_nr(o.cfg.species[sq].mass, wP / wQ, preQ, Q.U, r);
+        }
+    }
 }
 
 // NanbuCollision::collide (NanbuCollision.C:60-135).

@@ -93,6 +93,7 @@ class IonMcc(C.Structure):
 
 PAIRING_NANBU_YONEMURA, PAIRING_TAKIZUKA_ABE = range(2)
 COLLIDE_NANBU, COLLIDE_PEREZ = range(2)
+WEIGHT_CORRECTION_NONE, WEIGHT_CORRECTION_NANBU, WEIGHT_CORRECTION_SENTOKU_KEMP_NR, WEIGHT_CORRECTION_SENTOKU_KEMP = range(4)
 
 
 class Coulomb(C.Structure):

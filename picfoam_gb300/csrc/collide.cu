@@ -615,16 +615,83 @@ struct CoulombParams {
     const unsigned* step_dev;
 };
 
-// NanbuWeightCorrectionModel::correctVelocity (NanbuCorrection.C:50-66).
-__device__ __forceinline__ void weight_correct(const CoulombSpecies& C, const CoulombParams& K, int a, int b,
-                                               V3d preP, V3d preQ, V3d& UP, V3d& UQ, Rng& r) {
-    if (K.weight_corr != 1) return;
-    const double u = r.uniform();
-    if (u > C.w[a] / C.w[b]) UQ = preQ;
-    if (u > C.w[b] / C.w[a]) UP = preP;
+// Sentoku-Kemp weight corrections: the parcel of the larger weight keeps the
+// weight-averaged velocity (momentum) of before and after the collision
+// plus a kick orthogonal to it that restores the weight-averaged kinetic
+// (total) energy; the kick's azimuth is uniform.  Non-relativistic:
+// SentokuKempNonRelCorrection.C:50-125; relativistic (momenta, total
+// energies, Lorentz factors): SentokuKempCorrection.C:50-169.
+__device__ void sk_basis(V3d a, double amag, V3d& e2, V3d& e3) {
+    e2 = {0.0, 1.0, 0.0};
+    e3 = {0.0, 0.0, 1.0};
+    const double up = sqrt(a.y * a.y + a.z * a.z);
+    if (up > 1.0e-300) {
+        e2 = {0.0, a.z / up, -a.y / up};
+        const double den = amag * up;
+        e3 = {(up * up) / den, -(a.x * a.y) / den, -(a.x * a.z) / den};
+    }
 }
 
-// NanbuCollision::collide (NanbuCollision.C:60-135).
+__device__ void sentoku_kemp_nr(double mass, double wr, V3d pre, V3d& U, Rng& r) {
+    const V3d after = {(1.0 - wr) * pre.x + wr * U.x, (1.0 - wr) * pre.y + wr * U.y, (1.0 - wr) * pre.z + wr * U.z};
+    const double afterE = (1.0 - wr) * 0.5 * mass * dotd(pre, pre) + wr * 0.5 * mass * dotd(U, U);
+    const double dE = afterE - 0.5 * mass * dotd(after, after);
+    if (!(dE > 0.0)) return;
+    V3d e2, e3;
+    sk_basis(after, sqrt(dotd(after, after)), e2, e3);
+    const double eps = 6.283185307179586 * r.uniform();
+    const double sp = sqrt(dE * 2.0 / mass), ce = cos(eps), se = sin(eps);
+    U = {after.x + sp * (e2.x * ce + e3.x * se), after.y + sp * (e2.y * ce + e3.y * se),
+         after.z + sp * (e2.z * ce + e3.z * se)};
+}
+
+__device__ void sentoku_kemp(double mass, double dw, V3d pre, V3d& U, Rng& r) {
+    const double c = kC;
+    const double mpre = sqrt(dotd(pre, pre)) / c, mpost = sqrt(dotd(U, U)) / c;
+    const double g0 = 1.0 / sqrt(1.0 - mpre * mpre), g1 = 1.0 / sqrt(1.0 - mpost * mpost);
+    const V3d p0 = {mass * g0 * pre.x, mass * g0 * pre.y, mass * g0 * pre.z};
+    const V3d p1 = {mass * g1 * U.x, mass * g1 * U.y, mass * g1 * U.z};
+    const double mc = mass * c;
+    const double e0 = c * sqrt(dotd(p0, p0) + mc * mc), e1 = c * sqrt(dotd(p1, p1) + mc * mc);
+    const double aE = (1.0 - dw) * e0 + dw * e1;
+    const V3d aM = {(1.0 - dw) * p0.x + dw * p1.x, (1.0 - dw) * p0.y + dw * p1.y, (1.0 - dw) * p0.z + dw * p1.z};
+    const double aMm = sqrt(dotd(aM, aM));
+    const double ge = aE / (mass * (c * c));
+    const double gq = aMm / mc;
+    const double gp = sqrt(1.0 + gq * gq);
+    if (!(gp < ge)) return;
+    const double dp = mass * c * sqrt(ge * ge - gp * gp);
+    V3d e2, e3;
+    sk_basis(aM, aMm, e2, e3);
+    const double eps = 6.283185307179586 * r.uniform();
+    const double ce = cos(eps), se = sin(eps);
+    const V3d ps = {aM.x + dp * (e2.x * ce + e3.x * se), aM.y + dp * (e2.y * ce + e3.y * se),
+                    aM.z + dp * (e2.z * ce + e3.z * se)};
+    const double gs0 = sqrt(dotd(ps, ps)) / mc;
+    const double gs = sqrt(1.0 + gs0 * gs0);
+    U = {ps.x / (mass * gs), ps.y / (mass * gs), ps.z / (mass * gs)};
+}
+
+// WeightCorrection (CoulombCollisionModel): none, Nanbu
+// (NanbuCorrection.C:50-66), SentokuKempNR, SentokuKemp.
+__device__ __forceinline__ void weight_correct(const CoulombSpecies& C, const CoulombParams& K, int a, int b,
+                                               V3d preP, V3d preQ, V3d& UP, V3d& UQ, Rng& r) {
+    if (K.weight_corr == 1) {
+        const double u = r.uniform();
+        if (u > C.w[a] / C.w[b]) UQ = preQ;
+        if (u > C.w[b] / C.w[a]) UP = preP;
+    } else if (K.weight_corr == 2 || K.weight_corr == 3) {
+        const bool rel = K.weight_corr == 3;
+        if (C.w[a] > C.w[b]) {
+            if (rel) sentoku_kemp(C.m[a], C.w[b] / C.w[a], preP, UP, r);
+            else sentoku_kemp_nr(C.m[a], C.w[b] / C.w[a], preP, UP, r);
+        } else if (C.w[a] < C.w[b]) {
+            if (rel) sentoku_kemp(C.m[b], C.w[a] / C.w[b], preQ, UQ, r);
+            else sentoku_kemp_nr(C.m[b], C.w[a] / C.w[b], preQ, UQ, r);
+        }
+    }
+}
+
 template <class R>
 __device__ void nanbu_collide(const CoulombSpecies& C, const CoulombParams& K, int a, int ia, int b, int ib,
                               double lD, double nP, double nQ, double nPQ, Rng& r) {
@@ -987,7 +1054,7 @@ int collide_init(CollideState& st, const picgpu_config& cfg, const DMesh& m, cud
     if (cfg.coulomb.enabled) {
         const picgpu_coulomb& co = cfg.coulomb;
         if (co.pairing < 0 || co.pairing > 1 || co.collide < 0 || co.collide > 1 || co.coulomb_log < 0 ||
-            co.weight_correction < 0 || co.weight_correction > 1) {
+            co.weight_correction < 0 || co.weight_correction > 3) {
             *msg = "Coulomb: unknown pairing, collide or weight-correction model";
             return PICGPU_INVALID_ARG;
         }

@@ -360,3 +360,46 @@ def test_nanbu_weight_correction_unequal_weights(oracle_backend):
     assert st.coulomb_pairs > 0
     T1 = temperatures(sim, case)
     assert T1[0] < T0[0] and T1[1] > T0[1]
+
+
+def kinetic_energies(sim, case):
+    """(non-relativistic, relativistic) kinetic energy of all parcels, weighted."""
+    enr = erel = 0.0
+    c = 299792458.0
+    for s in range(case.cfg.n_species):
+        _, _, U = sim.get_particles(s)
+        m, w = case.cfg.species[s].mass, case.cfg.species[s].weight
+        b2 = (U * U).sum(axis=1) / c ** 2
+        r = np.sqrt(1.0 - b2)
+        enr += w * 0.5 * m * (U * U).sum()
+        erel += w * m * c ** 2 * (b2 / (r * (1.0 + r))).sum()      # (gamma - 1) m c^2 without cancellation
+    return enr, erel
+
+
+@pytest.mark.parametrize("wc,collide", [(abi.WEIGHT_CORRECTION_SENTOKU_KEMP_NR, abi.COLLIDE_NANBU),
+                                        (abi.WEIGHT_CORRECTION_SENTOKU_KEMP, abi.COLLIDE_PEREZ)])
+def test_sentoku_kemp_conserves_energy_with_unequal_weights(oracle_backend, wc, collide):
+    """The heavier parcel takes the weight-averaged velocity plus an
+    orthogonal kick that restores the weight-averaged (kinetic or total)
+    energy, so unequal-weight collisions conserve the total energy exactly
+    (SentokuKempNonRelCorrection.C, SentokuKempCorrection.C); without a
+    correction they do not."""
+    def run(w):
+        case = cases.coulomb_relaxation(w_i_factor=2.5, weight_correction=w, collide=collide, m_i=4.0 * cases.M_E,
+                                        T_i=1.0)
+        sim = cases.build(case, backend=oracle_backend.OracleBackend(2))
+        e0 = kinetic_energies(sim, case)
+        st = sim.step(8)
+        assert st.coulomb_pairs > 0
+        e1 = kinetic_energies(sim, case)
+        k = 0 if wc == abi.WEIGHT_CORRECTION_SENTOKU_KEMP_NR else 1
+        return abs(e1[k] / e0[k] - 1), sim, case
+    err, sim, case = run(wc)
+    # exact for the kinetic energy (non-relativistic); round-off of the
+    # Lorentz factors for the total energy (relativistic)
+    assert err < (1e-12 if wc == abi.WEIGHT_CORRECTION_SENTOKU_KEMP_NR else 1e-8)
+    err_none, _, _ = run(abi.WEIGHT_CORRECTION_NONE)
+    assert err_none > 1e-3
+    T = temperatures(sim, case)
+    assert all(t > 0 for t in T)
+

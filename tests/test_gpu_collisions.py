@@ -144,3 +144,16 @@ def test_weight_correction_fp64_matches_oracle(gpu, oracle_backend):
         assert a.coulomb_pairs == b.coulomb_pairs > 0
     for s in range(2):
         assert close_fraction(g, o, s, 1e-8) > 0.99
+
+
+@pytest.mark.parametrize("wc,collide", [(abi.WEIGHT_CORRECTION_SENTOKU_KEMP_NR, abi.COLLIDE_NANBU),
+                                        (abi.WEIGHT_CORRECTION_SENTOKU_KEMP, abi.COLLIDE_PEREZ)])
+def test_sentoku_kemp_fp64_matches_oracle(gpu, oracle_backend, wc, collide):
+    case = cases.coulomb_relaxation(w_i_factor=2.5, weight_correction=wc, collide=collide, m_i=4.0 * cases.M_E,
+                                    T_i=1.0, ragged=True)
+    g, o, sg, so = run_pair(case, gpu, oracle_backend, 4)
+    for a, b in zip(sg, so):
+        assert a.coulomb_pairs == b.coulomb_pairs > 0
+    for s in range(2):
+        assert close_fraction(g, o, s, 1e-8) > 0.99
+
