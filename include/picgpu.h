@@ -242,6 +242,27 @@ typedef struct {
     double  scale_correction; /* factor on the prolonged coarse correction (0: 1.6) */
 } picgpu_multigrid;
 
+/* BinaryCollisionModel IsotropicScattering (SM/CollisionModels/
+ * BinaryCollisionModel/BinaryCollisionModel.C:229-545,
+ * IsotropicScattering/IsotropicScattering.C): no-time-counter collisions
+ * among the parcels of the neutral (charge 0) species of each cell, partners
+ * from the same octant sub-cell when it holds another parcel; optionally
+ * collisions of those parcels with the background gas of picgpu_mcc
+ * (gas_density, gas_temperature, gas_velocity) whose particles are of
+ * background_species. */
+enum { PICGPU_XS_HARD_SPHERE = 0, PICGPU_XS_VARIABLE_HARD_SPHERE = 1 };
+typedef struct {
+    int32_t enabled;
+    int32_t cross_section;        /* TotalCrossSectionModel: HardSphere / VariableHardSphere */
+    int32_t weight_correction;    /* WeightCorrection: PICGPU_WEIGHT_CORRECTION_* */
+    int32_t background_species;   /* species of the background gas (-1: no background collisions) */
+    double  diameter[PICGPU_MAX_SPECIES];  /* moleculeProperties diameter [m] */
+    double  omega[PICGPU_MAX_SPECIES];     /* moleculeProperties omega (VHS viscosity index) */
+    double  tref;                 /* VariableHardSphereCoeffs Tref [K] */
+    double  sigma_tcr_max_init;   /* picSigmaTcRMax start value [m^3/s]; 0: BinaryCollisionModel::initialize */
+    double  init_temperature;     /* its temperature [K] (0: 293.15) */
+} picgpu_binary;
+
 typedef struct {
     int32_t pusher;               /* PICGPU_PUSHER_* */
     int32_t field_weighting;      /* PICGPU_WEIGHTING_* */
@@ -269,6 +290,7 @@ typedef struct {
     picgpu_coulomb coulomb;
     picgpu_learned learned;
     picgpu_multigrid mg;
+    picgpu_binary binary;
 } picgpu_config;
 
 typedef struct {
@@ -298,6 +320,10 @@ typedef struct {
     int32_t learned_samples;                    /* training pairs collected so far */
     int32_t learned_fallback;                   /* 1 once the net was switched off: it did not cut iterations */
     int32_t pcg_refinements;                    /* last multigrid solve: FP64 refinement steps (0 with Jacobi) */
+    int64_t binary_candidates;                  /* BinaryCollisionModel: neutral pairs tested */
+    int64_t binary_collisions;                  /* accepted */
+    int64_t binary_background_candidates;       /* neutral parcel - background gas tests */
+    int64_t binary_background_collisions;
 } picgpu_step_stats;
 
 typedef struct picgpu_ctx picgpu_ctx;

@@ -83,6 +83,10 @@ enum : uint32_t {
     kStreamInitParticle = 7u << 28,   // per (species, cell, tet << 24 | k) or (species, cell, k)
     kStreamInitLattice = 8u << 28,    // per (species, lattice index)
     kStreamInject = 9u << 28,         // per (injector << 4 | species, step, parcel)
+    kStreamBinary = 10u << 28,        // neutral pair collisions per (cell, step)
+    kStreamBinaryBg = 11u << 28,      // neutral - background collisions per (cell, step)
+    kStreamBinaryRemainder = 12u << 28,
+    kStreamBinaryBgRemainder = 13u << 28,
 };
 
 // List cross section: interpolateXY (ListCrossSection.C:33-88): linear in

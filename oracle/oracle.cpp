@@ -162,6 +162,8 @@ struct Oracle {
         PatchTriangles tri;
     };
     std::vector<Injector> injectors;
+    // BinaryCollisionModel state per cell
+    std::vector<double> bsmax, brem, bbgrem;
 };
 
 // ------------------------------------------------------------ pushers -----
@@ -1475,8 +1477,191 @@ void coulomb_pairs(Oracle& o, std::vector<std::vector<std::vector<int>>>& occ, p
 
 // PICCloud::buildCellOccupancy (PICCloud.C:327-354) + collisions() (PICCloud.C:526-539):
 // Coulomb, then electron-neutral, then ion-neutral.
+// BinaryCollisionModel::performCollisions (BinaryCollisionModel.C:229-373):
+// per cell, the parcels of the neutral species (species order, then parcel
+// order) are split into octant sub-cells around the cell centre; the NTC
+// count rem + nC (nC - 1) / 2 * w_max (sigma_T c_r)_max dt / V of
+// candidates picks P at random and Q from P's sub-cell when it holds another
+// parcel (else from the cell); acceptance sigma_T c_r / (sigma_T c_r)_max
+// with the cell's value at the start, the maximum updated as it is exceeded;
+// IsotropicScattering (IsotropicScattering.C:67-100) and the weight
+// correction.  performBackgroundCollisions (:375-515): rem + nN n_bg
+// (sigma_T c_r)_max dt candidates against background velocities
+// sqrt(kT/m) N(0,1)^3 + drift (uniformBackground.C:121-127).
+double sigma_tcr(const picgpu_binary& bc, double dP, double dQ, double omP, double omQ, double mP, double mQ,
+                 double G, const V3& UP, const V3& UQ) {
+    const double dPQ = 0.5 * (dP + dQ);
+    const V3 g = sub(UP, UQ);
+    const double cR = std::sqrt(dotv(g, g));
+    if (cR < 1.0e-300) return 0.0;  // vSmall
+    double sig;
+    if (bc.cross_section == PICGPU_XS_VARIABLE_HARD_SPHERE) {
+        const double omPQ = 0.5 * (omP + omQ);
+        const double mR = mP * mQ / (mP + mQ);
+        sig = kPi * dPQ * dPQ * std::pow(2.0 * kBoltzmann * bc.tref / (mR * cR * cR), omPQ - 0.5) / G;
+    } else {
+        sig = kPi * dPQ * dPQ;
+    }
+    return sig * cR;
+}
+
+void iso_scatter(double mP, double mQ, V3& UP, V3& UQ, ocoll::Philox& r) {
+    const double M = mP + mQ;
+    const V3 Ucm = v3((mP * UP.x + mQ * UQ.x) / M, (mP * UP.y + mQ * UQ.y) / M, (mP * UP.z + mQ * UQ.z) / M);
+    const V3 g = sub(UP, UQ);
+    const double cR = std::sqrt(dotv(g, g));
+    const double cosT = 2.0 * r.uniform() - 1.0;
+    const double sinT = std::sqrt(1.0 - cosT * cosT);
+    const double phi = 6.283185307179586 * r.uniform();
+    const V3 pr = v3(cR * cosT, cR * (sinT * std::cos(phi)), cR * (sinT * std::sin(phi)));
+    UP = v3(Ucm.x + pr.x * mQ / M, Ucm.y + pr.y * mQ / M, Ucm.z + pr.z * mQ / M);
+    UQ = v3(Ucm.x - pr.x * mP / M, Ucm.y - pr.y * mP / M, Ucm.z - pr.z * mP / M);
+}
+
+void weight_correct_pair(int model, double wP, double wQ, double mP, double mQ, const V3& preP, const V3& preQ,
+                         V3& UP, V3& UQ, ocoll::Philox& r) {
+    if (model == 1) {
+        const double u = r.uniform();
+        if (u > wP / wQ) UQ = preQ;
+        if (u > wQ / wP) UP = preP;
+    } else if (model == 2 || model == 3) {
+        if (wP > wQ) {
+            if (model == 3) sentoku_kemp(mP, wQ / wP, preP, UP, r);
+            else sentoku_kemp_nr(mP, wQ / wP, preP, UP, r);
+        } else if (wP < wQ) {
+            if (model == 3) sentoku_kemp(mQ, wP / wQ, preQ, UQ, r);
+            else sentoku_kemp_nr(mQ, wP / wQ, preQ, UQ, r);
+        }
+    }
+}
+
+void binary_collisions(Oracle& o, const std::vector<std::vector<std::vector<int>>>& occ, picgpu_step_stats* st) {
+    const picgpu_binary& bc = o.cfg.binary;
+    const HexMesh& m = o.m;
+    const int nc = m.n_cells;
+    std::vector<int> ns;
+    for (int s = 0; s < o.cfg.n_species; ++s)
+        if (o.cfg.species[s].charge == 0.0) ns.push_back(s);
+    if (ns.empty()) return;
+    if (o.bsmax.empty()) {
+        double smax = bc.sigma_tcr_max_init;
+        if (!(smax > 0)) {
+            const int sp = bc.background_species >= 0 ? bc.background_species : ns[0];
+            const double T = bc.init_temperature > 0 ? bc.init_temperature : 293.15;
+            const double d = bc.diameter[sp];
+            smax = kPi * d * d * std::sqrt(2.0 * kBoltzmann * T / o.cfg.species[sp].mass);
+        }
+        o.bsmax.assign(nc, smax);
+        o.brem.resize(nc);
+        o.bbgrem.resize(nc);
+        for (int c = 0; c < nc; ++c) {
+            ocoll::Philox r0(o.cfg.seed, ocoll::kStreamBinaryRemainder, uint32_t(c), 0u);
+            o.brem[c] = r0.uniform();
+            ocoll::Philox r1(o.cfg.seed, ocoll::kStreamBinaryBgRemainder, uint32_t(c), 0u);
+            o.bbgrem[c] = r1.uniform();
+        }
+    }
+    const int K = int(ns.size());
+    double G[PICGPU_MAX_SPECIES][PICGPU_MAX_SPECIES], Gbg[PICGPU_MAX_SPECIES];
+    for (int a = 0; a < K; ++a)
+        for (int b = 0; b < K; ++b) G[a][b] = std::exp(std::lgamma(2.5 - 0.5 * (bc.omega[ns[a]] + bc.omega[ns[b]])));
+    const int bs = bc.background_species;
+    const bool bg = bs >= 0 && o.cfg.mcc.gas_density > 0;
+    for (int a = 0; a < K; ++a) Gbg[a] = bg ? std::exp(std::lgamma(2.5 - 0.5 * (bc.omega[ns[a]] + bc.omega[bs]))) : 1.0;
+    long long tested = 0, collided = 0, btested = 0, bcollided = 0;
+    const double dt = o.cfg.dt;
+    for (int c = 0; c < nc; ++c) {
+        std::vector<std::pair<int, int>> list;  // (neutral species k, parcel index)
+        double wmax = 0.0;
+        for (int a = 0; a < K; ++a) {
+            for (int i : occ[ns[a]][c]) list.emplace_back(a, i);
+            if (!occ[ns[a]][c].empty() && o.cfg.species[ns[a]].weight > wmax) wmax = o.cfg.species[ns[a]].weight;
+        }
+        const int nC = int(list.size());
+        auto vel = [&](int j) -> V3& { return o.cloud[ns[list[j].first]][list[j].second].U; };
+        if (nC > 1) {
+            std::vector<int> sub[8], which(nC);
+            for (int j = 0; j < nC; ++j) {
+                const Parcel& p = o.cloud[ns[list[j].first]][list[j].second];
+                const double* off = &m.cls_offset[size_t(m.cell_class[c]) * 24];
+                double rel[3];
+                for (int q = 0; q < 3; ++q)
+                    rel[q] = p.y[1] * off[3 * m.tt.tri[p.tet][0] + q] + p.y[2] * off[3 * m.tt.tri[p.tet][1] + q] +
+                             p.y[3] * off[3 * m.tt.tri[p.tet][2] + q];
+                const int oc = (rel[0] >= 0.0 ? 1 : 0) + (rel[1] >= 0.0 ? 2 : 0) + (rel[2] >= 0.0 ? 4 : 0);
+                sub[oc].push_back(j);
+                which[j] = oc;
+            }
+            const double smax0 = o.bsmax[c];
+            const double sel = o.brem[c] + 0.5 * double(nC) * double(nC - 1) * wmax * smax0 * dt / m.vol[c];
+            const long long nCand = (long long)sel;
+            o.brem[c] = sel - double(nCand);
+            ocoll::Philox r(o.cfg.seed, ocoll::kStreamBinary, uint32_t(c), uint32_t(o.step_index));
+            for (long long q = 0; q < nCand; ++q) {
+                const int P = int(r.uniform() * double(nC));
+                const std::vector<int>& S = sub[which[P]];
+                const int nSC = int(S.size());
+                int Q = P;
+                for (int it = 0; it < 1000 && Q == P; ++it) {
+                    if (nSC > 1) Q = S[int(r.uniform() * double(nSC))];
+                    else Q = int(r.uniform() * double(nC));
+                }
+                if (Q == P) continue;
+                const int a = list[P].first, b = list[Q].first;
+                const int sa = ns[a], sb = ns[b];
+                V3& UP = vel(P);
+                V3& UQ = vel(Q);
+                const double mP = o.cfg.species[sa].mass, mQ = o.cfg.species[sb].mass;
+                const double sTcR = sigma_tcr(bc, bc.diameter[sa], bc.diameter[sb], bc.omega[sa], bc.omega[sb], mP,
+                                              mQ, G[a][b], UP, UQ);
+                ++tested;
+                if (sTcR > o.bsmax[c]) o.bsmax[c] = sTcR;
+                if (sTcR / smax0 > r.uniform()) {
+                    const V3 preP = UP, preQ = UQ;
+                    iso_scatter(mP, mQ, UP, UQ, r);
+                    weight_correct_pair(bc.weight_correction, o.cfg.species[sa].weight, o.cfg.species[sb].weight,
+                                        mP, mQ, preP, preQ, UP, UQ, r);
+                    ++collided;
+                }
+            }
+        }
+        if (bg && nC > 0) {
+            const double smaxb = o.bsmax[c];
+            const double coll = o.bbgrem[c] + double(nC) * o.cfg.mcc.gas_density * smaxb * dt;
+            const long long nCand = (long long)coll;
+            o.bbgrem[c] = coll - double(nCand);
+            ocoll::Philox r(o.cfg.seed, ocoll::kStreamBinaryBg, uint32_t(c), uint32_t(o.step_index));
+            const double mb = o.cfg.species[bs].mass;
+            const double vth = std::sqrt(kBoltzmann * o.cfg.mcc.gas_temperature / mb);
+            for (long long q = 0; q < nCand; ++q) {
+                const int P = int(r.uniform() * double(nC));
+                const int a = list[P].first, sa = ns[a];
+                V3& UP = vel(P);
+                const double n0 = r.normal(), n1 = r.normal(), n2 = r.normal();
+                V3 Ub = v3(vth * n0 + o.cfg.mcc.gas_velocity[0], vth * n1 + o.cfg.mcc.gas_velocity[1],
+                           vth * n2 + o.cfg.mcc.gas_velocity[2]);
+                const double mP = o.cfg.species[sa].mass;
+                const double sTcR = sigma_tcr(bc, bc.diameter[sa], bc.diameter[bs], bc.omega[sa], bc.omega[bs], mP,
+                                              mb, Gbg[a], UP, Ub);
+                ++btested;
+                if (sTcR > o.bsmax[c]) o.bsmax[c] = sTcR;
+                if (sTcR / smaxb > r.uniform()) {
+                    iso_scatter(mP, mb, UP, Ub, r);
+                    ++bcollided;
+                }
+            }
+        }
+    }
+    if (st) {
+        st->binary_candidates += tested;
+        st->binary_collisions += collided;
+        st->binary_background_candidates += btested;
+        st->binary_background_collisions += bcollided;
+    }
+}
+
 void collisions(Oracle& o, picgpu_step_stats* st) {
-    if (!o.cfg.mcc.enabled && !o.cfg.coulomb.enabled && !o.cfg.ion_mcc.enabled) return;
+    if (!o.cfg.mcc.enabled && !o.cfg.coulomb.enabled && !o.cfg.ion_mcc.enabled && !o.cfg.binary.enabled) return;
     std::vector<std::vector<std::vector<int>>> occ(o.cfg.n_species,
                                                    std::vector<std::vector<int>>(o.m.n_cells));
     for (int s = 0; s < o.cfg.n_species; ++s)
@@ -1484,6 +1669,7 @@ void collisions(Oracle& o, picgpu_step_stats* st) {
     if (o.cfg.coulomb.enabled) coulomb_pairs(o, occ, st);
     if (o.cfg.mcc.enabled) mcc_background(o, occ[o.cfg.electron_species], st);
     if (o.cfg.ion_mcc.enabled) ion_mcc_background(o, occ[o.cfg.ion_mcc.ion_species], st);
+    if (o.cfg.binary.enabled) binary_collisions(o, occ, st);
 }
 
 void fill_counts(const Oracle& o, picgpu_step_stats* st) {

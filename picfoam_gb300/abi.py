@@ -112,6 +112,18 @@ class Learned(C.Structure):
     ]
 
 
+XS_HARD_SPHERE, XS_VARIABLE_HARD_SPHERE = range(2)
+
+
+class Binary(C.Structure):
+    _fields_ = [
+        ("enabled", C.c_int32), ("cross_section", C.c_int32), ("weight_correction", C.c_int32),
+        ("background_species", C.c_int32), ("diameter", C.c_double * MAX_SPECIES),
+        ("omega", C.c_double * MAX_SPECIES), ("tref", C.c_double), ("sigma_tcr_max_init", C.c_double),
+        ("init_temperature", C.c_double),
+    ]
+
+
 class Multigrid(C.Structure):
     _fields_ = [
         ("pre_sweeps", C.c_int32), ("post_sweeps", C.c_int32), ("coarsest_cells", C.c_int32),
@@ -133,7 +145,7 @@ class Config(C.Structure):
         ("sort_interval", C.c_int32), ("pcg_precond", C.c_int32),
         ("seed", C.c_uint64),
         ("mcc", Mcc), ("ion_mcc", IonMcc), ("coulomb", Coulomb), ("learned", Learned),
-        ("mg", Multigrid),
+        ("mg", Multigrid), ("binary", Binary),
     ]
 
 
@@ -200,6 +212,8 @@ class StepStats(C.Structure):
         ("learned_loss", C.c_double), ("learned_alpha", C.c_double), ("learned_residual", C.c_double),
         ("learned_active", C.c_int32), ("learned_samples", C.c_int32),
         ("learned_fallback", C.c_int32), ("pcg_refinements", C.c_int32),
+        ("binary_candidates", C.c_int64), ("binary_collisions", C.c_int64),
+        ("binary_background_candidates", C.c_int64), ("binary_background_collisions", C.c_int64),
     ]
 
     def as_dict(self):

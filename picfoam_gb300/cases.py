@@ -544,6 +544,42 @@ def empty_case(n_cells=(8, 8, 8), length=(0.01, 0.01, 0.01), sides=None, boxes=(
     return Case("empty", mesh, cfg, {}, [], {})
 
 
+def neutral_gas(n_cells=4, per_cell=50, n=1e21, T=300.0, T_x=None, d=4.17e-10, L=4e-4, dt=1e-7, seed=1234,
+                precision=abi.PREC_FP64, cross_section=abi.XS_HARD_SPHERE, omega=0.5, tref=273.0,
+                weight_correction=0, background=None):
+    """Neutral argon parcels (charge 0) in a periodic box with binary (DSMC)
+    collisions, MaxwellSolver none: BinaryCollisionModel IsotropicScattering
+    with hard spheres (or VHS).  T_x != T starts anisotropic; background =
+    (n_bg, T_bg) adds collisions with a background argon gas."""
+    sides = [patch(abi.PATCH_CYCLIC) for _ in range(6)]
+    mesh = block_mesh((n_cells,) * 3, (L,) * 3, sides)
+    n_c = n_cells ** 3
+    N = n_c * per_cell
+    w = n * L ** 3 / N
+    cfg = base_config(dt, [(M_AR, 0.0, w, True)], maxwell=abi.MAXWELL_NONE, precision=precision, seed=seed,
+                      electron_species=-1)
+    b = cfg.binary
+    b.enabled = 1
+    b.cross_section = cross_section
+    b.weight_correction = weight_correction
+    b.diameter[0] = d
+    b.omega[0] = omega
+    b.tref = tref
+    b.init_temperature = T
+    b.background_species = -1
+    if background is not None:
+        b.background_species = 0
+        cfg.mcc.gas_density = background[0]
+        cfg.mcc.gas_temperature = background[1]
+        cfg.mcc.gas_mass = M_AR
+    rng = np.random.Generator(np.random.Philox(seed))
+    tet, bary = uniform_in_cells(rng, np.arange(n_c), per_cell)
+    vt = math.sqrt(K_B * T / M_AR)
+    vx = math.sqrt(K_B * (T if T_x is None else T_x) / M_AR)
+    U = rng.standard_normal((N, 3)) * np.array([vx, vt, vt])
+    return Case("neutral_gas", mesh, cfg, {0: (tet, bary, U)}, [], dict(n=n, T=T, w=w, N=N, d=d, V=L ** 3))
+
+
 def build_ensemble(case, backend=None):
     """Create an ensemble Simulation (one context, n_cases mesh copies)."""
     from .simulation import EnsembleBackend, Simulation

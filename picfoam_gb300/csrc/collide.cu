@@ -672,6 +672,26 @@ __device__ void sentoku_kemp(double mass, double dw, V3d pre, V3d& U, Rng& r) {
     U = {ps.x / (mass * gs), ps.y / (mass * gs), ps.z / (mass * gs)};
 }
 
+// WeightCorrection by model for a pair of species weights wP, wQ: none,
+// Nanbu (NanbuCorrection.C:50-66), SentokuKempNR, SentokuKemp.
+__device__ void weight_correct_pair(int model, double wP, double wQ, double mP, double mQ, V3d preP, V3d preQ,
+                                    V3d& UP, V3d& UQ, Rng& r) {
+    if (model == 1) {
+        const double u = r.uniform();
+        if (u > wP / wQ) UQ = preQ;
+        if (u > wQ / wP) UP = preP;
+    } else if (model == 2 || model == 3) {
+        const bool rel = model == 3;
+        if (wP > wQ) {
+            if (rel) sentoku_kemp(mP, wQ / wP, preP, UP, r);
+            else sentoku_kemp_nr(mP, wQ / wP, preP, UP, r);
+        } else if (wP < wQ) {
+            if (rel) sentoku_kemp(mQ, wP / wQ, preQ, UQ, r);
+            else sentoku_kemp_nr(mQ, wP / wQ, preQ, UQ, r);
+        }
+    }
+}
+
 // WeightCorrection (CoulombCollisionModel): none, Nanbu
 // (NanbuCorrection.C:50-66), SentokuKempNR, SentokuKemp.
 __device__ __forceinline__ void weight_correct(const CoulombSpecies& C, const CoulombParams& K, int a, int b,
@@ -979,6 +999,199 @@ double host_uniform(uint64_t seed, uint32_t stream, uint32_t cell) {
     return (double(a) * 67108864.0 + double(b)) * (1.0 / 9007199254740992.0);
 }
 
+// ---------------------------------------------- binary (neutral) collisions --
+// BinaryCollisionModel::performCollisions (BinaryCollisionModel.C:229-373)
+// and performBackgroundCollisions (:375-515) with IsotropicScattering
+// (IsotropicScattering.C:67-139), one thread per cell, candidates in the
+// reference's order from the cell's own Philox streams.
+struct BinaryParams {
+    int n_cells;
+    const double* vol;
+    const int* cell_class;
+    const double* offset;             // 24 per geometry class
+    int ns;                           // neutral species
+    double m[PICGPU_MAX_SPECIES], w[PICGPU_MAX_SPECIES], d[PICGPU_MAX_SPECIES], om[PICGPU_MAX_SPECIES];
+    double G[PICGPU_MAX_SPECIES][PICGPU_MAX_SPECIES];   // exp(lgamma(2.5 - omega_PQ)) (VHS)
+    const int* start[PICGPU_MAX_SPECIES];
+    const int* idx[PICGPU_MAX_SPECIES];
+    DSpecies p[PICGPU_MAX_SPECIES];
+    int vhs, weight_corr;
+    double tref;
+    double* smax;
+    double* rem;
+    double* bgrem;
+    int* list;
+    int* oct;
+    double dt;
+    uint64_t seed;
+    uint32_t step;
+    const unsigned* step_dev;
+    // background gas (uniformBackground)
+    int bg;
+    double bg_n, bg_T, bg_m, bg_d, bg_om, bg_u[3];
+    double Gbg[PICGPU_MAX_SPECIES];
+    unsigned long long* counts;
+};
+
+// TotalCrossSectionModel::sigmaTcR: HardSphere (HardSphere.C:47-70) or
+// VariableHardSphere (VariableHardSphere.C:48-85).
+__device__ double sigma_tcr(const BinaryParams& B, double dP, double dQ, double omP, double omQ, double mP,
+                            double mQ, double G, V3d UP, V3d UQ) {
+    const double dPQ = 0.5 * (dP + dQ);
+    const V3d g = {UP.x - UQ.x, UP.y - UQ.y, UP.z - UQ.z};
+    const double cR = sqrt(dotd(g, g));
+    if (cR < 1.0e-300) return 0.0;
+    double sig;
+    if (B.vhs) {
+        const double omPQ = 0.5 * (omP + omQ);
+        const double mR = mP * mQ / (mP + mQ);
+        sig = kPi * dPQ * dPQ * pow(2.0 * kKb * B.tref / (mR * cR * cR), omPQ - 0.5) / G;
+    } else {
+        sig = kPi * dPQ * dPQ;
+    }
+    return sig * cR;
+}
+
+// IsotropicScattering::updateVelocity: isotropic post-collision relative
+// velocity in the centre-of-mass frame.
+__device__ void iso_scatter(double mP, double mQ, V3d& UP, V3d& UQ, Rng& r) {
+    const double M = mP + mQ;
+    const V3d Ucm = {(mP * UP.x + mQ * UQ.x) / M, (mP * UP.y + mQ * UQ.y) / M, (mP * UP.z + mQ * UQ.z) / M};
+    const V3d g = {UP.x - UQ.x, UP.y - UQ.y, UP.z - UQ.z};
+    const double cR = sqrt(dotd(g, g));
+    const double cosT = 2.0 * r.uniform() - 1.0;
+    const double sinT = sqrt(1.0 - cosT * cosT);
+    const double phi = 6.283185307179586 * r.uniform();
+    const V3d pr = {cR * cosT, cR * (sinT * cos(phi)), cR * (sinT * sin(phi))};
+    UP = {Ucm.x + pr.x * mQ / M, Ucm.y + pr.y * mQ / M, Ucm.z + pr.z * mQ / M};
+    UQ = {Ucm.x - pr.x * mP / M, Ucm.y - pr.y * mP / M, Ucm.z - pr.z * mP / M};
+}
+
+// The cell-relative position of particle i of species k: y1 a + y2 b + y3 c
+// with the corner offsets of its tet's face triangle.
+template <class R>
+__device__ int octant(const BinaryParams& B, int k, int i) {
+    const int tet = B.p[k].tet[i];
+    const int cell = tet / 12, t = tet - 12 * cell;
+    const double* off = B.offset + size_t(B.cell_class[cell]) * 24;
+    double y[3];
+    if (sizeof(R) == 8) {
+        y[0] = B.p[k].y64[0][i]; y[1] = B.p[k].y64[1][i]; y[2] = B.p[k].y64[2][i];
+    } else {
+        y[0] = B.p[k].y32[0][i]; y[1] = B.p[k].y32[1][i]; y[2] = B.p[k].y32[2][i];
+    }
+    double rel[3];
+    for (int a = 0; a < 3; ++a)
+        rel[a] = y[0] * off[3 * c_tetC.tri[t][0] + a] + y[1] * off[3 * c_tetC.tri[t][1] + a] +
+                 y[2] * off[3 * c_tetC.tri[t][2] + a];
+    // pos0(x) + 2 pos0(y) + 4 pos0(z)
+    return (rel[0] >= 0.0 ? 1 : 0) + (rel[1] >= 0.0 ? 2 : 0) + (rel[2] >= 0.0 ? 4 : 0);
+}
+
+template <class R>
+__global__ void __launch_bounds__(64) binary_kernel(BinaryParams B) {
+    const int c = blockIdx.x * blockDim.x + threadIdx.x;
+    if (c >= B.n_cells) return;
+    const uint32_t step = B.step_dev ? *B.step_dev : B.step;
+    int cnt[PICGPU_MAX_SPECIES], off[PICGPU_MAX_SPECIES];
+    int nC = 0, base = 0;
+    double wmax = 0.0;
+    for (int k = 0; k < B.ns; ++k) {
+        const int s0 = B.start[k][c];
+        cnt[k] = B.start[k][c + 1] - s0;
+        off[k] = nC;
+        nC += cnt[k];
+        base += s0;
+        if (cnt[k] > 0 && B.w[k] > wmax) wmax = B.w[k];
+    }
+    auto locate = [&](int j, int& k, int& i) {
+        k = 0;
+        while (k + 1 < B.ns && off[k + 1] <= j) ++k;
+        i = B.idx[k][B.start[k][c] + (j - off[k])];
+    };
+    unsigned long long tested = 0, collided = 0, btested = 0, bcollided = 0;
+    if (nC > 1) {
+        int* L = B.list + base;
+        int* O = B.oct + base;
+        int scount[8] = {0, 0, 0, 0, 0, 0, 0, 0};
+        for (int j = 0; j < nC; ++j) {
+            int k, i;
+            locate(j, k, i);
+            const int o = octant<R>(B, k, i);
+            O[j] = o;
+            ++scount[o];
+        }
+        int soff[8], cur[8];
+        int acc = 0;
+        for (int o = 0; o < 8; ++o) {
+            soff[o] = acc;
+            cur[o] = acc;
+            acc += scount[o];
+        }
+        for (int j = 0; j < nC; ++j) L[cur[O[j]]++] = j;
+        const double smax0 = B.smax[c];
+        const double sel = B.rem[c] + 0.5 * double(nC) * double(nC - 1) * wmax * smax0 * B.dt / B.vol[c];
+        const long long nCand = (long long)sel;
+        B.rem[c] = sel - double(nCand);
+        Rng r(B.seed, kStreamBinary, uint32_t(c), step);
+        for (long long q = 0; q < nCand; ++q) {
+            const int P = int(r.uniform() * double(nC));
+            const int oP = O[P];
+            const int nSC = scount[oP];
+            int Q = P;
+            for (int it = 0; it < 1000 && Q == P; ++it) {
+                if (nSC > 1) Q = L[soff[oP] + int(r.uniform() * double(nSC))];
+                else Q = int(r.uniform() * double(nC));
+            }
+            if (Q == P) continue;
+            int kP, iP, kQ, iQ;
+            locate(P, kP, iP);
+            locate(Q, kQ, iQ);
+            V3d UP = Vel<R>::get(B.p[kP], iP), UQ = Vel<R>::get(B.p[kQ], iQ);
+            const double sTcR =
+                sigma_tcr(B, B.d[kP], B.d[kQ], B.om[kP], B.om[kQ], B.m[kP], B.m[kQ], B.G[kP][kQ], UP, UQ);
+            ++tested;
+            if (sTcR > B.smax[c]) B.smax[c] = sTcR;
+            if (sTcR / smax0 > r.uniform()) {
+                const V3d preP = UP, preQ = UQ;
+                iso_scatter(B.m[kP], B.m[kQ], UP, UQ, r);
+                weight_correct_pair(B.weight_corr, B.w[kP], B.w[kQ], B.m[kP], B.m[kQ], preP, preQ, UP, UQ, r);
+                Vel<R>::put(B.p[kP], iP, UP);
+                Vel<R>::put(B.p[kQ], iQ, UQ);
+                ++collided;
+            }
+        }
+    }
+    if (B.bg && nC > 0) {
+        const double smaxb = B.smax[c];
+        const double coll = B.bgrem[c] + double(nC) * B.bg_n * smaxb * B.dt;
+        const long long nCand = (long long)coll;
+        B.bgrem[c] = coll - double(nCand);
+        Rng r(B.seed, kStreamBinaryBg, uint32_t(c), step);
+        const double vth = sqrt(kKb * B.bg_T / B.bg_m);
+        for (long long q = 0; q < nCand; ++q) {
+            const int P = int(r.uniform() * double(nC));
+            int k, i;
+            locate(P, k, i);
+            V3d UP = Vel<R>::get(B.p[k], i);
+            const double n0 = r.normal(), n1 = r.normal(), n2 = r.normal();
+            V3d Ub = {vth * n0 + B.bg_u[0], vth * n1 + B.bg_u[1], vth * n2 + B.bg_u[2]};
+            const double sTcR = sigma_tcr(B, B.d[k], B.bg_d, B.om[k], B.bg_om, B.m[k], B.bg_m, B.Gbg[k], UP, Ub);
+            ++btested;
+            if (sTcR > B.smax[c]) B.smax[c] = sTcR;
+            if (sTcR / smaxb > r.uniform()) {
+                iso_scatter(B.m[k], B.bg_m, UP, Ub, r);
+                Vel<R>::put(B.p[k], i, UP);
+                ++bcollided;
+            }
+        }
+    }
+    if (tested) atomicAdd(B.counts + 8, tested);
+    if (collided) atomicAdd(B.counts + 9, collided);
+    if (btested) atomicAdd(B.counts + 10, btested);
+    if (bcollided) atomicAdd(B.counts + 11, bcollided);
+}
+
 // Table k of a packed cross-section block (energies first), linear between
 // the bracketing nodes (ListCrossSection.C:33-88).
 double host_xs(const std::vector<double>& xs, int n, int k, double x) {
@@ -1038,18 +1251,18 @@ bool ascending(const double* e, int n) {
 }  // namespace
 
 int collide_init(CollideState& st, const picgpu_config& cfg, const DMesh& m, cudaStream_t s, std::string* msg) {
-    st.enabled = cfg.mcc.enabled || cfg.coulomb.enabled || cfg.ion_mcc.enabled;
+    st.enabled = cfg.mcc.enabled || cfg.coulomb.enabled || cfg.ion_mcc.enabled || cfg.binary.enabled;
     if (!st.enabled) return PICGPU_OK;
     const int nc = m.n_cells;
     if (dmalloc(&st.cell_start, size_t(PICGPU_MAX_SPECIES) * (nc + 1)) ||
         dmalloc(&st.cell_count, size_t(PICGPU_MAX_SPECIES) * (nc + 1)) || dmalloc(&st.cell_cursor, nc + 1) ||
-        dmalloc(&st.counts, 8) || dmalloc(&st.scan_tmp, (nc + 1) / 1024 + 8) || dmalloc(&st.overflow, 1) ||
+        dmalloc(&st.counts, kCollideCounts) || dmalloc(&st.scan_tmp, (nc + 1) / 1024 + 8) || dmalloc(&st.overflow, 1) ||
         (cfg.mcc.enabled && dmalloc(&st.iz_cell, nc))) {
         *msg = "collision state: device allocation failed";
         return PICGPU_OOM;
     }
     cudaMemsetAsync(st.overflow, 0, sizeof(int), s);
-    cudaMemsetAsync(st.counts, 0, 8 * sizeof(unsigned long long), s);
+    cudaMemsetAsync(st.counts, 0, kCollideCounts * sizeof(unsigned long long), s);
     if (st.iz_cell) cudaMemsetAsync(st.iz_cell, 0, size_t(nc) * sizeof(unsigned long long), s);
     if (cfg.coulomb.enabled) {
         const picgpu_coulomb& co = cfg.coulomb;
@@ -1153,6 +1366,57 @@ int collide_init(CollideState& st, const picgpu_config& cfg, const DMesh& m, cud
             upload_mcc(&st.isvmax, &st.iremainder, &st.ixs, xs, sv, cfg.seed, kStreamIonRemainder, nc, s, msg);
         if (e) return e;
     }
+    if (cfg.binary.enabled) {
+        const picgpu_binary& bc = cfg.binary;
+        if (bc.cross_section < 0 || bc.cross_section > 1 || bc.weight_correction < 0 || bc.weight_correction > 3 ||
+            bc.background_species >= cfg.n_species) {
+            *msg = "binary collisions: unknown cross-section or weight-correction model";
+            return PICGPU_INVALID_ARG;
+        }
+        int first = -1;
+        for (int k = 0; k < cfg.n_species; ++k) {
+            if (cfg.species[k].charge != 0.0) continue;
+            if (first < 0) first = k;
+            if (!(bc.diameter[k] > 0)) {
+                *msg = "binary collisions: every neutral species needs a diameter";
+                return PICGPU_INVALID_ARG;
+            }
+        }
+        if (bc.cross_section == PICGPU_XS_VARIABLE_HARD_SPHERE && !(bc.tref > 0)) {
+            *msg = "binary collisions: VariableHardSphere needs Tref";
+            return PICGPU_INVALID_ARG;
+        }
+        // picSigmaTcRMax: given, or BinaryCollisionModel::initialize
+        // (BinaryCollisionModel.C:548-600): sigmaT v_mp(T) of the background
+        // species when set, else of the first neutral species
+        double smax = bc.sigma_tcr_max_init;
+        if (!(smax > 0)) {
+            const int sp = bc.background_species >= 0 ? bc.background_species : first;
+            if (sp < 0) {
+                *msg = "binary collisions: no neutral species";
+                return PICGPU_INVALID_ARG;
+            }
+            const double T = bc.init_temperature > 0 ? bc.init_temperature : 293.15;
+            const double d = bc.diameter[sp];
+            smax = kPi * d * d * std::sqrt(2.0 * kKb * T / cfg.species[sp].mass);
+        }
+        std::vector<double> sm(nc, smax), r0(nc), r1(nc);
+        for (int c = 0; c < nc; ++c) {
+            r0[c] = host_uniform(cfg.seed, kStreamBinaryRemainder, uint32_t(c));
+            r1[c] = host_uniform(cfg.seed, kStreamBinaryBgRemainder, uint32_t(c));
+        }
+        if (dmalloc(&st.bsmax, nc) || dmalloc(&st.brem, nc) || dmalloc(&st.bbgrem, nc)) {
+            *msg = "binary collisions: device allocation failed";
+            return PICGPU_OOM;
+        }
+        cudaMemcpyAsync(st.bsmax, sm.data(), nc * sizeof(double), cudaMemcpyHostToDevice, s);
+        cudaMemcpyAsync(st.brem, r0.data(), nc * sizeof(double), cudaMemcpyHostToDevice, s);
+        cudaMemcpyAsync(st.bbgrem, r1.data(), nc * sizeof(double), cudaMemcpyHostToDevice, s);
+        if (cudaStreamSynchronize(s) != cudaSuccess) {
+            *msg = "binary collisions: upload failed";
+            return PICGPU_CUDA_ERROR;
+        }
+    }
     return PICGPU_OK;
 }
 
@@ -1160,7 +1424,7 @@ void collide_free(CollideState& st) {
     void* ptrs[] = {st.svmax,      st.remainder,   st.xs,     st.isvmax,   st.iremainder, st.ixs,
                     st.cell_start, st.cell_count,  st.cell_cursor, st.counts, st.scan_tmp, st.ncand,
                     st.cand_off,   st.stage,       st.flags,  st.pos,      st.stage_tmp, st.overflow,
-                    st.iz_cell};
+                    st.iz_cell,    st.bsmax,       st.brem,   st.bbgrem,   st.blist,      st.boct};
     for (void* p : ptrs)
         if (p) cudaFree(p);
     for (int s = 0; s < PICGPU_MAX_SPECIES; ++s) {
@@ -1234,7 +1498,7 @@ int sort_species(CollideState& st, const DMesh& m, int s, const DSpecies& src, c
     if (!st.cell_start) {
         if (dmalloc(&st.cell_start, size_t(PICGPU_MAX_SPECIES) * (nc + 1)) ||
             dmalloc(&st.cell_count, size_t(PICGPU_MAX_SPECIES) * (nc + 1)) || dmalloc(&st.cell_cursor, nc + 1) ||
-            dmalloc(&st.counts, 8) || dmalloc(&st.scan_tmp, (nc + 1) / 1024 + 8)) {
+            dmalloc(&st.counts, kCollideCounts) || dmalloc(&st.scan_tmp, (nc + 1) / 1024 + 8)) {
             *msg = "cell sort: device allocation failed";
             return PICGPU_OOM;
         }
@@ -1377,13 +1641,83 @@ __global__ void append_commit_kernel(int* n_dev, const int* add, long cap, int* 
 
 }  // namespace
 
-int run_collisions(CollideState& st, const CollideArgs& a, int64_t counts[8], long newn[], int swapped[],
+// The neutral species, the scratch lists and the launch of binary_kernel.
+int launch_binary(CollideState& st, const CollideArgs& a, std::string* msg, int64_t* launches,
+                  const unsigned* step_dev = nullptr) {
+    const picgpu_config& cfg = *a.cfg;
+    const picgpu_binary& bc = cfg.binary;
+    const int nc = a.m.n_cells;
+    BinaryParams B{};
+    B.n_cells = nc;
+    B.vol = a.m.vol;
+    B.cell_class = a.m.cell_class;
+    B.offset = a.m.offset;
+    long need = 0;
+    int sps[PICGPU_MAX_SPECIES];
+    for (int s = 0; s < a.n_species; ++s) {
+        if (cfg.species[s].charge != 0.0) continue;
+        const int k = B.ns++;
+        sps[k] = s;
+        B.m[k] = cfg.species[s].mass;
+        B.w[k] = cfg.species[s].weight;
+        B.d[k] = bc.diameter[s];
+        B.om[k] = bc.omega[s];
+        B.start[k] = st.cell_start + size_t(s) * (nc + 1);
+        B.idx[k] = st.idx[s];
+        B.p[k] = a.sp[s];
+        need += a.cap[s];
+    }
+    if (B.ns == 0) return PICGPU_OK;
+    for (int k = 0; k < B.ns; ++k)
+        for (int q = 0; q < B.ns; ++q) B.G[k][q] = std::exp(std::lgamma(2.5 - 0.5 * (B.om[k] + B.om[q])));
+    if (st.bcap < need) {
+        if (st.blist) cudaFree(st.blist);
+        if (st.boct) cudaFree(st.boct);
+        st.blist = st.boct = nullptr;
+        if (dmalloc(&st.blist, need) || dmalloc(&st.boct, need)) {
+            *msg = "binary collisions: device allocation failed";
+            return PICGPU_OOM;
+        }
+        st.bcap = need;
+    }
+    B.vhs = bc.cross_section == PICGPU_XS_VARIABLE_HARD_SPHERE;
+    B.weight_corr = bc.weight_correction;
+    B.tref = bc.tref;
+    B.smax = st.bsmax;
+    B.rem = st.brem;
+    B.bgrem = st.bbgrem;
+    B.list = st.blist;
+    B.oct = st.boct;
+    B.dt = cfg.dt;
+    B.seed = cfg.seed;
+    B.step = uint32_t(a.step);
+    B.step_dev = step_dev;
+    B.counts = st.counts;
+    const int bs = bc.background_species;
+    if (bs >= 0 && cfg.mcc.gas_density > 0) {
+        B.bg = 1;
+        B.bg_n = cfg.mcc.gas_density;
+        B.bg_T = cfg.mcc.gas_temperature;
+        B.bg_m = cfg.species[bs].mass;
+        B.bg_d = bc.diameter[bs];
+        B.bg_om = bc.omega[bs];
+        for (int q = 0; q < 3; ++q) B.bg_u[q] = cfg.mcc.gas_velocity[q];
+        for (int k = 0; k < B.ns; ++k) B.Gbg[k] = std::exp(std::lgamma(2.5 - 0.5 * (B.om[k] + B.bg_om)));
+    }
+    (void)sps;
+    if (a.mixed) binary_kernel<float><<<(nc + 63) / 64, 64, 0, a.stream>>>(B);
+    else binary_kernel<double><<<(nc + 63) / 64, 64, 0, a.stream>>>(B);
+    *launches += 1;
+    return PICGPU_OK;
+}
+
+int run_collisions(CollideState& st, const CollideArgs& a, int64_t counts[kCollideCounts], long newn[], int swapped[],
                    std::string* msg, int64_t* launches, double* phase_ms) {
     (void)phase_ms;
     const picgpu_config& cfg = *a.cfg;
     const int nc = a.m.n_cells;
     for (int s = 0; s < a.n_species; ++s) { newn[s] = a.n[s]; swapped[s] = 0; }
-    cudaMemsetAsync(st.counts, 0, 8 * sizeof(unsigned long long), a.stream);
+    cudaMemsetAsync(st.counts, 0, kCollideCounts * sizeof(unsigned long long), a.stream);
     // cell occupancy of every species (PICCloud::buildCellOccupancy)
     for (int s = 0; s < a.n_species; ++s) {
         const int e = occupancy(st, a, s, msg, launches);
@@ -1466,13 +1800,17 @@ int run_collisions(CollideState& st, const CollideArgs& a, int64_t counts[8], lo
         else ion_mcc_kernel<double><<<(nc + st.mcc_block - 1) / st.mcc_block, st.mcc_block, 0, a.stream>>>(M, a.sp[is]);
         *launches += 1;
     }
-    unsigned long long h[8];
+    if (cfg.binary.enabled) {
+        const int e = launch_binary(st, a, msg, launches);
+        if (e) return e;
+    }
+    unsigned long long h[kCollideCounts];
     cudaMemcpyAsync(h, st.counts, sizeof h, cudaMemcpyDeviceToHost, a.stream);
     if (cudaStreamSynchronize(a.stream) != cudaSuccess) {
         *msg = "collision step failed";
         return PICGPU_CUDA_ERROR;
     }
-    for (int k = 0; k < 8; ++k) counts[k] = (int64_t)h[k];
+    for (int k = 0; k < kCollideCounts; ++k) counts[k] = (int64_t)h[k];
     return cudaGetLastError() == cudaSuccess ? PICGPU_OK : PICGPU_CUDA_ERROR;
 }
 
@@ -1583,6 +1921,10 @@ int run_collisions_device(CollideState& st, const CollideArgs& a, int* n_dev, in
         if (a.mixed) ion_mcc_kernel<float><<<(nc + st.mcc_block - 1) / st.mcc_block, st.mcc_block, 0, a.stream>>>(M, a.sp[is]);
         else ion_mcc_kernel<double><<<(nc + st.mcc_block - 1) / st.mcc_block, st.mcc_block, 0, a.stream>>>(M, a.sp[is]);
         *launches += 1;
+    }
+    if (cfg.binary.enabled) {
+        const int e = launch_binary(st, a, msg, launches, step_dev);
+        if (e) return e;
     }
     return cudaGetLastError() == cudaSuccess ? PICGPU_OK : PICGPU_CUDA_ERROR;
 }

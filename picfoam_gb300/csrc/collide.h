@@ -18,6 +18,11 @@ struct Secondary {
     double ui[3];
 };
 
+// Counters of one collision step: MCC candidates, elastic, excitation,
+// ionisation; Coulomb pairs; ion MCC candidates, elastic, charge exchange;
+// binary (neutral) pairs tested, collisions; background tests, collisions.
+constexpr int kCollideCounts = 12;
+
 // Device state owned by the collision step.
 struct CollideState {
     int enabled = 0;
@@ -51,6 +56,14 @@ struct CollideState {
     double svmax_init = 0.0;                // initial (sigma v)_max of the electron MCC
     int mcc_block = 128;                    // threads per block of the MCC kernel (one cell each)
     unsigned long long* iz_cell = nullptr;  // MCC ionisations per cell (accumulated)
+    // BinaryCollisionModel: (sigma_T c_r)_max, selection and background
+    // remainders per cell; per-cell segments of the combined neutral list
+    double* bsmax = nullptr;
+    double* brem = nullptr;
+    double* bbgrem = nullptr;
+    int* blist = nullptr;
+    int* boct = nullptr;
+    long bcap = 0;
 };
 
 struct CollideArgs {
@@ -73,10 +86,9 @@ void collide_free(CollideState& st);
 // particles: src -> dst, *kept = particles written.
 int sort_species(CollideState& st, const DMesh& m, int s, const DSpecies& src, const DSpecies& dst, long n,
                  bool mixed, long* kept, cudaStream_t stream, std::string* msg, int64_t* launches);
-// counts: candidates, elastic, excitation, ionisation, coulomb pairs, ion
-// candidates, ion elastic, ion charge exchange; newn
+// counts: kCollideCounts counters (see above); newn
 // receives the species counts after MCC secondaries were appended.
-int run_collisions(CollideState& st, const CollideArgs& a, int64_t counts[8], long newn[], int swapped[],
+int run_collisions(CollideState& st, const CollideArgs& a, int64_t counts[kCollideCounts], long newn[], int swapped[],
                    std::string* msg, int64_t* launches, double* phase_ms);
 
 // Device-driven form of run_collisions for a step captured in a CUDA graph:

@@ -729,7 +729,7 @@ picgpu_status one_step(picgpu_ctx* c, picgpu_step_stats* stats, bool fields) {
     } else if ((s = compact(c, false))) {
         return s;
     }
-    if (c->cfg.mcc.enabled || c->cfg.coulomb.enabled || c->cfg.ion_mcc.enabled) {
+    if (c->cfg.mcc.enabled || c->cfg.coulomb.enabled || c->cfg.ion_mcc.enabled || c->cfg.binary.enabled) {
         if ((s = pgd_collisions(c, stats))) return s;
     }
     if ((s = charge_update(c))) return s;
@@ -765,7 +765,7 @@ picgpu_status pgd_collisions(picgpu_ctx* c, picgpu_step_stats* stats) {
         a.cap[s] = c->sp[s].cap;
     }
     a.stream = c->stream;
-    int64_t counts[8] = {};
+    int64_t counts[pgd::kCollideCounts] = {};
     long newn[PICGPU_MAX_SPECIES] = {};
     int swapped[PICGPU_MAX_SPECIES] = {};
     std::string msg;
@@ -799,6 +799,10 @@ picgpu_status pgd_collisions(picgpu_ctx* c, picgpu_step_stats* stats) {
         stats->ion_mcc_candidates += counts[5];
         stats->ion_mcc_elastic += counts[6];
         stats->ion_mcc_charge_exchange += counts[7];
+        stats->binary_candidates += counts[8];
+        stats->binary_collisions += counts[9];
+        stats->binary_background_candidates += counts[10];
+        stats->binary_background_collisions += counts[11];
     }
     return PICGPU_OK;
 }
@@ -854,7 +858,7 @@ long total_particles(const picgpu_ctx* c) {
 }
 
 bool any_collisions(const picgpu_ctx* c) {
-    return c->cfg.mcc.enabled || c->cfg.coulomb.enabled || c->cfg.ion_mcc.enabled;
+    return c->cfg.mcc.enabled || c->cfg.coulomb.enabled || c->cfg.ion_mcc.enabled || c->cfg.binary.enabled;
 }
 
 pgd::CollideArgs collide_args(picgpu_ctx* c) {
@@ -1027,7 +1031,7 @@ picgpu_status graph_replay(picgpu_ctx* c, int steps, picgpu_step_stats* stats, f
     CK(cudaMemcpyAsync(c->step_dev, &step0, sizeof step0, cudaMemcpyHostToDevice, c->stream));
     CK(cudaMemsetAsync(c->counters, 0, sizeof(pgd::MoveCounters) * PICGPU_MAX_SPECIES, c->stream));
     if (any_collisions(c)) {
-        CK(cudaMemsetAsync(c->coll.counts, 0, 8 * sizeof(unsigned long long), c->stream));
+        CK(cudaMemsetAsync(c->coll.counts, 0, pgd::kCollideCounts * sizeof(unsigned long long), c->stream));
         CK(cudaMemsetAsync(c->coll.overflow, 0, sizeof(int), c->stream));
     }
     cudaGraphExec_t g;
@@ -1045,7 +1049,7 @@ picgpu_status graph_replay(picgpu_ctx* c, int steps, picgpu_step_stats* stats, f
     if ((s = read_counters(c))) return s;
     int nd[PICGPU_MAX_SPECIES] = {};
     int ovf = 0;
-    unsigned long long h[8] = {};
+    unsigned long long h[pgd::kCollideCounts] = {};
     CK(cudaMemcpyAsync(nd, c->n_dev, sizeof nd, cudaMemcpyDeviceToHost, c->stream));
     if (any_collisions(c)) {
         CK(cudaMemcpyAsync(&ovf, c->coll.overflow, sizeof ovf, cudaMemcpyDeviceToHost, c->stream));
@@ -1074,6 +1078,10 @@ picgpu_status graph_replay(picgpu_ctx* c, int steps, picgpu_step_stats* stats, f
         stats->ion_mcc_candidates += (int64_t)h[5];
         stats->ion_mcc_elastic += (int64_t)h[6];
         stats->ion_mcc_charge_exchange += (int64_t)h[7];
+        stats->binary_candidates += (int64_t)h[8];
+        stats->binary_collisions += (int64_t)h[9];
+        stats->binary_background_candidates += (int64_t)h[10];
+        stats->binary_background_collisions += (int64_t)h[11];
     }
     c->step_index += steps;
     return PICGPU_OK;

@@ -403,3 +403,73 @@ def test_sentoku_kemp_conserves_energy_with_unequal_weights(oracle_backend, wc, 
     T = temperatures(sim, case)
     assert all(t > 0 for t in T)
 
+
+
+# ------------------------------------------------ binary (neutral) collisions
+def test_binary_hard_sphere_rate_and_conservation(oracle_backend):
+    """NTC with hard spheres: accepted collisions per step are
+    N n sigma <c_r> dt / 2 with <c_r> = sqrt(16 k T / (pi m)); every collision
+    conserves momentum and energy (equal weights)."""
+    case = cases.neutral_gas(n_cells=4, per_cell=60)
+    sim = cases.build(case, backend=oracle_backend.OracleBackend(1))
+    m = cases.M_AR
+
+    def moments():
+        _, _, U = sim.get_particles(0)
+        return U.sum(axis=0) * m, 0.5 * m * (U * U).sum()
+    p0, e0 = moments()
+    steps, coll, cand = 6, 0, 0
+    for _ in range(steps):
+        st = sim.step(1)
+        coll += st.binary_collisions
+        cand += st.binary_candidates
+    p1, e1 = moments()
+    md = case.meta
+    sigma = math.pi * md["d"] ** 2
+    cr = math.sqrt(16 * cases.K_B * md["T"] / (math.pi * m))
+    expect = steps * 0.5 * md["N"] * md["n"] * sigma * cr * case.cfg.dt
+    assert cand > coll > 0
+    assert abs(coll / expect - 1) < 5 / math.sqrt(expect) + 0.05
+    assert np.allclose(p1, p0, atol=1e-12 * np.abs(p0).max() + 1e-30)
+    assert abs(e1 / e0 - 1) < 1e-12
+
+
+def test_binary_relaxes_anisotropy(oracle_backend):
+    case = cases.neutral_gas(n_cells=3, per_cell=80, T=300.0, T_x=900.0, dt=4e-7)
+    sim = cases.build(case, backend=oracle_backend.OracleBackend(1))
+
+    def ratio():
+        _, _, U = sim.get_particles(0)
+        v = (U * U).mean(axis=0)
+        return v[0] / (0.5 * (v[1] + v[2]))
+    r0 = ratio()
+    sim.step(25)
+    r1 = ratio()
+    assert r0 > 2.5 and 1.0 < r1 < 0.6 * r0
+
+
+def test_binary_vhs_with_omega_one_half_is_hard_sphere(oracle_backend):
+    """VHS at omega = 1/2 has the factor (...)^0 / Gamma(2) = 1: the run is the
+    hard-sphere run bit for bit."""
+    out = []
+    for xs in (abi.XS_HARD_SPHERE, abi.XS_VARIABLE_HARD_SPHERE):
+        case = cases.neutral_gas(n_cells=3, per_cell=40, cross_section=xs, omega=0.5)
+        sim = cases.build(case, backend=oracle_backend.OracleBackend(1))
+        st = sim.step(3)
+        out.append((st.binary_collisions, sim.get_particles(0)[2]))
+    assert out[0][0] == out[1][0] > 0 and np.array_equal(out[0][1], out[1][1])
+
+
+def test_binary_background_collision_rate(oracle_backend):
+    """Neutral parcels against a background gas: n_bg sigma <c_r> dt
+    collisions per parcel and step."""
+    nb, T = 2e21, 300.0
+    case = cases.neutral_gas(n_cells=3, per_cell=40, n=1e18, background=(nb, T))
+    sim = cases.build(case, backend=oracle_backend.OracleBackend(1))
+    steps, coll = 5, 0
+    for _ in range(steps):
+        coll += sim.step(1).binary_background_collisions
+    md = case.meta
+    cr = math.sqrt(16 * cases.K_B * T / (math.pi * cases.M_AR))
+    expect = steps * md["N"] * nb * math.pi * md["d"] ** 2 * cr * case.cfg.dt
+    assert coll > 50 and abs(coll / expect - 1) < 5 / math.sqrt(expect) + 0.05

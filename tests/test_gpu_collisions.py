@@ -157,3 +157,32 @@ def test_sentoku_kemp_fp64_matches_oracle(gpu, oracle_backend, wc, collide):
     for s in range(2):
         assert close_fraction(g, o, s, 1e-8) > 0.99
 
+
+
+@pytest.mark.parametrize("xs,omega,background", [(abi.XS_HARD_SPHERE, 0.5, None),
+                                                 (abi.XS_VARIABLE_HARD_SPHERE, 0.81, None),
+                                                 (abi.XS_HARD_SPHERE, 0.5, (2e21, 300.0))])
+def test_binary_collisions_fp64_match_oracle(gpu, oracle_backend, xs, omega, background):
+    """BinaryCollisionModel: the same candidates per step (the NTC counts
+    depend on the running (sigma_T c_r)_max), collisions within a few (the
+    acceptance draws compare against transcendental results), and velocities
+    equal to round-off for nearly all parcels."""
+    case = cases.neutral_gas(n_cells=4, per_cell=50, cross_section=xs, omega=omega, background=background,
+                             n=1e21 if background is None else 2e19)
+    g, o, sg, so = run_pair(case, gpu, oracle_backend, 4)
+    for a, b in zip(sg, so):
+        assert abs(a.binary_candidates - b.binary_candidates) <= 2
+        assert abs(a.binary_collisions - b.binary_collisions) <= 2
+        assert abs(a.binary_background_collisions - b.binary_background_collisions) <= 2
+    assert sum(a.binary_collisions + a.binary_background_collisions for a in sg) > 50
+    assert close_fraction(g, o, 0, 1e-9) > 0.99
+
+
+def test_binary_collisions_fp32_conserve_energy(gpu):
+    case = cases.neutral_gas(n_cells=4, per_cell=50, precision=abi.PREC_MIXED)
+    g = cases.build(case, backend=gpu)
+    _, _, U0 = g.get_particles(0)
+    st = g.step(4)
+    _, _, U1 = g.get_particles(0)
+    assert st.binary_collisions > 20
+    assert abs((U1 * U1).sum() / (U0 * U0).sum() - 1) < 1e-5
