@@ -20,6 +20,7 @@
 #include <cstring>
 #include <memory>
 #include <string>
+#include <thread>
 #include <vector>
 
 #include "collide.h"
@@ -56,6 +57,91 @@ struct SpeciesBuf {
     double* u64[2][3] = {};
     float* y32[2][3] = {};
     float* u32[2][3] = {};
+};
+
+// Host <-> device copies of caller (pageable) arrays through a pinned ring of
+// two slots: host threads copy chunk k into a slot while the DMA engine moves
+// chunk k - 1, so the copy runs at the host's memcpy bandwidth over all its
+// cores instead of through the driver's single bounce buffer.
+struct HostStager {
+    static constexpr size_t kSlot = size_t(64) << 20;
+    char* pinned = nullptr;
+    cudaEvent_t ev[2] = {nullptr, nullptr};
+    bool ready = false;
+
+    bool init() {
+        if (ready) return true;
+        if (cudaMallocHost(&pinned, 2 * kSlot) != cudaSuccess) return false;
+        for (int k = 0; k < 2; ++k)
+            if (cudaEventCreateWithFlags(&ev[k], cudaEventDisableTiming) != cudaSuccess) return false;
+        ready = true;
+        return true;
+    }
+    void release() {
+        if (pinned) cudaFreeHost(pinned);
+        for (auto& e : ev)
+            if (e) cudaEventDestroy(e);
+        pinned = nullptr;
+        ev[0] = ev[1] = nullptr;
+        ready = false;
+    }
+    static void par_copy(char* dst, const char* src, size_t n) {
+        unsigned t = std::thread::hardware_concurrency();
+        t = std::max(1u, std::min(t, 16u));
+        if (n < (size_t(4) << 20) || t == 1) {
+            std::memcpy(dst, src, n);
+            return;
+        }
+        std::vector<std::thread> th;
+        const size_t part = (n + t - 1) / t;
+        for (unsigned k = 0; k < t; ++k) {
+            const size_t a = k * part, b = std::min(n, a + part);
+            if (a >= b) break;
+            th.emplace_back([=] { std::memcpy(dst + a, src + a, b - a); });
+        }
+        for (auto& x : th) x.join();
+    }
+    cudaError_t upload(void* dev, const void* host, size_t n, cudaStream_t s) {
+        if (n < (size_t(8) << 20) || !init()) return cudaMemcpyAsync(dev, host, n, cudaMemcpyHostToDevice, s);
+        const char* src = static_cast<const char*>(host);
+        char* dst = static_cast<char*>(dev);
+        int k = 0;
+        for (size_t off = 0; off < n; off += kSlot, k ^= 1) {
+            const size_t len = std::min(kSlot, n - off);
+            cudaError_t e = cudaEventSynchronize(ev[k]);  // the slot's previous DMA is done
+            if (e != cudaSuccess) return e;
+            par_copy(pinned + k * kSlot, src + off, len);
+            if ((e = cudaMemcpyAsync(dst + off, pinned + k * kSlot, len, cudaMemcpyHostToDevice, s))) return e;
+            if ((e = cudaEventRecord(ev[k], s))) return e;
+        }
+        return cudaSuccess;
+    }
+    cudaError_t download(void* host, const void* dev, size_t n, cudaStream_t s) {
+        if (n < (size_t(8) << 20) || !init()) {
+            cudaError_t e = cudaMemcpyAsync(host, dev, n, cudaMemcpyDeviceToHost, s);
+            return e ? e : cudaStreamSynchronize(s);
+        }
+        char* dst = static_cast<char*>(host);
+        const char* src = static_cast<const char*>(dev);
+        const size_t nch = (n + kSlot - 1) / kSlot;
+        cudaError_t e;
+        // DMA of chunk k + 1 runs while the host drains chunk k
+        if ((e = cudaMemcpyAsync(pinned, src, std::min(kSlot, n), cudaMemcpyDeviceToHost, s))) return e;
+        if ((e = cudaEventRecord(ev[0], s))) return e;
+        for (size_t k = 0; k < nch; ++k) {
+            const int slot = int(k & 1);
+            if (k + 1 < nch) {
+                const size_t off = (k + 1) * kSlot, len = std::min(kSlot, n - off);
+                if ((e = cudaMemcpyAsync(pinned + (slot ^ 1) * kSlot, src + off, len, cudaMemcpyDeviceToHost, s)))
+                    return e;
+                if ((e = cudaEventRecord(ev[slot ^ 1], s))) return e;
+            }
+            if ((e = cudaEventSynchronize(ev[slot]))) return e;
+            const size_t off = k * kSlot, len = std::min(kSlot, n - off);
+            par_copy(dst + off, pinned + slot * kSlot, len);
+        }
+        return cudaSuccess;
+    }
 };
 
 // A SimpleInjection boundary model on one patch.
@@ -128,6 +214,13 @@ struct picgpu_ctx {
     double* tet_vol = nullptr;                  // 12 tet volumes per geometry class (initial conditions)
     std::vector<Injector> injectors;            // SimpleInjection boundary models
     int* inj_err = nullptr;                     // an emitted parcel could not be located
+    // row-major host arrays staged on the device (set/get_particles)
+    int32_t* rows_tet = nullptr;
+    double* rows_y = nullptr;
+    double* rows_u = nullptr;
+    size_t rows_cap = 0;
+    int* inj_flag = nullptr;                    // device flag of the row checks
+    HostStager stager;                          // pinned ring for caller arrays
     // batched ensembles and graph-stepped runs
     int n_cases = 1;
     int* n_dev = nullptr;          // species counts on the device (graph steps)
@@ -1342,7 +1435,8 @@ static picgpu_status create_with_mesh(picgpu_ctx* c, const picgpu_config* cfg) {
         (s = dalloc(c, &c->q, nc)) || (s = dalloc(c, &c->part, 4 * size_t(pgd::pcg_blocks(int(nc))) + 8)) ||
         (s = dalloc(c, &c->st, 1)) || (s = dalloc(c, &c->counters, PICGPU_MAX_SPECIES)) ||
         (s = dalloc(c, &c->diag, 64)) || (s = dalloc(c, &c->n_dev, PICGPU_MAX_SPECIES)) ||
-        (s = dalloc(c, &c->first_dev, PICGPU_MAX_SPECIES)) || (s = dalloc(c, &c->step_dev, 1)))
+        (s = dalloc(c, &c->first_dev, PICGPU_MAX_SPECIES)) || (s = dalloc(c, &c->step_dev, 1)) ||
+        (s = dalloc(c, &c->inj_flag, 1)))
         return s;
     if (c->mixed && ((s = dalloc(c, &c->acc9, size_t(cfg->n_species) * 9 * nc)) ||
                      (s = dalloc(c, &c->Ec4, 9 * nc))))
@@ -1412,6 +1506,7 @@ void picgpu_destroy(picgpu_ctx* c) {
     if (c->replay_ev[0]) { cudaEventDestroy(c->replay_ev[0]); cudaEventDestroy(c->replay_ev[1]); }
     if (c->st_host) cudaFreeHost(c->st_host);
     if (c->counters_host) cudaFreeHost(c->counters_host);
+    c->stager.release();
     if (c->stream) cudaStreamDestroy(c->stream);
     delete c;
 }
@@ -1427,16 +1522,43 @@ picgpu_status picgpu_mesh_query(const picgpu_ctx* c, picgpu_mesh_info* info) {
     return PICGPU_OK;
 }
 
+// Device staging of row-major host arrays (n tets, n x 3 bary, n x 3 U).
+static picgpu_status ensure_rows(picgpu_ctx* c, size_t n) {
+    if (c->rows_cap >= n) return PICGPU_OK;
+    dfree(c, c->rows_tet);
+    dfree(c, c->rows_y);
+    dfree(c, c->rows_u);
+    c->rows_cap = 0;
+    const size_t cap = std::max<size_t>(n, 1024);
+    picgpu_status s;
+    if ((s = dalloc(c, &c->rows_tet, cap)) || (s = dalloc(c, &c->rows_y, 3 * cap)) ||
+        (s = dalloc(c, &c->rows_u, 3 * cap)))
+        return s;
+    c->rows_cap = cap;
+    return PICGPU_OK;
+}
+
 picgpu_status picgpu_set_particles(picgpu_ctx* c, int species, size_t n, const int32_t* tet,
                                    const double* bary, const double* U) {
     if (!c || species < 0 || species >= c->cfg.n_species) return PICGPU_INVALID_ARG;
     if (n && (!tet || !bary || !U)) return PICGPU_INVALID_ARG;
     if (n > size_t(1) << 31) return bad(c, PICGPU_INVALID_ARG, "at most 2^31 particles per species");
-    const long long ntet = 12LL * c->m.n_cells;
-    for (size_t i = 0; i < n; ++i)
-        if (tet[i] < 0 || tet[i] >= ntet) return bad(c, PICGPU_INVALID_ARG, "particles: tet index out of range");
-    SpeciesBuf& B = c->sp[species];
     picgpu_status s;
+    if ((s = ensure_rows(c, n))) return s;
+    // the rows go to the device as they are; the checks and the column
+    // conversion run there
+    if (n) {
+        CK(c->stager.upload(c->rows_tet, tet, n * sizeof(int32_t), c->stream));
+        CK(c->stager.upload(c->rows_y, bary, 3 * n * sizeof(double), c->stream));
+        CK(c->stager.upload(c->rows_u, U, 3 * n * sizeof(double), c->stream));
+        CK(cudaMemsetAsync(c->inj_flag, 0, sizeof(int), c->stream));
+        pgd::launch_check_tets(c->rows_tet, long(n), 12LL * c->m.n_cells, c->inj_flag, c->stream);
+        int badt = 0;
+        CK(cudaMemcpyAsync(&badt, c->inj_flag, sizeof(int), cudaMemcpyDeviceToHost, c->stream));
+        CK(cudaStreamSynchronize(c->stream));
+        if (badt) return bad(c, PICGPU_INVALID_ARG, "particles: tet index out of range");
+    }
+    SpeciesBuf& B = c->sp[species];
     if (long(n) > B.cap) {
         const long cap = std::max<long>(long(n) + long(n) / 4, c->cfg.species[species].capacity_hint);
         if ((s = alloc_species(c, species, cap))) return s;
@@ -1444,23 +1566,9 @@ picgpu_status picgpu_set_particles(picgpu_ctx* c, int species, size_t n, const i
     B.cur = 0;
     B.n = long(n);
     B.alive = long(n);
-    CK(cudaMemcpy(B.tet[0], tet, n * sizeof(int32_t), cudaMemcpyHostToDevice));
-    std::vector<double> col(n);
-    std::vector<float> colf(n);
-    for (int a = 0; a < 3; ++a) {
-        for (int which = 0; which < 2; ++which) {
-            const double* src = which == 0 ? bary : U;
-            for (size_t i = 0; i < n; ++i) col[i] = src[3 * i + a];
-            if (c->mixed) {
-                for (size_t i = 0; i < n; ++i) colf[i] = float(col[i]);
-                CK(cudaMemcpy(which == 0 ? B.y32[0][a] : B.u32[0][a], colf.data(), n * sizeof(float),
-                              cudaMemcpyHostToDevice));
-            } else {
-                CK(cudaMemcpy(which == 0 ? B.y64[0][a] : B.u64[0][a], col.data(), n * sizeof(double),
-                              cudaMemcpyHostToDevice));
-            }
-        }
-    }
+    pgd::launch_scatter_rows(c->rows_tet, c->rows_y, c->rows_u, long(n), view(c, species, 0), c->mixed, c->stream);
+    CK(cudaStreamSynchronize(c->stream));
+    CK(cudaGetLastError());
     return PICGPU_OK;
 }
 
@@ -1475,38 +1583,31 @@ picgpu_status picgpu_get_particles(picgpu_ctx* c, int species, size_t cap, int32
     if (!c || !nout || species < 0 || species >= c->cfg.n_species) return PICGPU_INVALID_ARG;
     CK(cudaStreamSynchronize(c->stream));
     SpeciesBuf& B = c->sp[species];
-    const size_t n = size_t(B.n);
-    std::vector<int32_t> t(n);
-    CK(cudaMemcpy(t.data(), B.tet[B.cur], n * sizeof(int32_t), cudaMemcpyDeviceToHost));
-    size_t alive = 0;
-    for (size_t i = 0; i < n; ++i) alive += t[i] >= 0;
-    *nout = alive;
+    // compact into the scratch half of the double buffer (the store itself is
+    // left as it is), then rows on the device, one copy per array
+    pgd::DSpecies src = view(c, species, B.cur);
+    long kept = B.n;
+    if (B.n > 0) {
+        const long nblk = pgd::compact_blocks(B.n);
+        picgpu_status st = ensure_scan(c, nblk + 1);
+        if (st) return st;
+        const pgd::DSpecies dst = view(c, species, B.cur ^ 1);
+        CK(pgd::compact_species(src, dst, B.n, c->mixed, c->scan_buf, &kept, c->stream));
+        c->launches += 3;
+        src = dst;
+    }
+    *nout = size_t(kept);
     if (!tet) return PICGPU_OK;
-    if (cap < alive || !bary || !U) return PICGPU_INVALID_ARG;
-    std::vector<double> col[6];
-    for (int k = 0; k < 6; ++k) {
-        col[k].resize(n);
-        const int a = k % 3;
-        if (c->mixed) {
-            std::vector<float> f(n);
-            CK(cudaMemcpy(f.data(), k < 3 ? B.y32[B.cur][a] : B.u32[B.cur][a], n * sizeof(float),
-                          cudaMemcpyDeviceToHost));
-            for (size_t i = 0; i < n; ++i) col[k][i] = f[i];
-        } else {
-            CK(cudaMemcpy(col[k].data(), k < 3 ? B.y64[B.cur][a] : B.u64[B.cur][a], n * sizeof(double),
-                          cudaMemcpyDeviceToHost));
-        }
+    if (cap < size_t(kept) || !bary || !U) return PICGPU_INVALID_ARG;
+    picgpu_status st = ensure_rows(c, size_t(kept));
+    if (st) return st;
+    pgd::launch_gather_rows(src, kept, c->mixed, c->rows_tet, c->rows_y, c->rows_u, c->stream);
+    if (kept) {
+        CK(c->stager.download(tet, c->rows_tet, size_t(kept) * sizeof(int32_t), c->stream));
+        CK(c->stager.download(bary, c->rows_y, 3 * size_t(kept) * sizeof(double), c->stream));
+        CK(c->stager.download(U, c->rows_u, 3 * size_t(kept) * sizeof(double), c->stream));
     }
-    size_t w = 0;
-    for (size_t i = 0; i < n; ++i) {
-        if (t[i] < 0) continue;
-        tet[w] = t[i];
-        for (int a = 0; a < 3; ++a) {
-            bary[3 * w + a] = col[a][i];
-            U[3 * w + a] = col[3 + a][i];
-        }
-        ++w;
-    }
+    CK(cudaStreamSynchronize(c->stream));
     return PICGPU_OK;
 }
 

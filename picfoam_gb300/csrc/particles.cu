@@ -3,6 +3,8 @@
 // PICParcel.C:70) from the structure-of-arrays store.
 #include "particles.h"
 
+#include <algorithm>
+
 namespace pgd {
 
 namespace {
@@ -105,6 +107,70 @@ __global__ void scatter_kernel(const int32_t* __restrict__ tet, const R* __restr
 }  // namespace
 
 long compact_blocks(long n) { return (n + kTile - 1) / kTile; }
+
+namespace {
+
+// Host row-major arrays (n x 3 FP64) <-> the structure-of-arrays store.
+__global__ void check_tets_kernel(const int32_t* __restrict__ tet, long n, long long ntet, int* bad) {
+    for (long i = blockIdx.x * long(blockDim.x) + threadIdx.x; i < n; i += long(gridDim.x) * blockDim.x)
+        if (tet[i] < 0 || tet[i] >= ntet) *bad = 1;
+}
+
+template <class Real>
+__global__ void scatter_rows_kernel(const int32_t* __restrict__ tet, const double* __restrict__ bary,
+                                    const double* __restrict__ U, long n, DSpecies dst) {
+    for (long i = blockIdx.x * long(blockDim.x) + threadIdx.x; i < n; i += long(gridDim.x) * blockDim.x) {
+        dst.tet[i] = tet[i];
+        for (int a = 0; a < 3; ++a) {
+            if (sizeof(Real) == 8) {
+                dst.y64[a][i] = bary[3 * i + a];
+                dst.u64[a][i] = U[3 * i + a];
+            } else {
+                dst.y32[a][i] = float(bary[3 * i + a]);
+                dst.u32[a][i] = float(U[3 * i + a]);
+            }
+        }
+    }
+}
+
+template <class Real>
+__global__ void gather_rows_kernel(DSpecies src, long n, int32_t* __restrict__ tet, double* __restrict__ bary,
+                                   double* __restrict__ U) {
+    for (long i = blockIdx.x * long(blockDim.x) + threadIdx.x; i < n; i += long(gridDim.x) * blockDim.x) {
+        tet[i] = src.tet[i];
+        for (int a = 0; a < 3; ++a) {
+            if (sizeof(Real) == 8) {
+                bary[3 * i + a] = src.y64[a][i];
+                U[3 * i + a] = src.u64[a][i];
+            } else {
+                bary[3 * i + a] = double(src.y32[a][i]);
+                U[3 * i + a] = double(src.u32[a][i]);
+            }
+        }
+    }
+}
+
+}  // namespace
+
+void launch_check_tets(const int32_t* tet, long n, long long ntet, int* bad, cudaStream_t s) {
+    if (n > 0) check_tets_kernel<<<int(std::min<long>((n + 255) / 256, 152 * 16)), 256, 0, s>>>(tet, n, ntet, bad);
+}
+
+void launch_scatter_rows(const int32_t* tet, const double* bary, const double* U, long n, const DSpecies& dst,
+                         bool fp32, cudaStream_t s) {
+    if (n <= 0) return;
+    const int g = int(std::min<long>((n + 255) / 256, 152 * 16));
+    if (fp32) scatter_rows_kernel<float><<<g, 256, 0, s>>>(tet, bary, U, n, dst);
+    else scatter_rows_kernel<double><<<g, 256, 0, s>>>(tet, bary, U, n, dst);
+}
+
+void launch_gather_rows(const DSpecies& src, long n, bool fp32, int32_t* tet, double* bary, double* U,
+                        cudaStream_t s) {
+    if (n <= 0) return;
+    const int g = int(std::min<long>((n + 255) / 256, 152 * 16));
+    if (fp32) gather_rows_kernel<float><<<g, 256, 0, s>>>(src, n, tet, bary, U);
+    else gather_rows_kernel<double><<<g, 256, 0, s>>>(src, n, tet, bary, U);
+}
 
 cudaError_t compact_species(const DSpecies& src, const DSpecies& dst, long n, bool mixed, int* scan,
                             long* kept, cudaStream_t s) {
