@@ -1486,6 +1486,7 @@ static picgpu_status create_with_mesh(picgpu_ctx* c, const picgpu_config* cfg) {
         c->mg = std::make_unique<pgd::MultigridPCG>();
         if (!c->mg->init(c->m, Md, Mo, ms, &msg)) return bad(c, PICGPU_NOT_SUPPORTED, msg);
     }
+    c->stager.init();  // pinned ring for caller arrays (on failure, plain copies)
     CK(cudaStreamSynchronize(c->stream));
     c->err.clear();
     return PICGPU_OK;
