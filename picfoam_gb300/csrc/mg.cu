@@ -279,6 +279,55 @@ __global__ void __launch_bounds__(256) mg_prolong_kernel(Lv F, int CX, int CY, i
     x[v] = fmaf(scale, xc[I], x[v]);
 }
 
+// The prolongation fused into the first post sweep: x' = x + scale xc[parent]
+// on the active voxels (zero on holes), formed at the seven stencil points
+// from their own (i, j, k), then y = x' + omega D^-1 (b - A x').
+template <bool Uniform>
+__global__ void __launch_bounds__(256) mg_prolong_smooth_kernel(Lv L, int CX, int CY, int sx, int sy, int sz,
+                                                                const float* __restrict__ xc,
+                                                                const float* __restrict__ b,
+                                                                const float* __restrict__ x, float* __restrict__ y,
+                                                                float scale, float omega) {
+    int i, j, k, v;
+    if (!coords(L, i, j, k, v)) return;
+    const int X = L.X, XY = L.X * L.Y;
+    auto xp = [&](int w, int wi, int wj, int wk) {
+        if (L.inv[w] == 0.f) return 0.f;
+        return fmaf(scale, xc[(wi >> sx) + CX * ((wj >> sy) + CY * (wk >> sz))], x[w]);
+    };
+    // neighbours: index and coordinates, with the periodic wrap; across a
+    // non-periodic edge the point is v itself with a zero coefficient
+    int ni[6], nj[6], nk[6], nb[6];
+    bool ok[6];
+    ok[0] = i > 0 || L.cx;
+    ni[0] = i > 0 ? i - 1 : (L.cx ? L.X - 1 : i);
+    ok[1] = i < L.X - 1 || L.cx;
+    ni[1] = i < L.X - 1 ? i + 1 : (L.cx ? 0 : i);
+    nj[0] = nj[1] = j;
+    nk[0] = nk[1] = k;
+    ok[2] = j > 0 || L.cy;
+    nj[2] = j > 0 ? j - 1 : (L.cy ? L.Y - 1 : j);
+    ok[3] = j < L.Y - 1 || L.cy;
+    nj[3] = j < L.Y - 1 ? j + 1 : (L.cy ? 0 : j);
+    ni[2] = ni[3] = i;
+    nk[2] = nk[3] = k;
+    ok[4] = k > 0 || L.cz;
+    nk[4] = k > 0 ? k - 1 : (L.cz ? L.Z - 1 : k);
+    ok[5] = k < L.Z - 1 || L.cz;
+    nk[5] = k < L.Z - 1 ? k + 1 : (L.cz ? 0 : k);
+    ni[4] = ni[5] = i;
+    nj[4] = nj[5] = j;
+    for (int f = 0; f < 6; ++f) nb[f] = ni[f] + X * nj[f] + XY * nk[f];
+    const float xv = xp(v, i, j, k);
+    float s = L.diag[v] * xv;
+#pragma unroll
+    for (int f = 0; f < 6; ++f) {
+        const float a = Uniform ? (ok[f] ? L.coef[f] : 0.f) : L.off[f * L.V + v];
+        s = fmaf(a, xp(nb[f], ni[f], nj[f], nk[f]), s);
+    }
+    y[v] = fmaf(omega * L.inv[v], b[v] - s, xv);
+}
+
 // Coarsest level: x[idx[r]] = sum_k inv[r][k] b[idx[k]], one warp per row,
 // lane l adds k = l, l + 32, ... then an xor-tree.
 __global__ void __launch_bounds__(256) mg_coarse_kernel(const float* __restrict__ inv, const int* __restrict__ idx,
@@ -858,10 +907,23 @@ int MultigridPCG::vcycle(int l, cudaStream_t s) {
         mg_restrict_kernel<false><<<cs.grid, cs.block, 0, s>>>(v, cv, sx, sy, sz, L.b, cur, C.b);
     ++launched;
     launched += vcycle(l + 1, s);
-    mg_prolong_kernel<<<sh.grid, sh.block, 0, s>>>(v, C.n[0], C.n[1], sx, sy, sz, result(l + 1), cur,
-                                                  float(set_.scale));
+    const bool fuse = set_.post >= 1 && !(l == 0 && set_.post == 1);
+    if (fuse) {
+        // the prolongation inside the first post sweep
+        if (L.uniform)
+            mg_prolong_smooth_kernel<true><<<sh.grid, sh.block, 0, s>>>(v, C.n[0], C.n[1], sx, sy, sz, result(l + 1),
+                                                                        L.b, cur, oth, float(set_.scale), om);
+        else
+            mg_prolong_smooth_kernel<false><<<sh.grid, sh.block, 0, s>>>(v, C.n[0], C.n[1], sx, sy, sz,
+                                                                         result(l + 1), L.b, cur, oth,
+                                                                         float(set_.scale), om);
+        std::swap(cur, oth);
+    } else {
+        mg_prolong_kernel<<<sh.grid, sh.block, 0, s>>>(v, C.n[0], C.n[1], sx, sy, sz, result(l + 1), cur,
+                                                      float(set_.scale));
+    }
     ++launched;
-    for (int it = 0; it < set_.post; ++it) {
+    for (int it = fuse ? 1 : 0; it < set_.post; ++it) {
         const bool last0 = l == 0 && it == set_.post - 1;
         if (last0) {
             const Shape ss = shape_sum(L);
