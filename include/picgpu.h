@@ -87,13 +87,20 @@ enum {
     PICGPU_PATCH_EMPTY = 1,     /* reduced-D direction (OpenFOAM empty)               */
     PICGPU_PATCH_ABSORB = 2,    /* patch + BoundaryModel "none" (NoInflow.C:56-61)    */
     PICGPU_PATCH_WALL = 3,      /* wall + WallReflectionModel SpecularReflection      */
-    PICGPU_PATCH_FLOATING = 4   /* BoundaryModel FloatingPotential + circuitBoundary  */
+    PICGPU_PATCH_FLOATING = 4,  /* BoundaryModel FloatingPotential + circuitBoundary  */
+    PICGPU_PATCH_CIRCUIT = 5    /* electrode of a circuit BoundaryModel (circuitRLC,
+                                   IdealVoltageSource, IdealCurrentSource): charged
+                                   parcels absorbed and counted, neutral parcels
+                                   reflected (circuitRLC.C:268-288)               */
 };
 
-/* Potential boundary condition of an ABSORB or WALL patch. */
+/* Potential boundary condition of an ABSORB, WALL or CIRCUIT patch (RLC and
+ * CIRCUIT_GRADIENT only on the cathode of a circuit). */
 enum {
     PICGPU_PHI_FIXED_VALUE = 0,
-    PICGPU_PHI_ZERO_GRADIENT = 1
+    PICGPU_PHI_ZERO_GRADIENT = 1,
+    PICGPU_PHI_RLC = 2,              /* RLCBoundary (RLCBoundaryFvPatchField.C) of circuitRLC */
+    PICGPU_PHI_CIRCUIT_GRADIENT = 3  /* circuitBoundary driven by IdealCurrentSource */
 };
 
 typedef struct {
@@ -263,6 +270,37 @@ typedef struct {
     double  init_temperature;     /* its temperature [K] (0: 293.15) */
 } picgpu_binary;
 
+/* Circuit boundary models between an anode and a cathode patch (both of kind
+ * PICGPU_PATCH_CIRCUIT):
+ *   RLC            circuitRLC (SM/BoundaryModel/circuitRLC/circuitRLC.C): a
+ *                  series R-L-C circuit with source V sin(omega t + phase)
+ *                  drives the cathode through the RLCBoundary condition
+ *                  (anode fixedValue, cathode PICGPU_PHI_RLC);
+ *   IDEAL_VOLTAGE  IdealVoltageSource: both electrodes fixedValue; reports the
+ *                  running-average anode and cathode currents;
+ *   IDEAL_CURRENT  IdealCurrentSource: current I (or J * cathode area) into the
+ *                  cathode's circuitBoundary (PICGPU_PHI_CIRCUIT_GRADIENT). */
+enum {
+    PICGPU_CIRCUIT_NONE = 0,
+    PICGPU_CIRCUIT_RLC = 1,
+    PICGPU_CIRCUIT_IDEAL_VOLTAGE = 2,
+    PICGPU_CIRCUIT_IDEAL_CURRENT = 3
+};
+typedef struct {
+    int32_t model;          /* PICGPU_CIRCUIT_* */
+    int32_t anode_patch;    /* patch index (-1: none) */
+    int32_t cathode_patch;  /* patch index */
+    int32_t pad;
+    double  R, L, C;        /* circuitRLC: resistance [Ohm], inductance [H], capacitance [F] */
+    double  V, omega, phase;/* source V sin(omega t + phase) [V, rad/s, rad] (reference default phase pi/2) */
+    double  epsilon;        /* permittivity of the RLC coupling (<= 0: epsilon0) */
+    double  Q[4];           /* RLCBoundary start values Q, Q1, Q2, Q3 [C] */
+    double  sigma;          /* cathode surface charge density at the start [C/m^2] */
+    double  I;              /* IdealCurrentSource current [A] (< 0: unset) */
+    double  J;              /* IdealCurrentSource current density [A/m^2] (< 0: unset) */
+    double  ref_area;       /* IdealCurrentSource refArea (> 0: I scaled by cathode area / refArea) */
+} picgpu_circuit;
+
 typedef struct {
     int32_t pusher;               /* PICGPU_PUSHER_* */
     int32_t field_weighting;      /* PICGPU_WEIGHTING_* */
@@ -291,6 +329,7 @@ typedef struct {
     picgpu_learned learned;
     picgpu_multigrid mg;
     picgpu_binary binary;
+    picgpu_circuit circuit;
 } picgpu_config;
 
 typedef struct {
@@ -324,6 +363,10 @@ typedef struct {
     int64_t binary_collisions;                  /* accepted */
     int64_t binary_background_candidates;       /* neutral parcel - background gas tests */
     int64_t binary_background_collisions;
+    double  circuit_voltage;                    /* circuitRLC: cathode potential; IdealCurrentSource: mean cathode-cell potential */
+    double  circuit_current;                    /* circuitRLC: circuit current; IdealVoltageSource: mean anode current */
+    double  circuit_cathode_current;            /* IdealVoltageSource: mean cathode current */
+    double  circuit_charge;                     /* circuitRLC: capacitor charge Q; IdealCurrentSource: cathode surface charge */
 } picgpu_step_stats;
 
 typedef struct picgpu_ctx picgpu_ctx;

@@ -23,6 +23,7 @@
 #include "collisions.hpp"
 #include "picgpu_init.h"
 #include "../picfoam_gb300/csrc/hexmesh.hpp"
+#include "../picfoam_gb300/csrc/circuit.hpp"
 
 #include <algorithm>
 #include <chrono>
@@ -145,6 +146,12 @@ struct Oracle {
     double fixScale = 1.0;
     std::vector<double> Mdiag, Moff, dinv;   // SPD Poisson operator -laplacian
     std::vector<double> sigma, gradBC, Qconv; // per patch floating state
+    std::vector<double> rlcK;                 // per patch RLCBoundary a0 epsilon A
+    // circuit model (circuitRLC / IdealVoltageSource / IdealCurrentSource)
+    pg::RlcCoeffs rlc;
+    double circuitI = 0.0;
+    std::vector<int> cathodeFaces;
+    pg::CircuitState circuit{};
     bool rotation = false;
     double move_seconds = 0;
     long long step_index = 0;
@@ -357,14 +364,17 @@ void hit_patch(Oracle& o, Parcel& p, int species, int patch, double sf, TrackDat
         td.keep = false;
         return;
     }
-    if (P.kind == PICGPU_PATCH_FLOATING) {
+    // a circuit electrode (circuitRLC.C:268-288) deletes charged parcels and
+    // reflects neutral ones
+    const bool charged = o.cfg.species[species].charge != 0.0;
+    if (P.kind == PICGPU_PATCH_FLOATING || (P.kind == PICGPU_PATCH_CIRCUIT && charged)) {
         td.keep = false;
         td.qconv[patch] += o.cfg.species[species].weight * o.cfg.species[species].charge;
         return;
     }
     const int f = p.tet / 2;
     const double* n = &o.m.cls_fnormal[size_t(o.m.cell_class[p.cell]) * 18 + 3 * f];
-    if (P.kind == PICGPU_PATCH_WALL) {
+    if (P.kind == PICGPU_PATCH_WALL || P.kind == PICGPU_PATCH_CIRCUIT) {
         sync_velocity(o, p, species, sf - 0.5);
         td.walls++;
         td.requireResync = true;
@@ -528,6 +538,44 @@ void floating_pre_update(Oracle& o) {
     }
 }
 
+// Circuit models around the field solve (PICCloud.C:1457-1464), with the
+// source and averaging factor of the step and the cathode-face sum in the
+// device's lane order.
+double circuit_src(const Oracle& o) {
+    if (o.cfg.circuit.model != PICGPU_CIRCUIT_RLC) return 0.0;
+    return pg::circuit_source(o.cfg.circuit, double(o.step_index + 1) * o.cfg.dt);
+}
+
+void circuit_pre_update(Oracle& o) {
+    const picgpu_circuit& cc = o.cfg.circuit;
+    if (cc.model == PICGPU_CIRCUIT_NONE) return;
+    pg::circuit_pre_update(cc.model, cc.cathode_patch, o.rlc.a, o.m.patches[cc.cathode_patch].area, o.circuitI,
+                           o.cfg.dt, kEps0, circuit_src(o), o.Qconv.data(), o.gradBC.data(), o.circuit);
+}
+
+void circuit_post_update(Oracle& o) {
+    const picgpu_circuit& cc = o.cfg.circuit;
+    if (cc.model == PICGPU_CIRCUIT_NONE) return;
+    const HexMesh& m = o.m;
+    const int nf = int(o.cathodeFaces.size());
+    double sum = 0.0;
+    if (cc.model == PICGPU_CIRCUIT_RLC) {
+        sum = pg::circuit_face_sum(nf, [&](int i) {
+            const pg::BFace& B = m.bfaces[o.cathodeFaces[i]];
+            return pg::face_value(pg::kRuleRlc, 0.0, 0.0, o.rlc.k, B.delta, o.phi[B.cell]);
+        });
+    } else if (cc.model == PICGPU_CIRCUIT_IDEAL_CURRENT) {
+        sum = pg::circuit_face_sum(nf, [&](int i) {
+            const pg::BFace& B = m.bfaces[o.cathodeFaces[i]];
+            return B.area * o.phi[B.cell];
+        });
+    }
+    const double t = double(o.step_index + 1) * o.cfg.dt;
+    pg::circuit_post_update(cc.model, cc.anode_patch, cc.cathode_patch, nf, o.rlc.a,
+                            m.patches[cc.cathode_patch].area, o.cfg.dt, circuit_src(o), o.cfg.dt / t, sum,
+                            o.Qconv.data(), o.circuit);
+}
+
 // Right-hand side of -laplacian(phi) = rho/eps0 in integral form (the
 // fvm::laplacian(phiE) + rhoCharge/epsilon0 system of ElectroStaticSolver.C:61-64):
 // Dirichlet faces add a |S|/delta phi_b, circuitBoundary faces add |S| g
@@ -542,11 +590,9 @@ void assemble_rhs(const Oracle& o, const double* rho, std::vector<double>& b) {
             if (bf < 0) continue;
             const pg::BFace& B = m.bfaces[bf];
             const picgpu_patch& P = m.patches[B.patch].p;
-            if (P.kind == PICGPU_PATCH_FLOATING) {
-                t = t + B.area * o.gradBC[B.patch];
-            } else if (P.phi_bc == PICGPU_PHI_FIXED_VALUE) {
-                t = t + (B.area / B.delta) * P.phi;
-            }
+            const int rule = pg::face_rule(P.kind, P.phi_bc);
+            if (rule != pg::kRuleNone)
+                t = t + pg::face_rhs(rule, P.phi, o.gradBC[B.patch], o.rlcK[B.patch], B.area, B.delta);
         }
         b[c] = t;
     }
@@ -722,9 +768,8 @@ void compute_E(Oracle& o) {
                 if (bf < 0) continue;  // empty
                 const pg::BFace& B = m.bfaces[bf];
                 const picgpu_patch& P = m.patches[B.patch].p;
-                if (P.kind == PICGPU_PATCH_FLOATING) pf = o.phi[c] + o.gradBC[B.patch] * B.delta;
-                else if (P.phi_bc == PICGPU_PHI_FIXED_VALUE) pf = P.phi;
-                else pf = o.phi[c];
+                pf = pg::face_value(pg::face_rule(P.kind, P.phi_bc), P.phi, o.gradBC[B.patch], o.rlcK[B.patch],
+                                    B.delta, o.phi[c]);
             }
             const double area = m.cls_farea[size_t(cl) * 6 + f];
             const double* n = &m.cls_fnormal[size_t(cl) * 18 + 3 * f];
@@ -736,9 +781,8 @@ void compute_E(Oracle& o) {
         const pg::BFace& B = m.bfaces[b];
         const picgpu_patch& P = m.patches[B.patch].p;
         const double* Ec = &o.E[3 * size_t(B.cell)];
-        double sn = 0.0;
-        if (P.kind == PICGPU_PATCH_FLOATING) sn = o.gradBC[B.patch];
-        else if (P.phi_bc == PICGPU_PHI_FIXED_VALUE) sn = (P.phi - o.phi[B.cell]) / B.delta;
+        const double sn = pg::face_sn_grad(pg::face_rule(P.kind, P.phi_bc), P.phi, o.gradBC[B.patch],
+                                           o.rlcK[B.patch], B.delta, o.phi[B.cell]);
         const double En = Ec[0] * B.normal[0] + Ec[1] * B.normal[1] + Ec[2] * B.normal[2];
         for (int a = 0; a < 3; ++a)
             o.Eb[3 * b + a] = (Ec[a] - En * B.normal[a]) - sn * B.normal[a];
@@ -1677,6 +1721,12 @@ void fill_counts(const Oracle& o, picgpu_step_stats* st) {
     for (size_t s = 0; s < o.cloud.size(); ++s) st->n_particles[s] = (long long)o.cloud[s].size();
     for (size_t pa = 0; pa < o.m.patches.size() && pa < PICGPU_MAX_BOXES + 6; ++pa)
         st->floating_charge[pa] = o.sigma[pa] * o.m.patches[pa].area;
+    if (o.cfg.circuit.model != PICGPU_CIRCUIT_NONE) {
+        st->circuit_voltage = o.circuit.voltage;
+        st->circuit_current = o.circuit.current;
+        st->circuit_cathode_current = o.circuit.cathode_current;
+        st->circuit_charge = o.circuit.charge;
+    }
 }
 
 }  // namespace
@@ -2106,7 +2156,8 @@ void inject(Oracle& o) {
             const long long n = (long long)np;
             I.remainder[j] = np - double(n);
             if (n <= 0) continue;
-            if (m.patches[I.cfg.patch].p.kind == PICGPU_PATCH_FLOATING)
+            const int pk = m.patches[I.cfg.patch].p.kind;
+            if (pk == PICGPU_PATCH_FLOATING || pk == PICGPU_PATCH_CIRCUIT)
                 o.Qconv[I.cfg.patch] = o.Qconv[I.cfg.patch] - double(n) * S.charge * S.weight;
             const double temperature = I.cfg.eV[j] * 1.602176634e-19 / kBoltzmann;
             for (long long k = 0; k < n; ++k) {
@@ -2233,13 +2284,27 @@ int oracle_create(const picgpu_mesh_desc* mesh, const picgpu_config* cfg, int nt
     o.sigma.assign(m.patches.size(), 0.0);
     o.gradBC.assign(m.patches.size(), 0.0);
     o.Qconv.assign(m.patches.size(), 0.0);
+    {
+        const std::string ce = pg::check_circuit(m, cfg->circuit, cfg->dt);
+        if (!ce.empty()) { o.err = ce; *out = c; return PICGPU_INVALID_ARG; }
+    }
+    o.rlcK.assign(m.patches.size(), 0.0);
+    if (cfg->circuit.model != PICGPU_CIRCUIT_NONE) {
+        const picgpu_circuit& cc = cfg->circuit;
+        const double area = m.patches[cc.cathode_patch].area;
+        o.rlc = pg::rlc_coefficients(cc, cfg->dt, area);
+        if (cc.model == PICGPU_CIRCUIT_RLC) o.rlcK[cc.cathode_patch] = o.rlc.k;
+        o.circuitI = pg::circuit_current_source(cc, area);
+        o.cathodeFaces = pg::circuit_cathode_faces(m, cc);
+        o.circuit = pg::circuit_start(cc);
+        if (cc.model == PICGPU_CIRCUIT_IDEAL_CURRENT) o.gradBC[cc.cathode_patch] = o.circuit.sigma / kEps0;
+    }
     o.Mdiag.resize(m.n_cells);
     o.dinv.resize(m.n_cells);
     o.Moff.resize(6 * size_t(m.n_cells));
-    for (int i = 0; i < m.n_cells; ++i) {
-        o.Mdiag[i] = -m.lap_diag[i];
-        o.dinv[i] = 1.0 / o.Mdiag[i];
-    }
+    for (int i = 0; i < m.n_cells; ++i) o.Mdiag[i] = -m.lap_diag[i];
+    pg::circuit_add_diagonal(m, cfg->circuit, cfg->dt, o.Mdiag);
+    for (int i = 0; i < m.n_cells; ++i) o.dinv[i] = 1.0 / o.Mdiag[i];
     for (size_t i = 0; i < o.Moff.size(); ++i) o.Moff[i] = -m.lap_off[i];
     double qmax = 0;
     for (int s = 0; s < cfg->n_species; ++s)
@@ -2393,8 +2458,10 @@ int oracle_step(oracle_ctx* ctx, int nsteps, picgpu_step_stats* st) {
         collisions(o, st);
         calculate_fields(o);
         floating_pre_update(o);
+        circuit_pre_update(o);
         s = solve_fields(o, st);
         if (s) status = s;
+        circuit_post_update(o);
         o.step_index++;
     }
     fill_counts(o, st);

@@ -29,8 +29,9 @@ WEIGHTING_CELL_AVERAGE, WEIGHTING_VOLUME = range(2)
 MAXWELL_NONE, MAXWELL_ELECTROSTATIC = range(2)
 PREC_FP64, PREC_MIXED = range(2)
 DEPOSIT_ATOMIC_FP64, DEPOSIT_FIXED_POINT = range(2)
-PATCH_CYCLIC, PATCH_EMPTY, PATCH_ABSORB, PATCH_WALL, PATCH_FLOATING = range(5)
-PHI_FIXED_VALUE, PHI_ZERO_GRADIENT = range(2)
+PATCH_CYCLIC, PATCH_EMPTY, PATCH_ABSORB, PATCH_WALL, PATCH_FLOATING, PATCH_CIRCUIT = range(6)
+PHI_FIXED_VALUE, PHI_ZERO_GRADIENT, PHI_RLC, PHI_CIRCUIT_GRADIENT = range(4)
+CIRCUIT_NONE, CIRCUIT_RLC, CIRCUIT_IDEAL_VOLTAGE, CIRCUIT_IDEAL_CURRENT = range(4)
 PRECOND_JACOBI, PRECOND_MULTIGRID = range(2)
 FIELD_PHI, FIELD_E_CELL, FIELD_RHO, FIELD_E_POINT, FIELD_SIGMA_V_MAX = range(5)
 (PHASE_MOVE, PHASE_CHARGE, PHASE_POISSON, PHASE_EFIELD, PHASE_SORT, PHASE_MCC,
@@ -124,6 +125,16 @@ class Binary(C.Structure):
     ]
 
 
+class Circuit(C.Structure):
+    _fields_ = [
+        ("model", C.c_int32), ("anode_patch", C.c_int32), ("cathode_patch", C.c_int32), ("pad", C.c_int32),
+        ("R", C.c_double), ("L", C.c_double), ("C", C.c_double),
+        ("V", C.c_double), ("omega", C.c_double), ("phase", C.c_double), ("epsilon", C.c_double),
+        ("Q", C.c_double * 4), ("sigma", C.c_double),
+        ("I", C.c_double), ("J", C.c_double), ("ref_area", C.c_double),
+    ]
+
+
 class Multigrid(C.Structure):
     _fields_ = [
         ("pre_sweeps", C.c_int32), ("post_sweeps", C.c_int32), ("coarsest_cells", C.c_int32),
@@ -145,7 +156,7 @@ class Config(C.Structure):
         ("sort_interval", C.c_int32), ("pcg_precond", C.c_int32),
         ("seed", C.c_uint64),
         ("mcc", Mcc), ("ion_mcc", IonMcc), ("coulomb", Coulomb), ("learned", Learned),
-        ("mg", Multigrid), ("binary", Binary),
+        ("mg", Multigrid), ("binary", Binary), ("circuit", Circuit),
     ]
 
 
@@ -214,6 +225,8 @@ class StepStats(C.Structure):
         ("learned_fallback", C.c_int32), ("pcg_refinements", C.c_int32),
         ("binary_candidates", C.c_int64), ("binary_collisions", C.c_int64),
         ("binary_background_candidates", C.c_int64), ("binary_background_collisions", C.c_int64),
+        ("circuit_voltage", C.c_double), ("circuit_current", C.c_double),
+        ("circuit_cathode_current", C.c_double), ("circuit_charge", C.c_double),
     ]
 
     def as_dict(self):

@@ -544,6 +544,42 @@ def empty_case(n_cells=(8, 8, 8), length=(0.01, 0.01, 0.01), sides=None, boxes=(
     return Case("empty", mesh, cfg, {}, [], {})
 
 
+def circuit_case(model=abi.CIRCUIT_RLC, n=200, length=0.05, width=0.024, R=1.0, C=1e-6, L=0.04, V=100.0,
+                 omega=0.0, phase=math.pi / 2, I=-1.0, J=-1.0, ref_area=0.0, sigma=0.0, q0=(0.0,) * 4,
+                 per_cell=0, T_e=2.0, T_i=0.03, weight=1e6, dt=1e-11, seed=1234, precision=abi.PREC_FP64,
+                 cathode_phi=0.0, anode_phi=0.0):
+    """A 1-D gap like the rlcCircuit tutorial: n cells along x over `length`
+    (cross-section width x width, empty y/z sides), the cathode ("source") at
+    -x and the anode ("collector", fixedValue) at +x, both circuit
+    electrodes of `model`: circuitRLC (R, C, L, V sin(omega t + phase)),
+    IdealVoltageSource (both fixedValue) or IdealCurrentSource (I / J into
+    the cathode's circuitBoundary).  per_cell > 0 fills the gap with e- and
+    Ar+ parcels of `weight` at T_e / T_i eV."""
+    cathode_bc = {abi.CIRCUIT_RLC: abi.PHI_RLC, abi.CIRCUIT_IDEAL_VOLTAGE: abi.PHI_FIXED_VALUE,
+                  abi.CIRCUIT_IDEAL_CURRENT: abi.PHI_CIRCUIT_GRADIENT}[model]
+    sides = [patch(abi.PATCH_CIRCUIT, cathode_phi, cathode_bc), patch(abi.PATCH_CIRCUIT, anode_phi),
+             patch(abi.PATCH_EMPTY), patch(abi.PATCH_EMPTY), patch(abi.PATCH_EMPTY), patch(abi.PATCH_EMPTY)]
+    mesh = block_mesh((n, 1, 1), (length, width, width), sides)
+    cfg = base_config(dt, [(M_E, -E_CHARGE, weight, True), (M_AR, E_CHARGE, weight, True)],
+                      precision=precision, deposit=abi.DEPOSIT_FIXED_POINT, seed=seed)
+    c = cfg.circuit
+    c.model = model
+    c.cathode_patch, c.anode_patch = 0, 1
+    c.R, c.L, c.C, c.V, c.omega, c.phase = R, L, C, V, omega, phase
+    for i in range(4):
+        c.Q[i] = q0[i]
+    c.sigma = sigma
+    c.I, c.J, c.ref_area = I, J, ref_area
+    particles = {}
+    if per_cell > 0:
+        rng = np.random.Generator(np.random.Philox(seed))
+        for s, (m, T) in enumerate(((M_E, T_e), (M_AR, T_i))):
+            tet, bary = uniform_in_cells(rng, np.arange(n), per_cell)
+            U = rng.standard_normal((len(tet), 3)) * math.sqrt(T * E_CHARGE / m)
+            particles[s] = (tet, bary, U)
+    return Case("circuit", mesh, cfg, particles, [], dict(area=width * width))
+
+
 def neutral_gas(n_cells=4, per_cell=50, n=1e21, T=300.0, T_x=None, d=4.17e-10, L=4e-4, dt=1e-7, seed=1234,
                 precision=abi.PREC_FP64, cross_section=abi.XS_HARD_SPHERE, omega=0.5, tref=273.0,
                 weight_correction=0, background=None):

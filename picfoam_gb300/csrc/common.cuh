@@ -31,6 +31,7 @@ struct PatchConst {
     int phi_bc[kMaxPatches];
     double phi[kMaxPatches];
     double area[kMaxPatches];
+    double rlc_k[kMaxPatches];   // RLCBoundary cathode: a0 * epsilon * area (0 elsewhere)
 };
 
 // Shared-memory tables of the FP32 move kernel: the geometry of a uniform

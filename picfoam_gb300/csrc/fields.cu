@@ -15,6 +15,7 @@
 //   grad_E          E = -fvc::grad(phiE), Gauss linear (ElectroStaticSolver.C:68)
 //   boundary_E      corrected boundary values of E
 //   point_E         cell -> point interpolation (VolumeWeightingFW.C:70-75)
+#include "circuit.hpp"
 #include "fields.h"
 #include "reduce.cuh"
 
@@ -119,6 +120,48 @@ __global__ void floating_update_kernel(double* qconv, double* sigma, double* gra
     qconv[p] = 0.0;
 }
 
+// Circuit models: preUpdate_Boundary before the solve, postUpdate_Boundary
+// after it (PICCloud.C:1457-1464).  One thread / one block of
+// pg::kCircuitLanes lanes; the lane order of the cathode-face sum is the one
+// pg::circuit_face_sum restates.
+__global__ void circuit_pre_kernel(CircuitParams P, double src, double* qconv, double* grad_bc,
+                                   pg::CircuitState* S) {
+    if (threadIdx.x != 0 || blockIdx.x != 0) return;
+    pg::CircuitState st = *S;
+    pg::circuit_pre_update(P.model, P.cathode, P.a, P.area, P.I, P.dt, eps0(), src, qconv, grad_bc, st);
+    *S = st;
+}
+
+__global__ void __launch_bounds__(pg::kCircuitLanes)
+circuit_post_kernel(CircuitParams P, DMesh m, double src, double beta, const double* __restrict__ phi,
+                    double* qconv, pg::CircuitState* S) {
+    __shared__ double lane[pg::kCircuitLanes];
+    const int t = threadIdx.x;
+    double a = 0.0;
+    if (P.model == PICGPU_CIRCUIT_RLC) {
+        for (int i = t; i < P.n_faces; i += pg::kCircuitLanes) {
+            const int b = P.faces[i];
+            a = a + pg::face_value(pg::kRuleRlc, 0.0, 0.0, P.k, m.bf_delta[b], phi[m.bf_cell[b]]);
+        }
+    } else if (P.model == PICGPU_CIRCUIT_IDEAL_CURRENT) {
+        for (int i = t; i < P.n_faces; i += pg::kCircuitLanes) {
+            const int b = P.faces[i];
+            a = a + m.bf_area[b] * phi[m.bf_cell[b]];
+        }
+    }
+    lane[t] = a;
+    __syncthreads();
+    for (int s = pg::kCircuitLanes / 2; s > 0; s >>= 1) {
+        if (t < s) lane[t] = lane[t] + lane[t + s];
+        __syncthreads();
+    }
+    if (t != 0) return;
+    pg::CircuitState st = *S;
+    pg::circuit_post_update(P.model, P.anode, P.cathode, P.n_faces, P.a, P.area, P.dt, src, beta, lane[0], qconv,
+                            st);
+    *S = st;
+}
+
 // ----------------------------------------------------------- Poisson -----
 __global__ void rhs_kernel(DMesh m, const double* __restrict__ rho, const double* __restrict__ grad_bc,
                            double* __restrict__ b) {
@@ -129,9 +172,10 @@ __global__ void rhs_kernel(DMesh m, const double* __restrict__ rho, const double
         const int bf = m.cell_bface[6 * size_t(c) + f];
         if (bf < 0) continue;
         const int pa = m.bf_patch[bf];
-        if (c_patchF.kind[pa] == PICGPU_PATCH_FLOATING) t = t + m.bf_area[bf] * grad_bc[pa];
-        else if (c_patchF.phi_bc[pa] == PICGPU_PHI_FIXED_VALUE)
-            t = t + (m.bf_area[bf] / m.bf_delta[bf]) * c_patchF.phi[pa];
+        const int rule = pg::face_rule(c_patchF.kind[pa], c_patchF.phi_bc[pa]);
+        if (rule != pg::kRuleNone)
+            t = t + pg::face_rhs(rule, c_patchF.phi[pa], grad_bc[pa], c_patchF.rlc_k[pa], m.bf_area[bf],
+                                 m.bf_delta[bf]);
     }
     b[c] = t;
 }
@@ -382,9 +426,8 @@ __global__ void grad_E_kernel(DMesh m, const double* __restrict__ phi,
             const int bf = m.cell_bface[6 * size_t(c) + f];
             if (bf < 0) continue;
             const int pa = m.bf_patch[bf];
-            if (c_patchF.kind[pa] == PICGPU_PATCH_FLOATING) pf = phi[c] + grad_bc[pa] * m.bf_delta[bf];
-            else if (c_patchF.phi_bc[pa] == PICGPU_PHI_FIXED_VALUE) pf = c_patchF.phi[pa];
-            else pf = phi[c];
+            pf = pg::face_value(pg::face_rule(c_patchF.kind[pa], c_patchF.phi_bc[pa]), c_patchF.phi[pa],
+                                grad_bc[pa], c_patchF.rlc_k[pa], m.bf_delta[bf], phi[c]);
         }
         const double area = m.farea[size_t(cl) * 6 + f];
         const double* n = m.fnormal + size_t(cl) * 18 + 3 * f;
@@ -407,9 +450,8 @@ __global__ void boundary_E_kernel(DMesh m, const double* __restrict__ phi,
     const int pa = m.bf_patch[b];
     const double* Ec = E + 3 * size_t(c);
     const double* n = m.bf_normal + 3 * size_t(b);
-    double sn = 0.0;
-    if (c_patchF.kind[pa] == PICGPU_PATCH_FLOATING) sn = grad_bc[pa];
-    else if (c_patchF.phi_bc[pa] == PICGPU_PHI_FIXED_VALUE) sn = (c_patchF.phi[pa] - phi[c]) / m.bf_delta[b];
+    const double sn = pg::face_sn_grad(pg::face_rule(c_patchF.kind[pa], c_patchF.phi_bc[pa]), c_patchF.phi[pa],
+                                       grad_bc[pa], c_patchF.rlc_k[pa], m.bf_delta[b], phi[c]);
     const double En = Ec[0] * n[0] + Ec[1] * n[1] + Ec[2] * n[2];
     for (int a = 0; a < 3; ++a) Eb[3 * size_t(b) + a] = (Ec[a] - En * n[a]) - sn * n[a];
 }
@@ -504,6 +546,16 @@ void launch_charge_update(const DMesh& m, int vw, int fixed, double fix_scale, c
 
 void launch_floating_update(double* qconv, double* sigma, double* grad_bc, cudaStream_t s) {
     floating_update_kernel<<<1, 32, 0, s>>>(qconv, sigma, grad_bc);
+}
+
+void launch_circuit_pre(const CircuitParams& P, double src, double* qconv, double* grad_bc, pg::CircuitState* S,
+                        cudaStream_t s) {
+    circuit_pre_kernel<<<1, 32, 0, s>>>(P, src, qconv, grad_bc, S);
+}
+
+void launch_circuit_post(const CircuitParams& P, const DMesh& m, double src, double beta, const double* phi,
+                         double* qconv, pg::CircuitState* S, cudaStream_t s) {
+    circuit_post_kernel<<<1, pg::kCircuitLanes, 0, s>>>(P, m, src, beta, phi, qconv, S);
 }
 
 int pcg_blocks(int n) { return (n + kChunk - 1) / kChunk; }

@@ -3,6 +3,7 @@
 
 #include <algorithm>
 
+#include "circuit.hpp"
 #include "common.cuh"
 
 namespace pgd {
@@ -36,6 +37,21 @@ void launch_charge_update(const DMesh& m, int vw, int fixed, double fix_scale, c
                           const double* vtxd, const long long* ccf, const long long* vtxf,
                           double space_charge, double* rho, cudaStream_t s);
 void launch_floating_update(double* qconv, double* sigma, double* grad_bc, cudaStream_t s);
+
+// Circuit model of a context (constant over a run).
+struct CircuitParams {
+    int model, anode, cathode, n_faces;
+    const int* faces;     // the cathode's boundary faces, in face order
+    double a[5];          // circuitRLC backward-difference coefficients
+    double k;             // a0 * epsilon * cathode area
+    double area;          // cathode area
+    double I;             // IdealCurrentSource current
+    double dt;
+};
+void launch_circuit_pre(const CircuitParams& P, double src, double* qconv, double* grad_bc, pg::CircuitState* S,
+                        cudaStream_t s);
+void launch_circuit_post(const CircuitParams& P, const DMesh& m, double src, double beta, const double* phi,
+                         double* qconv, pg::CircuitState* S, cudaStream_t s);
 void launch_rhs(const DMesh& m, const double* rho, const double* grad_bc, double* b, int singular,
                 double* part, PcgState* st, cudaStream_t s);
 // PCG (Chronopoulos-Gear form, Jacobi preconditioner).  part holds 4 x

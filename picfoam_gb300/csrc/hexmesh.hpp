@@ -228,7 +228,7 @@ inline std::string validate_desc(const picgpu_mesh_desc& d) {
             return "mesh: an empty direction must be one cell thick";
         for (int s = 0; s < 2; ++s) {
             const int k = d.side[2 * a + s].kind;
-            if (k < PICGPU_PATCH_CYCLIC || k > PICGPU_PATCH_FLOATING)
+            if (k < PICGPU_PATCH_CYCLIC || k > PICGPU_PATCH_CIRCUIT)
                 return "mesh: unknown patch kind";
         }
     }
@@ -459,9 +459,9 @@ inline HexMesh build_hex_mesh(const picgpu_mesh_desc& d) {
                     b.centre[a] = m.cc[3 * size_t(c) + a] + fcr[a];
                 }
                 m.cell_bface[6 * size_t(c) + f] = int(m.bfaces.size());
-                const bool dirichlet =
-                    (P.p.kind == PICGPU_PATCH_ABSORB || P.p.kind == PICGPU_PATCH_WALL) &&
-                    P.p.phi_bc == PICGPU_PHI_FIXED_VALUE;
+                const bool dirichlet = (P.p.kind == PICGPU_PATCH_ABSORB || P.p.kind == PICGPU_PATCH_WALL ||
+                                        P.p.kind == PICGPU_PATCH_CIRCUIT) &&
+                                       P.p.phi_bc == PICGPU_PHI_FIXED_VALUE;
                 if (dirichlet) {
                     m.lap_diag[c] -= area / dP;
                     m.has_dirichlet = 1;

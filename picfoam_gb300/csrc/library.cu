@@ -183,6 +183,8 @@ struct picgpu_ctx {
     unsigned long long* acc9 = nullptr;   // FP32 form: per-species fixed-point deposit, 9 slots per cell
     float4* Ec4 = nullptr;                // FP32 form: E per cell, centre + 8 corners
     double *qconv = nullptr, *sigma = nullptr, *grad_bc = nullptr;
+    pgd::CircuitParams circ{};            // circuit model (model NONE: no circuit)
+    pg::CircuitState* circ_state = nullptr;
     double *b = nullptr, *r = nullptr, *z = nullptr, *p[2] = {nullptr, nullptr}, *q = nullptr,
            *part = nullptr;
     pgd::PcgState* st = nullptr;
@@ -755,7 +757,8 @@ picgpu_status inject(picgpu_ctx* c) {
             P.tri_fc = I.tri_fc;
             P.area = I.area;
             P.patch = I.cfg.patch;
-            if (c->m.patches[I.cfg.patch].p.kind == PICGPU_PATCH_FLOATING) {
+            const int pk = c->m.patches[I.cfg.patch].p.kind;
+            if (pk == PICGPU_PATCH_FLOATING || pk == PICGPU_PATCH_CIRCUIT) {
                 P.qconv = c->qconv;
                 P.ejected_charge = double(n) * S.charge * S.weight;
             }
@@ -829,7 +832,20 @@ picgpu_status one_step(picgpu_ctx* c, picgpu_step_stats* stats, bool fields) {
     if (!fields) return PICGPU_OK;
     pgd::launch_floating_update(c->qconv, c->sigma, c->grad_bc, c->stream);
     c->launches++;
+    // circuit models around the field solve (PICCloud.C:1457-1464); the
+    // source and the averaging factor are evaluated here, on the host
+    const double t_now = double(c->step_index + 1) * c->cfg.dt;
+    const double src = c->circ.model == PICGPU_CIRCUIT_RLC ? pg::circuit_source(c->cfg.circuit, t_now) : 0.0;
+    if (c->circ.model != PICGPU_CIRCUIT_NONE) {
+        pgd::launch_circuit_pre(c->circ, src, c->qconv, c->grad_bc, c->circ_state, c->stream);
+        c->launches++;
+    }
     if ((s = solve_fields(c, stats, true))) return s;
+    if (c->circ.model != PICGPU_CIRCUIT_NONE) {
+        pgd::launch_circuit_post(c->circ, c->dm, src, c->cfg.dt / t_now, c->phi, c->qconv, c->circ_state,
+                                 c->stream);
+        c->launches++;
+    }
     c->step_index++;
     return PICGPU_OK;
 }
@@ -1274,6 +1290,12 @@ static picgpu_status create_with_mesh(picgpu_ctx* c, const picgpu_config* cfg) {
         return bad(c, PICGPU_INVALID_ARG, "config: unknown precision");
     if (cfg->pcg_precond != PICGPU_PRECOND_JACOBI && cfg->pcg_precond != PICGPU_PRECOND_MULTIGRID)
         return bad(c, PICGPU_INVALID_ARG, "config: unknown PCG preconditioner");
+    {
+        const std::string ce = pg::check_circuit(c->m, cfg->circuit, cfg->dt);
+        if (!ce.empty()) return bad(c, PICGPU_INVALID_ARG, ce);
+        if (cfg->circuit.model != PICGPU_CIRCUIT_NONE && c->n_cases > 1)
+            return bad(c, PICGPU_NOT_SUPPORTED, "circuit: not for ensemble contexts");
+    }
     c->cfg = *cfg;
     c->mixed = cfg->precision == PICGPU_PREC_MIXED;
     c->rotation = cfg->B[0] != 0.0 || cfg->B[1] != 0.0 || cfg->B[2] != 0.0;
@@ -1304,6 +1326,22 @@ static picgpu_status create_with_mesh(picgpu_ctx* c, const picgpu_config* cfg) {
         c->pc.phi_bc[p] = m.patches[p].p.phi_bc;
         c->pc.phi[p] = m.patches[p].p.phi;
         c->pc.area[p] = m.patches[p].area;
+        c->pc.rlc_k[p] = 0.0;
+    }
+    if (cfg->circuit.model != PICGPU_CIRCUIT_NONE) {
+        const picgpu_circuit& cc = cfg->circuit;
+        const double area = m.patches[cc.cathode_patch].area;
+        const pg::RlcCoeffs rc = pg::rlc_coefficients(cc, cfg->dt, area);
+        pgd::CircuitParams& P = c->circ;
+        P.model = cc.model;
+        P.anode = cc.anode_patch;
+        P.cathode = cc.cathode_patch;
+        for (int i = 0; i < 5; ++i) P.a[i] = rc.a[i];
+        P.k = rc.k;
+        P.area = area;
+        P.I = pg::circuit_current_source(cc, area);
+        P.dt = cfg->dt;
+        if (cc.model == PICGPU_CIRCUIT_RLC) c->pc.rlc_k[cc.cathode_patch] = rc.k;
     }
     CK(pgd::move_fp64_set_tables(c->tc, c->pc));
     CK(pgd::init_set_tables(c->tc));
@@ -1362,10 +1400,9 @@ static picgpu_status create_with_mesh(picgpu_ctx* c, const picgpu_config* cfg) {
         bf_delta.push_back(bf.delta);
     }
     std::vector<double> Mdiag(m.n_cells), Moff(m.lap_off.size()), dinv(m.n_cells);
-    for (int i = 0; i < m.n_cells; ++i) {
-        Mdiag[i] = -m.lap_diag[i];
-        dinv[i] = 1.0 / Mdiag[i];
-    }
+    for (int i = 0; i < m.n_cells; ++i) Mdiag[i] = -m.lap_diag[i];
+    pg::circuit_add_diagonal(m, cfg->circuit, cfg->dt, Mdiag);
+    for (int i = 0; i < m.n_cells; ++i) dinv[i] = 1.0 / Mdiag[i];
     for (size_t i = 0; i < Moff.size(); ++i) Moff[i] = -m.lap_off[i];
     int* ip;
     double* dp;
@@ -1450,6 +1487,20 @@ static picgpu_status create_with_mesh(picgpu_ctx* c, const picgpu_config* cfg) {
     CK(cudaMemset(c->qconv, 0, npa * sizeof(double)));
     CK(cudaMemset(c->sigma, 0, npa * sizeof(double)));
     CK(cudaMemset(c->grad_bc, 0, npa * sizeof(double)));
+    if (cfg->circuit.model != PICGPU_CIRCUIT_NONE) {
+        const pg::CircuitState st0 = pg::circuit_start(cfg->circuit);
+        std::vector<int> faces = pg::circuit_cathode_faces(m, cfg->circuit);
+        int* fd = nullptr;
+        if ((s = upload(c, &fd, faces)) || (s = dalloc(c, &c->circ_state, 1))) return s;
+        c->circ.faces = fd;
+        c->circ.n_faces = int(faces.size());
+        CK(cudaMemcpy(c->circ_state, &st0, sizeof st0, cudaMemcpyHostToDevice));
+        if (cfg->circuit.model == PICGPU_CIRCUIT_IDEAL_CURRENT) {
+            // circuitBoundary's stored gradient: sigma / epsilon0
+            const double g0 = st0.sigma / (1.0 / (kMu0 * kCl * kCl));
+            CK(cudaMemcpy(c->grad_bc + cfg->circuit.cathode_patch, &g0, sizeof g0, cudaMemcpyHostToDevice));
+        }
+    }
     CK(cudaMemset(c->st, 0, sizeof(pgd::PcgState)));
     CK(cudaMallocHost(&c->st_host, sizeof(pgd::PcgState)));
     CK(cudaMallocHost(&c->counters_host, sizeof(pgd::MoveCounters) * PICGPU_MAX_SPECIES));
@@ -1482,6 +1533,7 @@ static picgpu_status create_with_mesh(picgpu_ctx* c, const picgpu_config* cfg) {
             return bad(c, PICGPU_INVALID_ARG, "config: multigrid settings out of range");
         std::vector<double> Md(c->m.n_cells), Mo(c->m.lap_off.size());
         for (int i = 0; i < c->m.n_cells; ++i) Md[i] = -c->m.lap_diag[i];
+        pg::circuit_add_diagonal(c->m, cfg->circuit, cfg->dt, Md);
         for (size_t i = 0; i < Mo.size(); ++i) Mo[i] = -c->m.lap_off[i];
         c->mg = std::make_unique<pgd::MultigridPCG>();
         if (!c->mg->init(c->m, Md, Mo, ms, &msg)) return bad(c, PICGPU_NOT_SUPPORTED, msg);
@@ -1998,6 +2050,14 @@ picgpu_status picgpu_step(picgpu_ctx* c, int nsteps, picgpu_step_stats* stats) {
         CK(cudaMemcpy(sg.data(), c->sigma, sg.size() * sizeof(double), cudaMemcpyDeviceToHost));
         for (size_t p = 0; p < sg.size() && p < PICGPU_MAX_BOXES + 6; ++p)
             stats->floating_charge[p] = sg[p] * c->m.patches[p].area;
+        if (c->circ_state) {
+            pg::CircuitState cs;
+            CK(cudaMemcpy(&cs, c->circ_state, sizeof cs, cudaMemcpyDeviceToHost));
+            stats->circuit_voltage = cs.voltage;
+            stats->circuit_current = cs.current;
+            stats->circuit_cathode_current = cs.cathode_current;
+            stats->circuit_charge = cs.charge;
+        }
     }
     return PICGPU_OK;
 }
@@ -2224,6 +2284,8 @@ picgpu_status picgpu_ensemble_case_stats(picgpu_ctx* c, int species, double* out
 picgpu_status picgpu_step_graph(picgpu_ctx* c, int nsteps, int steps_per_graph, picgpu_step_stats* stats) {
     if (c && !c->injectors.empty())
         return bad(c, PICGPU_NOT_SUPPORTED, "step_graph: injection runs only in picgpu_step");
+    if (c && c->circ.model != PICGPU_CIRCUIT_NONE)
+        return bad(c, PICGPU_NOT_SUPPORTED, "step_graph: circuit models run only in picgpu_step");
     if (!c || nsteps < 0 || steps_per_graph <= 0 || nsteps % steps_per_graph) return PICGPU_INVALID_ARG;
     if (!c->mixed || c->cfg.maxwell_solver != PICGPU_MAXWELL_NONE)
         return bad(c, PICGPU_NOT_SUPPORTED, "graph steps need the FP32 form and MaxwellSolver none");

@@ -206,7 +206,7 @@ __device__ __forceinline__ void track32(const MoveParams& P, const Tables32& T, 
         const int patch = -nb - 1;
         const int kind = T.kind[patch];
         if (kind == PICGPU_PATCH_ABSORB) { td.keep = false; return; }
-        if (kind == PICGPU_PATCH_FLOATING) {
+        if (kind == PICGPU_PATCH_FLOATING || (kind == PICGPU_PATCH_CIRCUIT && P.q != 0.0)) {
             td.keep = false;
             atomicAdd(P.qconv + patch, P.weight * P.q);
             return;
@@ -215,7 +215,7 @@ __device__ __forceinline__ void track32(const MoveParams& P, const Tables32& T, 
         const int f = s.tet >> 1;
         const float* n =
             P.m.uniform ? T.normal + 3 * f : P.m.fnormal32 + size_t(P.m.cell_class[s.cell]) * 18 + 3 * f;
-        const bool wall = kind == PICGPU_PATCH_WALL;
+        const bool wall = kind == PICGPU_PATCH_WALL || kind == PICGPU_PATCH_CIRCUIT;
         if (wall) {
             if (P.sync && P.charged) push32<PUSHER>(P, T, s, (sf - 0.5f) * dt);
             td.walls++;

@@ -287,14 +287,16 @@ __device__ __forceinline__ void hit_patch(const MoveParams& P, const TetConst& T
                                           PState<Real>& s, int patch, Real sf, TrackTally& td) {
     const int kind = PCs.kind[patch];
     if (kind == PICGPU_PATCH_ABSORB) { td.keep = false; return; }
-    if (kind == PICGPU_PATCH_FLOATING) {
+    // FloatingPotential deletes every parcel; a circuit electrode
+    // (circuitRLC.C:268-288) deletes charged parcels and reflects neutral ones
+    if (kind == PICGPU_PATCH_FLOATING || (kind == PICGPU_PATCH_CIRCUIT && P.q != 0.0)) {
         td.keep = false;
         atomicAdd(P.qconv + patch, P.weight * P.q);
         return;
     }
     const int f = s.tet / 2;
     const Real* n = fnormals<Real>(P.m) + size_t(P.m.cell_class[s.cell]) * 18 + 3 * f;
-    if (kind == PICGPU_PATCH_WALL) {
+    if (kind == PICGPU_PATCH_WALL || kind == PICGPU_PATCH_CIRCUIT) {
         sync_velocity(P, T, s, sf - Real(0.5));
         td.walls++;
         td.resync = true;
