@@ -460,6 +460,29 @@ typedef struct {
  * at zero.  Not for ensemble contexts or picgpu_step_graph. */
 picgpu_status picgpu_set_injection(picgpu_ctx* ctx, int n, const picgpu_injection* inj);
 
+/* FreeStream boundary model (SM/BoundaryModel/FreeStream/FreeStream.C:126-396):
+ * every step, before the move and after the SimpleInjection models, each
+ * boundary face of an ABSORB patch gains |S| n/w dt c_mp (e^{-s^2} +
+ * sqrt(pi) s (1 + erf s)) / (2 sqrt(pi)) parcels of each species (Bird eq.
+ * 4.22, c_mp = sqrt(2kT/m), s = U.n_in / c_mp) in a per-face accumulator.
+ * The integer part, plus one when the remainder exceeds a uniform draw, is
+ * emitted on the face: one of its two triangles by area, a uniform point on
+ * it, the normal speed by Bird's acceptance-rejection (eq. 12.5), thermal
+ * tangential components plus the drift's tangential part, then
+ * syncVelocityAtBoundary(-0.5).  Parcels reaching the patch are deleted.
+ * n = 0 removes all; accumulators restart at zero.  Not for ensemble
+ * contexts or picgpu_step_graph. */
+#define PICGPU_MAX_FREESTREAMS 8
+typedef struct {
+    int32_t patch;                               /* an ABSORB side or box patch */
+    int32_t n_species;                           /* entries of numberDensities */
+    int32_t species[PICGPU_MAX_SPECIES];
+    double  number_density[PICGPU_MAX_SPECIES];  /* numberDensities [1/m^3] (real particles) */
+    double  temperature;                         /* boundaryT on the patch [K] */
+    double  velocity[3];                         /* boundaryU on the patch [m/s] */
+} picgpu_freestream;
+picgpu_status picgpu_set_freestream(picgpu_ctx* ctx, int n, const picgpu_freestream* fs);
+
 /* Advance nsteps time steps. */
 picgpu_status picgpu_step(picgpu_ctx* ctx, int nsteps, picgpu_step_stats* stats);
 

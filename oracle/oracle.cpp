@@ -24,6 +24,7 @@
 #include "picgpu_init.h"
 #include "../picfoam_gb300/csrc/hexmesh.hpp"
 #include "../picfoam_gb300/csrc/circuit.hpp"
+#include "../picfoam_gb300/csrc/freestream.hpp"
 
 #include <algorithm>
 #include <chrono>
@@ -169,6 +170,13 @@ struct Oracle {
         PatchTriangles tri;
     };
     std::vector<Injector> injectors;
+    // FreeStream boundary models
+    struct FreeStream {
+        picgpu_freestream cfg{};
+        pg::FreeStreamFaces F;
+        std::vector<double> acc;   // n_faces * n_species
+    };
+    std::vector<FreeStream> freestreams;
     // BinaryCollisionModel state per cell
     std::vector<double> bsmax, brem, bbgrem;
 };
@@ -2138,6 +2146,77 @@ int oracle_initialise_impl(Oracle& o, const picgpu_init* in, picgpu_init_stats* 
 // velocity model about the inward normal (:420-535), constrainDirection,
 // syncVelocityAtBoundary(-0.5) (:401) -- and, on a floating patch, its
 // charge taken off the patch (particleEjection, SimpleInjection.C:295-302).
+// FreeStream::injection (SM/BoundaryModel/FreeStream/FreeStream.C:126-396):
+// per face and species the accumulator gains Bird's eq. 4.22 flux; the
+// integer part, plus one when the remainder exceeds a uniform draw, is
+// emitted on the face -- a triangle by area share, a uniform point on it, the
+// normal speed ratio by acceptance-rejection (eq. 12.5), thermal tangential
+// components plus the drift's tangential part -- then
+// syncVelocityAtBoundary(-0.5).  Faces in order, each face's parcels in turn.
+void freestream_inject(Oracle& o) {
+    using namespace oinit;
+    for (size_t i = 0; i < o.freestreams.size(); ++i) {
+        Oracle::FreeStream& Z = o.freestreams[i];
+        const pg::FreeStreamFaces& F = Z.F;
+        for (int j = 0; j < Z.cfg.n_species; ++j) {
+            const int sp = Z.cfg.species[j];
+            const picgpu_species& S = o.cfg.species[sp];
+            const uint32_t key = (uint32_t(i) << 4) | uint32_t(sp);
+            std::vector<int> counts(F.n_faces);
+            for (int f = 0; f < F.n_faces; ++f) {
+                const size_t q = size_t(f) * F.n_species + j;
+                double a = Z.acc[q] + F.add[q];
+                long long n = a < 2.0e9 ? (long long)a : (1LL << 31);
+                if (n < 0) n = 0;
+                ocoll::Philox r(o.cfg.seed, ocoll::kStreamFreeStreamCount | key, uint32_t(o.step_index), uint32_t(f));
+                if (a - double(n) > r.uniform()) ++n;
+                if (n > (1LL << 30)) n = 0;
+                Z.acc[q] = a - double(n);
+                counts[f] = int(n);
+            }
+            for (int f = 0; f < F.n_faces; ++f) {
+                if (counts[f] == 0) continue;
+                ocoll::Philox r(o.cfg.seed, ocoll::kStreamFreeStream | key, uint32_t(o.step_index), uint32_t(f));
+                const double s = F.s[size_t(f) * F.n_species + j];
+                const double root = std::sqrt(s * s + 2.0);
+                const double qa = s + root;
+                const double qb = 0.5 * (1.0 + s * (s - root));
+                const double scaling = s < -3.0 ? std::fabs(s) + 1.0 : 3.0;
+                const double* n = &F.n_in[3 * size_t(f)];
+                const double* t1 = &F.t1[3 * size_t(f)];
+                const double* t2 = &F.t2[3 * size_t(f)];
+                const double* Ud = Z.cfg.velocity;
+                const double d1 = t1[0] * Ud[0] + t1[1] * Ud[1] + t1[2] * Ud[2];
+                const double d2 = t2[0] * Ud[0] + t2[1] * Ud[1] + t2[2] * Ud[2];
+                for (int k = 0; k < counts[f]; ++k) {
+                    const double sel = r.uniform();
+                    const int t = F.tet0[f] + (F.frac0[f] >= sel ? 0 : 1);
+                    const double r1 = r.uniform(), r2 = r.uniform();
+                    const double sr = std::sqrt(r1);
+                    const double y[3] = {1.0 - sr, sr * (1.0 - r2), sr * r2};
+                    double u = 0.0;
+                    for (int it = 0; it < 10000; ++it) {  // do { ... } while (P < U01)
+                        const double ut = scaling * (2.0 * r.uniform() - 1.0);
+                        u = ut + s;
+                        const double pr = u < 0.0 ? -1.0 : 2.0 * u / qa * det_exp(qb - ut * ut);
+                        if (!(pr < r.uniform())) break;
+                    }
+                    double n1, n2;
+                    polar_pair(r, n1, n2);
+                    double U[3];
+                    for (int a = 0; a < 3; ++a)
+                        U[a] = ((F.v_t[j] * (n1 * t1[a] + n2 * t2[a]) + d1 * t1[a]) + d2 * t2[a]) +
+                               F.c_mp[j] * u * n[a];
+                    Parcel p = make_parcel(F.cell[f], t, y, v3(U[0], U[1], U[2]));
+                    if (o.cfg.sync_velocity_at_boundary && S.charge != 0.0 && o.cfg.pusher != PICGPU_PUSHER_NONE)
+                        push(o, p, sp, -0.5 * o.cfg.dt);
+                    o.cloud[sp].push_back(p);
+                }
+            }
+        }
+    }
+}
+
 void inject(Oracle& o) {
     using namespace oinit;
     const HexMesh& m = o.m;
@@ -2242,6 +2321,7 @@ void inject(Oracle& o) {
             }
         }
     }
+    freestream_inject(o);
 }
 
 struct oracle_ctx {
@@ -2422,6 +2502,27 @@ int oracle_set_injection(oracle_ctx* ctx, int n, const picgpu_injection* inj) {
         I.tri = patch_triangles(o.m, q.patch);
         if (I.tri.cell.empty()) return PICGPU_INVALID_ARG;
         o.injectors.push_back(I);
+    }
+    return 0;
+}
+
+int oracle_set_freestream(oracle_ctx* ctx, int n, const picgpu_freestream* fs) {
+    Oracle& o = ctx->o;
+    if (n < 0 || n > PICGPU_MAX_FREESTREAMS || (n > 0 && !fs)) return PICGPU_INVALID_ARG;
+    for (int i = 0; i < n; ++i) {
+        const std::string e = pg::check_freestream(o.m, o.cfg, fs[i]);
+        if (!e.empty()) {
+            o.err = e;
+            return PICGPU_INVALID_ARG;
+        }
+    }
+    o.freestreams.clear();
+    for (int i = 0; i < n; ++i) {
+        Oracle::FreeStream Z;
+        Z.cfg = fs[i];
+        Z.F = pg::freestream_faces(o.m, o.cfg, fs[i]);
+        Z.acc.assign(size_t(Z.F.n_faces) * Z.F.n_species, 0.0);
+        o.freestreams.push_back(Z);
     }
     return 0;
 }

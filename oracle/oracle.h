@@ -51,6 +51,8 @@ int  oracle_initialise(oracle_ctx* ctx, const picgpu_init* init, picgpu_init_sta
 double oracle_det_log(double x);
 /* SimpleInjection boundary models (picgpu_set_injection's oracle). */
 int  oracle_set_injection(oracle_ctx* ctx, int n, const picgpu_injection* inj);
+/* FreeStream boundary models (picgpu_set_freestream's oracle). */
+int  oracle_set_freestream(oracle_ctx* ctx, int n, const picgpu_freestream* fs);
 double oracle_det_sin(double x);
 int  oracle_step(oracle_ctx* ctx, int nsteps, picgpu_step_stats* stats);
 int  oracle_move(oracle_ctx* ctx, picgpu_step_stats* stats);

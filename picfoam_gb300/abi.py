@@ -173,6 +173,16 @@ class Injection(C.Structure):
     ]
 
 
+MAX_FREESTREAMS = 8
+
+
+class FreeStream(C.Structure):
+    _fields_ = [
+        ("patch", C.c_int32), ("n_species", C.c_int32), ("species", C.c_int32 * MAX_SPECIES),
+        ("number_density", C.c_double * MAX_SPECIES), ("temperature", C.c_double), ("velocity", C.c_double * 3),
+    ]
+
+
 # picgpu_init.h
 INIT_NONE, INIT_EQUIPARTITION, INIT_MAXWELLIAN, INIT_ISOTROPIZATION, INIT_QUASINEUTRAL_PLASMA, \
     INIT_UNIFORM_DISPLACEMENT = range(6)

@@ -530,6 +530,21 @@ def injection(patch, species, frequency, eV, model=abi.EMIT_MAXWELLIAN_FLUX, end
     return q
 
 
+def freestream(patch, species, number_density, temperature, velocity=(0.0, 0.0, 0.0)):
+    """An abi.FreeStream (FreeStreamCoeffs numberDensities per species [1/m^3],
+    boundaryT [K] and boundaryU [m/s] on the patch)."""
+    q = abi.FreeStream()
+    q.patch = patch
+    q.n_species = len(species)
+    for j, s in enumerate(species):
+        q.species[j] = s
+        q.number_density[j] = number_density[j]
+    q.temperature = temperature
+    for a in range(3):
+        q.velocity[a] = velocity[a]
+    return q
+
+
 def empty_case(n_cells=(8, 8, 8), length=(0.01, 0.01, 0.01), sides=None, boxes=(), species=None,
                precision=abi.PREC_FP64, dt=1e-12, origin=(0.0, 0.0, 0.0), electron_species=0):
     """A case without particles: block mesh and config for picInitialise runs.

@@ -201,6 +201,8 @@ enum : uint32_t {
     kStreamBinaryBg = 11u << 28,      // neutral - background collisions per (cell, step)
     kStreamBinaryRemainder = 12u << 28,
     kStreamBinaryBgRemainder = 13u << 28,
+    kStreamFreeStreamCount = 14u << 28,  // FreeStream remainder draw per (injector << 4 | species, step, face)
+    kStreamFreeStream = 15u << 28,       // FreeStream parcels per (injector << 4 | species, step, face)
 };
 
 }  // namespace pgd

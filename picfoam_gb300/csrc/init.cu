@@ -504,6 +504,84 @@ __global__ void __launch_bounds__(256) inject_kernel(InjectParams P) {
     }
 }
 
+// FreeStream::injection (FreeStream.C:126-396): the face accumulator gains
+// its share of the flux; the integer part is emitted, plus one parcel when
+// the remainder exceeds a uniform draw.
+__global__ void __launch_bounds__(256) freestream_count_kernel(FreeStreamParams P) {
+    for (int f = blockIdx.x * blockDim.x + threadIdx.x; f < P.n_faces; f += gridDim.x * blockDim.x) {
+        const size_t i = size_t(f) * P.n_species + P.j;
+        double a = P.acc[i] + P.add[i];
+        long long n = a < 2.0e9 ? (long long)a : (1LL << 31);
+        if (n < 0) n = 0;
+        Philox r(P.seed, kStreamFreeStreamCount | (uint32_t(P.injector) << 4) | uint32_t(P.species), P.step,
+                 uint32_t(f));
+        if (a - double(n) > r.uniform()) ++n;
+        if (n > (1LL << 30)) {
+            *P.error = 2;
+            n = 0;
+        }
+        P.acc[i] = a - double(n);
+        P.counts[f] = int(n);
+    }
+}
+
+// The parcels of one face: a face triangle by area share, a uniform point on
+// it (barycentric 0 at the cell centre), the normal speed ratio by Bird's
+// acceptance-rejection (eq. 12.5, the QA scaling of DSMC3), thermal
+// tangential components and the drift's tangential part.
+__global__ void __launch_bounds__(256) freestream_emit_kernel(FreeStreamParams P) {
+    for (int f = blockIdx.x * blockDim.x + threadIdx.x; f < P.n_faces; f += gridDim.x * blockDim.x) {
+        const int cnt = P.counts[f];
+        if (cnt == 0) continue;
+        Philox r(P.seed, kStreamFreeStream | (uint32_t(P.injector) << 4) | uint32_t(P.species), P.step,
+                 uint32_t(f));
+        const double s = P.s[size_t(f) * P.n_species + P.j];
+        const double root = sqrt(s * s + 2.0);
+        const double qa = s + root;
+        const double qb = 0.5 * (1.0 + s * (s - root));
+        const double scaling = s < -3.0 ? fabs(s) + 1.0 : 3.0;
+        const double* n = P.n_in + 3 * size_t(f);
+        const double* t1 = P.t1 + 3 * size_t(f);
+        const double* t2 = P.t2 + 3 * size_t(f);
+        const double d1 = t1[0] * P.U[0] + t1[1] * P.U[1] + t1[2] * P.U[2];
+        const double d2 = t2[0] * P.U[0] + t2[1] * P.U[1] + t2[2] * P.U[2];
+        const int c = P.cell[f];
+        const long long base = P.first + P.offsets[f];
+        for (int k = 0; k < cnt; ++k) {
+            const double sel = r.uniform();
+            const int t = P.tet0[f] + (P.frac0[f] >= sel ? 0 : 1);
+            const double r1 = r.uniform(), r2 = r.uniform();
+            const double sr = sqrt(r1);
+            const double y[3] = {1.0 - sr, sr * (1.0 - r2), sr * r2};
+            double u = 0.0;
+            for (int it = 0; it < 10000; ++it) {
+                const double ut = scaling * (2.0 * r.uniform() - 1.0);
+                u = ut + s;
+                const double pr = u < 0.0 ? -1.0 : 2.0 * u / qa * det_exp(qb - ut * ut);
+                if (!(pr < r.uniform())) break;
+            }
+            double n1, n2;
+            polar_pair(r, n1, n2);
+            double U[3];
+            for (int a = 0; a < 3; ++a)
+                U[a] = ((P.v_t * (n1 * t1[a] + n2 * t2[a]) + d1 * t1[a]) + d2 * t2[a]) + P.c_mp * u * n[a];
+            const long long i = base + k;
+            P.tet[i] = 12 * c + t;
+            if (P.y64[0]) {
+                for (int a = 0; a < 3; ++a) {
+                    P.y64[a][i] = y[a];
+                    P.u64[a][i] = U[a];
+                }
+            } else {
+                for (int a = 0; a < 3; ++a) {
+                    P.y32[a][i] = float(y[a]);
+                    P.u32[a][i] = float(U[a]);
+                }
+            }
+        }
+    }
+}
+
 // ------------------------------------------------------------- scan ------
 constexpr int kScanChunk = 1024;  // 256 threads x 4 counts
 
@@ -578,6 +656,14 @@ inline int nblocks(long long n, int bs, int cap) { return int(std::min<long long
 
 void launch_init_count(const InitParams& P, int* counts, cudaStream_t s) {
     init_count_kernel<<<nblocks(P.m.n_cells, 256, 1 << 30), 256, 0, s>>>(P, counts);
+}
+
+void launch_freestream_count(const FreeStreamParams& P, cudaStream_t s) {
+    if (P.n_faces > 0) freestream_count_kernel<<<nblocks(P.n_faces, 256, 152 * 16), 256, 0, s>>>(P);
+}
+
+void launch_freestream_emit(const FreeStreamParams& P, cudaStream_t s) {
+    if (P.n_faces > 0) freestream_emit_kernel<<<nblocks(P.n_faces, 256, 152 * 16), 256, 0, s>>>(P);
 }
 
 long long init_scan_scratch(int n) { return (n + kScanChunk - 1) / kScanChunk + 1; }

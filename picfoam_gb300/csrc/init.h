@@ -87,4 +87,35 @@ struct InjectParams {
 };
 void launch_inject(const InjectParams& P, cudaStream_t s);
 
+// FreeStream (FreeStream.C:126-396) for one model and one of its species:
+// the per-face accumulators and counts, then the parcels of every face at
+// first + offsets[f] (the exclusive scan of the counts).
+struct FreeStreamParams {
+    DMesh m;
+    uint64_t seed;
+    uint32_t step;
+    int injector, species, j, n_species, n_faces;
+    const int* cell;          // per face: owner cell
+    const int* tet0;          // per face: local tet of its first triangle
+    const double* frac0;      // per face: first triangle's area share
+    const double* n_in;       // 3 per face
+    const double* t1;
+    const double* t2;
+    const double* add;        // n_faces * n_species
+    const double* s;          // n_faces * n_species
+    double c_mp, v_t, U[3];
+    double* acc;              // n_faces * n_species accumulators
+    int* counts;              // n_faces
+    const long long* offsets; // n_faces + 1
+    long long first;
+    int32_t* tet;
+    double* y64[3];
+    double* u64[3];
+    float* y32[3];
+    float* u32[3];
+    int* error;               // set to 2 when one face would emit more than 2^30 parcels
+};
+void launch_freestream_count(const FreeStreamParams& P, cudaStream_t s);
+void launch_freestream_emit(const FreeStreamParams& P, cudaStream_t s);
+
 }  // namespace pgd

@@ -25,6 +25,7 @@
 
 #include "collide.h"
 #include "fields.h"
+#include "freestream.hpp"
 #include "init.h"
 #include "hexmesh.hpp"
 #include "kernels.h"
@@ -157,6 +158,19 @@ struct Injector {
     double* tri_fc = nullptr;
 };
 
+// FreeStream boundary model: per-face tables and accumulators on the device.
+struct FsInjector {
+    picgpu_freestream cfg{};
+    pg::FreeStreamFaces F;          // host copy of the face tables
+    int* cell = nullptr;
+    int* tet0 = nullptr;
+    double *frac0 = nullptr, *n_in = nullptr, *t1 = nullptr, *t2 = nullptr, *add = nullptr, *s = nullptr;
+    double* acc = nullptr;          // n_faces * n_species
+    int* counts = nullptr;          // n_faces
+    long long* offsets = nullptr;   // n_faces + 1
+    long long* sums = nullptr;      // scan scratch
+};
+
 struct EventPair {
     cudaEvent_t a, b;
     int phase;
@@ -215,6 +229,7 @@ struct picgpu_ctx {
     int mg_outer = 0;                           // refinement steps of the last multigrid solve
     double* tet_vol = nullptr;                  // 12 tet volumes per geometry class (initial conditions)
     std::vector<Injector> injectors;            // SimpleInjection boundary models
+    std::vector<FsInjector> freestreams;        // FreeStream boundary models
     int* inj_err = nullptr;                     // an emitted parcel could not be located
     // row-major host arrays staged on the device (set/get_particles)
     int32_t* rows_tet = nullptr;
@@ -785,13 +800,76 @@ picgpu_status inject(picgpu_ctx* c) {
             B.alive += n;
         }
     }
+    // FreeStream::injection (FreeStream.C:126-396): counts per face on the
+    // device, their scan, the total read back to size the store, the parcels
+    for (size_t i = 0; i < c->freestreams.size(); ++i) {
+        FsInjector& Z = c->freestreams[i];
+        for (int j = 0; j < Z.cfg.n_species; ++j) {
+            const int sp = Z.cfg.species[j];
+            pgd::FreeStreamParams P{};
+            P.m = c->dm;
+            P.seed = c->cfg.seed;
+            P.step = uint32_t(c->step_index);
+            P.injector = int(i);
+            P.species = sp;
+            P.j = j;
+            P.n_species = Z.F.n_species;
+            P.n_faces = Z.F.n_faces;
+            P.cell = Z.cell;
+            P.tet0 = Z.tet0;
+            P.frac0 = Z.frac0;
+            P.n_in = Z.n_in;
+            P.t1 = Z.t1;
+            P.t2 = Z.t2;
+            P.add = Z.add;
+            P.s = Z.s;
+            P.c_mp = Z.F.c_mp[j];
+            P.v_t = Z.F.v_t[j];
+            for (int a = 0; a < 3; ++a) P.U[a] = Z.cfg.velocity[a];
+            P.acc = Z.acc;
+            P.counts = Z.counts;
+            P.offsets = Z.offsets;
+            P.error = c->inj_err;
+            pgd::launch_freestream_count(P, c->stream);
+            CK(pgd::init_scan(Z.counts, Z.offsets, Z.sums, Z.F.n_faces, c->stream));
+            long long total = 0;
+            CK(cudaMemcpyAsync(&total, Z.offsets + Z.F.n_faces, sizeof total, cudaMemcpyDeviceToHost, c->stream));
+            CK(cudaStreamSynchronize(c->stream));
+            c->launches += 4;
+            if (total <= 0) continue;
+            picgpu_status st = reserve_species(c, sp, total);
+            if (st) return st;
+            SpeciesBuf& B = c->sp[sp];
+            P.first = B.n;
+            P.tet = B.tet[B.cur];
+            for (int a = 0; a < 3; ++a) {
+                P.y64[a] = B.y64[B.cur][a];
+                P.u64[a] = B.u64[B.cur][a];
+                P.y32[a] = B.y32[B.cur][a];
+                P.u32[a] = B.u32[B.cur][a];
+            }
+            pgd::launch_freestream_emit(P, c->stream);
+            c->launches++;
+            // syncVelocityAtBoundary(-0.5) of the new parcels (FreeStream.C:385)
+            const picgpu_species& S = c->cfg.species[sp];
+            if (c->cfg.sync_velocity_at_boundary && S.charge != 0.0 && c->cfg.pusher != PICGPU_PUSHER_NONE) {
+                pgd::MoveParams MP = move_params(c, sp, false);
+                MP.first = int(B.n);
+                MP.n = int(B.n + total);
+                pgd::launch_push_only(MP, c->mixed, -0.5 * c->cfg.dt, grid_for(c, total), c->stream);
+                c->launches++;
+            }
+            B.n += total;
+            B.alive += total;
+        }
+    }
     CK(cudaGetLastError());
     return PICGPU_OK;
 }
 
 picgpu_status one_step(picgpu_ctx* c, picgpu_step_stats* stats, bool fields) {
     picgpu_status s;
-    if (!c->injectors.empty() && (s = inject(c))) return s;
+    if ((!c->injectors.empty() || !c->freestreams.empty()) && (s = inject(c))) return s;
     if ((s = zero_accumulators(c))) return s;
     if ((s = move_species(c, false))) return s;
     if ((s = read_counters(c))) return s;
@@ -802,9 +880,10 @@ picgpu_status one_step(picgpu_ctx* c, picgpu_step_stats* stats, bool fields) {
                                               ? "particle velocity reached the speed of light"
                                               : "tracking exceeded track_max_steps for a particle");
     add_counters(c, stats);
-    if (!c->injectors.empty()) {
+    if (!c->injectors.empty() || !c->freestreams.empty()) {
         int ie = 0;
         CK(cudaMemcpy(&ie, c->inj_err, sizeof(int), cudaMemcpyDeviceToHost));
+        if (ie == 2) return bad(c, PICGPU_INVALID_ARG, "freestream: more than 2^30 parcels on one face in one step");
         if (ie) return bad(c, PICGPU_INVALID_ARG, "injection: an emitted parcel left its owner cell");
     }
     if (c->cfg.sort_interval > 0 && (c->step_index + 1) % c->cfg.sort_interval == 0) {
@@ -1727,6 +1806,46 @@ picgpu_status picgpu_set_injection(picgpu_ctx* c, int n, const picgpu_injection*
     return PICGPU_OK;
 }
 
+picgpu_status picgpu_set_freestream(picgpu_ctx* c, int n, const picgpu_freestream* fs) {
+    if (!c || n < 0 || n > PICGPU_MAX_FREESTREAMS || (n > 0 && !fs)) return PICGPU_INVALID_ARG;
+    if (c->n_cases != 1) return bad(c, PICGPU_NOT_SUPPORTED, "freestream: not for ensemble contexts");
+    for (int i = 0; i < n; ++i) {
+        const std::string e = pg::check_freestream(c->m, c->cfg, fs[i]);
+        if (!e.empty()) return bad(c, PICGPU_INVALID_ARG, e);
+        for (int j = 0; j < fs[i].n_species; ++j)
+            if (!(c->cfg.species[fs[i].species[j]].weight > 0))
+                return bad(c, PICGPU_INVALID_ARG, "freestream: species without a weight");
+    }
+    for (FsInjector& Z : c->freestreams) {
+        for (void* p : {(void*)Z.cell, (void*)Z.tet0, (void*)Z.frac0, (void*)Z.n_in, (void*)Z.t1, (void*)Z.t2,
+                        (void*)Z.add, (void*)Z.s, (void*)Z.acc, (void*)Z.counts, (void*)Z.offsets, (void*)Z.sums})
+            dfree(c, p);
+    }
+    c->freestreams.clear();
+    for (int i = 0; i < n; ++i) {
+        c->freestreams.emplace_back();
+        FsInjector& Z = c->freestreams.back();
+        Z.cfg = fs[i];
+        Z.F = pg::freestream_faces(c->m, c->cfg, fs[i]);
+        const size_t nf = size_t(Z.F.n_faces);
+        picgpu_status st;
+        if ((st = upload(c, &Z.cell, Z.F.cell)) || (st = upload(c, &Z.tet0, Z.F.tet0)) ||
+            (st = upload(c, &Z.frac0, Z.F.frac0)) || (st = upload(c, &Z.n_in, Z.F.n_in)) ||
+            (st = upload(c, &Z.t1, Z.F.t1)) || (st = upload(c, &Z.t2, Z.F.t2)) || (st = upload(c, &Z.add, Z.F.add)) ||
+            (st = upload(c, &Z.s, Z.F.s)) || (st = dalloc(c, &Z.acc, nf * Z.F.n_species)) ||
+            (st = dalloc(c, &Z.counts, nf)) || (st = dalloc(c, &Z.offsets, nf + 1)) ||
+            (st = dalloc(c, &Z.sums, size_t(pgd::init_scan_scratch(int(nf))) + 1)))
+            return st;
+        CK(cudaMemset(Z.acc, 0, nf * Z.F.n_species * sizeof(double)));
+    }
+    if (!c->inj_err) {
+        picgpu_status st = dalloc(c, &c->inj_err, 1);
+        if (st) return st;
+    }
+    CK(cudaMemset(c->inj_err, 0, sizeof(int)));
+    return PICGPU_OK;
+}
+
 // ------------------------------------------------ initial conditions ----
 // picInitialise (preProcess/picInitialise/picInitialise.C:30-319) for a
 // context; the placement runs on the device (csrc/init.cu).
@@ -2282,7 +2401,7 @@ picgpu_status picgpu_ensemble_case_stats(picgpu_ctx* c, int species, double* out
 }
 
 picgpu_status picgpu_step_graph(picgpu_ctx* c, int nsteps, int steps_per_graph, picgpu_step_stats* stats) {
-    if (c && !c->injectors.empty())
+    if (c && (!c->injectors.empty() || !c->freestreams.empty()))
         return bad(c, PICGPU_NOT_SUPPORTED, "step_graph: injection runs only in picgpu_step");
     if (c && c->circ.model != PICGPU_CIRCUIT_NONE)
         return bad(c, PICGPU_NOT_SUPPORTED, "step_graph: circuit models run only in picgpu_step");

@@ -40,6 +40,7 @@ def declare(lib, prefix, ctx_api=True):
     f("initialise_fields", i, [P])
     f("initialise", i, [P, C.POINTER(abi.Init), C.POINTER(abi.InitStats)])
     f("set_injection", i, [P, i, C.POINTER(abi.Injection)])
+    f("set_freestream", i, [P, i, C.POINTER(abi.FreeStream)])
     f("step", i, [P, i, C.POINTER(abi.StepStats)])
     f("move", i, [P, C.POINTER(abi.StepStats)])
     f("solve_poisson", i, [P, F64P, F64P, C.POINTER(abi.StepStats)])

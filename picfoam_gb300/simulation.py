@@ -141,6 +141,12 @@ class Simulation:
         arr = (abi.Injection * max(len(injectors), 1))(*injectors)
         self._check(self._fn("set_injection")(self._h, len(injectors), arr))
 
+    def set_freestream(self, models):
+        """FreeStream boundary models: a list of abi.FreeStream (empty removes
+        them; the face accumulators restart at zero)."""
+        arr = (abi.FreeStream * max(len(models), 1))(*models)
+        self._check(self._fn("set_freestream")(self._h, len(models), arr))
+
     def initialise(self, init):
         """picInitialise: place the particles of an abi.Init on the device (or
         in the oracle), compute the fields, optionally solve them and apply
