@@ -33,6 +33,11 @@ METRIC = "particle-steps/s (push+track+deposit)"
 UNIT = "particle-steps/s"
 BYTES_FP32 = 56   # int32 tet + 3 x f32 barycentric + 3 x f32 velocity, read + write
 BYTES_FP64 = 104  # int32 tet + 3 x f64 barycentric + 3 x f64 velocity, read + write
+# DRAM bytes (read + write) per particle-step of move_kernel_fp32 measured by
+# ncu (dram__bytes_read.sum + dram__bytes_write.sum) on the 40^3 case of this
+# workload; profiles/move_kernel_fp32_two_species_40cube.md.  The traffic is
+# per particle, so a full launch scales by its particles.
+TRAFFIC_FP32_PER_PARTICLE = 44.3
 
 
 def parse():
@@ -519,7 +524,11 @@ def run_ours(args, rank, ws):
             "dtype": "f32 push/track + f64 deposit" if prec == abi.PREC_MIXED else "f64",
             "data": "synthetic (seeded Maxwellian plasma, uniform positions)", "config": workload(args),
             "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
-                         "frac": achieved / peak, "traffic": None,
+                         "frac": achieved / peak,
+                         "traffic": (TRAFFIC_FP32_PER_PARTICLE * n_steps_particles / max(move_launches, 1)
+                                     if prec == abi.PREC_MIXED else None),
+                         "traffic_source": "ncu dram__bytes_read.sum + dram__bytes_write.sum, 40^3 capture "
+                                           "scaled by particles per launch (profiles/move_kernel_fp32_two_species_40cube.md)",
                          "peak_source": f"{peak_kind} (MEASURED_PEAKS.json hbm_gbs)" if peak_kind == "measured"
                          else "fallback 6.8 TB/s",
                          "kernel": "move_kernel_fp32" if prec == abi.PREC_MIXED else "move_kernel_fp64",
