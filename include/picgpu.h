@@ -483,6 +483,30 @@ typedef struct {
 } picgpu_freestream;
 picgpu_status picgpu_set_freestream(picgpu_ctx* ctx, int n, const picgpu_freestream* fs);
 
+/* EmissionModels of the circuit models (SM/Helper/Emission): electrons of
+ * the config's electron_species leave `patch` through the ParticleEmitter
+ * with the maxwellianFlux velocity model, n = J A dt / (w e) + remainder per
+ * step (A the patch area), after the SimpleInjection and FreeStream models.
+ *   THERMIONIC       ThermionicEmission.C: J = lambdaR A0 T^2 exp(-W e/(k T)),
+ *                    emitted at temperature T;
+ *   FOWLER_NORDHEIM  FowlerNordheim.C: J summed over the patch faces with an
+ *                    outward field E (Wang-Loew v(y), t = 1), emitted at
+ *                    temperature W e / k.
+ * The emitted charge is taken off a floating or circuit patch
+ * (particleEjection).  n = 0 removes all.  Not for ensemble contexts or
+ * picgpu_step_graph. */
+enum { PICGPU_EMISSION_THERMIONIC = 0, PICGPU_EMISSION_FOWLER_NORDHEIM = 1 };
+#define PICGPU_MAX_EMISSIONS 8
+typedef struct {
+    int32_t patch;          /* emitting patch (not cyclic / empty) */
+    int32_t model;          /* PICGPU_EMISSION_* */
+    double  work_function;  /* fnW [eV] */
+    double  temperature;    /* T [K] (thermionic) */
+    double  lambda_r;       /* lambdaR (thermionic) */
+    double  weight;         /* nParticle (<= 0: the electron species' weight; otherwise it must equal it) */
+} picgpu_emission;
+picgpu_status picgpu_set_emission(picgpu_ctx* ctx, int n, const picgpu_emission* em);
+
 /* Advance nsteps time steps. */
 picgpu_status picgpu_step(picgpu_ctx* ctx, int nsteps, picgpu_step_stats* stats);
 

@@ -24,6 +24,7 @@
 #include "picgpu_init.h"
 #include "../picfoam_gb300/csrc/hexmesh.hpp"
 #include "../picfoam_gb300/csrc/circuit.hpp"
+#include "../picfoam_gb300/csrc/emission.hpp"
 #include "../picfoam_gb300/csrc/freestream.hpp"
 
 #include <algorithm>
@@ -177,6 +178,14 @@ struct Oracle {
         std::vector<double> acc;   // n_faces * n_species
     };
     std::vector<FreeStream> freestreams;
+    // EmissionModels
+    struct Emitter {
+        picgpu_emission cfg{};
+        PatchTriangles tri;
+        double j = 0.0, remainder = 0.0;
+        std::vector<int> faces;
+    };
+    std::vector<Emitter> emitters;
     // BinaryCollisionModel state per cell
     std::vector<double> bsmax, brem, bbgrem;
 };
@@ -2217,17 +2226,110 @@ void freestream_inject(Oracle& o) {
     }
 }
 
-void inject(Oracle& o) {
+// ParticleEmitter::emitParticle for n parcels of species sp from the
+// patch's face triangles T (the RNG stream of emitter `index`), with the
+// floating / circuit patch charge taken off first.
+void emit_parcels(Oracle& o, const PatchTriangles& T, int index, int patch, int sp, long long n, int model,
+                  double temperature) {
     using namespace oinit;
     const HexMesh& m = o.m;
     const double dt = o.cfg.dt;
-    const double t = double(o.step_index + 1) * dt;
     const bool cons = m.empty[0] || m.empty[1] || m.empty[2];
+    const picgpu_species& S = o.cfg.species[sp];
+    const int ntri = int(T.cell.size());
+    const int pk = m.patches[patch].p.kind;
+    if (pk == PICGPU_PATCH_FLOATING || pk == PICGPU_PATCH_CIRCUIT)
+        o.Qconv[patch] = o.Qconv[patch] - double(n) * S.charge * S.weight;
+    for (long long k = 0; k < n; ++k) {
+        ocoll::Philox r(o.cfg.seed, ocoll::kStreamInject | (uint32_t(index) << 4) | uint32_t(sp),
+                        uint32_t(o.step_index), uint32_t(k));
+        const double af = r.uniform() * T.area;
+        int tri = 0;
+        for (int q = ntri - 1; q >= 0; --q)
+            if (af > T.cum[q]) { tri = q; break; }
+        const int c = T.cell[tri], tt = T.tet[tri];
+        const double* off = &m.cls_offset[size_t(m.cell_class[c]) * 24];
+        const double* cc = &m.cc[3 * size_t(c)];
+        double A[3], B[3], Cc[3];
+        for (int a = 0; a < 3; ++a) {
+            A[a] = cc[a] + off[3 * m.tt.tri[tt][0] + a];
+            B[a] = cc[a] + off[3 * m.tt.tri[tt][1] + a];
+            Cc[a] = cc[a] + off[3 * m.tt.tri[tt][2] + a];
+        }
+        // triPointRef::randomPoint: (1 - sqrt r1) A + sqrt r1 (1 - r2) B + sqrt r1 r2 C
+        const double r1 = r.uniform(), r2 = r.uniform();
+        const double sr = std::sqrt(r1);
+        double pf[3];
+        for (int a = 0; a < 3; ++a) pf[a] = (1.0 - sr) * A[a] + sr * (1.0 - r2) * B[a] + sr * r2 * Cc[a];
+        const double fa = 0.1 + 0.4 * r.uniform();  // scalarAB(0.1, 0.5)
+        const double* nrm = &T.normal[3 * size_t(tri)];
+        const double dn =
+            std::fabs((pf[0] - cc[0]) * nrm[0] + (pf[1] - cc[1]) * nrm[1] + (pf[2] - cc[2]) * nrm[2]);
+        double x[3];
+        for (int a = 0; a < 3; ++a) x[a] = pf[a] - fa * (dn * nrm[a]);
+        const double* fc = &T.centre[3 * size_t(tri)];
+        double nn[3], t1[3], t2[3];
+        for (int a = 0; a < 3; ++a) {
+            nn[a] = -nrm[a];
+            t1[a] = fc[a] - A[a];
+        }
+        const double m1 = std::sqrt(t1[0] * t1[0] + t1[1] * t1[1] + t1[2] * t1[2]);
+        for (int a = 0; a < 3; ++a) t1[a] = t1[a] / m1;
+        t2[0] = nn[1] * t1[2] - nn[2] * t1[1];
+        t2[1] = nn[2] * t1[0] - nn[0] * t1[2];
+        t2[2] = nn[0] * t1[1] - nn[1] * t1[0];
+        const double m2 = std::sqrt(t2[0] * t2[0] + t2[1] * t2[1] + t2[2] * t2[2]);
+        for (int a = 0; a < 3; ++a) t2[a] = t2[a] / m2;
+        double U[3];
+        const double vt = std::sqrt(kBoltzmann * temperature / S.mass);
+        if (model == PICGPU_EMIT_MOST_PROBABLE_SPEED) {
+            const double vmp = std::sqrt(2.0 * kBoltzmann * temperature / S.mass);
+            for (int a = 0; a < 3; ++a) U[a] = vmp * nn[a];
+        } else {
+            double n1, n2;
+            polar_pair(r, n1, n2);
+            double tg[3];
+            for (int a = 0; a < 3; ++a) tg[a] = vt * (n1 * t1[a] + n2 * t2[a]);
+            double un;
+            if (model == PICGPU_EMIT_BIRD_MAXWELLIAN_FLUX) {
+                const double vmp = std::sqrt(2.0 * kBoltzmann * temperature / S.mass);
+                double u = 0.0;
+                for (int it = 0; it < 1000; ++it) {  // do { ... } while (P < U01)
+                    u = 3.0 * (2.0 * r.uniform() - 1.0);
+                    const double pr = u < 0.0 ? -1.0 : 2.0 * u / 1.4142135623730951 * det_exp(0.5 - u * u);
+                    if (!(pr < r.uniform())) break;
+                }
+                un = vmp * u;
+            } else if (model == PICGPU_EMIT_HALF_MAXWELLIAN_FLUX) {
+                double n3, n4;
+                polar_pair(r, n3, n4);
+                un = std::fabs(n3) * vt;
+            } else {
+                const double R = r.uniform();
+                un = vt * std::sqrt(-2.0 * det_log(1.0 - R));
+            }
+            for (int a = 0; a < 3; ++a) U[a] = tg[a] + un * nn[a];
+        }
+        for (int a = 0; a < 3; ++a)
+            if (cons && m.empty[a]) x[a] = 0.0;
+        int tet = 0;
+        double y[3] = {0, 0, 0};
+        locate_in_cell(m, c, x, tet, y);
+        Parcel p = make_parcel(c, tet, y, v3(U[0], U[1], U[2]));
+        if (o.cfg.sync_velocity_at_boundary && S.charge != 0.0 && o.cfg.pusher != PICGPU_PUSHER_NONE)
+            push(o, p, sp, -0.5 * dt);
+        o.cloud[sp].push_back(p);
+    }
+}
+
+void inject(Oracle& o) {
+    using namespace oinit;
+    const double dt = o.cfg.dt;
+    const double t = double(o.step_index + 1) * dt;
     for (size_t i = 0; i < o.injectors.size(); ++i) {
         Oracle::Injector& I = o.injectors[i];
         if (t > I.cfg.end_time) continue;
         const PatchTriangles& T = I.tri;
-        const int ntri = int(T.cell.size());
         for (int j = 0; j < I.cfg.n_species; ++j) {
             const int sp = I.cfg.species[j];
             const picgpu_species& S = o.cfg.species[sp];
@@ -2235,93 +2337,33 @@ void inject(Oracle& o) {
             const long long n = (long long)np;
             I.remainder[j] = np - double(n);
             if (n <= 0) continue;
-            const int pk = m.patches[I.cfg.patch].p.kind;
-            if (pk == PICGPU_PATCH_FLOATING || pk == PICGPU_PATCH_CIRCUIT)
-                o.Qconv[I.cfg.patch] = o.Qconv[I.cfg.patch] - double(n) * S.charge * S.weight;
-            const double temperature = I.cfg.eV[j] * 1.602176634e-19 / kBoltzmann;
-            for (long long k = 0; k < n; ++k) {
-                ocoll::Philox r(o.cfg.seed, ocoll::kStreamInject | (uint32_t(i) << 4) | uint32_t(sp),
-                                uint32_t(o.step_index), uint32_t(k));
-                const double af = r.uniform() * T.area;
-                int tri = 0;
-                for (int q = ntri - 1; q >= 0; --q)
-                    if (af > T.cum[q]) { tri = q; break; }
-                const int c = T.cell[tri], tt = T.tet[tri];
-                const double* off = &m.cls_offset[size_t(m.cell_class[c]) * 24];
-                const double* cc = &m.cc[3 * size_t(c)];
-                double A[3], B[3], Cc[3];
-                for (int a = 0; a < 3; ++a) {
-                    A[a] = cc[a] + off[3 * m.tt.tri[tt][0] + a];
-                    B[a] = cc[a] + off[3 * m.tt.tri[tt][1] + a];
-                    Cc[a] = cc[a] + off[3 * m.tt.tri[tt][2] + a];
-                }
-                // triPointRef::randomPoint: (1 - sqrt r1) A + sqrt r1 (1 - r2) B + sqrt r1 r2 C
-                const double r1 = r.uniform(), r2 = r.uniform();
-                const double sr = std::sqrt(r1);
-                double pf[3];
-                for (int a = 0; a < 3; ++a) pf[a] = (1.0 - sr) * A[a] + sr * (1.0 - r2) * B[a] + sr * r2 * Cc[a];
-                const double fa = 0.1 + 0.4 * r.uniform();  // scalarAB(0.1, 0.5)
-                const double* nrm = &T.normal[3 * size_t(tri)];
-                const double dn =
-                    std::fabs((pf[0] - cc[0]) * nrm[0] + (pf[1] - cc[1]) * nrm[1] + (pf[2] - cc[2]) * nrm[2]);
-                double x[3];
-                for (int a = 0; a < 3; ++a) x[a] = pf[a] - fa * (dn * nrm[a]);
-                const double* fc = &T.centre[3 * size_t(tri)];
-                double nn[3], t1[3], t2[3];
-                for (int a = 0; a < 3; ++a) {
-                    nn[a] = -nrm[a];
-                    t1[a] = fc[a] - A[a];
-                }
-                const double m1 = std::sqrt(t1[0] * t1[0] + t1[1] * t1[1] + t1[2] * t1[2]);
-                for (int a = 0; a < 3; ++a) t1[a] = t1[a] / m1;
-                t2[0] = nn[1] * t1[2] - nn[2] * t1[1];
-                t2[1] = nn[2] * t1[0] - nn[0] * t1[2];
-                t2[2] = nn[0] * t1[1] - nn[1] * t1[0];
-                const double m2 = std::sqrt(t2[0] * t2[0] + t2[1] * t2[1] + t2[2] * t2[2]);
-                for (int a = 0; a < 3; ++a) t2[a] = t2[a] / m2;
-                double U[3];
-                const double vt = std::sqrt(kBoltzmann * temperature / S.mass);
-                if (I.cfg.velocity_model == PICGPU_EMIT_MOST_PROBABLE_SPEED) {
-                    const double vmp = std::sqrt(2.0 * kBoltzmann * temperature / S.mass);
-                    for (int a = 0; a < 3; ++a) U[a] = vmp * nn[a];
-                } else {
-                    double n1, n2;
-                    polar_pair(r, n1, n2);
-                    double tg[3];
-                    for (int a = 0; a < 3; ++a) tg[a] = vt * (n1 * t1[a] + n2 * t2[a]);
-                    double un;
-                    if (I.cfg.velocity_model == PICGPU_EMIT_BIRD_MAXWELLIAN_FLUX) {
-                        const double vmp = std::sqrt(2.0 * kBoltzmann * temperature / S.mass);
-                        double u = 0.0;
-                        for (int it = 0; it < 1000; ++it) {  // do { ... } while (P < U01)
-                            u = 3.0 * (2.0 * r.uniform() - 1.0);
-                            const double pr = u < 0.0 ? -1.0 : 2.0 * u / 1.4142135623730951 * det_exp(0.5 - u * u);
-                            if (!(pr < r.uniform())) break;
-                        }
-                        un = vmp * u;
-                    } else if (I.cfg.velocity_model == PICGPU_EMIT_HALF_MAXWELLIAN_FLUX) {
-                        double n3, n4;
-                        polar_pair(r, n3, n4);
-                        un = std::fabs(n3) * vt;
-                    } else {
-                        const double R = r.uniform();
-                        un = vt * std::sqrt(-2.0 * det_log(1.0 - R));
-                    }
-                    for (int a = 0; a < 3; ++a) U[a] = tg[a] + un * nn[a];
-                }
-                for (int a = 0; a < 3; ++a)
-                    if (cons && m.empty[a]) x[a] = 0.0;
-                int tet = 0;
-                double y[3] = {0, 0, 0};
-                locate_in_cell(m, c, x, tet, y);
-                Parcel p = make_parcel(c, tet, y, v3(U[0], U[1], U[2]));
-                if (o.cfg.sync_velocity_at_boundary && S.charge != 0.0 && o.cfg.pusher != PICGPU_PUSHER_NONE)
-                    push(o, p, sp, -0.5 * dt);
-                o.cloud[sp].push_back(p);
-            }
+            emit_parcels(o, T, int(i), I.cfg.patch, sp, n, I.cfg.velocity_model,
+                         I.cfg.eV[j] * 1.602176634e-19 / kBoltzmann);
         }
     }
     freestream_inject(o);
+    // EmissionModels (SM/Helper/Emission): n = J A dt / (w e) + remainder
+    for (size_t i = 0; i < o.emitters.size(); ++i) {
+        Oracle::Emitter& Z = o.emitters[i];
+        const int sp = o.cfg.electron_species;
+        const picgpu_species& S = o.cfg.species[sp];
+        const double qe = std::fabs(S.charge);
+        double j = Z.j;
+        double temperature = Z.cfg.temperature;
+        if (Z.cfg.model == PICGPU_EMISSION_FOWLER_NORDHEIM) {
+            j = pg::emission_face_sum(int(Z.faces.size()), [&](int k) {
+                const int b = Z.faces[k];
+                return pg::fowler_nordheim_face(&o.Eb[3 * size_t(b)], o.m.bfaces[b].normal, Z.cfg.work_function);
+            });
+            temperature = Z.cfg.work_function * qe / kBoltzmann;
+        }
+        const double ne = j * Z.tri.area * dt / (S.weight * qe) + Z.remainder;
+        const long long n = (long long)ne;
+        Z.remainder = ne - double(n);
+        if (n > 0)
+            emit_parcels(o, Z.tri, PICGPU_MAX_INJECTORS + int(i), Z.cfg.patch, sp, n, PICGPU_EMIT_MAXWELLIAN_FLUX,
+                         temperature);
+    }
 }
 
 struct oracle_ctx {
@@ -2502,6 +2544,39 @@ int oracle_set_injection(oracle_ctx* ctx, int n, const picgpu_injection* inj) {
         I.tri = patch_triangles(o.m, q.patch);
         if (I.tri.cell.empty()) return PICGPU_INVALID_ARG;
         o.injectors.push_back(I);
+    }
+    return 0;
+}
+
+int oracle_set_emission(oracle_ctx* ctx, int n, const picgpu_emission* em) {
+    Oracle& o = ctx->o;
+    if (n < 0 || n > PICGPU_MAX_EMISSIONS || (n > 0 && !em)) return PICGPU_INVALID_ARG;
+    const int es = o.cfg.electron_species;
+    for (int i = 0; i < n; ++i) {
+        const picgpu_emission& q = em[i];
+        if (es < 0 || es >= o.cfg.n_species || o.cfg.species[es].charge == 0.0) return PICGPU_INVALID_ARG;
+        if (q.patch < 0 || q.patch >= int(o.m.patches.size())) return PICGPU_INVALID_ARG;
+        const int kind = o.m.patches[q.patch].p.kind;
+        if (kind == PICGPU_PATCH_CYCLIC || kind == PICGPU_PATCH_EMPTY) return PICGPU_INVALID_ARG;
+        if (q.model != PICGPU_EMISSION_THERMIONIC && q.model != PICGPU_EMISSION_FOWLER_NORDHEIM)
+            return PICGPU_INVALID_ARG;
+        if (!(q.work_function > 0.0)) return PICGPU_INVALID_ARG;
+        if (q.model == PICGPU_EMISSION_THERMIONIC && !(q.temperature > 0.0 && q.lambda_r >= 0.0))
+            return PICGPU_INVALID_ARG;
+        if (q.weight > 0.0 && q.weight != o.cfg.species[es].weight) return PICGPU_INVALID_ARG;
+    }
+    o.emitters.clear();
+    for (int i = 0; i < n; ++i) {
+        Oracle::Emitter Z;
+        Z.cfg = em[i];
+        Z.tri = patch_triangles(o.m, em[i].patch);
+        if (Z.tri.cell.empty()) return PICGPU_INVALID_ARG;
+        if (em[i].model == PICGPU_EMISSION_THERMIONIC)
+            Z.j = pg::thermionic_current(em[i].lambda_r, em[i].temperature, em[i].work_function,
+                                         std::fabs(o.cfg.species[es].charge));
+        for (size_t b = 0; b < o.m.bfaces.size(); ++b)
+            if (o.m.bfaces[b].patch == em[i].patch) Z.faces.push_back(int(b));
+        o.emitters.push_back(Z);
     }
     return 0;
 }

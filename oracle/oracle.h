@@ -53,6 +53,8 @@ double oracle_det_log(double x);
 int  oracle_set_injection(oracle_ctx* ctx, int n, const picgpu_injection* inj);
 /* FreeStream boundary models (picgpu_set_freestream's oracle). */
 int  oracle_set_freestream(oracle_ctx* ctx, int n, const picgpu_freestream* fs);
+/* EmissionModels (picgpu_set_emission's oracle). */
+int  oracle_set_emission(oracle_ctx* ctx, int n, const picgpu_emission* em);
 double oracle_det_sin(double x);
 int  oracle_step(oracle_ctx* ctx, int nsteps, picgpu_step_stats* stats);
 int  oracle_move(oracle_ctx* ctx, picgpu_step_stats* stats);

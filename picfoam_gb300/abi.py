@@ -183,6 +183,17 @@ class FreeStream(C.Structure):
     ]
 
 
+EMISSION_THERMIONIC, EMISSION_FOWLER_NORDHEIM = range(2)
+MAX_EMISSIONS = 8
+
+
+class Emission(C.Structure):
+    _fields_ = [
+        ("patch", C.c_int32), ("model", C.c_int32), ("work_function", C.c_double), ("temperature", C.c_double),
+        ("lambda_r", C.c_double), ("weight", C.c_double),
+    ]
+
+
 # picgpu_init.h
 INIT_NONE, INIT_EQUIPARTITION, INIT_MAXWELLIAN, INIT_ISOTROPIZATION, INIT_QUASINEUTRAL_PLASMA, \
     INIT_UNIFORM_DISPLACEMENT = range(6)

@@ -545,6 +545,19 @@ def freestream(patch, species, number_density, temperature, velocity=(0.0, 0.0, 
     return q
 
 
+def emission(patch, model, work_function, temperature=0.0, lambda_r=0.5, weight=0.0):
+    """An abi.Emission (ThermionicEmissionCoeffs / FowlerNordheimCoeffs:
+    fnW [eV], T [K], lambdaR, nParticle)."""
+    q = abi.Emission()
+    q.patch = patch
+    q.model = model
+    q.work_function = work_function
+    q.temperature = temperature
+    q.lambda_r = lambda_r
+    q.weight = weight
+    return q
+
+
 def empty_case(n_cells=(8, 8, 8), length=(0.01, 0.01, 0.01), sides=None, boxes=(), species=None,
                precision=abi.PREC_FP64, dt=1e-12, origin=(0.0, 0.0, 0.0), electron_species=0):
     """A case without particles: block mesh and config for picInitialise runs.

@@ -16,6 +16,7 @@
 //   boundary_E      corrected boundary values of E
 //   point_E         cell -> point interpolation (VolumeWeightingFW.C:70-75)
 #include "circuit.hpp"
+#include "emission.hpp"
 #include "fields.h"
 #include "reduce.cuh"
 
@@ -160,6 +161,28 @@ circuit_post_kernel(CircuitParams P, DMesh m, double src, double beta, const dou
     pg::circuit_post_update(P.model, P.anode, P.cathode, P.n_faces, P.a, P.area, P.dt, src, beta, lane[0], qconv,
                             st);
     *S = st;
+}
+
+// FowlerNordheim::emission (FowlerNordheim.C:64-86): the current density
+// summed over the patch faces, in the lane order pg::emission_face_sum
+// restates.
+__global__ void __launch_bounds__(pg::kEmissionLanes)
+fowler_nordheim_kernel(DMesh m, const double* __restrict__ Eb, const int* __restrict__ faces, int n, double W,
+                       double* out) {
+    __shared__ double lane[pg::kEmissionLanes];
+    const int t = threadIdx.x;
+    double a = 0.0;
+    for (int i = t; i < n; i += pg::kEmissionLanes) {
+        const int b = faces[i];
+        a = a + pg::fowler_nordheim_face(Eb + 3 * size_t(b), m.bf_normal + 3 * size_t(b), W);
+    }
+    lane[t] = a;
+    __syncthreads();
+    for (int s = pg::kEmissionLanes / 2; s > 0; s >>= 1) {
+        if (t < s) lane[t] = lane[t] + lane[t + s];
+        __syncthreads();
+    }
+    if (t == 0) *out = lane[0];
 }
 
 // ----------------------------------------------------------- Poisson -----
@@ -556,6 +579,11 @@ void launch_circuit_pre(const CircuitParams& P, double src, double* qconv, doubl
 void launch_circuit_post(const CircuitParams& P, const DMesh& m, double src, double beta, const double* phi,
                          double* qconv, pg::CircuitState* S, cudaStream_t s) {
     circuit_post_kernel<<<1, pg::kCircuitLanes, 0, s>>>(P, m, src, beta, phi, qconv, S);
+}
+
+void launch_fowler_nordheim(const DMesh& m, const double* Eb, const int* faces, int n, double W, double* out,
+                            cudaStream_t s) {
+    fowler_nordheim_kernel<<<1, pg::kEmissionLanes, 0, s>>>(m, Eb, faces, n, W, out);
 }
 
 int pcg_blocks(int n) { return (n + kChunk - 1) / kChunk; }

@@ -50,6 +50,9 @@ struct CircuitParams {
 };
 void launch_circuit_pre(const CircuitParams& P, double src, double* qconv, double* grad_bc, pg::CircuitState* S,
                         cudaStream_t s);
+// Fowler-Nordheim current density summed over the given boundary faces -> *out.
+void launch_fowler_nordheim(const DMesh& m, const double* Eb, const int* faces, int n, double W, double* out,
+                            cudaStream_t s);
 void launch_circuit_post(const CircuitParams& P, const DMesh& m, double src, double beta, const double* phi,
                          double* qconv, pg::CircuitState* S, cudaStream_t s);
 void launch_rhs(const DMesh& m, const double* rho, const double* grad_bc, double* b, int singular,

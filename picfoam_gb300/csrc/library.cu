@@ -25,6 +25,7 @@
 
 #include "collide.h"
 #include "fields.h"
+#include "emission.hpp"
 #include "freestream.hpp"
 #include "init.h"
 #include "hexmesh.hpp"
@@ -156,6 +157,12 @@ struct Injector {
     int* tri_tet = nullptr;
     double* tri_normal = nullptr;
     double* tri_fc = nullptr;
+    // EmissionModel (picgpu_set_emission) on the patch
+    picgpu_emission em{};
+    double em_j = 0.0;             // thermionic current density [A/m^2]
+    double em_remainder = 0.0;     // pRemainder_
+    int* em_faces = nullptr;       // Fowler-Nordheim: the patch's boundary faces
+    int em_n_faces = 0;
 };
 
 // FreeStream boundary model: per-face tables and accumulators on the device.
@@ -230,6 +237,8 @@ struct picgpu_ctx {
     double* tet_vol = nullptr;                  // 12 tet volumes per geometry class (initial conditions)
     std::vector<Injector> injectors;            // SimpleInjection boundary models
     std::vector<FsInjector> freestreams;        // FreeStream boundary models
+    std::vector<Injector> emitters;             // EmissionModels
+    double* em_sum = nullptr;                   // Fowler-Nordheim patch current (device scalar)
     int* inj_err = nullptr;                     // an emitted parcel could not be located
     // row-major host arrays staged on the device (set/get_particles)
     int32_t* rows_tet = nullptr;
@@ -734,12 +743,71 @@ picgpu_status reserve_species(picgpu_ctx* c, int s, long long add) {
     return grow_species(c, s, cap);
 }
 
+// ParticleEmitter::emitParticle for n parcels of species sp from the patch
+// of I (the RNG stream of emitter `index`), then syncVelocityAtBoundary(-0.5);
+// the emitted charge comes off a floating or circuit patch.
+picgpu_status emit_parcels(picgpu_ctx* c, const Injector& I, int index, int patch, int sp, long long n,
+                           int model, double temperature) {
+    const double dt = c->cfg.dt;
+    const bool any_empty = c->m.empty[0] || c->m.empty[1] || c->m.empty[2];
+    const picgpu_species& S = c->cfg.species[sp];
+    picgpu_status st = reserve_species(c, sp, n);
+    if (st) return st;
+    SpeciesBuf& B = c->sp[sp];
+    pgd::InjectParams P{};
+    P.m = c->dm;
+    P.seed = c->cfg.seed;
+    P.step = uint32_t(c->step_index);
+    P.injector = index;
+    P.species = sp;
+    P.model = model;
+    P.constrain = any_empty;
+    P.mass = S.mass;
+    P.temperature = temperature;
+    P.n = n;
+    P.n_tri = I.n_tri;
+    P.tri_cum = I.tri_cum;
+    P.tri_cell = I.tri_cell;
+    P.tri_tet = I.tri_tet;
+    P.tri_normal = I.tri_normal;
+    P.tri_fc = I.tri_fc;
+    P.area = I.area;
+    P.patch = patch;
+    const int pk = c->m.patches[patch].p.kind;
+    if (pk == PICGPU_PATCH_FLOATING || pk == PICGPU_PATCH_CIRCUIT) {
+        P.qconv = c->qconv;
+        P.ejected_charge = double(n) * S.charge * S.weight;
+    }
+    P.first = B.n;
+    P.tet = B.tet[B.cur];
+    for (int a = 0; a < 3; ++a) {
+        P.y64[a] = B.y64[B.cur][a];
+        P.u64[a] = B.u64[B.cur][a];
+        P.y32[a] = B.y32[B.cur][a];
+        P.u32[a] = B.u32[B.cur][a];
+    }
+    P.error = c->inj_err;
+    pgd::launch_inject(P, c->stream);
+    c->launches++;
+    // syncVelocityAtBoundary(-0.5) of the new parcels (ParticleEmitter.C:401)
+    if (c->cfg.sync_velocity_at_boundary && S.charge != 0.0 && c->cfg.pusher != PICGPU_PUSHER_NONE) {
+        pgd::MoveParams MP = move_params(c, sp, false);
+        MP.first = int(B.n);
+        MP.n = int(B.n + n);
+        pgd::launch_push_only(MP, c->mixed, -0.5 * dt, grid_for(c, n), c->stream);
+        c->launches++;
+    }
+    B.n += n;
+    B.alive += n;
+    return PICGPU_OK;
+}
+
 // boundaryModels().injection() (PICCloud.C:1435): SimpleInjection::injection
-// (SimpleInjection.C:197-240) for every injector, before the move.
+// (SimpleInjection.C:197-240) for every injector, before the move; then the
+// FreeStream models and the EmissionModels.
 picgpu_status inject(picgpu_ctx* c) {
     const double dt = c->cfg.dt;
     const double t = double(c->step_index + 1) * dt;  // OpenFOAM advances the time before evolve
-    bool any_empty = c->m.empty[0] || c->m.empty[1] || c->m.empty[2];
     for (size_t i = 0; i < c->injectors.size(); ++i) {
         Injector& I = c->injectors[i];
         if (t > I.cfg.end_time) continue;
@@ -750,54 +818,9 @@ picgpu_status inject(picgpu_ctx* c) {
             const long long n = (long long)np;
             I.remainder[j] = np - double(n);
             if (n <= 0) continue;
-            picgpu_status st = reserve_species(c, sp, n);
+            picgpu_status st = emit_parcels(c, I, int(i), I.cfg.patch, sp, n, I.cfg.velocity_model,
+                                            I.cfg.eV[j] * 1.602176634e-19 / 1.380649e-23);
             if (st) return st;
-            SpeciesBuf& B = c->sp[sp];
-            pgd::InjectParams P{};
-            P.m = c->dm;
-            P.seed = c->cfg.seed;
-            P.step = uint32_t(c->step_index);
-            P.injector = int(i);
-            P.species = sp;
-            P.model = I.cfg.velocity_model;
-            P.constrain = any_empty;
-            P.mass = S.mass;
-            P.temperature = I.cfg.eV[j] * 1.602176634e-19 / 1.380649e-23;
-            P.n = n;
-            P.n_tri = I.n_tri;
-            P.tri_cum = I.tri_cum;
-            P.tri_cell = I.tri_cell;
-            P.tri_tet = I.tri_tet;
-            P.tri_normal = I.tri_normal;
-            P.tri_fc = I.tri_fc;
-            P.area = I.area;
-            P.patch = I.cfg.patch;
-            const int pk = c->m.patches[I.cfg.patch].p.kind;
-            if (pk == PICGPU_PATCH_FLOATING || pk == PICGPU_PATCH_CIRCUIT) {
-                P.qconv = c->qconv;
-                P.ejected_charge = double(n) * S.charge * S.weight;
-            }
-            P.first = B.n;
-            P.tet = B.tet[B.cur];
-            for (int a = 0; a < 3; ++a) {
-                P.y64[a] = B.y64[B.cur][a];
-                P.u64[a] = B.u64[B.cur][a];
-                P.y32[a] = B.y32[B.cur][a];
-                P.u32[a] = B.u32[B.cur][a];
-            }
-            P.error = c->inj_err;
-            pgd::launch_inject(P, c->stream);
-            c->launches++;
-            // syncVelocityAtBoundary(-0.5) of the new parcels (ParticleEmitter.C:401)
-            if (c->cfg.sync_velocity_at_boundary && S.charge != 0.0 && c->cfg.pusher != PICGPU_PUSHER_NONE) {
-                pgd::MoveParams MP = move_params(c, sp, false);
-                MP.first = int(B.n);
-                MP.n = int(B.n + n);
-                pgd::launch_push_only(MP, c->mixed, -0.5 * dt, grid_for(c, n), c->stream);
-                c->launches++;
-            }
-            B.n += n;
-            B.alive += n;
         }
     }
     // FreeStream::injection (FreeStream.C:126-396): counts per face on the
@@ -863,13 +886,37 @@ picgpu_status inject(picgpu_ctx* c) {
             B.alive += total;
         }
     }
+    // EmissionModels (SM/Helper/Emission): n = J A dt / (w e) + remainder
+    for (size_t i = 0; i < c->emitters.size(); ++i) {
+        Injector& I = c->emitters[i];
+        const int sp = c->cfg.electron_species;
+        const picgpu_species& S = c->cfg.species[sp];
+        const double qe = std::fabs(S.charge);
+        double j = I.em_j;
+        double temperature = I.em.temperature;
+        if (I.em.model == PICGPU_EMISSION_FOWLER_NORDHEIM) {
+            pgd::launch_fowler_nordheim(c->dm, c->Eb, I.em_faces, I.em_n_faces, I.em.work_function, c->em_sum,
+                                        c->stream);
+            c->launches++;
+            CK(cudaMemcpyAsync(&j, c->em_sum, sizeof j, cudaMemcpyDeviceToHost, c->stream));
+            CK(cudaStreamSynchronize(c->stream));
+            temperature = I.em.work_function * qe / 1.380649e-23;
+        }
+        const double ne = j * I.area * dt / (S.weight * qe) + I.em_remainder;
+        const long long n = (long long)ne;
+        I.em_remainder = ne - double(n);
+        if (n <= 0) continue;
+        picgpu_status st = emit_parcels(c, I, PICGPU_MAX_INJECTORS + int(i), I.em.patch, sp, n,
+                                        PICGPU_EMIT_MAXWELLIAN_FLUX, temperature);
+        if (st) return st;
+    }
     CK(cudaGetLastError());
     return PICGPU_OK;
 }
 
 picgpu_status one_step(picgpu_ctx* c, picgpu_step_stats* stats, bool fields) {
     picgpu_status s;
-    if ((!c->injectors.empty() || !c->freestreams.empty()) && (s = inject(c))) return s;
+    if ((!c->injectors.empty() || !c->freestreams.empty() || !c->emitters.empty()) && (s = inject(c))) return s;
     if ((s = zero_accumulators(c))) return s;
     if ((s = move_species(c, false))) return s;
     if ((s = read_counters(c))) return s;
@@ -880,7 +927,7 @@ picgpu_status one_step(picgpu_ctx* c, picgpu_step_stats* stats, bool fields) {
                                               ? "particle velocity reached the speed of light"
                                               : "tracking exceeded track_max_steps for a particle");
     add_counters(c, stats);
-    if (!c->injectors.empty() || !c->freestreams.empty()) {
+    if (!c->injectors.empty() || !c->freestreams.empty() || !c->emitters.empty()) {
         int ie = 0;
         CK(cudaMemcpy(&ie, c->inj_err, sizeof(int), cudaMemcpyDeviceToHost));
         if (ie == 2) return bad(c, PICGPU_INVALID_ARG, "freestream: more than 2^30 parcels on one face in one step");
@@ -1846,6 +1893,65 @@ picgpu_status picgpu_set_freestream(picgpu_ctx* c, int n, const picgpu_freestrea
     return PICGPU_OK;
 }
 
+picgpu_status picgpu_set_emission(picgpu_ctx* c, int n, const picgpu_emission* em) {
+    if (!c || n < 0 || n > PICGPU_MAX_EMISSIONS || (n > 0 && !em)) return PICGPU_INVALID_ARG;
+    if (c->n_cases != 1) return bad(c, PICGPU_NOT_SUPPORTED, "emission: not for ensemble contexts");
+    const int es = c->cfg.electron_species;
+    for (int i = 0; i < n; ++i) {
+        const picgpu_emission& q = em[i];
+        if (es < 0 || es >= c->cfg.n_species || c->cfg.species[es].charge == 0.0)
+            return bad(c, PICGPU_INVALID_ARG, "emission: the config names no charged electron species");
+        if (q.patch < 0 || q.patch >= int(c->m.patches.size()))
+            return bad(c, PICGPU_INVALID_ARG, "emission: no such patch");
+        const int kind = c->m.patches[q.patch].p.kind;
+        if (kind == PICGPU_PATCH_CYCLIC || kind == PICGPU_PATCH_EMPTY)
+            return bad(c, PICGPU_INVALID_ARG, "emission: the patch must not be cyclic or empty");
+        if (q.model != PICGPU_EMISSION_THERMIONIC && q.model != PICGPU_EMISSION_FOWLER_NORDHEIM)
+            return bad(c, PICGPU_INVALID_ARG, "emission: unknown model");
+        if (!(q.work_function > 0.0)) return bad(c, PICGPU_INVALID_ARG, "emission: fnW must be > 0");
+        if (q.model == PICGPU_EMISSION_THERMIONIC && !(q.temperature > 0.0 && q.lambda_r >= 0.0))
+            return bad(c, PICGPU_INVALID_ARG, "emission: thermionic emission needs T > 0 and lambdaR >= 0");
+        if (q.weight > 0.0 && q.weight != c->cfg.species[es].weight)
+            return bad(c, PICGPU_INVALID_ARG,
+                       "emission: nParticle must equal the electron species' weight (one weight per species)");
+    }
+    for (Injector& I : c->emitters) {
+        for (void* p : {(void*)I.tri_cum, (void*)I.tri_cell, (void*)I.tri_tet, (void*)I.tri_normal,
+                        (void*)I.tri_fc, (void*)I.em_faces})
+            dfree(c, p);
+    }
+    c->emitters.clear();
+    for (int i = 0; i < n; ++i) {
+        const picgpu_emission& q = em[i];
+        const pg::PatchTriangles T = pg::patch_triangles(c->m, q.patch);
+        if (T.cell.empty()) return bad(c, PICGPU_INVALID_ARG, "emission: the patch has no boundary faces");
+        c->emitters.emplace_back();
+        Injector& J = c->emitters.back();
+        J.em = q;
+        J.n_tri = int(T.cell.size());
+        J.area = T.area;
+        if (q.model == PICGPU_EMISSION_THERMIONIC)
+            J.em_j = pg::thermionic_current(q.lambda_r, q.temperature, q.work_function,
+                                            std::fabs(c->cfg.species[es].charge));
+        std::vector<int> faces;
+        for (size_t b = 0; b < c->m.bfaces.size(); ++b)
+            if (c->m.bfaces[b].patch == q.patch) faces.push_back(int(b));
+        J.em_n_faces = int(faces.size());
+        picgpu_status st;
+        if ((st = upload(c, &J.tri_cum, T.cum)) || (st = upload(c, &J.tri_cell, T.cell)) ||
+            (st = upload(c, &J.tri_tet, T.tet)) || (st = upload(c, &J.tri_normal, T.normal)) ||
+            (st = upload(c, &J.tri_fc, T.centre)) || (st = upload(c, &J.em_faces, faces)))
+            return st;
+    }
+    picgpu_status st;
+    if (!c->em_sum && (st = dalloc(c, &c->em_sum, 1))) return st;
+    if (!c->inj_err) {
+        if ((st = dalloc(c, &c->inj_err, 1))) return st;
+    }
+    CK(cudaMemset(c->inj_err, 0, sizeof(int)));
+    return PICGPU_OK;
+}
+
 // ------------------------------------------------ initial conditions ----
 // picInitialise (preProcess/picInitialise/picInitialise.C:30-319) for a
 // context; the placement runs on the device (csrc/init.cu).
@@ -2401,7 +2507,7 @@ picgpu_status picgpu_ensemble_case_stats(picgpu_ctx* c, int species, double* out
 }
 
 picgpu_status picgpu_step_graph(picgpu_ctx* c, int nsteps, int steps_per_graph, picgpu_step_stats* stats) {
-    if (c && (!c->injectors.empty() || !c->freestreams.empty()))
+    if (c && (!c->injectors.empty() || !c->freestreams.empty() || !c->emitters.empty()))
         return bad(c, PICGPU_NOT_SUPPORTED, "step_graph: injection runs only in picgpu_step");
     if (c && c->circ.model != PICGPU_CIRCUIT_NONE)
         return bad(c, PICGPU_NOT_SUPPORTED, "step_graph: circuit models run only in picgpu_step");

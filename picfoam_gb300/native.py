@@ -41,6 +41,7 @@ def declare(lib, prefix, ctx_api=True):
     f("initialise", i, [P, C.POINTER(abi.Init), C.POINTER(abi.InitStats)])
     f("set_injection", i, [P, i, C.POINTER(abi.Injection)])
     f("set_freestream", i, [P, i, C.POINTER(abi.FreeStream)])
+    f("set_emission", i, [P, i, C.POINTER(abi.Emission)])
     f("step", i, [P, i, C.POINTER(abi.StepStats)])
     f("move", i, [P, C.POINTER(abi.StepStats)])
     f("solve_poisson", i, [P, F64P, F64P, C.POINTER(abi.StepStats)])

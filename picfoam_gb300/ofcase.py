@@ -12,7 +12,8 @@
   electronTypeId), MaxwellSolver, ParticlePusher, BoundaryModels
   (WallReflectionModel SpecularReflection; FloatingPotential,
   SimpleInjection, FreeStream with `0/boundaryT` / `0/boundaryU`,
-  circuitRLC, IdealVoltageSource, IdealCurrentSource), CollisionModels
+  circuitRLC, IdealVoltageSource, IdealCurrentSource with their Thermionic
+  and FowlerNordheim EmissionModels), CollisionModels
   (CoulombCollisionModel with its pairing and collide models,
   BinaryCollisionModel IsotropicScattering);
 - `system/controlDict` (deltaT, endTime, writeInterval), `system/fvSolution`
@@ -57,6 +58,7 @@ class OFCase:
     init: object = None                  # abi.Init or None
     injections: list = field(default_factory=list)
     freestreams: list = field(default_factory=list)
+    emissions: list = field(default_factory=list)
     delta_t: float = 0.0
     end_time: float = 0.0
     write_interval: float = 0.0
@@ -71,6 +73,8 @@ class OFCase:
             sim.set_injection(self.injections)
         if self.freestreams:
             sim.set_freestream(self.freestreams)
+        if self.emissions:
+            sim.set_emission(self.emissions)
         if initialise and self.init is not None:
             sim.initialise(self.init)
         sim.initialise_fields()
@@ -271,7 +275,7 @@ def load_case(path, allow_unsupported=False, precision=abi.PREC_FP64, seed=1234)
     for name, t in patch_types.items():
         kinds[name] = {"cyclic": abi.PATCH_CYCLIC, "empty": abi.PATCH_EMPTY,
                        "wall": abi.PATCH_WALL}.get(t, abi.PATCH_ABSORB)
-    injections, freestreams = [], []
+    injections, freestreams, emission_models = [], [], []
     boundaryT = _read_optional(os.path.join(zero, "boundaryT")).sub("boundaryField")
     boundaryU = _read_optional(os.path.join(zero, "boundaryU")).sub("boundaryField")
     circuit_model, circuit = None, None
@@ -325,8 +329,8 @@ def load_case(path, allow_unsupported=False, precision=abi.PREC_FP64, seed=1234)
         elif mtype in ("circuitRLC", "IdealVoltageSource", "IdealCurrentSource"):
             if circuit is not None:
                 raise UnsupportedCase("BoundaryModels: more than one circuit model")
-            if coeffs.get("EmissionModels"):
-                bad(f"{mtype}: EmissionModels")
+            for em_type in coeffs.get("EmissionModels", []) or []:
+                emission_models.append((str(em_type), coeffs.sub(f"{em_type}Coeffs")))
             circuit_model = mtype
             circuit = {"coeffs": coeffs, "anode": None, "cathode": None}
             for p in targets:
@@ -399,6 +403,16 @@ def load_case(path, allow_unsupported=False, precision=abi.PREC_FP64, seed=1234)
             eps0 = 1.0 / (4e-7 * math.pi * 299792458.0 ** 2)
             c.sigma = kb.number("circuitGradient", kb.number("gradient", 0.0)) * eps0
 
+    emissions = []
+    for em_type, eco in emission_models:
+        if em_type not in ("Thermionic", "FowlerNordheim"):
+            bad(f"EmissionModel {em_type}")
+            continue
+        model = abi.EMISSION_THERMIONIC if em_type == "Thermionic" else abi.EMISSION_FOWLER_NORDHEIM
+        emissions.append(cases.emission(cfg.circuit.cathode_patch, model, eco.number("fnW"),
+                                        temperature=eco.number("T", 0.0), lambda_r=eco.number("lambdaR", 0.0),
+                                        weight=eco.number("nParticle", -1.0)))
+
     _collisions(props.sub("CollisionModels"), cfg, names, mol, bad)
     if props.word("ParticleMerging", "none") != "none":
         bad(f"ParticleMerging {props.word('ParticleMerging')}")
@@ -407,7 +421,7 @@ def load_case(path, allow_unsupported=False, precision=abi.PREC_FP64, seed=1234)
     return OFCase(path=path, mesh=mesh, cfg=cfg, species=names, side_names=side_names, patches=patch_sides,
                   patch_types=patch_types, phi_bc={k: bfield.sub(k) for k in patch_sides},
                   cell_order=cell_order, init=init, injections=[q for _, q in injections],
-                  freestreams=[q for _, q in freestreams], delta_t=dt, end_time=control.number("endTime", 0.0),
+                  freestreams=[q for _, q in freestreams], emissions=emissions, delta_t=dt, end_time=control.number("endTime", 0.0),
                   write_interval=control.number("writeInterval", 0.0), unsupported=bad.items)
 
 

@@ -147,6 +147,12 @@ class Simulation:
         arr = (abi.FreeStream * max(len(models), 1))(*models)
         self._check(self._fn("set_freestream")(self._h, len(models), arr))
 
+    def set_emission(self, models):
+        """EmissionModels (Thermionic, FowlerNordheim): a list of abi.Emission
+        (empty removes them)."""
+        arr = (abi.Emission * max(len(models), 1))(*models)
+        self._check(self._fn("set_emission")(self._h, len(models), arr))
+
     def initialise(self, init):
         """picInitialise: place the particles of an abi.Init on the device (or
         in the oracle), compute the fields, optionally solve them and apply
