@@ -422,6 +422,23 @@ picgpu_status picgpu_count_particles(picgpu_ctx* ctx, int species, size_t* n);
 picgpu_status picgpu_get_particles(picgpu_ctx* ctx, int species, size_t cap,
                                    int32_t* tet, double* bary, double* U, size_t* n);
 
+/* The whole population as one set of parcels (the cloud's IDLList of
+ * PICParcel, PICParcel.H:182-195, with typeId per parcel): species[i],
+ * tet[i] = 12 cell + local tet, bary[3 i..3 i+2] the coordinates of the
+ * tet's three face points, U[3 i..3 i+2].  Upload replaces every species'
+ * particles (parcels grouped by species in the given order); download
+ * writes species 0 first, then 1, ..., each compacted in storage order. */
+typedef struct {
+    int32_t* species;
+    int32_t* tet;
+    double*  bary;
+    double*  U;
+} picgpu_particles_soa;
+picgpu_status picgpu_upload_particles(picgpu_ctx* ctx, const picgpu_particles_soa* p, size_t n);
+/* cap: room in p; *n: parcels written (on PICGPU_INVALID_ARG with cap too
+ * small, *n is the number needed and nothing is written). */
+picgpu_status picgpu_download_particles(picgpu_ctx* ctx, picgpu_particles_soa* p, size_t cap, size_t* n);
+
 /* Deposit the current particles and solve the fields (what picInitialise does
  * before the first step: calculateFields + solveFields). */
 picgpu_status picgpu_initialise_fields(picgpu_ctx* ctx);
@@ -520,6 +537,8 @@ picgpu_status picgpu_solve_poisson(picgpu_ctx* ctx, const double* rho,
                                    double* phi_inout, picgpu_step_stats* stats);
 
 picgpu_status picgpu_get_field(picgpu_ctx* ctx, int which, double* out, size_t n);
+/* phi (n_cells), cell E (n_cells x 3) and rho (n_cells) at once; any may be NULL. */
+picgpu_status picgpu_get_fields(picgpu_ctx* ctx, double* phi, double* E, double* rho);
 picgpu_status picgpu_set_field(picgpu_ctx* ctx, int which, const double* in, size_t n);
 
 /* Diagnostics (KineticEnergyInfo, FieldEnergyInfo, TemperatureInfo). */

@@ -42,6 +42,11 @@ MAX_BOXES = 8
 MAX_SPECIES = 4
 
 
+class ParticlesSoa(C.Structure):
+    _fields_ = [("species", C.POINTER(C.c_int32)), ("tet", C.POINTER(C.c_int32)),
+                ("bary", C.POINTER(C.c_double)), ("U", C.POINTER(C.c_double))]
+
+
 class Patch(C.Structure):
     _fields_ = [("kind", C.c_int32), ("phi_bc", C.c_int32), ("phi", C.c_double)]
 

@@ -2312,6 +2312,71 @@ picgpu_status picgpu_solve_poisson(picgpu_ctx* c, const double* rho, double* phi
     return s;
 }
 
+picgpu_status picgpu_upload_particles(picgpu_ctx* c, const picgpu_particles_soa* p, size_t n) {
+    if (!c || !p || (n > 0 && (!p->species || !p->tet || !p->bary || !p->U))) return PICGPU_INVALID_ARG;
+    const int ns = c->cfg.n_species;
+    std::vector<std::vector<size_t>> idx(ns);
+    for (size_t i = 0; i < n; ++i) {
+        const int s = p->species[i];
+        if (s < 0 || s >= ns) return bad(c, PICGPU_INVALID_ARG, "upload_particles: species out of range");
+        idx[s].push_back(i);
+    }
+    std::vector<int32_t> tet;
+    std::vector<double> bary, U;
+    for (int s = 0; s < ns; ++s) {
+        const size_t m = idx[s].size();
+        tet.resize(m);
+        bary.resize(3 * m);
+        U.resize(3 * m);
+        for (size_t k = 0; k < m; ++k) {
+            const size_t i = idx[s][k];
+            tet[k] = p->tet[i];
+            for (int a = 0; a < 3; ++a) {
+                bary[3 * k + a] = p->bary[3 * i + a];
+                U[3 * k + a] = p->U[3 * i + a];
+            }
+        }
+        picgpu_status st = picgpu_set_particles(c, s, m, tet.data(), bary.data(), U.data());
+        if (st) return st;
+    }
+    return PICGPU_OK;
+}
+
+picgpu_status picgpu_download_particles(picgpu_ctx* c, picgpu_particles_soa* p, size_t cap, size_t* n) {
+    if (!c || !p || !n) return PICGPU_INVALID_ARG;
+    size_t total = 0;
+    std::vector<size_t> cnt(c->cfg.n_species);
+    for (int s = 0; s < c->cfg.n_species; ++s) {
+        picgpu_status st = picgpu_count_particles(c, s, &cnt[s]);
+        if (st) return st;
+        total += cnt[s];
+    }
+    *n = total;
+    if (total > cap) return bad(c, PICGPU_INVALID_ARG, "download_particles: the buffers are too small");
+    if (total > 0 && (!p->species || !p->tet || !p->bary || !p->U)) return PICGPU_INVALID_ARG;
+    size_t at = 0;
+    for (int s = 0; s < c->cfg.n_species; ++s) {
+        size_t got = 0;
+        picgpu_status st =
+            picgpu_get_particles(c, s, cap - at, p->tet + at, p->bary + 3 * at, p->U + 3 * at, &got);
+        if (st) return st;
+        for (size_t k = 0; k < got; ++k) p->species[at + k] = s;
+        at += got;
+    }
+    *n = at;
+    return PICGPU_OK;
+}
+
+picgpu_status picgpu_get_fields(picgpu_ctx* c, double* phi, double* E, double* rho) {
+    if (!c) return PICGPU_INVALID_ARG;
+    const size_t nc = c->m.n_cells;
+    picgpu_status st;
+    if (phi && (st = picgpu_get_field(c, PICGPU_FIELD_PHI, phi, nc))) return st;
+    if (E && (st = picgpu_get_field(c, PICGPU_FIELD_E_CELL, E, 3 * nc))) return st;
+    if (rho && (st = picgpu_get_field(c, PICGPU_FIELD_RHO, rho, nc))) return st;
+    return PICGPU_OK;
+}
+
 picgpu_status picgpu_get_field(picgpu_ctx* c, int which, double* out, size_t n) {
     if (!c || !out) return PICGPU_INVALID_ARG;
     const double* src = nullptr;

@@ -53,7 +53,7 @@ MIRRORS = {
     "Multigrid": "picgpu_multigrid", "Config": "picgpu_config", "StepStats": "picgpu_step_stats",
     "MeshInfo": "picgpu_mesh_info", "Diagnostics": "picgpu_diagnostics",
     "Binary": "picgpu_binary", "Circuit": "picgpu_circuit", "FreeStream": "picgpu_freestream",
-    "Injection": "picgpu_injection", "Emission": "picgpu_emission",
+    "Injection": "picgpu_injection", "Emission": "picgpu_emission", "ParticlesSoa": "picgpu_particles_soa",
 }
 
 
