@@ -16,8 +16,10 @@
 // and the per-step counters.
 #include <cuda_runtime.h>
 
+#include <condition_variable>
 #include <cstdio>
 #include <cstring>
+#include <mutex>
 #include <memory>
 #include <string>
 #include <thread>
@@ -65,21 +67,95 @@ struct SpeciesBuf {
 // two slots: host threads copy chunk k into a slot while the DMA engine moves
 // chunk k - 1, so the copy runs at the host's memcpy bandwidth over all its
 // cores instead of through the driver's single bounce buffer.
+// Host-side copy workers of the staging ring: started once with the
+// context, they wait on a condition variable; a copy splits into one segment
+// per worker plus one for the calling thread.
+class CopyPool {
+  public:
+    void start(unsigned workers) {
+        for (unsigned k = 0; k < workers; ++k) th_.emplace_back([this, k] { run(k + 1); });
+    }
+    void stop() {
+        {
+            std::lock_guard<std::mutex> g(m_);
+            quit_ = true;
+        }
+        cv_.notify_all();
+        for (auto& t : th_) t.join();
+        th_.clear();
+        quit_ = false;
+    }
+    void copy(char* dst, const char* src, size_t n) {
+        const unsigned parts = unsigned(th_.size()) + 1;
+        if (th_.empty() || n < (size_t(4) << 20)) {
+            std::memcpy(dst, src, n);
+            return;
+        }
+        {
+            std::lock_guard<std::mutex> g(m_);
+            dst_ = dst;
+            src_ = src;
+            n_ = n;
+            part_ = (n + parts - 1) / parts;
+            pending_ = unsigned(th_.size());
+            ++gen_;
+        }
+        cv_.notify_all();
+        segment(0);
+        std::unique_lock<std::mutex> g(m_);
+        done_.wait(g, [this] { return pending_ == 0; });
+    }
+
+  private:
+    void segment(unsigned k) {
+        const size_t a = k * part_, b = std::min(n_, a + part_);
+        if (a < b) std::memcpy(dst_ + a, src_ + a, b - a);
+    }
+    void run(unsigned k) {
+        unsigned seen = 0;
+        for (;;) {
+            {
+                std::unique_lock<std::mutex> g(m_);
+                cv_.wait(g, [&] { return quit_ || gen_ != seen; });
+                if (quit_) return;
+                seen = gen_;
+            }
+            segment(k);
+            {
+                std::lock_guard<std::mutex> g(m_);
+                if (--pending_ == 0) done_.notify_all();
+            }
+        }
+    }
+    std::vector<std::thread> th_;
+    std::mutex m_;
+    std::condition_variable cv_, done_;
+    char* dst_ = nullptr;
+    const char* src_ = nullptr;
+    size_t n_ = 0, part_ = 0;
+    unsigned gen_ = 0, pending_ = 0;
+    bool quit_ = false;
+};
+
 struct HostStager {
     static constexpr size_t kSlot = size_t(64) << 20;
     char* pinned = nullptr;
     cudaEvent_t ev[2] = {nullptr, nullptr};
     bool ready = false;
+    CopyPool pool;
 
     bool init() {
         if (ready) return true;
         if (cudaMallocHost(&pinned, 2 * kSlot) != cudaSuccess) return false;
         for (int k = 0; k < 2; ++k)
             if (cudaEventCreateWithFlags(&ev[k], cudaEventDisableTiming) != cudaSuccess) return false;
+        const unsigned t = std::max(1u, std::min(std::thread::hardware_concurrency(), 16u));
+        pool.start(t - 1);
         ready = true;
         return true;
     }
     void release() {
+        if (ready) pool.stop();
         if (pinned) cudaFreeHost(pinned);
         for (auto& e : ev)
             if (e) cudaEventDestroy(e);
@@ -87,22 +163,7 @@ struct HostStager {
         ev[0] = ev[1] = nullptr;
         ready = false;
     }
-    static void par_copy(char* dst, const char* src, size_t n) {
-        unsigned t = std::thread::hardware_concurrency();
-        t = std::max(1u, std::min(t, 16u));
-        if (n < (size_t(4) << 20) || t == 1) {
-            std::memcpy(dst, src, n);
-            return;
-        }
-        std::vector<std::thread> th;
-        const size_t part = (n + t - 1) / t;
-        for (unsigned k = 0; k < t; ++k) {
-            const size_t a = k * part, b = std::min(n, a + part);
-            if (a >= b) break;
-            th.emplace_back([=] { std::memcpy(dst + a, src + a, b - a); });
-        }
-        for (auto& x : th) x.join();
-    }
+    void par_copy(char* dst, const char* src, size_t n) { pool.copy(dst, src, n); }
     cudaError_t upload(void* dev, const void* host, size_t n, cudaStream_t s) {
         if (n < (size_t(8) << 20) || !init()) return cudaMemcpyAsync(dev, host, n, cudaMemcpyHostToDevice, s);
         const char* src = static_cast<const char*>(host);
