@@ -166,6 +166,15 @@ typedef struct {
     const double* xs_elastic;  /* [n_xs] m^2 */
     const double* xs_excitation;
     const double* xs_ionization;
+    /* Collisions with neutral parcels (performCollisions,
+     * ElectronNeutralCollisionModel.C:833-1009): NTC candidates
+     * eC nC w_max (sigma c_R)_max dt / V per cell with the neutral_species
+     * parcels, before the background-gas collisions (which need
+     * gas_density > 0).  The cross sections above are the neutral species'. */
+    int32_t neutral_parcels;        /* 1: collide with the parcels of neutral_species */
+    int32_t neutral_species;        /* species of the neutral parcels (charge 0) */
+    int32_t keep_neutrals;          /* deleteNeutral false: an ionised neutral parcel stays */
+    int32_t keep_neutral_velocity;  /* updateNeutralVelocity false: the neutral keeps its velocity */
 } picgpu_mcc;
 
 /* Null-collision MCC of ions against the background gas

@@ -159,6 +159,7 @@ struct Oracle {
     long long step_index = 0;
     // collision state
     std::vector<double> svmax, remainder;
+    std::vector<double> psvmax, premainder;  // electron - neutral parcels
     std::vector<double> isvmax, iremainder;  // ion-neutral
     int last_pcg_iter = 0;
     double last_res_l2 = 0, last_res_of = 0;
@@ -1117,6 +1118,123 @@ void mcc_background(Oracle& o, std::vector<std::vector<int>>& occ, picgpu_step_s
     }
 }
 
+// ElectronNeutralCollisionModel::performCollisions
+// (ElectronNeutralCollisionModel.C:833-1009): collisions with the neutral
+// parcels of the cell (NTC candidates eC nC w_max (sigma_T c_R)_max dt / V,
+// a random neutral and a random electron each), with the events of the
+// background model and the parcel as partner (:489-645); an ionised neutral
+// is deleted unless deleteNeutral is off.
+void mcc_parcels(Oracle& o, std::vector<std::vector<std::vector<int>>>& occ, picgpu_step_stats* st) {
+    const picgpu_mcc& mc = o.cfg.mcc;
+    const int es = o.cfg.electron_species, ns = mc.neutral_species;
+    const double me = o.cfg.species[es].mass, mn = o.cfg.species[ns].mass;
+    const double wE = o.cfg.species[es].weight, wN = o.cfg.species[ns].weight;
+    const double wmax = std::max(wE, wN);
+    const double dt = o.cfg.dt;
+    const bool update_neutral = !mc.keep_neutral_velocity, delete_neutral = !mc.keep_neutrals;
+    auto& el = o.cloud[es];
+    auto& neu = o.cloud[ns];
+    std::vector<Parcel> new_e, new_i;
+    long long cand = 0, nel = 0, nex = 0, niz = 0;
+    for (int c = 0; c < o.m.n_cells; ++c) {
+        const std::vector<int>& elist = occ[es][c];
+        std::vector<int>& nlist = occ[ns][c];
+        const long eC = long(elist.size());
+        long nC = long(nlist.size());
+        const double sv = o.psvmax[c];
+        if (!(sv > 0.0) || nC == 0 || eC == 0) continue;
+        const double selected = o.premainder[c] + double(int(eC) * int(nC)) * wmax * sv * dt / o.m.vol[c];
+        const long nCand = long(selected);
+        o.premainder[c] = selected - double(nCand);
+        cand += nCand;
+        if (nCand == 0) continue;
+        ocoll::Philox r(o.cfg.seed, ocoll::kStreamMcc | 1u, uint32_t(c), uint32_t(o.step_index));
+        for (long i = 0; i < nCand; ++i) {
+            long jn = long(r.uniform() * double(nC));
+            if (jn >= nC) jn = nC - 1;
+            long je = long(r.uniform() * double(eC));
+            if (je >= eC) je = eC - 1;
+            Parcel& n = neu[nlist[jn]];
+            Parcel& e = el[elist[je]];
+            V3 Un = n.U;
+            const double cR = magv(sub(e.U, Un));
+            const double gamma = 1.0 / std::sqrt(1.0 - (cR * cR) / (kC * kC));
+            double eV = (gamma - 1.0) * me * kC * kC / ocoll::kEcharge;
+            const double Qel = ocoll::interp_xs(eV, o.xs.e, o.xs.el);
+            const double Qex = ocoll::interp_xs(eV, o.xs.e, o.xs.ex);
+            const double Qiz = ocoll::interp_xs(eV, o.xs.e, o.xs.iz);
+            const double Qt = Qel + Qex + Qiz;
+            if (Qt * cR > o.psvmax[c]) o.psvmax[c] = Qt * cR;
+            const double R = r.uniform();
+            if (R <= Qel * cR / sv) {
+                nel++;
+                electron_scatter(o, eV, e.U, Un, me, mn, r);
+                if (update_neutral) n.U = Un;
+            } else if (eV >= mc.ex_threshold && R <= (Qel + Qex) * cR / sv) {
+                nex++;
+                e.U = smul(std::sqrt(1.0 - mc.ex_threshold / eV), e.U);
+                eV -= mc.ex_threshold;
+                electron_scatter(o, eV, e.U, Un, me, mn, r);
+                if (update_neutral) n.U = Un;
+            } else if (eV >= mc.iz_threshold && R <= Qt * cR / sv) {
+                const double th = mc.iz_threshold;
+                const double E0 = 2.0 - 100.0 / (eV + 10.0);
+                const double E1 = (eV - th) / 2.0 - E0;
+                const double alpha = 10.3;
+                const double Ep = E0 + alpha * std::tan(r.uniform() * (std::atan(E1 / alpha) + std::atan(E0 / alpha)) -
+                                                        std::atan(E0 / alpha));
+                const V3 preUe = e.U;
+                const V3 preUn = Un;
+                e.U = smul(std::sqrt(1.0 - (th + Ep) / eV), e.U);
+                eV -= (th + Ep);
+                const double wEwN = wE / wN, wNwE = 1.0 / wEwN;
+                electron_scatter(o, eV, e.U, Un, me, mn, r);
+                const double rndU = r.uniform();
+                bool created = false;
+                if (rndU <= wEwN && mc.create_ion) {
+                    Parcel ion = n;          // at the neutral's position, with its scattered velocity
+                    ion.U = Un;
+                    new_i.push_back(ion);
+                    created = true;
+                }
+                if (rndU > wNwE) e.U = preUe;
+                if (rndU <= wEwN && mc.create_electron) {
+                    Parcel ne = e;
+                    const double sp = std::sqrt(2.0 * Ep * ocoll::kEcharge / me);
+                    ne.U = smul(sp, sdiv(preUe, magv(preUe)));
+                    V3 un2 = preUn;
+                    electron_scatter(o, Ep, ne.U, un2, me, mn, r);
+                    new_e.push_back(ne);
+                }
+                if (update_neutral) n.U = Un;
+                if (created) {
+                    niz++;
+                    if (delete_neutral) {
+                        n.alive = false;
+                        nlist.erase(nlist.begin() + jn);
+                        --nC;
+                        if (nC < 1) break;
+                    }
+                }
+            }
+        }
+    }
+    // deleted neutrals leave the cloud in order
+    size_t w = 0;
+    for (size_t k = 0; k < neu.size(); ++k)
+        if (neu[k].alive) neu[w++] = neu[k];
+    neu.resize(w);
+    for (auto& p : new_e) el.push_back(p);
+    if (mc.ion_species >= 0 && mc.create_ion)
+        for (auto& p : new_i) o.cloud[mc.ion_species].push_back(p);
+    if (st) {
+        st->mcc_candidates += cand;
+        st->mcc_elastic += nel;
+        st->mcc_excitation += nex;
+        st->mcc_ionization += niz;
+    }
+}
+
 // IonNeutralCollisionModel::performBackgroundCollisions
 // (IonNeutralCollisionModel.C:453-577): IsotropicScattering elastic
 // (IonIsotropicScattering.C:103-143) or charge exchange (:419-426).
@@ -1728,6 +1846,7 @@ void collisions(Oracle& o, picgpu_step_stats* st) {
     for (int s = 0; s < o.cfg.n_species; ++s)
         for (size_t i = 0; i < o.cloud[s].size(); ++i) occ[s][o.cloud[s][i].cell].push_back(int(i));
     if (o.cfg.coulomb.enabled) coulomb_pairs(o, occ, st);
+    if (o.cfg.mcc.enabled && o.cfg.mcc.neutral_parcels) mcc_parcels(o, occ, st);
     if (o.cfg.mcc.enabled) mcc_background(o, occ[o.cfg.electron_species], st);
     if (o.cfg.ion_mcc.enabled) ion_mcc_background(o, occ[o.cfg.ion_mcc.ion_species], st);
     if (o.cfg.binary.enabled) binary_collisions(o, occ, st);
@@ -2439,6 +2558,23 @@ int oracle_create(const picgpu_mesh_desc* mesh, const picgpu_config* cfg, int nt
     if (cfg->mcc.enabled) {
         std::string e = ocoll::init_mcc(o.cfg, o.xs, m.n_cells, o.svmax, o.remainder);
         if (!e.empty()) { o.err = e; *out = c; return PICGPU_INVALID_ARG; }
+        if (cfg->mcc.neutral_parcels) {
+            const int ns = cfg->mcc.neutral_species;
+            if (ns < 0 || ns >= cfg->n_species || cfg->species[ns].charge != 0.0 ||
+                cfg->species[ns].weight != cfg->species[cfg->electron_species].weight ||
+                (cfg->mcc.create_ion && cfg->species[ns].weight != cfg->species[cfg->mcc.ion_species].weight) ||
+                cfg->binary.enabled) {
+                o.err = "mcc: unsupported neutral-parcel set-up";
+                *out = c;
+                return PICGPU_INVALID_ARG;
+            }
+            o.psvmax = o.svmax;
+            o.premainder.resize(m.n_cells);
+            for (int k = 0; k < m.n_cells; ++k) {
+                ocoll::Philox r(cfg->seed, ocoll::kStreamRemainder | 1u, uint32_t(k), 0u);
+                o.premainder[k] = r.uniform();
+            }
+        }
     }
     o.isvmax.assign(m.n_cells, 0.0);
     o.iremainder.assign(m.n_cells, 0.0);

@@ -84,6 +84,8 @@ class Mcc(C.Structure):
         ("find_energy_step", C.c_double),
         ("xs_energy", C.POINTER(C.c_double)), ("xs_elastic", C.POINTER(C.c_double)),
         ("xs_excitation", C.POINTER(C.c_double)), ("xs_ionization", C.POINTER(C.c_double)),
+        ("neutral_parcels", C.c_int32), ("neutral_species", C.c_int32), ("keep_neutrals", C.c_int32),
+        ("keep_neutral_velocity", C.c_int32),
     ]
 
 

@@ -262,6 +262,60 @@ def electron_swarm(nx=32, ny=32, nz=256, N=10_000_000, Ez=1e4, gas_density=1e21,
                 dict(dt=dt, E_over_N_Td=Ez / gas_density * 1e21, N=N))
 
 
+def neutral_parcel_ionization(n_cells=(4, 4, 4), L=1e-3, per_cell=(20, 40), T_e_eV=100.0, T_n=300.0, n_n=1e20,
+                              sigma_iz=3.43943e-20, threshold=15.76, dt=1e-11, seed=1234, precision=abi.PREC_FP64,
+                              keep_neutrals=False, keep_neutral_velocity=False, exact_max=True):
+    """The ionization tutorial's collision set-up: electrons, neutral Ar
+    parcels and Ar+ with equal weights in a periodic box, MaxwellSolver
+    none, electron-neutral MCC against the parcels (performCollisions) with
+    a FixedValue ionisation cross section (threshold 15.76 eV), no elastic or
+    excitation.  per_cell = (electrons, neutrals); electrons monoenergetic at
+    T_e_eV (isotropic directions).  exact_max starts (sigma c_R)_max at
+    sigma_iz times the electron speed."""
+    sides = [patch(abi.PATCH_CYCLIC) for _ in range(6)]
+    mesh = block_mesh(n_cells, (L,) * 3, sides)
+    n_c = n_cells[0] * n_cells[1] * n_cells[2]
+    w = n_n * L ** 3 / (n_c * per_cell[1])
+    cfg = base_config(dt, [(M_E, -E_CHARGE, w, True), (M_AR, 0.0, w, True), (M_AR, E_CHARGE, w, True)],
+                      maxwell=abi.MAXWELL_NONE, precision=precision, seed=seed)
+    e = np.array([0.0, 1e5])
+    zero = np.zeros(2)
+    iz = np.full(2, sigma_iz)
+    arrs = [np.ascontiguousarray(a, dtype=np.float64) for a in (e, zero, zero, iz)]
+    import ctypes as C
+    mc = cfg.mcc
+    mc.enabled = 1
+    mc.scatter = 1                      # RelativisticElectronNeutral, as the tutorial
+    mc.create_electron = 1
+    mc.create_ion = 1
+    mc.ion_species = 2
+    mc.n_xs = 2
+    mc.gas_density = 0.0                # BackgroundGasModel none
+    mc.gas_mass = M_AR
+    mc.gas_weight = w
+    mc.ex_threshold = 11.5
+    mc.iz_threshold = threshold
+    v_e = math.sqrt(2 * E_CHARGE * T_e_eV / M_E)
+    mc.sigma_v_max_init = sigma_iz * v_e * 1.01 if exact_max else 0.0
+    mc.find_max_energy = 2 * T_e_eV
+    mc.find_energy_step = 0.01
+    mc.xs_energy, mc.xs_elastic, mc.xs_excitation, mc.xs_ionization = [
+        a.ctypes.data_as(C.POINTER(C.c_double)) for a in arrs]
+    mc.neutral_parcels = 1
+    mc.neutral_species = 1
+    mc.keep_neutrals = 1 if keep_neutrals else 0
+    mc.keep_neutral_velocity = 1 if keep_neutral_velocity else 0
+    rng = np.random.Generator(np.random.Philox(seed))
+    te, be = uniform_in_cells(rng, np.arange(n_c), per_cell[0])
+    d = rng.standard_normal((len(te), 3))
+    Ue = v_e * d / np.linalg.norm(d, axis=1)[:, None]
+    tn, bn = uniform_in_cells(rng, np.arange(n_c), per_cell[1])
+    Un = rng.standard_normal((len(tn), 3)) * math.sqrt(K_B * T_n / M_AR)
+    parts = {0: (te, be, Ue), 1: (tn, bn, Un), 2: (np.zeros(0, np.int32), np.zeros((0, 3)), np.zeros((0, 3)))}
+    return Case("neutral_parcel_ionization", mesh, cfg, parts, arrs,
+                dict(w=w, v_e=v_e, n_n=n_n, V=L ** 3, N_e=len(te), N_n=len(tn), n_c=n_c))
+
+
 def set_coulomb(cfg, pairing=abi.PAIRING_NANBU_YONEMURA, collide=abi.COLLIDE_NANBU, coulomb_log=15.0,
                 calculate_bmin=True, debye_drift=True, weight_correction=0, allow_intra=True):
     """CoulombCollisionModel dictionary: coulomb_log 0 computes the logarithm

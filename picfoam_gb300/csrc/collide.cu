@@ -450,6 +450,8 @@ __global__ void mcc_kernel(MccParams M, DSpecies el, Secondary* __restrict__ sta
                 sc.tet = el.tet[pi];
                 if (el.y64[0]) { sc.y[0] = el.y64[0][pi]; sc.y[1] = el.y64[1][pi]; sc.y[2] = el.y64[2][pi]; }
                 else { sc.y[0] = el.y32[0][pi]; sc.y[1] = el.y32[1][pi]; sc.y[2] = el.y32[2][pi]; }
+                sc.tet_i = sc.tet;
+                for (int a = 0; a < 3; ++a) sc.y_i[a] = sc.y[a];
             }
             if (room) stage[base + i] = sc;
             continue;
@@ -461,6 +463,174 @@ __global__ void mcc_kernel(MccParams M, DSpecies el, Secondary* __restrict__ sta
     if (nel) atomicAdd(M.counts + 1, nel);
     if (nex) atomicAdd(M.counts + 2, nex);
     if (niz) atomicAdd(M.counts + 3, niz);
+}
+
+// ---------------------------------------------- neutral-parcel MCC -----
+// ElectronNeutralCollisionModel::performCollisions
+// (ElectronNeutralCollisionModel.C:833-1009): per cell, NTC candidates
+// eC nC w_max (sigma_T c_R)_max dt / V, a random neutral parcel and a random
+// electron per candidate, the running maximum updated, the events of the
+// background model with the parcel's velocity as the partner
+// (:489-645: the neutral takes its recoil unless updateNeutralVelocity is
+// off; an ion is created at the neutral's position with its velocity, and
+// the ionised neutral is deleted unless deleteNeutral is off).
+struct MccParcelParams {
+    int n_cells;
+    const int* e_start;   // n_cells + 1
+    const int* e_idx;
+    const int* n_start;   // neutral species, n_cells + 1
+    int* n_idx;           // its per-cell lists (deleted parcels are erased in place)
+    double* svmax;
+    double* rem;
+    const double* vol;
+    const double* xs;     // 4 x n_xs
+    int n_xs;
+    double me, mn, dt, wE, wN, wmax;
+    double ex_th, iz_th;
+    int create_e, create_i, relativistic, update_neutral, delete_neutral;
+    uint64_t seed;
+    uint32_t step;
+    const int* cand_off;
+    long stage_cap;
+    int* overflow;
+    unsigned long long* counts;
+};
+
+__device__ __forceinline__ long parcel_candidates(const MccParcelParams& M, int c, double* sel) {
+    const int eC = M.e_start[c + 1] - M.e_start[c];
+    const int nC = M.n_start[c + 1] - M.n_start[c];
+    const double sv = M.svmax[c];
+    if (!(sv > 0.0) || nC == 0 || eC == 0) return 0;
+    *sel = M.rem[c] + double(eC * nC) * M.wmax * sv * M.dt / M.vol[c];
+    return long(*sel);
+}
+
+__global__ void mcc_parcel_count_kernel(MccParcelParams M, int* __restrict__ ncand) {
+    const int c = blockIdx.x * blockDim.x + threadIdx.x;
+    if (c >= M.n_cells) return;
+    double sel = 0.0;
+    ncand[c] = int(parcel_candidates(M, c, &sel));
+}
+
+template <class R>
+__device__ __forceinline__ void stage_pos(const DSpecies& p, int i, int32_t& tet, double* y) {
+    tet = p.tet[i];
+    if (p.y64[0]) { y[0] = p.y64[0][i]; y[1] = p.y64[1][i]; y[2] = p.y64[2][i]; }
+    else { y[0] = p.y32[0][i]; y[1] = p.y32[1][i]; y[2] = p.y32[2][i]; }
+}
+
+template <class R>
+__global__ void mcc_parcel_kernel(MccParcelParams M, DSpecies el, DSpecies neu, Secondary* __restrict__ stage) {
+    const int c = blockIdx.x * blockDim.x + threadIdx.x;
+    if (c >= M.n_cells) return;
+    double selected = 0.0;
+    const long nCand = parcel_candidates(M, c, &selected);
+    const int eC = M.e_start[c + 1] - M.e_start[c];
+    int nC = M.n_start[c + 1] - M.n_start[c];
+    const double sv = M.svmax[c];
+    if (!(sv > 0.0) || nC == 0 || eC == 0) return;
+    M.rem[c] = selected - double(nCand);
+    if (nCand == 0) return;
+    const int* elist = M.e_idx + M.e_start[c];
+    int* nlist = M.n_idx + M.n_start[c];
+    const double* E = M.xs;
+    const double* EL = M.xs + M.n_xs;
+    const double* EX = M.xs + 2 * M.n_xs;
+    const double* IZ = M.xs + 3 * M.n_xs;
+    Rng r(M.seed, kStreamMcc | 1u, uint32_t(c), M.step);
+    unsigned long long nel = 0, nex = 0, niz = 0, ndel = 0, ncand = 0;
+    const int base = M.cand_off[c];
+    const bool room = long(base) + nCand <= M.stage_cap;
+    if (!room) atomicExch(M.overflow, 1);
+    long i = 0;
+    for (; i < nCand; ++i) {
+        ++ncand;
+        long jn = long(r.uniform() * double(nC));
+        if (jn >= nC) jn = nC - 1;
+        long je = long(r.uniform() * double(eC));
+        if (je >= eC) je = eC - 1;
+        const int pn = nlist[jn], pe = elist[je];
+        V3d Ue = Vel<R>::get(el, pe);
+        V3d Un = Vel<R>::get(neu, pn);
+        const V3d d = {Ue.x - Un.x, Ue.y - Un.y, Ue.z - Un.z};
+        const double cR = magd(d);
+        const double gamma = 1.0 / sqrt(1.0 - (cR * cR) / (kC * kC));
+        double eV = (gamma - 1.0) * M.me * kC * kC / kEch;
+        const double Qel = interp_xs(eV, E, EL, M.n_xs);
+        const double Qex = interp_xs(eV, E, EX, M.n_xs);
+        const double Qiz = interp_xs(eV, E, IZ, M.n_xs);
+        const double Qt = Qel + Qex + Qiz;
+        if (Qt * cR > M.svmax[c]) M.svmax[c] = Qt * cR;
+        const double rndU = r.uniform();
+        Secondary sc{};
+        if (rndU <= Qel * cR / sv) {
+            nel++;
+            electron_scatter(M.relativistic, eV, Ue, Un, M.me, M.mn, r);
+            Vel<R>::put(el, pe, Ue);
+            if (M.update_neutral) Vel<R>::put(neu, pn, Un);
+        } else if (eV >= M.ex_th && rndU <= (Qel + Qex) * cR / sv) {
+            nex++;
+            const double f = sqrt(1.0 - M.ex_th / eV);
+            Ue = {f * Ue.x, f * Ue.y, f * Ue.z};
+            eV -= M.ex_th;
+            electron_scatter(M.relativistic, eV, Ue, Un, M.me, M.mn, r);
+            Vel<R>::put(el, pe, Ue);
+            if (M.update_neutral) Vel<R>::put(neu, pn, Un);
+        } else if (eV >= M.iz_th && rndU <= Qt * cR / sv) {
+            const double th = M.iz_th;
+            const double E0 = 2.0 - 100.0 / (eV + 10.0);
+            const double E1 = (eV - th) / 2.0 - E0;
+            const double alpha = 10.3;
+            const double Ep = E0 + alpha * tan(r.uniform() * (atan(E1 / alpha) + atan(E0 / alpha)) - atan(E0 / alpha));
+            const V3d preUe = Ue;
+            const V3d preUn = Un;
+            const double f = sqrt(1.0 - (th + Ep) / eV);
+            Ue = {f * Ue.x, f * Ue.y, f * Ue.z};
+            eV -= (th + Ep);
+            const double wEwN = M.wE / M.wN, wNwE = 1.0 / wEwN;
+            electron_scatter(M.relativistic, eV, Ue, Un, M.me, M.mn, r);
+            const double rndU2 = r.uniform();
+            bool created = false;
+            if (rndU2 <= wEwN && M.create_i) {
+                sc.flag |= 2;
+                sc.ui[0] = Un.x; sc.ui[1] = Un.y; sc.ui[2] = Un.z;
+                stage_pos<R>(neu, pn, sc.tet_i, sc.y_i);
+                created = true;
+            }
+            if (rndU2 > wNwE) Ue = preUe;
+            Vel<R>::put(el, pe, Ue);
+            if (rndU2 <= wEwN && M.create_e) {
+                const double sp = sqrt(2.0 * Ep * kEch / M.me);
+                const double mp = magd(preUe);
+                V3d ne = {sp * (preUe.x / mp), sp * (preUe.y / mp), sp * (preUe.z / mp)};
+                V3d un2 = preUn;
+                electron_scatter(M.relativistic, Ep, ne, un2, M.me, M.mn, r);
+                sc.flag |= 1;
+                sc.ue[0] = ne.x; sc.ue[1] = ne.y; sc.ue[2] = ne.z;
+                stage_pos<R>(el, pe, sc.tet, sc.y);
+            }
+            if (M.update_neutral) Vel<R>::put(neu, pn, Un);
+            if (created) {
+                niz++;
+                if (M.delete_neutral) {
+                    neu.tet[pn] = -1;
+                    for (long k = jn; k + 1 < nC; ++k) nlist[k] = nlist[k + 1];
+                    --nC;
+                    ++ndel;
+                }
+            }
+        }
+        if (room) stage[base + i] = sc;
+        if (nC < 1) { ++i; break; }
+    }
+    if (room)
+        for (; i < nCand; ++i) stage[base + i].flag = 0;   // candidates left after the last neutral went
+    (void)ncand;
+    atomicAdd(M.counts + 0, (unsigned long long)nCand);
+    if (nel) atomicAdd(M.counts + 1, nel);
+    if (nex) atomicAdd(M.counts + 2, nex);
+    if (niz) atomicAdd(M.counts + 3, niz);
+    if (ndel) atomicAdd(M.counts + 12, ndel);
 }
 
 // n_dev (optional): the staged count is read on the device; slots from it
@@ -487,12 +657,13 @@ __global__ void stage_append_kernel(const Secondary* __restrict__ stage, int n, 
     }
     const int k = int(kk);
     const Secondary& s = stage[i];
-    dst.tet[k] = s.tet;
+    dst.tet[k] = bit == 1 ? s.tet : s.tet_i;
     const double* u = bit == 1 ? s.ue : s.ui;
+    const double* y = bit == 1 ? s.y : s.y_i;
     if (dst.y64[0]) {
-        for (int a = 0; a < 3; ++a) { dst.y64[a][k] = s.y[a]; dst.u64[a][k] = u[a]; }
+        for (int a = 0; a < 3; ++a) { dst.y64[a][k] = y[a]; dst.u64[a][k] = u[a]; }
     } else {
-        for (int a = 0; a < 3; ++a) { dst.y32[a][k] = float(s.y[a]); dst.u32[a][k] = float(u[a]); }
+        for (int a = 0; a < 3; ++a) { dst.y32[a][k] = float(y[a]); dst.u32[a][k] = float(u[a]); }
     }
 }
 
@@ -1330,6 +1501,29 @@ int collide_init(CollideState& st, const picgpu_config& cfg, const DMesh& m, cud
             *msg = "MCC state: device allocation failed";
             return PICGPU_OOM;
         }
+        if (mc.neutral_parcels) {
+            const int ns = mc.neutral_species;
+            if (ns < 0 || ns >= cfg.n_species || cfg.species[ns].charge != 0.0) {
+                *msg = "MCC: neutral_species must name a species of charge 0";
+                return PICGPU_INVALID_ARG;
+            }
+            const double wn = cfg.species[ns].weight;
+            if (wn != cfg.species[cfg.electron_species].weight ||
+                (mc.create_ion && wn != cfg.species[mc.ion_species].weight)) {
+                *msg = "MCC: neutral parcels need the electron and ion weights of the neutral species";
+                return PICGPU_NOT_SUPPORTED;
+            }
+            if (cfg.binary.enabled) {
+                *msg = "MCC: neutral-parcel collisions together with BinaryCollisionModel are not supported";
+                return PICGPU_NOT_SUPPORTED;
+            }
+            // the same start value; remainders from their own stream
+            double* xs_unused = nullptr;
+            const int e2 = upload_mcc(&st.psvmax, &st.premainder, &xs_unused, xs, sv, cfg.seed, kStreamRemainder | 1u,
+                                      nc, s, msg);
+            if (e2) return e2;
+            cudaFree(xs_unused);
+        }
     }
     if (cfg.ion_mcc.enabled) {
         const picgpu_ion_mcc& im = cfg.ion_mcc;
@@ -1711,6 +1905,111 @@ int launch_binary(CollideState& st, const CollideArgs& a, std::string* msg, int6
     return PICGPU_OK;
 }
 
+// Staging room for `total` candidates.
+int ensure_stage(CollideState& st, long total, std::string* msg) {
+    if (st.stage_cap >= total) return PICGPU_OK;
+    if (st.stage) cudaFree(st.stage);
+    if (st.flags) cudaFree(st.flags);
+    if (st.pos) cudaFree(st.pos);
+    if (st.stage_tmp) cudaFree(st.stage_tmp);
+    st.stage = nullptr;
+    st.flags = st.pos = st.stage_tmp = nullptr;
+    const long cap = std::max<long>(total + total / 2, 4096);
+    if (dmalloc(&st.stage, cap) || dmalloc(&st.flags, cap + 1) || dmalloc(&st.pos, cap + 2) ||
+        dmalloc(&st.stage_tmp, cap / 1024 + 8)) {
+        *msg = "MCC staging: device allocation failed";
+        return PICGPU_OOM;
+    }
+    st.stage_cap = cap;
+    return PICGPU_OK;
+}
+
+// Staged secondaries appended to the electron (bit 1) and ion (bit 2)
+// species in (cell, candidate) order.
+int append_stage(CollideState& st, const CollideArgs& a, int total, long newn[], std::string* msg,
+                 int64_t* launches) {
+    const picgpu_mcc& mc = a.cfg->mcc;
+    const int es = a.cfg->electron_species;
+    for (int bit = 1; bit <= 2; bit <<= 1) {
+        const int s = bit == 1 ? es : mc.ion_species;
+        if (s < 0 || (bit == 1 && !mc.create_electron) || (bit == 2 && !mc.create_ion)) continue;
+        stage_flags_kernel<<<(total + 255) / 256, 256, 0, a.stream>>>(st.stage, total, bit, st.flags);
+        exclusive_scan(st.flags, st.pos, total, st.stage_tmp, a.stream, launches);
+        int add = 0;
+        cudaMemcpyAsync(&add, st.pos + total, sizeof(int), cudaMemcpyDeviceToHost, a.stream);
+        if (cudaStreamSynchronize(a.stream) != cudaSuccess) { *msg = "MCC: append failed"; return PICGPU_CUDA_ERROR; }
+        *launches += 1;
+        if (add == 0) continue;
+        if (newn[s] + add > a.cap[s]) {
+            *msg = "particle storage capacity exceeded by MCC secondaries (raise capacity_hint)";
+            return PICGPU_CAPACITY;
+        }
+        if (a.mixed)
+            stage_append_kernel<float><<<(total + 255) / 256, 256, 0, a.stream>>>(st.stage, total, bit, st.pos,
+                                                                                 a.sp[s], int(newn[s]));
+        else
+            stage_append_kernel<double><<<(total + 255) / 256, 256, 0, a.stream>>>(st.stage, total, bit, st.pos,
+                                                                                  a.sp[s], int(newn[s]));
+        *launches += 1;
+        newn[s] += add;
+    }
+    return PICGPU_OK;
+}
+
+// ElectronNeutralCollisionModel::performCollisions with the neutral parcels.
+int mcc_parcels(CollideState& st, const CollideArgs& a, long newn[], std::string* msg, int64_t* launches) {
+    const picgpu_config& cfg = *a.cfg;
+    const picgpu_mcc& mc = cfg.mcc;
+    const int nc = a.m.n_cells;
+    const int es = cfg.electron_species, ns = mc.neutral_species;
+    MccParcelParams M{};
+    M.n_cells = nc;
+    M.e_start = st.cell_start + size_t(es) * (nc + 1);
+    M.e_idx = st.idx[es];
+    M.n_start = st.cell_start + size_t(ns) * (nc + 1);
+    M.n_idx = st.idx[ns];
+    M.svmax = st.psvmax;
+    M.rem = st.premainder;
+    M.vol = a.m.vol;
+    M.xs = st.xs;
+    M.n_xs = st.n_xs;
+    M.me = cfg.species[es].mass;
+    M.mn = cfg.species[ns].mass;
+    M.dt = cfg.dt;
+    M.wE = cfg.species[es].weight;
+    M.wN = cfg.species[ns].weight;
+    M.wmax = std::max(M.wE, M.wN);
+    M.ex_th = mc.ex_threshold;
+    M.iz_th = mc.iz_threshold;
+    M.create_e = mc.create_electron;
+    M.create_i = mc.create_ion;
+    M.relativistic = mc.scatter == 1;
+    M.update_neutral = mc.keep_neutral_velocity ? 0 : 1;
+    M.delete_neutral = mc.keep_neutrals ? 0 : 1;
+    M.seed = cfg.seed;
+    M.step = uint32_t(a.step);
+    M.counts = st.counts;
+    M.overflow = st.overflow;
+    mcc_parcel_count_kernel<<<(nc + 255) / 256, 256, 0, a.stream>>>(M, st.ncand);
+    exclusive_scan(st.ncand, st.cand_off, nc, st.scan_tmp, a.stream, launches);
+    int total = 0;
+    cudaMemcpyAsync(&total, st.cand_off + nc, sizeof(int), cudaMemcpyDeviceToHost, a.stream);
+    if (cudaStreamSynchronize(a.stream) != cudaSuccess) { *msg = "MCC: candidate count failed"; return PICGPU_CUDA_ERROR; }
+    int e = ensure_stage(st, total, msg);
+    if (e) return e;
+    M.cand_off = st.cand_off;
+    M.stage_cap = st.stage_cap;
+    if (a.mixed)
+        mcc_parcel_kernel<float><<<(nc + st.mcc_block - 1) / st.mcc_block, st.mcc_block, 0, a.stream>>>(
+            M, a.sp[es], a.sp[ns], st.stage);
+    else
+        mcc_parcel_kernel<double><<<(nc + st.mcc_block - 1) / st.mcc_block, st.mcc_block, 0, a.stream>>>(
+            M, a.sp[es], a.sp[ns], st.stage);
+    *launches += 2;
+    if (total > 0 && (e = append_stage(st, a, total, newn, msg, launches))) return e;
+    return PICGPU_OK;
+}
+
 int run_collisions(CollideState& st, const CollideArgs& a, int64_t counts[kCollideCounts], long newn[], int swapped[],
                    std::string* msg, int64_t* launches, double* phase_ms) {
     (void)phase_ms;
@@ -1733,6 +2032,10 @@ int run_collisions(CollideState& st, const CollideArgs& a, int64_t counts[kColli
         if (a.mixed) coulomb_kernel<float><<<(nc + 63) / 64, 64, 0, a.stream>>>(C, K);
         else coulomb_kernel<double><<<(nc + 63) / 64, 64, 0, a.stream>>>(C, K);
         *launches += 1;
+    }
+    if (cfg.mcc.enabled && cfg.mcc.neutral_parcels) {
+        const int e = mcc_parcels(st, a, newn, msg, launches);
+        if (e) return e;
     }
     if (cfg.mcc.enabled) {
         const picgpu_mcc& mc = cfg.mcc;

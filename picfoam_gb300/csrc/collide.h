@@ -8,20 +8,25 @@
 
 namespace pgd {
 
-// A secondary staged by the MCC kernel: the ionising electron's position and
-// the velocities of the new electron and ion.
+// A secondary staged by the MCC kernels: the ionising electron's position
+// (the new electron's), the new ion's position (the electron's with a
+// background gas, the neutral parcel's otherwise) and their velocities.
 struct Secondary {
     int32_t tet;
     int32_t flag;         // bit 0: electron, bit 1: ion
     double y[3];
     double ue[3];
     double ui[3];
+    int32_t tet_i;
+    int32_t pad;
+    double y_i[3];
 };
 
 // Counters of one collision step: MCC candidates, elastic, excitation,
 // ionisation; Coulomb pairs; ion MCC candidates, elastic, charge exchange;
-// binary (neutral) pairs tested, collisions; background tests, collisions.
-constexpr int kCollideCounts = 12;
+// binary (neutral) pairs tested, collisions; background tests, collisions;
+// neutral parcels deleted by ionisation.
+constexpr int kCollideCounts = 13;
 
 // Device state owned by the collision step.
 struct CollideState {
@@ -54,6 +59,8 @@ struct CollideState {
     long stage_cap = 0;
     int* overflow = nullptr;                // staging or store overflow (device-driven step)
     double svmax_init = 0.0;                // initial (sigma v)_max of the electron MCC
+    double* psvmax = nullptr;               // electron - neutral parcel (sigma_T c_R)_max per cell
+    double* premainder = nullptr;           // and its collision remainder per cell
     int mcc_block = 128;                    // threads per block of the MCC kernel (one cell each)
     unsigned long long* iz_cell = nullptr;  // MCC ionisations per cell (accumulated)
     // BinaryCollisionModel: (sigma_T c_r)_max, selection and background

@@ -1071,6 +1071,8 @@ picgpu_status pgd_collisions(picgpu_ctx* c, picgpu_step_stats* stats) {
         st = picgpu_status(pgd::run_collisions(c->coll, a, counts, newn, swapped, &msg, &c->launches, nullptr));
     }
     if (st) return bad(c, st, msg);
+    // neutral parcels deleted by ionisation stay in the store as removed slots
+    if (c->cfg.mcc.enabled && c->cfg.mcc.neutral_parcels) c->sp[c->cfg.mcc.neutral_species].alive -= counts[12];
     for (int s = 0; s < c->cfg.n_species; ++s) {
         const long old = c->sp[s].n;
         c->sp[s].n = newn[s];
@@ -2637,6 +2639,8 @@ picgpu_status picgpu_step_graph(picgpu_ctx* c, int nsteps, int steps_per_graph, 
         return bad(c, PICGPU_NOT_SUPPORTED, "step_graph: injection runs only in picgpu_step");
     if (c && c->circ.model != PICGPU_CIRCUIT_NONE)
         return bad(c, PICGPU_NOT_SUPPORTED, "step_graph: circuit models run only in picgpu_step");
+    if (c && c->cfg.mcc.enabled && c->cfg.mcc.neutral_parcels)
+        return bad(c, PICGPU_NOT_SUPPORTED, "step_graph: collisions with neutral parcels run only in picgpu_step");
     if (!c || nsteps < 0 || steps_per_graph <= 0 || nsteps % steps_per_graph) return PICGPU_INVALID_ARG;
     if (!c->mixed || c->cfg.maxwell_solver != PICGPU_MAXWELL_NONE)
         return bad(c, PICGPU_NOT_SUPPORTED, "graph steps need the FP32 form and MaxwellSolver none");
