@@ -14,7 +14,8 @@
   SimpleInjection, FreeStream with `0/boundaryT` / `0/boundaryU`,
   circuitRLC, IdealVoltageSource, IdealCurrentSource with their Thermionic
   and FowlerNordheim EmissionModels), CollisionModels
-  (CoulombCollisionModel with its pairing and collide models,
+  (ElectronNeutralCollisionModel with neutral parcels and FixedValue cross
+  sections, CoulombCollisionModel with its pairing and collide models,
   BinaryCollisionModel IsotropicScattering);
 - `system/controlDict` (deltaT, endTime, writeInterval), `system/fvSolution`
   (phiE: tolerance; GAMG selects the multigrid preconditioner),
@@ -63,6 +64,7 @@ class OFCase:
     end_time: float = 0.0
     write_interval: float = 0.0
     unsupported: list = field(default_factory=list)
+    keepalive: list = field(default_factory=list)   # arrays the config points to
 
     def build(self, backend=None, initialise=True):
         """A Simulation of the case: boundary models attached, picInitialise
@@ -413,25 +415,97 @@ def load_case(path, allow_unsupported=False, precision=abi.PREC_FP64, seed=1234)
                                         temperature=eco.number("T", 0.0), lambda_r=eco.number("lambdaR", 0.0),
                                         weight=eco.number("nParticle", -1.0)))
 
-    _collisions(props.sub("CollisionModels"), cfg, names, mol, bad)
+    init_dict = _read_optional(os.path.join(path, "system", "picInitialiseDict"))
+    keep = []
+    _collisions(props.sub("CollisionModels"), cfg, names, mol, bad, init_dict, keep)
     if props.word("ParticleMerging", "none") != "none":
         bad(f"ParticleMerging {props.word('ParticleMerging')}")
 
-    init = _init(_read_optional(os.path.join(path, "system", "picInitialiseDict")), names, cfg, seed, bad)
+    init = _init(init_dict, names, cfg, seed, bad)
     return OFCase(path=path, mesh=mesh, cfg=cfg, species=names, side_names=side_names, patches=patch_sides,
                   patch_types=patch_types, phi_bc={k: bfield.sub(k) for k in patch_sides},
                   cell_order=cell_order, init=init, injections=[q for _, q in injections],
                   freestreams=[q for _, q in freestreams], emissions=emissions, delta_t=dt, end_time=control.number("endTime", 0.0),
-                  write_interval=control.number("writeInterval", 0.0), unsupported=bad.items)
+                  write_interval=control.number("writeInterval", 0.0), unsupported=bad.items, keepalive=keep)
 
 
-def _collisions(cm, cfg, names, mol, bad):
-    """CollisionModels: Coulomb (fixed or computed coulombLog) and binary
-    IsotropicScattering map; the MCC models (their cross-section tables) and
-    charge exchange are not read from a case."""
-    for key in ("ElectronNeutralCollisionModel", "IonNeutralCollisionModel"):
-        if cm.word(key, "none") != "none":
-            bad(f"{key} {cm.word(key)} (cross sections are set through picgpu_mcc / picgpu_ion_mcc)")
+def _electron_neutral(cm, cfg, names, mol, init_dict, bad, keep):
+    """ElectronNeutralCollisionModel with neutral parcels (BackgroundGasModel
+    none): one neutral species, FixedValue or none cross sections
+    (FixedValueCrossSection.C: the value at every energy, the threshold
+    applied by the collision model), FindMaximum start values."""
+    model = cm.word("ElectronNeutralCollisionModel", "none")
+    if model == "none":
+        return
+    scatter = {"NanbuElectronNeutral": 0, "RelativisticElectronNeutral": 1}.get(model)
+    if scatter is None:
+        raise UnsupportedCase(f"ElectronNeutralCollisionModel {model}")
+    if cm.word("BackgroundGasModel", "none") != "none":
+        bad("ElectronNeutralCollisionModel with a background gas (set picgpu_mcc's gas fields)")
+        return
+    co = cm.sub("ElectronNeutralCollisionCoeffs")
+    if co.word("WeightCorrection", "none") not in ("none", "Nanbu"):
+        bad(f"ElectronNeutral WeightCorrection {co.word('WeightCorrection')}")
+    xs = co.sub("CrossSectionModels")
+    neutrals = [k for k, v in xs.items() if isinstance(v, foam.Dict)]
+    if len(neutrals) != 1 or neutrals[0] not in names:
+        raise UnsupportedCase("ElectronNeutralCollisionModel: exactly one neutral species is supported")
+    nname = neutrals[0]
+    d = xs.sub(nname)
+    values, thresholds = {}, {}
+    for kind in ("Elastic", "Excitation", "Ionization"):
+        t = d.word(f"{kind}CrossSection", "none")
+        if t == "none":
+            values[kind], thresholds[kind] = 0.0, 0.0
+        elif t == "FixedValue":
+            fc = d.sub(f"{kind}FixedValueCoeffs")
+            values[kind], thresholds[kind] = fc.number("value", 0.0), fc.number("threshold", 0.0)
+        else:
+            raise UnsupportedCase(f"{kind}CrossSection {t} (only FixedValue and none are read from a case)")
+    ion_name = None
+    for _, rel in mol.sub("SpeciesRelations").items():
+        if isinstance(rel, foam.Dict) and rel.word("neutralTypeId") == nname:
+            ion_name = rel.word("ionTypeId")
+    tables = [np.array([0.0, 1e6]), np.full(2, values["Elastic"]), np.full(2, values["Excitation"]),
+              np.full(2, values["Ionization"])]
+    tables = [np.ascontiguousarray(a, dtype=np.float64) for a in tables]
+    keep.extend(tables)
+    import ctypes as C
+    mc = cfg.mcc
+    mc.enabled = 1
+    mc.scatter = scatter
+    mc.create_electron = 1 if co.flag("createElectron", True) else 0
+    mc.create_ion = 1 if (co.flag("createIon", True) and ion_name in names) else 0
+    mc.ion_species = names.index(ion_name) if ion_name in names else -1
+    mc.n_xs = 2
+    ns = names.index(nname)
+    mc.gas_mass = cfg.species[ns].mass
+    mc.gas_weight = cfg.species[ns].weight
+    mc.ex_threshold = thresholds["Excitation"]
+    mc.iz_threshold = thresholds["Ionization"]
+    search = init_dict.sub("CrossSectionInitialization").sub("electronNeutral_searchParameter")
+    mc.find_max_energy = search.number("maximumEnergy", 1000.0)
+    mc.find_energy_step = search.number("energyStep", 0.01)
+    mc.xs_energy, mc.xs_elastic, mc.xs_excitation, mc.xs_ionization = [
+        a.ctypes.data_as(C.POINTER(C.c_double)) for a in tables]
+    mc.neutral_parcels = 1
+    mc.neutral_species = ns
+    mc.keep_neutrals = 0 if co.flag("deleteNeutral", True) else 1
+    mc.keep_neutral_velocity = 0 if co.flag("updateNeutralVelocity", True) else 1
+    if co.number("ionization_nEquivalentParticles", 0.0) > 0:
+        bad("ionization_nEquivalentParticles (one weight per species)")
+
+
+def _collisions(cm, cfg, names, mol, bad, init_dict=None, keep=None):
+    """CollisionModels: electron-neutral collisions with neutral parcels
+    (FixedValue cross sections), Coulomb (fixed or computed coulombLog) and
+    binary IsotropicScattering map; background-gas MCC and ion-neutral
+    collisions are set through picgpu_mcc / picgpu_ion_mcc."""
+    _electron_neutral(cm, cfg, names, mol, init_dict if init_dict is not None else foam.Dict(), bad,
+                      keep if keep is not None else [])
+    if cm.word("IonNeutralCollisionModel", "none") != "none":
+        bad(f"IonNeutralCollisionModel {cm.word('IonNeutralCollisionModel')} "
+            "(cross sections are set through picgpu_ion_mcc)")
     coul = cm.word("CoulombCollisionModel", "none")
     if coul != "none":
         co = cm.sub("CoulombCollisionCoeffs")

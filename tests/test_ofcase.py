@@ -236,7 +236,7 @@ REF = "/root/reference/tutorials"
 @pytest.mark.skipif(not os.path.isdir(REF), reason="reference tutorials not present")
 @pytest.mark.parametrize("name,strict", [("plasmaOscillation", True), ("rlcCircuit", True), ("thermalization", True),
                                          ("thermalization_binaryCollision", True), ("floatingBoundary", False),
-                                         ("ionization", False), ("magneticRotation", False),
+                                         ("ionization", True), ("magneticRotation", False),
                                          ("electricAcceleration", False)])
 def test_reference_tutorials_load(name, strict):
     c = ofcase.load_case(os.path.join(REF, name), allow_unsupported=not strict)
@@ -252,6 +252,11 @@ def test_reference_tutorials_load(name, strict):
         assert c.cfg.coulomb.enabled and c.cfg.coulomb.collide == abi.COLLIDE_PEREZ and c.cfg.coulomb.coulomb_log == 15
     if name == "thermalization_binaryCollision":
         assert c.cfg.binary.enabled and c.cfg.binary.weight_correction == abi.WEIGHT_CORRECTION_NANBU
+    if name == "ionization":
+        mc = c.cfg.mcc
+        assert mc.enabled and mc.neutral_parcels and c.species[mc.neutral_species] == "Ar"
+        assert c.species[mc.ion_species] == "Ar+" and mc.iz_threshold == 15.76 and mc.scatter == 1
+        assert mc.xs_ionization[0] == 3.43943e-20 and mc.xs_elastic[0] == 0.0 and mc.find_max_energy == 500
     if name == "floatingBoundary":
         assert c.mesh.side[1].kind == abi.PATCH_FLOATING and len(c.injections) == 1
 
