@@ -20,7 +20,7 @@
 - `system/controlDict` (deltaT, endTime, writeInterval), `system/fvSolution`
   (phiE: tolerance; GAMG selects the multigrid preconditioner),
   `system/picInitialiseDict` (Equipartition, Maxwellian, Isotropization,
-  QuasineutralPlasma, UniformDisplacement, none).
+  QuasineutralPlasma, UniformDisplacement, ParticleList, none).
 Anything else raises `UnsupportedCase` naming it, unless
 `allow_unsupported=True` (then it is listed in `OFCase.unsupported` and left
 out).
@@ -65,6 +65,7 @@ class OFCase:
     write_interval: float = 0.0
     unsupported: list = field(default_factory=list)
     keepalive: list = field(default_factory=list)   # arrays the config points to
+    particle_list: list = field(default_factory=list)  # ParticleList parcels: (species, position, velocity)
 
     def build(self, backend=None, initialise=True):
         """A Simulation of the case: boundary models attached, picInitialise
@@ -77,6 +78,15 @@ class OFCase:
             sim.set_freestream(self.freestreams)
         if self.emissions:
             sim.set_emission(self.emissions)
+        if initialise and self.particle_list:
+            from .simulation import Mesh
+            m = Mesh(self.mesh)
+            for s in range(len(self.species)):
+                mine = [(p, u) for sp, p, u in self.particle_list if sp == s]
+                if not mine:
+                    continue
+                tet, bary = m.locate(np.array([p for p, _ in mine], dtype=np.float64))
+                sim.set_particles(s, tet, bary, np.array([u for _, u in mine], dtype=np.float64))
         if initialise and self.init is not None:
             sim.initialise(self.init)
         sim.initialise_fields()
@@ -421,12 +431,14 @@ def load_case(path, allow_unsupported=False, precision=abi.PREC_FP64, seed=1234)
     if props.word("ParticleMerging", "none") != "none":
         bad(f"ParticleMerging {props.word('ParticleMerging')}")
 
-    init = _init(init_dict, names, cfg, seed, bad)
+    plist = []
+    init = _init(init_dict, names, cfg, seed, bad, plist)
     return OFCase(path=path, mesh=mesh, cfg=cfg, species=names, side_names=side_names, patches=patch_sides,
                   patch_types=patch_types, phi_bc={k: bfield.sub(k) for k in patch_sides},
                   cell_order=cell_order, init=init, injections=[q for _, q in injections],
                   freestreams=[q for _, q in freestreams], emissions=emissions, delta_t=dt, end_time=control.number("endTime", 0.0),
-                  write_interval=control.number("writeInterval", 0.0), unsupported=bad.items, keepalive=keep)
+                  write_interval=control.number("writeInterval", 0.0), unsupported=bad.items, keepalive=keep,
+                  particle_list=plist)
 
 
 def _electron_neutral(cm, cfg, names, mol, init_dict, bad, keep):
@@ -559,11 +571,29 @@ def _collisions(cm, cfg, names, mol, bad, init_dict=None, keep=None):
         bad("BinaryCollisionModel with a background gas (set picgpu_binary.background_species)")
 
 
-def _init(d, names, cfg, seed, bad):
-    """system/picInitialiseDict as an abi.Init (None without the file)."""
+def _init(d, names, cfg, seed, bad, plist=None):
+    """system/picInitialiseDict as an abi.Init (None without the file).  A
+    ParticleList (ParticleListInitialization: one parcel per entry, species,
+    position, velocity) goes to plist as (species, position, velocity) and
+    the Init places nothing, then applies the leapfrog and field settings to
+    the listed parcels."""
     if not d:
         return None
     model = d.word("InitializationModel", "none")
+    if model == "ParticleList" and plist is not None:
+        for _, e in d.sub("ParticleListCoeffs").items():
+            if not isinstance(e, foam.Dict):
+                continue
+            if e.number("temperature", 0.0) != 0.0:
+                bad("ParticleList: a parcel with a temperature (thermal spread)")
+            sp = str(e.word("species"))
+            if sp not in names:
+                raise UnsupportedCase(f"ParticleList: no species {sp}")
+            plist.append((names.index(sp), [float(x) for x in e["position"]],
+                          [float(x) for x in e.get("velocity", [0, 0, 0])]))
+        return cases.init_config(abi.INIT_NONE, seed=seed, clear=False,
+                                 solve_fields=d.flag("solveMaxwellEquations", False),
+                                 leapfrog=d.flag("initalizeLeapFrog", False))
     code = _INIT.get(model)
     if code is None:
         bad(f"InitializationModel {model}")

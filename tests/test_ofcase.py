@@ -236,7 +236,7 @@ REF = "/root/reference/tutorials"
 @pytest.mark.skipif(not os.path.isdir(REF), reason="reference tutorials not present")
 @pytest.mark.parametrize("name,strict", [("plasmaOscillation", True), ("rlcCircuit", True), ("thermalization", True),
                                          ("thermalization_binaryCollision", True), ("floatingBoundary", False),
-                                         ("ionization", True), ("magneticRotation", False),
+                                         ("ionization", True), ("magneticRotation", True),
                                          ("electricAcceleration", False)])
 def test_reference_tutorials_load(name, strict):
     c = ofcase.load_case(os.path.join(REF, name), allow_unsupported=not strict)
@@ -265,3 +265,20 @@ def test_reference_tutorials_load(name, strict):
 def test_reference_gmsh_case_is_refused():
     with pytest.raises(ofcase.UnsupportedCase):
         ofcase.load_case(os.path.join(REF, "ionDriftVelocity"), allow_unsupported=True)
+
+
+@pytest.mark.skipif(not os.path.isdir(REF), reason="reference tutorials not present")
+def test_reference_magnetic_rotation_gyrates(oracle_backend):
+    # ParticleList: one electron at 0.1 c in B_z = 1 T; HigueraCary keeps the
+    # gyration radius and the speed
+    c = ofcase.load_case(os.path.join(REF, "magneticRotation"))
+    assert c.particle_list and c.cfg.pusher == abi.PUSHER_HIGUERA_CARY
+    sim = c.build(backend=oracle_backend.OracleBackend(1))
+    m = Mesh(c.mesh)
+    r0 = abs(c.particle_list[0][1][1])
+    for _ in range(3):
+        sim.step(50)
+        t, b, U = sim.get_particles(0)
+        x = m.position(t, b)
+        assert np.linalg.norm(x[0, :2]) == pytest.approx(r0, rel=1e-7)
+        assert np.linalg.norm(U[0]) == pytest.approx(29979246.0, rel=1e-12)
