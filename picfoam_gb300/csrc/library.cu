@@ -722,6 +722,8 @@ picgpu_status poisson(picgpu_ctx* c, picgpu_step_stats* stats, bool learned = fa
             stats->learned_fallback = c->ws->fallback;
         }
     }
+    if (!std::isfinite(S.bb) || !std::isfinite(S.rr))
+        return bad(c, PICGPU_NAN_DETECTED, "Poisson: the charge density or the potential is not finite");
     if (!S.converged) {
         char msg[160];
         std::snprintf(msg, sizeof msg, "PCG did not converge within pcg_max_iter (%d iterations, %d refinements, "
