@@ -444,6 +444,12 @@ def run_ours(args, rank, ws):
     from picfoam_gb300 import abi, cases
     from picfoam_gb300.simulation import Simulation
     local = int(os.environ.get("LOCAL_RANK", "0"))
+    if ws > 1:
+        # one GPU per rank: the library uses the current device of its own
+        # (static) CUDA runtime, so the rank's GPU is the only one it sees
+        vis = os.environ.get("CUDA_VISIBLE_DEVICES")
+        devs = [d for d in vis.split(",") if d] if vis else None
+        os.environ["CUDA_VISIBLE_DEVICES"] = devs[local % len(devs)] if devs else str(local)
     prec = abi.PREC_MIXED if args.precision == "mixed" else abi.PREC_FP64
     case = cases.two_species_3d(n_cells=args.cells, per_cell=args.ppc, precision=prec, seed=1234 + rank)
     case.cfg.sort_interval = args.sort_interval
