@@ -192,6 +192,15 @@ typedef struct {
     const double* xs_energy;   /* [n_xs] eV, ascending */
     const double* xs_elastic;  /* [n_xs] m^2 */
     const double* xs_charge_exchange;
+    /* Collisions with neutral parcels (performCollisions,
+     * IonNeutralCollisionModel.C:579-707): NTC candidates nC iC w_max
+     * (sigma_T c_R)_max dt / V per cell, isotropic elastic scattering of the
+     * pair or the charge-exchange identity switch, before the background-gas
+     * collisions (which need picgpu_mcc's gas_density > 0). */
+    int32_t neutral_parcels;        /* 1: collide with the parcels of neutral_species */
+    int32_t neutral_species;        /* species of the neutral parcels (charge 0) */
+    int32_t keep_neutral_velocity;  /* updateNeutralVelocity false */
+    int32_t pad2;
 } picgpu_ion_mcc;
 
 /* Binary Coulomb collisions (CoulombCollisionModel.C:241-309). */

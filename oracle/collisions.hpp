@@ -159,7 +159,7 @@ inline std::string init_ion_mcc(const picgpu_config& cfg, Tables& t, int n_cells
     if (m.n_xs < 2 || m.n_xs > PICGPU_MAX_XS_POINTS || !m.xs_energy || !m.xs_elastic || !m.xs_charge_exchange)
         return "ion_mcc: cross-section tables missing";
     if (m.ion_species < 0 || m.ion_species >= cfg.n_species) return "ion_mcc: ion species not set";
-    if (!(cfg.mcc.gas_density > 0) || !(cfg.mcc.gas_mass > 0))
+    if ((!(cfg.mcc.gas_density > 0) && !m.neutral_parcels) || !(cfg.mcc.gas_mass > 0))
         return "ion_mcc: background gas (mcc.gas_*) not set";
     t.e.assign(m.xs_energy, m.xs_energy + m.n_xs);
     t.el.assign(m.xs_elastic, m.xs_elastic + m.n_xs);

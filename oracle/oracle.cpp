@@ -160,6 +160,7 @@ struct Oracle {
     // collision state
     std::vector<double> svmax, remainder;
     std::vector<double> psvmax, premainder;  // electron - neutral parcels
+    std::vector<double> ipsvmax, ipremainder;  // ion - neutral parcels
     std::vector<double> isvmax, iremainder;  // ion-neutral
     int last_pcg_iter = 0;
     double last_res_l2 = 0, last_res_of = 0;
@@ -1235,6 +1236,77 @@ void mcc_parcels(Oracle& o, std::vector<std::vector<std::vector<int>>>& occ, pic
     }
 }
 
+// IonNeutralCollisionModel::performCollisions (IonNeutralCollisionModel.C:
+// 579-707): ions with the neutral parcels of the cell, isotropic elastic
+// scattering of the pair (neutral P, ion Q; IonIsotropicScattering.C:60-100)
+// or the charge-exchange identity switch (:401-413).
+void ion_parcels(Oracle& o, std::vector<std::vector<std::vector<int>>>& occ, picgpu_step_stats* st) {
+    const picgpu_ion_mcc& im = o.cfg.ion_mcc;
+    const int is = im.ion_species, ns = im.neutral_species;
+    const double mi = o.cfg.species[is].mass, mn = o.cfg.species[ns].mass;
+    const double wI = o.cfg.species[is].weight, wN = o.cfg.species[ns].weight;
+    const double wmax = std::max(wN, wI), dt = o.cfg.dt, mt = mn + mi;
+    const bool update_neutral = !im.keep_neutral_velocity;
+    auto& ions = o.cloud[is];
+    auto& neu = o.cloud[ns];
+    long long cand = 0, nel = 0, ncx = 0;
+    for (int c = 0; c < o.m.n_cells; ++c) {
+        const std::vector<int>& ilist = occ[is][c];
+        const std::vector<int>& nlist = occ[ns][c];
+        const long iC = long(ilist.size()), nC = long(nlist.size());
+        if (nC == 0 || iC == 0) continue;
+        const double sv = o.ipsvmax[c];
+        const double selected = o.ipremainder[c] + double(int(nC) * int(iC)) * wmax * sv * dt / o.m.vol[c];
+        const long nCand = long(selected);
+        o.ipremainder[c] = selected - double(nCand);
+        cand += nCand;
+        if (nCand == 0) continue;
+        ocoll::Philox r(o.cfg.seed, ocoll::kStreamIonMcc | 1u, uint32_t(c), uint32_t(o.step_index));
+        for (long k = 0; k < nCand; ++k) {
+            long jp = long(r.uniform() * double(nC));
+            if (jp >= nC) jp = nC - 1;
+            long jq = long(r.uniform() * double(iC));
+            if (jq >= iC) jq = iC - 1;
+            Parcel& P = neu[nlist[jp]];
+            Parcel& Q = ions[ilist[jq]];
+            const double cR = magv(sub(Q.U, P.U));
+            const double gamma = 1.0 / std::sqrt(1.0 - (cR * cR) / (kC * kC));
+            const double eV = (gamma - 1.0) * mi * kC * kC / ocoll::kEcharge;
+            const double Qel = ocoll::interp_xs(eV, o.ixs.e, o.ixs.el);
+            const double Qcx = ocoll::interp_xs(eV, o.ixs.e, o.ixs.ex);
+            const double Qt = Qel + Qcx;
+            if (Qt * cR > o.ipsvmax[c]) o.ipsvmax[c] = Qt * cR;
+            const double rndU = r.uniform();
+            if (rndU <= Qel * cR / sv) {
+                nel++;
+                const V3 preUP = P.U;
+                const V3 Ucm = v3((mn * P.U.x + mi * Q.U.x) / mt, (mn * P.U.y + mi * Q.U.y) / mt,
+                                  (mn * P.U.z + mi * Q.U.z) / mt);
+                const double cr = magv(sub(P.U, Q.U));
+                const double cosT = 2.0 * r.uniform() - 1.0;
+                const double sinT = std::sqrt(1.0 - cosT * cosT);
+                const double phi = 2.0 * kPi * r.uniform();
+                const V3 rel = v3(cr * cosT, cr * (sinT * std::cos(phi)), cr * (sinT * std::sin(phi)));
+                P.U = v3(Ucm.x + rel.x * mi / mt, Ucm.y + rel.y * mi / mt, Ucm.z + rel.z * mi / mt);
+                Q.U = v3(Ucm.x - rel.x * mn / mt, Ucm.y - rel.y * mn / mt, Ucm.z - rel.z * mn / mt);
+                if (!update_neutral) P.U = preUP;
+            } else if (eV >= im.cx_threshold && rndU <= Qt * cR / sv) {
+                ncx++;
+                const double u = r.uniform();
+                const V3 tmpP = P.U;
+                if (u <= wI / wN) P.U = Q.U;
+                if (u <= wN / wI) Q.U = tmpP;
+                if (!update_neutral) P.U = tmpP;
+            }
+        }
+    }
+    if (st) {
+        st->ion_mcc_candidates += cand;
+        st->ion_mcc_elastic += nel;
+        st->ion_mcc_charge_exchange += ncx;
+    }
+}
+
 // IonNeutralCollisionModel::performBackgroundCollisions
 // (IonNeutralCollisionModel.C:453-577): IsotropicScattering elastic
 // (IonIsotropicScattering.C:103-143) or charge exchange (:419-426).
@@ -1848,6 +1920,7 @@ void collisions(Oracle& o, picgpu_step_stats* st) {
     if (o.cfg.coulomb.enabled) coulomb_pairs(o, occ, st);
     if (o.cfg.mcc.enabled && o.cfg.mcc.neutral_parcels) mcc_parcels(o, occ, st);
     if (o.cfg.mcc.enabled) mcc_background(o, occ[o.cfg.electron_species], st);
+    if (o.cfg.ion_mcc.enabled && o.cfg.ion_mcc.neutral_parcels) ion_parcels(o, occ, st);
     if (o.cfg.ion_mcc.enabled) ion_mcc_background(o, occ[o.cfg.ion_mcc.ion_species], st);
     if (o.cfg.binary.enabled) binary_collisions(o, occ, st);
 }
@@ -2581,6 +2654,20 @@ int oracle_create(const picgpu_mesh_desc* mesh, const picgpu_config* cfg, int nt
     if (cfg->ion_mcc.enabled) {
         std::string e = ocoll::init_ion_mcc(o.cfg, o.ixs, m.n_cells, o.isvmax, o.iremainder);
         if (!e.empty()) { o.err = e; *out = c; return PICGPU_INVALID_ARG; }
+        if (cfg->ion_mcc.neutral_parcels) {
+            const int ns = cfg->ion_mcc.neutral_species;
+            if (ns < 0 || ns >= cfg->n_species || cfg->species[ns].charge != 0.0 || cfg->binary.enabled) {
+                o.err = "ion mcc: unsupported neutral-parcel set-up";
+                *out = c;
+                return PICGPU_INVALID_ARG;
+            }
+            o.ipsvmax = o.isvmax;
+            o.ipremainder.resize(m.n_cells);
+            for (int k = 0; k < m.n_cells; ++k) {
+                ocoll::Philox r(cfg->seed, ocoll::kStreamIonRemainder | 1u, uint32_t(k), 0u);
+                o.ipremainder[k] = r.uniform();
+            }
+        }
     }
     if (cfg->coulomb.enabled && cfg->coulomb.pairing == 1) {
         double w = -1.0;

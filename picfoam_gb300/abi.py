@@ -96,6 +96,8 @@ class IonMcc(C.Structure):
         ("find_max_energy", C.c_double), ("find_energy_step", C.c_double),
         ("xs_energy", C.POINTER(C.c_double)), ("xs_elastic", C.POINTER(C.c_double)),
         ("xs_charge_exchange", C.POINTER(C.c_double)),
+        ("neutral_parcels", C.c_int32), ("neutral_species", C.c_int32), ("keep_neutral_velocity", C.c_int32),
+        ("pad2", C.c_int32),
     ]
 
 

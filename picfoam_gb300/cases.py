@@ -316,6 +316,46 @@ def neutral_parcel_ionization(n_cells=(4, 4, 4), L=1e-3, per_cell=(20, 40), T_e_
                 dict(w=w, v_e=v_e, n_n=n_n, V=L ** 3, N_e=len(te), N_n=len(tn), n_c=n_c))
 
 
+def ion_neutral_parcels(n_cells=(4, 4, 4), L=1e-3, per_cell=(30, 30), T_i_eV=5.0, T_n=300.0, n_n=1e22,
+                        sigma_el=5e-19, sigma_cx=3e-19, dt=2e-9, seed=1234, precision=abi.PREC_FP64,
+                        keep_neutral_velocity=False):
+    """Ar+ ions and neutral Ar parcels of equal weight in a periodic box,
+    MaxwellSolver none, IonNeutralCollisionModel against the parcels
+    (performCollisions) with constant elastic and charge-exchange cross
+    sections.  per_cell = (ions, neutrals)."""
+    sides = [patch(abi.PATCH_CYCLIC) for _ in range(6)]
+    mesh = block_mesh(n_cells, (L,) * 3, sides)
+    n_c = n_cells[0] * n_cells[1] * n_cells[2]
+    w = n_n * L ** 3 / (n_c * per_cell[1])
+    cfg = base_config(dt, [(M_AR, 0.0, w, True), (M_AR, E_CHARGE, w, True)], maxwell=abi.MAXWELL_NONE,
+                      precision=precision, seed=seed, electron_species=-1)
+    mc = cfg.mcc
+    mc.gas_density = 0.0
+    mc.gas_mass = M_AR
+    mc.gas_temperature = T_n
+    mc.gas_weight = w
+    arrs = [np.ascontiguousarray(a, dtype=np.float64) for a in ([0.0, 1e6], [sigma_el] * 2, [sigma_cx] * 2)]
+    import ctypes as C
+    im = cfg.ion_mcc
+    im.enabled = 1
+    im.ion_species = 1
+    im.n_xs = 2
+    im.cx_threshold = 0.0
+    vmax = math.sqrt(2 * E_CHARGE * 10 * T_i_eV / M_AR)
+    im.sigma_v_max_init = (sigma_el + sigma_cx) * vmax
+    im.xs_energy, im.xs_elastic, im.xs_charge_exchange = [a.ctypes.data_as(C.POINTER(C.c_double)) for a in arrs]
+    im.neutral_parcels = 1
+    im.neutral_species = 0
+    im.keep_neutral_velocity = 1 if keep_neutral_velocity else 0
+    rng = np.random.Generator(np.random.Philox(seed))
+    tn, bn = uniform_in_cells(rng, np.arange(n_c), per_cell[1])
+    Un = rng.standard_normal((len(tn), 3)) * math.sqrt(K_B * T_n / M_AR)
+    ti, bi = uniform_in_cells(rng, np.arange(n_c), per_cell[0])
+    Ui = rng.standard_normal((len(ti), 3)) * math.sqrt(E_CHARGE * T_i_eV / M_AR)
+    return Case("ion_neutral_parcels", mesh, cfg, {0: (tn, bn, Un), 1: (ti, bi, Ui)}, arrs,
+                dict(w=w, n_n=n_n, V=L ** 3, sigma=sigma_el + sigma_cx))
+
+
 def set_coulomb(cfg, pairing=abi.PAIRING_NANBU_YONEMURA, collide=abi.COLLIDE_NANBU, coulomb_log=15.0,
                 calculate_bmin=True, debye_drift=True, weight_correction=0, allow_intra=True):
     """CoulombCollisionModel dictionary: coulomb_log 0 computes the logarithm

@@ -667,6 +667,98 @@ __global__ void stage_append_kernel(const Secondary* __restrict__ stage, int n, 
     }
 }
 
+// IonNeutralCollisionModel::performCollisions (IonNeutralCollisionModel.C:
+// 579-707) with the parcels of one neutral species: NTC candidates
+// nC iC w_max (sigma_T c_R)_max dt / V per cell; IonIsotropicScattering of
+// the pair (neutral P, ion Q; IonIsotropicScattering.C:60-100) or the
+// charge-exchange identity switch with its weight gates (:401-413).
+struct IonParcelParams {
+    int n_cells;
+    const int* i_start;
+    const int* i_idx;
+    const int* n_start;
+    const int* n_idx;
+    double* svmax;
+    double* rem;
+    const double* vol;
+    const double* xs;     // 3 x n_xs: energy, elastic, charge exchange
+    int n_xs;
+    double mi, mn, dt, wI, wN, wmax, cx_th;
+    int update_neutral;
+    uint64_t seed;
+    uint32_t step;
+    unsigned long long* counts;
+};
+
+template <class R>
+__global__ void ion_parcel_kernel(IonParcelParams M, DSpecies ions, DSpecies neu) {
+    const int c = blockIdx.x * blockDim.x + threadIdx.x;
+    if (c >= M.n_cells) return;
+    const int iC = M.i_start[c + 1] - M.i_start[c];
+    const int nC = M.n_start[c + 1] - M.n_start[c];
+    if (nC == 0 || iC == 0) return;
+    const double sv = M.svmax[c];
+    const double selected = M.rem[c] + double(nC * iC) * M.wmax * sv * M.dt / M.vol[c];
+    const long nCand = long(selected);
+    M.rem[c] = selected - double(nCand);
+    if (nCand == 0) return;
+    const int* ilist = M.i_idx + M.i_start[c];
+    const int* nlist = M.n_idx + M.n_start[c];
+    const double* E = M.xs;
+    const double* EL = M.xs + M.n_xs;
+    const double* CX = M.xs + 2 * M.n_xs;
+    Rng r(M.seed, kStreamIonMcc | 1u, uint32_t(c), M.step);
+    unsigned long long nel = 0, ncx = 0;
+    const double mt = M.mn + M.mi;
+    for (long k = 0; k < nCand; ++k) {
+        long jp = long(r.uniform() * double(nC));
+        if (jp >= nC) jp = nC - 1;
+        long jq = long(r.uniform() * double(iC));
+        if (jq >= iC) jq = iC - 1;
+        const int pp = nlist[jp], pq = ilist[jq];
+        V3d UP = Vel<R>::get(neu, pp);
+        V3d UQ = Vel<R>::get(ions, pq);
+        const V3d d = {UQ.x - UP.x, UQ.y - UP.y, UQ.z - UP.z};
+        const double cR = magd(d);
+        const double gamma = 1.0 / sqrt(1.0 - (cR * cR) / (kC * kC));
+        const double eV = (gamma - 1.0) * M.mi * kC * kC / kEch;
+        const double Qel = interp_xs(eV, E, EL, M.n_xs);
+        const double Qcx = interp_xs(eV, E, CX, M.n_xs);
+        const double Qt = Qel + Qcx;
+        if (Qt * cR > M.svmax[c]) M.svmax[c] = Qt * cR;
+        const double rndU = r.uniform();
+        if (rndU <= Qel * cR / sv) {
+            nel++;
+            const V3d preUP = UP;
+            const V3d Ucm = {(M.mn * UP.x + M.mi * UQ.x) / mt, (M.mn * UP.y + M.mi * UQ.y) / mt,
+                             (M.mn * UP.z + M.mi * UQ.z) / mt};
+            const V3d g = {UP.x - UQ.x, UP.y - UQ.y, UP.z - UQ.z};
+            const double cr = magd(g);
+            const double cosT = 2.0 * r.uniform() - 1.0;
+            const double sinT = sqrt(1.0 - cosT * cosT);
+            const double phi = 2.0 * kPi * r.uniform();
+            const V3d rel = {cr * cosT, cr * (sinT * cos(phi)), cr * (sinT * sin(phi))};
+            UP = {Ucm.x + rel.x * M.mi / mt, Ucm.y + rel.y * M.mi / mt, Ucm.z + rel.z * M.mi / mt};
+            UQ = {Ucm.x - rel.x * M.mn / mt, Ucm.y - rel.y * M.mn / mt, Ucm.z - rel.z * M.mn / mt};
+            if (!M.update_neutral) UP = preUP;
+            Vel<R>::put(neu, pp, UP);
+            Vel<R>::put(ions, pq, UQ);
+        } else if (eV >= M.cx_th && rndU <= Qt * cR / sv) {
+            ncx++;
+            const double u = r.uniform();
+            const V3d tmpP = UP;
+            if (u <= M.wI / M.wN) UP = UQ;
+            if (u <= M.wN / M.wI) UQ = tmpP;
+            if (!M.update_neutral) UP = tmpP;
+            Vel<R>::put(neu, pp, UP);
+            Vel<R>::put(ions, pq, UQ);
+        }
+    }
+    atomicAdd(M.counts + 5, (unsigned long long)nCand);
+    if (nel) atomicAdd(M.counts + 6, nel);
+    if (ncx) atomicAdd(M.counts + 7, ncx);
+}
+
 // --------------------------------------------------------- ion-neutral ---
 struct IonMccParams {
     int n_cells;
@@ -1536,7 +1628,7 @@ int collide_init(CollideState& st, const picgpu_config& cfg, const DMesh& m, cud
             *msg = "ion MCC: ion species not set";
             return PICGPU_INVALID_ARG;
         }
-        if (!(cfg.mcc.gas_density > 0) || !(cfg.mcc.gas_mass > 0)) {
+        if ((!(cfg.mcc.gas_density > 0) && !im.neutral_parcels) || !(cfg.mcc.gas_mass > 0)) {
             *msg = "ion MCC: background gas (mcc.gas_*) not set";
             return PICGPU_INVALID_ARG;
         }
@@ -1559,6 +1651,18 @@ int collide_init(CollideState& st, const picgpu_config& cfg, const DMesh& m, cud
         const int e =
             upload_mcc(&st.isvmax, &st.iremainder, &st.ixs, xs, sv, cfg.seed, kStreamIonRemainder, nc, s, msg);
         if (e) return e;
+        if (im.neutral_parcels) {
+            const int ns = im.neutral_species;
+            if (ns < 0 || ns >= cfg.n_species || cfg.species[ns].charge != 0.0 || cfg.binary.enabled) {
+                *msg = "ion MCC: neutral_species must name a species of charge 0 (and no BinaryCollisionModel)";
+                return PICGPU_INVALID_ARG;
+            }
+            double* xs_unused = nullptr;
+            const int e2 = upload_mcc(&st.ipsvmax, &st.ipremainder, &xs_unused, xs, sv, cfg.seed,
+                                      kStreamIonRemainder | 1u, nc, s, msg);
+            if (e2) return e2;
+            cudaFree(xs_unused);
+        }
     }
     if (cfg.binary.enabled) {
         const picgpu_binary& bc = cfg.binary;
@@ -2096,6 +2200,34 @@ int run_collisions(CollideState& st, const CollideArgs& a, int64_t counts[kColli
         }
     }
     // ion-neutral last, over the ions present before this step's secondaries
+    if (cfg.ion_mcc.enabled && cfg.ion_mcc.neutral_parcels) {
+        const int is = cfg.ion_mcc.ion_species, ns = cfg.ion_mcc.neutral_species;
+        IonParcelParams M{};
+        M.n_cells = nc;
+        M.i_start = st.cell_start + size_t(is) * (nc + 1);
+        M.i_idx = st.idx[is];
+        M.n_start = st.cell_start + size_t(ns) * (nc + 1);
+        M.n_idx = st.idx[ns];
+        M.svmax = st.ipsvmax;
+        M.rem = st.ipremainder;
+        M.vol = a.m.vol;
+        M.xs = st.ixs;
+        M.n_xs = st.n_ixs;
+        M.mi = cfg.species[is].mass;
+        M.mn = cfg.species[ns].mass;
+        M.dt = cfg.dt;
+        M.wI = cfg.species[is].weight;
+        M.wN = cfg.species[ns].weight;
+        M.wmax = std::max(M.wN, M.wI);
+        M.cx_th = cfg.ion_mcc.cx_threshold;
+        M.update_neutral = cfg.ion_mcc.keep_neutral_velocity ? 0 : 1;
+        M.seed = cfg.seed;
+        M.step = uint32_t(a.step);
+        M.counts = st.counts;
+        if (a.mixed) ion_parcel_kernel<float><<<(nc + st.mcc_block - 1) / st.mcc_block, st.mcc_block, 0, a.stream>>>(M, a.sp[is], a.sp[ns]);
+        else ion_parcel_kernel<double><<<(nc + st.mcc_block - 1) / st.mcc_block, st.mcc_block, 0, a.stream>>>(M, a.sp[is], a.sp[ns]);
+        *launches += 1;
+    }
     if (cfg.ion_mcc.enabled) {
         const int is = cfg.ion_mcc.ion_species;
         const IonMccParams M = ion_setup(st, a);

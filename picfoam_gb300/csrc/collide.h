@@ -61,6 +61,8 @@ struct CollideState {
     double svmax_init = 0.0;                // initial (sigma v)_max of the electron MCC
     double* psvmax = nullptr;               // electron - neutral parcel (sigma_T c_R)_max per cell
     double* premainder = nullptr;           // and its collision remainder per cell
+    double* ipsvmax = nullptr;              // ion - neutral parcel (sigma_T c_R)_max per cell
+    double* ipremainder = nullptr;
     int mcc_block = 128;                    // threads per block of the MCC kernel (one cell each)
     unsigned long long* iz_cell = nullptr;  // MCC ionisations per cell (accumulated)
     // BinaryCollisionModel: (sigma_T c_r)_max, selection and background

@@ -2641,7 +2641,8 @@ picgpu_status picgpu_step_graph(picgpu_ctx* c, int nsteps, int steps_per_graph, 
         return bad(c, PICGPU_NOT_SUPPORTED, "step_graph: injection runs only in picgpu_step");
     if (c && c->circ.model != PICGPU_CIRCUIT_NONE)
         return bad(c, PICGPU_NOT_SUPPORTED, "step_graph: circuit models run only in picgpu_step");
-    if (c && c->cfg.mcc.enabled && c->cfg.mcc.neutral_parcels)
+    if (c && ((c->cfg.mcc.enabled && c->cfg.mcc.neutral_parcels) ||
+              (c->cfg.ion_mcc.enabled && c->cfg.ion_mcc.neutral_parcels)))
         return bad(c, PICGPU_NOT_SUPPORTED, "step_graph: collisions with neutral parcels run only in picgpu_step");
     if (!c || nsteps < 0 || steps_per_graph <= 0 || nsteps % steps_per_graph) return PICGPU_INVALID_ARG;
     if (!c->mixed || c->cfg.maxwell_solver != PICGPU_MAXWELL_NONE)
