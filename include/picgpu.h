@@ -200,7 +200,11 @@ typedef struct {
     int32_t neutral_parcels;        /* 1: collide with the parcels of neutral_species */
     int32_t neutral_species;        /* species of the neutral parcels (charge 0) */
     int32_t keep_neutral_velocity;  /* updateNeutralVelocity false */
-    int32_t pad2;
+    /* WeightCorrection of an elastic ion-neutral parcel pair
+     * (IonNeutralCollisionModel.C:443-444, applied after the isotropic
+     * scatter and before the updateNeutralVelocity reset):
+     * PICGPU_WEIGHT_CORRECTION_* (none, Nanbu, SentokuKempNR, SentokuKemp). */
+    int32_t weight_correction;
 } picgpu_ion_mcc;
 
 /* Binary Coulomb collisions (CoulombCollisionModel.C:241-309). */
@@ -385,6 +389,16 @@ typedef struct {
     double  circuit_current;                    /* circuitRLC: circuit current; IdealVoltageSource: mean anode current */
     double  circuit_cathode_current;            /* IdealVoltageSource: mean cathode current */
     double  circuit_charge;                     /* circuitRLC: capacitor charge Q; IdealCurrentSource: cathode surface charge */
+    /* Collisions with neutral parcels, counted apart from the background-gas
+     * collisions above (picFoam reports performCollisions and
+     * performBackgroundCollisions separately). */
+    int64_t mcc_parcel_candidates;              /* electron - neutral parcel pairs tested */
+    int64_t mcc_parcel_elastic;
+    int64_t mcc_parcel_excitation;
+    int64_t mcc_parcel_ionization;
+    int64_t ion_parcel_candidates;              /* ion - neutral parcel pairs tested */
+    int64_t ion_parcel_elastic;
+    int64_t ion_parcel_charge_exchange;
 } picgpu_step_stats;
 
 typedef struct picgpu_ctx picgpu_ctx;

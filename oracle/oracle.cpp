@@ -1229,12 +1229,15 @@ void mcc_parcels(Oracle& o, std::vector<std::vector<std::vector<int>>>& occ, pic
     if (mc.ion_species >= 0 && mc.create_ion)
         for (auto& p : new_i) o.cloud[mc.ion_species].push_back(p);
     if (st) {
-        st->mcc_candidates += cand;
-        st->mcc_elastic += nel;
-        st->mcc_excitation += nex;
-        st->mcc_ionization += niz;
+        st->mcc_parcel_candidates += cand;
+        st->mcc_parcel_elastic += nel;
+        st->mcc_parcel_excitation += nex;
+        st->mcc_parcel_ionization += niz;
     }
 }
+
+void weight_correct_pair(int model, double wP, double wQ, double mP, double mQ, const V3& preP, const V3& preQ,
+                         V3& UP, V3& UQ, ocoll::Philox& r);
 
 // IonNeutralCollisionModel::performCollisions (IonNeutralCollisionModel.C:
 // 579-707): ions with the neutral parcels of the cell, isotropic elastic
@@ -1280,6 +1283,7 @@ void ion_parcels(Oracle& o, std::vector<std::vector<std::vector<int>>>& occ, pic
             if (rndU <= Qel * cR / sv) {
                 nel++;
                 const V3 preUP = P.U;
+                const V3 preUQ = Q.U;
                 const V3 Ucm = v3((mn * P.U.x + mi * Q.U.x) / mt, (mn * P.U.y + mi * Q.U.y) / mt,
                                   (mn * P.U.z + mi * Q.U.z) / mt);
                 const double cr = magv(sub(P.U, Q.U));
@@ -1289,6 +1293,10 @@ void ion_parcels(Oracle& o, std::vector<std::vector<std::vector<int>>>& occ, pic
                 const V3 rel = v3(cr * cosT, cr * (sinT * std::cos(phi)), cr * (sinT * std::sin(phi)));
                 P.U = v3(Ucm.x + rel.x * mi / mt, Ucm.y + rel.y * mi / mt, Ucm.z + rel.z * mi / mt);
                 Q.U = v3(Ucm.x - rel.x * mn / mt, Ucm.y - rel.y * mn / mt, Ucm.z - rel.z * mn / mt);
+                // weightCorrection_->correctVelocity(pP, pQ, preUp, preUq)
+                // (IonNeutralCollisionModel.C:443-444), before the
+                // updateNeutralVelocity reset
+                weight_correct_pair(im.weight_correction, wN, wI, mn, mi, preUP, preUQ, P.U, Q.U, r);
                 if (!update_neutral) P.U = preUP;
             } else if (eV >= im.cx_threshold && rndU <= Qt * cR / sv) {
                 ncx++;
@@ -1301,9 +1309,9 @@ void ion_parcels(Oracle& o, std::vector<std::vector<std::vector<int>>>& occ, pic
         }
     }
     if (st) {
-        st->ion_mcc_candidates += cand;
-        st->ion_mcc_elastic += nel;
-        st->ion_mcc_charge_exchange += ncx;
+        st->ion_parcel_candidates += cand;
+        st->ion_parcel_elastic += nel;
+        st->ion_parcel_charge_exchange += ncx;
     }
 }
 

@@ -97,7 +97,7 @@ class IonMcc(C.Structure):
         ("xs_energy", C.POINTER(C.c_double)), ("xs_elastic", C.POINTER(C.c_double)),
         ("xs_charge_exchange", C.POINTER(C.c_double)),
         ("neutral_parcels", C.c_int32), ("neutral_species", C.c_int32), ("keep_neutral_velocity", C.c_int32),
-        ("pad2", C.c_int32),
+        ("weight_correction", C.c_int32),
     ]
 
 
@@ -257,6 +257,10 @@ class StepStats(C.Structure):
         ("binary_background_candidates", C.c_int64), ("binary_background_collisions", C.c_int64),
         ("circuit_voltage", C.c_double), ("circuit_current", C.c_double),
         ("circuit_cathode_current", C.c_double), ("circuit_charge", C.c_double),
+        ("mcc_parcel_candidates", C.c_int64), ("mcc_parcel_elastic", C.c_int64),
+        ("mcc_parcel_excitation", C.c_int64), ("mcc_parcel_ionization", C.c_int64),
+        ("ion_parcel_candidates", C.c_int64), ("ion_parcel_elastic", C.c_int64),
+        ("ion_parcel_charge_exchange", C.c_int64),
     ]
 
     def as_dict(self):

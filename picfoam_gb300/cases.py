@@ -264,14 +264,19 @@ def electron_swarm(nx=32, ny=32, nz=256, N=10_000_000, Ez=1e4, gas_density=1e21,
 
 def neutral_parcel_ionization(n_cells=(4, 4, 4), L=1e-3, per_cell=(20, 40), T_e_eV=100.0, T_n=300.0, n_n=1e20,
                               sigma_iz=3.43943e-20, threshold=15.76, dt=1e-11, seed=1234, precision=abi.PREC_FP64,
-                              keep_neutrals=False, keep_neutral_velocity=False, exact_max=True):
+                              keep_neutrals=False, keep_neutral_velocity=False, exact_max=True, ions_per_cell=0,
+                              ion_collisions=None):
     """The ionization tutorial's collision set-up: electrons, neutral Ar
     parcels and Ar+ with equal weights in a periodic box, MaxwellSolver
     none, electron-neutral MCC against the parcels (performCollisions) with
     a FixedValue ionisation cross section (threshold 15.76 eV), no elastic or
     excitation.  per_cell = (electrons, neutrals); electrons monoenergetic at
     T_e_eV (isotropic directions).  exact_max starts (sigma c_R)_max at
-    sigma_iz times the electron speed."""
+    sigma_iz times the electron speed.  ions_per_cell places Ar+ parcels at
+    the start (1 eV Maxwellian); ion_collisions = (sigma_el, sigma_cx) adds
+    ion collisions with the same neutral parcels (IonNeutralCollisionModel
+    performCollisions, which runs after the electron step and sees the lists
+    without the neutrals that step ionised and deleted)."""
     sides = [patch(abi.PATCH_CYCLIC) for _ in range(6)]
     mesh = block_mesh(n_cells, (L,) * 3, sides)
     n_c = n_cells[0] * n_cells[1] * n_cells[2]
@@ -305,30 +310,52 @@ def neutral_parcel_ionization(n_cells=(4, 4, 4), L=1e-3, per_cell=(20, 40), T_e_
     mc.neutral_species = 1
     mc.keep_neutrals = 1 if keep_neutrals else 0
     mc.keep_neutral_velocity = 1 if keep_neutral_velocity else 0
+    if ion_collisions is not None:
+        iarrs = [np.ascontiguousarray(a, dtype=np.float64)
+                 for a in ([0.0, 1e6], [ion_collisions[0]] * 2, [ion_collisions[1]] * 2)]
+        arrs = arrs + iarrs
+        im = cfg.ion_mcc
+        im.enabled = 1
+        im.ion_species = 2
+        im.n_xs = 2
+        im.cx_threshold = 0.0
+        im.sigma_v_max_init = (ion_collisions[0] + ion_collisions[1]) * math.sqrt(2 * E_CHARGE * 10.0 / M_AR)
+        im.xs_energy, im.xs_elastic, im.xs_charge_exchange = [
+            a.ctypes.data_as(C.POINTER(C.c_double)) for a in iarrs]
+        im.neutral_parcels = 1
+        im.neutral_species = 1
+        im.keep_neutral_velocity = 1 if keep_neutral_velocity else 0
     rng = np.random.Generator(np.random.Philox(seed))
     te, be = uniform_in_cells(rng, np.arange(n_c), per_cell[0])
     d = rng.standard_normal((len(te), 3))
     Ue = v_e * d / np.linalg.norm(d, axis=1)[:, None]
     tn, bn = uniform_in_cells(rng, np.arange(n_c), per_cell[1])
     Un = rng.standard_normal((len(tn), 3)) * math.sqrt(K_B * T_n / M_AR)
-    parts = {0: (te, be, Ue), 1: (tn, bn, Un), 2: (np.zeros(0, np.int32), np.zeros((0, 3)), np.zeros((0, 3)))}
+    if ions_per_cell:
+        ti, bi = uniform_in_cells(rng, np.arange(n_c), ions_per_cell)
+        ions = (ti, bi, rng.standard_normal((len(ti), 3)) * math.sqrt(E_CHARGE * 1.0 / M_AR))
+    else:
+        ions = (np.zeros(0, np.int32), np.zeros((0, 3)), np.zeros((0, 3)))
+    parts = {0: (te, be, Ue), 1: (tn, bn, Un), 2: ions}
     return Case("neutral_parcel_ionization", mesh, cfg, parts, arrs,
                 dict(w=w, v_e=v_e, n_n=n_n, V=L ** 3, N_e=len(te), N_n=len(tn), n_c=n_c))
 
 
 def ion_neutral_parcels(n_cells=(4, 4, 4), L=1e-3, per_cell=(30, 30), T_i_eV=5.0, T_n=300.0, n_n=1e22,
                         sigma_el=5e-19, sigma_cx=3e-19, dt=2e-9, seed=1234, precision=abi.PREC_FP64,
-                        keep_neutral_velocity=False):
-    """Ar+ ions and neutral Ar parcels of equal weight in a periodic box,
-    MaxwellSolver none, IonNeutralCollisionModel against the parcels
-    (performCollisions) with constant elastic and charge-exchange cross
-    sections.  per_cell = (ions, neutrals)."""
+                        keep_neutral_velocity=False, ion_weight_ratio=1.0, weight_correction=0):
+    """Ar+ ions and neutral Ar parcels in a periodic box, MaxwellSolver none,
+    IonNeutralCollisionModel against the parcels (performCollisions) with
+    constant elastic and charge-exchange cross sections.  per_cell = (ions,
+    neutrals); the ion weight is ion_weight_ratio times the neutral weight,
+    and weight_correction (PICGPU_WEIGHT_CORRECTION_*) corrects elastic pairs
+    of unequal weight."""
     sides = [patch(abi.PATCH_CYCLIC) for _ in range(6)]
     mesh = block_mesh(n_cells, (L,) * 3, sides)
     n_c = n_cells[0] * n_cells[1] * n_cells[2]
     w = n_n * L ** 3 / (n_c * per_cell[1])
-    cfg = base_config(dt, [(M_AR, 0.0, w, True), (M_AR, E_CHARGE, w, True)], maxwell=abi.MAXWELL_NONE,
-                      precision=precision, seed=seed, electron_species=-1)
+    cfg = base_config(dt, [(M_AR, 0.0, w, True), (M_AR, E_CHARGE, w * ion_weight_ratio, True)],
+                      maxwell=abi.MAXWELL_NONE, precision=precision, seed=seed, electron_species=-1)
     mc = cfg.mcc
     mc.gas_density = 0.0
     mc.gas_mass = M_AR
@@ -347,6 +374,7 @@ def ion_neutral_parcels(n_cells=(4, 4, 4), L=1e-3, per_cell=(30, 30), T_i_eV=5.0
     im.neutral_parcels = 1
     im.neutral_species = 0
     im.keep_neutral_velocity = 1 if keep_neutral_velocity else 0
+    im.weight_correction = weight_correction
     rng = np.random.Generator(np.random.Philox(seed))
     tn, bn = uniform_in_cells(rng, np.arange(n_c), per_cell[1])
     Un = rng.standard_normal((len(tn), 3)) * math.sqrt(K_B * T_n / M_AR)

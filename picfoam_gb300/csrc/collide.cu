@@ -494,6 +494,7 @@ struct MccParcelParams {
     long stage_cap;
     int* overflow;
     unsigned long long* counts;
+    int* n_live;          // per cell: neutral parcels left in the list at the end (read by the ion step)
 };
 
 __device__ __forceinline__ long parcel_candidates(const MccParcelParams& M, int c, double* sel) {
@@ -527,6 +528,7 @@ __global__ void mcc_parcel_kernel(MccParcelParams M, DSpecies el, DSpecies neu, 
     const long nCand = parcel_candidates(M, c, &selected);
     const int eC = M.e_start[c + 1] - M.e_start[c];
     int nC = M.n_start[c + 1] - M.n_start[c];
+    M.n_live[c] = nC;
     const double sv = M.svmax[c];
     if (!(sv > 0.0) || nC == 0 || eC == 0) return;
     M.rem[c] = selected - double(nCand);
@@ -626,10 +628,13 @@ __global__ void mcc_parcel_kernel(MccParcelParams M, DSpecies el, DSpecies neu, 
     if (room)
         for (; i < nCand; ++i) stage[base + i].flag = 0;   // candidates left after the last neutral went
     (void)ncand;
-    atomicAdd(M.counts + 0, (unsigned long long)nCand);
-    if (nel) atomicAdd(M.counts + 1, nel);
-    if (nex) atomicAdd(M.counts + 2, nex);
-    if (niz) atomicAdd(M.counts + 3, niz);
+    // the ion - neutral parcel step reads this cell's list through the live
+    // count: deleted neutrals were erased from it in place
+    M.n_live[c] = nC;
+    atomicAdd(M.counts + kCountMccParcel, (unsigned long long)nCand);
+    if (nel) atomicAdd(M.counts + kCountMccParcel + 1, nel);
+    if (nex) atomicAdd(M.counts + kCountMccParcel + 2, nex);
+    if (niz) atomicAdd(M.counts + kCountMccParcel + 3, niz);
     if (ndel) atomicAdd(M.counts + 12, ndel);
 }
 
@@ -685,17 +690,22 @@ struct IonParcelParams {
     int n_xs;
     double mi, mn, dt, wI, wN, wmax, cx_th;
     int update_neutral;
+    int weight_corr;      // PICGPU_WEIGHT_CORRECTION_* after an elastic scatter
     uint64_t seed;
     uint32_t step;
     unsigned long long* counts;
+    const int* n_live;    // when set: live neutral parcels per cell (the electron step erased the ionised ones)
 };
+
+__device__ void weight_correct_pair(int model, double wP, double wQ, double mP, double mQ, V3d preP, V3d preQ,
+                                    V3d& UP, V3d& UQ, Rng& r);
 
 template <class R>
 __global__ void ion_parcel_kernel(IonParcelParams M, DSpecies ions, DSpecies neu) {
     const int c = blockIdx.x * blockDim.x + threadIdx.x;
     if (c >= M.n_cells) return;
     const int iC = M.i_start[c + 1] - M.i_start[c];
-    const int nC = M.n_start[c + 1] - M.n_start[c];
+    const int nC = M.n_live ? M.n_live[c] : M.n_start[c + 1] - M.n_start[c];
     if (nC == 0 || iC == 0) return;
     const double sv = M.svmax[c];
     const double selected = M.rem[c] + double(nC * iC) * M.wmax * sv * M.dt / M.vol[c];
@@ -730,6 +740,7 @@ __global__ void ion_parcel_kernel(IonParcelParams M, DSpecies ions, DSpecies neu
         if (rndU <= Qel * cR / sv) {
             nel++;
             const V3d preUP = UP;
+            const V3d preUQ = UQ;
             const V3d Ucm = {(M.mn * UP.x + M.mi * UQ.x) / mt, (M.mn * UP.y + M.mi * UQ.y) / mt,
                              (M.mn * UP.z + M.mi * UQ.z) / mt};
             const V3d g = {UP.x - UQ.x, UP.y - UQ.y, UP.z - UQ.z};
@@ -740,6 +751,8 @@ __global__ void ion_parcel_kernel(IonParcelParams M, DSpecies ions, DSpecies neu
             const V3d rel = {cr * cosT, cr * (sinT * cos(phi)), cr * (sinT * sin(phi))};
             UP = {Ucm.x + rel.x * M.mi / mt, Ucm.y + rel.y * M.mi / mt, Ucm.z + rel.z * M.mi / mt};
             UQ = {Ucm.x - rel.x * M.mn / mt, Ucm.y - rel.y * M.mn / mt, Ucm.z - rel.z * M.mn / mt};
+            // weightCorrection_->correctVelocity(pP, pQ, preUp, preUq) (:443-444)
+            weight_correct_pair(M.weight_corr, M.wN, M.wI, M.mn, M.mi, preUP, preUQ, UP, UQ, r);
             if (!M.update_neutral) UP = preUP;
             Vel<R>::put(neu, pp, UP);
             Vel<R>::put(ions, pq, UQ);
@@ -754,9 +767,9 @@ __global__ void ion_parcel_kernel(IonParcelParams M, DSpecies ions, DSpecies neu
             Vel<R>::put(ions, pq, UQ);
         }
     }
-    atomicAdd(M.counts + 5, (unsigned long long)nCand);
-    if (nel) atomicAdd(M.counts + 6, nel);
-    if (ncx) atomicAdd(M.counts + 7, ncx);
+    atomicAdd(M.counts + kCountIonParcel, (unsigned long long)nCand);
+    if (nel) atomicAdd(M.counts + kCountIonParcel + 1, nel);
+    if (ncx) atomicAdd(M.counts + kCountIonParcel + 2, ncx);
 }
 
 // --------------------------------------------------------- ion-neutral ---
@@ -1615,6 +1628,10 @@ int collide_init(CollideState& st, const picgpu_config& cfg, const DMesh& m, cud
                                       nc, s, msg);
             if (e2) return e2;
             cudaFree(xs_unused);
+            if (dmalloc(&st.n_live, nc)) {
+                *msg = "MCC: device allocation failed";
+                return PICGPU_OOM;
+            }
         }
     }
     if (cfg.ion_mcc.enabled) {
@@ -1655,6 +1672,11 @@ int collide_init(CollideState& st, const picgpu_config& cfg, const DMesh& m, cud
             const int ns = im.neutral_species;
             if (ns < 0 || ns >= cfg.n_species || cfg.species[ns].charge != 0.0 || cfg.binary.enabled) {
                 *msg = "ion MCC: neutral_species must name a species of charge 0 (and no BinaryCollisionModel)";
+                return PICGPU_INVALID_ARG;
+            }
+            if (im.weight_correction < PICGPU_WEIGHT_CORRECTION_NONE ||
+                im.weight_correction > PICGPU_WEIGHT_CORRECTION_SENTOKU_KEMP) {
+                *msg = "ion MCC: unknown weight-correction model";
                 return PICGPU_INVALID_ARG;
             }
             double* xs_unused = nullptr;
@@ -1722,7 +1744,8 @@ void collide_free(CollideState& st) {
     void* ptrs[] = {st.svmax,      st.remainder,   st.xs,     st.isvmax,   st.iremainder, st.ixs,
                     st.cell_start, st.cell_count,  st.cell_cursor, st.counts, st.scan_tmp, st.ncand,
                     st.cand_off,   st.stage,       st.flags,  st.pos,      st.stage_tmp, st.overflow,
-                    st.iz_cell,    st.bsmax,       st.brem,   st.bbgrem,   st.blist,      st.boct};
+                    st.iz_cell,    st.bsmax,       st.brem,   st.bbgrem,   st.blist,      st.boct,
+                    st.psvmax,     st.premainder,  st.ipsvmax, st.ipremainder, st.n_live};
     for (void* p : ptrs)
         if (p) cudaFree(p);
     for (int s = 0; s < PICGPU_MAX_SPECIES; ++s) {
@@ -2094,6 +2117,7 @@ int mcc_parcels(CollideState& st, const CollideArgs& a, long newn[], std::string
     M.step = uint32_t(a.step);
     M.counts = st.counts;
     M.overflow = st.overflow;
+    M.n_live = st.n_live;
     mcc_parcel_count_kernel<<<(nc + 255) / 256, 256, 0, a.stream>>>(M, st.ncand);
     exclusive_scan(st.ncand, st.cand_off, nc, st.scan_tmp, a.stream, launches);
     int total = 0;
@@ -2221,9 +2245,14 @@ int run_collisions(CollideState& st, const CollideArgs& a, int64_t counts[kColli
         M.wmax = std::max(M.wN, M.wI);
         M.cx_th = cfg.ion_mcc.cx_threshold;
         M.update_neutral = cfg.ion_mcc.keep_neutral_velocity ? 0 : 1;
+        M.weight_corr = cfg.ion_mcc.weight_correction;
         M.seed = cfg.seed;
         M.step = uint32_t(a.step);
         M.counts = st.counts;
+        // after electron - parcel collisions on the same neutral species the
+        // lists hold only the neutrals that were not ionised and deleted
+        // (sortedCellOccupancy is erased in place, ElectronNeutralCollisionModel.C:959-963)
+        M.n_live = (cfg.mcc.enabled && cfg.mcc.neutral_parcels && cfg.mcc.neutral_species == ns) ? st.n_live : nullptr;
         if (a.mixed) ion_parcel_kernel<float><<<(nc + st.mcc_block - 1) / st.mcc_block, st.mcc_block, 0, a.stream>>>(M, a.sp[is], a.sp[ns]);
         else ion_parcel_kernel<double><<<(nc + st.mcc_block - 1) / st.mcc_block, st.mcc_block, 0, a.stream>>>(M, a.sp[is], a.sp[ns]);
         *launches += 1;

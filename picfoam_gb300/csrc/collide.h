@@ -22,11 +22,16 @@ struct Secondary {
     double y_i[3];
 };
 
-// Counters of one collision step: MCC candidates, elastic, excitation,
-// ionisation; Coulomb pairs; ion MCC candidates, elastic, charge exchange;
-// binary (neutral) pairs tested, collisions; background tests, collisions;
-// neutral parcels deleted by ionisation.
-constexpr int kCollideCounts = 13;
+// Counters of one collision step: background MCC candidates, elastic,
+// excitation, ionisation (0-3); Coulomb pairs (4); ion background MCC
+// candidates, elastic, charge exchange (5-7); binary (neutral) pairs tested,
+// collisions; background tests, collisions (8-11); neutral parcels deleted
+// by ionisation (12); electron - neutral parcel candidates, elastic,
+// excitation, ionisation (13-16); ion - neutral parcel candidates, elastic,
+// charge exchange (17-19).
+constexpr int kCollideCounts = 20;
+constexpr int kCountMccParcel = 13;
+constexpr int kCountIonParcel = 17;
 
 // Device state owned by the collision step.
 struct CollideState {
@@ -63,6 +68,7 @@ struct CollideState {
     double* premainder = nullptr;           // and its collision remainder per cell
     double* ipsvmax = nullptr;              // ion - neutral parcel (sigma_T c_R)_max per cell
     double* ipremainder = nullptr;
+    int* n_live = nullptr;                  // neutral parcels per cell left after the electron - parcel step
     int mcc_block = 128;                    // threads per block of the MCC kernel (one cell each)
     unsigned long long* iz_cell = nullptr;  // MCC ionisations per cell (accumulated)
     // BinaryCollisionModel: (sigma_T c_r)_max, selection and background

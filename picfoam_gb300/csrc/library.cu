@@ -1103,6 +1103,13 @@ picgpu_status pgd_collisions(picgpu_ctx* c, picgpu_step_stats* stats) {
         stats->binary_collisions += counts[9];
         stats->binary_background_candidates += counts[10];
         stats->binary_background_collisions += counts[11];
+        stats->mcc_parcel_candidates += counts[pgd::kCountMccParcel];
+        stats->mcc_parcel_elastic += counts[pgd::kCountMccParcel + 1];
+        stats->mcc_parcel_excitation += counts[pgd::kCountMccParcel + 2];
+        stats->mcc_parcel_ionization += counts[pgd::kCountMccParcel + 3];
+        stats->ion_parcel_candidates += counts[pgd::kCountIonParcel];
+        stats->ion_parcel_elastic += counts[pgd::kCountIonParcel + 1];
+        stats->ion_parcel_charge_exchange += counts[pgd::kCountIonParcel + 2];
     }
     return PICGPU_OK;
 }

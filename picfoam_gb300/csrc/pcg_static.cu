@@ -90,7 +90,10 @@ extern "C" picgpu_status picgpu_solve_ldu_noalloc(int n_cells, const double* dia
     m.dinv = dinv;
     pgd::launch_pcg_init(m, b, x, r, u, w, part, st, tol, s);
     pgd::PcgState h{};
-    if (cudaMemcpyAsync(&h, st, sizeof h, cudaMemcpyDeviceToHost, s) != cudaSuccess ||
+    // a launch error of the set-up kernels must not pass for convergence when
+    // the start guess already meets the tolerance and no iteration runs
+    if (cudaGetLastError() != cudaSuccess ||
+        cudaMemcpyAsync(&h, st, sizeof h, cudaMemcpyDeviceToHost, s) != cudaSuccess ||
         cudaStreamSynchronize(s) != cudaSuccess)
         return PICGPU_CUDA_ERROR;
     int k = 1, batch = 4;

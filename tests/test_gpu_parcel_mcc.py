@@ -25,8 +25,8 @@ def test_parcel_mcc_matches_oracle(gpu, oracle_backend, keep):
     o = cases.build(case, backend=oracle_backend.OracleBackend(1))
     for _ in range(3):
         sg, so = g.step(1), o.step(1)
-        assert (sg.mcc_candidates, sg.mcc_ionization) == (so.mcc_candidates, so.mcc_ionization)
-    assert sg.mcc_ionization > 20
+        assert (sg.mcc_parcel_candidates, sg.mcc_parcel_ionization) == (so.mcc_parcel_candidates, so.mcc_parcel_ionization)
+    assert sg.mcc_parcel_ionization > 20
     for s in (0, 1, 2):
         tg, bg, ug = g.get_particles(s)
         to, bo, uo = o.get_particles(s)
@@ -37,11 +37,40 @@ def test_parcel_mcc_matches_oracle(gpu, oracle_backend, keep):
             assert close.mean() > 0.999
 
 
+@pytest.mark.parametrize("precision", [abi.PREC_FP64, abi.PREC_MIXED])
+def test_ion_parcels_after_neutral_deletion_match_oracle(gpu, oracle_backend, precision):
+    # electron - parcel ionisation deletes neutrals, then the ion - parcel
+    # step draws from the same per-cell lists: its candidate count uses the
+    # neutrals left, and no deleted neutral is drawn
+    kw = dict(ions_per_cell=20, ion_collisions=(2e-17, 1e-17), n_n=3e22)
+    g = cases.build(make(precision=precision, **kw), backend=gpu)
+    o = cases.build(make(**kw), backend=oracle_backend.OracleBackend(1))
+    deleted = 0
+    for _ in range(3):
+        sg, so = g.step(1), o.step(1)
+        assert (sg.mcc_parcel_candidates, sg.ion_parcel_candidates) == \
+               (so.mcc_parcel_candidates, so.ion_parcel_candidates)
+        if precision == abi.PREC_FP64:
+            assert (sg.mcc_parcel_ionization, sg.ion_parcel_elastic, sg.ion_parcel_charge_exchange) == \
+                   (so.mcc_parcel_ionization, so.ion_parcel_elastic, so.ion_parcel_charge_exchange)
+        deleted += so.mcc_parcel_ionization
+        assert sg.mcc_candidates == 0 and sg.ion_mcc_candidates == 0    # no background gas
+    assert deleted > 100 and so.ion_parcel_elastic + so.ion_parcel_charge_exchange > 50
+    if precision != abi.PREC_FP64:
+        return
+    for s in (0, 1, 2):
+        tg, bg, ug = g.get_particles(s)
+        to, bo, uo = o.get_particles(s)
+        np.testing.assert_array_equal(tg, to)
+        close = np.isclose(ug, uo, rtol=1e-9, atol=1e-9 * max(np.abs(uo).max(), 1e-300)).all(axis=1)
+        assert close.mean() > 0.999
+
+
 def test_fp32_form_close_to_oracle(gpu, oracle_backend):
     g = cases.build(make(precision=abi.PREC_MIXED), backend=gpu)
     o = cases.build(make(), backend=oracle_backend.OracleBackend(1))
-    ng = sum(g.step(1).mcc_ionization for _ in range(2))
-    no = sum(o.step(1).mcc_ionization for _ in range(2))
+    ng = sum(g.step(1).mcc_parcel_ionization for _ in range(2))
+    no = sum(o.step(1).mcc_parcel_ionization for _ in range(2))
     assert abs(ng - no) <= 4 * np.sqrt(no) and no > 50
     assert g.count(2) == ng and g.count(1) == make().meta["N_n"] - ng
 

@@ -2,7 +2,11 @@
 (IonNeutralCollisionModel::performCollisions): events at the NTC rate,
 momentum and energy of the ion-neutral system kept by isotropic elastic
 scattering and charge exchange of equal masses, neutral velocities kept
-when updateNeutralVelocity is off."""
+when updateNeutralVelocity is off; with unequal weights the WeightCorrection
+of an elastic pair (IonNeutralCollisionModel.C:443-444): Nanbu keeps the
+heavier-weight ion's new velocity with probability w_n / w_i, Sentoku-Kemp
+keeps the weighted kinetic energy (momentum only on average: its
+perpendicular kick is random)."""
 import numpy as np
 import pytest
 
@@ -16,11 +20,11 @@ def run(oracle_backend, steps, **kw):
     return case, sim, stats
 
 
-def momentum_energy(sim, case):
+def momentum_energy(sim, case, weighted=False):
     P, K = np.zeros(3), 0.0
     for s in (0, 1):
         _, _, U = sim.get_particles(s)
-        m = case.cfg.species[s].mass
+        m = case.cfg.species[s].mass * (case.cfg.species[s].weight if weighted else 1.0)
         P += m * U.sum(axis=0)
         K += 0.5 * m * (U * U).sum()
     return P, K
@@ -31,10 +35,10 @@ def test_rate_and_conservation(oracle_backend):
     sim = cases.build(case, backend=oracle_backend.OracleBackend(1))
     P0, K0 = momentum_energy(sim, case)
     st = [sim.step(1) for _ in range(3)]
-    events = sum(s.ion_mcc_elastic + s.ion_mcc_charge_exchange for s in st)
-    cands = sum(s.ion_mcc_candidates for s in st)
+    events = sum(s.ion_parcel_elastic + s.ion_parcel_charge_exchange for s in st)
+    cands = sum(s.ion_parcel_candidates for s in st)
     assert events > 300 and cands >= events
-    assert sum(s.ion_mcc_elastic for s in st) > 0 and sum(s.ion_mcc_charge_exchange for s in st) > 0
+    assert sum(s.ion_parcel_elastic for s in st) > 0 and sum(s.ion_parcel_charge_exchange for s in st) > 0
     P1, K1 = momentum_energy(sim, case)
     scale = np.abs(P0).max() + 1e-30 + case.cfg.species[1].mass * 1e4 * 1920
     assert np.abs(P1 - P0).max() <= 1e-9 * scale
@@ -45,6 +49,48 @@ def test_neutral_velocity_kept_when_asked(oracle_backend):
     case, sim, st = run(oracle_backend, 0, keep_neutral_velocity=True)
     _, _, U0 = sim.get_particles(0)
     st = [sim.step(1) for _ in range(2)]
-    assert sum(s.ion_mcc_elastic for s in st) > 0
+    assert sum(s.ion_parcel_elastic for s in st) > 0
     _, _, U1 = sim.get_particles(0)
     np.testing.assert_array_equal(U0, U1)
+
+
+def test_nanbu_correction_of_unequal_weights(oracle_backend):
+    # ions of twice the neutral weight, elastic only: every neutral partner
+    # takes its new velocity (u > w_i / w_n never holds), an ion keeps its new
+    # one with probability w_n / w_i = 1/2.  Ions are pushed every step (the
+    # relativistic round trip moves their last bits), hence the tolerance.
+    case, sim, _ = run(oracle_backend, 0, ion_weight_ratio=2.0, sigma_cx=0.0, dt=1e-9, per_cell=(100, 100),
+                       n_n=3e22, weight_correction=abi.WEIGHT_CORRECTION_NANBU)
+    _, _, Un0 = sim.get_particles(0)
+    _, _, Ui0 = sim.get_particles(1)
+    st = sim.step(1)
+    _, _, Un1 = sim.get_particles(0)
+    _, _, Ui1 = sim.get_particles(1)
+
+    def changed(a, b):
+        return int((np.abs(a - b).max(axis=1) > 1e-6 * np.abs(b).max(axis=1)).sum())
+
+    nel = st.ion_parcel_elastic
+    n_changed, i_changed = changed(Un1, Un0), changed(Ui1, Ui0)
+    assert nel > 800
+    assert 0.85 * nel <= n_changed <= nel           # a neutral drawn twice counts once
+    assert abs(i_changed / n_changed - 0.5) < 0.08
+
+
+@pytest.mark.parametrize("model", [abi.WEIGHT_CORRECTION_SENTOKU_KEMP_NR, abi.WEIGHT_CORRECTION_SENTOKU_KEMP])
+def test_sentoku_kemp_correction_keeps_weighted_invariants(oracle_backend, model):
+    case, sim, _ = run(oracle_backend, 0, ion_weight_ratio=3.0, sigma_cx=0.0, weight_correction=model)
+    P0, K0 = momentum_energy(sim, case, weighted=True)
+    st = [sim.step(1) for _ in range(2)]
+    assert sum(s.ion_parcel_elastic for s in st) > 100
+    _, K1 = momentum_energy(sim, case, weighted=True)
+    # the relativistic form conserves gamma m c^2: at 5 eV argon the kinetic
+    # energy is 1e-10 of it, so its FP64 differences cancel to about 1e-6
+    assert K1 == pytest.approx(K0, rel=1e-8 if model == abi.WEIGHT_CORRECTION_SENTOKU_KEMP_NR else 1e-5)
+    _, Kn = momentum_energy(sim_without_correction(oracle_backend), case, weighted=True)
+    assert abs(Kn / K0 - 1) > 100 * abs(K1 / K0 - 1)
+
+
+def sim_without_correction(oracle_backend):
+    case, sim, _ = run(oracle_backend, 2, ion_weight_ratio=3.0, sigma_cx=0.0)
+    return sim

@@ -230,10 +230,11 @@ def test_time_directory_round_trip(tmp_path, oracle_backend):
     assert phi["source"]["value"] == ("uniform", 10.0) and phi["walls"]["type"] == "zeroGradient"
 
 
-REF = "/root/reference/tutorials"
+# picFoam's tutorials directory (PICFOAM_TUTORIALS=<picFoam source>/tutorials)
+REF = os.environ.get("PICFOAM_TUTORIALS", "")
 
 
-@pytest.mark.skipif(not os.path.isdir(REF), reason="reference tutorials not present")
+@pytest.mark.skipif(not REF or not os.path.isdir(REF), reason="PICFOAM_TUTORIALS is not set to picFoam's tutorials")
 @pytest.mark.parametrize("name,strict", [("plasmaOscillation", True), ("rlcCircuit", True), ("thermalization", True),
                                          ("thermalization_binaryCollision", True), ("floatingBoundary", False),
                                          ("ionization", True), ("magneticRotation", True),
@@ -261,13 +262,13 @@ def test_reference_tutorials_load(name, strict):
         assert c.mesh.side[1].kind == abi.PATCH_FLOATING and len(c.injections) == 1
 
 
-@pytest.mark.skipif(not os.path.isdir(REF), reason="reference tutorials not present")
+@pytest.mark.skipif(not REF or not os.path.isdir(REF), reason="PICFOAM_TUTORIALS is not set to picFoam's tutorials")
 def test_reference_gmsh_case_is_refused():
     with pytest.raises(ofcase.UnsupportedCase):
         ofcase.load_case(os.path.join(REF, "ionDriftVelocity"), allow_unsupported=True)
 
 
-@pytest.mark.skipif(not os.path.isdir(REF), reason="reference tutorials not present")
+@pytest.mark.skipif(not REF or not os.path.isdir(REF), reason="PICFOAM_TUTORIALS is not set to picFoam's tutorials")
 def test_reference_magnetic_rotation_gyrates(oracle_backend):
     # ParticleList: one electron at 0.1 c in B_z = 1 T; HigueraCary keeps the
     # gyration radius and the speed

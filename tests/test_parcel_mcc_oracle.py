@@ -28,9 +28,9 @@ def test_ionisation_rate(oracle_backend):
     st = sim.step(1)
     expect = m["N_e"] * m["n_n"] * SIGMA * m["v_e"] * case.cfg.dt
     assert expect > 50
-    assert abs(st.mcc_ionization - expect) < 4 * math.sqrt(expect)
+    assert abs(st.mcc_parcel_ionization - expect) < 4 * math.sqrt(expect)
     # every candidate is above threshold and (sigma c_R)_max is 1 % above sigma v
-    assert st.mcc_ionization <= st.mcc_candidates and st.mcc_ionization > 0.95 * st.mcc_candidates
+    assert st.mcc_parcel_ionization <= st.mcc_parcel_candidates and st.mcc_parcel_ionization > 0.95 * st.mcc_parcel_candidates
 
 
 @pytest.mark.parametrize("keep", [False, True])
@@ -39,7 +39,7 @@ def test_pairs_created_and_neutrals_deleted(oracle_backend, keep):
     m = case.meta
     total = 0
     for _ in range(3):
-        total += sim.step(1).mcc_ionization
+        total += sim.step(1).mcc_parcel_ionization
     assert total > 100
     assert sim.count(2) == total and sim.count(0) == m["N_e"] + total
     assert sim.count(1) == m["N_n"] - (0 if keep else total)
