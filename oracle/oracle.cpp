@@ -1220,11 +1220,19 @@ void mcc_parcels(Oracle& o, std::vector<std::vector<std::vector<int>>>& occ, pic
             }
         }
     }
-    // deleted neutrals leave the cloud in order
+    // deleted neutrals leave the cloud in order; the cell lists, which the
+    // ion - neutral parcel step reads next (picFoam's sortedCellOccupancy
+    // holds parcel pointers), follow the parcels to their new indices
     size_t w = 0;
+    std::vector<int> moved(neu.size(), -1);
     for (size_t k = 0; k < neu.size(); ++k)
-        if (neu[k].alive) neu[w++] = neu[k];
+        if (neu[k].alive) {
+            moved[k] = int(w);
+            neu[w++] = neu[k];
+        }
     neu.resize(w);
+    for (auto& list : occ[ns])
+        for (int& idx : list) idx = moved[idx];
     for (auto& p : new_e) el.push_back(p);
     if (mc.ion_species >= 0 && mc.create_ion)
         for (auto& p : new_i) o.cloud[mc.ion_species].push_back(p);

@@ -47,6 +47,19 @@ struct Tables32 {
     int kind[kMaxPatches];
 };
 
+// Cell-local geometry of the canonical hex for the FP32 in-cell mover, in
+// coordinates normalised by the cell size about the cell centre (the cell is
+// [-1/2, 1/2]^3; barycentric coordinates are affine invariants, so one set of
+// tables serves every axis-aligned uniform block mesh).
+struct CellTables32 {
+    float4 fwd[12][3];   // tet t, k = 0..2: corner tri[t][k] - centre (xyz)
+    float4 inv[12][3];   // tet t: y_{k+1} = dot(inv[t][k].xyz, x)
+    float4 diag[6];      // face f: normal of the plane through the centre and the face
+                         // diagonal tri[2f][0] - tri[2f][2]; dot(diag, x) >= 0 selects tet 2f
+    float4 dth;          // dt / cell size per axis (xyz)
+    float4 keep;         // 1 on solved axes, 0 on empty ones (tracking returns to the centre plane)
+};
+
 // Read-only mesh arrays on the device.
 struct DMesh {
     int n_cells, n_points, n_bfaces, n_classes;
@@ -106,6 +119,16 @@ struct MoveCounters {
     int pad;
 };
 
+// Particles that leave their cell in the FP32 in-cell mover wait for the
+// crossing tracker in a per-block segment: block b of the mover wrote
+// count[b] particle indices at queue[start[b] ...].
+struct CrossQueue {
+    int* queue;              // the species' idle double-buffer tet array (capacity >= n)
+    int* count;              // per mover block
+    int* start;
+    int capacity;            // blocks the count / start arrays hold
+};
+
 struct MoveParams {
     DMesh m;
     int n;                   // particles in this species (including removed slots)
@@ -134,6 +157,10 @@ struct MoveParams {
     float dt_f;
     float B_f[3];
     float centre_f[3];
+    const Tables32* t32;          // FP32 form: tables of this context's mesh (device memory)
+    const CellTables32* ct32;     // FP32 form: in-cell mover tables (uniform block meshes)
+    CrossQueue xq;                // FP32 form: particles at reflecting patches (queue null: general kernel only)
+    int reflecting;               // a patch reflects this species (wall, or a circuit electrode for neutrals)
     unsigned long long* acc9;     // this species' 2^-kDepositBits fixed-point deposit per cell: centre + 8 corners
     const float4* Ec4;            // E per cell: centre + 8 corners (FP32 form)
     const double* E;         // 3 n_cells

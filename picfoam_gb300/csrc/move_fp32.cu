@@ -4,25 +4,34 @@
 // PICMCCFVM/parcels/Templates/PICParcel/PICParcel.C:38-144), laid out for
 // throughput rather than for bit-exact agreement with the oracle:
 //   * barycentric coordinates and velocity in FP32, fast-math intrinsics;
-//   * one flat loop of tet steps: after an internal or cyclic cell-face
-//     crossing the particle continues with the unused fraction of the same
-//     displacement (the FP64 form recomputes f dt U - d, which is the same
-//     vector); the displacement is recomputed only after a wall reflection;
-//   * a tet step first tries the common case "no coordinate reaches zero"
-//     (no division); the hit search runs only when one does;
+//   * on a uniform block mesh, the in-cell mover (move_cell_kernel_fp32)
+//     pushes every particle, moves it in cell coordinates normalised by the
+//     cell size and, when the end point lies in the same cell, finds its tet
+//     directly: the face pyramid from the dominant coordinate, the side of the
+//     face diagonal from one dot product.  Crossings of the tet faces inside a
+//     cell are no events of the physics (no patch, no field change), so this
+//     is the barycentric tracker's end state without its per-face loop, and
+//     every lane of a warp runs the same instructions.  A particle whose end
+//     point lies outside its cell is queued with its pushed velocity, and the
+//     crossing tracker (track_queue_kernel_fp32) follows it face by face with
+//     the barycentric tracker below, patches included, on full warps;
+//   * the general kernel (move_kernel_fp32) serves meshes of several cell
+//     shapes: one flat loop of tet steps; after an internal or cyclic
+//     cell-face crossing the particle continues with the unused fraction of
+//     the same displacement (the FP64 form recomputes f dt U - d, which is the
+//     same vector); a tet step first tries the common case "no coordinate
+//     reaches zero" (no division); the hit search runs only when one does;
 //   * E at the particle from a per-cell block of 9 float4 (centre + 8
 //     corners), so the gather needs no cell -> point indirection;
 //   * tet geometry and the tet-crossing tables of the canonical hex in shared
 //     memory (lanes index them by different tets; constant memory would
-//     serialise that);
+//     serialise that), copied from the context's own device tables;
 //   * charge deposited as 2^-25 fixed-point weights into per-cell corner slots
 //     (order-independent integer sums), reduced to points by the charge update.
 #include "kernels.h"
 #include "move_impl.cuh"
 
 namespace pgd {
-
-__constant__ Tables32 c_t32;
 
 namespace {
 
@@ -36,14 +45,14 @@ struct S32 {
     float U[3];
 };
 
-__device__ __forceinline__ void field32(const MoveParams& P, const Tables32& T, const S32& s, float* E) {
+__device__ __forceinline__ void field32(const MoveParams& P, const unsigned* tri_of, const S32& s, float* E) {
     const float4* e = P.Ec4 + 9 * s.cell;
     const float4 a = __ldg(e);
     if (P.field_weighting == PICGPU_WEIGHTING_CELL_AVERAGE) {
         E[0] = a.x; E[1] = a.y; E[2] = a.z;
         return;
     }
-    const unsigned tri = T.tri[s.tet];
+    const unsigned tri = tri_of[s.tet];
     const float4 b = __ldg(e + 1 + (tri & 15u));
     const float4 c = __ldg(e + 1 + ((tri >> 4) & 15u));
     const float4 d = __ldg(e + 1 + ((tri >> 8) & 15u));
@@ -81,9 +90,9 @@ __device__ __forceinline__ void boris32(const MoveParams& P, const float* E, flo
 }
 
 template <int PUSHER>
-__device__ __forceinline__ void push32(const MoveParams& P, const Tables32& T, S32& s, float tt) {
+__device__ __forceinline__ void push32(const MoveParams& P, const unsigned* tri_of, S32& s, float tt) {
     float E[3];
-    field32(P, T, s, E);
+    field32(P, tri_of, s, E);
     if (PUSHER == PICGPU_PUSHER_BORIS) boris32(P, E, s.U, tt);
     else if (PUSHER == PICGPU_PUSHER_BORIS_NR) push_boris_nr<float>(P, E, s.U, tt);
     else if (PUSHER == PICGPU_PUSHER_VAY) push_vay<float>(P, E, s.U, tt);
@@ -126,7 +135,7 @@ struct Tally {
 // the particle reached the speed of light (it is then removed).
 template <int PUSHER>
 __device__ __forceinline__ bool push_phase(const MoveParams& P, const Tables32& T, S32& s, Tally& td) {
-    if (P.charged) push32<PUSHER>(P, T, s, P.dt_f);
+    if (P.charged) push32<PUSHER>(P, T.tri, s, P.dt_f);
     if (!(s.U[0] * s.U[0] + s.U[1] * s.U[1] + s.U[2] * s.U[2] < float(kC) * float(kC))) {
         td.keep = false;
         atomicMax(&P.counters->error, int(PICGPU_SPEED_OF_LIGHT));
@@ -217,7 +226,7 @@ __device__ __forceinline__ void track32(const MoveParams& P, const Tables32& T, 
             P.m.uniform ? T.normal + 3 * f : P.m.fnormal32 + size_t(P.m.cell_class[s.cell]) * 18 + 3 * f;
         const bool wall = kind == PICGPU_PATCH_WALL || kind == PICGPU_PATCH_CIRCUIT;
         if (wall) {
-            if (P.sync && P.charged) push32<PUSHER>(P, T, s, (sf - 0.5f) * dt);
+            if (P.sync && P.charged) push32<PUSHER>(P, T.tri, s, (sf - 0.5f) * dt);
             td.walls++;
         }
         const float Un = s.U[0] * n[0] + s.U[1] * n[1] + s.U[2] * n[2];
@@ -227,7 +236,7 @@ __device__ __forceinline__ void track32(const MoveParams& P, const Tables32& T, 
             s.U[1] -= t * n[1];
             s.U[2] -= t * n[2];
         }
-        if (wall && ++resync <= 1 && P.sync && P.charged) push32<PUSHER>(P, T, s, (0.5f - sf) * dt);
+        if (wall && ++resync <= 1 && P.sync && P.charged) push32<PUSHER>(P, T.tri, s, (0.5f - sf) * dt);
         base = sf;
         rem = 1.f;
         displacement(P, T, s, (1.f - sf) * dt, disp);
@@ -249,14 +258,14 @@ __device__ __forceinline__ void win_add(unsigned* slot, unsigned long long* gslo
     if (old + v < old) atomicAdd(gslot, 1ull << 32);
 }
 
-__device__ __forceinline__ void deposit32(const MoveParams& P, const Tables32& T, const S32& s, int w0,
+__device__ __forceinline__ void deposit32(const MoveParams& P, const unsigned* tri_of, const S32& s, int w0,
                                           unsigned* win) {
     if (!P.has_value) return;
     constexpr float kScale = float(1u << kDepositBits);
     const int rel = s.cell - w0;
     unsigned long long* g = P.acc9 + 9 * size_t(s.cell);
     const bool average = P.charge_distribution == PICGPU_WEIGHTING_CELL_AVERAGE;
-    const unsigned tri = T.tri[s.tet];
+    const unsigned tri = tri_of[s.tet];
     const unsigned w0v = average ? (1u << kDepositBits) : __float2uint_rn(s.y[0] * kScale);
     if (unsigned(rel) < unsigned(kWindow)) {
         unsigned* a = win + 9 * rel;
@@ -312,7 +321,7 @@ __global__ void __launch_bounds__(256, 5) move_kernel_fp32(MoveParams P, int chu
     const int end = min(n_end, start + ch);
     if (start >= end) return;  // block-uniform: nothing to move (e.g. no secondaries this step)
     {
-        const unsigned* src = reinterpret_cast<const unsigned*>(&c_t32);
+        const unsigned* src = reinterpret_cast<const unsigned*>(P.t32);
         unsigned* dst = reinterpret_cast<unsigned*>(&T);
         for (int k = threadIdx.x; k < int(sizeof(Tables32) / 4); k += blockDim.x) dst[k] = src[k];
         for (int k = threadIdx.x; k < kWindow * 9; k += blockDim.x) win[k] = 0u;
@@ -367,7 +376,7 @@ __global__ void __launch_bounds__(256, 5) move_kernel_fp32(MoveParams P, int chu
             __stcs(P.p.u32[1] + ci, s.U[1]);
             __stcs(P.p.u32[2] + ci, s.U[2]);
         }
-        deposit32(P, T, s, w0, win);
+        deposit32(P, T.tri, s, w0, win);
     }
     __syncthreads();
     // flush the window
@@ -385,16 +394,318 @@ __global__ void __launch_bounds__(256, 5) move_kernel_fp32(MoveParams P, int chu
     warp_add_counter<float>(&P.counters->absorbed, ab);
 }
 
+// ------------------------------------------------------ in-cell mover ---
 
+// The tet of the canonical hex holding the cell-local point x (normalised
+// coordinates, |x_a| <= 1/2) and the point's barycentric coordinates there.
+__device__ __forceinline__ void cell_locate(const CellTables32& G, float x0, float x1, float x2, S32& s) {
+    const float a0 = fabsf(x0), a1 = fabsf(x1), a2 = fabsf(x2);
+    int f;
+    if (a0 >= a1 && a0 >= a2) f = x0 > 0.f ? 1 : 0;
+    else if (a1 >= a2) f = x1 > 0.f ? 3 : 2;
+    else f = x2 > 0.f ? 5 : 4;
+    const float4 dg = G.diag[f];
+    const int t = 2 * f + (dg.x * x0 + dg.y * x1 + dg.z * x2 >= 0.f ? 0 : 1);
+    const float4 i0 = G.inv[t][0], i1 = G.inv[t][1], i2 = G.inv[t][2];
+    s.tet = t;
+    s.y[1] = i0.x * x0 + i0.y * x1 + i0.z * x2;
+    s.y[2] = i1.x * x0 + i1.y * x1 + i1.z * x2;
+    s.y[3] = i2.x * x0 + i2.y * x1 + i2.z * x2;
+    s.y[0] = 1.f - s.y[1] - s.y[2] - s.y[3];
+}
+
+__device__ __forceinline__ void store_rec(const DSpecies& p, int i, const S32& s, int cell_tet) {
+    __stcs(p.tet + i, cell_tet);
+    __stcs(p.y32[0] + i, s.y[1]);
+    __stcs(p.y32[1] + i, s.y[2]);
+    __stcs(p.y32[2] + i, s.y[3]);
+    __stcs(p.u32[0] + i, s.U[0]);
+    __stcs(p.u32[1] + i, s.U[1]);
+    __stcs(p.u32[2] + i, s.U[2]);
+}
+
+// Uniform block meshes.  Each block moves one contiguous chunk of the store,
+// 256 particles per tile, the next tile's records loaded before the current
+// tile is processed.  Every particle is pushed (PICParcel::move) and its
+// displaced point followed in normalised cell coordinates: inside the cell
+// it takes the tet found by cell_locate (tracking inside a cell crosses only
+// tet faces, which carry no event); across a cell face into a neighbour the
+// point moves one cell over; an absorbing patch removes the particle, a
+// floating or circuit patch removes a charged one and keeps its charge
+// (PICParcel::hitPatch, PICParcel.C:153-184).  A particle that reaches a
+// reflecting patch keeps its start record, gets its pushed velocity written
+// back and joins the block's segment of the crossing queue, whose tracker
+// repeats its step with the wall's velocity sync.  The in-cell path uses
+// selects only (no indexed registers, no calls), so it needs no stack.
+template <int PUSHER>
+__global__ void __launch_bounds__(256, 5) move_cell_kernel_fp32(MoveParams P, int chunk) {
+    __shared__ CellTables32 G;
+    __shared__ unsigned tri_s[12];
+    __shared__ int kind_s[kMaxPatches];
+    __shared__ int w0s, qn;
+    extern __shared__ unsigned win[];  // kWindow * 9 slots (32-bit, carry to global)
+    int n_end = P.n, first = P.first, ch = chunk;
+    if (P.n_dev) {
+        n_end = *P.n_dev;
+        first = P.first_dev ? *P.first_dev : 0;
+        const long tiles = (long(n_end) - first + 255) / 256;
+        ch = int(((tiles + gridDim.x - 1) / gridDim.x) * 256);
+        if (ch <= 0) ch = 256;
+    }
+    const int start = first + blockIdx.x * ch;
+    const int end = min(n_end, start + ch);
+    if (start >= end) {
+        // block-uniform: nothing to move; the crossing tracker reads the count
+        if (threadIdx.x == 0) {
+            P.xq.count[blockIdx.x] = 0;
+            P.xq.start[blockIdx.x] = 0;
+        }
+        return;
+    }
+    {
+        const unsigned* src = reinterpret_cast<const unsigned*>(P.ct32);
+        unsigned* dst = reinterpret_cast<unsigned*>(&G);
+        for (int k = threadIdx.x; k < int(sizeof(CellTables32) / 4); k += blockDim.x) dst[k] = src[k];
+        if (threadIdx.x < 12) tri_s[threadIdx.x] = P.t32->tri[threadIdx.x];
+        if (threadIdx.x < kMaxPatches) kind_s[threadIdx.x] = P.t32->kind[threadIdx.x];
+        for (int k = threadIdx.x; k < kWindow * 9; k += blockDim.x) win[k] = 0u;
+    }
+    if (threadIdx.x == 0) {
+        int c0 = 0;
+        for (int k = start; k < end && k < start + 64; ++k) {
+            const int t = P.p.tet[k];
+            if (t >= 0) { c0 = t / 12; break; }
+        }
+        w0s = max(0, c0 - kWindow / 16);
+        qn = 0;
+    }
+    __syncthreads();
+    const int w0 = w0s;
+    unsigned ts = 0, fc = 0, ab = 0;
+    int i = start + threadIdx.x;
+    Rec next{-1, 0, 0, 0, 0, 0, 0};
+    if (i < end) next = load_rec(P.p, i);
+    for (int base = start; base < end; base += 256) {
+        const Rec r = next;
+        const int ci = i;
+        i += 256;
+        if (i < end) next = load_rec(P.p, i);
+        if (ci >= end || r.tet < 0) continue;
+        S32 s;
+        s.cell = r.tet / 12;
+        s.tet = r.tet - 12 * s.cell;
+        s.y[1] = r.y1;
+        s.y[2] = r.y2;
+        s.y[3] = r.y3;
+        s.y[0] = 1.f - s.y[1] - s.y[2] - s.y[3];
+        s.U[0] = r.u0;
+        s.U[1] = r.u1;
+        s.U[2] = r.u2;
+        if (P.solve_movement) {
+            if (P.charged) push32<PUSHER>(P, tri_s, s, P.dt_f);
+            if (!(s.U[0] * s.U[0] + s.U[1] * s.U[1] + s.U[2] * s.U[2] < float(kC) * float(kC))) {
+                atomicMax(&P.counters->error, int(PICGPU_SPEED_OF_LIGHT));
+                P.p.tet[ci] = -1;
+                ++ab;
+                continue;
+            }
+            // the start point in normalised cell coordinates (empty axes: the
+            // centre plane) and the displacement U dt
+            const float4 f0 = G.fwd[s.tet][0], f1 = G.fwd[s.tet][1], f2 = G.fwd[s.tet][2];
+            float x0 = (s.y[1] * f0.x + s.y[2] * f1.x + s.y[3] * f2.x) * G.keep.x;
+            float x1 = (s.y[1] * f0.y + s.y[2] * f1.y + s.y[3] * f2.y) * G.keep.y;
+            float x2 = (s.y[1] * f0.z + s.y[2] * f1.z + s.y[3] * f2.z) * G.keep.z;
+            float d0 = s.U[0] * G.dth.x, d1 = s.U[1] * G.dth.y, d2 = s.U[2] * G.dth.z;
+            float e0 = x0 + d0, e1 = x1 + d1, e2 = x2 + d2;
+            int fate = 0;  // 0: moved, 1: removed, 2: reflecting patch (queued)
+            unsigned faces = 0;
+            if (fmaxf(fabsf(e0), fmaxf(fabsf(e1), fabsf(e2))) > 0.5f) {
+                // through cell faces: the first face on the way per axis
+                // (|x_a| <= 1/2 after the clamp, so d_a != 0 where |e_a| > 1/2)
+                x0 = fminf(fmaxf(x0, -0.5f), 0.5f);
+                x1 = fminf(fmaxf(x1, -0.5f), 0.5f);
+                x2 = fminf(fmaxf(x2, -0.5f), 0.5f);
+                e0 = x0 + d0;
+                e1 = x1 + d1;
+                e2 = x2 + d2;
+                int budget = P.max_steps;
+                while (true) {
+                    float t = 2.f;
+                    int ax = 0;
+                    if (fabsf(e0) > 0.5f) t = __fdividef(copysignf(0.5f, e0) - x0, d0);
+                    if (fabsf(e1) > 0.5f) {
+                        const float ta = __fdividef(copysignf(0.5f, e1) - x1, d1);
+                        if (ta < t) { t = ta; ax = 1; }
+                    }
+                    if (fabsf(e2) > 0.5f) {
+                        const float ta = __fdividef(copysignf(0.5f, e2) - x2, d2);
+                        if (ta < t) { t = ta; ax = 2; }
+                    }
+                    t = fminf(fmaxf(t, 0.f), 1.f);
+                    const float ea = ax == 0 ? e0 : ax == 1 ? e1 : e2;
+                    const float face = ea > 0.f ? 0.5f : -0.5f;
+                    x0 = ax == 0 ? face : fminf(fmaxf(x0 + t * d0, -0.5f), 0.5f);
+                    x1 = ax == 1 ? face : fminf(fmaxf(x1 + t * d1, -0.5f), 0.5f);
+                    x2 = ax == 2 ? face : fminf(fmaxf(x2 + t * d2, -0.5f), 0.5f);
+                    const float rest = 1.f - t;
+                    d0 *= rest;
+                    d1 *= rest;
+                    d2 *= rest;
+                    ++faces;
+                    const int nb = __ldg(P.m.nbr + 6 * s.cell + 2 * ax + (ea > 0.f ? 1 : 0));
+                    if (nb < 0) {
+                        const int patch = -nb - 1;
+                        const int kind = kind_s[patch];
+                        fate = 1;
+                        if (kind == PICGPU_PATCH_FLOATING || (kind == PICGPU_PATCH_CIRCUIT && P.q != 0.0))
+                            atomicAdd(P.qconv + patch, P.weight * P.q);
+                        else if (kind != PICGPU_PATCH_ABSORB)
+                            fate = 2;
+                        break;
+                    }
+                    // the neighbour: the point sits on its opposite face
+                    s.cell = nb;
+                    x0 = ax == 0 ? -face : x0;
+                    x1 = ax == 1 ? -face : x1;
+                    x2 = ax == 2 ? -face : x2;
+                    e0 = x0 + d0;
+                    e1 = x1 + d1;
+                    e2 = x2 + d2;
+                    if (fmaxf(fabsf(e0), fmaxf(fabsf(e1), fabsf(e2))) <= 0.5f) break;
+                    if (--budget <= 0) {
+                        atomicMax(&P.counters->error, int(PICGPU_TRACK_LOOP_CAP));
+                        fate = 1;
+                        break;
+                    }
+                }
+            }
+            if (fate == 1) {
+                P.p.tet[ci] = -1;
+                ++ab;
+                fc += faces;
+                continue;
+            }
+            if (fate == 2) {
+                // a reflecting patch: the crossing tracker repeats this step
+                // from the start record with the pushed velocity
+                __stcs(P.p.u32[0] + ci, s.U[0]);
+                __stcs(P.p.u32[1] + ci, s.U[1]);
+                __stcs(P.p.u32[2] + ci, s.U[2]);
+                P.xq.queue[start + atomicAdd(&qn, 1)] = ci;
+                continue;
+            }
+            cell_locate(G, e0, e1, e2, s);
+            ++ts;
+            fc += faces;
+            store_rec(P.p, ci, s, 12 * s.cell + s.tet);
+        }
+        deposit32(P, tri_s, s, w0, win);
+    }
+    __syncthreads();
+    if (P.has_value) {
+        const int nslot = min(kWindow, P.m.n_cells - w0) * 9;
+        unsigned long long* g = P.acc9 + 9 * size_t(w0);
+        for (int k = threadIdx.x; k < nslot; k += blockDim.x) {
+            const unsigned v = win[k];
+            if (v) atomicAdd(g + k, (unsigned long long)v);
+        }
+    }
+    if (threadIdx.x == 0) {
+        P.xq.count[blockIdx.x] = qn;
+        P.xq.start[blockIdx.x] = start;
+    }
+    warp_add_counter<float>(&P.counters->tet_steps, ts);
+    warp_add_counter<float>(&P.counters->faces, fc);
+    warp_add_counter<float>(&P.counters->absorbed, ab);
+}
+
+// Charge deposit straight into the global accumulators.
+__device__ __forceinline__ void deposit_global32(const MoveParams& P, const unsigned* tri_of, const S32& s) {
+    if (!P.has_value) return;
+    constexpr float kScale = float(1u << kDepositBits);
+    unsigned long long* g = P.acc9 + 9 * size_t(s.cell);
+    if (P.charge_distribution == PICGPU_WEIGHTING_CELL_AVERAGE) {
+        atomicAdd(g, (unsigned long long)(1u << kDepositBits));
+        return;
+    }
+    const unsigned tri = tri_of[s.tet];
+    atomicAdd(g, (unsigned long long)__float2uint_rn(s.y[0] * kScale));
+    atomicAdd(g + 1 + (tri & 15u), (unsigned long long)__float2uint_rn(s.y[1] * kScale));
+    atomicAdd(g + 1 + ((tri >> 4) & 15u), (unsigned long long)__float2uint_rn(s.y[2] * kScale));
+    atomicAdd(g + 1 + ((tri >> 8) & 15u), (unsigned long long)__float2uint_rn(s.y[3] * kScale));
+}
+
+// The particles the in-cell mover queued, block b of this grid taking block
+// b's segment: barycentric tracking from the start position with the pushed
+// velocity (PICParcel::moveForward: cell faces, patches, velocity sync),
+// then store and deposit.
+template <int PUSHER>
+__global__ void __launch_bounds__(256) track_queue_kernel_fp32(MoveParams P) {
+    __shared__ Tables32 T;
+    const int cnt = P.xq.count[blockIdx.x];
+    if (cnt <= 0) return;  // block-uniform
+    const int qs = P.xq.start[blockIdx.x];
+    {
+        const unsigned* src = reinterpret_cast<const unsigned*>(P.t32);
+        unsigned* dst = reinterpret_cast<unsigned*>(&T);
+        for (int k = threadIdx.x; k < int(sizeof(Tables32) / 4); k += blockDim.x) dst[k] = src[k];
+    }
+    __syncthreads();
+    unsigned ts = 0, fc = 0, wl = 0, ab = 0;
+    for (int k = threadIdx.x; k < cnt; k += blockDim.x) {
+        const int i = P.xq.queue[qs + k];
+        const Rec r = load_rec(P.p, i);
+        S32 s;
+        s.cell = r.tet / 12;
+        s.tet = r.tet - 12 * s.cell;
+        s.y[1] = r.y1;
+        s.y[2] = r.y2;
+        s.y[3] = r.y3;
+        s.y[0] = 1.f - s.y[1] - s.y[2] - s.y[3];
+        s.U[0] = r.u0;
+        s.U[1] = r.u1;
+        s.U[2] = r.u2;
+        Tally td{0u, 0u, 0u, true};
+        track32<PUSHER>(P, T, s, td);
+        ts += td.tet_steps;
+        fc += td.faces;
+        wl += td.walls;
+        if (!td.keep) {
+            P.p.tet[i] = -1;
+            ++ab;
+            continue;
+        }
+        store_rec(P.p, i, s, 12 * s.cell + s.tet);
+        deposit_global32(P, T.tri, s);
+    }
+    warp_add_counter<float>(&P.counters->tet_steps, ts);
+    warp_add_counter<float>(&P.counters->faces, fc);
+    warp_add_counter<float>(&P.counters->walls, wl);
+    warp_add_counter<float>(&P.counters->absorbed, ab);
+}
+
+template <int PUSHER>
+int launch_pusher(const MoveParams& P, int blocks, int chunk, bool cell, cudaStream_t s) {
+    const size_t smem = size_t(kWindow) * 9 * sizeof(unsigned);
+    if (!cell) {
+        move_kernel_fp32<PUSHER><<<blocks, 256, smem, s>>>(P, chunk);
+        return 1;
+    }
+    move_cell_kernel_fp32<PUSHER><<<blocks, 256, smem, s>>>(P, chunk);
+    if (!P.solve_movement || !P.reflecting) return 1;
+    track_queue_kernel_fp32<PUSHER><<<blocks, 256, 0, s>>>(P);
+    return 2;
+}
 
 }  // namespace
-
-cudaError_t move_fp32_set_tables(const Tables32& t) { return cudaMemcpyToSymbol(c_t32, &t, sizeof t); }
 
 // grid: the number of resident blocks to use (5 per SM); each block takes one
 // contiguous chunk (a multiple of 256 particles) of [P.first, P.n).  With
 // P.n_dev set the counts are read on the device and all grid blocks launch.
-void launch_move_fp32(const MoveParams& P, int grid, cudaStream_t s) {
+// Uniform block meshes with a crossing queue run the in-cell mover and the
+// crossing tracker; other meshes the general kernel.  Returns the number of
+// kernels launched.
+int launch_move_fp32(const MoveParams& P, int grid, cudaStream_t s) {
     int blocks, chunk;
     if (P.n_dev) {
         // device-resident counts: the kernel sizes its chunks; grid fixed
@@ -402,25 +713,19 @@ void launch_move_fp32(const MoveParams& P, int grid, cudaStream_t s) {
         chunk = 0;
     } else {
         const long work = long(P.n) - P.first;
-        if (work <= 0) return;
+        if (work <= 0) return 0;
         const long tiles = (work + 255) / 256;
         const long per = (tiles + grid - 1) / grid;
         chunk = int(per * 256);
         blocks = int((work + chunk - 1) / chunk);
     }
-    const size_t smem = size_t(kWindow) * 9 * sizeof(unsigned);
+    const bool cell = P.m.uniform && P.ct32 && P.xq.queue && blocks <= P.xq.capacity;
     switch (P.pusher) {
-        case PICGPU_PUSHER_BORIS:
-            move_kernel_fp32<PICGPU_PUSHER_BORIS><<<blocks, 256, smem, s>>>(P, chunk);
-            break;
-        case PICGPU_PUSHER_BORIS_NR:
-            move_kernel_fp32<PICGPU_PUSHER_BORIS_NR><<<blocks, 256, smem, s>>>(P, chunk);
-            break;
-        case PICGPU_PUSHER_VAY: move_kernel_fp32<PICGPU_PUSHER_VAY><<<blocks, 256, smem, s>>>(P, chunk); break;
-        case PICGPU_PUSHER_HIGUERA_CARY:
-            move_kernel_fp32<PICGPU_PUSHER_HIGUERA_CARY><<<blocks, 256, smem, s>>>(P, chunk);
-            break;
-        default: move_kernel_fp32<PICGPU_PUSHER_NONE><<<blocks, 256, smem, s>>>(P, chunk); break;
+        case PICGPU_PUSHER_BORIS: return launch_pusher<PICGPU_PUSHER_BORIS>(P, blocks, chunk, cell, s);
+        case PICGPU_PUSHER_BORIS_NR: return launch_pusher<PICGPU_PUSHER_BORIS_NR>(P, blocks, chunk, cell, s);
+        case PICGPU_PUSHER_VAY: return launch_pusher<PICGPU_PUSHER_VAY>(P, blocks, chunk, cell, s);
+        case PICGPU_PUSHER_HIGUERA_CARY: return launch_pusher<PICGPU_PUSHER_HIGUERA_CARY>(P, blocks, chunk, cell, s);
+        default: return launch_pusher<PICGPU_PUSHER_NONE>(P, blocks, chunk, cell, s);
     }
 }
 

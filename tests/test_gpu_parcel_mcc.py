@@ -14,8 +14,8 @@ from picfoam_gb300.simulation import PicError
 pytestmark = pytest.mark.gpu
 
 
-def make(precision=abi.PREC_FP64, **kw):
-    return cases.neutral_parcel_ionization(n_n=1e22, dt=4e-11, precision=precision, **kw)
+def make(precision=abi.PREC_FP64, n_n=1e22, **kw):
+    return cases.neutral_parcel_ionization(n_n=n_n, dt=4e-11, precision=precision, **kw)
 
 
 @pytest.mark.parametrize("keep", [False, True])
@@ -48,11 +48,15 @@ def test_ion_parcels_after_neutral_deletion_match_oracle(gpu, oracle_backend, pr
     deleted = 0
     for _ in range(3):
         sg, so = g.step(1), o.step(1)
-        assert (sg.mcc_parcel_candidates, sg.ion_parcel_candidates) == \
-               (so.mcc_parcel_candidates, so.ion_parcel_candidates)
         if precision == abi.PREC_FP64:
+            assert (sg.mcc_parcel_candidates, sg.ion_parcel_candidates) == \
+                   (so.mcc_parcel_candidates, so.ion_parcel_candidates)
             assert (sg.mcc_parcel_ionization, sg.ion_parcel_elastic, sg.ion_parcel_charge_exchange) == \
                    (so.mcc_parcel_ionization, so.ion_parcel_elastic, so.ion_parcel_charge_exchange)
+        else:
+            # FP32 velocities move the running (sigma c_R)_max and the remainders by rounding
+            assert abs(sg.mcc_parcel_candidates - so.mcc_parcel_candidates) <= 0.02 * so.mcc_parcel_candidates + 2
+            assert abs(sg.ion_parcel_candidates - so.ion_parcel_candidates) <= 0.02 * so.ion_parcel_candidates + 2
         deleted += so.mcc_parcel_ionization
         assert sg.mcc_candidates == 0 and sg.ion_mcc_candidates == 0    # no background gas
     assert deleted > 100 and so.ion_parcel_elastic + so.ion_parcel_charge_exchange > 50
