@@ -22,10 +22,8 @@
 #include "oracle.h"
 #include "collisions.hpp"
 #include "picgpu_init.h"
-#include "../picfoam_gb300/csrc/hexmesh.hpp"
-#include "../picfoam_gb300/csrc/circuit.hpp"
-#include "../picfoam_gb300/csrc/emission.hpp"
-#include "../picfoam_gb300/csrc/freestream.hpp"
+#include "omesh.hpp"
+#include "oboundary.hpp"
 
 #include <algorithm>
 #include <chrono>
@@ -38,9 +36,9 @@
 
 namespace {
 
-using pg::HexMesh;
-using pg::PatchTriangles;
-using pg::patch_triangles;
+using HexMesh = om::Mesh;
+using om::PatchTriangles;
+using om::patch_triangles;
 
 // CODATA constants (values used throughout the project).
 constexpr double kC = 299792458.0;
@@ -150,10 +148,10 @@ struct Oracle {
     std::vector<double> sigma, gradBC, Qconv; // per patch floating state
     std::vector<double> rlcK;                 // per patch RLCBoundary a0 epsilon A
     // circuit model (circuitRLC / IdealVoltageSource / IdealCurrentSource)
-    pg::RlcCoeffs rlc;
+    ob::RlcCoeffs rlc;
     double circuitI = 0.0;
     std::vector<int> cathodeFaces;
-    pg::CircuitState circuit{};
+    ob::CircuitState circuit{};
     bool rotation = false;
     double move_seconds = 0;
     long long step_index = 0;
@@ -176,7 +174,7 @@ struct Oracle {
     // FreeStream boundary models
     struct FreeStream {
         picgpu_freestream cfg{};
-        pg::FreeStreamFaces F;
+        ob::FreeStreamFaces F;
         std::vector<double> acc;   // n_faces * n_species
     };
     std::vector<FreeStream> freestreams;
@@ -331,7 +329,7 @@ struct TrackData {
 
 V3 position_of(const Oracle& o, const Parcel& p) {
     double x[3];
-    pg::position(o.m, 12LL * p.cell + p.tet, &p.y[1], x);
+    om::position(o.m, 12LL * p.cell + p.tet, &p.y[1], x);
     return v3(x[0], x[1], x[2]);
 }
 
@@ -562,13 +560,13 @@ void floating_pre_update(Oracle& o) {
 // device's lane order.
 double circuit_src(const Oracle& o) {
     if (o.cfg.circuit.model != PICGPU_CIRCUIT_RLC) return 0.0;
-    return pg::circuit_source(o.cfg.circuit, double(o.step_index + 1) * o.cfg.dt);
+    return ob::circuit_source(o.cfg.circuit, double(o.step_index + 1) * o.cfg.dt);
 }
 
 void circuit_pre_update(Oracle& o) {
     const picgpu_circuit& cc = o.cfg.circuit;
     if (cc.model == PICGPU_CIRCUIT_NONE) return;
-    pg::circuit_pre_update(cc.model, cc.cathode_patch, o.rlc.a, o.m.patches[cc.cathode_patch].area, o.circuitI,
+    ob::circuit_pre_update(cc.model, cc.cathode_patch, o.rlc.a, o.m.patches[cc.cathode_patch].area, o.circuitI,
                            o.cfg.dt, kEps0, circuit_src(o), o.Qconv.data(), o.gradBC.data(), o.circuit);
 }
 
@@ -579,18 +577,18 @@ void circuit_post_update(Oracle& o) {
     const int nf = int(o.cathodeFaces.size());
     double sum = 0.0;
     if (cc.model == PICGPU_CIRCUIT_RLC) {
-        sum = pg::circuit_face_sum(nf, [&](int i) {
-            const pg::BFace& B = m.bfaces[o.cathodeFaces[i]];
-            return pg::face_value(pg::kRuleRlc, 0.0, 0.0, o.rlc.k, B.delta, o.phi[B.cell]);
+        sum = ob::lane_sum(nf, [&](int i) {
+            const om::BFace& B = m.bfaces[o.cathodeFaces[i]];
+            return ob::face_value(ob::kRuleRlc, 0.0, 0.0, o.rlc.k, B.delta, o.phi[B.cell]);
         });
     } else if (cc.model == PICGPU_CIRCUIT_IDEAL_CURRENT) {
-        sum = pg::circuit_face_sum(nf, [&](int i) {
-            const pg::BFace& B = m.bfaces[o.cathodeFaces[i]];
+        sum = ob::lane_sum(nf, [&](int i) {
+            const om::BFace& B = m.bfaces[o.cathodeFaces[i]];
             return B.area * o.phi[B.cell];
         });
     }
     const double t = double(o.step_index + 1) * o.cfg.dt;
-    pg::circuit_post_update(cc.model, cc.anode_patch, cc.cathode_patch, nf, o.rlc.a,
+    ob::circuit_post_update(cc.model, cc.anode_patch, cc.cathode_patch, nf, o.rlc.a,
                             m.patches[cc.cathode_patch].area, o.cfg.dt, circuit_src(o), o.cfg.dt / t, sum,
                             o.Qconv.data(), o.circuit);
 }
@@ -607,11 +605,11 @@ void assemble_rhs(const Oracle& o, const double* rho, std::vector<double>& b) {
         for (int f = 0; f < 6; ++f) {
             const int bf = m.cell_bface[6 * size_t(c) + f];
             if (bf < 0) continue;
-            const pg::BFace& B = m.bfaces[bf];
+            const om::BFace& B = m.bfaces[bf];
             const picgpu_patch& P = m.patches[B.patch].p;
-            const int rule = pg::face_rule(P.kind, P.phi_bc);
-            if (rule != pg::kRuleNone)
-                t = t + pg::face_rhs(rule, P.phi, o.gradBC[B.patch], o.rlcK[B.patch], B.area, B.delta);
+            const int rule = ob::face_rule(P.kind, P.phi_bc);
+            if (rule != ob::kRuleNone)
+                t = t + ob::face_rhs(rule, P.phi, o.gradBC[B.patch], o.rlcK[B.patch], B.area, B.delta);
         }
         b[c] = t;
     }
@@ -785,9 +783,9 @@ void compute_E(Oracle& o) {
             } else {
                 const int bf = m.cell_bface[6 * size_t(c) + f];
                 if (bf < 0) continue;  // empty
-                const pg::BFace& B = m.bfaces[bf];
+                const om::BFace& B = m.bfaces[bf];
                 const picgpu_patch& P = m.patches[B.patch].p;
-                pf = pg::face_value(pg::face_rule(P.kind, P.phi_bc), P.phi, o.gradBC[B.patch], o.rlcK[B.patch],
+                pf = ob::face_value(ob::face_rule(P.kind, P.phi_bc), P.phi, o.gradBC[B.patch], o.rlcK[B.patch],
                                     B.delta, o.phi[c]);
             }
             const double area = m.cls_farea[size_t(cl) * 6 + f];
@@ -797,10 +795,10 @@ void compute_E(Oracle& o) {
         for (int a = 0; a < 3; ++a) o.E[3 * size_t(c) + a] = -(g[a] / m.vol[c]);
     }
     for (size_t b = 0; b < m.bfaces.size(); ++b) {
-        const pg::BFace& B = m.bfaces[b];
+        const om::BFace& B = m.bfaces[b];
         const picgpu_patch& P = m.patches[B.patch].p;
         const double* Ec = &o.E[3 * size_t(B.cell)];
-        const double sn = pg::face_sn_grad(pg::face_rule(P.kind, P.phi_bc), P.phi, o.gradBC[B.patch],
+        const double sn = ob::face_sn_grad(ob::face_rule(P.kind, P.phi_bc), P.phi, o.gradBC[B.patch],
                                            o.rlcK[B.patch], B.delta, o.phi[B.cell]);
         const double En = Ec[0] * B.normal[0] + Ec[1] * B.normal[1] + Ec[2] * B.normal[2];
         for (int a = 0; a < 3; ++a)
@@ -2077,7 +2075,7 @@ bool locate_in_cell(const HexMesh& m, int c, const double* x, int& tet, double* 
     int best = -1;
     for (int t = 0; t < 12; ++t) {
         double q[3];
-        tet_coords(m, c, t, x, q);
+        om::tet_coords(m, c, t, x, q);
         const double q0 = 1.0 - q[0] - q[1] - q[2];
         const double mn = std::fmin(std::fmin(q0, q[0]), std::fmin(q[1], q[2]));
         if (mn > best_min) {
@@ -2235,7 +2233,7 @@ int oracle_initialise_impl(Oracle& o, const picgpu_init* in, picgpu_init_stats* 
         } else if (in->model == PICGPU_INIT_UNIFORM_DISPLACEMENT) {
             // UniformInitialization.C:60-125
             double lo[3], hi[3], dir[3], span[3], delta[3];
-            const int gtop = grid_point_id(m, m.n[0], m.n[1], m.n[2]);
+            const int gtop = om::grid_point_id(m, m.n[0], m.n[1], m.n[2]);
             for (int a = 0; a < 3; ++a) {
                 lo[a] = in->use_bounds ? in->min[a] : m.grid_pts[a];
                 hi[a] = in->use_bounds ? in->max[a] : m.grid_pts[3 * size_t(gtop) + a];
@@ -2260,7 +2258,7 @@ int oracle_initialise_impl(Oracle& o, const picgpu_init* in, picgpu_init_stats* 
                         double x[3];
                         for (int a = 0; a < 3; ++a) x[a] = p[a] + dir[a] * cur;
                         double by[3];
-                        const long long tg = locate(m, x, by);  // mesh.findCell
+                        const long long tg = om::locate(m, x, by);  // mesh.findCell
                         if (tg < 0) { o.err = "initialise: tried to create a particle outside of the mesh"; return PICGPU_INVALID_ARG; }
                         int t = 0;
                         double y[3];
@@ -2273,7 +2271,7 @@ int oracle_initialise_impl(Oracle& o, const picgpu_init* in, picgpu_init_stats* 
             // probability of the remainder
             for (int c = 0; c < nc; ++c)
                 for (int t = 0; t < 12; ++t) {
-                    const double V = tet_volume(m, m.cell_class[c], t);
+                    const double V = om::tet_volume(m, m.cell_class[c], t);
                     const double req = (q.n * V) / q.w;
                     long long cnt = (long long)req;
                     ocoll::Philox rc(in->seed, ocoll::kStreamInitCount | uint32_t(sp), uint32_t(c), uint32_t(t));
@@ -2374,7 +2372,7 @@ void freestream_inject(Oracle& o) {
     using namespace oinit;
     for (size_t i = 0; i < o.freestreams.size(); ++i) {
         Oracle::FreeStream& Z = o.freestreams[i];
-        const pg::FreeStreamFaces& F = Z.F;
+        const ob::FreeStreamFaces& F = Z.F;
         for (int j = 0; j < Z.cfg.n_species; ++j) {
             const int sp = Z.cfg.species[j];
             const picgpu_species& S = o.cfg.species[sp];
@@ -2559,9 +2557,9 @@ void inject(Oracle& o) {
         double j = Z.j;
         double temperature = Z.cfg.temperature;
         if (Z.cfg.model == PICGPU_EMISSION_FOWLER_NORDHEIM) {
-            j = pg::emission_face_sum(int(Z.faces.size()), [&](int k) {
+            j = ob::lane_sum(int(Z.faces.size()), [&](int k) {
                 const int b = Z.faces[k];
-                return pg::fowler_nordheim_face(&o.Eb[3 * size_t(b)], o.m.bfaces[b].normal, Z.cfg.work_function);
+                return ob::fowler_nordheim_face(&o.Eb[3 * size_t(b)], o.m.bfaces[b].normal, Z.cfg.work_function);
             });
             temperature = Z.cfg.work_function * qe / kBoltzmann;
         }
@@ -2587,7 +2585,7 @@ int oracle_create(const picgpu_mesh_desc* mesh, const picgpu_config* cfg, int nt
     auto* c = new oracle_ctx();
     Oracle& o = c->o;
     try {
-        o.m = pg::build_hex_mesh(*mesh);
+        o.m = om::build(*mesh);
     } catch (const std::exception& e) {
         o.err = e.what();
         *out = c;
@@ -2615,25 +2613,25 @@ int oracle_create(const picgpu_mesh_desc* mesh, const picgpu_config* cfg, int nt
     o.gradBC.assign(m.patches.size(), 0.0);
     o.Qconv.assign(m.patches.size(), 0.0);
     {
-        const std::string ce = pg::check_circuit(m, cfg->circuit, cfg->dt);
+        const std::string ce = ob::check_circuit(m, cfg->circuit, cfg->dt);
         if (!ce.empty()) { o.err = ce; *out = c; return PICGPU_INVALID_ARG; }
     }
     o.rlcK.assign(m.patches.size(), 0.0);
     if (cfg->circuit.model != PICGPU_CIRCUIT_NONE) {
         const picgpu_circuit& cc = cfg->circuit;
         const double area = m.patches[cc.cathode_patch].area;
-        o.rlc = pg::rlc_coefficients(cc, cfg->dt, area);
+        o.rlc = ob::rlc_coefficients(cc, cfg->dt, area);
         if (cc.model == PICGPU_CIRCUIT_RLC) o.rlcK[cc.cathode_patch] = o.rlc.k;
-        o.circuitI = pg::circuit_current_source(cc, area);
-        o.cathodeFaces = pg::circuit_cathode_faces(m, cc);
-        o.circuit = pg::circuit_start(cc);
+        o.circuitI = ob::circuit_current_source(cc, area);
+        o.cathodeFaces = ob::circuit_cathode_faces(m, cc);
+        o.circuit = ob::circuit_start(cc);
         if (cc.model == PICGPU_CIRCUIT_IDEAL_CURRENT) o.gradBC[cc.cathode_patch] = o.circuit.sigma / kEps0;
     }
     o.Mdiag.resize(m.n_cells);
     o.dinv.resize(m.n_cells);
     o.Moff.resize(6 * size_t(m.n_cells));
     for (int i = 0; i < m.n_cells; ++i) o.Mdiag[i] = -m.lap_diag[i];
-    pg::circuit_add_diagonal(m, cfg->circuit, cfg->dt, o.Mdiag);
+    ob::circuit_add_diagonal(m, cfg->circuit, cfg->dt, o.Mdiag);
     for (int i = 0; i < m.n_cells; ++i) o.dinv[i] = 1.0 / o.Mdiag[i];
     for (size_t i = 0; i < o.Moff.size(); ++i) o.Moff[i] = -m.lap_off[i];
     double qmax = 0;
@@ -2811,7 +2809,7 @@ int oracle_set_emission(oracle_ctx* ctx, int n, const picgpu_emission* em) {
         Z.tri = patch_triangles(o.m, em[i].patch);
         if (Z.tri.cell.empty()) return PICGPU_INVALID_ARG;
         if (em[i].model == PICGPU_EMISSION_THERMIONIC)
-            Z.j = pg::thermionic_current(em[i].lambda_r, em[i].temperature, em[i].work_function,
+            Z.j = ob::thermionic_current(em[i].lambda_r, em[i].temperature, em[i].work_function,
                                          std::fabs(o.cfg.species[es].charge));
         for (size_t b = 0; b < o.m.bfaces.size(); ++b)
             if (o.m.bfaces[b].patch == em[i].patch) Z.faces.push_back(int(b));
@@ -2824,7 +2822,7 @@ int oracle_set_freestream(oracle_ctx* ctx, int n, const picgpu_freestream* fs) {
     Oracle& o = ctx->o;
     if (n < 0 || n > PICGPU_MAX_FREESTREAMS || (n > 0 && !fs)) return PICGPU_INVALID_ARG;
     for (int i = 0; i < n; ++i) {
-        const std::string e = pg::check_freestream(o.m, o.cfg, fs[i]);
+        const std::string e = ob::check_freestream(o.m, o.cfg, fs[i]);
         if (!e.empty()) {
             o.err = e;
             return PICGPU_INVALID_ARG;
@@ -2834,7 +2832,7 @@ int oracle_set_freestream(oracle_ctx* ctx, int n, const picgpu_freestream* fs) {
     for (int i = 0; i < n; ++i) {
         Oracle::FreeStream Z;
         Z.cfg = fs[i];
-        Z.F = pg::freestream_faces(o.m, o.cfg, fs[i]);
+        Z.F = ob::freestream_faces(o.m, o.cfg, fs[i]);
         Z.acc.assign(size_t(Z.F.n_faces) * Z.F.n_species, 0.0);
         o.freestreams.push_back(Z);
     }

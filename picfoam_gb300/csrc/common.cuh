@@ -47,19 +47,6 @@ struct Tables32 {
     int kind[kMaxPatches];
 };
 
-// Cell-local geometry of the canonical hex for the FP32 in-cell mover, in
-// coordinates normalised by the cell size about the cell centre (the cell is
-// [-1/2, 1/2]^3; barycentric coordinates are affine invariants, so one set of
-// tables serves every axis-aligned uniform block mesh).
-struct CellTables32 {
-    float4 fwd[12][3];   // tet t, k = 0..2: corner tri[t][k] - centre (xyz)
-    float4 inv[12][3];   // tet t: y_{k+1} = dot(inv[t][k].xyz, x)
-    float4 diag[6];      // face f: normal of the plane through the centre and the face
-                         // diagonal tri[2f][0] - tri[2f][2]; dot(diag, x) >= 0 selects tet 2f
-    float4 dth;          // dt / cell size per axis (xyz)
-    float4 keep;         // 1 on solved axes, 0 on empty ones (tracking returns to the centre plane)
-};
-
 // Read-only mesh arrays on the device.
 struct DMesh {
     int n_cells, n_points, n_bfaces, n_classes;
@@ -158,7 +145,10 @@ struct MoveParams {
     float B_f[3];
     float centre_f[3];
     const Tables32* t32;          // FP32 form: tables of this context's mesh (device memory)
-    const CellTables32* ct32;     // FP32 form: in-cell mover tables (uniform block meshes)
+    // FP32 in-cell mover (uniform block meshes): dt / cell size per axis and
+    // 1 on solved axes, 0 on empty ones (tracking returns to the centre plane)
+    int cell_mover;
+    float dth[3], keep[3];
     CrossQueue xq;                // FP32 form: particles at reflecting patches (queue null: general kernel only)
     int reflecting;               // a patch reflects this species (wall, or a circuit electrode for neutrals)
     unsigned long long* acc9;     // this species' 2^-kDepositBits fixed-point deposit per cell: centre + 8 corners

@@ -265,7 +265,8 @@ struct picgpu_ctx {
     unsigned long long* acc9 = nullptr;   // FP32 form: per-species fixed-point deposit, 9 slots per cell
     float4* Ec4 = nullptr;                // FP32 form: E per cell, centre + 8 corners
     pgd::Tables32* t32 = nullptr;         // FP32 form: this mesh's move tables (device)
-    pgd::CellTables32* ct32 = nullptr;    // FP32 form: in-cell mover tables (device)
+    float cell_dth[3] = {0, 0, 0};        // FP32 in-cell mover: dt / cell size per axis (0: empty axis)
+    float cell_keep[3] = {1, 1, 1};       // 0 on empty axes
     int* xq_count = nullptr;              // FP32 form: crossing-queue counts and starts per mover block
     int* xq_start = nullptr;
     int xq_cap = 0;
@@ -562,9 +563,13 @@ pgd::MoveParams move_params(picgpu_ctx* c, int s, bool deposit_only) {
     for (const auto& pt : c->m.patches)
         if (pt.p.kind == PICGPU_PATCH_WALL || (pt.p.kind == PICGPU_PATCH_CIRCUIT && S.charge == 0.0))
             P.reflecting = 1;
-    if (c->mixed && c->dm.uniform && c->ct32 && c->xq_count) {
+    if (c->mixed && c->dm.uniform && c->xq_count) {
         // the idle double-buffer tet array holds the crossing queue
-        P.ct32 = c->ct32;
+        P.cell_mover = 1;
+        for (int a = 0; a < 3; ++a) {
+            P.dth[a] = c->cell_dth[a];
+            P.keep[a] = c->cell_keep[a];
+        }
         P.xq.queue = c->sp[s].tet[1 - c->sp[s].cur];
         P.xq.count = c->xq_count;
         P.xq.start = c->xq_start;
@@ -1594,54 +1599,14 @@ static picgpu_status create_with_mesh(picgpu_ctx* c, const picgpu_config* cfg) {
         if (us) return us;
     }
     if (c->mixed) {
-        // in-cell mover: the canonical hex in coordinates normalised by the
-        // cell size (corner c at its (i, j, k) bits - 1/2)
-        pgd::CellTables32 g{};
-        auto corner = [](int cn, double* v) {
-            for (int a = 0; a < 3; ++a) v[a] = double(pg::kCornerBits[cn][a]) - 0.5;
-        };
-        for (int tt = 0; tt < 12; ++tt) {
-            double A[3][3];  // columns: the triangle corners
-            for (int k = 0; k < 3; ++k) {
-                double v[3];
-                corner(m.tt.tri[tt][k], v);
-                for (int a = 0; a < 3; ++a) A[a][k] = v[a];
-                g.fwd[tt][k] = make_float4(float(v[0]), float(v[1]), float(v[2]), 0.f);
-            }
-            const double det = A[0][0] * (A[1][1] * A[2][2] - A[1][2] * A[2][1]) -
-                               A[0][1] * (A[1][0] * A[2][2] - A[1][2] * A[2][0]) +
-                               A[0][2] * (A[1][0] * A[2][1] - A[1][1] * A[2][0]);
-            double inv[3][3];
-            for (int r = 0; r < 3; ++r)
-                for (int q = 0; q < 3; ++q) {
-                    // cofactor of A[q][r] over det
-                    const int r0 = (q + 1) % 3, r1 = (q + 2) % 3, c0 = (r + 1) % 3, c1 = (r + 2) % 3;
-                    inv[r][q] = (A[r0][c0] * A[r1][c1] - A[r0][c1] * A[r1][c0]) / det;
-                }
-            for (int k = 0; k < 3; ++k)
-                g.inv[tt][k] = make_float4(float(inv[k][0]), float(inv[k][1]), float(inv[k][2]), 0.f);
-        }
-        for (int f = 0; f < 6; ++f) {
-            double a[3], b[3], q[3];
-            corner(pg::kFaceCorners[f][0], a);
-            corner(pg::kFaceCorners[f][2], b);
-            corner(pg::kFaceCorners[f][1], q);
-            double nrm[3] = {a[1] * b[2] - a[2] * b[1], a[2] * b[0] - a[0] * b[2], a[0] * b[1] - a[1] * b[0]};
-            if (nrm[0] * q[0] + nrm[1] * q[1] + nrm[2] * q[2] < 0)
-                for (double& v : nrm) v = -v;
-            g.diag[f] = make_float4(float(nrm[0]), float(nrm[1]), float(nrm[2]), 0.f);
-        }
-        float dth[3], keep[3];
+        // in-cell mover: dt per cell size along each axis (uniform block
+        // meshes: class 0's corner 6 sits at +h/2)
         for (int a = 0; a < 3; ++a) {
-            const double h = 2.0 * m.cls_offset[3 * 6 + a];   // class 0: corner 6 sits at +h/2
-            keep[a] = m.empty[a] ? 0.f : 1.f;
-            dth[a] = m.empty[a] ? 0.f : float(cfg->dt / h);
+            const double h = 2.0 * m.cls_offset[3 * 6 + a];
+            c->cell_keep[a] = m.empty[a] ? 0.f : 1.f;
+            c->cell_dth[a] = m.empty[a] ? 0.f : float(cfg->dt / h);
         }
-        g.dth = make_float4(dth[0], dth[1], dth[2], 0.f);
-        g.keep = make_float4(keep[0], keep[1], keep[2], 0.f);
-        const std::vector<pgd::CellTables32> gv(1, g);
-        picgpu_status us = upload(c, &c->ct32, gv);
-        if (us) return us;
+        picgpu_status us;
         c->xq_cap = 16 * c->sm_count;
         if ((us = dalloc(c, &c->xq_count, size_t(c->xq_cap))) || (us = dalloc(c, &c->xq_start, size_t(c->xq_cap))))
             return us;

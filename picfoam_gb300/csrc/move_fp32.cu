@@ -396,22 +396,53 @@ __global__ void __launch_bounds__(256, 5) move_kernel_fp32(MoveParams P, int chu
 
 // ------------------------------------------------------ in-cell mover ---
 
-// The tet of the canonical hex holding the cell-local point x (normalised
-// coordinates, |x_a| <= 1/2) and the point's barycentric coordinates there.
-__device__ __forceinline__ void cell_locate(const CellTables32& G, float x0, float x1, float x2, S32& s) {
+// The canonical hex in the normalised cell frame (centre 0, corners at
+// +-1/2).  Tet t = 2 f + k lies on local face f (normal axis a = f / 2,
+// outward side + for odd f); its corners are the face's base point p0 and
+// p1, p2 (k = 0) or p2, p3 (k = 1).  In the face's own axes -- the normal n
+// and the in-plane axes u, v with p1 - p0 along u and p3 - p0 along v, which
+// are the axes a + 1, a + 2 on a + face and a + 2, a + 1 on a - face -- the
+// corners sit at (u, v) = (-,-), (+,-), (+,+), (-,+), all at n = +-1/2, so
+// both maps between barycentric and cell coordinates are sums of the
+// coordinates with unit weights:
+//   x_n = +-(y1 + y2 + y3) / 2,
+//   k = 0: x_u = (-y1 + y2 + y3) / 2, x_v = (-y1 - y2 + y3) / 2,
+//   k = 1: x_u = (-y1 + y2 - y3) / 2, x_v = (-y1 + y2 + y3) / 2,
+// and back, with h = |x_n|: y0 = 1 - 2 h,
+//   k = 0: (y1, y2, y3) = (h - x_u, x_u - x_v, h + x_v),
+//   k = 1: (y1, y2, y3) = (h - x_v, h + x_u, x_v - x_u);
+// the point lies on face f's pyramid when |x_a| is the largest coordinate,
+// and in tet k = 1 when x_v > x_u (the plane through the centre and the
+// diagonal p0 p2 separates the two).
+__device__ __forceinline__ void bary_to_cell(int tet, const float* y, float& x0, float& x1, float& x2) {
+    const int f = tet >> 1, a = f >> 1;
+    const bool plus = f & 1, k1 = tet & 1;
+    const float xn = (plus ? 0.5f : -0.5f) * (y[1] + y[2] + y[3]);
+    const float xu = 0.5f * (k1 ? (y[2] - y[1] - y[3]) : (y[2] + y[3] - y[1]));
+    const float xv = 0.5f * (k1 ? (y[2] + y[3] - y[1]) : (y[3] - y[1] - y[2]));
+    const float xp = plus ? xu : xv;  // axis a + 1
+    const float xq = plus ? xv : xu;  // axis a + 2
+    x0 = a == 0 ? xn : a == 1 ? xq : xp;
+    x1 = a == 1 ? xn : a == 2 ? xq : xp;
+    x2 = a == 2 ? xn : a == 0 ? xq : xp;
+}
+
+__device__ __forceinline__ void cell_to_bary(float x0, float x1, float x2, S32& s) {
     const float a0 = fabsf(x0), a1 = fabsf(x1), a2 = fabsf(x2);
-    int f;
-    if (a0 >= a1 && a0 >= a2) f = x0 > 0.f ? 1 : 0;
-    else if (a1 >= a2) f = x1 > 0.f ? 3 : 2;
-    else f = x2 > 0.f ? 5 : 4;
-    const float4 dg = G.diag[f];
-    const int t = 2 * f + (dg.x * x0 + dg.y * x1 + dg.z * x2 >= 0.f ? 0 : 1);
-    const float4 i0 = G.inv[t][0], i1 = G.inv[t][1], i2 = G.inv[t][2];
-    s.tet = t;
-    s.y[1] = i0.x * x0 + i0.y * x1 + i0.z * x2;
-    s.y[2] = i1.x * x0 + i1.y * x1 + i1.z * x2;
-    s.y[3] = i2.x * x0 + i2.y * x1 + i2.z * x2;
-    s.y[0] = 1.f - s.y[1] - s.y[2] - s.y[3];
+    const bool ax0 = a0 >= a1 && a0 >= a2, ax1 = !ax0 && a1 >= a2;
+    const int a = ax0 ? 0 : ax1 ? 1 : 2;
+    const float xn = ax0 ? x0 : ax1 ? x1 : x2;
+    const float xp = ax0 ? x1 : ax1 ? x2 : x0;  // axis a + 1
+    const float xq = ax0 ? x2 : ax1 ? x0 : x1;  // axis a + 2
+    const bool plus = xn > 0.f;
+    const float h = fabsf(xn);
+    const float xu = plus ? xp : xq, xv = plus ? xq : xp;
+    const bool k1 = xv > xu;
+    s.tet = 4 * a + (plus ? 2 : 0) + (k1 ? 1 : 0);
+    s.y[1] = h - (k1 ? xv : xu);
+    s.y[2] = k1 ? h + xu : xu - xv;
+    s.y[3] = k1 ? xv - xu : h + xv;
+    s.y[0] = 1.f - 2.f * h;
 }
 
 __device__ __forceinline__ void store_rec(const DSpecies& p, int i, const S32& s, int cell_tet) {
@@ -428,7 +459,7 @@ __device__ __forceinline__ void store_rec(const DSpecies& p, int i, const S32& s
 // 256 particles per tile, the next tile's records loaded before the current
 // tile is processed.  Every particle is pushed (PICParcel::move) and its
 // displaced point followed in normalised cell coordinates: inside the cell
-// it takes the tet found by cell_locate (tracking inside a cell crosses only
+// it takes the tet found by cell_to_bary (tracking inside a cell crosses only
 // tet faces, which carry no event); across a cell face into a neighbour the
 // point moves one cell over; an absorbing patch removes the particle, a
 // floating or circuit patch removes a charged one and keeps its charge
@@ -439,7 +470,6 @@ __device__ __forceinline__ void store_rec(const DSpecies& p, int i, const S32& s
 // selects only (no indexed registers, no calls), so it needs no stack.
 template <int PUSHER>
 __global__ void __launch_bounds__(256, 5) move_cell_kernel_fp32(MoveParams P, int chunk) {
-    __shared__ CellTables32 G;
     __shared__ unsigned tri_s[12];
     __shared__ int kind_s[kMaxPatches];
     __shared__ int w0s, qn;
@@ -463,9 +493,6 @@ __global__ void __launch_bounds__(256, 5) move_cell_kernel_fp32(MoveParams P, in
         return;
     }
     {
-        const unsigned* src = reinterpret_cast<const unsigned*>(P.ct32);
-        unsigned* dst = reinterpret_cast<unsigned*>(&G);
-        for (int k = threadIdx.x; k < int(sizeof(CellTables32) / 4); k += blockDim.x) dst[k] = src[k];
         if (threadIdx.x < 12) tri_s[threadIdx.x] = P.t32->tri[threadIdx.x];
         if (threadIdx.x < kMaxPatches) kind_s[threadIdx.x] = P.t32->kind[threadIdx.x];
         for (int k = threadIdx.x; k < kWindow * 9; k += blockDim.x) win[k] = 0u;
@@ -511,15 +538,40 @@ __global__ void __launch_bounds__(256, 5) move_cell_kernel_fp32(MoveParams P, in
             }
             // the start point in normalised cell coordinates (empty axes: the
             // centre plane) and the displacement U dt
-            const float4 f0 = G.fwd[s.tet][0], f1 = G.fwd[s.tet][1], f2 = G.fwd[s.tet][2];
-            float x0 = (s.y[1] * f0.x + s.y[2] * f1.x + s.y[3] * f2.x) * G.keep.x;
-            float x1 = (s.y[1] * f0.y + s.y[2] * f1.y + s.y[3] * f2.y) * G.keep.y;
-            float x2 = (s.y[1] * f0.z + s.y[2] * f1.z + s.y[3] * f2.z) * G.keep.z;
-            float d0 = s.U[0] * G.dth.x, d1 = s.U[1] * G.dth.y, d2 = s.U[2] * G.dth.z;
+            float x0, x1, x2;
+            bary_to_cell(s.tet, s.y, x0, x1, x2);
+            x0 *= P.keep[0];
+            x1 *= P.keep[1];
+            x2 *= P.keep[2];
+            float d0 = s.U[0] * P.dth[0], d1 = s.U[1] * P.dth[1], d2 = s.U[2] * P.dth[2];
             float e0 = x0 + d0, e1 = x1 + d1, e2 = x2 + d2;
             int fate = 0;  // 0: moved, 1: removed, 2: reflecting patch (queued)
             unsigned faces = 0;
-            if (fmaxf(fabsf(e0), fmaxf(fabsf(e1), fabsf(e2))) > 0.5f) {
+            const bool out0 = fabsf(e0) > 0.5f, out1 = fabsf(e1) > 0.5f, out2 = fabsf(e2) > 0.5f;
+            if (int(out0) + int(out1) + int(out2) == 1) {
+                // through one face: into the neighbour, whose frame is this
+                // one shifted by a cell along the axis; a patch decides
+                // without the crossing time
+                const int ax = out0 ? 0 : out1 ? 1 : 2;
+                const float ea = out0 ? e0 : out1 ? e1 : e2;
+                const int nb = __ldg(P.m.nbr + 6 * s.cell + 2 * ax + (ea > 0.f ? 1 : 0));
+                faces = 1;
+                if (nb >= 0) {
+                    s.cell = nb;
+                    const float shift = ea > 0.f ? 1.f : -1.f;
+                    e0 = out0 ? e0 - shift : e0;
+                    e1 = out1 ? e1 - shift : e1;
+                    e2 = out2 ? e2 - shift : e2;
+                } else {
+                    const int patch = -nb - 1;
+                    const int kind = kind_s[patch];
+                    fate = 1;
+                    if (kind == PICGPU_PATCH_FLOATING || (kind == PICGPU_PATCH_CIRCUIT && P.q != 0.0))
+                        atomicAdd(P.qconv + patch, P.weight * P.q);
+                    else if (kind != PICGPU_PATCH_ABSORB)
+                        fate = 2;
+                }
+            } else if (out0 || out1 || out2) {
                 // through cell faces: the first face on the way per axis
                 // (|x_a| <= 1/2 after the clamp, so d_a != 0 where |e_a| > 1/2)
                 x0 = fminf(fmaxf(x0, -0.5f), 0.5f);
@@ -594,7 +646,7 @@ __global__ void __launch_bounds__(256, 5) move_cell_kernel_fp32(MoveParams P, in
                 P.xq.queue[start + atomicAdd(&qn, 1)] = ci;
                 continue;
             }
-            cell_locate(G, e0, e1, e2, s);
+            cell_to_bary(e0, e1, e2, s);
             ++ts;
             fc += faces;
             store_rec(P.p, ci, s, 12 * s.cell + s.tet);
@@ -719,7 +771,7 @@ int launch_move_fp32(const MoveParams& P, int grid, cudaStream_t s) {
         chunk = int(per * 256);
         blocks = int((work + chunk - 1) / chunk);
     }
-    const bool cell = P.m.uniform && P.ct32 && P.xq.queue && blocks <= P.xq.capacity;
+    const bool cell = P.cell_mover && P.xq.queue && blocks <= P.xq.capacity;
     switch (P.pusher) {
         case PICGPU_PUSHER_BORIS: return launch_pusher<PICGPU_PUSHER_BORIS>(P, blocks, chunk, cell, s);
         case PICGPU_PUSHER_BORIS_NR: return launch_pusher<PICGPU_PUSHER_BORIS_NR>(P, blocks, chunk, cell, s);

@@ -63,7 +63,7 @@ def test_coulomb_fp64_matches_oracle(gpu, oracle_backend):
 
 
 def test_coulomb_mixed_isotropisation_rate(gpu, oracle_backend):
-    case = cases.coulomb_thermalisation(n_cells=4, per_cell=200, L=2e-5)
+    case = cases.coulomb_thermalisation(n_cells=4, per_cell=800, L=2e-5)
     o = cases.build(case, backend=oracle_backend.OracleBackend(4))
     case.cfg.precision = abi.PREC_MIXED
     g = cases.build(case, backend=gpu)
@@ -76,7 +76,8 @@ def test_coulomb_mixed_isotropisation_rate(gpu, oracle_backend):
     for _ in range(2):
         g.step(25)
         o.step(25)
-        # 12800 electrons: the anisotropy agrees to a few percent
+        # 51200 electrons: the two runs' anisotropies each carry about 1.2 %
+        # of sampling noise (their trajectories decorrelate), so 0.05 is ~3 sigma
         assert abs(anis(g) - anis(o)) < 0.05
 
 
