@@ -528,13 +528,16 @@ __global__ void __launch_bounds__(256, 5) move_cell_kernel_fp32(MoveParams P, in
         s.U[0] = r.u0;
         s.U[1] = r.u1;
         s.U[2] = r.u2;
+        // the outcome: 0 moved, 1 removed, 2 at a reflecting patch (queued).
+        // The rare outcomes set flags only, so the common tail below runs
+        // once for the warp, whatever its lanes met on the way.
+        int fate = 0;
+        unsigned faces = 0;
         if (P.solve_movement) {
             if (P.charged) push32<PUSHER>(P, tri_s, s, P.dt_f);
             if (!(s.U[0] * s.U[0] + s.U[1] * s.U[1] + s.U[2] * s.U[2] < float(kC) * float(kC))) {
                 atomicMax(&P.counters->error, int(PICGPU_SPEED_OF_LIGHT));
-                P.p.tet[ci] = -1;
-                ++ab;
-                continue;
+                fate = 1;
             }
             // the start point in normalised cell coordinates (empty axes: the
             // centre plane) and the displacement U dt
@@ -545,10 +548,10 @@ __global__ void __launch_bounds__(256, 5) move_cell_kernel_fp32(MoveParams P, in
             x2 *= P.keep[2];
             float d0 = s.U[0] * P.dth[0], d1 = s.U[1] * P.dth[1], d2 = s.U[2] * P.dth[2];
             float e0 = x0 + d0, e1 = x1 + d1, e2 = x2 + d2;
-            int fate = 0;  // 0: moved, 1: removed, 2: reflecting patch (queued)
-            unsigned faces = 0;
             const bool out0 = fabsf(e0) > 0.5f, out1 = fabsf(e1) > 0.5f, out2 = fabsf(e2) > 0.5f;
-            if (int(out0) + int(out1) + int(out2) == 1) {
+            if (fate != 0) {
+                // removed before moving
+            } else if (int(out0) + int(out1) + int(out2) == 1) {
                 // through one face: into the neighbour, whose frame is this
                 // one shifted by a cell along the axis; a patch decides
                 // without the crossing time
@@ -631,27 +634,24 @@ __global__ void __launch_bounds__(256, 5) move_cell_kernel_fp32(MoveParams P, in
                     }
                 }
             }
-            if (fate == 1) {
+            if (fate == 0) {
+                cell_to_bary(e0, e1, e2, s);
+                ++ts;
+                store_rec(P.p, ci, s, 12 * s.cell + s.tet);
+            } else if (fate == 1) {
                 P.p.tet[ci] = -1;
                 ++ab;
-                fc += faces;
-                continue;
-            }
-            if (fate == 2) {
+            } else {
                 // a reflecting patch: the crossing tracker repeats this step
                 // from the start record with the pushed velocity
                 __stcs(P.p.u32[0] + ci, s.U[0]);
                 __stcs(P.p.u32[1] + ci, s.U[1]);
                 __stcs(P.p.u32[2] + ci, s.U[2]);
                 P.xq.queue[start + atomicAdd(&qn, 1)] = ci;
-                continue;
             }
-            cell_to_bary(e0, e1, e2, s);
-            ++ts;
             fc += faces;
-            store_rec(P.p, ci, s, 12 * s.cell + s.tet);
         }
-        deposit32(P, tri_s, s, w0, win);
+        if (fate == 0) deposit32(P, tri_s, s, w0, win);
     }
     __syncthreads();
     if (P.has_value) {
