@@ -91,6 +91,32 @@ enum : uint32_t {
     kStreamFreeStream = 15u << 28,       // FreeStream parcels per (injector << 4 | species, step, face)
 };
 
+// The Coulomb stream of a cell and step: the pairing shuffles draw from
+// counter block 0 on; the collision of ordinal k (its position in the
+// sequential pairing order of the cell) draws from blocks 2^31 + 8k on (a
+// collision takes at most three uniforms, two blocks), so that collisions
+// with disjoint parcels can run in any order.
+inline Philox coulomb_pair_stream(uint64_t seed, uint32_t cell, uint32_t step, long k) {
+    Philox p(seed, kStreamCoulomb, cell, step);
+    p.ctr[0] = 0x80000000u + uint32_t(k) * 8u;
+    return p;
+}
+
+// The sum of f(t), t in [0, n), in the order of a 32-lane warp reduction:
+// lane l adds t = l, l + 32, ... from zero, then lanes l < off add lane
+// l + off for off = 16, 8, 4, 2, 1; lane 0 holds the sum.
+template <class F>
+inline double warp_sum(long n, F f) {
+    double p[32];
+    for (int l = 0; l < 32; ++l) {
+        p[l] = 0.0;
+        for (long t = l; t < n; t += 32) p[l] += f(t);
+    }
+    for (int off = 16; off > 0; off >>= 1)
+        for (int l = 0; l < off; ++l) p[l] += p[l + off];
+    return p[0];
+}
+
 // List cross section: interpolateXY (ListCrossSection.C:33-88): linear in
 // energy between the bracketing nodes, end values held outside the table.
 inline double interp_xs(double x, const std::vector<double>& xs, const std::vector<double>& ys) {

@@ -1544,8 +1544,11 @@ void perez_collide(Oracle& o, Parcel& P, int sp, Parcel& Q, int sq, double lD, d
     weight_correct(o, P, sp, Q, sq, preP, preQ, r);
 }
 
+// One Coulomb collision with the random stream of its ordinal in cell c
+// (ord counts the cell's collisions in the sequential pairing order).
 void coulomb_collide(Oracle& o, Parcel& P, int sp, Parcel& Q, int sq, double lD, double nP, double nQ,
-                     double nPQ, ocoll::Philox& r) {
+                     double nPQ, int c, long& ord) {
+    ocoll::Philox r = ocoll::coulomb_pair_stream(o.cfg.seed, uint32_t(c), uint32_t(o.step_index), ord++);
     if (o.cfg.coulomb.collide == 1) perez_collide(o, P, sp, Q, sq, lD, nP, nQ, nPQ, r);
     else nanbu_collide(o, P, sp, Q, sq, lD, nP, nQ, nPQ, r);
 }
@@ -1565,15 +1568,16 @@ double debye_length(const Oracle& o, const std::vector<int>& charged,
     double debye = 0.0, n_max = 0.0;
     for (int s : charged) {
         const double mass = o.cfg.species[s].mass, w = o.cfg.species[s].weight, q = o.cfg.species[s].charge;
-        double vSqr = 0.0, n = 0.0, charge = 0.0;
-        V3 v = v3(0, 0, 0);
-        for (int idx : occ[s][c]) {
-            const Parcel& p = o.cloud[s][idx];
-            vSqr += dotv(p.U, p.U) * w;
-            charge += q * w;
-            v = add(v, smul(w, p.U));
-            n += w;
-        }
+        // the per-species sums in the lane order of the device's warp
+        const std::vector<int>& L = occ[s][c];
+        const long cnt = long(L.size());
+        const auto& cl = o.cloud[s];
+        double vSqr = ocoll::warp_sum(cnt, [&](long t) { return dotv(cl[L[t]].U, cl[L[t]].U) * w; });
+        double charge = ocoll::warp_sum(cnt, [&](long) { return q * w; });
+        V3 v = v3(ocoll::warp_sum(cnt, [&](long t) { return w * cl[L[t]].U.x; }),
+                  ocoll::warp_sum(cnt, [&](long t) { return w * cl[L[t]].U.y; }),
+                  ocoll::warp_sum(cnt, [&](long t) { return w * cl[L[t]].U.z; }));
+        double n = ocoll::warp_sum(cnt, [&](long) { return w; });
         if (n <= 0.0) continue;
         v = sdiv(v, n);
         charge /= n;
@@ -1601,7 +1605,10 @@ void coulomb_pairs(Oracle& o, std::vector<std::vector<std::vector<int>>>& occ, p
     long long pairs = 0;
     for (int c = 0; c < o.m.n_cells; ++c) {
         const double V = o.m.vol[c];
+        // the shuffles draw from the cell's stream in order, each collision
+        // from the counter range of its ordinal
         ocoll::Philox r(o.cfg.seed, ocoll::kStreamCoulomb, uint32_t(c), uint32_t(o.step_index));
+        long ord = 0;
         const double lD = need_debye ? debye_length(o, charged, occ, c) : 0.0;
         for (size_t i = 0; i < charged.size(); ++i) {
             for (size_t jj = charged.size(); jj-- > 0;) {
@@ -1627,15 +1634,15 @@ void coulomb_pairs(Oracle& o, std::vector<std::vector<std::vector<int>>>& occ, p
                             Parcel& P = ca[LA[sel[0]]];
                             Parcel& Q = ca[LA[sel[1]]];
                             Parcel& R = ca[LA[sel[2]]];
-                            coulomb_collide(o, P, a, Q, a, lD, n, n, n12, r);
-                            coulomb_collide(o, Q, a, R, a, lD, n, n, n12, r);
-                            coulomb_collide(o, P, a, R, a, lD, n, n, n12, r);
+                            coulomb_collide(o, P, a, Q, a, lD, n, n, n12, c, ord);
+                            coulomb_collide(o, Q, a, R, a, lD, n, n, n12, c, ord);
+                            coulomb_collide(o, P, a, R, a, lD, n, n, n12, c, ord);
                             for (long x = 3; x < nA - 1; x += 2)
-                                coulomb_collide(o, ca[LA[sel[x]]], a, ca[LA[sel[x + 1]]], a, lD, n, n, n12, r);
+                                coulomb_collide(o, ca[LA[sel[x]]], a, ca[LA[sel[x + 1]]], a, lD, n, n, n12, c, ord);
                             pairs += 2 + nA / 2;
                         } else {
                             for (long x = 0; x < nA - 1; x += 2)
-                                coulomb_collide(o, ca[LA[sel[x]]], a, ca[LA[sel[x + 1]]], a, lD, n, n, n, r);
+                                coulomb_collide(o, ca[LA[sel[x]]], a, ca[LA[sel[x + 1]]], a, lD, n, n, n, c, ord);
                             pairs += nA / 2;
                         }
                         continue;
@@ -1646,15 +1653,15 @@ void coulomb_pairs(Oracle& o, std::vector<std::vector<std::vector<int>>>& occ, p
                         for (long x = 0; x < nA - 2; x += 2) nAA += 2.0 * wA;
                         const double n12 = nAA / V;
                         for (long x = 0; x < nA - 2; x += 2)
-                            coulomb_collide(o, ca[LA[sel[x]]], a, ca[LA[sel[x + 1]]], a, lD, n, n, n12, r);
-                        coulomb_collide(o, ca[LA[sel[nA - 1]]], a, ca[LA[sel[0]]], a, lD, n, n, n12, r);
+                            coulomb_collide(o, ca[LA[sel[x]]], a, ca[LA[sel[x + 1]]], a, lD, n, n, n12, c, ord);
+                        coulomb_collide(o, ca[LA[sel[nA - 1]]], a, ca[LA[sel[0]]], a, lD, n, n, n12, c, ord);
                         pairs += 1 + nA / 2;
                     } else {
                         double nAA = 0.0;
                         for (long x = 0; x < nA - 1; x += 2) nAA += 2.0 * wA;
                         const double n12 = nAA / V;
                         for (long x = 0; x < nA - 1; x += 2)
-                            coulomb_collide(o, ca[LA[sel[x]]], a, ca[LA[sel[x + 1]]], a, lD, n, n, n12, r);
+                            coulomb_collide(o, ca[LA[sel[x]]], a, ca[LA[sel[x + 1]]], a, lD, n, n, n12, c, ord);
                         pairs += nA / 2;
                     }
                 } else if (a != b && std::min(nA, nB) != 0) {
@@ -1676,7 +1683,7 @@ void coulomb_pairs(Oracle& o, std::vector<std::vector<std::vector<int>>>& occ, p
                             nPQ = nAB / V;
                         }
                         for (long k = 0; k < nA; ++k)
-                            coulomb_collide(o, ca[LA[sel[k]]], a, cb[LB[sel[nA - k - 1]]], b, lD, nP, nQ, nPQ, r);
+                            coulomb_collide(o, ca[LA[sel[k]]], a, cb[LB[sel[nA - k - 1]]], b, lD, nP, nQ, nPQ, c, ord);
                         pairs += nA;
                     } else {
                         const int minS = nA < nB ? a : b, maxS = nA > nB ? a : b;
@@ -1702,7 +1709,7 @@ void coulomb_pairs(Oracle& o, std::vector<std::vector<std::vector<int>>>& occ, p
                                 for (long g = 0; g < g1max; ++g) {
                                     if (s1 >= g1min) s1 = 0;
                                     coulomb_collide(o, cmax[Lmax[smax[s2]]], maxS, cmin[Lmin[smin[s1]]], minS, lD, nMaxS,
-                                                    nMinS, nMaxS, r);
+                                                    nMinS, nMaxS, c, ord);
                                     ++s1;
                                     ++s2;
                                 }
@@ -1712,7 +1719,7 @@ void coulomb_pairs(Oracle& o, std::vector<std::vector<std::vector<int>>>& occ, p
                             for (long g = 0; g < g2max; ++g) {
                                 if (s1 >= g2min + g1min) s1 = g1min;
                                 coulomb_collide(o, cmax[Lmax[smax[s2]]], maxS, cmin[Lmin[smin[s1]]], minS, lD, nMaxS,
-                                                nMinS, nMaxS, r);
+                                                nMinS, nMaxS, c, ord);
                                 ++s1;
                                 ++s2;
                             }
@@ -1728,7 +1735,7 @@ void coulomb_pairs(Oracle& o, std::vector<std::vector<std::vector<int>>>& occ, p
                         for (long l = 0; l < nMax; ++l) {
                             if (k >= nMin) k = 0;
                             coulomb_collide(o, cmax[Lmax[smax[l]]], maxS, cmin[Lmin[smin[k]]], minS, lD, nMaxS, nMinS,
-                                            n12, r);
+                                            n12, c, ord);
                             ++k;
                         }
                         pairs += nMax;

@@ -20,7 +20,7 @@
 //                    with NanbuCollision::collide (NanbuCollision.C:60-161) or
 //                    PerezRelativisticCollision::collide (PerezRelativisticCollision.C:60-220),
 //                    fixed or Debye-length Coulomb logarithm
-//                    (CoulombCollisionModel.C:249-309), one thread per cell
+//                    (CoulombCollisionModel.C:249-309), one warp per cell
 // The collision arithmetic is FP64 for both particle forms.
 #include <algorithm>
 #include <vector>
@@ -1067,23 +1067,41 @@ __device__ __forceinline__ void collide(const CoulombSpecies& C, const CoulombPa
 }
 
 // CoulombCollisionModel::debyeLength (CoulombCollisionModel.C:249-309) over
-// the colliding species of cell c, before any of its pairs collide.
+// the colliding species of cell c, before any of its pairs collide, by the
+// cell's warp: lane l sums the parcels l, l + 32, ... of a species, the
+// lanes' sums are added in a fixed tree (lane l < off takes lane l + off's
+// for off = 16 .. 1), so the result does not depend on scheduling.  Every
+// lane returns the length.
+__device__ __forceinline__ double warp_tree_sum(double v) {
+#pragma unroll
+    for (int off = 16; off > 0; off >>= 1) v += __shfl_down_sync(0xffffffffu, v, off);
+    return __shfl_sync(0xffffffffu, v, 0);
+}
+
 template <class R>
-__device__ double debye_length(const CoulombSpecies& C, const CoulombParams& K, int c) {
+__device__ double debye_length_warp(const CoulombSpecies& C, const CoulombParams& K, int c, int lane) {
     double debye = 0.0, n_max = 0.0;
     for (int k = 0; k < C.n; ++k) {
         const double w = C.w[k], q = C.q[k];
-        double vSqr = 0.0, n = 0.0, charge = 0.0;
-        V3d v = {0.0, 0.0, 0.0};
-        for (int t = C.start[k][c]; t < C.start[k][c + 1]; ++t) {
+        double vSqr = 0.0, n = 0.0, charge = 0.0, vx = 0.0, vy = 0.0, vz = 0.0;
+        const int s0 = C.start[k][c], s1 = C.start[k][c + 1];
+        for (int t = s0 + lane; t < s1; t += 32) {
             const V3d U = Vel<R>::get(C.p[k], C.idx[k][t]);
             vSqr += dotd(U, U) * w;
             charge += q * w;
-            v = {v.x + w * U.x, v.y + w * U.y, v.z + w * U.z};
+            vx += w * U.x;
+            vy += w * U.y;
+            vz += w * U.z;
             n += w;
         }
+        vSqr = warp_tree_sum(vSqr);
+        charge = warp_tree_sum(charge);
+        vx = warp_tree_sum(vx);
+        vy = warp_tree_sum(vy);
+        vz = warp_tree_sum(vz);
+        n = warp_tree_sum(n);
         if (n <= 0.0) continue;
-        v = {v.x / n, v.y / n, v.z / n};
+        V3d v = {vx / n, vy / n, vz / n};
         charge /= n;
         vSqr /= n;
         n /= K.vol[c];
@@ -1098,21 +1116,80 @@ __device__ double debye_length(const CoulombSpecies& C, const CoulombParams& K, 
     return fmax(r_min, sqrt(1 / debye));
 }
 
-__device__ void shuffle(int* a, int n, Rng& r) {
-    for (int k = n - 1; k > 0; --k) {
-        int j = int(r.uniform() * double(k + 1));
-        if (j > k) j = k;
-        const int t = a[k]; a[k] = a[j]; a[j] = t;
+// The random numbers of a cell's Coulomb step.  The shuffles take the
+// uniforms of the cell's stream (seed, Coulomb, cell, step) in order: draw t
+// is the (t & 1) half of counter block t / 2, so any lane can compute any
+// draw.  The collision of ordinal k (its position in the sequential pairing
+// order of the cell) draws from counter blocks 2^31 + 8 k on (at most three
+// uniforms), so collisions of disjoint parcels can run on different lanes.
+struct CellStream {
+    uint64_t seed;
+    uint32_t cell, step;
+    __device__ double draw(long t) const {
+        Philox p(seed, kStreamCoulomb, cell, step);
+        p.c0 = uint32_t(t >> 1);
+        p.block();
+        p.used = int(t & 1) * 2;
+        return p.uniform();
     }
+    __device__ Rng collision(long k) const {
+        Rng r(seed, kStreamCoulomb, cell, step);
+        r.p.c0 = 0x80000000u + uint32_t(k) * 8u;
+        return r;
+    }
+};
+
+// Fisher-Yates over sel[0, n) with the draws nd, nd + 1, ... (draw
+// nd + n - 1 - k picks the partner of position k): the lanes compute 32
+// draws at a time, lane 0 applies their swaps in order.
+__device__ void shuffle_warp(int* sel, int n, const CellStream& cs, long& nd, int lane) {
+    for (int k = lane; k < n; k += 32) sel[k] = k;
+    __syncwarp();
+    for (int base = 0; base < n - 1; base += 32) {
+        const int t = base + lane;
+        int j = 0;
+        if (t < n - 1) {
+            const int k = n - 1 - t;
+            j = int(cs.draw(nd + t) * double(k + 1));
+            if (j > k) j = k;
+        }
+        const int m = min(32, n - 1 - base);
+        for (int q = 0; q < m; ++q) {
+            const int jq = __shfl_sync(0xffffffffu, j, q);
+            if (lane == 0) {
+                const int k = n - 1 - (base + q);
+                const int tmp = sel[k];
+                sel[k] = sel[jq];
+                sel[jq] = tmp;
+            }
+        }
+    }
+    __syncwarp();
+    nd += n > 1 ? n - 1 : 0;
 }
 
+// Per-warp shared buffers for the shuffled positions; larger cells use the
+// species' global scratch (same layout as the cell lists).
+constexpr int kCoulombWarps = 4;
+constexpr int kCoulombShared = 512;
+
+// NanbuYonemuraPairing::pairANDcollide (NanbuYonemuraPairing.C:56-325) and
+// TakizukaAbePairing::pairANDcollide (TakizukaAbePairing.C:60-341), one warp
+// per cell.  The pairings and their collision parameters are the sequential
+// ones; each collision gets the random stream of its ordinal, and the lanes
+// take chains of collisions that share no parcel: disjoint pairs one each,
+// and where one parcel meets several partners (odd counts, unequal species
+// counts) the partners of that parcel in their sequential order.
 template <class R>
-__global__ void coulomb_kernel(CoulombSpecies C, CoulombParams K) {
-    const int c = blockIdx.x * blockDim.x + threadIdx.x;
-    if (c >= K.n_cells) return;
+__global__ void __launch_bounds__(32 * kCoulombWarps) coulomb_kernel(CoulombSpecies C, CoulombParams K) {
+    __shared__ int sh_sel[kCoulombWarps][2][kCoulombShared];
+    const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
+    const int c = int((long(blockIdx.x) * blockDim.x + threadIdx.x) >> 5);
+    if (c >= K.n_cells) return;  // warp-uniform
     const double V = K.vol[c];
-    Rng r(K.seed, kStreamCoulomb, uint32_t(c), K.step_dev ? *K.step_dev : K.step);
-    const double lD = K.cl == 0.0 ? debye_length<R>(C, K, c) : 0.0;
+    const CellStream cs{K.seed, uint32_t(c), K.step_dev ? *K.step_dev : K.step};
+    const double lD = K.cl == 0.0 ? debye_length_warp<R>(C, K, c, lane) : 0.0;
+    long nd = 0, ord = 0;
     unsigned long long pairs = 0;
     for (int i = 0; i < C.n; ++i) {
         for (int jj = C.n - 1; jj >= i; --jj) {
@@ -1125,52 +1202,77 @@ __global__ void coulomb_kernel(CoulombSpecies C, CoulombParams K) {
             const double sB = a != b ? double(nB) * C.w[b] : 0.0;
             if (a == b && nA > 1) {
                 if (!K.allow_intra) continue;
-                int* sel = C.sel[a] + sa;
-                for (int k = 0; k < nA; ++k) sel[k] = k;
-                shuffle(sel, nA, r);
+                int* sel = nA <= kCoulombShared ? sh_sel[wib][0] : C.sel[a] + sa;
+                shuffle_warp(sel, nA, cs, nd, lane);
                 if (K.takizuka_abe) {
                     // TakizukaAbePairing.C:108-153: an odd count collides
-                    // P-Q, Q-R and P-R, then pairs from the fourth parcel on
+                    // P-Q, Q-R and P-R (one chain), then pairs from the
+                    // fourth parcel on
                     const double n = double(nA) * C.w[a] / V;
                     if (nA % 2 != 0) {
                         const double n12 = (double(nA) + 3.0) * C.w[a] / V;
-                        const int P = LA[sel[0]], Q = LA[sel[1]], Rr = LA[sel[2]];
-                        collide<R>(C, K, a, P, a, Q, lD, n, n, n12, r);
-                        collide<R>(C, K, a, Q, a, Rr, lD, n, n, n12, r);
-                        collide<R>(C, K, a, P, a, Rr, lD, n, n, n12, r);
-                        for (int x = 3; x < nA - 1; x += 2)
-                            collide<R>(C, K, a, LA[sel[x]], a, LA[sel[x + 1]], lD, n, n, n12, r);
+                        if (lane == 0) {
+                            const int P = LA[sel[0]], Q = LA[sel[1]], Rr = LA[sel[2]];
+                            Rng r0 = cs.collision(ord), r1 = cs.collision(ord + 1), r2 = cs.collision(ord + 2);
+                            collide<R>(C, K, a, P, a, Q, lD, n, n, n12, r0);
+                            collide<R>(C, K, a, Q, a, Rr, lD, n, n, n12, r1);
+                            collide<R>(C, K, a, P, a, Rr, lD, n, n, n12, r2);
+                        }
+                        const int np = (nA - 3) / 2;
+                        for (int x = lane; x < np; x += 32) {
+                            Rng r = cs.collision(ord + 3 + x);
+                            collide<R>(C, K, a, LA[sel[3 + 2 * x]], a, LA[sel[4 + 2 * x]], lD, n, n, n12, r);
+                        }
+                        ord += 3 + np;
                         pairs += 2 + nA / 2;
                     } else {
-                        for (int x = 0; x < nA - 1; x += 2)
-                            collide<R>(C, K, a, LA[sel[x]], a, LA[sel[x + 1]], lD, n, n, n, r);
+                        const int np = nA / 2;
+                        for (int x = lane; x < np; x += 32) {
+                            Rng r = cs.collision(ord + x);
+                            collide<R>(C, K, a, LA[sel[2 * x]], a, LA[sel[2 * x + 1]], lD, n, n, n, r);
+                        }
+                        ord += np;
                         pairs += nA / 2;
                     }
+                    __syncwarp();
                     continue;
                 }
                 const double n = sA / V;
                 if (nA % 2 != 0) {
+                    // the pairs (0 1) (2 3) ... then (nA-1 0): the last
+                    // collision follows the first one's on parcel sel[0]
                     double nAA = 2.0 * C.w[a];
                     for (int x = 0; x < nA - 2; x += 2) nAA += 2.0 * C.w[a];
                     const double n12 = nAA / V;
-                    for (int x = 0; x < nA - 2; x += 2)
-                        collide<R>(C, K, a, LA[sel[x]], a, LA[sel[x + 1]], lD, n, n, n12, r);
-                    collide<R>(C, K, a, LA[sel[nA - 1]], a, LA[sel[0]], lD, n, n, n12, r);
+                    const int np = (nA - 1) / 2;
+                    for (int x = lane; x < np; x += 32) {
+                        Rng r = cs.collision(ord + x);
+                        collide<R>(C, K, a, LA[sel[2 * x]], a, LA[sel[2 * x + 1]], lD, n, n, n12, r);
+                        if (x == 0) {
+                            Rng rl = cs.collision(ord + np);
+                            collide<R>(C, K, a, LA[sel[nA - 1]], a, LA[sel[0]], lD, n, n, n12, rl);
+                        }
+                    }
+                    ord += np + 1;
                     pairs += 1 + nA / 2;
                 } else {
                     double nAA = 0.0;
                     for (int x = 0; x < nA - 1; x += 2) nAA += 2.0 * C.w[a];
                     const double n12 = nAA / V;
-                    for (int x = 0; x < nA - 1; x += 2)
-                        collide<R>(C, K, a, LA[sel[x]], a, LA[sel[x + 1]], lD, n, n, n12, r);
+                    const int np = nA / 2;
+                    for (int x = lane; x < np; x += 32) {
+                        Rng r = cs.collision(ord + x);
+                        collide<R>(C, K, a, LA[sel[2 * x]], a, LA[sel[2 * x + 1]], lD, n, n, n12, r);
+                    }
+                    ord += np;
                     pairs += nA / 2;
                 }
+                __syncwarp();
             } else if (a != b && min(nA, nB) != 0) {
                 const double wmin = fmin(C.w[a], C.w[b]);
                 if (nA == nB) {
-                    int* sel = C.sel[a] + sa;
-                    for (int k = 0; k < nA; ++k) sel[k] = k;
-                    shuffle(sel, nA, r);
+                    int* sel = nA <= kCoulombShared ? sh_sel[wib][0] : C.sel[a] + sa;
+                    shuffle_warp(sel, nA, cs, nd, lane);
                     double nP, nQ, nPQ;
                     if (K.takizuka_abe) {
                         nP = double(nA) * C.w[a] / V;
@@ -1183,8 +1285,11 @@ __global__ void coulomb_kernel(CoulombSpecies C, CoulombParams K) {
                         for (int k = 0; k < nA; ++k) nAB += wmin;
                         nPQ = nAB / V;
                     }
-                    for (int k = 0; k < nA; ++k)
+                    for (int k = lane; k < nA; k += 32) {
+                        Rng r = cs.collision(ord + k);
                         collide<R>(C, K, a, LA[sel[k]], b, LB[sel[nA - k - 1]], lD, nP, nQ, nPQ, r);
+                    }
+                    ord += nA;
                     pairs += nA;
                 } else {
                     const bool aMin = nA < nB;
@@ -1192,15 +1297,15 @@ __global__ void coulomb_kernel(CoulombSpecies C, CoulombParams K) {
                     const int* Lmin = aMin ? LA : LB;
                     const int* Lmax = aMin ? LB : LA;
                     const int nMax = max(nA, nB), nMin = min(nA, nB);
-                    int* smin = C.sel[minS] + (aMin ? sa : sb);
-                    int* smax = C.sel2[maxS] + (aMin ? sb : sa);
-                    for (int k = 0; k < nMax; ++k) { smax[k] = k; if (k < nMin) smin[k] = k; }
-                    shuffle(smin, nMin, r);
-                    shuffle(smax, nMax, r);
+                    int* smin = nMin <= kCoulombShared ? sh_sel[wib][0] : C.sel[minS] + (aMin ? sa : sb);
+                    int* smax = nMax <= kCoulombShared ? sh_sel[wib][1] : C.sel2[maxS] + (aMin ? sb : sa);
+                    shuffle_warp(smin, nMin, cs, nd, lane);
+                    shuffle_warp(smax, nMax, cs, nd, lane);
                     if (K.takizuka_abe) {
                         // TakizukaAbePairing.C:197-314: group 1 spreads the
                         // remainder nMax % nMin over delta + 1 partners each,
-                        // group 2 gives the other minority parcels delta each
+                        // group 2 gives the other minority parcels delta
+                        // each; a lane takes one minority parcel's partners
                         const double nMinS = double(nMin) * C.w[a] / V, nMaxS = double(nMax) * C.w[a] / V;
                         const int delta = nMax / nMin;
                         const double delta_r = double(nMax % nMin) / double(nMin);
@@ -1208,25 +1313,27 @@ __global__ void coulomb_kernel(CoulombSpecies C, CoulombParams K) {
                         const int g1max = int(double(delta + 1) * delta_r * double(nMin));
                         const int g2min = int((1.0 - delta_r) * double(nMin));
                         const int g2max = int(double(delta) * (1.0 - delta_r) * double(nMin));
-                        int s1 = 0, s2 = 0;
                         if (g1min > 0) {
-                            for (int g = 0; g < g1max; ++g) {
-                                if (s1 >= g1min) s1 = 0;
-                                collide<R>(C, K, maxS, Lmax[smax[s2]], minS, Lmin[smin[s1]], lD, nMaxS, nMinS, nMaxS,
-                                           r);
-                                ++s1;
-                                ++s2;
+                            for (int k = lane; k < g1min && k < g1max; k += 32)
+                                for (int g = k; g < g1max; g += g1min) {
+                                    Rng r = cs.collision(ord + g);
+                                    collide<R>(C, K, maxS, Lmax[smax[g]], minS, Lmin[smin[k]], lD, nMaxS, nMinS,
+                                               nMaxS, r);
+                                }
+                            ord += g1max;
+                        }
+                        // minority position g1min + g mod g2min (all g1min
+                        // when g2min is 0), majority g1max + g
+                        const int chains = g2min > 0 ? g2min : 1;
+                        for (int k = lane; k < chains && k < g2max; k += 32)
+                            for (int g = k; g < g2max; g += chains) {
+                                Rng r = cs.collision(ord + g);
+                                collide<R>(C, K, maxS, Lmax[smax[g1max + g]], minS, Lmin[smin[g1min + k]], lD, nMaxS,
+                                           nMinS, nMaxS, r);
                             }
-                        }
-                        s1 = g1min;
-                        s2 = g1max;
-                        for (int g = 0; g < g2max; ++g) {
-                            if (s1 >= g2min + g1min) s1 = g1min;
-                            collide<R>(C, K, maxS, Lmax[smax[s2]], minS, Lmin[smin[s1]], lD, nMaxS, nMinS, nMaxS, r);
-                            ++s1;
-                            ++s2;
-                        }
+                        ord += g2max;
                         pairs += g1max + g2max;
+                        __syncwarp();
                         continue;
                     }
                     const double nMaxS = (maxS == a ? sA : sB) / V;
@@ -1234,18 +1341,27 @@ __global__ void coulomb_kernel(CoulombSpecies C, CoulombParams K) {
                     double nAB = 0.0;
                     for (int l = 0; l < nMax; ++l) nAB += wmin;
                     const double n12 = nAB / V;
-                    int k = 0;
-                    for (int l = 0; l < nMax; ++l) {
-                        if (k >= nMin) k = 0;
-                        collide<R>(C, K, maxS, Lmax[smax[l]], minS, Lmin[smin[k]], lD, nMaxS, nMinS, n12, r);
-                        ++k;
-                    }
+                    // majority parcel l meets minority parcel l mod nMin
+                    for (int k = lane; k < nMin; k += 32)
+                        for (int l = k; l < nMax; l += nMin) {
+                            Rng r = cs.collision(ord + l);
+                            collide<R>(C, K, maxS, Lmax[smax[l]], minS, Lmin[smin[k]], lD, nMaxS, nMinS, n12, r);
+                        }
+                    ord += nMax;
                     pairs += nMax;
                 }
+                __syncwarp();
             }
         }
     }
-    if (pairs) atomicAdd(K.counts + 4, pairs);
+    if (pairs && lane == 0) atomicAdd(K.counts + 4, pairs);
+}
+
+void launch_coulomb(const CoulombSpecies& C, const CoulombParams& K, bool mixed, cudaStream_t stream) {
+    const int threads = 32 * kCoulombWarps;
+    const unsigned blocks = unsigned((long(K.n_cells) * 32 + threads - 1) / threads);
+    if (mixed) coulomb_kernel<float><<<blocks, threads, 0, stream>>>(C, K);
+    else coulomb_kernel<double><<<blocks, threads, 0, stream>>>(C, K);
 }
 
 template <class T>
@@ -2157,8 +2273,7 @@ int run_collisions(CollideState& st, const CollideArgs& a, int64_t counts[kColli
         CoulombSpecies C;
         CoulombParams K;
         coulomb_setup(st, a, C, K);
-        if (a.mixed) coulomb_kernel<float><<<(nc + 63) / 64, 64, 0, a.stream>>>(C, K);
-        else coulomb_kernel<double><<<(nc + 63) / 64, 64, 0, a.stream>>>(C, K);
+        launch_coulomb(C, K, a.mixed, a.stream);
         *launches += 1;
     }
     if (cfg.mcc.enabled && cfg.mcc.neutral_parcels) {
@@ -2346,8 +2461,7 @@ int run_collisions_device(CollideState& st, const CollideArgs& a, int* n_dev, in
         CoulombParams K;
         coulomb_setup(st, a, C, K);
         K.step_dev = step_dev;
-        if (a.mixed) coulomb_kernel<float><<<(nc + 63) / 64, 64, 0, a.stream>>>(C, K);
-        else coulomb_kernel<double><<<(nc + 63) / 64, 64, 0, a.stream>>>(C, K);
+        launch_coulomb(C, K, a.mixed, a.stream);
         *launches += 1;
     }
     if (cfg.mcc.enabled) {

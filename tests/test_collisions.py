@@ -302,8 +302,9 @@ def test_perez_conserves_relativistic_momentum_and_energy(oracle_backend):
 
 
 def test_perez_matches_nanbu_at_low_temperature(oracle_backend):
-    # the Perez scattering parameter reduces to Nanbu's when v << c, and both
-    # draw cos(chi) then the azimuth from the same streams
+    # the Perez scattering parameter reduces to Nanbu's when v << c (up to
+    # its low-temperature cap s_max), and both draw cos(chi) then the
+    # azimuth from the same streams: the anisotropies agree to 2 %
     out = []
     for col in (abi.COLLIDE_NANBU, abi.COLLIDE_PEREZ):
         case = cases.coulomb_thermalisation(n_cells=4, per_cell=200, L=2e-5, collide=col)
@@ -312,7 +313,7 @@ def test_perez_matches_nanbu_at_low_temperature(oracle_backend):
         d = sim.diagnostics()
         v = np.array(d.velocity_sq[0]) / d.weight_sum[0]
         out.append(v[0] / (0.5 * (v[1] + v[2])))
-    assert out[0] < 1.9 and abs(out[0] - out[1]) < 1e-2
+    assert out[0] < 1.9 and abs(out[0] - out[1]) < 2e-2
 
 
 def test_debye_length_matches_formula(oracle_backend):
