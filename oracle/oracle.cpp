@@ -2585,6 +2585,108 @@ struct oracle_ctx {
 
 extern "C" {
 
+// Known-answer checks of the oracle's mesh from first principles; out[k] is
+// the worst deviation of check k (all should be at round-off):
+//  0 tet volumes summed per cell against the cell volume dx dy dz (relative)
+//  1 position(locate(x)) - x over pseudo-random points (per cell size)
+//  2 barycentric coordinates of each tet's own vertices against unit vectors
+//  3 the Gauss Laplacian of a linear potential in cells without boundary faces
+//    (relative to the sum of the coefficients' magnitudes)
+//  4 the distance weights of VolumeWeighting summed over the cells at a point, minus 1
+//  5 the point-interpolation weights summed per point, minus 1
+//  6 the outward face area vectors summed over a cell (closed surface), per face area
+//  7 tet moves: crossing a face and crossing back returns the start tet (0 or 1)
+// Returns the number of checks, or -1 when the mesh cannot be built.
+int oracle_mesh_selfcheck(const picgpu_mesh_desc* desc, double* out, int n_out) {
+    om::Mesh m;
+    try {
+        m = om::build(*desc);
+    } catch (const std::exception&) {
+        return -1;
+    }
+    double r[8] = {0, 0, 0, 0, 0, 0, 0, 0};
+    double h[3], vcell = 1.0;
+    for (int a = 0; a < 3; ++a) {
+        h[a] = desc->length[a] / desc->n[a];
+        vcell *= h[a];
+    }
+    double vt = 0.0;
+    for (int t = 0; t < 12; ++t) vt += om::tet_volume(m, 0, t);
+    r[0] = std::fabs(vt - vcell) / vcell;
+    uint64_t lcg = 0x9E3779B97F4A7C15ull;
+    auto uni = [&lcg]() {
+        lcg = lcg * 6364136223846793005ull + 1442695040888963407ull;
+        return double(lcg >> 11) * (1.0 / 9007199254740992.0);
+    };
+    for (int k = 0; k < 4000; ++k) {
+        double x[3], y[3], back[3];
+        for (int a = 0; a < 3; ++a) x[a] = desc->origin[a] + desc->length[a] * (0.001 + 0.998 * uni());
+        const long long tet = om::locate(m, x, y);
+        if (tet < 0) continue;  // inside a removed box
+        om::position(m, tet, y, back);
+        for (int a = 0; a < 3; ++a) r[1] = std::fmax(r[1], std::fabs(back[a] - x[a]) / h[a]);
+    }
+    const double* off = m.cls_offset.data();
+    for (int t = 0; t < 12; ++t)
+        for (int v = 0; v < 3; ++v) {
+            double x[3], y[3];
+            for (int a = 0; a < 3; ++a) x[a] = m.cc[a] + off[3 * m.tt.tri[t][v] + a];
+            om::tet_coords(m, 0, t, x, y);
+            for (int k = 0; k < 3; ++k) r[2] = std::fmax(r[2], std::fabs(y[k] - (k == v ? 1.0 : 0.0)));
+        }
+    const double g[3] = {0.3, -1.7, 2.9};
+    for (int c = 0; c < m.n_cells; ++c) {
+        bool inner = true;
+        for (int f = 0; f < 6; ++f) {
+            const int nb = m.nbr[6 * size_t(c) + f];
+            // a coupled face that wraps (cyclic) does not see a linear field
+            if (nb < 0 || std::abs(m.cell_ijk[3 * size_t(nb) + f / 2] - m.cell_ijk[3 * size_t(c) + f / 2]) != 1)
+                inner = false;
+        }
+        if (!inner) continue;
+        double lap = 0.0, scale = 0.0;
+        for (int f = 0; f < 6; ++f) {
+            const int nb = m.nbr[6 * size_t(c) + f];
+            double dphi = 0.0;
+            for (int a = 0; a < 3; ++a) dphi += g[a] * (m.cc[3 * size_t(nb) + a] - m.cc[3 * size_t(c) + a]);
+            lap += m.lap_off[6 * size_t(c) + f] * dphi;
+            scale += std::fabs(m.lap_off[6 * size_t(c) + f] * dphi);
+        }
+        if (scale > 0) r[3] = std::fmax(r[3], std::fabs(lap) / scale);
+    }
+    // points inside removed boxes touch no cell and carry no weights
+    std::vector<double> wsum(m.n_points, 0.0);
+    std::vector<char> used(m.n_points, 0);
+    for (int c = 0; c < m.n_cells; ++c)
+        for (int q = 0; q < 8; ++q) {
+            wsum[m.cell_pt[8 * size_t(c) + q]] += m.vw_weight[8 * size_t(c) + q];
+            used[m.cell_pt[8 * size_t(c) + q]] = 1;
+        }
+    for (int p = 0; p < m.n_points; ++p)
+        if (used[p]) r[4] = std::fmax(r[4], std::fabs(wsum[p] - 1.0));
+    for (int p = 0; p < m.n_points; ++p) {
+        if (!used[p]) continue;
+        double w = 0.0;
+        for (int k = m.pi_start[p]; k < m.pi_start[p + 1]; ++k) w += m.pi_w[k];
+        r[5] = std::fmax(r[5], std::fabs(w - 1.0));
+    }
+    double S[3] = {0, 0, 0};
+    for (int f = 0; f < 6; ++f)
+        for (int a = 0; a < 3; ++a) S[a] += m.cls_farea[f] * m.cls_fnormal[3 * f + a];
+    r[6] = std::sqrt(S[0] * S[0] + S[1] * S[1] + S[2] * S[2]) / m.cls_farea[0];
+    for (int t = 0; t < 12; ++t) {
+        for (int i = 1; i <= 3; ++i) {
+            const int u = m.tt.inner_next[t][i];
+            bool back = false;
+            for (int j = 1; j <= 3; ++j) back |= m.tt.inner_next[u][j] == t;
+            if (!back) r[7] = 1.0;
+        }
+        if (m.tt.cross_next[m.tt.cross_next[t]] != t) r[7] = 1.0;
+    }
+    for (int k = 0; k < n_out && k < 8; ++k) out[k] = r[k];
+    return 8;
+}
+
 int oracle_create(const picgpu_mesh_desc* mesh, const picgpu_config* cfg, int nthreads,
                   oracle_ctx** out) {
     if (!mesh || !cfg || !out) return PICGPU_INVALID_ARG;

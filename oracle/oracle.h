@@ -38,6 +38,8 @@ void oracle_destroy(oracle_ctx* ctx);
 const char* oracle_last_error(const oracle_ctx* ctx);
 int  oracle_set_precond(oracle_ctx* ctx, int precond);
 int  oracle_mesh_query(const oracle_ctx* ctx, picgpu_mesh_info* info);
+int  oracle_mesh_selfcheck(const picgpu_mesh_desc* desc, double* out, int n_out);
+int  oracle_set_step_index(oracle_ctx* ctx, int64_t steps_done);
 int  oracle_set_particles(oracle_ctx* ctx, int species, size_t n, const int32_t* tet,
                           const double* bary, const double* U);
 int  oracle_count_particles(oracle_ctx* ctx, int species, size_t* n);

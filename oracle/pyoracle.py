@@ -49,6 +49,8 @@ def load():
         lib.oracle_set_precond.argtypes = [P, C.c_int]
         lib.oracle_mesh_query.restype = C.c_int
         lib.oracle_mesh_query.argtypes = [P, C.POINTER(abi.MeshInfo)]
+        lib.oracle_mesh_selfcheck.restype = C.c_int
+        lib.oracle_mesh_selfcheck.argtypes = [C.POINTER(abi.MeshDesc), C.POINTER(C.c_double), C.c_int]
         lib.oracle_move_seconds.restype = C.c_double
         lib.oracle_move_seconds.argtypes = [P]
         lib.oracle_philox4x32.restype = None
