@@ -75,6 +75,11 @@ def parse():
                    help="Poisson preconditioner of the electrode driver")
     p.add_argument("--no-multigrid", action="store_true", help="skip the multigrid-preconditioned Poisson arm")
     p.add_argument("--no-init", action="store_true", help="skip the device initial-condition measurement")
+    p.add_argument("--no-forms", action="store_true",
+                   help="skip the FP64 form and the BorisNR / Vay / Higuera-Cary runs of the workload")
+    p.add_argument("--no-collisions", action="store_true", help="skip the MCC swarm and Coulomb timings")
+    p.add_argument("--pusher", default="boris", choices=["boris", "boris_nr", "vay", "hc"],
+                   help="pusher of the headline workload")
     return p.parse_args()
 
 
@@ -175,11 +180,16 @@ class Clocks:
                 "reasons": sorted(reasons), "samples": len(sm)}
 
 
-def workload(args):
+PUSHER_NAMES = {"boris": "Boris", "boris_nr": "BorisNR", "vay": "Vay", "hc": "HigueraCary"}
+
+
+def workload(args, precision=None):
+    prec = precision or ("FP32 push/track, FP64 deposit" if args.precision == "mixed" else "FP64")
     return {"workload": f"3-D two-species electrostatic PIC, {args.cells}^3 hex cells in a 0.05 m cube, "
-                        f"e- + Ar+ at {args.ppc}/cell each, B_z = 0.01 T, Boris, absorbing walls",
+                        f"e- + Ar+ at {args.ppc}/cell each, B_z = 0.01 T, {PUSHER_NAMES[args.pusher]}, "
+                        f"absorbing walls",
             "cells": args.cells ** 3, "particles": 2 * args.ppc * args.cells ** 3,
-            "precision": "FP32 push/track, FP64 deposit" if args.precision == "mixed" else "FP64",
+            "precision": prec,
             "l2": "particle store larger than L2 (no flush needed)"}
 
 
@@ -221,8 +231,9 @@ def run_reference(args, rank, ws):
     import pyoracle
     from picfoam_gb300 import abi, cases
     cores = os.cpu_count() or 1
-    ppc = max(1, min(args.ppc, 2))
-    case = cases.two_species_3d(n_cells=args.cells, per_cell=ppc, precision=abi.PREC_FP64)
+    ppc = args.ppc
+    case = cases.two_species_3d(n_cells=args.cells, per_cell=ppc, precision=abi.PREC_FP64,
+                                pusher=PUSHERS[args.pusher])
     sim = cases.build(case, backend=pyoracle.OracleBackend(cores))
     sim.initialise_fields()
     for _ in range(args.warmup):
@@ -241,15 +252,124 @@ def run_reference(args, rank, ws):
     line = {"impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": args.gpus,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * dt / args.steps,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
-            "data": "synthetic (seeded Maxwellian plasma)", "config": workload(args),
+            "data": "synthetic (seeded Maxwellian plasma)",
+            "config": workload(args, precision="FP64 (picFoam's own arithmetic; the CPU restatement has no "
+                                                "FP32 form)"),
             "cpu_baseline": {"value": value, "unit": UNIT, "cores": cores, "kind": "port",
-                             "sample": f"{args.cells}^3 cells, {ppc}/cell per species ({n} particles) per step; "
+                             "sample": f"the whole workload: {args.cells}^3 cells, {ppc}/cell per species "
+                                       f"({n} particles), {args.steps} timed steps on {cores} threads; "
                                        "CPU restatement of picFoam's move + deposit (the reference needs "
                                        "OpenFOAM-9 and cannot be built here)"},
             "e2e": {"value": tot / wall, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     sim.close()
     print(json.dumps(line), flush=True)
     return 0
+
+
+PUSHERS = {"boris": 1, "boris_nr": 2, "vay": 3, "hc": 4}
+
+
+def time_moves(sim, steps=10, warm=3):
+    """Device time of `steps` picgpu_move passes (CUDA events around each
+    move phase) after `warm` untimed ones: (particle-steps/s of the move
+    kernels, ms per kernel launch, particle-steps timed)."""
+    sim.set_profiling(True)
+    for _ in range(warm):
+        sim.move()
+    sim.phase_times(reset=True)
+    n = 0
+    for _ in range(steps):
+        n += sim.count(0) + sim.count(1)
+        sim.move()
+    ms, launches = sim.phase_times()["move"]
+    return n / (ms * 1e-3), ms / max(launches, 1), n
+
+
+def forms(args, case, peak):
+    """The BASELINE config-2 runs beside the headline: the plain FP64 path
+    (move_kernel_fp64, 104 B per particle-step) and the FP32 form with the
+    BorisNR, Vay and Higuera-Cary pushers, each on the same particles."""
+    import numpy as np
+    from picfoam_gb300 import abi, cases
+    from picfoam_gb300.simulation import Simulation
+    out = {}
+    for name, pid in (("boris_nr", abi.PUSHER_BORIS_NR), ("vay", abi.PUSHER_VAY), ("hc", abi.PUSHER_HIGUERA_CARY)):
+        cfg = abi.Config.from_buffer_copy(case.cfg)
+        cfg.pusher = pid
+        sim = Simulation(case.mesh, cfg)
+        for s, (tet, bary, U) in case.particles.items():
+            sim.set_particles(s, tet, bary, U)
+        sim.initialise_fields()
+        v, ms_launch, n = time_moves(sim)
+        sim.close()
+        out[f"fp32_{name}"] = {"particle_steps_per_s": v, "kernel_ms_per_launch": ms_launch,
+                               "hbm_frac": BYTES_FP32 * v / 1e9 / peak}
+    fcase = cases.two_species_3d(n_cells=args.cells, per_cell=args.ppc, precision=abi.PREC_FP64)
+    for name, pid in (("boris", abi.PUSHER_BORIS), ("vay", abi.PUSHER_VAY), ("hc", abi.PUSHER_HIGUERA_CARY)):
+        cfg = abi.Config.from_buffer_copy(fcase.cfg)
+        cfg.pusher = pid
+        sim = Simulation(fcase.mesh, cfg)
+        for s, (tet, bary, U) in fcase.particles.items():
+            sim.set_particles(s, tet, bary, U)
+        sim.initialise_fields()
+        v, ms_launch, n = time_moves(sim, steps=5)
+        sim.close()
+        out[f"fp64_{name}"] = {"particle_steps_per_s": v, "kernel_ms_per_launch": ms_launch,
+                               "hbm_frac": BYTES_FP64 * v / 1e9 / peak, "kernel": "move_kernel_fp64",
+                               "bytes_per_particle_step": BYTES_FP64}
+    out["note"] = ("same mesh, population and seed as the headline; FP64: the exact form (bit-exact against the "
+                   "oracle), FP32: the mixed form; particle-steps/s of the move kernels from CUDA events")
+    return out
+
+
+def collisions(args):
+    """BASELINE config 3 at size: the electron swarm (10M electrons on
+    32x32x256 cells, E = 1e4 V/m, argon-like gas at 1e21, MCC with
+    ionisation, FP32 push) and the Coulomb thermalisation (16^3 cells, 400
+    electrons per cell, NanbuYonemura + Nanbu, coulombLog 15): ms per
+    collision phase and particle-steps/s of whole steps."""
+    from picfoam_gb300 import abi, cases
+    out = {}
+    case = cases.electron_swarm()
+    sim = cases.build(case)
+    sim.set_profiling(True)
+    for _ in range(3):
+        sim.step(1)
+    sim.phase_times(reset=True)
+    n0 = sim.count(0)
+    steps = 10
+    sim.synchronize()
+    sim.timer_start()
+    ps = 0
+    for _ in range(steps):
+        ps += sim.count(0) + sim.count(1)
+        st = sim.step(1)
+    ms = sim.timer_stop()
+    ph = sim.phase_times()
+    out["swarm"] = {"electrons_at_start": n0, "electrons_at_end": sim.count(0), "steps": steps,
+                    "mcc_ms_per_step": ph["mcc"][0] / steps, "move_ms_per_step": ph["move"][0] / steps,
+                    "step_ms": ms / steps, "particle_steps_per_s": ps / (ms * 1e-3),
+                    "mcc_candidates_last_step": int(st.mcc_candidates),
+                    "config": "32x32x256 cells, 0.02x0.02x0.16 m, E_z = 1e4 V/m, n_gas = 1e21 m^-3, 256-point "
+                              "elastic/excitation/ionisation tables, NanbuElectronNeutral, FP32 push"}
+    sim.close()
+    case = cases.coulomb_thermalisation(n_cells=16, per_cell=400, precision=abi.PREC_MIXED)
+    sim = cases.build(case)
+    sim.set_profiling(True)
+    sim.step(2)
+    sim.phase_times(reset=True)
+    steps = 5
+    sim.synchronize()
+    sim.timer_start()
+    sim.step(steps)
+    ms = sim.timer_stop()
+    ph = sim.phase_times()
+    out["coulomb"] = {"electrons": sim.count(0), "steps": steps, "coulomb_ms_per_step": ph["coulomb"][0] / steps,
+                      "step_ms": ms / steps, "particle_steps_per_s": sim.count(0) * steps / (ms * 1e-3),
+                      "config": "16^3 cells, 400 e-/cell, n = 1e18 m^-3, T_x = 2 eV, T_yz = 1 eV, NanbuYonemura "
+                                "pairing, Nanbu collide, coulombLog 15, FP32 push"}
+    sim.close()
+    return out
 
 
 def learned_vs_plain(args):
@@ -451,7 +571,8 @@ def run_ours(args, rank, ws):
         devs = [d for d in vis.split(",") if d] if vis else None
         os.environ["CUDA_VISIBLE_DEVICES"] = devs[local % len(devs)] if devs else str(local)
     prec = abi.PREC_MIXED if args.precision == "mixed" else abi.PREC_FP64
-    case = cases.two_species_3d(n_cells=args.cells, per_cell=args.ppc, precision=prec, seed=1234 + rank)
+    case = cases.two_species_3d(n_cells=args.cells, per_cell=args.ppc, precision=prec, seed=1234 + rank,
+                                pusher=PUSHERS[args.pusher])
     case.cfg.sort_interval = args.sort_interval
     sim = cases.build(case)
     sim.initialise_fields()
@@ -512,6 +633,32 @@ def run_ours(args, rank, ws):
                                  "pcg_iterations_per_step": float(np.mean(mit)),
                                  "note": "FP64 flexible PCG with the FP32 aggregation V-cycle, same tolerance "
                                          "and start guesses"}
+        # whole picgpu_step (push + track + deposit, charge update, Poisson,
+        # E and its interpolation, store maintenance) with either preconditioner
+        full = {}
+        for precond in ("jacobi", "multigrid"):
+            if precond == "jacobi":
+                fs = sim
+            else:
+                if args.no_multigrid:
+                    continue
+                cfg_mg = abi.Config.from_buffer_copy(case.cfg)
+                cfg_mg.pcg_precond = abi.PRECOND_MULTIGRID
+                fs = Simulation(case.mesh, cfg_mg)
+                for sp, (tet, bary, U) in case.particles.items():
+                    fs.set_particles(sp, tet, bary, U)
+                fs.initialise_fields()
+                fs.step(2)
+            nps = fs.count(0) + fs.count(1)
+            fs.synchronize()
+            fs.timer_start()
+            fs.step(args.poisson_steps)
+            fms = fs.timer_stop()
+            full[precond] = {"particle_steps_per_s": nps * args.poisson_steps / (fms * 1e-3),
+                             "ms_per_step": fms / args.poisson_steps}
+            if fs is not sim:
+                fs.close()
+        pois["full_step"] = full
     sim.close()
     # e2e through the public API with host buffers: upload the population,
     # K move passes (each returns its counters to the host), download it.
@@ -579,6 +726,16 @@ def run_ours(args, rank, ws):
             line["ensemble"] = ensemble(args)
         except Exception as ex:  # reported, not fatal
             line["ensemble"] = {"error": str(ex)}
+    if rank == 0 and ws == 1 and not args.no_forms:
+        try:
+            line["forms"] = forms(args, case, peak)
+        except Exception as ex:  # reported, not fatal
+            line["forms"] = {"error": str(ex)}
+    if rank == 0 and ws == 1 and not args.no_collisions:
+        try:
+            line["collisions"] = collisions(args)
+        except Exception as ex:  # reported, not fatal
+            line["collisions"] = {"error": str(ex)}
     if rank == 0 and ws == 1 and not args.no_cpu_baseline:
         try:
             line["cpu_baseline"] = cpu_baseline(args)

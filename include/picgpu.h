@@ -409,7 +409,17 @@ enum {
     PICGPU_FIELD_E_CELL = 1,     /* n_cells x 3      */
     PICGPU_FIELD_RHO = 2,        /* n_cells          */
     PICGPU_FIELD_E_POINT = 3,    /* n_points x 3 (cyclic-merged point numbering) */
-    PICGPU_FIELD_SIGMA_V_MAX = 4 /* n_cells          */
+    PICGPU_FIELD_SIGMA_V_MAX = 4, /* n_cells          */
+    /* n_cells x 3: magnetic field per cell, the B[celli] every picFoam
+     * pusher reads (BorisPusher.C:100, VayPusher.C:78, HigueraCary.C:99,
+     * BorisNRPusher.C:92).  Setting it replaces the uniform picgpu_config.B
+     * for the rest of the run; until then get_field returns the uniform B. */
+    PICGPU_FIELD_B_CELL = 5,
+    /* 6 + n_boxes (one per patch): surface charge density of the floating
+     * patches (FloatingPotential's sigma, FloatingPotential.C:89-100); other
+     * patches read 0 and ignore what is set.  Setting it (a restart) also
+     * sets the patches' circuitBoundary gradient sigma / eps0. */
+    PICGPU_FIELD_PATCH_SIGMA = 6
 };
 
 /* Size queries. */
@@ -562,6 +572,13 @@ picgpu_status picgpu_step(picgpu_ctx* ctx, int nsteps, picgpu_step_stats* stats)
 /* One pass of push + track + deposit over all particles (no collisions, no
  * field solve): the particle hot path alone. */
 picgpu_status picgpu_move(picgpu_ctx* ctx, picgpu_step_stats* stats);
+
+/* Restart: the number of time steps already done, i.e. the time index the
+ * picFoam run continues from (startFrom latestTime reads it from the time
+ * directory, Time::setTime).  The random streams of the collision and
+ * injection models, the cell re-sort schedule and the circuit sources are
+ * keyed by it. */
+picgpu_status picgpu_set_step_index(picgpu_ctx* ctx, int64_t steps_done);
 
 /* ElectroStatic solve on a caller charge density (n_cells); writes the
  * potential (n_cells) and updates E. phi_inout is the initial guess. */

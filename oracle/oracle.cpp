@@ -153,6 +153,7 @@ struct Oracle {
     std::vector<int> cathodeFaces;
     ob::CircuitState circuit{};
     bool rotation = false;
+    std::vector<double> Bcell;   // per-cell magnetic field (3 per cell); empty: the uniform cfg.B
     double move_seconds = 0;
     long long step_index = 0;
     // collision state
@@ -209,10 +210,17 @@ V3 field_at(const Oracle& o, const Parcel& p) {
     return v3(r[0], r[1], r[2]);
 }
 
+// The magnetic field of a parcel's cell: the per-cell field when one was
+// set, else the uniform one.
+V3 cell_B(const Oracle& o, int cell) {
+    if (o.Bcell.empty()) return v3(o.cfg.B[0], o.cfg.B[1], o.cfg.B[2]);
+    return v3(o.Bcell[3 * size_t(cell)], o.Bcell[3 * size_t(cell) + 1], o.Bcell[3 * size_t(cell) + 2]);
+}
+
 // BorisPusher::updateVelocity (SM/ParticlePusher/BorisPusher/BorisPusher.C:69-112)
 void push_boris(const Oracle& o, Parcel& p, double q, double mass, double trackTime) {
     const V3 E = field_at(o, p);
-    const V3 B = v3(o.cfg.B[0], o.cfg.B[1], o.cfg.B[2]);  // B[celli], uniform
+    const V3 B = cell_B(o, p.cell);  // B[celli] (BorisPusher.C:100)
     const double dt2 = 0.5 * trackTime;
     const double mU = magv(p.U) / kC;
     V3 rU = sdiv(p.U, std::sqrt(1.0 - mU * mU));
@@ -237,7 +245,7 @@ void push_boris(const Oracle& o, Parcel& p, double q, double mass, double trackT
 // BorisNRPusher::updateVelocity (SM/ParticlePusher/BorisNRPusher/BorisNRPusher.C:69-99)
 void push_boris_nr(const Oracle& o, Parcel& p, double q, double mass, double trackTime) {
     const V3 E = field_at(o, p);
-    const V3 B = v3(o.cfg.B[0], o.cfg.B[1], o.cfg.B[2]);
+    const V3 B = cell_B(o, p.cell);
     const double dt2 = 0.5 * trackTime;
     const double alpha = q * dt2 / mass;
     V3 U = add(p.U, smul(alpha, E));
@@ -254,7 +262,7 @@ void push_boris_nr(const Oracle& o, Parcel& p, double q, double mass, double tra
 // the rotation term uses the velocity v, not u (VayPusher.C:81).
 void push_vay(const Oracle& o, Parcel& p, double q, double mass, double trackTime) {
     const V3 E = field_at(o, p);
-    const V3 B = v3(o.cfg.B[0], o.cfg.B[1], o.cfg.B[2]);
+    const V3 B = cell_B(o, p.cell);
     const double dt2 = 0.5 * trackTime;
     const double mU = magv(p.U) / kC;
     const double lF = 1.0 / std::sqrt(1.0 - mU * mU);
@@ -280,7 +288,7 @@ void push_vay(const Oracle& o, Parcel& p, double q, double mass, double trackTim
 // HigueraCaryPusher::updateVelocity (SM/ParticlePusher/HigueraCary/HigueraCary.C:69-115)
 void push_hc(const Oracle& o, Parcel& p, double q, double mass, double trackTime) {
     const V3 E = field_at(o, p);
-    const V3 B = v3(o.cfg.B[0], o.cfg.B[1], o.cfg.B[2]);
+    const V3 B = cell_B(o, p.cell);
     const double dt2 = 0.5 * trackTime;
     const double mU = magv(p.U) / kC;
     V3 rU = sdiv(p.U, std::sqrt(1.0 - mU * mU));
@@ -3004,6 +3012,12 @@ int oracle_solve_poisson(oracle_ctx* ctx, const double* rho, double* phi_inout,
     return s;
 }
 
+int oracle_set_step_index(oracle_ctx* ctx, int64_t steps_done) {
+    if (!ctx || steps_done < 0) return PICGPU_INVALID_ARG;
+    ctx->o.step_index = steps_done;
+    return 0;
+}
+
 int oracle_get_field(oracle_ctx* ctx, int which, double* out, size_t n) {
     Oracle& o = ctx->o;
     const std::vector<double>* v = nullptr;
@@ -3013,6 +3027,19 @@ int oracle_get_field(oracle_ctx* ctx, int which, double* out, size_t n) {
         case PICGPU_FIELD_RHO: v = &o.rho; break;
         case PICGPU_FIELD_E_POINT: v = &o.Ept; break;
         case PICGPU_FIELD_SIGMA_V_MAX: v = &o.svmax; break;
+        case PICGPU_FIELD_PATCH_SIGMA:
+            if (n < o.m.patches.size()) return PICGPU_INVALID_ARG;
+            for (size_t p = 0; p < o.m.patches.size(); ++p)
+                out[p] = o.m.patches[p].p.kind == PICGPU_PATCH_FLOATING ? o.sigma[p] : 0.0;
+            return 0;
+        case PICGPU_FIELD_B_CELL:
+            if (o.Bcell.empty()) {
+                if (n < 3 * size_t(o.m.n_cells)) return PICGPU_INVALID_ARG;
+                for (size_t k = 0; k < 3 * size_t(o.m.n_cells); ++k) out[k] = o.cfg.B[k % 3];
+                return 0;
+            }
+            v = &o.Bcell;
+            break;
         default: return PICGPU_INVALID_ARG;
     }
     if (n < v->size()) return PICGPU_INVALID_ARG;
@@ -3028,6 +3055,22 @@ int oracle_set_field(oracle_ctx* ctx, int which, const double* in, size_t n) {
         case PICGPU_FIELD_E_CELL: v = &o.E; break;
         case PICGPU_FIELD_RHO: v = &o.rho; break;
         case PICGPU_FIELD_E_POINT: v = &o.Ept; break;
+        case PICGPU_FIELD_PATCH_SIGMA:
+            if (n < o.m.patches.size()) return PICGPU_INVALID_ARG;
+            for (size_t p = 0; p < o.m.patches.size(); ++p) {
+                if (o.m.patches[p].p.kind != PICGPU_PATCH_FLOATING) continue;
+                o.sigma[p] = in[p];
+                o.Qconv[p] = 0.0;
+            }
+            floating_pre_update(o);
+            return 0;
+        case PICGPU_FIELD_B_CELL: {
+            if (n < 3 * size_t(o.m.n_cells)) return PICGPU_INVALID_ARG;
+            o.Bcell.assign(in, in + 3 * size_t(o.m.n_cells));
+            o.rotation = false;
+            for (double b : o.Bcell) o.rotation = o.rotation || b != 0.0;
+            return 0;
+        }
         default: return PICGPU_INVALID_ARG;
     }
     if (n < v->size()) return PICGPU_INVALID_ARG;

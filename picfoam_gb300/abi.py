@@ -33,7 +33,7 @@ PATCH_CYCLIC, PATCH_EMPTY, PATCH_ABSORB, PATCH_WALL, PATCH_FLOATING, PATCH_CIRCU
 PHI_FIXED_VALUE, PHI_ZERO_GRADIENT, PHI_RLC, PHI_CIRCUIT_GRADIENT = range(4)
 CIRCUIT_NONE, CIRCUIT_RLC, CIRCUIT_IDEAL_VOLTAGE, CIRCUIT_IDEAL_CURRENT = range(4)
 PRECOND_JACOBI, PRECOND_MULTIGRID = range(2)
-FIELD_PHI, FIELD_E_CELL, FIELD_RHO, FIELD_E_POINT, FIELD_SIGMA_V_MAX = range(5)
+FIELD_PHI, FIELD_E_CELL, FIELD_RHO, FIELD_E_POINT, FIELD_SIGMA_V_MAX, FIELD_B_CELL, FIELD_PATCH_SIGMA = range(7)
 (PHASE_MOVE, PHASE_CHARGE, PHASE_POISSON, PHASE_EFIELD, PHASE_SORT, PHASE_MCC,
  PHASE_COULOMB, PHASE_COUNT) = range(8)
 PHASE_NAMES = ["move", "charge", "poisson", "efield", "sort", "mcc", "coulomb"]

@@ -144,6 +144,8 @@ struct MoveParams {
     float dt_f;
     float B_f[3];
     float centre_f[3];
+    const double* Bc;             // per-cell magnetic field (3 n_cells), or null: the uniform B
+    const float4* Bc4;            // FP32 form: the same per cell (xyz), or null
     const Tables32* t32;          // FP32 form: tables of this context's mesh (device memory)
     // FP32 in-cell mover (uniform block meshes): dt / cell size per axis and
     // 1 on solved axes, 0 on empty ones (tracking returns to the centre plane)

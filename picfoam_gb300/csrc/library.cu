@@ -265,6 +265,8 @@ struct picgpu_ctx {
     unsigned long long* acc9 = nullptr;   // FP32 form: per-species fixed-point deposit, 9 slots per cell
     float4* Ec4 = nullptr;                // FP32 form: E per cell, centre + 8 corners
     pgd::Tables32* t32 = nullptr;         // FP32 form: this mesh's move tables (device)
+    double* Bc = nullptr;                 // per-cell magnetic field (3 n_cells), null: uniform cfg.B
+    float4* Bc4 = nullptr;                // its FP32 copy
     float cell_dth[3] = {0, 0, 0};        // FP32 in-cell mover: dt / cell size per axis (0: empty axis)
     float cell_keep[3] = {1, 1, 1};       // 0 on empty axes
     int* xq_count = nullptr;              // FP32 form: crossing-queue counts and starts per mover block
@@ -560,6 +562,8 @@ pgd::MoveParams move_params(picgpu_ctx* c, int s, bool deposit_only) {
     P.acc9 = c->acc9 ? c->acc9 + size_t(s) * 9 * c->m.n_cells : nullptr;
     P.Ec4 = c->Ec4;
     P.t32 = c->t32;
+    P.Bc = c->Bc;
+    P.Bc4 = c->Bc4;
     for (const auto& pt : c->m.patches)
         if (pt.p.kind == PICGPU_PATCH_WALL || (pt.p.kind == PICGPU_PATCH_CIRCUIT && S.charge == 0.0))
             P.reflecting = 1;
@@ -1903,6 +1907,12 @@ picgpu_status picgpu_get_particles(picgpu_ctx* c, int species, size_t cap, int32
     return PICGPU_OK;
 }
 
+picgpu_status picgpu_set_step_index(picgpu_ctx* c, int64_t steps_done) {
+    if (!c || steps_done < 0) return PICGPU_INVALID_ARG;
+    c->step_index = steps_done;
+    return PICGPU_OK;
+}
+
 picgpu_status picgpu_initialise_fields(picgpu_ctx* c) {
     if (!c) return PICGPU_INVALID_ARG;
     picgpu_status s;
@@ -2504,6 +2514,24 @@ picgpu_status picgpu_get_field(picgpu_ctx* c, int which, double* out, size_t n) 
             cnt = c->m.n_cells;
             if (!src) return bad(c, PICGPU_INVALID_ARG, "no MCC state");
             break;
+        case PICGPU_FIELD_PATCH_SIGMA: {
+            const size_t np = c->m.patches.size();
+            if (n < np) return bad(c, PICGPU_INVALID_ARG, "output buffer too small");
+            std::vector<double> sg(np);
+            CK(cudaStreamSynchronize(c->stream));
+            CK(cudaMemcpy(sg.data(), c->sigma, np * sizeof(double), cudaMemcpyDeviceToHost));
+            for (size_t p = 0; p < np; ++p) out[p] = c->m.patches[p].p.kind == PICGPU_PATCH_FLOATING ? sg[p] : 0.0;
+            return PICGPU_OK;
+        }
+        case PICGPU_FIELD_B_CELL:
+            src = c->Bc;
+            cnt = 3 * size_t(c->m.n_cells);
+            if (!src) {
+                if (n < cnt) return bad(c, PICGPU_INVALID_ARG, "output buffer too small");
+                for (size_t k = 0; k < cnt; ++k) out[k] = c->cfg.B[k % 3];
+                return PICGPU_OK;
+            }
+            break;
         default: return PICGPU_INVALID_ARG;
     }
     if (n < cnt) return bad(c, PICGPU_INVALID_ARG, "output buffer too small");
@@ -2514,6 +2542,41 @@ picgpu_status picgpu_get_field(picgpu_ctx* c, int which, double* out, size_t n) 
 
 picgpu_status picgpu_set_field(picgpu_ctx* c, int which, const double* in, size_t n) {
     if (!c || !in) return PICGPU_INVALID_ARG;
+    if (which == PICGPU_FIELD_PATCH_SIGMA) {
+        const size_t np = c->m.patches.size();
+        if (n < np) return bad(c, PICGPU_INVALID_ARG, "input buffer too small");
+        std::vector<double> sg(np);
+        CK(cudaStreamSynchronize(c->stream));
+        CK(cudaMemcpy(sg.data(), c->sigma, np * sizeof(double), cudaMemcpyDeviceToHost));
+        for (size_t p = 0; p < np; ++p)
+            if (c->m.patches[p].p.kind == PICGPU_PATCH_FLOATING) sg[p] = in[p];
+        CK(cudaMemcpy(c->sigma, sg.data(), np * sizeof(double), cudaMemcpyHostToDevice));
+        // the floating update with an empty accumulator: gradient sigma / eps0
+        pgd::launch_floating_update(c->qconv, c->sigma, c->grad_bc, c->stream);
+        c->launches++;
+        CK(cudaStreamSynchronize(c->stream));
+        return PICGPU_OK;
+    }
+    if (which == PICGPU_FIELD_B_CELL) {
+        const size_t nb = 3 * size_t(c->m.n_cells);
+        if (n < nb) return bad(c, PICGPU_INVALID_ARG, "input buffer too small");
+        if (c->n_cases > 1 || !c->graphs.empty())
+            return bad(c, PICGPU_NOT_SUPPORTED, "a per-cell magnetic field is not supported with ensembles or graph steps");
+        picgpu_status st;
+        if (!c->Bc && ((st = dalloc(c, &c->Bc, nb)) || (st = dalloc(c, &c->Bc4, size_t(c->m.n_cells))))) return st;
+        std::vector<float4> b4(c->m.n_cells);
+        bool any = false;
+        for (size_t k = 0; k < size_t(c->m.n_cells); ++k) {
+            b4[k] = make_float4(float(in[3 * k]), float(in[3 * k + 1]), float(in[3 * k + 2]), 0.f);
+            any = any || in[3 * k] != 0.0 || in[3 * k + 1] != 0.0 || in[3 * k + 2] != 0.0;
+        }
+        CK(cudaStreamSynchronize(c->stream));
+        CK(cudaMemcpy(c->Bc, in, nb * sizeof(double), cudaMemcpyHostToDevice));
+        CK(cudaMemcpy(c->Bc4, b4.data(), b4.size() * sizeof(float4), cudaMemcpyHostToDevice));
+        // the pushers skip the rotation only when B vanishes everywhere (BorisPusher.C:43-55)
+        c->rotation = any;
+        return PICGPU_OK;
+    }
     double* dst = nullptr;
     size_t cnt = 0;
     switch (which) {

@@ -61,20 +61,37 @@ __device__ __forceinline__ void field32(const MoveParams& P, const unsigned* tri
     E[2] = a.z * s.y[0] + b.z * s.y[1] + c.z * s.y[2] + d.z * s.y[3];
 }
 
+// Lorentz factors in FP32 through their distance from 1.  At plasma
+// energies gamma = 1 + 5e-6 rounds to 1 + k 2^-23 in FP32, and the rounding
+// of gamma on the way in (u = gamma v) and on the way out (v = u / gamma)
+// does not cancel: the kinetic energy then drifts by ~1e-7 per push (3e-4
+// over the 2000 steps of the plasma oscillation).  With a = v^2/c^2,
+// b = u^2/c^2 the pushers use
+//   gamma - 1     = a / (s (1 + s)),  s = sqrt(1 - a)   (v -> u: u = v + v (gamma - 1))
+//   1 - 1 / gamma = b / (q (1 + q)),  q = sqrt(1 + b)   (u -> v: v = u - u (1 - 1/gamma))
+// whose rounding scales with gamma - 1, not with gamma.
+__device__ __forceinline__ float gamma_less_one(float a) {
+    const float s = sqrtf(1.f - a);
+    return __fdividef(a, s * (1.f + s));
+}
+__device__ __forceinline__ float one_less_inv_gamma(float b) {
+    const float q = sqrtf(1.f + b);
+    return __fdividef(b, q * (1.f + q));
+}
+
 // Relativistic Boris (BorisPusher.C:69-112) in FP32: the Lorentz factor of
 // the incoming velocity is reused for the averaged factor of the rotation.
-__device__ __forceinline__ void boris32(const MoveParams& P, const float* E, float* U, float tt) {
+__device__ __forceinline__ void boris32(const MoveParams& P, const float* E, const float* Bv, float* U, float tt) {
     constexpr float ic2 = float(1.0 / (kC * kC));
-    const float u2 = U[0] * U[0] + U[1] * U[1] + U[2] * U[2];
-    const float g_in = rsqrtf(1.f - u2 * ic2);  // gamma of the incoming velocity
-    float r0 = U[0] * g_in, r1 = U[1] * g_in, r2 = U[2] * g_in;
+    const float dg_in = gamma_less_one((U[0] * U[0] + U[1] * U[1] + U[2] * U[2]) * ic2);
+    float r0 = U[0] + U[0] * dg_in, r1 = U[1] + U[1] * dg_in, r2 = U[2] + U[2] * dg_in;
     const float qdm = P.qm_f * (0.5f * tt);
     const float e0 = qdm * E[0], e1 = qdm * E[1], e2 = qdm * E[2];
     r0 += e0; r1 += e1; r2 += e2;
     if (P.rotation) {
         const float g_mid = sqrtf(1.f + (r0 * r0 + r1 * r1 + r2 * r2) * ic2);
-        const float k = qdm * __fdividef(2.f, g_in + g_mid);
-        const float t0 = k * P.B_f[0], t1 = k * P.B_f[1], t2 = k * P.B_f[2];
+        const float k = qdm * __fdividef(2.f, 1.f + dg_in + g_mid);
+        const float t0 = k * Bv[0], t1 = k * Bv[1], t2 = k * Bv[2];
         const float d0 = r0 + (r1 * t2 - r2 * t1);
         const float d1 = r1 + (r2 * t0 - r0 * t2);
         const float d2 = r2 + (r0 * t1 - r1 * t0);
@@ -85,18 +102,87 @@ __device__ __forceinline__ void boris32(const MoveParams& P, const float* E, flo
         r2 += d0 * s1 - d1 * s0;
     }
     r0 += e0; r1 += e1; r2 += e2;
-    const float g_out = rsqrtf(1.f + (r0 * r0 + r1 * r1 + r2 * r2) * ic2);
-    U[0] = r0 * g_out; U[1] = r1 * g_out; U[2] = r2 * g_out;
+    const float dg_out = one_less_inv_gamma((r0 * r0 + r1 * r1 + r2 * r2) * ic2);
+    U[0] = r0 - r0 * dg_out; U[1] = r1 - r1 * dg_out; U[2] = r2 - r2 * dg_out;
+}
+
+// VayPusher::updateVelocity (VayPusher.C:54-100) in FP32, U x T with v
+// (VayPusher.C:81), the Lorentz factors of the conversions as above.
+__device__ __forceinline__ void vay32(const MoveParams& P, const float* E, const float* Bv, float* U, float tt) {
+    constexpr float ic = float(1.0 / kC), ic2 = float(1.0 / (kC * kC));
+    const float dg = gamma_less_one((U[0] * U[0] + U[1] * U[1] + U[2] * U[2]) * ic2);
+    const float qe = P.qm_f * tt, qb = P.qm_f * (0.5f * tt);
+    float u0 = U[0] + U[0] * dg + qe * E[0], u1 = U[1] + U[1] * dg + qe * E[1], u2 = U[2] + U[2] * dg + qe * E[2];
+    float T0 = qb * Bv[0], T1 = qb * Bv[1], T2 = qb * Bv[2];
+    u0 += U[1] * T2 - U[2] * T1;
+    u1 += U[2] * T0 - U[0] * T2;
+    u2 += U[0] * T1 - U[1] * T0;
+    const float alpha0 = 1.f + (u0 * u0 + u1 * u1 + u2 * u2) * ic2;
+    const float TT = T0 * T0 + T1 * T1 + T2 * T2;
+    const float sg = alpha0 - TT;
+    const float udt = (u0 * T0 + u1 * T1 + u2 * T2) * ic;
+    const float inv_g = rsqrtf(0.5f * (sg + sqrtf(sg * sg + 4.f * (TT + udt * udt))));
+    T0 *= inv_g; T1 *= inv_g; T2 *= inv_g;
+    const float sc = __fdividef(1.f, 1.f + T0 * T0 + T1 * T1 + T2 * T2);
+    const float ut = u0 * T0 + u1 * T1 + u2 * T2;
+    const float r0 = sc * ((u0 + ut * T0) + (u1 * T2 - u2 * T1));
+    const float r1 = sc * ((u1 + ut * T1) + (u2 * T0 - u0 * T2));
+    const float r2 = sc * ((u2 + ut * T2) + (u0 * T1 - u1 * T0));
+    const float dg_out = one_less_inv_gamma((r0 * r0 + r1 * r1 + r2 * r2) * ic2);
+    U[0] = r0 - r0 * dg_out; U[1] = r1 - r1 * dg_out; U[2] = r2 - r2 * dg_out;
+}
+
+// HigueraCaryPusher::updateVelocity (HigueraCary.C:69-115) in FP32, the
+// Lorentz factors of the conversions as above.
+__device__ __forceinline__ void hc32(const MoveParams& P, const float* E, const float* Bv, float* U, float tt) {
+    constexpr float ic2 = float(1.0 / (kC * kC));
+    const float dg = gamma_less_one((U[0] * U[0] + U[1] * U[1] + U[2] * U[2]) * ic2);
+    float r0 = U[0] + U[0] * dg, r1 = U[1] + U[1] * dg, r2 = U[2] + U[2] * dg;
+    const float qdm = P.qm_f * (0.5f * tt);
+    const float e0 = qdm * E[0], e1 = qdm * E[1], e2 = qdm * E[2];
+    r0 += e0; r1 += e1; r2 += e2;
+    if (P.rotation) {
+        const float gfm2 = 1.f + (r0 * r0 + r1 * r1 + r2 * r2) * ic2;
+        float t0 = qdm * Bv[0], t1 = qdm * Bv[1], t2 = qdm * Bv[2];
+        const float beta2 = t0 * t0 + t1 * t1 + t2 * t2;
+        const float gb = gfm2 - beta2;
+        const float tr = t0 * r0 + t1 * r1 + t2 * r2;
+        // (t . u)^2 without the 1/c^2 of the textbook form, as HigueraCary.C:103 has it
+        const float iG = rsqrtf(0.5f * (gb + sqrtf(gb * gb + 4.f * (beta2 + tr * tr))));
+        t0 *= iG; t1 *= iG; t2 *= iG;
+        const float d0 = r0 + (r1 * t2 - r2 * t1);
+        const float d1 = r1 + (r2 * t0 - r0 * t2);
+        const float d2 = r2 + (r0 * t1 - r1 * t0);
+        const float h = __fdividef(2.f, 1.f + t0 * t0 + t1 * t1 + t2 * t2);
+        const float s0 = h * t0, s1 = h * t1, s2 = h * t2;
+        r0 += d1 * s2 - d2 * s1;
+        r1 += d2 * s0 - d0 * s2;
+        r2 += d0 * s1 - d1 * s0;
+    }
+    r0 += e0; r1 += e1; r2 += e2;
+    const float dg_out = one_less_inv_gamma((r0 * r0 + r1 * r1 + r2 * r2) * ic2);
+    U[0] = r0 - r0 * dg_out; U[1] = r1 - r1 * dg_out; U[2] = r2 - r2 * dg_out;
 }
 
 template <int PUSHER>
 __device__ __forceinline__ void push32(const MoveParams& P, const unsigned* tri_of, S32& s, float tt) {
-    float E[3];
+    float E[3], Bv[3];
     field32(P, tri_of, s, E);
-    if (PUSHER == PICGPU_PUSHER_BORIS) boris32(P, E, s.U, tt);
-    else if (PUSHER == PICGPU_PUSHER_BORIS_NR) push_boris_nr<float>(P, E, s.U, tt);
-    else if (PUSHER == PICGPU_PUSHER_VAY) push_vay<float>(P, E, s.U, tt);
-    else if (PUSHER == PICGPU_PUSHER_HIGUERA_CARY) push_hc<float>(P, E, s.U, tt);
+    if (P.Bc4) {
+        // per-cell magnetic field (B[celli])
+        const float4 b = __ldg(P.Bc4 + s.cell);
+        Bv[0] = b.x;
+        Bv[1] = b.y;
+        Bv[2] = b.z;
+    } else {
+        Bv[0] = P.B_f[0];
+        Bv[1] = P.B_f[1];
+        Bv[2] = P.B_f[2];
+    }
+    if (PUSHER == PICGPU_PUSHER_BORIS) boris32(P, E, Bv, s.U, tt);
+    else if (PUSHER == PICGPU_PUSHER_BORIS_NR) push_boris_nr<float>(P, E, Bv, s.U, tt);
+    else if (PUSHER == PICGPU_PUSHER_VAY) vay32(P, E, Bv, s.U, tt);
+    else if (PUSHER == PICGPU_PUSHER_HIGUERA_CARY) hc32(P, E, Bv, s.U, tt);
 }
 
 __device__ __forceinline__ void remap(unsigned code, S32& s) {
@@ -284,6 +370,40 @@ __device__ __forceinline__ void deposit32(const MoveParams& P, const unsigned* t
     atomicAdd(g + 1 + ((tri >> 8) & 15u), (unsigned long long)__float2uint_rn(s.y[3] * kScale));
 }
 
+// The in-cell mover's window: per cell kCellSub copies of the centre slot,
+// lane l adding to copy l % kCellSub (the store is cell-sorted, so most
+// lanes of a warp share a cell and would otherwise serialise on one
+// address), then the 8 corner slots; the flush adds the copies.
+constexpr int kCellSub = 4;
+constexpr int kCellSlots = kCellSub + 8;
+constexpr int kCellWindow = 768;
+
+__device__ __forceinline__ void deposit_cell32(const MoveParams& P, const unsigned* tri_of, const S32& s, int w0,
+                                               unsigned* win) {
+    if (!P.has_value) return;
+    constexpr float kScale = float(1u << kDepositBits);
+    const int rel = s.cell - w0;
+    unsigned long long* g = P.acc9 + 9 * size_t(s.cell);
+    const bool average = P.charge_distribution == PICGPU_WEIGHTING_CELL_AVERAGE;
+    const unsigned tri = tri_of[s.tet];
+    const unsigned w0v = average ? (1u << kDepositBits) : __float2uint_rn(s.y[0] * kScale);
+    if (unsigned(rel) < unsigned(kCellWindow)) {
+        unsigned* a = win + kCellSlots * rel;
+        win_add(a + (threadIdx.x & (kCellSub - 1)), g, w0v);
+        if (average) return;
+        const unsigned k1 = tri & 15u, k2 = (tri >> 4) & 15u, k3 = (tri >> 8) & 15u;
+        win_add(a + kCellSub + k1, g + 1 + k1, __float2uint_rn(s.y[1] * kScale));
+        win_add(a + kCellSub + k2, g + 1 + k2, __float2uint_rn(s.y[2] * kScale));
+        win_add(a + kCellSub + k3, g + 1 + k3, __float2uint_rn(s.y[3] * kScale));
+        return;
+    }
+    atomicAdd(g, (unsigned long long)w0v);
+    if (average) return;
+    atomicAdd(g + 1 + (tri & 15u), (unsigned long long)__float2uint_rn(s.y[1] * kScale));
+    atomicAdd(g + 1 + ((tri >> 4) & 15u), (unsigned long long)__float2uint_rn(s.y[2] * kScale));
+    atomicAdd(g + 1 + ((tri >> 8) & 15u), (unsigned long long)__float2uint_rn(s.y[3] * kScale));
+}
+
 struct Rec {
     int tet;
     float y1, y2, y3, u0, u1, u2;
@@ -442,7 +562,9 @@ __device__ __forceinline__ void cell_to_bary(float x0, float x1, float x2, S32& 
     s.y[1] = h - (k1 ? xv : xu);
     s.y[2] = k1 ? h + xu : xu - xv;
     s.y[3] = k1 ? xv - xu : h + xv;
-    s.y[0] = 1.f - 2.f * h;
+    // the centre coordinate as every later reader forms it from the stored
+    // three (so a deposit-only pass over the store deposits the same weights)
+    s.y[0] = 1.f - s.y[1] - s.y[2] - s.y[3];
 }
 
 __device__ __forceinline__ void store_rec(const DSpecies& p, int i, const S32& s, int cell_tet) {
@@ -473,7 +595,7 @@ __global__ void __launch_bounds__(256, 5) move_cell_kernel_fp32(MoveParams P, in
     __shared__ unsigned tri_s[12];
     __shared__ int kind_s[kMaxPatches];
     __shared__ int w0s, qn;
-    extern __shared__ unsigned win[];  // kWindow * 9 slots (32-bit, carry to global)
+    extern __shared__ unsigned win[];  // kCellWindow * kCellSlots slots (32-bit, carry to global)
     int n_end = P.n, first = P.first, ch = chunk;
     if (P.n_dev) {
         n_end = *P.n_dev;
@@ -495,7 +617,7 @@ __global__ void __launch_bounds__(256, 5) move_cell_kernel_fp32(MoveParams P, in
     {
         if (threadIdx.x < 12) tri_s[threadIdx.x] = P.t32->tri[threadIdx.x];
         if (threadIdx.x < kMaxPatches) kind_s[threadIdx.x] = P.t32->kind[threadIdx.x];
-        for (int k = threadIdx.x; k < kWindow * 9; k += blockDim.x) win[k] = 0u;
+        for (int k = threadIdx.x; k < kCellWindow * kCellSlots; k += blockDim.x) win[k] = 0u;
     }
     if (threadIdx.x == 0) {
         int c0 = 0;
@@ -503,7 +625,7 @@ __global__ void __launch_bounds__(256, 5) move_cell_kernel_fp32(MoveParams P, in
             const int t = P.p.tet[k];
             if (t >= 0) { c0 = t / 12; break; }
         }
-        w0s = max(0, c0 - kWindow / 16);
+        w0s = max(0, c0 - kCellWindow / 16);
         qn = 0;
     }
     __syncthreads();
@@ -539,76 +661,35 @@ __global__ void __launch_bounds__(256, 5) move_cell_kernel_fp32(MoveParams P, in
                 atomicMax(&P.counters->error, int(PICGPU_SPEED_OF_LIGHT));
                 fate = 1;
             }
-            // the start point in normalised cell coordinates (empty axes: the
-            // centre plane) and the displacement U dt
-            float x0, x1, x2;
-            bary_to_cell(s.tet, s.y, x0, x1, x2);
-            x0 *= P.keep[0];
-            x1 *= P.keep[1];
-            x2 *= P.keep[2];
+            // the displacement U dt in normalised cell units, followed in
+            // the cell frame (empty axes: the centre plane)
             float d0 = s.U[0] * P.dth[0], d1 = s.U[1] * P.dth[1], d2 = s.U[2] * P.dth[2];
-            float e0 = x0 + d0, e1 = x1 + d1, e2 = x2 + d2;
-            const bool out0 = fabsf(e0) > 0.5f, out1 = fabsf(e1) > 0.5f, out2 = fabsf(e2) > 0.5f;
-            if (fate != 0) {
-                // removed before moving
-            } else if (int(out0) + int(out1) + int(out2) == 1) {
-                // through one face: into the neighbour, whose frame is this
-                // one shifted by a cell along the axis; a patch decides
-                // without the crossing time
-                const int ax = out0 ? 0 : out1 ? 1 : 2;
-                const float ea = out0 ? e0 : out1 ? e1 : e2;
-                const int nb = __ldg(P.m.nbr + 6 * s.cell + 2 * ax + (ea > 0.f ? 1 : 0));
-                faces = 1;
-                if (nb >= 0) {
-                    s.cell = nb;
-                    const float shift = ea > 0.f ? 1.f : -1.f;
-                    e0 = out0 ? e0 - shift : e0;
-                    e1 = out1 ? e1 - shift : e1;
-                    e2 = out2 ? e2 - shift : e2;
-                } else {
-                    const int patch = -nb - 1;
-                    const int kind = kind_s[patch];
-                    fate = 1;
-                    if (kind == PICGPU_PATCH_FLOATING || (kind == PICGPU_PATCH_CIRCUIT && P.q != 0.0))
-                        atomicAdd(P.qconv + patch, P.weight * P.q);
-                    else if (kind != PICGPU_PATCH_ABSORB)
-                        fate = 2;
-                }
-            } else if (out0 || out1 || out2) {
-                // through cell faces: the first face on the way per axis
-                // (|x_a| <= 1/2 after the clamp, so d_a != 0 where |e_a| > 1/2)
-                x0 = fminf(fmaxf(x0, -0.5f), 0.5f);
-                x1 = fminf(fmaxf(x1, -0.5f), 0.5f);
-                x2 = fminf(fmaxf(x2, -0.5f), 0.5f);
+            float e0 = 0.f, e1 = 0.f, e2 = 0.f;
+            if (fate == 0) {
+                float x0, x1, x2;
+                bary_to_cell(s.tet, s.y, x0, x1, x2);
+                x0 *= P.keep[0];
+                x1 *= P.keep[1];
+                x2 *= P.keep[2];
                 e0 = x0 + d0;
                 e1 = x1 + d1;
                 e2 = x2 + d2;
-                int budget = P.max_steps;
-                while (true) {
-                    float t = 2.f;
-                    int ax = 0;
-                    if (fabsf(e0) > 0.5f) t = __fdividef(copysignf(0.5f, e0) - x0, d0);
-                    if (fabsf(e1) > 0.5f) {
-                        const float ta = __fdividef(copysignf(0.5f, e1) - x1, d1);
-                        if (ta < t) { t = ta; ax = 1; }
-                    }
-                    if (fabsf(e2) > 0.5f) {
-                        const float ta = __fdividef(copysignf(0.5f, e2) - x2, d2);
-                        if (ta < t) { t = ta; ax = 2; }
-                    }
-                    t = fminf(fmaxf(t, 0.f), 1.f);
-                    const float ea = ax == 0 ? e0 : ax == 1 ? e1 : e2;
-                    const float face = ea > 0.f ? 0.5f : -0.5f;
-                    x0 = ax == 0 ? face : fminf(fmaxf(x0 + t * d0, -0.5f), 0.5f);
-                    x1 = ax == 1 ? face : fminf(fmaxf(x1 + t * d1, -0.5f), 0.5f);
-                    x2 = ax == 2 ? face : fminf(fmaxf(x2 + t * d2, -0.5f), 0.5f);
-                    const float rest = 1.f - t;
-                    d0 *= rest;
-                    d1 *= rest;
-                    d2 *= rest;
-                    ++faces;
+                const bool out0 = fabsf(e0) > 0.5f, out1 = fabsf(e1) > 0.5f, out2 = fabsf(e2) > 0.5f;
+                if (int(out0) + int(out1) + int(out2) == 1) {
+                    // through one face: into the neighbour, whose frame is this
+                    // one shifted by a cell along the axis; a patch decides
+                    // without the crossing time
+                    const int ax = out0 ? 0 : out1 ? 1 : 2;
+                    const float ea = out0 ? e0 : out1 ? e1 : e2;
                     const int nb = __ldg(P.m.nbr + 6 * s.cell + 2 * ax + (ea > 0.f ? 1 : 0));
-                    if (nb < 0) {
+                    faces = 1;
+                    if (nb >= 0) {
+                        s.cell = nb;
+                        const float shift = ea > 0.f ? 1.f : -1.f;
+                        e0 = out0 ? e0 - shift : e0;
+                        e1 = out1 ? e1 - shift : e1;
+                        e2 = out2 ? e2 - shift : e2;
+                    } else {
                         const int patch = -nb - 1;
                         const int kind = kind_s[patch];
                         fate = 1;
@@ -616,21 +697,65 @@ __global__ void __launch_bounds__(256, 5) move_cell_kernel_fp32(MoveParams P, in
                             atomicAdd(P.qconv + patch, P.weight * P.q);
                         else if (kind != PICGPU_PATCH_ABSORB)
                             fate = 2;
-                        break;
                     }
-                    // the neighbour: the point sits on its opposite face
-                    s.cell = nb;
-                    x0 = ax == 0 ? -face : x0;
-                    x1 = ax == 1 ? -face : x1;
-                    x2 = ax == 2 ? -face : x2;
+                } else if (out0 || out1 || out2) {
+                    // through cell faces: the first face on the way per axis
+                    // (|x_a| <= 1/2 after the clamp, so d_a != 0 where |e_a| > 1/2)
+                    x0 = fminf(fmaxf(x0, -0.5f), 0.5f);
+                    x1 = fminf(fmaxf(x1, -0.5f), 0.5f);
+                    x2 = fminf(fmaxf(x2, -0.5f), 0.5f);
                     e0 = x0 + d0;
                     e1 = x1 + d1;
                     e2 = x2 + d2;
-                    if (fmaxf(fabsf(e0), fmaxf(fabsf(e1), fabsf(e2))) <= 0.5f) break;
-                    if (--budget <= 0) {
-                        atomicMax(&P.counters->error, int(PICGPU_TRACK_LOOP_CAP));
-                        fate = 1;
-                        break;
+                    int budget = P.max_steps;
+                    while (true) {
+                        float t = 2.f;
+                        int ax = 0;
+                        if (fabsf(e0) > 0.5f) t = __fdividef(copysignf(0.5f, e0) - x0, d0);
+                        if (fabsf(e1) > 0.5f) {
+                            const float ta = __fdividef(copysignf(0.5f, e1) - x1, d1);
+                            if (ta < t) { t = ta; ax = 1; }
+                        }
+                        if (fabsf(e2) > 0.5f) {
+                            const float ta = __fdividef(copysignf(0.5f, e2) - x2, d2);
+                            if (ta < t) { t = ta; ax = 2; }
+                        }
+                        t = fminf(fmaxf(t, 0.f), 1.f);
+                        const float ea = ax == 0 ? e0 : ax == 1 ? e1 : e2;
+                        const float face = ea > 0.f ? 0.5f : -0.5f;
+                        x0 = ax == 0 ? face : fminf(fmaxf(x0 + t * d0, -0.5f), 0.5f);
+                        x1 = ax == 1 ? face : fminf(fmaxf(x1 + t * d1, -0.5f), 0.5f);
+                        x2 = ax == 2 ? face : fminf(fmaxf(x2 + t * d2, -0.5f), 0.5f);
+                        const float rest = 1.f - t;
+                        d0 *= rest;
+                        d1 *= rest;
+                        d2 *= rest;
+                        ++faces;
+                        const int nb = __ldg(P.m.nbr + 6 * s.cell + 2 * ax + (ea > 0.f ? 1 : 0));
+                        if (nb < 0) {
+                            const int patch = -nb - 1;
+                            const int kind = kind_s[patch];
+                            fate = 1;
+                            if (kind == PICGPU_PATCH_FLOATING || (kind == PICGPU_PATCH_CIRCUIT && P.q != 0.0))
+                                atomicAdd(P.qconv + patch, P.weight * P.q);
+                            else if (kind != PICGPU_PATCH_ABSORB)
+                                fate = 2;
+                            break;
+                        }
+                        // the neighbour: the point sits on its opposite face
+                        s.cell = nb;
+                        x0 = ax == 0 ? -face : x0;
+                        x1 = ax == 1 ? -face : x1;
+                        x2 = ax == 2 ? -face : x2;
+                        e0 = x0 + d0;
+                        e1 = x1 + d1;
+                        e2 = x2 + d2;
+                        if (fmaxf(fabsf(e0), fmaxf(fabsf(e1), fabsf(e2))) <= 0.5f) break;
+                        if (--budget <= 0) {
+                            atomicMax(&P.counters->error, int(PICGPU_TRACK_LOOP_CAP));
+                            fate = 1;
+                            break;
+                        }
                     }
                 }
             }
@@ -651,15 +776,23 @@ __global__ void __launch_bounds__(256, 5) move_cell_kernel_fp32(MoveParams P, in
             }
             fc += faces;
         }
-        if (fate == 0) deposit32(P, tri_s, s, w0, win);
+        if (fate == 0) deposit_cell32(P, tri_s, s, w0, win);
     }
     __syncthreads();
     if (P.has_value) {
-        const int nslot = min(kWindow, P.m.n_cells - w0) * 9;
+        const int nslot = min(kCellWindow, P.m.n_cells - w0) * 9;
         unsigned long long* g = P.acc9 + 9 * size_t(w0);
         for (int k = threadIdx.x; k < nslot; k += blockDim.x) {
-            const unsigned v = win[k];
-            if (v) atomicAdd(g + k, (unsigned long long)v);
+            const int rel = k / 9, j = k - 9 * rel;
+            const unsigned* a = win + kCellSlots * rel;
+            unsigned long long v = 0;
+            if (j == 0) {
+#pragma unroll
+                for (int q = 0; q < kCellSub; ++q) v += a[q];
+            } else {
+                v = a[kCellSub - 1 + j];
+            }
+            if (v) atomicAdd(g + k, v);
         }
     }
     if (threadIdx.x == 0) {
@@ -743,7 +876,8 @@ int launch_pusher(const MoveParams& P, int blocks, int chunk, bool cell, cudaStr
         move_kernel_fp32<PUSHER><<<blocks, 256, smem, s>>>(P, chunk);
         return 1;
     }
-    move_cell_kernel_fp32<PUSHER><<<blocks, 256, smem, s>>>(P, chunk);
+    const size_t cell_smem = size_t(kCellWindow) * kCellSlots * sizeof(unsigned);
+    move_cell_kernel_fp32<PUSHER><<<blocks, 256, cell_smem, s>>>(P, chunk);
     if (!P.solve_movement || !P.reflecting) return 1;
     track_queue_kernel_fp32<PUSHER><<<blocks, 256, 0, s>>>(P);
     return 2;

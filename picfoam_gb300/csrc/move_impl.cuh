@@ -106,7 +106,7 @@ __device__ __forceinline__ void field_at(const MoveParams& P, const TetConst& T,
 
 // BorisPusher::updateVelocity (submodels/ParticlePusher/BorisPusher/BorisPusher.C:69-112)
 template <class Real>
-__device__ __forceinline__ void push_boris(const MoveParams& P, const Real* E, Real* U, Real tt) {
+__device__ __forceinline__ void push_boris(const MoveParams& P, const Real* E, const Real* Bv, Real* U, Real tt) {
     const Real c = Real(kC);
     const Real dt2 = Real(0.5) * tt;
     const Real mU = sqrt(dot3(U, U)) / c;
@@ -119,7 +119,7 @@ __device__ __forceinline__ void push_boris(const MoveParams& P, const Real* E, R
     if (P.rotation) {
         const Real a0 = sqrt(dot3(oldrU, oldrU)) / c, a1 = sqrt(dot3(rU, rU)) / c;
         const Real lF = (sqrt(Real(1) + a0 * a0) + sqrt(Real(1) + a1 * a1)) / Real(2);
-        const Real t[3] = {qdm * PC<Real>::B(P, 0) / lF, qdm * PC<Real>::B(P, 1) / lF, qdm * PC<Real>::B(P, 2) / lF};
+        const Real t[3] = {qdm * Bv[0] / lF, qdm * Bv[1] / lF, qdm * Bv[2] / lF};
         Real cr[3];
         cross3(rU, t, cr);
         const Real Ud[3] = {rU[0] + cr[0], rU[1] + cr[1], rU[2] + cr[2]};
@@ -136,12 +136,12 @@ __device__ __forceinline__ void push_boris(const MoveParams& P, const Real* E, R
 
 // BorisNRPusher::updateVelocity (BorisNRPusher.C:69-99)
 template <class Real>
-__device__ __forceinline__ void push_boris_nr(const MoveParams& P, const Real* E, Real* U, Real tt) {
+__device__ __forceinline__ void push_boris_nr(const MoveParams& P, const Real* E, const Real* Bv, Real* U, Real tt) {
     const Real dt2 = Real(0.5) * tt;
     const Real alpha = PC<Real>::qdm(P, dt2);
     Real W[3] = {U[0] + alpha * E[0], U[1] + alpha * E[1], U[2] + alpha * E[2]};
     if (P.rotation) {
-        const Real t[3] = {alpha * PC<Real>::B(P, 0), alpha * PC<Real>::B(P, 1), alpha * PC<Real>::B(P, 2)};
+        const Real t[3] = {alpha * Bv[0], alpha * Bv[1], alpha * Bv[2]};
         Real cr[3];
         cross3(W, t, cr);
         const Real Ud[3] = {W[0] + cr[0], W[1] + cr[1], W[2] + cr[2]};
@@ -155,7 +155,7 @@ __device__ __forceinline__ void push_boris_nr(const MoveParams& P, const Real* E
 
 // VayPusher::updateVelocity (VayPusher.C:54-100); U x T uses v (VayPusher.C:81).
 template <class Real>
-__device__ __forceinline__ void push_vay(const MoveParams& P, const Real* E, Real* U, Real tt) {
+__device__ __forceinline__ void push_vay(const MoveParams& P, const Real* E, const Real* Bv, Real* U, Real tt) {
     const Real c = Real(kC);
     const Real dt2 = Real(0.5) * tt;
     const Real mU = sqrt(dot3(U, U)) / c;
@@ -164,7 +164,7 @@ __device__ __forceinline__ void push_vay(const MoveParams& P, const Real* E, Rea
     const Real qe = PC<Real>::qdm(P, tt);
     Real Ud[3] = {rU0[0] + qe * E[0], rU0[1] + qe * E[1], rU0[2] + qe * E[2]};
     const Real qb = PC<Real>::qdm(P, dt2);
-    Real T[3] = {qb * PC<Real>::B(P, 0), qb * PC<Real>::B(P, 1), qb * PC<Real>::B(P, 2)};
+    Real T[3] = {qb * Bv[0], qb * Bv[1], qb * Bv[2]};
     Real cr[3];
     cross3(U, T, cr);
     Ud[0] = Ud[0] + cr[0]; Ud[1] = Ud[1] + cr[1]; Ud[2] = Ud[2] + cr[2];
@@ -189,7 +189,7 @@ __device__ __forceinline__ void push_vay(const MoveParams& P, const Real* E, Rea
 
 // HigueraCaryPusher::updateVelocity (HigueraCary.C:69-115)
 template <class Real>
-__device__ __forceinline__ void push_hc(const MoveParams& P, const Real* E, Real* U, Real tt) {
+__device__ __forceinline__ void push_hc(const MoveParams& P, const Real* E, const Real* Bv, Real* U, Real tt) {
     const Real c = Real(kC);
     const Real dt2 = Real(0.5) * tt;
     const Real mU = sqrt(dot3(U, U)) / c;
@@ -201,7 +201,7 @@ __device__ __forceinline__ void push_hc(const MoveParams& P, const Real* E, Real
     if (P.rotation) {
         const Real mr0 = sqrt(dot3(rU, rU)) / c;
         const Real gfm2 = Real(1) + mr0 * mr0;
-        Real t[3] = {qdm * PC<Real>::B(P, 0), qdm * PC<Real>::B(P, 1), qdm * PC<Real>::B(P, 2)};
+        Real t[3] = {qdm * Bv[0], qdm * Bv[1], qdm * Bv[2]};
         const Real beta2 = dot3(t, t);
         const Real gb = gfm2 - beta2;
         const Real tr = dot3(t, rU);
@@ -221,16 +221,31 @@ __device__ __forceinline__ void push_hc(const MoveParams& P, const Real* E, Real
     U[0] = rU[0] / g1; U[1] = rU[1] / g1; U[2] = rU[2] / g1;
 }
 
+// The magnetic field the pushers use: the cell value (B[celli], as every
+// picFoam pusher reads it, e.g. BorisPusher.C:100) when a per-cell field is
+// set, else the uniform one.
+template <class Real>
+__device__ __forceinline__ void cell_B(const MoveParams& P, int cell, Real* Bv) {
+    if (P.Bc) {
+#pragma unroll
+        for (int a = 0; a < 3; ++a) Bv[a] = Real(P.Bc[3 * size_t(cell) + a]);
+    } else {
+#pragma unroll
+        for (int a = 0; a < 3; ++a) Bv[a] = PC<Real>::B(P, a);
+    }
+}
+
 template <class Real>
 __device__ __forceinline__ void push(const MoveParams& P, const TetConst& T, PState<Real>& s, Real tt) {
     if (P.pusher == PICGPU_PUSHER_NONE) return;
-    Real E[3];
+    Real E[3], Bv[3];
     field_at(P, T, s, E);
+    cell_B(P, s.cell, Bv);
     switch (P.pusher) {
-        case PICGPU_PUSHER_BORIS: push_boris(P, E, s.U, tt); break;
-        case PICGPU_PUSHER_BORIS_NR: push_boris_nr(P, E, s.U, tt); break;
-        case PICGPU_PUSHER_VAY: push_vay(P, E, s.U, tt); break;
-        default: push_hc(P, E, s.U, tt); break;
+        case PICGPU_PUSHER_BORIS: push_boris(P, E, Bv, s.U, tt); break;
+        case PICGPU_PUSHER_BORIS_NR: push_boris_nr(P, E, Bv, s.U, tt); break;
+        case PICGPU_PUSHER_VAY: push_vay(P, E, Bv, s.U, tt); break;
+        default: push_hc(P, E, Bv, s.U, tt); break;
     }
 }
 

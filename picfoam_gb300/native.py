@@ -47,6 +47,7 @@ def declare(lib, prefix, ctx_api=True):
     f("solve_poisson", i, [P, F64P, F64P, C.POINTER(abi.StepStats)])
     f("get_field", i, [P, i, F64P, C.c_size_t])
     f("set_field", i, [P, i, F64P, C.c_size_t])
+    f("set_step_index", i, [P, C.c_int64])
 
 
 def load():

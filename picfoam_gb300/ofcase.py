@@ -699,12 +699,17 @@ def _write_vol(path, obj, dims, values_of, vector, case, phi=False):
         f.write(_boundary_field(case, values_of, vector, phi))
 
 
-def write_fields(sim, case, t, cloud="pic"):
+def write_fields(sim, case, t, cloud="pic", step_index=None):
     """Write time directory `t` of the case: phiE, E, rhoCharge (cells in the
     case's order) and lagrangian/<cloud>/{U, typeId, chargeModifier,
     nParticle} (PICParcelIO.C:107-166) plus cartesianPositions (a vector
     field of this writer: positions as points, not OpenFOAM's barycentric
-    coordinates).  Returns the directory."""
+    coordinates).  For a restart with this library (`restart`) it also
+    writes the exact particle state -- picgpuTet (the context's tet index,
+    cell 12 + local tet) and picgpuBarycentric (coordinates 1..3) -- and
+    uniform/picgpuState (the step index and the floating patches' surface
+    charge density).  Every number has 17 significant digits, so the state
+    reads back bit for bit.  Returns the directory."""
     d = os.path.join(case.path, time_name(t))
     os.makedirs(d, exist_ok=True)
     order = case.cell_order
@@ -716,7 +721,7 @@ def write_fields(sim, case, t, cloud="pic"):
     _write_vol(os.path.join(d, "rhoCharge"), "rhoCharge", _RHO_DIM, rho, False, case)
     from .simulation import Mesh
     m = Mesh(case.mesh)
-    U, tid, npart, pos = [], [], [], []
+    U, tid, npart, pos, tets, barys = [], [], [], [], [], []
     for s in range(len(case.species)):
         tet, bary, u = sim.get_particles(s)
         if len(tet) == 0:
@@ -725,20 +730,102 @@ def write_fields(sim, case, t, cloud="pic"):
         tid.append(np.full(len(tet), s, dtype=np.int64))
         npart.append(np.full(len(tet), case.cfg.species[s].weight))
         pos.append(m.position(tet, bary))
+        tets.append(tet.astype(np.int64))
+        barys.append(bary)
     if U:
         ld = os.path.join(d, "lagrangian", cloud)
         os.makedirs(ld, exist_ok=True)
-        U, tid, npart, pos = (np.concatenate(x) for x in (U, tid, npart, pos))
+        U, tid, npart, pos, tets, barys = (np.concatenate(x) for x in (U, tid, npart, pos, tets, barys))
         loc = os.path.join(time_name(t), "lagrangian", cloud)
         for name, cls, body in (("U", "vectorField", foam.format_vectors(U)),
                                 ("typeId", "labelField", foam.format_labels(tid)),
                                 ("chargeModifier", "labelField", foam.format_labels(np.ones_like(tid))),
                                 ("nParticle", "scalarField", foam.format_scalars(npart)),
-                                ("cartesianPositions", "vectorField", foam.format_vectors(pos))):
+                                ("cartesianPositions", "vectorField", foam.format_vectors(pos)),
+                                ("picgpuTet", "labelField", foam.format_labels(tets)),
+                                ("picgpuBarycentric", "vectorField", foam.format_vectors(barys))):
             with open(os.path.join(ld, name), "w") as f:
                 f.write(foam.header(cls, name, location=loc))
                 f.write(body)
+    if step_index is None:
+        step_index = int(round(t / case.delta_t)) if case.delta_t > 0 else 0
+    sigma = sim.field(abi.FIELD_PATCH_SIGMA)
+    ud = os.path.join(d, "uniform")
+    os.makedirs(ud, exist_ok=True)
+    with open(os.path.join(ud, "picgpuState"), "w") as f:
+        f.write(foam.header("dictionary", "picgpuState", location=os.path.join(time_name(t), "uniform")))
+        f.write(f"stepIndex       {int(step_index)};\n\n")
+        f.write("patchSigma      " + foam.format_scalars(sigma).replace("\n", " ") + ";\n")
     return d
+
+
+def read_list(path):
+    """The list after the FoamFile header of a lagrangian or polyMesh file
+    (labels, scalars or vectors) as a numpy array."""
+    with open(path) as f:
+        txt = f.read()
+    body = txt[txt.index("}", txt.index("FoamFile")) + 1:]
+    inner = body[body.index("(") + 1:body.rindex(")")]
+    vectors = "(" in inner
+    vals = np.array(inner.replace("(", " ").replace(")", " ").split(), dtype=np.float64)
+    return vals.reshape(-1, 3) if vectors else vals
+
+
+def latest_time(case):
+    """The latest time directory of the case (controlDict startFrom latestTime)."""
+    times = []
+    for name in os.listdir(case.path):
+        try:
+            t = float(name)
+        except ValueError:
+            continue
+        if os.path.isdir(os.path.join(case.path, name)) and t > 0:
+            times.append(t)
+    if not times:
+        raise FileNotFoundError(f"{case.path}: no time directory to restart from")
+    return max(times)
+
+
+def restart(sim, case, t=None, cloud="pic"):
+    """Continue a run from time directory `t` (default: the latest), the
+    startFrom latestTime of picFoam (PICParcelIO.C:83-120 reads the parcels
+    back): particles from picgpuTet / picgpuBarycentric / U / typeId (the
+    state this library writes; without them the cartesianPositions are
+    located again, which rounds the coordinates), the potential phiE, the
+    step index and the floating patches' surface charge.  The charge density
+    and E are recomputed from them: with the written potential as the start
+    guess the Poisson solve is already converged, so a FP64 run continues
+    bit for bit.  Not restored: the remainders of injection, emission and
+    collision models, MCC (sigma v)_max and circuit states.  Returns t."""
+    if t is None:
+        t = latest_time(case)
+    d = os.path.join(case.path, time_name(t))
+    ld = os.path.join(d, "lagrangian", cloud)
+    if os.path.isdir(ld):
+        tid = read_list(os.path.join(ld, "typeId")).astype(np.int64)
+        U = read_list(os.path.join(ld, "U")).reshape(-1, 3)
+        if os.path.exists(os.path.join(ld, "picgpuTet")):
+            tet = read_list(os.path.join(ld, "picgpuTet")).astype(np.int32)
+            bary = read_list(os.path.join(ld, "picgpuBarycentric")).reshape(-1, 3)
+        else:
+            from .simulation import Mesh
+            tet, bary = Mesh(case.mesh).locate(read_list(os.path.join(ld, "cartesianPositions")).reshape(-1, 3))
+        for s in range(len(case.species)):
+            sel = tid == s
+            sim.set_particles(s, tet[sel], bary[sel], U[sel])
+    phi_case = read_field(os.path.join(d, "phiE"))
+    phi = np.empty_like(phi_case)
+    phi[case.cell_order] = phi_case
+    state_path = os.path.join(d, "uniform", "picgpuState")
+    step_index = int(round(t / case.delta_t)) if case.delta_t > 0 else 0
+    if os.path.exists(state_path):
+        st = foam.read(state_path)
+        step_index = int(st["stepIndex"])
+        sim.set_field(abi.FIELD_PATCH_SIGMA, foam.numeric_list(st["patchSigma"]))
+    sim.set_step_index(step_index)
+    sim.set_field(abi.FIELD_PHI, phi)
+    sim.initialise_fields()
+    return t
 
 
 def read_field(path):

@@ -2,13 +2,15 @@
 loop, solver/picFoam/picFoam.C, over the picgpu C ABI).
 
     python -m picfoam_gb300.run CASE [--steps N] [--write-mesh] [--mixed]
-                                     [--allow-unsupported] [--oracle]
+                                     [--restart] [--allow-unsupported] [--oracle]
 
 Reads the case (`ofcase.load_case`), runs picInitialise when the case has a
 picInitialiseDict, steps to controlDict's endTime (or N steps) and writes a
 time directory (phiE, E, rhoCharge, lagrangian/pic) every writeInterval and
-at the end.  --write-mesh also writes constant/polyMesh.  --oracle runs the
-CPU oracle instead of the GPU (test use only).
+at the end.  --write-mesh also writes constant/polyMesh.  --restart continues
+from the latest time directory (startFrom latestTime; see ofcase.restart for
+what is restored).  --oracle runs the CPU oracle instead of the GPU (test use
+only).
 """
 import argparse
 import sys
@@ -24,6 +26,7 @@ def main(argv=None):
     ap.add_argument("--write-mesh", action="store_true")
     ap.add_argument("--mixed", action="store_true", help="FP32 push/track, FP64 charge and Poisson")
     ap.add_argument("--allow-unsupported", action="store_true")
+    ap.add_argument("--restart", action="store_true", help="continue from the latest time directory")
     ap.add_argument("--oracle", action="store_true", help=argparse.SUPPRESS)
     args = ap.parse_args(argv)
 
@@ -39,11 +42,16 @@ def main(argv=None):
         backend = pyoracle.OracleBackend(1)
     if args.write_mesh:
         ofcase.write_poly_mesh(case)
-    sim = case.build(backend=backend)
-    steps = args.steps if args.steps is not None else int(round(case.end_time / case.delta_t))
+    sim = case.build(backend=backend, initialise=not args.restart)
+    done = 0
+    if args.restart:
+        t_start = ofcase.restart(sim, case)
+        done = int(round(t_start / case.delta_t))
+        print(f"[picfoam_gb300] restarted at Time = {ofcase.time_name(t_start)}", flush=True)
+    total = int(round(case.end_time / case.delta_t))
+    steps = done + args.steps if args.steps is not None else total
     every = max(1, int(round(case.write_interval / case.delta_t))) if case.write_interval > 0 else steps
     t0 = time.time()
-    done = 0
     while done < steps:
         k = min(every - done % every, steps - done)
         st = sim.step(k)
@@ -52,7 +60,7 @@ def main(argv=None):
         counts = " ".join(f"{n}={st.n_particles[s]}" for s, n in enumerate(case.species))
         print(f"Time = {ofcase.time_name(t)}  {counts}  PCG iterations {st.pcg_iterations}", flush=True)
         if done % every == 0 or done == steps:
-            ofcase.write_fields(sim, case, t)
+            ofcase.write_fields(sim, case, t, step_index=done)
     print(f"[picfoam_gb300] {done} steps in {time.time() - t0:.2f} s")
     return 0
 

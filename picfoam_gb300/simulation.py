@@ -209,7 +209,8 @@ class Simulation:
     # -------------------------------------------------------------- fields
     def _field_len(self, which, n_cells, n_points):
         return {abi.FIELD_PHI: n_cells, abi.FIELD_E_CELL: 3 * n_cells, abi.FIELD_RHO: n_cells,
-                abi.FIELD_E_POINT: 3 * n_points, abi.FIELD_SIGMA_V_MAX: n_cells}[which]
+                abi.FIELD_E_POINT: 3 * n_points, abi.FIELD_SIGMA_V_MAX: n_cells,
+                abi.FIELD_B_CELL: 3 * n_cells, abi.FIELD_PATCH_SIGMA: 6 + self.mesh_desc.n_boxes}[which]
 
     def sizes(self):
         """(n_cells, n_points) of the mesh."""
@@ -224,9 +225,13 @@ class Simulation:
         n = self._field_len(which, nc, npnt)
         out = np.zeros(n)
         self._check(self._fn("get_field")(self._h, which, out.ctypes.data_as(C.POINTER(C.c_double)), n))
-        if which in (abi.FIELD_E_CELL, abi.FIELD_E_POINT):
+        if which in (abi.FIELD_E_CELL, abi.FIELD_E_POINT, abi.FIELD_B_CELL):
             out = out.reshape(-1, 3)
         return out
+
+    def set_step_index(self, steps_done):
+        """Continue a run after `steps_done` steps (restart from a time directory)."""
+        self._check(self._fn("set_step_index")(self._h, int(steps_done)))
 
     def set_field(self, which, values):
         v, vp = _f64(np.ravel(values))

@@ -39,3 +39,28 @@ def test_case_runner_writes_time_directories(gpu, tmp_path):
     assert os.path.exists(os.path.join(str(tmp_path), "constant", "polyMesh", "faces"))
     phi = ofcase.read_field(os.path.join(str(tmp_path), "4e-12", "phiE"))
     assert np.all(np.isfinite(phi)) and phi.shape == (120,)
+
+
+@pytest.mark.parametrize("mixed", [False, True])
+def test_restart_continues_bit_for_bit_on_gpu(tmp_path, mixed):
+    """startFrom latestTime on the GPU: written at step 2 and continued, the
+    run ends where the uninterrupted one does, bit for bit (FP64 and the
+    FP32 store alike: the state is written with 17 digits)."""
+    from picfoam_gb300 import foam
+    from test_ofcase import make_case as make
+    a, b = str(tmp_path / "a"), str(tmp_path / "b")
+    make(a, injection=False)
+    make(b, injection=False)
+    extra = ["--mixed"] if mixed else []
+    assert run.main([a, "--steps", "4"] + extra) == 0
+    assert run.main([b, "--steps", "2"] + extra) == 0
+    assert run.main([b, "--restart", "--steps", "2"] + extra) == 0
+    la, lb = (os.path.join(p, "4e-12", "lagrangian", "pic") for p in (a, b))
+    for name in ("picgpuTet", "picgpuBarycentric", "U", "typeId"):
+        np.testing.assert_array_equal(ofcase.read_list(os.path.join(la, name)),
+                                      ofcase.read_list(os.path.join(lb, name)))
+    np.testing.assert_array_equal(ofcase.read_field(os.path.join(a, "4e-12", "phiE")),
+                                  ofcase.read_field(os.path.join(b, "4e-12", "phiE")))
+    sa = foam.read(os.path.join(a, "4e-12", "uniform", "picgpuState"))
+    sb = foam.read(os.path.join(b, "4e-12", "uniform", "picgpuState"))
+    np.testing.assert_array_equal(foam.numeric_list(sa["patchSigma"]), foam.numeric_list(sb["patchSigma"]))

@@ -51,8 +51,13 @@ def write(path, rel, text):
         fh.write(HEADER % os.path.basename(rel) + text)
 
 
-def make_case(path, pusher="Boris"):
-    """A 6 x 4 x 5 block whose local axes are x1 = -y, x2 = -z, x3 = +x."""
+def make_case(path, pusher="Boris", injection=True):
+    """A 6 x 4 x 5 block whose local axes are x1 = -y, x2 = -z, x3 = +x
+    (injection=False leaves the SimpleInjection of the source patch out)."""
+    source = ("""source { type SimpleInjection; SimpleInjectionCoeffs { frequencies (1e15 2e14); injectionEndTime 1;
+                     eV (2 0.1); injectionTypeIds (e Ar+); velocityModel halfMaxwellianFlux;
+                     interactions { e { type deletion; } Ar+ { type deletion; } } } }"""
+              if injection else "")
     write(path, "system/blockMeshDict", """
 convertToMeters 0.001;
 vertices ((0 4 5) (0 0 5) (0 0 0) (0 4 0) (6 4 5) (6 0 5) (6 0 0) (6 4 0));
@@ -96,9 +101,7 @@ BoundaryModels
     {{
         modelList
         (
-            source {{ type SimpleInjection; SimpleInjectionCoeffs {{ frequencies (1e15 2e14); injectionEndTime 1;
-                     eV (2 0.1); injectionTypeIds (e Ar+); velocityModel halfMaxwellianFlux;
-                     interactions {{ e {{ type deletion; }} Ar+ {{ type deletion; }} }} }} }}
+            {source}
             collector {{ type FloatingPotential; }}
         );
     }}
@@ -283,3 +286,28 @@ def test_reference_magnetic_rotation_gyrates(oracle_backend):
         x = m.position(t, b)
         assert np.linalg.norm(x[0, :2]) == pytest.approx(r0, rel=1e-7)
         assert np.linalg.norm(U[0]) == pytest.approx(29979246.0, rel=1e-12)
+
+
+def test_restart_continues_bit_for_bit(oracle_backend, tmp_path):
+    """startFrom latestTime (PICParcelIO.C:83-120): a run written at step 2
+    and continued from that time directory reproduces the uninterrupted run
+    -- particles, potential and the floating patch's charge -- bit for bit
+    in FP64."""
+    from picfoam_gb300 import run
+    a, b = str(tmp_path / "a"), str(tmp_path / "b")
+    make_case(a, injection=False)
+    make_case(b, injection=False)
+    assert run.main([a, "--oracle", "--steps", "4"]) == 0
+    assert run.main([b, "--oracle", "--steps", "2"]) == 0
+    assert run.main([b, "--oracle", "--restart", "--steps", "2"]) == 0
+    la, lb = (os.path.join(p, "4e-12", "lagrangian", "pic") for p in (a, b))
+    for name in ("picgpuTet", "picgpuBarycentric", "U", "typeId"):
+        np.testing.assert_array_equal(ofcase.read_list(os.path.join(la, name)),
+                                      ofcase.read_list(os.path.join(lb, name)))
+    np.testing.assert_array_equal(ofcase.read_field(os.path.join(a, "4e-12", "phiE")),
+                                  ofcase.read_field(os.path.join(b, "4e-12", "phiE")))
+    sa = foam.read(os.path.join(a, "4e-12", "uniform", "picgpuState"))
+    sb = foam.read(os.path.join(b, "4e-12", "uniform", "picgpuState"))
+    assert sa["stepIndex"] == sb["stepIndex"] == 4
+    np.testing.assert_array_equal(foam.numeric_list(sa["patchSigma"]), foam.numeric_list(sb["patchSigma"]))
+    assert np.abs(foam.numeric_list(sa["patchSigma"])).max() > 0      # the collector has charged
