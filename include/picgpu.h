@@ -323,6 +323,54 @@ typedef struct {
     double  ref_area;       /* IdealCurrentSource refArea (> 0: I scaled by cathode area / refArea) */
 } picgpu_circuit;
 
+/* ParticleMerging PairMerging (SM/ParticleMerging/PairMerging/PairMerging.C:35-259),
+ * run at the end of every step (PICCloud::evolve, PICCloud.C:1470).  In a
+ * cell whose parcels of a listed species outnumber cell_parcels_max, random
+ * parcels are merged with a neighbour in speed order (the nCheckNeighbors
+ * window) into one parcel at their weighted centre with their summed
+ * nParticle and weighted mean velocity, until the count is down to
+ * reduction_factor of it (at most merge_maximum_per_cell merges) or
+ * max_checks attempts.  Listed species keep per-parcel attributes. */
+typedef struct {
+    int32_t enabled;
+    int32_t n_species;                 /* entries of species[] (merge order) */
+    int32_t species[PICGPU_MAX_SPECIES];
+    double  n_deviation[PICGPU_MAX_SPECIES]; /* nDeviation: largest nParticle difference of a pair */
+    double  reduction_factor;          /* reductionFactor */
+    double  angle_difference;          /* angleDifference [degrees] */
+    double  velocity_ratio;            /* velocityRatio */
+    int32_t cell_parcels_max;          /* cellParcelsMax */
+    int32_t max_checks;                /* maxChecks */
+    int32_t n_check_neighbors;         /* nCheckNeighbors */
+    int32_t merge_maximum_per_cell;    /* mergeMaximumPerCell */
+} picgpu_merging;
+
+/* CoulombCollisionModel IonizationModel Perez (PerezIonizationModel.C:30-118,
+ * selected at CoulombCollisionModel.C:72-79): electron-impact ionisation of
+ * ion parcels inside their Coulomb collisions with electrons (the
+ * electron species is picgpu_config.electron_species).  Per ion species its
+ * atomic number, the ionisation limit (< 0: the atomic number; 0: no
+ * ionisation), the orbital binding energies and the ionisation energies of
+ * the charge states [eV] (atomicNumber entries each).  An ionisation raises
+ * the ion parcel's charge modifier and adds an electron parcel with the
+ * ion's nParticle, so the ion and electron species keep per-parcel
+ * attributes. */
+#define PICGPU_PEREZ_MAX_Z 64
+#define PICGPU_PEREZ_MAX_IONS 4
+typedef struct {
+    int32_t species;              /* ionSpecies */
+    int32_t atomic_number;        /* atomicNumber (<= PICGPU_PEREZ_MAX_Z) */
+    int32_t ionization_limit;     /* ionizationLimit */
+    int32_t pad;
+    double  binding_energy[PICGPU_PEREZ_MAX_Z];     /* bindingEnergy [eV] */
+    double  ionization_energy[PICGPU_PEREZ_MAX_Z];  /* ionizationEnergy [eV] */
+} picgpu_perez_ion;
+typedef struct {
+    int32_t enabled;
+    int32_t n_ions;
+    picgpu_perez_ion ion[PICGPU_PEREZ_MAX_IONS];
+} picgpu_perez;
+
 typedef struct {
     int32_t pusher;               /* PICGPU_PUSHER_* */
     int32_t field_weighting;      /* PICGPU_WEIGHTING_* */
@@ -352,6 +400,8 @@ typedef struct {
     picgpu_multigrid mg;
     picgpu_binary binary;
     picgpu_circuit circuit;
+    picgpu_merging merging;
+    picgpu_perez perez;
 } picgpu_config;
 
 typedef struct {
@@ -399,6 +449,11 @@ typedef struct {
     int64_t ion_parcel_candidates;              /* ion - neutral parcel pairs tested */
     int64_t ion_parcel_elastic;
     int64_t ion_parcel_charge_exchange;
+    int64_t merged_parcels;                     /* PairMerging: merges this step */
+    int64_t merge_checks;                       /* candidate partners checked */
+    double  merge_kinetic_energy_error;         /* kinetic energy after - before the merges [J] */
+    int64_t coulomb_ionizations;                /* Perez ionisation: collisions that ionised */
+    int64_t coulomb_ionization_electrons;       /* electron parcels they added */
 } picgpu_step_stats;
 
 typedef struct picgpu_ctx picgpu_ctx;
@@ -463,6 +518,22 @@ picgpu_status picgpu_count_particles(picgpu_ctx* ctx, int species, size_t* n);
 /* Copy one species out, compacted (removed particles dropped), in storage order. */
 picgpu_status picgpu_get_particles(picgpu_ctx* ctx, int species, size_t cap,
                                    int32_t* tet, double* bary, double* U, size_t* n);
+
+/* Per-parcel weight and charge state of one species: PICParcel's
+ * nParticle_ and chargeModifier_ (PICParcel.H:182-195; charge = species
+ * charge x chargeModifier, PICCloud.C:368), in the order of
+ * picgpu_get_particles.  Until set here, or until a model that changes them
+ * (PairMerging, the Perez ionisation model) acts on the species, every
+ * parcel has the species weight and charge modifier 1 and the store keeps
+ * no per-parcel arrays.  Set: n must equal the species' parcel count,
+ * nParticle in (0, 4096 x species weight], chargeModifier in [0, 1024];
+ * the store is compacted first.  Parcels created later (injection,
+ * collisions, picInitialise) get the defaults (PICCloud::addNewParcel,
+ * PICCloud.C:707-723).  Get works with or without per-parcel arrays. */
+picgpu_status picgpu_set_parcel_attributes(picgpu_ctx* ctx, int species, size_t n,
+                                           const double* nParticle, const int32_t* chargeModifier);
+picgpu_status picgpu_get_parcel_attributes(picgpu_ctx* ctx, int species, size_t cap,
+                                           double* nParticle, int32_t* chargeModifier, size_t* n);
 
 /* The whole population as one set of parcels (the cloud's IDLList of
  * PICParcel, PICParcel.H:182-195, with typeId per parcel): species[i],
@@ -572,6 +643,13 @@ picgpu_status picgpu_step(picgpu_ctx* ctx, int nsteps, picgpu_step_stats* stats)
 /* One pass of push + track + deposit over all particles (no collisions, no
  * field solve): the particle hot path alone. */
 picgpu_status picgpu_move(picgpu_ctx* ctx, picgpu_step_stats* stats);
+
+/* E (cells, points and the FP32 corner blocks) from the current potential
+ * and boundary conditions, without a Poisson solve: the field part of
+ * ElectroStaticSolver::solveFields (ElectroStaticSolver.C:52-71, E = -grad
+ * phiE) for a run that continues from a written potential.  No-op when the
+ * Maxwell solver is not ElectroStatic. */
+picgpu_status picgpu_compute_field(picgpu_ctx* ctx);
 
 /* Restart: the number of time steps already done, i.e. the time index the
  * picFoam run continues from (startFrom latestTime reads it from the time

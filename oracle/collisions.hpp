@@ -74,6 +74,8 @@ struct Philox {
 };
 
 enum : uint32_t {
+    kStreamMerge = 0u,                   // PairMerging per (merge-list entry, cell, step)
+    kStreamIonize = 1u << 27,            // Perez ionisation per (Coulomb collision ordinal, cell, step)
     kStreamMcc = 1u << 28,
     kStreamCoulomb = 2u << 28,
     kStreamRemainder = 3u << 28,
@@ -100,6 +102,12 @@ inline Philox coulomb_pair_stream(uint64_t seed, uint32_t cell, uint32_t step, l
     Philox p(seed, kStreamCoulomb, cell, step);
     p.ctr[0] = 0x80000000u + uint32_t(k) * 8u;
     return p;
+}
+
+// The Perez ionisation draws of the Coulomb collision of ordinal k in a cell
+// and step.
+inline Philox ionize_stream(uint64_t seed, uint32_t cell, uint32_t step, long k) {
+    return Philox(seed, kStreamIonize | uint32_t(k), cell, step);
 }
 
 // The sum of f(t), t in [0, n), in the order of a 32-lane warp reduction:

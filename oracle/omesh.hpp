@@ -447,6 +447,31 @@ inline long long locate(const Mesh& m, const double* x, double* y) {
     return 12LL * c + best;
 }
 
+// x in cell c (known): the tet whose smallest barycentric coordinate is
+// largest, coordinates clamped to >= 0 and renormalised, as locate() does
+// once it has the cell.  Returns cell 12 + tet.
+inline long long locate_in_cell(const Mesh& m, int c, const double* x, double* y) {
+    int best = 0;
+    double best_min = -1e300, q[3] = {0.0, 0.0, 0.0};
+    for (int t = 0; t < 12; ++t) {
+        double w[3];
+        tet_coords(m, c, t, x, w);
+        const double lowest = std::fmin(std::fmin(1.0 - w[0] - w[1] - w[2], w[0]), std::fmin(w[1], w[2]));
+        if (lowest > best_min) {
+            best_min = lowest;
+            best = t;
+            q[0] = w[0];
+            q[1] = w[1];
+            q[2] = w[2];
+        }
+    }
+    const double all[4] = {std::fmax(1.0 - q[0] - q[1] - q[2], 0.0), std::fmax(q[0], 0.0), std::fmax(q[1], 0.0),
+                           std::fmax(q[2], 0.0)};
+    const double sum = all[0] + all[1] + all[2] + all[3];
+    for (int k = 0; k < 3; ++k) y[k] = all[k + 1] / sum;
+    return 12LL * c + best;
+}
+
 // The point of barycentric coordinates y (1..3) in tet `tet` (cell 12 + t).
 inline void position(const Mesh& m, long long tet, const double* y, double* x) {
     const long long c = tet / 12;

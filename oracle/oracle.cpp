@@ -64,6 +64,10 @@ struct Parcel {
     double y[4] = {1, 0, 0, 0};
     V3 U{0, 0, 0};
     bool alive = true;
+    // PICParcel nParticle_ (negative: the species weight, as addNewParcel
+    // sets it, PICCloud.C:707-723) and chargeModifier_ (PICParcel.H:182-195)
+    double nw = -1.0;
+    int zq = 1;
 };
 
 // Deterministic reduction: the fixed order the CUDA kernels reduce in (256
@@ -154,6 +158,15 @@ struct Oracle {
     ob::CircuitState circuit{};
     bool rotation = false;
     std::vector<double> Bcell;   // per-cell magnetic field (3 per cell); empty: the uniform cfg.B
+    // parcels of the step's cell occupancy per species (the slots before the
+    // collision secondaries; neutral parcels deleted on the way come off)
+    std::vector<long> occ_n;
+    // Perez ionisation tables per species (inactive: limit < 0)
+    struct PerezTab {
+        int atomic = 0, limit = -1;
+        std::vector<double> cs, te, le;   // [Zstar][100]: cross section, transferred and lost energy
+    };
+    std::vector<PerezTab> perez;
     double move_seconds = 0;
     long long step_index = 0;
     // collision state
@@ -196,6 +209,11 @@ struct Oracle {
 // VolumeWeighting (VolumeWeightingFW.C:60-67 -> interpolationCellPoint):
 //   E = y0 E_cell + y1 E_pt[tri0] + y2 E_pt[tri1] + y3 E_pt[tri2].
 // CellAverage (CellAverageFW.C:58-65): E = E_cell.
+// A parcel's nParticle and charge (species charge x chargeModifier,
+// PICCloud.C:368).
+double pweight(const Oracle& o, const Parcel& p, int s) { return p.nw < 0.0 ? o.cfg.species[s].weight : p.nw; }
+double pcharge(const Oracle& o, const Parcel& p, int s) { return o.cfg.species[s].charge * double(p.zq); }
+
 V3 field_at(const Oracle& o, const Parcel& p) {
     const HexMesh& m = o.m;
     const double* Ec = &o.E[3 * size_t(p.cell)];
@@ -315,7 +333,7 @@ void push_hc(const Oracle& o, Parcel& p, double q, double mass, double trackTime
 
 // ParticlePusher::updateVelocity dispatch (ParticlePusher.H:131-134)
 void push(const Oracle& o, Parcel& p, int species, double trackTime) {
-    const double q = o.cfg.species[species].charge, mass = o.cfg.species[species].mass;
+    const double q = pcharge(o, p, species), mass = o.cfg.species[species].mass;
     switch (o.cfg.pusher) {
         case PICGPU_PUSHER_BORIS: push_boris(o, p, q, mass, trackTime); break;
         case PICGPU_PUSHER_BORIS_NR: push_boris_nr(o, p, q, mass, trackTime); break;
@@ -374,7 +392,7 @@ int tet_step(const Oracle& o, Parcel& p, const double* dx, double* lambda) {
 
 // PICParcel::syncVelocityAtBoundary (PIC/parcels/Templates/PICParcel/PICParcel.C:220-227)
 void sync_velocity(const Oracle& o, Parcel& p, int species, double fraction) {
-    if (o.cfg.sync_velocity_at_boundary && o.cfg.species[species].charge != 0.0)
+    if (o.cfg.sync_velocity_at_boundary && pcharge(o, p, species) != 0.0)
         push(o, p, species, fraction * o.cfg.dt);
 }
 
@@ -394,7 +412,7 @@ void hit_patch(Oracle& o, Parcel& p, int species, int patch, double sf, TrackDat
     const bool charged = o.cfg.species[species].charge != 0.0;
     if (P.kind == PICGPU_PATCH_FLOATING || (P.kind == PICGPU_PATCH_CIRCUIT && charged)) {
         td.keep = false;
-        td.qconv[patch] += o.cfg.species[species].weight * o.cfg.species[species].charge;
+        td.qconv[patch] += pweight(o, p, species) * pcharge(o, p, species);
         return;
     }
     const int f = p.tet / 2;
@@ -465,7 +483,7 @@ void move_parcel(Oracle& o, Parcel& p, int species, TrackData& td) {
     // the particle store holds three barycentric coordinates; the centre one
     // is re-derived at the start of every step
     p.y[0] = 1.0 - p.y[1] - p.y[2] - p.y[3];
-    if (sp.charge != 0.0) push(o, p, species, o.cfg.dt);
+    if (pcharge(o, p, species) != 0.0) push(o, p, species, o.cfg.dt);
     if (!(magv(p.U) < kC)) { td.keep = false; td.superluminal = true; return; }
     const HexMesh& m = o.m;
     double sf = 0.0;
@@ -510,7 +528,7 @@ void reset_charge(Oracle& o) {
 // ChargeDistribution::add: VolumeWeighting (VolumeWeighting.C:105-124),
 // CellAverage (CellAverage.C:53-60).
 void deposit(Oracle& o, const Parcel& p, int species) {
-    const double value = o.cfg.species[species].charge * o.cfg.species[species].weight;
+    const double value = pcharge(o, p, species) * pweight(o, p, species);
     if (value == 0.0) return;
     const HexMesh& m = o.m;
     const bool fixed = o.cfg.deposit_mode == PICGPU_DEPOSIT_FIXED_POINT;
@@ -1236,6 +1254,7 @@ void mcc_parcels(Oracle& o, std::vector<std::vector<std::vector<int>>>& occ, pic
             moved[k] = int(w);
             neu[w++] = neu[k];
         }
+    if (size_t(ns) < o.occ_n.size()) o.occ_n[ns] -= long(neu.size() - w);
     neu.resize(w);
     for (auto& list : occ[ns])
         for (int& idx : list) idx = moved[idx];
@@ -1472,7 +1491,7 @@ void sentoku_kemp(double mass, double dw, const V3& pre, V3& U, ocoll::Philox& r
 void weight_correct(Oracle& o, Parcel& P, int sp, Parcel& Q, int sq, const V3& preP, const V3& preQ,
                     ocoll::Philox& r) {
     const int wc = o.cfg.coulomb.weight_correction;
-    const double wP = o.cfg.species[sp].weight, wQ = o.cfg.species[sq].weight;
+    const double wP = pweight(o, P, sp), wQ = pweight(o, Q, sq);
     if (wc == 1) {
         const double u = r.uniform();
         if (u > wP / wQ) Q.U = preQ;
@@ -1491,8 +1510,8 @@ void weight_correct(Oracle& o, Parcel& P, int sp, Parcel& Q, int sq, const V3& p
 // NanbuCollision::collide (NanbuCollision.C:60-135).
 void nanbu_collide(Oracle& o, Parcel& P, int sp, Parcel& Q, int sq, double lD, double nP, double nQ,
                    double nPQ, ocoll::Philox& r) {
-    const double mP = o.cfg.species[sp].mass, qP = o.cfg.species[sp].charge;
-    const double mQ = o.cfg.species[sq].mass, qQ = o.cfg.species[sq].charge;
+    const double mP = o.cfg.species[sp].mass, qP = pcharge(o, P, sp);
+    const double mQ = o.cfg.species[sq].mass, qQ = pcharge(o, Q, sq);
     const double reMass = mP * mQ / (mP + mQ);
     const V3 g = sub(P.U, Q.U);
     const double gm = magv(g);
@@ -1521,8 +1540,8 @@ void nanbu_collide(Oracle& o, Parcel& P, int sp, Parcel& Q, int sq, double lD, d
 // PerezRelativisticCollision::collide (PerezRelativisticCollision.C:60-192).
 void perez_collide(Oracle& o, Parcel& P, int sp, Parcel& Q, int sq, double lD, double nP, double nQ,
                    double nPQ, ocoll::Philox& r) {
-    const double mP = o.cfg.species[sp].mass, qP = o.cfg.species[sp].charge;
-    const double mQ = o.cfg.species[sq].mass, qQ = o.cfg.species[sq].charge;
+    const double mP = o.cfg.species[sp].mass, qP = pcharge(o, P, sp);
+    const double mQ = o.cfg.species[sq].mass, qQ = pcharge(o, Q, sq);
     CoM f;
     if (!com_frame(P.U, Q.U, mP, mQ, f)) return;
     const double mgsum = mP * f.gP + mQ * f.gQ;
@@ -1552,13 +1571,244 @@ void perez_collide(Oracle& o, Parcel& P, int sp, Parcel& Q, int sq, double lD, d
     weight_correct(o, P, sp, Q, sq, preP, preQ, r);
 }
 
+// ---- PerezIonizationModel (CoulombCollisionModel/IonizationModel/
+// PerezIonizationModel/PerezIonizationModel.C) ------------------------------
+
+// IonizationData::calculateIonizationCrossSection (PerezIonizationModel.C:
+// 405-484): per charge state the orbital-summed cross section, and the mean
+// energies transferred to the new electron and lost by the colliding one
+// (in m_e c^2), on 100 log-spaced energies 1 eV - 10 MeV; binding energies
+// after Carlson (bindingEnergy, :395-399).
+Oracle::PerezTab perez_tables(const picgpu_perez_ion& in) {
+    Oracle::PerezTab T;
+    const int A = in.atomic_number;
+    T.atomic = A;
+    T.limit = in.ionization_limit < 0 ? A : std::min(in.ionization_limit, A);
+    T.cs.assign(size_t(A) * 100, 0.0);
+    T.te.assign(size_t(A) * 100, 0.0);
+    T.le.assign(size_t(A) * 100, 0.0);
+    auto binding = [&](int Z, int k) {
+        return in.ionization_energy[Z] - in.binding_energy[A - Z - 1] + in.binding_energy[k];
+    };
+    const double r_e = 2.8179403227e-15;
+    const double step = 99.0 / std::log(1e7 / 1.0);
+    for (int Z = 0; Z < A; ++Z)
+        for (int i = 0; i < 100; ++i) {
+            const double E = std::exp(double(i) / step);
+            int N = 1;
+            double cs = 0.0, te = 0.0, le = 0.0;
+            for (int k = 0; k < A - Z; ++k) {
+                const double Bk = binding(Z, k);
+                if (k < A - Z - 1 && Bk == binding(Z, k + 1)) {
+                    N++;
+                    continue;
+                }
+                const double eps = E / Bk;
+                if (eps > 1.0) {
+                    const double b_dash = Bk / 510997.37;
+                    const double eps_dash = E / 510997.37;
+                    const double u_dash = b_dash;
+                    const double beta_eps2 = 1.0 - 1.0 / ((1.0 + eps_dash) * (1.0 + eps_dash));
+                    const double beta_b2 = 1.0 - 1.0 / ((1.0 + b_dash) * (1.0 + b_dash));
+                    const double beta_u2 = 1.0 - 1.0 / ((1.0 + u_dash) * (1.0 + u_dash));
+                    const double sigma0 = 2.0 * kPi * r_e * r_e * N / (b_dash * (beta_eps2 + beta_b2 + beta_u2));
+                    double ediv2 = 1.0 + eps_dash * 0.5;
+                    ediv2 *= ediv2;
+                    const double A1 = 1.0 / (1.0 + eps) * (1.0 + 2 * eps_dash) / ediv2;
+                    const double A2 = (eps - 1.0) / 2.0 * b_dash * b_dash / ediv2;
+                    const double A3 = std::log(beta_eps2 / (1.0 - beta_eps2)) - beta_eps2 - std::log(2.0 * b_dash);
+                    const double sk = sigma0 * (0.5 * A3 * (1.0 - 1.0 / (eps * eps)) + 1.0 - 1.0 / eps + A2 -
+                                                A1 * std::log(eps));
+                    const double wk = sigma0 * (0.5 * A3 * (eps - 1.0) * (eps - 1.0) / (eps * (eps - 1.0)) +
+                                                2.0 * std::log((eps + 1.0) * 0.5) - std::log(eps) +
+                                                A2 * (eps - 1.0) * 0.25 -
+                                                A1 * (std::log(eps) - (eps + 1.0) * std::log(0.5 * (eps + 1.0))));
+                    const double ek = sk + wk;
+                    cs += sk;
+                    te += wk * b_dash;
+                    le += ek * b_dash;
+                }
+                N = 1;
+            }
+            if (cs > 0.0) {
+                te /= cs;
+                le /= cs;
+            }
+            T.cs[size_t(Z) * 100 + i] = cs;
+            T.te[size_t(Z) * 100 + i] = te;
+            T.le[size_t(Z) * 100 + i] = le;
+        }
+    return T;
+}
+
+// The model's state between the calls of one species pair (the members
+// np_, ne_, nei_ of PerezIonizationModel): initIonization (:129-137) and
+// prepareNumberDensities (:140-195).
+struct Ionizer {
+    double np = 0.0, ne = 0.0, nei = 0.0;
+    std::vector<Parcel> electrons;   // parcels added by addNewParcel, appended after the step
+};
+
+bool perez_active(const Oracle& o, int s) { return size_t(s) < o.perez.size() && o.perez[s].limit >= 0 && o.perez[s].atomic > 0; }
+
+void perez_init(const Oracle& o, Ionizer& I, int p, int q, double nP, double nQ) {
+    I.ne = 0.0;
+    I.nei = 0.0;
+    if (p == o.cfg.electron_species) I.np = nQ;
+    else if (q == o.cfg.electron_species) I.np = nP;
+}
+
+// the electron's kinetic energy [eV] from its Lorentz factor
+double electron_eV(const Oracle& o, const Parcel& e) {
+    const double m = o.cfg.species[o.cfg.electron_species].mass;
+    const double b = magv(e.U) / kC;
+    const double gamma = 1.0 / std::sqrt(1.0 - b * b);
+    return (gamma - 1.0) * m * kC * kC / ocoll::kEcharge;
+}
+
+void perez_prepare_densities(const Oracle& o, Ionizer& I, const Parcel& P, int sp, const Parcel& Q, int sq) {
+    const int es = o.cfg.electron_species;
+    const Parcel* e;
+    const Parcel* ion;
+    int si;
+    if (sp == es) { e = &P; ion = &Q; si = sq; }
+    else if (sq == es) { e = &Q; ion = &P; si = sp; }
+    else return;
+    if (!perez_active(o, si) || ion->zq >= o.perez[si].limit) return;
+    double x = 6.142165 * std::log(electron_eV(o, *e));
+    if (x < 0.0) x = 0.0;
+    else if (x > 99.0) x = 99.0;
+    const double cs = o.perez[si].cs[size_t(ion->zq) * 100 + size_t(int(x))];
+    if (cs > 0.0) {
+        const double We = pweight(o, *e, es), Wi = pweight(o, *ion, si);
+        I.ne += We;
+        I.nei += We < Wi ? We : Wi;
+    }
+}
+
+// prepareIonization (:198-234): the pair's electron and ion when the ion
+// species ionises, its charge state is below the limit and nei > 0.
+bool perez_prepare(const Oracle& o, const Ionizer& I, int sp, const Parcel& P, int sq, const Parcel& Q) {
+    const int es = o.cfg.electron_species;
+    int si;
+    const Parcel* ion;
+    if (sp == es && perez_active(o, sq)) { si = sq; ion = &Q; }
+    else if (sq == es && perez_active(o, sp)) { si = sp; ion = &P; }
+    else return false;
+    if (ion->zq >= o.perez[si].limit) return false;
+    return I.nei > 0.0;
+}
+
+// ionize (:237-385) for the electron e and ion of species si after their
+// Coulomb collision; random numbers from the stream of the collision
+// ordinal.  Returns whether the charge state rose.
+bool perez_ionize(Oracle& o, Ionizer& I, Parcel& e, Parcel& ion, int si, int cell, long ordinal) {
+    const int es = o.cfg.electron_species;
+    const Oracle::PerezTab& T = o.perez[si];
+    const int atomicNumber = T.atomic;
+    int Zstar = ion.zq;
+    const int initialZstar = Zstar;
+    const double c = kC, c2 = kC * kC;
+    double gammaE = 1.0 / std::sqrt(1.0 - (magv(e.U) / c) * (magv(e.U) / c));
+    const double gammaP = 1.0 / std::sqrt(1.0 - (magv(ion.U) / c) * (magv(ion.U) / c));
+    const double massE = o.cfg.species[es].mass, massP = o.cfg.species[si].mass;
+    const double deltaT = o.cfg.dt;
+    const double wE = pweight(o, e, es), wP = pweight(o, ion, si);
+    const double wEwP = wE / wP;
+    const double wPwE = 1.0 / wEwP;
+    double gamma_s = gammaP * gammaE * (1.0 - magv(ion.U) * magv(e.U) / c2);
+    if (gamma_s <= 1.0) return false;
+    ocoll::Philox r = ocoll::ionize_stream(o.cfg.seed, uint32_t(cell), uint32_t(o.step_index), ordinal);
+    const double ionCoeff_s = c * std::sqrt(gamma_s * gamma_s - 1.0) / gammaP * (I.np * I.ne / I.nei) * deltaT;
+    const double eVkin_s = (gamma_s - 1.0) * massE * c * c / ocoll::kEcharge;
+    const double rndU = r.uniform();
+    const int ionizationMax = T.limit - Zstar - 1;
+    std::vector<double> rate(atomicNumber, 0.0), rate_inv(atomicNumber, 0.0), prop(atomicNumber, 0.0);
+    double com = 0.0;
+    for (int k = 0; k <= ionizationMax; ++k) {
+        const double s = 6.142165 * std::log(eVkin_s);
+        if (s < 0.0) break;
+        const double* cs = &T.cs[size_t(Zstar) * 100];
+        const double* te = &T.te[size_t(Zstar) * 100];
+        const double* le = &T.le[size_t(Zstar) * 100];
+        double crossSection, transferred, lost;
+        if (s < 99.0) {
+            const int l = int(s);
+            const double d = s - double(l);
+            crossSection = (cs[l + 1] - cs[l]) * d + cs[l];
+            transferred = (te[l + 1] - te[l]) * d + te[l];
+            lost = (le[l + 1] - le[l]) * d + le[l];
+        } else {
+            const double d = s - 99.0;
+            crossSection = (cs[99] - cs[98]) * d + cs[99];
+            transferred = te[99];
+            lost = le[99];
+        }
+        if (crossSection <= 0.0) break;
+        if (lost > gamma_s - 1.0) break;
+        rate[k] = ionCoeff_s * crossSection / gammaE;
+        rate_inv[k] = 1.0 / rate[k];
+        prop[k] = std::exp(-rate[k]);
+        if (k == 0) {
+            com = prop[k];
+        } else {
+            for (int x = 0; x < k; ++x) {
+                double cp = 1.0 - rate[k] * rate_inv[x];
+                for (int b = 0; b < x; ++b) cp *= 1.0 - rate[x] * rate_inv[b];
+                for (int b = x + 1; b < k; ++b) cp *= 1.0 - rate[x] * rate_inv[b];
+                if (k < ionizationMax) com += (prop[k] - prop[x]) / cp;
+                else com += (1.0 - prop[k] + rate[k] * rate_inv[x] * (prop[x] - 1.0)) / cp;
+            }
+        }
+        if (rndU < com) break;
+        const V3 pOld = v3(e.U.x * gammaE * massE, e.U.y * gammaE * massE, e.U.z * gammaE * massE);
+        const V3 pI = v3(ion.U.x * gammaP * massP, ion.U.y * gammaP * massP, ion.U.z * gammaP * massP);
+        const double p2 = gamma_s * gamma_s - 1.0;
+        const double rndU2 = r.uniform();
+        if (rndU2 < wEwP) {
+            ion.zq++;
+            const double gammaW = transferred + 1.0;
+            const double alpha_w = std::sqrt((gammaW * gammaW - 1.0) / p2);
+            const double f = gammaW - alpha_w * gamma_s;
+            const V3 pNew = v3(alpha_w * pOld.x + f * pI.x * massE / massP, alpha_w * pOld.y + f * pI.y * massE / massP,
+                               alpha_w * pOld.z + f * pI.z * massE / massP);
+            const double gNew = std::sqrt(1.0 + std::pow(magv(pNew) / (massE * c), 2));
+            Parcel ne = e;
+            ne.nw = wP;
+            ne.zq = 1;
+            ne.U = sdiv(pNew, massE * gNew);
+            I.electrons.push_back(ne);
+        }
+        if (rndU2 < wPwE) {
+            const double alpha_e = std::sqrt((std::pow(gamma_s - lost, 2) - 1.0) / p2);
+            const double f = (1.0 - alpha_e) * gamma_s - lost;
+            const V3 pLost = v3(alpha_e * pOld.x + f * pI.x * massE / massP, alpha_e * pOld.y + f * pI.y * massE / massP,
+                                alpha_e * pOld.z + f * pI.z * massE / massP);
+            const double gLost = std::sqrt(1.0 + std::pow(magv(pLost) / (massE * c), 2));
+            e.U = sdiv(pLost, massE * gLost);
+            gammaE += ((1.0 - alpha_e) * gamma_s - lost) * gammaP;
+            gamma_s -= lost;
+        }
+        Zstar++;
+    }
+    return Zstar != initialZstar;
+}
+
 // One Coulomb collision with the random stream of its ordinal in cell c
-// (ord counts the cell's collisions in the sequential pairing order).
+// (ord counts the cell's collisions in the sequential pairing order); with
+// an ionisation model, prepareIonization before and ionize after it.
 void coulomb_collide(Oracle& o, Parcel& P, int sp, Parcel& Q, int sq, double lD, double nP, double nQ,
-                     double nPQ, int c, long& ord) {
+                     double nPQ, int c, long& ord, Ionizer* I = nullptr, long long* ionized = nullptr) {
+    const long k = ord;
+    const bool ionize = I && perez_prepare(o, *I, sp, P, sq, Q);
     ocoll::Philox r = ocoll::coulomb_pair_stream(o.cfg.seed, uint32_t(c), uint32_t(o.step_index), ord++);
     if (o.cfg.coulomb.collide == 1) perez_collide(o, P, sp, Q, sq, lD, nP, nQ, nPQ, r);
     else nanbu_collide(o, P, sp, Q, sq, lD, nP, nQ, nPQ, r);
+    if (ionize) {
+        const int es = o.cfg.electron_species;
+        const bool pe = sp == es;
+        if (perez_ionize(o, *I, pe ? P : Q, pe ? Q : P, pe ? sq : sp, c, k) && ionized) ++*ionized;
+    }
 }
 
 void shuffle(std::vector<int>& a, ocoll::Philox& r) {
@@ -1575,17 +1825,19 @@ double debye_length(const Oracle& o, const std::vector<int>& charged,
                     std::vector<std::vector<std::vector<int>>>& occ, int c) {
     double debye = 0.0, n_max = 0.0;
     for (int s : charged) {
-        const double mass = o.cfg.species[s].mass, w = o.cfg.species[s].weight, q = o.cfg.species[s].charge;
-        // the per-species sums in the lane order of the device's warp
+        const double mass = o.cfg.species[s].mass;
+        // the per-species sums (CoulombCollisionModel.C:270-277, per parcel
+        // nParticle and charge) in the lane order of the device's warp
         const std::vector<int>& L = occ[s][c];
         const long cnt = long(L.size());
         const auto& cl = o.cloud[s];
-        double vSqr = ocoll::warp_sum(cnt, [&](long t) { return dotv(cl[L[t]].U, cl[L[t]].U) * w; });
-        double charge = ocoll::warp_sum(cnt, [&](long) { return q * w; });
-        V3 v = v3(ocoll::warp_sum(cnt, [&](long t) { return w * cl[L[t]].U.x; }),
-                  ocoll::warp_sum(cnt, [&](long t) { return w * cl[L[t]].U.y; }),
-                  ocoll::warp_sum(cnt, [&](long t) { return w * cl[L[t]].U.z; }));
-        double n = ocoll::warp_sum(cnt, [&](long) { return w; });
+        auto w = [&](long t) { return pweight(o, cl[L[t]], s); };
+        double vSqr = ocoll::warp_sum(cnt, [&](long t) { return dotv(cl[L[t]].U, cl[L[t]].U) * w(t); });
+        double charge = ocoll::warp_sum(cnt, [&](long t) { return pcharge(o, cl[L[t]], s) * w(t); });
+        V3 v = v3(ocoll::warp_sum(cnt, [&](long t) { return w(t) * cl[L[t]].U.x; }),
+                  ocoll::warp_sum(cnt, [&](long t) { return w(t) * cl[L[t]].U.y; }),
+                  ocoll::warp_sum(cnt, [&](long t) { return w(t) * cl[L[t]].U.z; }));
+        double n = ocoll::warp_sum(cnt, [&](long t) { return w(t); });
         if (n <= 0.0) continue;
         v = sdiv(v, n);
         charge /= n;
@@ -1610,7 +1862,9 @@ void coulomb_pairs(Oracle& o, std::vector<std::vector<std::vector<int>>>& occ, p
         if (o.cfg.species[s].charge != 0.0 && o.cfg.species[s].solve_movement) charged.push_back(s);
     const bool ta = o.cfg.coulomb.pairing == 1;
     const bool need_debye = o.cfg.coulomb.coulomb_log == 0.0;
-    long long pairs = 0;
+    long long pairs = 0, ionized = 0;
+    Ionizer ionizer;
+    Ionizer* I = o.cfg.perez.enabled ? &ionizer : nullptr;
     for (int c = 0; c < o.m.n_cells; ++c) {
         const double V = o.m.vol[c];
         // the shuffles draw from the cell's stream in order, each collision
@@ -1625,11 +1879,18 @@ void coulomb_pairs(Oracle& o, std::vector<std::vector<std::vector<int>>>& occ, p
                 std::vector<int>& LA = occ[a][c];
                 std::vector<int>& LB = occ[b][c];
                 const long nA = long(LA.size()), nB = long(LB.size());
-                const double wA = o.cfg.species[a].weight, wB = o.cfg.species[b].weight;
-                const double sA = double(nA) * wA;
-                const double sB = a != b ? double(nB) * wB : 0.0;
+                const double wA = o.cfg.species[a].weight;
                 auto& ca = o.cloud[a];
                 auto& cb = o.cloud[b];
+                // NanbuYonemuraPairing.C:96-113: the real particles of each
+                // species, parcel by parcel
+                double sA = 0.0, sB = 0.0;
+                for (long t = 0; t < nA; ++t) sA += pweight(o, ca[LA[t]], a);
+                if (a != b)
+                    for (long t = 0; t < nB; ++t) sB += pweight(o, cb[LB[t]], b);
+                auto pw = [&](const std::vector<Parcel>& cl, const std::vector<int>& L, int k, int sp) {
+                    return pweight(o, cl[L[k]], sp);
+                };
                 if (a == b && nA > 1) {
                     if (!o.cfg.coulomb.allow_intra) continue;
                     std::vector<int> sel(nA);
@@ -1657,8 +1918,11 @@ void coulomb_pairs(Oracle& o, std::vector<std::vector<std::vector<int>>>& occ, p
                     }
                     const double n = sA / V;
                     if (nA % 2 != 0) {
-                        double nAA = 2.0 * wA;  // the extra (last, first) pair
-                        for (long x = 0; x < nA - 2; x += 2) nAA += 2.0 * wA;
+                        // the extra (last, first) pair first (NanbuYonemuraPairing.C:128-141)
+                        double nAA = 0.0;
+                        nAA += 2.0 * std::fmin(pw(ca, LA, sel[nA - 1], a), pw(ca, LA, sel[0], a));
+                        for (long x = 0; x < nA - 2; x += 2)
+                            nAA += 2.0 * std::fmin(pw(ca, LA, sel[x], a), pw(ca, LA, sel[x + 1], a));
                         const double n12 = nAA / V;
                         for (long x = 0; x < nA - 2; x += 2)
                             coulomb_collide(o, ca[LA[sel[x]]], a, ca[LA[sel[x + 1]]], a, lD, n, n, n12, c, ord);
@@ -1666,14 +1930,14 @@ void coulomb_pairs(Oracle& o, std::vector<std::vector<std::vector<int>>>& occ, p
                         pairs += 1 + nA / 2;
                     } else {
                         double nAA = 0.0;
-                        for (long x = 0; x < nA - 1; x += 2) nAA += 2.0 * wA;
+                        for (long x = 0; x < nA - 1; x += 2)
+                            nAA += 2.0 * std::fmin(pw(ca, LA, sel[x], a), pw(ca, LA, sel[x + 1], a));
                         const double n12 = nAA / V;
                         for (long x = 0; x < nA - 1; x += 2)
                             coulomb_collide(o, ca[LA[sel[x]]], a, ca[LA[sel[x + 1]]], a, lD, n, n, n12, c, ord);
                         pairs += nA / 2;
                     }
                 } else if (a != b && std::min(nA, nB) != 0) {
-                    const double wmin = std::fmin(wA, wB);
                     if (nA == nB) {
                         std::vector<int> sel(nA);
                         for (long k = 0; k < nA; ++k) sel[k] = int(k);
@@ -1686,12 +1950,19 @@ void coulomb_pairs(Oracle& o, std::vector<std::vector<std::vector<int>>>& occ, p
                         } else {
                             nP = sA / V;
                             nQ = sB / V;
-                            double nAB = 0.0;
-                            for (long k = 0; k < nA; ++k) nAB += wmin;
-                            nPQ = nAB / V;
                         }
+                        // initIonization + prepareNumberDensities over the pairs
+                        // (NanbuYonemuraPairing.C:198-208, TakizukaAbePairing.C:165-180)
+                        if (I) perez_init(o, *I, a, b, nP, nQ);
+                        double nAB = 0.0;
+                        for (long k = 0; k < nA; ++k) {
+                            if (!ta) nAB += std::fmin(pw(ca, LA, sel[k], a), pw(cb, LB, sel[nA - k - 1], b));
+                            if (I) perez_prepare_densities(o, *I, ca[LA[sel[k]]], a, cb[LB[sel[nA - k - 1]]], b);
+                        }
+                        if (!ta) nPQ = nAB / V;
                         for (long k = 0; k < nA; ++k)
-                            coulomb_collide(o, ca[LA[sel[k]]], a, cb[LB[sel[nA - k - 1]]], b, lD, nP, nQ, nPQ, c, ord);
+                            coulomb_collide(o, ca[LA[sel[k]]], a, cb[LB[sel[nA - k - 1]]], b, lD, nP, nQ, nPQ, c, ord,
+                                            I, &ionized);
                         pairs += nA;
                     } else {
                         const int minS = nA < nB ? a : b, maxS = nA > nB ? a : b;
@@ -1714,12 +1985,28 @@ void coulomb_pairs(Oracle& o, std::vector<std::vector<std::vector<int>>>& occ, p
                             const long g2max = long(double(delta) * (1.0 - delta_r) * double(nMin));
                             long s1 = 0, s2 = 0;
                             if (g1min > 0) {
+                                if (I) {
+                                    perez_init(o, *I, minS, maxS, nMinS, nMaxS);
+                                    for (long g = 0, q1 = 0; g < g1max; ++g, ++q1) {
+                                        if (q1 >= g1min) q1 = 0;
+                                        perez_prepare_densities(o, *I, cmin[Lmin[smin[q1]]], minS, cmax[Lmax[smax[g]]],
+                                                                maxS);
+                                    }
+                                }
                                 for (long g = 0; g < g1max; ++g) {
                                     if (s1 >= g1min) s1 = 0;
                                     coulomb_collide(o, cmax[Lmax[smax[s2]]], maxS, cmin[Lmin[smin[s1]]], minS, lD, nMaxS,
-                                                    nMinS, nMaxS, c, ord);
+                                                    nMinS, nMaxS, c, ord, I, &ionized);
                                     ++s1;
                                     ++s2;
+                                }
+                            }
+                            if (I) {
+                                perez_init(o, *I, minS, maxS, nMinS, nMaxS);
+                                for (long g = 0, q1 = g1min; g < g2max; ++g, ++q1) {
+                                    if (q1 >= g2min + g1min) q1 = g1min;
+                                    perez_prepare_densities(o, *I, cmin[Lmin[smin[q1]]], minS, cmax[Lmax[smax[g1max + g]]],
+                                                            maxS);
                                 }
                             }
                             s1 = g1min;
@@ -1727,7 +2014,7 @@ void coulomb_pairs(Oracle& o, std::vector<std::vector<std::vector<int>>>& occ, p
                             for (long g = 0; g < g2max; ++g) {
                                 if (s1 >= g2min + g1min) s1 = g1min;
                                 coulomb_collide(o, cmax[Lmax[smax[s2]]], maxS, cmin[Lmin[smin[s1]]], minS, lD, nMaxS,
-                                                nMinS, nMaxS, c, ord);
+                                                nMinS, nMaxS, c, ord, I, &ionized);
                                 ++s1;
                                 ++s2;
                             }
@@ -1736,14 +2023,19 @@ void coulomb_pairs(Oracle& o, std::vector<std::vector<std::vector<int>>>& occ, p
                         }
                         const double nMaxS = (maxS == a ? sA : sB) / V;
                         const double nMinS = (maxS == a ? sB : sA) / V;
+                        if (I) perez_init(o, *I, minS, maxS, nMinS, nMaxS);
                         double nAB = 0.0;
-                        for (long l = 0; l < nMax; ++l) nAB += wmin;
+                        for (long l = 0, k = 0; l < nMax; ++l, ++k) {
+                            if (k >= nMin) k = 0;
+                            nAB += std::fmin(pw(cmin, Lmin, smin[k], minS), pw(cmax, Lmax, smax[l], maxS));
+                            if (I) perez_prepare_densities(o, *I, cmin[Lmin[smin[k]]], minS, cmax[Lmax[smax[l]]], maxS);
+                        }
                         const double n12 = nAB / V;
                         long k = 0;
                         for (long l = 0; l < nMax; ++l) {
                             if (k >= nMin) k = 0;
                             coulomb_collide(o, cmax[Lmax[smax[l]]], maxS, cmin[Lmin[smin[k]]], minS, lD, nMaxS, nMinS,
-                                            n12, c, ord);
+                                            n12, c, ord, I, &ionized);
                             ++k;
                         }
                         pairs += nMax;
@@ -1752,7 +2044,15 @@ void coulomb_pairs(Oracle& o, std::vector<std::vector<std::vector<int>>>& occ, p
             }
         }
     }
-    if (st) st->coulomb_pairs += pairs;
+    if (st) {
+        st->coulomb_pairs += pairs;
+        st->coulomb_ionizations += ionized;
+        st->coulomb_ionization_electrons += (long long)ionizer.electrons.size();
+    }
+    // the electrons added by ionisations join the cloud after the step
+    // (addNewParcel; not in this step's cell lists)
+    if (I)
+        for (const Parcel& p : ionizer.electrons) o.cloud[o.cfg.electron_species].push_back(p);
 }
 
 // PICCloud::buildCellOccupancy (PICCloud.C:327-354) + collisions() (PICCloud.C:526-539):
@@ -1952,6 +2252,126 @@ void collisions(Oracle& o, picgpu_step_stats* st) {
     if (o.cfg.ion_mcc.enabled && o.cfg.ion_mcc.neutral_parcels) ion_parcels(o, occ, st);
     if (o.cfg.ion_mcc.enabled) ion_mcc_background(o, occ[o.cfg.ion_mcc.ion_species], st);
     if (o.cfg.binary.enabled) binary_collisions(o, occ, st);
+}
+
+
+// PairMerging::mergeParticles (PIC/submodels/ParticleMerging/PairMerging/
+// PairMerging.C:71-259), cell by cell for each listed species, over the
+// parcels of the step's cell occupancy.  Kept as picFoam has it: the speeds
+// in the acceptance tests are those of the LIST positions pId1 / pId2 (not
+// of the parcels they select, and not shifted after a merge), a pair whose
+// velocities are closer in angle than angleDifference is rejected, and the
+// merged parcel (addNewParcel) gets charge modifier 1.  The speed order is
+// made total by the list position (std::sort's order of equal speeds is
+// unspecified); the parcel draw sampleAB(0, N) takes floor(u N) from the
+// stream (seed, merge-list entry, cell, step).
+void merge_parcels(Oracle& o, picgpu_step_stats* st) {
+    const picgpu_merging& mg = o.cfg.merging;
+    const double cos_angle = std::cos(mg.angle_difference * kPi / 180.0);
+    long long merged_total = 0, checked_total = 0;
+    double kin_total = 0.0;
+    for (int li = 0; li < mg.n_species; ++li) {
+        const int s = mg.species[li];
+        auto& cl = o.cloud[s];
+        const double wS = o.cfg.species[s].weight, mass = o.cfg.species[s].mass;
+        const long nocc = std::min<long>(size_t(s) < o.occ_n.size() ? o.occ_n[s] : 0, long(cl.size()));
+        std::vector<std::vector<int>> occ(o.m.n_cells);
+        for (long i = 0; i < nocc; ++i) occ[cl[i].cell].push_back(int(i));
+        std::vector<char> dead(cl.size(), 0);
+        std::vector<Parcel> added;
+        auto pw = [&](int i) { return cl[i].nw < 0.0 ? wS : cl[i].nw; };
+        for (int c = 0; c < o.m.n_cells; ++c) {
+            const std::vector<int>& L = occ[c];
+            int N = int(L.size());
+            if (N <= mg.cell_parcels_max) continue;
+            int nTarget = int(double(N) * mg.reduction_factor);
+            if (N - nTarget > mg.merge_maximum_per_cell) nTarget = N - mg.merge_maximum_per_cell;
+            std::vector<double> speed(N);
+            std::vector<int> sel(N);
+            for (int k = 0; k < N; ++k) {
+                speed[k] = magv(cl[L[k]].U);
+                sel[k] = k;
+            }
+            std::sort(sel.begin(), sel.end(),
+                      [&](int a, int b) { return speed[a] < speed[b] || (speed[a] == speed[b] && a < b); });
+            ocoll::Philox rng(o.cfg.seed, ocoll::kStreamMerge | uint32_t(li), uint32_t(c), uint32_t(o.step_index));
+            int checks = 0;
+            while (N > nTarget) {
+                int pId1 = int(rng.uniform() * double(N));
+                if (pId1 >= N) pId1 = N - 1;
+                const int i1 = L[sel[pId1]];
+                int pId2 = pId1 - mg.n_check_neighbors / 2;
+                if (pId2 < 0) pId2 = 0;
+                if (pId2 + mg.n_check_neighbors > N - 1) pId2 = N - mg.n_check_neighbors - 1;
+                if (pId2 < 0) pId2 = 0;
+                int found = -1;
+                for (int k = 0; k < mg.n_check_neighbors; ++k) {
+                    if (pId2 == pId1) pId2++;
+                    if (pId2 >= N) break;
+                    const int i2 = L[sel[pId2]];
+                    checked_total++;
+                    if (mg.n_deviation[li] - std::fabs(pw(i2) - pw(i1)) < 0.0) { pId2++; continue; }
+                    if (cl[i2].zq != cl[i1].zq) { pId2++; continue; }
+                    const V3 U1 = cl[i1].U, U2 = cl[i2].U;
+                    if (U2.x * U1.x + U2.y * U1.y + U2.z * U1.z > speed[pId2] * speed[pId1] * cos_angle) {
+                        pId2++;
+                        continue;
+                    }
+                    double ratio = speed[pId2] / speed[pId1];
+                    if (ratio > 1.0) ratio = 1.0 / ratio;
+                    if (ratio < mg.velocity_ratio) { pId2++; continue; }
+                    found = pId2;
+                    break;
+                }
+                if (found >= 0) {
+                    pId2 = found;
+                    const int i2 = L[sel[pId2]];
+                    const double n1 = pw(i1), n2 = pw(i2), nSum = n1 + n2;
+                    const V3 x1 = position_of(o, cl[i1]), x2 = position_of(o, cl[i2]);
+                    const V3 U1 = cl[i1].U, U2 = cl[i2].U;
+                    const double com[3] = {(n1 * x1.x + n2 * x2.x) / nSum, (n1 * x1.y + n2 * x2.y) / nSum,
+                                           (n1 * x1.z + n2 * x2.z) / nSum};
+                    const V3 nU = v3((n1 * U1.x + n2 * U2.x) / nSum, (n1 * U1.y + n2 * U2.y) / nSum,
+                                     (n1 * U1.z + n2 * U2.z) / nSum);
+                    const double pre = 0.5 * mass *
+                                       ((U1.x * U1.x + U1.y * U1.y + U1.z * U1.z) * n1 +
+                                        (U2.x * U2.x + U2.y * U2.y + U2.z * U2.z) * n2);
+                    const double post = 0.5 * mass * (nU.x * nU.x + nU.y * nU.y + nU.z * nU.z) * nSum;
+                    kin_total += post - pre;
+                    Parcel p;
+                    double y[3];
+                    const long long tg = om::locate_in_cell(o.m, c, com, y);
+                    p.cell = int(tg / 12);
+                    p.tet = int(tg % 12);
+                    p.y[1] = y[0];
+                    p.y[2] = y[1];
+                    p.y[3] = y[2];
+                    p.y[0] = 1.0 - y[0] - y[1] - y[2];
+                    p.U = nU;
+                    p.nw = nSum;
+                    p.zq = 1;
+                    added.push_back(p);
+                    dead[i1] = dead[i2] = 1;
+                    merged_total++;
+                    const int minPos = std::min(pId1, pId2), maxPos = std::max(pId1, pId2);
+                    for (int k = minPos; k < N - 2; ++k) sel[k] = k >= maxPos - 1 ? sel[k + 2] : sel[k + 1];
+                    N -= 2;
+                }
+                checks++;
+                if (checks > mg.max_checks) break;
+            }
+        }
+        size_t w = 0;
+        for (size_t i = 0; i < cl.size(); ++i)
+            if (!dead[i]) cl[w++] = cl[i];
+        cl.resize(w);
+        for (const Parcel& p : added) cl.push_back(p);
+    }
+    if (st) {
+        st->merged_parcels += merged_total;
+        st->merge_checks += checked_total;
+        st->merge_kinetic_energy_error += kin_total;
+    }
 }
 
 void fill_counts(const Oracle& o, picgpu_step_stats* st) {
@@ -2800,6 +3220,40 @@ int oracle_create(const picgpu_mesh_desc* mesh, const picgpu_config* cfg, int nt
             }
         }
     }
+    o.perez.assign(size_t(cfg->n_species), Oracle::PerezTab{});
+    if (cfg->perez.enabled) {
+        // PerezIonizationModel.C:30-118: one entry per ion species; a limit
+        // below 1 switches the species off
+        const picgpu_perez& pz = cfg->perez;
+        const int es = cfg->electron_species;
+        bool okp = cfg->coulomb.enabled && es >= 0 && es < cfg->n_species && cfg->species[es].charge != 0.0 &&
+                   pz.n_ions >= 0 && pz.n_ions <= PICGPU_PEREZ_MAX_IONS;
+        for (int k = 0; okp && k < pz.n_ions; ++k) {
+            const picgpu_perez_ion& in = pz.ion[k];
+            okp = in.species >= 0 && in.species < cfg->n_species && in.species != es && in.atomic_number >= 1 &&
+                  in.atomic_number <= PICGPU_PEREZ_MAX_Z;
+            if (okp && in.ionization_limit != 0) o.perez[size_t(in.species)] = perez_tables(in);
+        }
+        if (!okp) {
+            o.err = "Perez ionisation: bad settings";
+            *out = c;
+            return PICGPU_INVALID_ARG;
+        }
+    }
+    if (cfg->merging.enabled) {
+        // PairMerging.C:35-68: the settings and the species list
+        const picgpu_merging& mg = cfg->merging;
+        bool okm = mg.n_species >= 1 && mg.n_species <= PICGPU_MAX_SPECIES && mg.n_check_neighbors >= 1 &&
+                   mg.reduction_factor > 0.0 && mg.reduction_factor <= 1.0 && mg.cell_parcels_max >= 1 &&
+                   mg.max_checks >= 0 && mg.merge_maximum_per_cell >= 0 && mg.velocity_ratio >= 0.0 &&
+                   double(mg.cell_parcels_max) * mg.reduction_factor >= double(mg.n_check_neighbors);
+        for (int k = 0; okm && k < mg.n_species; ++k) okm = mg.species[k] >= 0 && mg.species[k] < cfg->n_species;
+        if (!okm) {
+            o.err = "PairMerging: bad settings";
+            *out = c;
+            return PICGPU_INVALID_ARG;
+        }
+    }
     if (cfg->coulomb.enabled && cfg->coulomb.pairing == 1) {
         double w = -1.0;
         for (int s = 0; s < cfg->n_species; ++s) {
@@ -2850,6 +3304,38 @@ int oracle_set_particles(oracle_ctx* ctx, int species, size_t n, const int32_t* 
         p.y[3] = bary[3 * i + 2];
         p.y[0] = 1.0 - p.y[1] - p.y[2] - p.y[3];
         p.U = v3(U[3 * i], U[3 * i + 1], U[3 * i + 2]);
+    }
+    return 0;
+}
+
+int oracle_set_parcel_attributes(oracle_ctx* ctx, int species, size_t n, const double* nParticle,
+                                 const int32_t* chargeModifier) {
+    Oracle& o = ctx->o;
+    if (species < 0 || species >= o.cfg.n_species) return PICGPU_INVALID_ARG;
+    auto& cl = o.cloud[species];
+    if (n != cl.size() || (n && (!nParticle || !chargeModifier))) return PICGPU_INVALID_ARG;
+    const double w = o.cfg.species[species].weight;
+    for (size_t i = 0; i < n; ++i)
+        if (!(nParticle[i] > 0.0) || !(nParticle[i] <= 4096.0 * w) || chargeModifier[i] < 0 || chargeModifier[i] > 1024)
+            return PICGPU_INVALID_ARG;
+    for (size_t i = 0; i < n; ++i) {
+        cl[i].nw = nParticle[i];
+        cl[i].zq = chargeModifier[i];
+    }
+    return 0;
+}
+
+int oracle_get_parcel_attributes(oracle_ctx* ctx, int species, size_t cap, double* nParticle,
+                                 int32_t* chargeModifier, size_t* n) {
+    Oracle& o = ctx->o;
+    if (species < 0 || species >= o.cfg.n_species) return PICGPU_INVALID_ARG;
+    const auto& cl = o.cloud[species];
+    *n = cl.size();
+    if (!nParticle) return 0;
+    if (cap < cl.size() || !chargeModifier) return PICGPU_INVALID_ARG;
+    for (size_t i = 0; i < cl.size(); ++i) {
+        nParticle[i] = pweight(o, cl[i], species);
+        chargeModifier[i] = cl[i].zq;
     }
     return 0;
 }
@@ -2985,6 +3471,8 @@ int oracle_step(oracle_ctx* ctx, int nsteps, picgpu_step_stats* st) {
         inject(o);
         int s = move_all(o, st);
         if (s) return s;
+        o.occ_n.assign(o.cloud.size(), 0);
+        for (size_t q = 0; q < o.cloud.size(); ++q) o.occ_n[q] = long(o.cloud[q].size());
         collisions(o, st);
         calculate_fields(o);
         floating_pre_update(o);
@@ -2992,6 +3480,8 @@ int oracle_step(oracle_ctx* ctx, int nsteps, picgpu_step_stats* st) {
         s = solve_fields(o, st);
         if (s) status = s;
         circuit_post_update(o);
+        // ParticleMerging::checkAndMerge, the last call of the step (PICCloud.C:1470)
+        if (o.cfg.merging.enabled) merge_parcels(o, st);
         o.step_index++;
     }
     fill_counts(o, st);
@@ -3010,6 +3500,12 @@ int oracle_solve_poisson(oracle_ctx* ctx, const double* rho, double* phi_inout,
     o.cfg.maxwell_solver = saved;
     std::copy(o.phi.begin(), o.phi.end(), phi_inout);
     return s;
+}
+
+int oracle_compute_field(oracle_ctx* ctx) {
+    if (!ctx) return PICGPU_INVALID_ARG;
+    if (ctx->o.cfg.maxwell_solver == PICGPU_MAXWELL_ELECTROSTATIC) compute_E(ctx->o);
+    return 0;
 }
 
 int oracle_set_step_index(oracle_ctx* ctx, int64_t steps_done) {
@@ -3083,8 +3579,9 @@ int oracle_diagnostics(oracle_ctx* ctx, picgpu_diagnostics* out) {
     Oracle& o = ctx->o;
     std::memset(out, 0, sizeof *out);
     for (size_t s = 0; s < o.cloud.size(); ++s) {
-        const double m = o.cfg.species[s].mass, w = o.cfg.species[s].weight;
+        const double m = o.cfg.species[s].mass;
         for (const Parcel& p : o.cloud[s]) {
+            const double w = pweight(o, p, int(s));
             const double u2 = dotv(p.U, p.U);
             out->kinetic_energy[s] += 0.5 * m * u2 * w;
             const double b = magv(p.U) / kC;

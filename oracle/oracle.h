@@ -40,8 +40,13 @@ int  oracle_set_precond(oracle_ctx* ctx, int precond);
 int  oracle_mesh_query(const oracle_ctx* ctx, picgpu_mesh_info* info);
 int  oracle_mesh_selfcheck(const picgpu_mesh_desc* desc, double* out, int n_out);
 int  oracle_set_step_index(oracle_ctx* ctx, int64_t steps_done);
+int  oracle_compute_field(oracle_ctx* ctx);
 int  oracle_set_particles(oracle_ctx* ctx, int species, size_t n, const int32_t* tet,
                           const double* bary, const double* U);
+int  oracle_set_parcel_attributes(oracle_ctx* ctx, int species, size_t n, const double* nParticle,
+                                  const int32_t* chargeModifier);
+int  oracle_get_parcel_attributes(oracle_ctx* ctx, int species, size_t cap, double* nParticle,
+                                  int32_t* chargeModifier, size_t* n);
 int  oracle_count_particles(oracle_ctx* ctx, int species, size_t* n);
 int  oracle_get_particles(oracle_ctx* ctx, int species, size_t cap, int32_t* tet,
                           double* bary, double* U, size_t* n);

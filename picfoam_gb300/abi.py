@@ -151,6 +151,31 @@ class Multigrid(C.Structure):
     ]
 
 
+class Merging(C.Structure):
+    _fields_ = [
+        ("enabled", C.c_int32), ("n_species", C.c_int32), ("species", C.c_int32 * MAX_SPECIES),
+        ("n_deviation", C.c_double * MAX_SPECIES), ("reduction_factor", C.c_double),
+        ("angle_difference", C.c_double), ("velocity_ratio", C.c_double),
+        ("cell_parcels_max", C.c_int32), ("max_checks", C.c_int32), ("n_check_neighbors", C.c_int32),
+        ("merge_maximum_per_cell", C.c_int32),
+    ]
+
+
+PEREZ_MAX_Z = 64
+PEREZ_MAX_IONS = 4
+
+
+class PerezIon(C.Structure):
+    _fields_ = [
+        ("species", C.c_int32), ("atomic_number", C.c_int32), ("ionization_limit", C.c_int32), ("pad", C.c_int32),
+        ("binding_energy", C.c_double * PEREZ_MAX_Z), ("ionization_energy", C.c_double * PEREZ_MAX_Z),
+    ]
+
+
+class Perez(C.Structure):
+    _fields_ = [("enabled", C.c_int32), ("n_ions", C.c_int32), ("ion", PerezIon * PEREZ_MAX_IONS)]
+
+
 class Config(C.Structure):
     _fields_ = [
         ("pusher", C.c_int32), ("field_weighting", C.c_int32),
@@ -165,7 +190,7 @@ class Config(C.Structure):
         ("sort_interval", C.c_int32), ("pcg_precond", C.c_int32),
         ("seed", C.c_uint64),
         ("mcc", Mcc), ("ion_mcc", IonMcc), ("coulomb", Coulomb), ("learned", Learned),
-        ("mg", Multigrid), ("binary", Binary), ("circuit", Circuit),
+        ("mg", Multigrid), ("binary", Binary), ("circuit", Circuit), ("merging", Merging), ("perez", Perez),
     ]
 
 
@@ -261,6 +286,8 @@ class StepStats(C.Structure):
         ("mcc_parcel_excitation", C.c_int64), ("mcc_parcel_ionization", C.c_int64),
         ("ion_parcel_candidates", C.c_int64), ("ion_parcel_elastic", C.c_int64),
         ("ion_parcel_charge_exchange", C.c_int64),
+        ("merged_parcels", C.c_int64), ("merge_checks", C.c_int64), ("merge_kinetic_energy_error", C.c_double),
+        ("coulomb_ionizations", C.c_int64), ("coulomb_ionization_electrons", C.c_int64),
     ]
 
     def as_dict(self):

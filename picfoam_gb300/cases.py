@@ -16,6 +16,7 @@ benchmark configurations of the particle hot path (seeded synthetic inputs):
   swarm_ensemble          64 swarm cases of 16x16x128 cells, 10-1000 Td, 1e5-4e6 e- each
   electrode_box           128^3 cells, two floating boxes, one 100 V box
 """
+import ctypes as C
 import dataclasses
 import math
 
@@ -678,6 +679,85 @@ def emission(patch, model, work_function, temperature=0.0, lambda_r=0.5, weight=
     q.lambda_r = lambda_r
     q.weight = weight
     return q
+
+
+def set_merging(cfg, species, cell_parcels_max=20, reduction_factor=0.7, max_checks=200, n_check_neighbors=4,
+                angle_difference=30.0, velocity_ratio=0.5, n_deviation=None, merge_maximum_per_cell=100):
+    """ParticleMerging PairMerging dictionary (PairMerging.C:35-68):
+    species in merge order, nDeviation per listed species (default: 10
+    species weights)."""
+    mg = cfg.merging
+    mg.enabled = 1
+    mg.n_species = len(species)
+    for k, s in enumerate(species):
+        mg.species[k] = s
+        mg.n_deviation[k] = (n_deviation[k] if n_deviation is not None else 10.0 * cfg.species[s].weight)
+    mg.reduction_factor = reduction_factor
+    mg.angle_difference = angle_difference
+    mg.velocity_ratio = velocity_ratio
+    mg.cell_parcels_max = cell_parcels_max
+    mg.max_checks = max_checks
+    mg.n_check_neighbors = n_check_neighbors
+    mg.merge_maximum_per_cell = merge_maximum_per_cell
+
+
+def merging_plasma(n_cells=4, e_per_cell=40, i_per_cell=30, n=1e15, T_e=2.0, T_i=0.5, L=4e-4, seed=1234,
+                   precision=abi.PREC_FP64, dt_factor=0.05, ragged=True, **merge):
+    """Electrons and Ar+ in a periodic box with the field solve and
+    PairMerging of both species; ragged gives the cells 1/4 to 7/4 of the
+    mean count, so some cells stay under cellParcelsMax."""
+    sides = [patch(abi.PATCH_CYCLIC) for _ in range(6)]
+    mesh = block_mesh((n_cells,) * 3, (L,) * 3, sides)
+    n_c = n_cells ** 3
+    rng = np.random.Generator(np.random.Philox(seed))
+    parts = {}
+    counts = []
+    for s, (per, T, mass) in enumerate([(e_per_cell, T_e, M_E), (i_per_cell, T_i, M_AR)]):
+        if ragged:
+            cnt = np.maximum(1, (per * (0.25 + 1.5 * rng.random(n_c))).astype(int))
+        else:
+            cnt = np.full(n_c, per)
+        cells = np.repeat(np.arange(n_c), cnt)
+        tet = (12 * cells + rng.integers(0, 12, cells.shape[0])).astype(np.int32)
+        b = rng.random((cells.shape[0], 4))
+        b /= b.sum(axis=1, keepdims=True)
+        parts[s] = (tet, np.ascontiguousarray(b[:, 1:]), maxwellian(rng, cells.shape[0], T, mass))
+        counts.append(cells.shape[0])
+    w = n * L ** 3 / counts[0]
+    wpe = plasma_frequency(n)
+    cfg = base_config(dt_factor / wpe, [(M_E, -E_CHARGE, w, True), (M_AR, E_CHARGE, w, True)],
+                      precision=precision, deposit=abi.DEPOSIT_FIXED_POINT, seed=seed)
+    cfg.sort_interval = 0
+    set_merging(cfg, [0, 1], **merge)
+    return Case("merging_plasma", mesh, cfg, parts, [], dict(counts=counts, weight=w))
+
+
+def perez_plasma(perez, n_cells=4, e_per_cell=40, i_per_cell=40, n=1e27, T_e=400.0, T_i=1.0, L=2e-8, seed=1234,
+                 precision=abi.PREC_FP64, dt=5e-15, collide=abi.COLLIDE_NANBU, w_i_factor=1.0, ragged=True):
+    """Hot electrons (T_e in eV) and Ar+ in a periodic box without a field
+    solve: Coulomb collisions (NanbuYonemura pairing) with the Perez
+    ionisation model `perez` (an abi.Perez for species e = 0, ion = 1; the
+    thermalization tutorial's argon coefficients, for instance)."""
+    sides = [patch(abi.PATCH_CYCLIC) for _ in range(6)]
+    mesh = block_mesh((n_cells,) * 3, (L,) * 3, sides)
+    n_c = n_cells ** 3
+    rng = np.random.Generator(np.random.Philox(seed))
+    parts = {}
+    counts = []
+    for s, (per, T, mass) in enumerate([(e_per_cell, T_e, M_E), (i_per_cell, T_i, M_AR)]):
+        cnt = (np.maximum(1, (per * (0.25 + 1.5 * rng.random(n_c))).astype(int)) if ragged else np.full(n_c, per))
+        cells = np.repeat(np.arange(n_c), cnt)
+        tet = (12 * cells + rng.integers(0, 12, cells.shape[0])).astype(np.int32)
+        b = rng.random((cells.shape[0], 4))
+        b /= b.sum(axis=1, keepdims=True)
+        parts[s] = (tet, np.ascontiguousarray(b[:, 1:]), maxwellian(rng, cells.shape[0], T, mass))
+        counts.append(cells.shape[0])
+    w = n * L ** 3 / counts[0]
+    cfg = base_config(dt, [(M_E, -E_CHARGE, w, True), (M_AR, E_CHARGE, w * w_i_factor, True)],
+                      maxwell=abi.MAXWELL_NONE, precision=precision, seed=seed)
+    set_coulomb(cfg, collide=collide, coulomb_log=10.0)
+    C.memmove(C.addressof(cfg.perez), C.addressof(perez), C.sizeof(abi.Perez))
+    return Case("perez_plasma", mesh, cfg, parts, [], dict(counts=counts, weight=w))
 
 
 def empty_case(n_cells=(8, 8, 8), length=(0.01, 0.01, 0.01), sides=None, boxes=(), species=None,

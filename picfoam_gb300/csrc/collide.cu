@@ -859,6 +859,15 @@ struct CoulombSpecies {
     DSpecies p[PICGPU_MAX_SPECIES];
 };
 
+// A parcel's nParticle and charge (species charge x chargeModifier,
+// PICCloud.C:368): per parcel when the store has the arrays.
+__device__ __forceinline__ double pweight(const CoulombSpecies& C, int k, int i) {
+    return C.p[k].nw ? C.p[k].nw[i] : C.w[k];
+}
+__device__ __forceinline__ double pcharge(const CoulombSpecies& C, int k, int i) {
+    return C.p[k].zq ? C.q[k] * double(C.p[k].zq[i]) : C.q[k];
+}
+
 __device__ double cos_chi(double s, Rng& r) {
     double U = r.uniform();
     if (s < 0.1) {
@@ -971,19 +980,20 @@ __device__ void weight_correct_pair(int model, double wP, double wQ, double mP, 
 // WeightCorrection (CoulombCollisionModel): none, Nanbu
 // (NanbuCorrection.C:50-66), SentokuKempNR, SentokuKemp.
 __device__ __forceinline__ void weight_correct(const CoulombSpecies& C, const CoulombParams& K, int a, int b,
-                                               V3d preP, V3d preQ, V3d& UP, V3d& UQ, Rng& r) {
+                                               double wP, double wQ, V3d preP, V3d preQ, V3d& UP, V3d& UQ,
+                                               Rng& r) {
     if (K.weight_corr == 1) {
         const double u = r.uniform();
-        if (u > C.w[a] / C.w[b]) UQ = preQ;
-        if (u > C.w[b] / C.w[a]) UP = preP;
+        if (u > wP / wQ) UQ = preQ;
+        if (u > wQ / wP) UP = preP;
     } else if (K.weight_corr == 2 || K.weight_corr == 3) {
         const bool rel = K.weight_corr == 3;
-        if (C.w[a] > C.w[b]) {
-            if (rel) sentoku_kemp(C.m[a], C.w[b] / C.w[a], preP, UP, r);
-            else sentoku_kemp_nr(C.m[a], C.w[b] / C.w[a], preP, UP, r);
-        } else if (C.w[a] < C.w[b]) {
-            if (rel) sentoku_kemp(C.m[b], C.w[a] / C.w[b], preQ, UQ, r);
-            else sentoku_kemp_nr(C.m[b], C.w[a] / C.w[b], preQ, UQ, r);
+        if (wP > wQ) {
+            if (rel) sentoku_kemp(C.m[a], wQ / wP, preP, UP, r);
+            else sentoku_kemp_nr(C.m[a], wQ / wP, preP, UP, r);
+        } else if (wP < wQ) {
+            if (rel) sentoku_kemp(C.m[b], wP / wQ, preQ, UQ, r);
+            else sentoku_kemp_nr(C.m[b], wP / wQ, preQ, UQ, r);
         }
     }
 }
@@ -991,7 +1001,7 @@ __device__ __forceinline__ void weight_correct(const CoulombSpecies& C, const Co
 template <class R>
 __device__ void nanbu_collide(const CoulombSpecies& C, const CoulombParams& K, int a, int ia, int b, int ib,
                               double lD, double nP, double nQ, double nPQ, Rng& r) {
-    const double mP = C.m[a], qP = C.q[a], mQ = C.m[b], qQ = C.q[b];
+    const double mP = C.m[a], qP = pcharge(C, a, ia), mQ = C.m[b], qQ = pcharge(C, b, ib);
     V3d UP = Vel<R>::get(C.p[a], ia), UQ = Vel<R>::get(C.p[b], ib);
     const double reMass = mP * mQ / (mP + mQ);
     const V3d g = {UP.x - UQ.x, UP.y - UQ.y, UP.z - UQ.z};
@@ -1015,7 +1025,7 @@ __device__ void nanbu_collide(const CoulombSpecies& C, const CoulombParams& K, i
     const double kp = mQ / (mP + mQ), kq = mP / (mP + mQ);
     V3d nUP = {UP.x - kp * d.x, UP.y - kp * d.y, UP.z - kp * d.z};
     V3d nUQ = {UQ.x + kq * d.x, UQ.y + kq * d.y, UQ.z + kq * d.z};
-    weight_correct(C, K, a, b, UP, UQ, nUP, nUQ, r);
+    weight_correct(C, K, a, b, pweight(C, a, ia), pweight(C, b, ib), UP, UQ, nUP, nUQ, r);
     Vel<R>::put(C.p[a], ia, nUP);
     Vel<R>::put(C.p[b], ib, nUQ);
 }
@@ -1025,7 +1035,7 @@ __device__ void nanbu_collide(const CoulombSpecies& C, const CoulombParams& K, i
 template <class R>
 __device__ void perez_collide(const CoulombSpecies& C, const CoulombParams& K, int a, int ia, int b, int ib,
                               double lD, double nP, double nQ, double nPQ, Rng& r) {
-    const double mP = C.m[a], qP = C.q[a], mQ = C.m[b], qQ = C.q[b];
+    const double mP = C.m[a], qP = pcharge(C, a, ia), mQ = C.m[b], qQ = pcharge(C, b, ib);
     const V3d UP = Vel<R>::get(C.p[a], ia), UQ = Vel<R>::get(C.p[b], ib);
     CoM f;
     if (!com_frame(UP, UQ, mP, mQ, f)) return;
@@ -1054,7 +1064,7 @@ __device__ void perez_collide(const CoulombSpecies& C, const CoulombParams& K, i
     const double eps = 2.0 * kPi * r.uniform();
     V3d nUP = UP, nUQ = UQ;
     com_rotate(f, cosChi, sinChi, eps, mP, mQ, nUP, nUQ);
-    weight_correct(C, K, a, b, UP, UQ, nUP, nUQ, r);
+    weight_correct(C, K, a, b, pweight(C, a, ia), pweight(C, b, ib), UP, UQ, nUP, nUQ, r);
     Vel<R>::put(C.p[a], ia, nUP);
     Vel<R>::put(C.p[b], ib, nUQ);
 }
@@ -1082,13 +1092,14 @@ template <class R>
 __device__ double debye_length_warp(const CoulombSpecies& C, const CoulombParams& K, int c, int lane) {
     double debye = 0.0, n_max = 0.0;
     for (int k = 0; k < C.n; ++k) {
-        const double w = C.w[k], q = C.q[k];
         double vSqr = 0.0, n = 0.0, charge = 0.0, vx = 0.0, vy = 0.0, vz = 0.0;
         const int s0 = C.start[k][c], s1 = C.start[k][c + 1];
         for (int t = s0 + lane; t < s1; t += 32) {
-            const V3d U = Vel<R>::get(C.p[k], C.idx[k][t]);
+            const int i = C.idx[k][t];
+            const V3d U = Vel<R>::get(C.p[k], i);
+            const double w = pweight(C, k, i);
             vSqr += dotd(U, U) * w;
-            charge += q * w;
+            charge += pcharge(C, k, i) * w;
             vx += w * U.x;
             vy += w * U.y;
             vz += w * U.z;
@@ -1114,6 +1125,204 @@ __device__ double debye_length_warp(const CoulombSpecies& C, const CoulombParams
     if (debye <= 0.0) return 0.0;
     const double r_min = pow(4.0 * kPi * n_max / 3.0, -1.0 / 3.0);
     return fmax(r_min, sqrt(1 / debye));
+}
+
+// ------------------------------------------------ Perez ionisation ---
+// PerezIonizationModel (CoulombCollisionModel/IonizationModel/
+// PerezIonizationModel/PerezIonizationModel.C:129-385) inside the Coulomb
+// step: the pair densities of initIonization / prepareNumberDensities
+// (lane 0, in the pairing order), prepareIonization before and ionize
+// after each electron - ion collision.  The tables per species (C index):
+// cross section, transferred and lost energy, each [Zstar][100].
+struct PerezDev {
+    int on;
+    int ek;                                // C index of the electron species, -1: none
+    int limit[PICGPU_MAX_SPECIES];         // ionisation limit per C index, -1: does not ionise
+    int atomic[PICGPU_MAX_SPECIES];
+    const double* tab[PICGPU_MAX_SPECIES];
+    double mE;
+    PerezElectron* out;
+    unsigned long long* n_out;
+    long cap;
+};
+
+// initIonization: np is the density of the pair's non-electron species
+__device__ __forceinline__ void perez_init(const PerezDev& Z, int kp, int kq, double nP, double nQ, double& np,
+                                           double& ne, double& nei) {
+    ne = 0.0;
+    nei = 0.0;
+    if (kp == Z.ek) np = nQ;
+    else if (kq == Z.ek) np = nP;
+}
+
+__device__ __forceinline__ double electron_eV(double mE, V3d U) {
+    const double b = magd(U) / kC;
+    const double gamma = 1.0 / sqrt(1.0 - b * b);
+    return (gamma - 1.0) * mE * kC * kC / kEch;
+}
+
+__device__ __forceinline__ int zstar(const CoulombSpecies& C, int k, int i) {
+    return C.p[k].zq ? C.p[k].zq[i] : 1;
+}
+
+// prepareNumberDensities for the pair (kp, ip), (kq, iq)
+template <class R>
+__device__ void perez_densities(const CoulombSpecies& C, const PerezDev& Z, int kp, int ip, int kq, int iq,
+                                double& ne, double& nei) {
+    int ke, ie, ki, ii;
+    if (kp == Z.ek) { ke = kp; ie = ip; ki = kq; ii = iq; }
+    else if (kq == Z.ek) { ke = kq; ie = iq; ki = kp; ii = ip; }
+    else return;
+    const int zs = zstar(C, ki, ii);
+    if (Z.limit[ki] < 0 || zs >= Z.limit[ki]) return;
+    double x = 6.142165 * log(electron_eV(Z.mE, Vel<R>::get(C.p[ke], ie)));
+    if (x < 0.0) x = 0.0;
+    else if (x > 99.0) x = 99.0;
+    const double cs = Z.tab[ki][size_t(zs) * 100 + size_t(int(x))];
+    if (cs > 0.0) {
+        const double We = pweight(C, ke, ie), Wi = pweight(C, ki, ii);
+        ne += We;
+        nei += We < Wi ? We : Wi;
+    }
+}
+
+// prepareIonization: 1 when (kp, ip) is the electron, 2 when (kq, iq) is,
+// 0 when the pair does not ionise
+__device__ __forceinline__ int perez_pair(const CoulombSpecies& C, const PerezDev& Z, int kp, int ip, int kq, int iq,
+                                          double nei) {
+    int which = 0, ki = 0, ii = 0;
+    if (kp == Z.ek && Z.limit[kq] >= 0) { which = 1; ki = kq; ii = iq; }
+    else if (kq == Z.ek && Z.limit[kp] >= 0) { which = 2; ki = kp; ii = ip; }
+    if (!which || zstar(C, ki, ii) >= Z.limit[ki] || !(nei > 0.0)) return 0;
+    return which;
+}
+
+// ionize for the electron (ke, ie) and the ion (ki, ii) after their
+// collision; draws from the stream of the collision ordinal.  Returns 1 when
+// the charge state rose.
+template <class R>
+__device__ int perez_ionize(const CoulombSpecies& C, const CoulombParams& K, const PerezDev& Z, int ke, int ie,
+                            int ki, int ii, double np, double ne, double nei, uint32_t cell, uint32_t step,
+                            long ord) {
+    const int A = Z.atomic[ki];
+    const double* cs = Z.tab[ki];
+    const double* te = cs + size_t(A) * 100;
+    const double* le = te + size_t(A) * 100;
+    int Zstar = zstar(C, ki, ii);
+    const int initialZstar = Zstar;
+    const double c = kC;
+    V3d Ue = Vel<R>::get(C.p[ke], ie);
+    const V3d Ui = Vel<R>::get(C.p[ki], ii);
+    const double me_ = magd(Ue), mi_ = magd(Ui);
+    double gammaE = 1.0 / sqrt(1.0 - (me_ / c) * (me_ / c));
+    const double gammaP = 1.0 / sqrt(1.0 - (mi_ / c) * (mi_ / c));
+    const double massE = C.m[ke], massP = C.m[ki];
+    const double wE = pweight(C, ke, ie), wP = pweight(C, ki, ii);
+    const double wEwP = wE / wP;
+    const double wPwE = 1.0 / wEwP;
+    double gamma_s = gammaP * gammaE * (1.0 - mi_ * me_ / (c * c));
+    if (gamma_s <= 1.0) return 0;
+    Philox r(K.seed, kStreamIonize | uint32_t(ord), cell, step);
+    const double ionCoeff_s = c * sqrt(gamma_s * gamma_s - 1.0) / gammaP * (np * ne / nei) * K.dt;
+    const double eVkin_s = (gamma_s - 1.0) * massE * c * c / kEch;
+    const double rndU = r.uniform();
+    const int ionizationMax = Z.limit[ki] - Zstar - 1;
+    double rate[PICGPU_PEREZ_MAX_Z], rate_inv[PICGPU_PEREZ_MAX_Z], prop[PICGPU_PEREZ_MAX_Z];
+    double com = 0.0;
+    int added = 0;
+    for (int k = 0; k <= ionizationMax; ++k) {
+        const double s = 6.142165 * log(eVkin_s);
+        if (s < 0.0) break;
+        const double* csz = cs + size_t(Zstar) * 100;
+        const double* tez = te + size_t(Zstar) * 100;
+        const double* lez = le + size_t(Zstar) * 100;
+        double crossSection, transferred, lost;
+        if (s < 99.0) {
+            const int l = int(s);
+            const double d = s - double(l);
+            crossSection = (csz[l + 1] - csz[l]) * d + csz[l];
+            transferred = (tez[l + 1] - tez[l]) * d + tez[l];
+            lost = (lez[l + 1] - lez[l]) * d + lez[l];
+        } else {
+            const double d = s - 99.0;
+            crossSection = (csz[99] - csz[98]) * d + csz[99];
+            transferred = tez[99];
+            lost = lez[99];
+        }
+        if (crossSection <= 0.0) break;
+        if (lost > gamma_s - 1.0) break;
+        rate[k] = ionCoeff_s * crossSection / gammaE;
+        rate_inv[k] = 1.0 / rate[k];
+        prop[k] = exp(-rate[k]);
+        if (k == 0) {
+            com = prop[k];
+        } else {
+            for (int x = 0; x < k; ++x) {
+                double cp = 1.0 - rate[k] * rate_inv[x];
+                for (int b = 0; b < x; ++b) cp *= 1.0 - rate[x] * rate_inv[b];
+                for (int b = x + 1; b < k; ++b) cp *= 1.0 - rate[x] * rate_inv[b];
+                if (k < ionizationMax) com += (prop[k] - prop[x]) / cp;
+                else com += (1.0 - prop[k] + rate[k] * rate_inv[x] * (prop[x] - 1.0)) / cp;
+            }
+        }
+        if (rndU < com) break;
+        const V3d pOld = {Ue.x * gammaE * massE, Ue.y * gammaE * massE, Ue.z * gammaE * massE};
+        const V3d pI = {Ui.x * gammaP * massP, Ui.y * gammaP * massP, Ui.z * gammaP * massP};
+        const double p2 = gamma_s * gamma_s - 1.0;
+        const double rndU2 = r.uniform();
+        if (rndU2 < wEwP) {
+            C.p[ki].zq[ii] += 1;
+            const double gammaW = transferred + 1.0;
+            const double alpha_w = sqrt((gammaW * gammaW - 1.0) / p2);
+            const double f = gammaW - alpha_w * gamma_s;
+            const V3d pNew = {alpha_w * pOld.x + f * pI.x * massE / massP, alpha_w * pOld.y + f * pI.y * massE / massP,
+                              alpha_w * pOld.z + f * pI.z * massE / massP};
+            const double gNew = sqrt(1.0 + pow(magd(pNew) / (massE * c), 2.0));
+            const unsigned long long slot = atomicAdd(Z.n_out, 1ull);
+            if (slot < (unsigned long long)Z.cap) {
+                PerezElectron& o = Z.out[slot];
+                o.key = (static_cast<unsigned long long>(cell) << 32) | (static_cast<unsigned long long>(ord) << 6) |
+                        static_cast<unsigned long long>(k);
+                o.tet = C.p[ke].tet[ie];
+                for (int a = 0; a < 3; ++a) o.y[a] = sizeof(R) == 8 ? C.p[ke].y64[a][ie] : double(C.p[ke].y32[a][ie]);
+                const double den = massE * gNew;
+                o.U[0] = pNew.x / den;
+                o.U[1] = pNew.y / den;
+                o.U[2] = pNew.z / den;
+                o.nw = wP;
+            }
+            ++added;
+        }
+        if (rndU2 < wPwE) {
+            const double alpha_e = sqrt((pow(gamma_s - lost, 2.0) - 1.0) / p2);
+            const double f = (1.0 - alpha_e) * gamma_s - lost;
+            const V3d pLost = {alpha_e * pOld.x + f * pI.x * massE / massP, alpha_e * pOld.y + f * pI.y * massE / massP,
+                               alpha_e * pOld.z + f * pI.z * massE / massP};
+            const double gLost = sqrt(1.0 + pow(magd(pLost) / (massE * c), 2.0));
+            const double den = massE * gLost;
+            Ue = {pLost.x / den, pLost.y / den, pLost.z / den};
+            Vel<R>::put(C.p[ke], ie, Ue);
+            gammaE += ((1.0 - alpha_e) * gamma_s - lost) * gammaP;
+            gamma_s -= lost;
+        }
+        Zstar++;
+    }
+    (void)added;
+    return Zstar != initialZstar ? 1 : 0;
+}
+
+// One inter-species collision with prepareIonization before and ionize
+// after it (which: perez_pair's answer for the pair as passed).
+template <class R>
+__device__ __forceinline__ int collide_ionize(const CoulombSpecies& C, const CoulombParams& K, const PerezDev& Z,
+                                              int a, int ia, int b, int ib, double lD, double nP, double nQ,
+                                              double nPQ, Rng& r, double np, double ne, double nei, uint32_t cell,
+                                              uint32_t step, long ord) {
+    const int which = Z.on ? perez_pair(C, Z, a, ia, b, ib, nei) : 0;
+    collide<R>(C, K, a, ia, b, ib, lD, nP, nQ, nPQ, r);
+    if (which == 1) return perez_ionize<R>(C, K, Z, a, ia, b, ib, np, ne, nei, cell, step, ord);
+    if (which == 2) return perez_ionize<R>(C, K, Z, b, ib, a, ia, np, ne, nei, cell, step, ord);
+    return 0;
 }
 
 // The random numbers of a cell's Coulomb step.  The shuffles take the
@@ -1181,7 +1390,7 @@ constexpr int kCoulombShared = 512;
 // and where one parcel meets several partners (odd counts, unequal species
 // counts) the partners of that parcel in their sequential order.
 template <class R>
-__global__ void __launch_bounds__(32 * kCoulombWarps) coulomb_kernel(CoulombSpecies C, CoulombParams K) {
+__global__ void __launch_bounds__(32 * kCoulombWarps) coulomb_kernel(CoulombSpecies C, CoulombParams K, PerezDev Z) {
     __shared__ int sh_sel[kCoulombWarps][2][kCoulombShared];
     const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
     const int c = int((long(blockIdx.x) * blockDim.x + threadIdx.x) >> 5);
@@ -1190,7 +1399,9 @@ __global__ void __launch_bounds__(32 * kCoulombWarps) coulomb_kernel(CoulombSpec
     const CellStream cs{K.seed, uint32_t(c), K.step_dev ? *K.step_dev : K.step};
     const double lD = K.cl == 0.0 ? debye_length_warp<R>(C, K, c, lane) : 0.0;
     long nd = 0, ord = 0;
-    unsigned long long pairs = 0;
+    unsigned long long pairs = 0, ionized = 0;
+    const uint32_t step = cs.step;
+    double np = 0.0, ne = 0.0, nei = 0.0;   // the ionisation model's pair densities
     for (int i = 0; i < C.n; ++i) {
         for (int jj = C.n - 1; jj >= i; --jj) {
             const int a = i, b = jj;
@@ -1198,8 +1409,18 @@ __global__ void __launch_bounds__(32 * kCoulombWarps) coulomb_kernel(CoulombSpec
             const int nA = C.start[a][c + 1] - sa, nB = C.start[b][c + 1] - sb;
             const int* LA = C.idx[a] + sa;
             const int* LB = C.idx[b] + sb;
-            const double sA = double(nA) * C.w[a];
-            const double sB = a != b ? double(nB) * C.w[b] : 0.0;
+            // NanbuYonemuraPairing.C:96-113: the real particles of each
+            // species, parcel by parcel in list order (lane 0)
+            double sA = 0.0, sB = 0.0;
+            if (!K.takizuka_abe) {
+                if (lane == 0) {
+                    for (int t = 0; t < nA; ++t) sA += pweight(C, a, LA[t]);
+                    if (a != b)
+                        for (int t = 0; t < nB; ++t) sB += pweight(C, b, LB[t]);
+                }
+                sA = __shfl_sync(0xffffffffu, sA, 0);
+                sB = __shfl_sync(0xffffffffu, sB, 0);
+            }
             if (a == b && nA > 1) {
                 if (!K.allow_intra) continue;
                 int* sel = nA <= kCoulombShared ? sh_sel[wib][0] : C.sel[a] + sa;
@@ -1241,9 +1462,15 @@ __global__ void __launch_bounds__(32 * kCoulombWarps) coulomb_kernel(CoulombSpec
                 if (nA % 2 != 0) {
                     // the pairs (0 1) (2 3) ... then (nA-1 0): the last
                     // collision follows the first one's on parcel sel[0]
-                    double nAA = 2.0 * C.w[a];
-                    for (int x = 0; x < nA - 2; x += 2) nAA += 2.0 * C.w[a];
-                    const double n12 = nAA / V;
+                    // NanbuYonemuraPairing.C:128-141: real particles that
+                    // collide, the extra pair first
+                    double nAA = 0.0;
+                    if (lane == 0) {
+                        nAA += 2.0 * fmin(pweight(C, a, LA[sel[nA - 1]]), pweight(C, a, LA[sel[0]]));
+                        for (int x = 0; x < nA - 2; x += 2)
+                            nAA += 2.0 * fmin(pweight(C, a, LA[sel[x]]), pweight(C, a, LA[sel[x + 1]]));
+                    }
+                    const double n12 = __shfl_sync(0xffffffffu, nAA, 0) / V;
                     const int np = (nA - 1) / 2;
                     for (int x = lane; x < np; x += 32) {
                         Rng r = cs.collision(ord + x);
@@ -1257,8 +1484,10 @@ __global__ void __launch_bounds__(32 * kCoulombWarps) coulomb_kernel(CoulombSpec
                     pairs += 1 + nA / 2;
                 } else {
                     double nAA = 0.0;
-                    for (int x = 0; x < nA - 1; x += 2) nAA += 2.0 * C.w[a];
-                    const double n12 = nAA / V;
+                    if (lane == 0)
+                        for (int x = 0; x < nA - 1; x += 2)
+                            nAA += 2.0 * fmin(pweight(C, a, LA[sel[x]]), pweight(C, a, LA[sel[x + 1]]));
+                    const double n12 = __shfl_sync(0xffffffffu, nAA, 0) / V;
                     const int np = nA / 2;
                     for (int x = lane; x < np; x += 32) {
                         Rng r = cs.collision(ord + x);
@@ -1269,7 +1498,6 @@ __global__ void __launch_bounds__(32 * kCoulombWarps) coulomb_kernel(CoulombSpec
                 }
                 __syncwarp();
             } else if (a != b && min(nA, nB) != 0) {
-                const double wmin = fmin(C.w[a], C.w[b]);
                 if (nA == nB) {
                     int* sel = nA <= kCoulombShared ? sh_sel[wib][0] : C.sel[a] + sa;
                     shuffle_warp(sel, nA, cs, nd, lane);
@@ -1281,13 +1509,27 @@ __global__ void __launch_bounds__(32 * kCoulombWarps) coulomb_kernel(CoulombSpec
                     } else {
                         nP = sA / V;
                         nQ = sB / V;
-                        double nAB = 0.0;
-                        for (int k = 0; k < nA; ++k) nAB += wmin;
-                        nPQ = nAB / V;
+                        nPQ = 0.0;
                     }
+                    // the pairs' real particles and the ionisation densities
+                    // (initIonization, prepareNumberDensities), lane 0 in order
+                    double nAB = 0.0;
+                    if (lane == 0) {
+                        if (Z.on) perez_init(Z, a, b, nP, nQ, np, ne, nei);
+                        for (int k = 0; k < nA; ++k) {
+                            if (!K.takizuka_abe)
+                                nAB += fmin(pweight(C, a, LA[sel[k]]), pweight(C, b, LB[sel[nA - k - 1]]));
+                            if (Z.on) perez_densities<R>(C, Z, a, LA[sel[k]], b, LB[sel[nA - k - 1]], ne, nei);
+                        }
+                    }
+                    if (!K.takizuka_abe) nPQ = __shfl_sync(0xffffffffu, nAB, 0) / V;
+                    np = __shfl_sync(0xffffffffu, np, 0);
+                    ne = __shfl_sync(0xffffffffu, ne, 0);
+                    nei = __shfl_sync(0xffffffffu, nei, 0);
                     for (int k = lane; k < nA; k += 32) {
                         Rng r = cs.collision(ord + k);
-                        collide<R>(C, K, a, LA[sel[k]], b, LB[sel[nA - k - 1]], lD, nP, nQ, nPQ, r);
+                        ionized += collide_ionize<R>(C, K, Z, a, LA[sel[k]], b, LB[sel[nA - k - 1]], lD, nP, nQ, nPQ,
+                                                     r, np, ne, nei, uint32_t(c), step, ord + k);
                     }
                     ord += nA;
                     pairs += nA;
@@ -1314,22 +1556,50 @@ __global__ void __launch_bounds__(32 * kCoulombWarps) coulomb_kernel(CoulombSpec
                         const int g2min = int((1.0 - delta_r) * double(nMin));
                         const int g2max = int(double(delta) * (1.0 - delta_r) * double(nMin));
                         if (g1min > 0) {
+                            if (Z.on) {
+                                if (lane == 0) {
+                                    perez_init(Z, minS, maxS, nMinS, nMaxS, np, ne, nei);
+                                    for (int g = 0, q1 = 0; g < g1max; ++g, ++q1) {
+                                        if (q1 >= g1min) q1 = 0;
+                                        perez_densities<R>(C, Z, minS, Lmin[smin[q1]], maxS, Lmax[smax[g]], ne, nei);
+                                    }
+                                }
+                                np = __shfl_sync(0xffffffffu, np, 0);
+                                ne = __shfl_sync(0xffffffffu, ne, 0);
+                                nei = __shfl_sync(0xffffffffu, nei, 0);
+                            }
                             for (int k = lane; k < g1min && k < g1max; k += 32)
                                 for (int g = k; g < g1max; g += g1min) {
                                     Rng r = cs.collision(ord + g);
-                                    collide<R>(C, K, maxS, Lmax[smax[g]], minS, Lmin[smin[k]], lD, nMaxS, nMinS,
-                                               nMaxS, r);
+                                    ionized += collide_ionize<R>(C, K, Z, maxS, Lmax[smax[g]], minS, Lmin[smin[k]], lD,
+                                                                 nMaxS, nMinS, nMaxS, r, np, ne, nei, uint32_t(c), step,
+                                                                 ord + g);
                                 }
                             ord += g1max;
+                            __syncwarp();
                         }
                         // minority position g1min + g mod g2min (all g1min
-                        // when g2min is 0), majority g1max + g
+                        // when g2min is 0), majority g1max + g; the group's
+                        // densities after group 1 collided
+                        if (Z.on) {
+                            if (lane == 0) {
+                                perez_init(Z, minS, maxS, nMinS, nMaxS, np, ne, nei);
+                                for (int g = 0, q1 = g1min; g < g2max; ++g, ++q1) {
+                                    if (q1 >= g2min + g1min) q1 = g1min;
+                                    perez_densities<R>(C, Z, minS, Lmin[smin[q1]], maxS, Lmax[smax[g1max + g]], ne, nei);
+                                }
+                            }
+                            np = __shfl_sync(0xffffffffu, np, 0);
+                            ne = __shfl_sync(0xffffffffu, ne, 0);
+                            nei = __shfl_sync(0xffffffffu, nei, 0);
+                        }
                         const int chains = g2min > 0 ? g2min : 1;
                         for (int k = lane; k < chains && k < g2max; k += 32)
                             for (int g = k; g < g2max; g += chains) {
                                 Rng r = cs.collision(ord + g);
-                                collide<R>(C, K, maxS, Lmax[smax[g1max + g]], minS, Lmin[smin[g1min + k]], lD, nMaxS,
-                                           nMinS, nMaxS, r);
+                                ionized += collide_ionize<R>(C, K, Z, maxS, Lmax[smax[g1max + g]], minS,
+                                                             Lmin[smin[g1min + k]], lD, nMaxS, nMinS, nMaxS, r, np, ne,
+                                                             nei, uint32_t(c), step, ord + g);
                             }
                         ord += g2max;
                         pairs += g1max + g2max;
@@ -1339,13 +1609,24 @@ __global__ void __launch_bounds__(32 * kCoulombWarps) coulomb_kernel(CoulombSpec
                     const double nMaxS = (maxS == a ? sA : sB) / V;
                     const double nMinS = (maxS == a ? sB : sA) / V;
                     double nAB = 0.0;
-                    for (int l = 0; l < nMax; ++l) nAB += wmin;
-                    const double n12 = nAB / V;
+                    if (lane == 0) {
+                        if (Z.on) perez_init(Z, minS, maxS, nMinS, nMaxS, np, ne, nei);
+                        for (int l = 0, k = 0; l < nMax; ++l, ++k) {
+                            if (k >= nMin) k = 0;
+                            nAB += fmin(pweight(C, minS, Lmin[smin[k]]), pweight(C, maxS, Lmax[smax[l]]));
+                            if (Z.on) perez_densities<R>(C, Z, minS, Lmin[smin[k]], maxS, Lmax[smax[l]], ne, nei);
+                        }
+                    }
+                    const double n12 = __shfl_sync(0xffffffffu, nAB, 0) / V;
+                    np = __shfl_sync(0xffffffffu, np, 0);
+                    ne = __shfl_sync(0xffffffffu, ne, 0);
+                    nei = __shfl_sync(0xffffffffu, nei, 0);
                     // majority parcel l meets minority parcel l mod nMin
                     for (int k = lane; k < nMin; k += 32)
                         for (int l = k; l < nMax; l += nMin) {
                             Rng r = cs.collision(ord + l);
-                            collide<R>(C, K, maxS, Lmax[smax[l]], minS, Lmin[smin[k]], lD, nMaxS, nMinS, n12, r);
+                            ionized += collide_ionize<R>(C, K, Z, maxS, Lmax[smax[l]], minS, Lmin[smin[k]], lD, nMaxS,
+                                                         nMinS, n12, r, np, ne, nei, uint32_t(c), step, ord + l);
                         }
                     ord += nMax;
                     pairs += nMax;
@@ -1355,13 +1636,38 @@ __global__ void __launch_bounds__(32 * kCoulombWarps) coulomb_kernel(CoulombSpec
         }
     }
     if (pairs && lane == 0) atomicAdd(K.counts + 4, pairs);
+    for (int off = 16; off > 0; off >>= 1) ionized += __shfl_down_sync(0xffffffffu, ionized, off);
+    if (ionized && lane == 0) atomicAdd(K.counts + 20, ionized);
 }
 
-void launch_coulomb(const CoulombSpecies& C, const CoulombParams& K, bool mixed, cudaStream_t stream) {
+void launch_coulomb(const CoulombSpecies& C, const CoulombParams& K, const PerezDev& Z, bool mixed,
+                    cudaStream_t stream) {
     const int threads = 32 * kCoulombWarps;
     const unsigned blocks = unsigned((long(K.n_cells) * 32 + threads - 1) / threads);
-    if (mixed) coulomb_kernel<float><<<blocks, threads, 0, stream>>>(C, K);
-    else coulomb_kernel<double><<<blocks, threads, 0, stream>>>(C, K);
+    if (mixed) coulomb_kernel<float><<<blocks, threads, 0, stream>>>(C, K, Z);
+    else coulomb_kernel<double><<<blocks, threads, 0, stream>>>(C, K, Z);
+}
+
+// The electrons of this step's ionisations: sorted by their key (the order
+// of picFoam's sequential loop) and appended to the electron store from slot
+// first on, with their nParticle and charge modifier 1.
+template <class R>
+__global__ void perez_append_kernel(const PerezElectron* __restrict__ e, long n, DSpecies p, long first) {
+    for (long j = blockIdx.x * long(blockDim.x) + threadIdx.x; j < n; j += long(gridDim.x) * blockDim.x) {
+        const long d = first + j;
+        p.tet[d] = e[j].tet;
+        for (int a = 0; a < 3; ++a) {
+            if (sizeof(R) == 8) {
+                p.y64[a][d] = e[j].y[a];
+                p.u64[a][d] = e[j].U[a];
+            } else {
+                p.y32[a][d] = float(e[j].y[a]);
+                p.u32[a][d] = float(e[j].U[a]);
+            }
+        }
+        p.nw[d] = e[j].nw;
+        p.zq[d] = 1;
+    }
 }
 
 template <class T>
@@ -1642,8 +1948,75 @@ bool ascending(const double* e, int n) {
 
 }  // namespace
 
+namespace {
+
+// IonizationData::calculateIonizationCrossSection (PerezIonizationModel.C:
+// 405-484): per charge state Z the cross section summed over the orbitals
+// k (Carlson binding energies, bindingEnergy :395-399; orbitals of equal
+// binding energy counted together) and the energies transferred to the new
+// electron and lost by the colliding one, averaged over the orbitals (units
+// of m_e c^2), on 100 energies log-spaced over 1 eV - 10 MeV.  Layout:
+// cs[Z][100], then transferred, then lost.
+std::vector<double> perez_tables(const picgpu_perez_ion& in) {
+    const int A = in.atomic_number;
+    std::vector<double> t(size_t(3) * A * 100, 0.0);
+    double* cs = t.data();
+    double* te = cs + size_t(A) * 100;
+    double* le = te + size_t(A) * 100;
+    const double r_e = 2.8179403227e-15;
+    const double step = 99.0 / std::log(1e7 / 1.0);
+    auto bind = [&](int Z, int k) { return in.ionization_energy[Z] - in.binding_energy[A - Z - 1] + in.binding_energy[k]; };
+    for (int Z = 0; Z < A; ++Z)
+        for (int i = 0; i < 100; ++i) {
+            const double E = std::exp(double(i) / step);
+            int N = 1;
+            double sig = 0.0, tr = 0.0, lo = 0.0;
+            for (int k = 0; k < A - Z; ++k) {
+                const double Bk = bind(Z, k);
+                if (k < A - Z - 1 && Bk == bind(Z, k + 1)) {
+                    N++;
+                    continue;
+                }
+                const double eps = E / Bk;
+                if (eps > 1.0) {
+                    const double b_dash = Bk / 510997.37, eps_dash = E / 510997.37, u_dash = b_dash;
+                    const double beta_eps2 = 1.0 - 1.0 / ((1.0 + eps_dash) * (1.0 + eps_dash));
+                    const double beta_b2 = 1.0 - 1.0 / ((1.0 + b_dash) * (1.0 + b_dash));
+                    const double beta_u2 = 1.0 - 1.0 / ((1.0 + u_dash) * (1.0 + u_dash));
+                    const double sigma0 = 2.0 * kPi * r_e * r_e * N / (b_dash * (beta_eps2 + beta_b2 + beta_u2));
+                    double ediv2 = 1.0 + eps_dash * 0.5;
+                    ediv2 *= ediv2;
+                    const double A1 = 1.0 / (1.0 + eps) * (1.0 + 2 * eps_dash) / ediv2;
+                    const double A2 = (eps - 1.0) / 2.0 * b_dash * b_dash / ediv2;
+                    const double A3 = std::log(beta_eps2 / (1.0 - beta_eps2)) - beta_eps2 - std::log(2.0 * b_dash);
+                    const double sk = sigma0 * (0.5 * A3 * (1.0 - 1.0 / (eps * eps)) + 1.0 - 1.0 / eps + A2 -
+                                                A1 * std::log(eps));
+                    const double wk = sigma0 * (0.5 * A3 * (eps - 1.0) * (eps - 1.0) / (eps * (eps - 1.0)) +
+                                                2.0 * std::log((eps + 1.0) * 0.5) - std::log(eps) +
+                                                A2 * (eps - 1.0) * 0.25 -
+                                                A1 * (std::log(eps) - (eps + 1.0) * std::log(0.5 * (eps + 1.0))));
+                    sig += sk;
+                    tr += wk * b_dash;
+                    lo += (sk + wk) * b_dash;
+                }
+                N = 1;
+            }
+            if (sig > 0.0) {
+                tr /= sig;
+                lo /= sig;
+            }
+            cs[size_t(Z) * 100 + i] = sig;
+            te[size_t(Z) * 100 + i] = tr;
+            le[size_t(Z) * 100 + i] = lo;
+        }
+    return t;
+}
+
+}  // namespace
+
 int collide_init(CollideState& st, const picgpu_config& cfg, const DMesh& m, cudaStream_t s, std::string* msg) {
-    st.enabled = cfg.mcc.enabled || cfg.coulomb.enabled || cfg.ion_mcc.enabled || cfg.binary.enabled;
+    st.enabled = cfg.mcc.enabled || cfg.coulomb.enabled || cfg.ion_mcc.enabled || cfg.binary.enabled ||
+                 cfg.merging.enabled;
     if (!st.enabled) return PICGPU_OK;
     const int nc = m.n_cells;
     if (dmalloc(&st.cell_start, size_t(PICGPU_MAX_SPECIES) * (nc + 1)) ||
@@ -1656,6 +2029,59 @@ int collide_init(CollideState& st, const picgpu_config& cfg, const DMesh& m, cud
     cudaMemsetAsync(st.overflow, 0, sizeof(int), s);
     cudaMemsetAsync(st.counts, 0, kCollideCounts * sizeof(unsigned long long), s);
     if (st.iz_cell) cudaMemsetAsync(st.iz_cell, 0, size_t(nc) * sizeof(unsigned long long), s);
+    if (cfg.perez.enabled) {
+        // PerezIonizationModel.C:30-118: one entry per ion species; a limit
+        // below 1 switches the species off
+        const picgpu_perez& pz = cfg.perez;
+        const int es = cfg.electron_species;
+        bool ok = cfg.coulomb.enabled && es >= 0 && es < cfg.n_species && cfg.species[es].charge != 0.0 &&
+                  pz.n_ions >= 0 && pz.n_ions <= PICGPU_PEREZ_MAX_IONS;
+        for (int k = 0; ok && k < pz.n_ions; ++k) {
+            const picgpu_perez_ion& in = pz.ion[k];
+            ok = in.species >= 0 && in.species < cfg.n_species && in.species != es && in.atomic_number >= 1 &&
+                 in.atomic_number <= PICGPU_PEREZ_MAX_Z;
+            if (!ok || in.ionization_limit == 0) continue;
+            const std::vector<double> t = perez_tables(in);
+            if (dmalloc(&st.ptab[in.species], t.size()) ||
+                cudaMemcpy(st.ptab[in.species], t.data(), t.size() * sizeof(double), cudaMemcpyHostToDevice) !=
+                    cudaSuccess) {
+                *msg = "Perez ionisation: device allocation failed";
+                return PICGPU_OOM;
+            }
+            st.patomic[in.species] = in.atomic_number;
+            st.plimit[in.species] = in.ionization_limit < 0 ? in.atomic_number
+                                                            : std::min(in.ionization_limit, in.atomic_number);
+        }
+        if (!ok) {
+            *msg = "Perez ionisation: bad settings (needs Coulomb collisions, a charged electron species and "
+                   "ion species other than it, atomic numbers 1 - 64)";
+            return PICGPU_INVALID_ARG;
+        }
+        st.pstage_cap = 1 << 20;
+        if (dmalloc(&st.pstage, st.pstage_cap) || dmalloc(&st.pcount, 1)) {
+            *msg = "Perez ionisation: device allocation failed";
+            return PICGPU_OOM;
+        }
+    }
+    if (cfg.merging.enabled) {
+        // PairMerging.C:35-68: the settings and the species list
+        const picgpu_merging& mg = cfg.merging;
+        if (mg.n_species < 1 || mg.n_species > PICGPU_MAX_SPECIES || mg.n_check_neighbors < 1 ||
+            !(mg.reduction_factor > 0.0 && mg.reduction_factor <= 1.0) || mg.cell_parcels_max < 1 ||
+            mg.max_checks < 0 || mg.merge_maximum_per_cell < 0 || !(mg.velocity_ratio >= 0.0)) {
+            *msg = "PairMerging: bad settings";
+            return PICGPU_INVALID_ARG;
+        }
+        if (double(mg.cell_parcels_max) * mg.reduction_factor < double(mg.n_check_neighbors)) {
+            *msg = "PairMerging: cellParcelsMax x reductionFactor is below nCheckNeighbors";
+            return PICGPU_INVALID_ARG;
+        }
+        for (int k = 0; k < mg.n_species; ++k)
+            if (mg.species[k] < 0 || mg.species[k] >= cfg.n_species) {
+                *msg = "PairMerging: species not defined";
+                return PICGPU_INVALID_ARG;
+            }
+    }
     if (cfg.coulomb.enabled) {
         const picgpu_coulomb& co = cfg.coulomb;
         if (co.pairing < 0 || co.pairing > 1 || co.collide < 0 || co.collide > 1 || co.coulomb_log < 0 ||
@@ -1861,10 +2287,13 @@ void collide_free(CollideState& st) {
                     st.cell_start, st.cell_count,  st.cell_cursor, st.counts, st.scan_tmp, st.ncand,
                     st.cand_off,   st.stage,       st.flags,  st.pos,      st.stage_tmp, st.overflow,
                     st.iz_cell,    st.bsmax,       st.brem,   st.bbgrem,   st.blist,      st.boct,
-                    st.psvmax,     st.premainder,  st.ipsvmax, st.ipremainder, st.n_live};
+                    st.psvmax,     st.premainder,  st.ipsvmax, st.ipremainder, st.n_live,
+                    st.mspeed,     st.mstage,      st.mcount, st.moff,     st.mcounts,    st.mkin,
+                    st.pstage,     st.pcount};
     for (void* p : ptrs)
         if (p) cudaFree(p);
     for (int s = 0; s < PICGPU_MAX_SPECIES; ++s) {
+        if (st.ptab[s]) cudaFree(st.ptab[s]);
         if (st.idx[s]) cudaFree(st.idx[s]);
         if (st.sel[s]) cudaFree(st.sel[s]);
         if (st.sel2[s]) cudaFree(st.sel2[s]);
@@ -1924,6 +2353,10 @@ __global__ void permute_kernel(const int* __restrict__ idx, int total, DSpecies 
         } else {
             for (int a = 0; a < 3; ++a) { dst.y32[a][j] = src.y32[a][i]; dst.u32[a][j] = src.u32[a][i]; }
         }
+        if (src.nw) {
+            dst.nw[j] = src.nw[i];
+            dst.zq[j] = src.zq[i];
+        }
     }
 }
 
@@ -1965,6 +2398,28 @@ int sort_species(CollideState& st, const DMesh& m, int s, const DSpecies& src, c
 }
 
 namespace {
+
+PerezDev perez_setup(const CollideState& st, const CollideArgs& a, const CoulombSpecies& C) {
+    PerezDev Z{};
+    Z.ek = -1;
+    for (int k = 0; k < PICGPU_MAX_SPECIES; ++k) Z.limit[k] = -1;
+    if (!a.cfg->perez.enabled) return Z;
+    for (int k = 0; k < C.n; ++k) {
+        const int s = C.sp[k];
+        if (s == a.cfg->electron_species) Z.ek = k;
+        if (st.ptab[s]) {
+            Z.limit[k] = st.plimit[s];
+            Z.atomic[k] = st.patomic[s];
+            Z.tab[k] = st.ptab[s];
+        }
+    }
+    Z.on = Z.ek >= 0;
+    Z.mE = a.cfg->species[a.cfg->electron_species].mass;
+    Z.out = st.pstage;
+    Z.n_out = st.pcount;
+    Z.cap = st.pstage_cap;
+    return Z;
+}
 
 void coulomb_setup(const CollideState& st, const CollideArgs& a, CoulombSpecies& C, CoulombParams& K) {
     const picgpu_config& cfg = *a.cfg;
@@ -2254,6 +2709,48 @@ int mcc_parcels(CollideState& st, const CollideArgs& a, long newn[], std::string
     return PICGPU_OK;
 }
 
+// The electrons of the step's Perez ionisations: read back, put in key
+// order and appended behind the electron store (room for them is the
+// caller's: the store keeps an eighth of its size free for collision
+// products).
+int perez_append(CollideState& st, const CollideArgs& a, long newn[], long long* added, std::string* msg,
+                 int64_t* launches) {
+    const int es = a.cfg->electron_species;
+    unsigned long long cnt = 0;
+    if (cudaMemcpyAsync(&cnt, st.pcount, sizeof cnt, cudaMemcpyDeviceToHost, a.stream) != cudaSuccess ||
+        cudaStreamSynchronize(a.stream) != cudaSuccess) {
+        *msg = "Perez ionisation: reading the new electrons failed";
+        return PICGPU_CUDA_ERROR;
+    }
+    *added = (long long)cnt;
+    if (cnt == 0) return PICGPU_OK;
+    if (cnt > (unsigned long long)st.pstage_cap) {
+        *msg = "Perez ionisation: more new electrons in one step than the staging holds";
+        return PICGPU_CAPACITY;
+    }
+    if (newn[es] + long(cnt) > a.cap[es]) {
+        *msg = "Perez ionisation: the electron store has no room for the new electrons";
+        return PICGPU_CAPACITY;
+    }
+    std::vector<PerezElectron> h(cnt);
+    if (cudaMemcpyAsync(h.data(), st.pstage, cnt * sizeof(PerezElectron), cudaMemcpyDeviceToHost, a.stream) !=
+            cudaSuccess ||
+        cudaStreamSynchronize(a.stream) != cudaSuccess)
+        return PICGPU_CUDA_ERROR;
+    std::sort(h.begin(), h.end(), [](const PerezElectron& x, const PerezElectron& y) { return x.key < y.key; });
+    if (cudaMemcpyAsync(st.pstage, h.data(), cnt * sizeof(PerezElectron), cudaMemcpyHostToDevice, a.stream) !=
+        cudaSuccess)
+        return PICGPU_CUDA_ERROR;
+    const int g = grid_of(long(cnt), 256);
+    if (a.mixed) perez_append_kernel<float><<<g, 256, 0, a.stream>>>(st.pstage, long(cnt), a.sp[es], newn[es]);
+    else perez_append_kernel<double><<<g, 256, 0, a.stream>>>(st.pstage, long(cnt), a.sp[es], newn[es]);
+    *launches += 1;
+    newn[es] += long(cnt);
+    // the host copy must stay alive until the upload has run
+    if (cudaStreamSynchronize(a.stream) != cudaSuccess) return PICGPU_CUDA_ERROR;
+    return cudaGetLastError() == cudaSuccess ? PICGPU_OK : PICGPU_CUDA_ERROR;
+}
+
 int run_collisions(CollideState& st, const CollideArgs& a, int64_t counts[kCollideCounts], long newn[], int swapped[],
                    std::string* msg, int64_t* launches, double* phase_ms) {
     (void)phase_ms;
@@ -2261,6 +2758,7 @@ int run_collisions(CollideState& st, const CollideArgs& a, int64_t counts[kColli
     const int nc = a.m.n_cells;
     for (int s = 0; s < a.n_species; ++s) { newn[s] = a.n[s]; swapped[s] = 0; }
     cudaMemsetAsync(st.counts, 0, kCollideCounts * sizeof(unsigned long long), a.stream);
+    long long perez_electrons = 0;
     // cell occupancy of every species (PICCloud::buildCellOccupancy)
     for (int s = 0; s < a.n_species; ++s) {
         const int e = occupancy(st, a, s, msg, launches);
@@ -2273,8 +2771,14 @@ int run_collisions(CollideState& st, const CollideArgs& a, int64_t counts[kColli
         CoulombSpecies C;
         CoulombParams K;
         coulomb_setup(st, a, C, K);
-        launch_coulomb(C, K, a.mixed, a.stream);
+        const PerezDev Z = perez_setup(st, a, C);
+        if (Z.on) cudaMemsetAsync(st.pcount, 0, sizeof(unsigned long long), a.stream);
+        launch_coulomb(C, K, Z, a.mixed, a.stream);
         *launches += 1;
+        if (Z.on) {
+            const int e = perez_append(st, a, newn, &perez_electrons, msg, launches);
+            if (e) return e;
+        }
     }
     if (cfg.mcc.enabled && cfg.mcc.neutral_parcels) {
         const int e = mcc_parcels(st, a, newn, msg, launches);
@@ -2390,6 +2894,7 @@ int run_collisions(CollideState& st, const CollideArgs& a, int64_t counts[kColli
         return PICGPU_CUDA_ERROR;
     }
     for (int k = 0; k < kCollideCounts; ++k) counts[k] = (int64_t)h[k];
+    counts[21] = perez_electrons;
     return cudaGetLastError() == cudaSuccess ? PICGPU_OK : PICGPU_CUDA_ERROR;
 }
 
@@ -2461,7 +2966,9 @@ int run_collisions_device(CollideState& st, const CollideArgs& a, int* n_dev, in
         CoulombParams K;
         coulomb_setup(st, a, C, K);
         K.step_dev = step_dev;
-        launch_coulomb(C, K, a.mixed, a.stream);
+        PerezDev Z{};
+        Z.ek = -1;
+        launch_coulomb(C, K, Z, a.mixed, a.stream);
         *launches += 1;
     }
     if (cfg.mcc.enabled) {
@@ -2506,5 +3013,328 @@ int run_collisions_device(CollideState& st, const CollideArgs& a, int* n_dev, in
     }
     return cudaGetLastError() == cudaSuccess ? PICGPU_OK : PICGPU_CUDA_ERROR;
 }
+
+// ------------------------------------------------------- PairMerging ---
+namespace {
+
+struct MergeParams {
+    int n_cells;
+    DMesh m;
+    const int* start;          // cell occupancy of the species
+    const int* idx;
+    int* sel;                  // scratch: mergeSelect per cell (same layout as idx)
+    double* speed;             // scratch: |U| per list position
+    DSpecies p;
+    double w, mass;
+    int li;                    // entry of the merge list (random stream)
+    double n_dev, reduction, cos_angle, velocity_ratio;
+    int cell_max, max_checks, n_check, max_per_cell;
+    uint64_t seed;
+    uint32_t step;
+    MergedParcel* stage;       // cell c stages from start[c] / 2 on
+    int* count;                // merges per cell
+    unsigned long long* counts;  // merged, checked
+    double* kin;
+};
+
+template <class R>
+__device__ __forceinline__ double mw(const MergeParams& M, int i) {
+    return M.p.nw ? M.p.nw[i] : M.w;
+}
+
+// The parcel's position: cell centre plus its tet's face-triangle offsets
+// weighted by the barycentric coordinates 1..3 (the oracle's position()).
+template <class R>
+__device__ void parcel_position(const MergeParams& M, int i, double* x) {
+    const int tg = M.p.tet[i];
+    const int c = tg / 12, t = tg - 12 * c;
+    const double* off = M.m.offset + size_t(M.m.cell_class[c]) * 24;
+    double y[3];
+    for (int a = 0; a < 3; ++a) y[a] = sizeof(R) == 8 ? M.p.y64[a][i] : double(M.p.y32[a][i]);
+    for (int a = 0; a < 3; ++a)
+        x[a] = M.m.cc[3 * size_t(c) + a] + y[0] * off[3 * c_tetC.tri[t][0] + a] +
+               y[1] * off[3 * c_tetC.tri[t][1] + a] + y[2] * off[3 * c_tetC.tri[t][2] + a];
+}
+
+// x in cell c: the tet whose smallest barycentric coordinate is largest,
+// coordinates clamped to >= 0 and renormalised (mesh locate within a known
+// cell).  Returns the tet index cell 12 + t.
+__device__ int locate_in_cell(const DMesh& m, int c, const double* x, double* y) {
+    const double r[3] = {x[0] - m.cc[3 * size_t(c)], x[1] - m.cc[3 * size_t(c) + 1], x[2] - m.cc[3 * size_t(c) + 2]};
+    int best = 0;
+    double best_min = -1e300, q[3] = {0.0, 0.0, 0.0};
+    for (int t = 0; t < 12; ++t) {
+        const double* row = m.tetinv + (size_t(m.cell_class[c]) * 12 + t) * 9;
+        double w[3];
+        for (int k = 0; k < 3; ++k) w[k] = row[3 * k] * r[0] + row[3 * k + 1] * r[1] + row[3 * k + 2] * r[2];
+        const double lowest = fmin(fmin(1.0 - w[0] - w[1] - w[2], w[0]), fmin(w[1], w[2]));
+        if (lowest > best_min) {
+            best_min = lowest;
+            best = t;
+            q[0] = w[0];
+            q[1] = w[1];
+            q[2] = w[2];
+        }
+    }
+    const double all[4] = {fmax(1.0 - q[0] - q[1] - q[2], 0.0), fmax(q[0], 0.0), fmax(q[1], 0.0), fmax(q[2], 0.0)};
+    const double sum = all[0] + all[1] + all[2] + all[3];
+    for (int k = 0; k < 3; ++k) y[k] = all[k + 1] / sum;
+    return 12 * c + best;
+}
+
+// Heap sort of sel[0, n) by (key[sel], sel): the ascending speed order of
+// PairMerging.C:110-113, ties by list position.
+__device__ __forceinline__ bool merge_less(const double* key, int a, int b) {
+    return key[a] < key[b] || (key[a] == key[b] && a < b);
+}
+__device__ void sift_down(int* sel, const double* key, int root, int n) {
+    while (true) {
+        int child = 2 * root + 1;
+        if (child >= n) return;
+        if (child + 1 < n && merge_less(key, sel[child], sel[child + 1])) ++child;
+        if (!merge_less(key, sel[root], sel[child])) return;
+        const int t = sel[root];
+        sel[root] = sel[child];
+        sel[child] = t;
+        root = child;
+    }
+}
+__device__ void heap_sort(int* sel, const double* key, int n) {
+    for (int k = n / 2 - 1; k >= 0; --k) sift_down(sel, key, k, n);
+    for (int e = n - 1; e > 0; --e) {
+        const int t = sel[0];
+        sel[0] = sel[e];
+        sel[e] = t;
+        sift_down(sel, key, 0, e);
+    }
+}
+
+// PairMerging::mergeParticles (PairMerging.C:71-259) for one cell, one
+// thread per cell, with the reference's quirks: the speeds of the
+// acceptance tests are those of the LIST positions pId1 / pId2 (not of the
+// parcels they select, and not shifted after a merge), a well-aligned pair
+// (velocity angle below angleDifference) is rejected, and the merged parcel
+// gets charge modifier 1 (PICCloud::addNewParcel).
+template <class R>
+__global__ void merge_kernel(MergeParams M) {
+    const int c = blockIdx.x * blockDim.x + threadIdx.x;
+    if (c >= M.n_cells) return;
+    const int s0 = M.start[c];
+    int N = M.start[c + 1] - s0;
+    int merged = 0;
+    if (N <= M.cell_max) {
+        M.count[c] = 0;
+        return;
+    }
+    const int* L = M.idx + s0;
+    int* sel = M.sel + s0;
+    double* speed = M.speed + s0;
+    int nTarget = int(double(N) * M.reduction);
+    if (N - nTarget > M.max_per_cell) nTarget = N - M.max_per_cell;
+    for (int k = 0; k < N; ++k) {
+        const int i = L[k];
+        double U[3];
+        for (int a = 0; a < 3; ++a) U[a] = sizeof(R) == 8 ? M.p.u64[a][i] : double(M.p.u32[a][i]);
+        speed[k] = sqrt(U[0] * U[0] + U[1] * U[1] + U[2] * U[2]);
+        sel[k] = k;
+    }
+    heap_sort(sel, speed, N);
+    Philox rng(M.seed, kStreamMerge | uint32_t(M.li), uint32_t(c), M.step);
+    MergedParcel* out = M.stage + s0 / 2;
+    unsigned long long checked = 0;
+    double kin = 0.0;
+    int checks = 0;
+    while (N > nTarget) {
+        int pId1 = int(rng.uniform() * double(N));
+        if (pId1 >= N) pId1 = N - 1;
+        const int i1 = L[sel[pId1]];
+        int pId2 = pId1 - M.n_check / 2;
+        if (pId2 < 0) pId2 = 0;
+        if (pId2 + M.n_check > N - 1) pId2 = N - M.n_check - 1;
+        if (pId2 < 0) pId2 = 0;
+        int found = -1;
+        for (int k = 0; k < M.n_check; ++k) {
+            if (pId2 == pId1) pId2++;
+            if (pId2 >= N) break;
+            const int i2 = L[sel[pId2]];
+            checked++;
+            if (M.n_dev - fabs(mw<R>(M, i2) - mw<R>(M, i1)) < 0.0) { pId2++; continue; }
+            if ((M.p.zq ? M.p.zq[i2] : 1) != (M.p.zq ? M.p.zq[i1] : 1)) { pId2++; continue; }
+            double U1[3], U2[3];
+            for (int a = 0; a < 3; ++a) {
+                U1[a] = sizeof(R) == 8 ? M.p.u64[a][i1] : double(M.p.u32[a][i1]);
+                U2[a] = sizeof(R) == 8 ? M.p.u64[a][i2] : double(M.p.u32[a][i2]);
+            }
+            if (U2[0] * U1[0] + U2[1] * U1[1] + U2[2] * U1[2] > speed[pId2] * speed[pId1] * M.cos_angle) {
+                pId2++;
+                continue;
+            }
+            double ratio = speed[pId2] / speed[pId1];
+            if (ratio > 1.0) ratio = 1.0 / ratio;
+            if (ratio < M.velocity_ratio) { pId2++; continue; }
+            found = pId2;
+            break;
+        }
+        if (found >= 0) {
+            pId2 = found;
+            const int i2 = L[sel[pId2]];
+            const double n1 = mw<R>(M, i1), n2 = mw<R>(M, i2);
+            const double nSum = n1 + n2;
+            double x1[3], x2[3], U1[3], U2[3], com[3], nU[3];
+            parcel_position<R>(M, i1, x1);
+            parcel_position<R>(M, i2, x2);
+            for (int a = 0; a < 3; ++a) {
+                U1[a] = sizeof(R) == 8 ? M.p.u64[a][i1] : double(M.p.u32[a][i1]);
+                U2[a] = sizeof(R) == 8 ? M.p.u64[a][i2] : double(M.p.u32[a][i2]);
+                com[a] = (n1 * x1[a] + n2 * x2[a]) / nSum;
+                nU[a] = (n1 * U1[a] + n2 * U2[a]) / nSum;
+            }
+            const double pre = 0.5 * M.mass *
+                               ((U1[0] * U1[0] + U1[1] * U1[1] + U1[2] * U1[2]) * n1 +
+                                (U2[0] * U2[0] + U2[1] * U2[1] + U2[2] * U2[2]) * n2);
+            const double post = 0.5 * M.mass * (nU[0] * nU[0] + nU[1] * nU[1] + nU[2] * nU[2]) * nSum;
+            kin += post - pre;
+            MergedParcel& mp = out[merged++];
+            mp.tet = locate_in_cell(M.m, c, com, mp.y);
+            for (int a = 0; a < 3; ++a) mp.U[a] = nU[a];
+            mp.nw = nSum;
+            M.p.tet[i1] = -1;
+            M.p.tet[i2] = -1;
+            const int minPos = min(pId1, pId2), maxPos = max(pId1, pId2);
+            for (int k = minPos; k < N - 2; ++k) sel[k] = k >= maxPos - 1 ? sel[k + 2] : sel[k + 1];
+            N -= 2;
+        }
+        checks++;
+        if (checks > M.max_checks) break;
+    }
+    M.count[c] = merged;
+    if (merged) atomicAdd(M.counts, (unsigned long long)merged);
+    if (checked) atomicAdd(M.counts + 1, checked);
+    if (kin != 0.0) atomicAdd(M.kin, kin);
+}
+
+template <class R>
+__global__ void merge_append_kernel(int n_cells, const int* __restrict__ start, const int* __restrict__ count,
+                                    const int* __restrict__ off, const MergedParcel* __restrict__ stage, DSpecies p,
+                                    long first) {
+    const int c = blockIdx.x * blockDim.x + threadIdx.x;
+    if (c >= n_cells) return;
+    const MergedParcel* src = stage + start[c] / 2;
+    for (int k = 0; k < count[c]; ++k) {
+        const long j = first + off[c] + k;
+        const MergedParcel& mp = src[k];
+        p.tet[j] = mp.tet;
+        for (int a = 0; a < 3; ++a) {
+            if (sizeof(R) == 8) {
+                p.y64[a][j] = mp.y[a];
+                p.u64[a][j] = mp.U[a];
+            } else {
+                p.y32[a][j] = float(mp.y[a]);
+                p.u32[a][j] = float(mp.U[a]);
+            }
+        }
+        p.nw[j] = mp.nw;
+        p.zq[j] = 1;
+    }
+}
+
+}  // namespace
+
+int merge_select(CollideState& st, const CollideArgs& a, int li, int s, long long* total, std::string* msg,
+                 int64_t* launches) {
+    const picgpu_merging& mg = a.cfg->merging;
+    const int nc = a.m.n_cells;
+    *total = 0;
+    int e = occupancy(st, a, s, msg, launches);
+    if (e) return e;
+    const long n = a.n[s];
+    if (st.mspeed_cap < std::max<long>(n, 1) || !st.mcount) {
+        if (st.mspeed) cudaFree(st.mspeed);
+        if (st.mstage) cudaFree(st.mstage);
+        st.mspeed = nullptr;
+        st.mstage = nullptr;
+        const long cap = std::max<long>(n + n / 4, 1024);
+        if (dmalloc(&st.mspeed, cap) || dmalloc(&st.mstage, cap / 2 + 1) ||
+            (!st.mcount && (dmalloc(&st.mcount, nc + 1) || dmalloc(&st.moff, nc + 1) || dmalloc(&st.mcounts, 2) ||
+                            dmalloc(&st.mkin, 1)))) {
+            *msg = "merging: device allocation failed";
+            return PICGPU_OOM;
+        }
+        st.mspeed_cap = cap;
+        st.mstage_cap = cap / 2 + 1;
+        cudaMemsetAsync(st.mcounts, 0, 2 * sizeof(unsigned long long), a.stream);
+        cudaMemsetAsync(st.mkin, 0, sizeof(double), a.stream);
+    }
+    MergeParams M{};
+    M.n_cells = nc;
+    M.m = a.m;
+    M.start = st.cell_start + size_t(s) * (nc + 1);
+    M.idx = st.idx[s];
+    M.sel = st.sel[s];
+    M.speed = st.mspeed;
+    M.p = a.sp[s];
+    M.w = a.cfg->species[s].weight;
+    M.mass = a.cfg->species[s].mass;
+    M.li = li;
+    M.n_dev = mg.n_deviation[li];
+    M.reduction = mg.reduction_factor;
+    M.cos_angle = std::cos(mg.angle_difference * 3.14159265358979323846 / 180.0);
+    M.velocity_ratio = mg.velocity_ratio;
+    M.cell_max = mg.cell_parcels_max;
+    M.max_checks = mg.max_checks;
+    M.n_check = mg.n_check_neighbors;
+    M.max_per_cell = mg.merge_maximum_per_cell;
+    M.seed = a.cfg->seed;
+    M.step = uint32_t(a.step);
+    M.stage = st.mstage;
+    M.count = st.mcount;
+    M.counts = st.mcounts;
+    M.kin = st.mkin;
+    if (a.mixed) merge_kernel<float><<<(nc + 127) / 128, 128, 0, a.stream>>>(M);
+    else merge_kernel<double><<<(nc + 127) / 128, 128, 0, a.stream>>>(M);
+    exclusive_scan(st.mcount, st.moff, nc, st.scan_tmp, a.stream, launches);
+    *launches += 1;
+    int t = 0;
+    if (cudaMemcpyAsync(&t, st.moff + nc, sizeof(int), cudaMemcpyDeviceToHost, a.stream) != cudaSuccess ||
+        cudaStreamSynchronize(a.stream) != cudaSuccess)
+        return PICGPU_CUDA_ERROR;
+    *total = t;
+    return cudaGetLastError() == cudaSuccess ? PICGPU_OK : PICGPU_CUDA_ERROR;
+}
+
+int merge_append(CollideState& st, const CollideArgs& a, int s, long first, long long total, std::string* msg,
+                 int64_t* launches) {
+    (void)msg;
+    if (total <= 0) return PICGPU_OK;
+    const int nc = a.m.n_cells;
+    const int* start = st.cell_start + size_t(s) * (nc + 1);
+    if (a.mixed)
+        merge_append_kernel<float><<<(nc + 255) / 256, 256, 0, a.stream>>>(nc, start, st.mcount, st.moff, st.mstage,
+                                                                          a.sp[s], first);
+    else
+        merge_append_kernel<double><<<(nc + 255) / 256, 256, 0, a.stream>>>(nc, start, st.mcount, st.moff, st.mstage,
+                                                                           a.sp[s], first);
+    *launches += 1;
+    return cudaGetLastError() == cudaSuccess ? PICGPU_OK : PICGPU_CUDA_ERROR;
+}
+
+int merge_counters(CollideState& st, cudaStream_t s, long long* merged, long long* checked, double* kin_err) {
+    *merged = *checked = 0;
+    *kin_err = 0.0;
+    if (!st.mcounts) return PICGPU_OK;
+    unsigned long long h[2];
+    double k = 0.0;
+    if (cudaMemcpyAsync(h, st.mcounts, sizeof h, cudaMemcpyDeviceToHost, s) != cudaSuccess ||
+        cudaMemcpyAsync(&k, st.mkin, sizeof k, cudaMemcpyDeviceToHost, s) != cudaSuccess ||
+        cudaStreamSynchronize(s) != cudaSuccess)
+        return PICGPU_CUDA_ERROR;
+    cudaMemsetAsync(st.mcounts, 0, 2 * sizeof(unsigned long long), s);
+    cudaMemsetAsync(st.mkin, 0, sizeof(double), s);
+    *merged = (long long)h[0];
+    *checked = (long long)h[1];
+    *kin_err = k;
+    return PICGPU_OK;
+}
+
 
 }  // namespace pgd

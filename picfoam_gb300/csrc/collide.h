@@ -22,6 +22,27 @@ struct Secondary {
     double y_i[3];
 };
 
+// A parcel made by PairMerging, staged per cell until it is appended.
+struct MergedParcel {
+    int32_t tet;
+    int32_t pad;
+    double y[3];
+    double U[3];
+    double nw;
+};
+
+// An electron parcel added by a Perez ionisation, staged with its sort key
+// (cell << 32 | collision ordinal << 6 | ionisation level): appended in key
+// order, the order picFoam's sequential loop adds them in.
+struct PerezElectron {
+    unsigned long long key;
+    int32_t tet;
+    int32_t pad;
+    double y[3];
+    double U[3];
+    double nw;
+};
+
 // Counters of one collision step: background MCC candidates, elastic,
 // excitation, ionisation (0-3); Coulomb pairs (4); ion background MCC
 // candidates, elastic, charge exchange (5-7); binary (neutral) pairs tested,
@@ -29,7 +50,8 @@ struct Secondary {
 // by ionisation (12); electron - neutral parcel candidates, elastic,
 // excitation, ionisation (13-16); ion - neutral parcel candidates, elastic,
 // charge exchange (17-19).
-constexpr int kCollideCounts = 20;
+// Perez ionisation: ionising collisions, electrons added (20-21).
+constexpr int kCollideCounts = 22;
 constexpr int kCountMccParcel = 13;
 constexpr int kCountIonParcel = 17;
 
@@ -79,6 +101,25 @@ struct CollideState {
     int* blist = nullptr;
     int* boct = nullptr;
     long bcap = 0;
+    // PairMerging: parcel speeds in list order, staged merged parcels and
+    // their per-cell counts and offsets, counters (merged, checked) and the
+    // kinetic-energy change
+    double* mspeed = nullptr;
+    long mspeed_cap = 0;
+    MergedParcel* mstage = nullptr;
+    long mstage_cap = 0;
+    int* mcount = nullptr;
+    int* moff = nullptr;
+    unsigned long long* mcounts = nullptr;
+    double* mkin = nullptr;
+    // Perez ionisation: tables (cs, transferred, lost energy per charge
+    // state and 100 energies) per species, staged electrons and their count
+    double* ptab[PICGPU_MAX_SPECIES] = {};
+    int patomic[PICGPU_MAX_SPECIES] = {};
+    int plimit[PICGPU_MAX_SPECIES] = {};
+    PerezElectron* pstage = nullptr;
+    long pstage_cap = 0;
+    unsigned long long* pcount = nullptr;
 };
 
 struct CollideArgs {
@@ -115,5 +156,20 @@ int run_collisions(CollideState& st, const CollideArgs& a, int64_t counts[kColli
 int collide_reserve_device(CollideState& st, const CollideArgs& a, std::string* msg);
 int run_collisions_device(CollideState& st, const CollideArgs& a, int* n_dev, int* first_dev,
                           const unsigned* step_dev, std::string* msg, int64_t* launches);
+
+// PairMerging (PairMerging::mergeParticles, PairMerging.C:71-259) of species
+// s, entry li of the merge list, over the parcels in slots [0, a.n[s]) (the
+// cell occupancy of the step; parcels created by this step's collisions do
+// not take part): merged pairs are removed from the store (tet = -1) and the
+// new parcels staged; *total receives their number.  merge_append then
+// writes them to slots [first, first + total) of a.sp[s] (room reserved by
+// the caller), with nParticle and charge modifier 1 (PICCloud::addNewParcel).
+int merge_select(CollideState& st, const CollideArgs& a, int li, int s, long long* total, std::string* msg,
+                 int64_t* launches);
+int merge_append(CollideState& st, const CollideArgs& a, int s, long first, long long total, std::string* msg,
+                 int64_t* launches);
+// Merged parcels, candidates checked and the kinetic-energy change of the
+// merges since the last call (and resets them).
+int merge_counters(CollideState& st, cudaStream_t s, long long* merged, long long* checked, double* kin_err);
 
 }  // namespace pgd

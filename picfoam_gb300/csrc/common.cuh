@@ -94,6 +94,11 @@ struct DSpecies {
     double* u64[3];
     float* y32[3];
     float* u32[3];
+    // per-parcel weight and charge state (PICParcel nParticle_,
+    // chargeModifier_), or null: every parcel has the species weight and
+    // charge modifier 1
+    double* nw;
+    int32_t* zq;
 };
 
 // Counters written by the move kernels (one set per launch).
@@ -207,6 +212,10 @@ struct Philox {
 };
 
 enum : uint32_t {
+    // PairMerging per (merge-list entry, cell, step); high nibble 0, bit 27 clear
+    kStreamMerge = 0u,
+    // Perez ionisation per (Coulomb collision ordinal, cell, step)
+    kStreamIonize = 1u << 27,
     kStreamMcc = 1u << 28,
     kStreamCoulomb = 2u << 28,
     kStreamRemainder = 3u << 28,

@@ -514,11 +514,12 @@ __global__ void fill_kernel(double* a, long n, double v) {
 __global__ void diagnostics_kernel(const int32_t* __restrict__ tet, const double* __restrict__ u0,
                                    const double* __restrict__ u1, const double* __restrict__ u2,
                                    const float* __restrict__ f0, const float* __restrict__ f1,
-                                   const float* __restrict__ f2, int n, double mass, double weight,
-                                   double* out /* 10 */) {
+                                   const float* __restrict__ f2, int n, double mass, double species_weight,
+                                   const double* __restrict__ nw, double* out /* 10 */) {
     double ke = 0, ker = 0, mx = 0, my = 0, mz = 0, vx = 0, vy = 0, vz = 0, w = 0;
     for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
         if (tet[i] < 0) continue;
+        const double weight = nw ? nw[i] : species_weight;   // the parcel's nParticle
         const double a = u0 ? u0[i] : double(f0[i]);
         const double b = u0 ? u1[i] : double(f1[i]);
         const double c = u0 ? u2[i] : double(f2[i]);
@@ -641,10 +642,10 @@ void launch_fill(double* a, long n, double v, cudaStream_t s) {
 
 void launch_diagnostics(const int32_t* tet, const double* u0, const double* u1, const double* u2,
                         const float* f0, const float* f1, const float* f2, int n, double mass,
-                        double weight, double* out, cudaStream_t s) {
+                        double weight, const double* nw, double* out, cudaStream_t s) {
     if (n <= 0) return;
     diagnostics_kernel<<<std::min(blocks(n, 256), 1216), 256, 0, s>>>(tet, u0, u1, u2, f0, f1, f2, n, mass,
-                                                                       weight, out);
+                                                                       weight, nw, out);
 }
 
 void launch_field_energy(const double* E, const double* vol, int n, double* out, cudaStream_t s) {

@@ -71,7 +71,7 @@ void launch_to_float(const double* a, float* b, long n, cudaStream_t s);
 void launch_fill(double* a, long n, double v, cudaStream_t s);
 void launch_diagnostics(const int32_t* tet, const double* u0, const double* u1, const double* u2,
                         const float* f0, const float* f1, const float* f2, int n, double mass,
-                        double weight, double* out, cudaStream_t s);
+                        double weight, const double* nw, double* out, cudaStream_t s);
 void launch_field_energy(const double* E, const double* vol, int n, double* out, cudaStream_t s);
 
 }  // namespace pgd

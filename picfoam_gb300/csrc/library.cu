@@ -61,6 +61,11 @@ struct SpeciesBuf {
     double* u64[2][3] = {};
     float* y32[2][3] = {};
     float* u32[2][3] = {};
+    // per-parcel nParticle and chargeModifier (both halves), allocated when
+    // a caller sets them or a model (PairMerging, Perez ionisation) needs them
+    bool attrs = false;
+    double* nw[2] = {nullptr, nullptr};
+    int32_t* zq[2] = {nullptr, nullptr};
 };
 
 // Host <-> device copies of caller (pageable) arrays through a pinned ring of
@@ -438,12 +443,17 @@ picgpu_status alloc_species(picgpu_ctx* c, int s, long cap) {
             b.y32[k][a] = b.u32[k][a] = nullptr;
         }
         b.tet[k] = nullptr;
+        dfree(c, b.nw[k]);
+        dfree(c, b.zq[k]);
+        b.nw[k] = nullptr;
+        b.zq[k] = nullptr;
     }
     b.cap = cap;
     b.cur = 0;
     for (int k = 0; k < 2; ++k) {
         picgpu_status st = dalloc(c, &b.tet[k], cap);
         if (st) return st;
+        if (b.attrs && ((st = dalloc(c, &b.nw[k], cap)) || (st = dalloc(c, &b.zq[k], cap)))) return st;
         for (int a = 0; a < 3; ++a) {
             if (c->mixed) {
                 if ((st = dalloc(c, &b.y32[k][a], cap))) return st;
@@ -466,9 +476,11 @@ picgpu_status grow_species(picgpu_ctx* c, int s, long cap) {
     nb.n = old.n;
     nb.alive = old.alive;
     nb.cap = cap;
+    nb.attrs = old.attrs;
     picgpu_status st;
     for (int q = 0; q < 2; ++q) {
         if ((st = dalloc(c, &nb.tet[q], cap))) return st;
+        if (nb.attrs && ((st = dalloc(c, &nb.nw[q], cap)) || (st = dalloc(c, &nb.zq[q], cap)))) return st;
         for (int a = 0; a < 3; ++a) {
             if (c->mixed) {
                 if ((st = dalloc(c, &nb.y32[q][a], cap)) || (st = dalloc(c, &nb.u32[q][a], cap))) return st;
@@ -479,6 +491,10 @@ picgpu_status grow_species(picgpu_ctx* c, int s, long cap) {
     }
     const size_t n = size_t(old.n);
     CK(cudaMemcpyAsync(nb.tet[0], old.tet[k], n * sizeof(int32_t), cudaMemcpyDeviceToDevice, c->stream));
+    if (nb.attrs) {
+        CK(cudaMemcpyAsync(nb.nw[0], old.nw[k], n * sizeof(double), cudaMemcpyDeviceToDevice, c->stream));
+        CK(cudaMemcpyAsync(nb.zq[0], old.zq[k], n * sizeof(int32_t), cudaMemcpyDeviceToDevice, c->stream));
+    }
     for (int a = 0; a < 3; ++a) {
         if (c->mixed) {
             CK(cudaMemcpyAsync(nb.y32[0][a], old.y32[k][a], n * sizeof(float), cudaMemcpyDeviceToDevice, c->stream));
@@ -491,6 +507,8 @@ picgpu_status grow_species(picgpu_ctx* c, int s, long cap) {
     CK(cudaStreamSynchronize(c->stream));
     for (int q = 0; q < 2; ++q) {
         dfree(c, old.tet[q]);
+        dfree(c, old.nw[q]);
+        dfree(c, old.zq[q]);
         for (int a = 0; a < 3; ++a) {
             dfree(c, old.y64[q][a]); dfree(c, old.u64[q][a]); dfree(c, old.y32[q][a]); dfree(c, old.u32[q][a]);
         }
@@ -504,6 +522,8 @@ pgd::DSpecies view(const picgpu_ctx* c, int s, int k) {
     const SpeciesBuf& b = c->sp[s];
     pgd::DSpecies v{};
     v.tet = b.tet[k];
+    v.nw = b.attrs ? b.nw[k] : nullptr;
+    v.zq = b.attrs ? b.zq[k] : nullptr;
     for (int a = 0; a < 3; ++a) {
         v.y64[a] = b.y64[k][a];
         v.u64[a] = b.u64[k][a];
@@ -511,6 +531,25 @@ pgd::DSpecies view(const picgpu_ctx* c, int s, int k) {
         v.u32[a] = b.u32[k][a];
     }
     return v;
+}
+
+// Per-parcel attributes for species s: both halves of the store get the
+// arrays, the parcels stored so far the defaults (species weight, charge
+// modifier 1).
+picgpu_status enable_attributes(picgpu_ctx* c, int s) {
+    SpeciesBuf& b = c->sp[s];
+    if (b.attrs) return PICGPU_OK;
+    if (c->n_cases > 1 || !c->graphs.empty())
+        return bad(c, PICGPU_NOT_SUPPORTED, "per-parcel attributes are not supported with ensembles or graph steps");
+    picgpu_status st;
+    if (b.cap > 0)
+        for (int k = 0; k < 2; ++k)
+            if ((st = dalloc(c, &b.nw[k], size_t(b.cap))) || (st = dalloc(c, &b.zq[k], size_t(b.cap)))) return st;
+    b.attrs = true;
+    pgd::launch_fill_attributes(view(c, s, b.cur), 0, b.n, c->cfg.species[s].weight, c->stream);
+    CK(cudaStreamSynchronize(c->stream));
+    CK(cudaGetLastError());
+    return PICGPU_OK;
 }
 
 int grid_for(const picgpu_ctx* c, long n, int per_thread_block = 256) {
@@ -881,6 +920,7 @@ picgpu_status emit_parcels(picgpu_ctx* c, const Injector& I, int index, int patc
     P.error = c->inj_err;
     pgd::launch_inject(P, c->stream);
     c->launches++;
+    pgd::launch_fill_attributes(view(c, sp, B.cur), B.n, B.n + n, S.weight, c->stream);
     // syncVelocityAtBoundary(-0.5) of the new parcels (ParticleEmitter.C:401)
     if (c->cfg.sync_velocity_at_boundary && S.charge != 0.0 && c->cfg.pusher != PICGPU_PUSHER_NONE) {
         pgd::MoveParams MP = move_params(c, sp, false);
@@ -967,6 +1007,7 @@ picgpu_status inject(picgpu_ctx* c) {
             c->launches++;
             // syncVelocityAtBoundary(-0.5) of the new parcels (FreeStream.C:385)
             const picgpu_species& S = c->cfg.species[sp];
+            pgd::launch_fill_attributes(view(c, sp, B.cur), B.n, B.n + total, S.weight, c->stream);
             if (c->cfg.sync_velocity_at_boundary && S.charge != 0.0 && c->cfg.pusher != PICGPU_PUSHER_NONE) {
                 pgd::MoveParams MP = move_params(c, sp, false);
                 MP.first = int(B.n);
@@ -1003,6 +1044,48 @@ picgpu_status inject(picgpu_ctx* c) {
         if (st) return st;
     }
     CK(cudaGetLastError());
+    return PICGPU_OK;
+}
+
+// PairMerging over the listed species, in list order: each species' merges
+// are selected on its occupancy (slots [0, n_occ)), then the merged parcels
+// appended behind the store.
+picgpu_status merge_parcels(picgpu_ctx* c, picgpu_step_stats* stats, const long* n_occ) {
+    const picgpu_merging& mg = c->cfg.merging;
+    pgd::CollideArgs a{};
+    a.m = c->dm;
+    a.cfg = &c->cfg;
+    a.step = c->step_index;
+    a.n_species = c->cfg.n_species;
+    a.mixed = c->mixed;
+    a.stream = c->stream;
+    std::string msg;
+    for (int li = 0; li < mg.n_species; ++li) {
+        const int sp = mg.species[li];
+        SpeciesBuf& B = c->sp[sp];
+        a.sp[sp] = view(c, sp, B.cur);
+        a.n[sp] = std::min(n_occ[sp], B.n);
+        a.cap[sp] = B.cap;
+        long long total = 0;
+        int e = pgd::merge_select(c->coll, a, li, sp, &total, &msg, &c->launches);
+        if (e) return bad(c, picgpu_status(e), msg);
+        if (total <= 0) continue;
+        picgpu_status st = reserve_species(c, sp, total);
+        if (st) return st;
+        a.sp[sp] = view(c, sp, B.cur);
+        e = pgd::merge_append(c->coll, a, sp, B.n, total, &msg, &c->launches);
+        if (e) return bad(c, picgpu_status(e), msg);
+        B.n += total;
+        B.alive -= total;   // two parcels out, one in, per merge
+    }
+    long long merged = 0, checked = 0;
+    double kin = 0.0;
+    if (pgd::merge_counters(c->coll, c->stream, &merged, &checked, &kin)) CK(cudaGetLastError());
+    if (stats) {
+        stats->merged_parcels += merged;
+        stats->merge_checks += checked;
+        stats->merge_kinetic_energy_error += kin;
+    }
     return PICGPU_OK;
 }
 
@@ -1043,6 +1126,10 @@ picgpu_status one_step(picgpu_ctx* c, picgpu_step_stats* stats, bool fields) {
     } else if ((s = compact(c, false))) {
         return s;
     }
+    // the parcels of the cell occupancy (PICCloud::buildCellOccupancy):
+    // collision secondaries of this step come after them
+    long n_occ[PICGPU_MAX_SPECIES] = {};
+    for (int k = 0; k < c->cfg.n_species; ++k) n_occ[k] = c->sp[k].n;
     if (c->cfg.mcc.enabled || c->cfg.coulomb.enabled || c->cfg.ion_mcc.enabled || c->cfg.binary.enabled) {
         if ((s = pgd_collisions(c, stats))) return s;
     }
@@ -1064,6 +1151,8 @@ picgpu_status one_step(picgpu_ctx* c, picgpu_step_stats* stats, bool fields) {
                                  c->stream);
         c->launches++;
     }
+    // ParticleMerging::checkAndMerge, the last call of the step (PICCloud.C:1470)
+    if (c->cfg.merging.enabled && (s = merge_parcels(c, stats, n_occ))) return s;
     c->step_index++;
     return PICGPU_OK;
 }
@@ -1109,6 +1198,12 @@ picgpu_status pgd_collisions(picgpu_ctx* c, picgpu_step_stats* stats) {
         c->sp[s].n = newn[s];
         c->sp[s].alive += newn[s] - old;
         if (newn[s] > old) {
+            // parcels created by the MCC models carry the species defaults
+            // (PICCloud::addNewParcel, PICCloud.C:707-723); the electrons of
+            // Perez ionisations, appended first, have their own nParticle
+            const long own = s == c->cfg.electron_species ? long(counts[21]) : 0;
+            pgd::launch_fill_attributes(view(c, s, c->sp[s].cur), old + own, newn[s], c->cfg.species[s].weight,
+                                        c->stream);
             // deposit the secondaries created this step (calculateFields sees
             // every parcel, PICCloud.C:616-660)
             pgd::MoveParams P = move_params(c, s, true);
@@ -1128,6 +1223,8 @@ picgpu_status pgd_collisions(picgpu_ctx* c, picgpu_step_stats* stats) {
         stats->mcc_excitation += counts[2];
         stats->mcc_ionization += counts[3];
         stats->coulomb_pairs += counts[4];
+        stats->coulomb_ionizations += counts[20];
+        stats->coulomb_ionization_electrons += counts[21];
         stats->ion_mcc_candidates += counts[5];
         stats->ion_mcc_elastic += counts[6];
         stats->ion_mcc_charge_exchange += counts[7];
@@ -1758,6 +1855,20 @@ static picgpu_status create_with_mesh(picgpu_ctx* c, const picgpu_config* cfg) {
     std::string msg;
     const int cs = pgd::collide_init(c->coll, c->cfg, c->dm, c->stream, &msg);
     if (cs) return bad(c, picgpu_status(cs), msg);
+    if (cfg->perez.enabled) {
+        // ionisation raises an ion's charge modifier and adds electrons with
+        // the ion's nParticle (PerezIonizationModel.C:336-346)
+        if (c->n_cases > 1) return bad(c, PICGPU_NOT_SUPPORTED, "Perez ionisation is not supported with ensembles");
+        if ((s = enable_attributes(c, cfg->electron_species))) return s;
+        for (int k = 0; k < cfg->perez.n_ions; ++k)
+            if ((s = enable_attributes(c, cfg->perez.ion[k].species))) return s;
+    }
+    if (cfg->merging.enabled) {
+        // merged parcels carry their summed nParticle (PairMerging.C:210-214)
+        if (c->n_cases > 1) return bad(c, PICGPU_NOT_SUPPORTED, "PairMerging is not supported with ensembles");
+        for (int k = 0; k < cfg->merging.n_species; ++k)
+            if ((s = enable_attributes(c, cfg->merging.species[k]))) return s;
+    }
     if (cfg->learned.enabled) {
         if (cfg->maxwell_solver != PICGPU_MAXWELL_ELECTROSTATIC)
             return bad(c, PICGPU_INVALID_ARG, "learned warm start needs the electrostatic Maxwell solver");
@@ -1863,6 +1974,8 @@ picgpu_status picgpu_set_particles(picgpu_ctx* c, int species, size_t n, const i
     B.n = long(n);
     B.alive = long(n);
     pgd::launch_scatter_rows(c->rows_tet, c->rows_y, c->rows_u, long(n), view(c, species, 0), c->mixed, c->stream);
+    // new parcels: the species weight and charge modifier 1
+    pgd::launch_fill_attributes(view(c, species, 0), 0, long(n), c->cfg.species[species].weight, c->stream);
     CK(cudaStreamSynchronize(c->stream));
     CK(cudaGetLastError());
     return PICGPU_OK;
@@ -1907,9 +2020,74 @@ picgpu_status picgpu_get_particles(picgpu_ctx* c, int species, size_t cap, int32
     return PICGPU_OK;
 }
 
+picgpu_status picgpu_set_parcel_attributes(picgpu_ctx* c, int species, size_t n, const double* nParticle,
+                                           const int32_t* chargeModifier) {
+    if (!c || species < 0 || species >= c->cfg.n_species) return PICGPU_INVALID_ARG;
+    if (n && (!nParticle || !chargeModifier)) return PICGPU_INVALID_ARG;
+    SpeciesBuf& B = c->sp[species];
+    const double w = c->cfg.species[species].weight;
+    for (size_t i = 0; i < n; ++i) {
+        // a parcel's weight multiple of the species weight and its charge
+        // modifier scale the fixed-point charge deposit: both are bounded
+        if (!(nParticle[i] > 0.0) || !(nParticle[i] <= 4096.0 * w) || chargeModifier[i] < 0 ||
+            chargeModifier[i] > 1024)
+            return bad(c, PICGPU_INVALID_ARG,
+                       "parcel attributes: nParticle in (0, 4096 w] and chargeModifier in [0, 1024]");
+    }
+    CK(cudaStreamSynchronize(c->stream));
+    // the attributes follow the order of picgpu_get_particles: the store is
+    // compacted first
+    picgpu_status st;
+    if ((st = compact(c, true))) return st;
+    if (size_t(B.n) != n) return bad(c, PICGPU_INVALID_ARG, "parcel attributes: n differs from the parcel count");
+    if ((st = enable_attributes(c, species))) return st;
+    if (n) {
+        CK(cudaMemcpyAsync(B.nw[B.cur], nParticle, n * sizeof(double), cudaMemcpyHostToDevice, c->stream));
+        CK(cudaMemcpyAsync(B.zq[B.cur], chargeModifier, n * sizeof(int32_t), cudaMemcpyHostToDevice, c->stream));
+    }
+    CK(cudaStreamSynchronize(c->stream));
+    return PICGPU_OK;
+}
+
+picgpu_status picgpu_get_parcel_attributes(picgpu_ctx* c, int species, size_t cap, double* nParticle,
+                                           int32_t* chargeModifier, size_t* nout) {
+    if (!c || !nout || species < 0 || species >= c->cfg.n_species) return PICGPU_INVALID_ARG;
+    CK(cudaStreamSynchronize(c->stream));
+    SpeciesBuf& B = c->sp[species];
+    picgpu_status st;
+    if ((st = compact(c, true))) return st;
+    *nout = size_t(B.n);
+    if (!nParticle) return PICGPU_OK;
+    if (cap < size_t(B.n) || !chargeModifier) return PICGPU_INVALID_ARG;
+    if (!B.attrs) {
+        for (long i = 0; i < B.n; ++i) {
+            nParticle[i] = c->cfg.species[species].weight;
+            chargeModifier[i] = 1;
+        }
+        return PICGPU_OK;
+    }
+    if (B.n) {
+        CK(cudaMemcpyAsync(nParticle, B.nw[B.cur], size_t(B.n) * sizeof(double), cudaMemcpyDeviceToHost, c->stream));
+        CK(cudaMemcpyAsync(chargeModifier, B.zq[B.cur], size_t(B.n) * sizeof(int32_t), cudaMemcpyDeviceToHost,
+                           c->stream));
+    }
+    CK(cudaStreamSynchronize(c->stream));
+    return PICGPU_OK;
+}
+
 picgpu_status picgpu_set_step_index(picgpu_ctx* c, int64_t steps_done) {
     if (!c || steps_done < 0) return PICGPU_INVALID_ARG;
     c->step_index = steps_done;
+    return PICGPU_OK;
+}
+
+picgpu_status picgpu_compute_field(picgpu_ctx* c) {
+    if (!c) return PICGPU_INVALID_ARG;
+    picgpu_status s;
+    if (c->cfg.maxwell_solver != PICGPU_MAXWELL_ELECTROSTATIC) return PICGPU_OK;
+    if ((s = efield(c))) return s;
+    CK(cudaStreamSynchronize(c->stream));
+    if (c->profiling) harvest_events(c);
     return PICGPU_OK;
 }
 
@@ -2297,6 +2475,7 @@ picgpu_status picgpu_initialise(picgpu_ctx* c, const picgpu_init* in, picgpu_ini
                        e == 2 ? "initialise: more than 2^24 particles in one tet"
                               : "initialise: tried to create a particle outside of the mesh");
         }
+        pgd::launch_fill_attributes(view(c, sp, B.cur), B.n, B.n + total, c->cfg.species[sp].weight, c->stream);
         B.n += total;
         B.alive += total;
         S.added[sp] = total;
@@ -2323,7 +2502,7 @@ picgpu_status picgpu_initialise(picgpu_ctx* c, const picgpu_init* in, picgpu_ini
         CK(cudaMemsetAsync(c->diag, 0, 10 * sizeof(double), c->stream));
         const pgd::DSpecies v = view(c, sp, B.cur);
         pgd::launch_diagnostics(v.tet, v.u64[0], v.u64[1], v.u64[2], v.u32[0], v.u32[1], v.u32[2], int(B.n),
-                                P.mass, P.weight, c->diag, c->stream);
+                                P.mass, P.weight, v.nw, c->diag, c->stream);
         double d[10];
         CK(cudaMemcpyAsync(d, c->diag, sizeof d, cudaMemcpyDeviceToHost, c->stream));
         CK(cudaStreamSynchronize(c->stream));
@@ -2609,7 +2788,8 @@ picgpu_status picgpu_diagnostics_compute(picgpu_ctx* c, picgpu_diagnostics* out)
         pgd::launch_diagnostics(B.tet[B.cur], c->mixed ? nullptr : B.u64[B.cur][0],
                                 c->mixed ? nullptr : B.u64[B.cur][1], c->mixed ? nullptr : B.u64[B.cur][2],
                                 B.u32[B.cur][0], B.u32[B.cur][1], B.u32[B.cur][2], int(B.n),
-                                c->cfg.species[s].mass, c->cfg.species[s].weight, c->diag + 10 * s, c->stream);
+                                c->cfg.species[s].mass, c->cfg.species[s].weight,
+                                B.attrs ? B.nw[B.cur] : nullptr, c->diag + 10 * s, c->stream);
         c->launches++;
     }
     pgd::launch_field_energy(c->E, c->dm.vol, c->m.n_cells, c->diag + 60, c->stream);

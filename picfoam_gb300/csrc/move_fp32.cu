@@ -43,7 +43,29 @@ struct S32 {
     int cell, tet;
     float y[4];
     float U[3];
+    float zf;   // charge modifier (1 without per-parcel attributes)
+    float dm;   // deposit multiple: chargeModifier x nParticle / species weight (1 without)
 };
+
+// The parcel's charge modifier and deposit multiple: from the store's
+// per-parcel attributes in the kernels built for them (ATTRS), else the
+// constants 1 and 1, which the compiler folds away.
+template <bool ATTRS>
+__device__ __forceinline__ void load_attributes32(const MoveParams& P, int i, S32& s) {
+    if (ATTRS) {
+        const int z = P.p.zq[i];
+        s.zf = float(z);
+        s.dm = float(double(z) * P.p.nw[i] / P.weight);
+    } else {
+        s.zf = 1.f;
+        s.dm = 1.f;
+    }
+}
+
+// Charge a parcel leaves on a floating or circuit patch: nParticle x charge.
+__device__ __forceinline__ double parcel_charge(const MoveParams& P, const S32& s) {
+    return double(s.dm) * P.weight * P.q;
+}
 
 __device__ __forceinline__ void field32(const MoveParams& P, const unsigned* tri_of, const S32& s, float* E) {
     const float4* e = P.Ec4 + 9 * s.cell;
@@ -81,11 +103,12 @@ __device__ __forceinline__ float one_less_inv_gamma(float b) {
 
 // Relativistic Boris (BorisPusher.C:69-112) in FP32: the Lorentz factor of
 // the incoming velocity is reused for the averaged factor of the rotation.
-__device__ __forceinline__ void boris32(const MoveParams& P, const float* E, const float* Bv, float* U, float tt) {
+__device__ __forceinline__ void boris32(const MoveParams& P, const float* E, const float* Bv, float* U, float tt,
+                                        float zf) {
     constexpr float ic2 = float(1.0 / (kC * kC));
     const float dg_in = gamma_less_one((U[0] * U[0] + U[1] * U[1] + U[2] * U[2]) * ic2);
     float r0 = U[0] + U[0] * dg_in, r1 = U[1] + U[1] * dg_in, r2 = U[2] + U[2] * dg_in;
-    const float qdm = P.qm_f * (0.5f * tt);
+    const float qdm = P.qm_f * zf * (0.5f * tt);
     const float e0 = qdm * E[0], e1 = qdm * E[1], e2 = qdm * E[2];
     r0 += e0; r1 += e1; r2 += e2;
     if (P.rotation) {
@@ -108,10 +131,11 @@ __device__ __forceinline__ void boris32(const MoveParams& P, const float* E, con
 
 // VayPusher::updateVelocity (VayPusher.C:54-100) in FP32, U x T with v
 // (VayPusher.C:81), the Lorentz factors of the conversions as above.
-__device__ __forceinline__ void vay32(const MoveParams& P, const float* E, const float* Bv, float* U, float tt) {
+__device__ __forceinline__ void vay32(const MoveParams& P, const float* E, const float* Bv, float* U, float tt,
+                                      float zf) {
     constexpr float ic = float(1.0 / kC), ic2 = float(1.0 / (kC * kC));
     const float dg = gamma_less_one((U[0] * U[0] + U[1] * U[1] + U[2] * U[2]) * ic2);
-    const float qe = P.qm_f * tt, qb = P.qm_f * (0.5f * tt);
+    const float qe = P.qm_f * zf * tt, qb = P.qm_f * zf * (0.5f * tt);
     float u0 = U[0] + U[0] * dg + qe * E[0], u1 = U[1] + U[1] * dg + qe * E[1], u2 = U[2] + U[2] * dg + qe * E[2];
     float T0 = qb * Bv[0], T1 = qb * Bv[1], T2 = qb * Bv[2];
     u0 += U[1] * T2 - U[2] * T1;
@@ -134,11 +158,12 @@ __device__ __forceinline__ void vay32(const MoveParams& P, const float* E, const
 
 // HigueraCaryPusher::updateVelocity (HigueraCary.C:69-115) in FP32, the
 // Lorentz factors of the conversions as above.
-__device__ __forceinline__ void hc32(const MoveParams& P, const float* E, const float* Bv, float* U, float tt) {
+__device__ __forceinline__ void hc32(const MoveParams& P, const float* E, const float* Bv, float* U, float tt,
+                                     float zf) {
     constexpr float ic2 = float(1.0 / (kC * kC));
     const float dg = gamma_less_one((U[0] * U[0] + U[1] * U[1] + U[2] * U[2]) * ic2);
     float r0 = U[0] + U[0] * dg, r1 = U[1] + U[1] * dg, r2 = U[2] + U[2] * dg;
-    const float qdm = P.qm_f * (0.5f * tt);
+    const float qdm = P.qm_f * zf * (0.5f * tt);
     const float e0 = qdm * E[0], e1 = qdm * E[1], e2 = qdm * E[2];
     r0 += e0; r1 += e1; r2 += e2;
     if (P.rotation) {
@@ -179,10 +204,10 @@ __device__ __forceinline__ void push32(const MoveParams& P, const unsigned* tri_
         Bv[1] = P.B_f[1];
         Bv[2] = P.B_f[2];
     }
-    if (PUSHER == PICGPU_PUSHER_BORIS) boris32(P, E, Bv, s.U, tt);
-    else if (PUSHER == PICGPU_PUSHER_BORIS_NR) push_boris_nr<float>(P, E, Bv, s.U, tt);
-    else if (PUSHER == PICGPU_PUSHER_VAY) vay32(P, E, Bv, s.U, tt);
-    else if (PUSHER == PICGPU_PUSHER_HIGUERA_CARY) hc32(P, E, Bv, s.U, tt);
+    if (PUSHER == PICGPU_PUSHER_BORIS) boris32(P, E, Bv, s.U, tt, s.zf);
+    else if (PUSHER == PICGPU_PUSHER_BORIS_NR) push_boris_nr<float>(P, E, Bv, s.U, tt, s.zf);
+    else if (PUSHER == PICGPU_PUSHER_VAY) vay32(P, E, Bv, s.U, tt, s.zf);
+    else if (PUSHER == PICGPU_PUSHER_HIGUERA_CARY) hc32(P, E, Bv, s.U, tt, s.zf);
 }
 
 __device__ __forceinline__ void remap(unsigned code, S32& s) {
@@ -221,7 +246,7 @@ struct Tally {
 // the particle reached the speed of light (it is then removed).
 template <int PUSHER>
 __device__ __forceinline__ bool push_phase(const MoveParams& P, const Tables32& T, S32& s, Tally& td) {
-    if (P.charged) push32<PUSHER>(P, T.tri, s, P.dt_f);
+    if (P.charged && s.zf != 0.f) push32<PUSHER>(P, T.tri, s, P.dt_f);
     if (!(s.U[0] * s.U[0] + s.U[1] * s.U[1] + s.U[2] * s.U[2] < float(kC) * float(kC))) {
         td.keep = false;
         atomicMax(&P.counters->error, int(PICGPU_SPEED_OF_LIGHT));
@@ -303,7 +328,7 @@ __device__ __forceinline__ void track32(const MoveParams& P, const Tables32& T, 
         if (kind == PICGPU_PATCH_ABSORB) { td.keep = false; return; }
         if (kind == PICGPU_PATCH_FLOATING || (kind == PICGPU_PATCH_CIRCUIT && P.q != 0.0)) {
             td.keep = false;
-            atomicAdd(P.qconv + patch, P.weight * P.q);
+            atomicAdd(P.qconv + patch, parcel_charge(P, s));
             return;
         }
         const float sf = base + (1.f - base) * (1.f - rem);
@@ -312,7 +337,7 @@ __device__ __forceinline__ void track32(const MoveParams& P, const Tables32& T, 
             P.m.uniform ? T.normal + 3 * f : P.m.fnormal32 + size_t(P.m.cell_class[s.cell]) * 18 + 3 * f;
         const bool wall = kind == PICGPU_PATCH_WALL || kind == PICGPU_PATCH_CIRCUIT;
         if (wall) {
-            if (P.sync && P.charged) push32<PUSHER>(P, T.tri, s, (sf - 0.5f) * dt);
+            if (P.sync && P.charged && s.zf != 0.f) push32<PUSHER>(P, T.tri, s, (sf - 0.5f) * dt);
             td.walls++;
         }
         const float Un = s.U[0] * n[0] + s.U[1] * n[1] + s.U[2] * n[2];
@@ -322,7 +347,7 @@ __device__ __forceinline__ void track32(const MoveParams& P, const Tables32& T, 
             s.U[1] -= t * n[1];
             s.U[2] -= t * n[2];
         }
-        if (wall && ++resync <= 1 && P.sync && P.charged) push32<PUSHER>(P, T.tri, s, (0.5f - sf) * dt);
+        if (wall && ++resync <= 1 && P.sync && P.charged && s.zf != 0.f) push32<PUSHER>(P, T.tri, s, (0.5f - sf) * dt);
         base = sf;
         rem = 1.f;
         displacement(P, T, s, (1.f - sf) * dt, disp);
@@ -344,15 +369,36 @@ __device__ __forceinline__ void win_add(unsigned* slot, unsigned long long* gslo
     if (old + v < old) atomicAdd(gslot, 1ull << 32);
 }
 
+// A parcel whose deposit multiple exceeds 64 (merged or multiply charged
+// parcels with per-parcel attributes): its fixed-point weights may pass
+// 2^31, so they go straight to the 64-bit cell slots.
+__device__ __noinline__ void deposit_heavy32(const MoveParams& P, const unsigned* tri_of, const S32& s) {
+    const float sc = float(1u << kDepositBits) * s.dm;
+    unsigned long long* g = P.acc9 + 9 * size_t(s.cell);
+    if (P.charge_distribution == PICGPU_WEIGHTING_CELL_AVERAGE) {
+        atomicAdd(g, __float2ull_rn(sc));
+        return;
+    }
+    const unsigned tri = tri_of[s.tet];
+    atomicAdd(g, __float2ull_rn(s.y[0] * sc));
+    atomicAdd(g + 1 + (tri & 15u), __float2ull_rn(s.y[1] * sc));
+    atomicAdd(g + 1 + ((tri >> 4) & 15u), __float2ull_rn(s.y[2] * sc));
+    atomicAdd(g + 1 + ((tri >> 8) & 15u), __float2ull_rn(s.y[3] * sc));
+}
+
 __device__ __forceinline__ void deposit32(const MoveParams& P, const unsigned* tri_of, const S32& s, int w0,
                                           unsigned* win) {
     if (!P.has_value) return;
-    constexpr float kScale = float(1u << kDepositBits);
+    if (s.dm > 64.f) {
+        deposit_heavy32(P, tri_of, s);
+        return;
+    }
+    const float kScale = float(1u << kDepositBits) * s.dm;
     const int rel = s.cell - w0;
     unsigned long long* g = P.acc9 + 9 * size_t(s.cell);
     const bool average = P.charge_distribution == PICGPU_WEIGHTING_CELL_AVERAGE;
     const unsigned tri = tri_of[s.tet];
-    const unsigned w0v = average ? (1u << kDepositBits) : __float2uint_rn(s.y[0] * kScale);
+    const unsigned w0v = average ? __float2uint_rn(kScale) : __float2uint_rn(s.y[0] * kScale);
     if (unsigned(rel) < unsigned(kWindow)) {
         unsigned* a = win + 9 * rel;
         win_add(a, g, w0v);
@@ -381,12 +427,16 @@ constexpr int kCellWindow = 768;
 __device__ __forceinline__ void deposit_cell32(const MoveParams& P, const unsigned* tri_of, const S32& s, int w0,
                                                unsigned* win) {
     if (!P.has_value) return;
-    constexpr float kScale = float(1u << kDepositBits);
+    if (s.dm > 64.f) {
+        deposit_heavy32(P, tri_of, s);
+        return;
+    }
+    const float kScale = float(1u << kDepositBits) * s.dm;
     const int rel = s.cell - w0;
     unsigned long long* g = P.acc9 + 9 * size_t(s.cell);
     const bool average = P.charge_distribution == PICGPU_WEIGHTING_CELL_AVERAGE;
     const unsigned tri = tri_of[s.tet];
-    const unsigned w0v = average ? (1u << kDepositBits) : __float2uint_rn(s.y[0] * kScale);
+    const unsigned w0v = average ? __float2uint_rn(kScale) : __float2uint_rn(s.y[0] * kScale);
     if (unsigned(rel) < unsigned(kCellWindow)) {
         unsigned* a = win + kCellSlots * rel;
         win_add(a + (threadIdx.x & (kCellSub - 1)), g, w0v);
@@ -424,7 +474,7 @@ __device__ __forceinline__ Rec load_rec(const DSpecies& p, int i) {
 // Each block moves one contiguous chunk of the store, 256 particles per
 // tile; the next tile's records are loaded before the current tile is
 // processed, so their DRAM latency overlaps the push and the tracking.
-template <int PUSHER>
+template <int PUSHER, bool ATTRS>
 __global__ void __launch_bounds__(256, 5) move_kernel_fp32(MoveParams P, int chunk) {
     __shared__ Tables32 T;
     extern __shared__ unsigned win[];  // kWindow * 9 slots (32-bit, carry to global)
@@ -477,6 +527,7 @@ __global__ void __launch_bounds__(256, 5) move_kernel_fp32(MoveParams P, int chu
         s.U[0] = r.u0;
         s.U[1] = r.u1;
         s.U[2] = r.u2;
+        load_attributes32<ATTRS>(P, ci, s);
         Tally td{0u, 0u, 0u, true};
         if (P.solve_movement) move32<PUSHER>(P, T, s, td);
         ts += td.tet_steps;
@@ -590,7 +641,7 @@ __device__ __forceinline__ void store_rec(const DSpecies& p, int i, const S32& s
 // back and joins the block's segment of the crossing queue, whose tracker
 // repeats its step with the wall's velocity sync.  The in-cell path uses
 // selects only (no indexed registers, no calls), so it needs no stack.
-template <int PUSHER>
+template <int PUSHER, bool ATTRS>
 __global__ void __launch_bounds__(256, 5) move_cell_kernel_fp32(MoveParams P, int chunk) {
     __shared__ unsigned tri_s[12];
     __shared__ int kind_s[kMaxPatches];
@@ -650,13 +701,14 @@ __global__ void __launch_bounds__(256, 5) move_cell_kernel_fp32(MoveParams P, in
         s.U[0] = r.u0;
         s.U[1] = r.u1;
         s.U[2] = r.u2;
+        load_attributes32<ATTRS>(P, ci, s);
         // the outcome: 0 moved, 1 removed, 2 at a reflecting patch (queued).
         // The rare outcomes set flags only, so the common tail below runs
         // once for the warp, whatever its lanes met on the way.
         int fate = 0;
         unsigned faces = 0;
         if (P.solve_movement) {
-            if (P.charged) push32<PUSHER>(P, tri_s, s, P.dt_f);
+            if (P.charged && s.zf != 0.f) push32<PUSHER>(P, tri_s, s, P.dt_f);
             if (!(s.U[0] * s.U[0] + s.U[1] * s.U[1] + s.U[2] * s.U[2] < float(kC) * float(kC))) {
                 atomicMax(&P.counters->error, int(PICGPU_SPEED_OF_LIGHT));
                 fate = 1;
@@ -675,10 +727,11 @@ __global__ void __launch_bounds__(256, 5) move_cell_kernel_fp32(MoveParams P, in
                 e1 = x1 + d1;
                 e2 = x2 + d2;
                 const bool out0 = fabsf(e0) > 0.5f, out1 = fabsf(e1) > 0.5f, out2 = fabsf(e2) > 0.5f;
-                if (int(out0) + int(out1) + int(out2) == 1) {
-                    // through one face: into the neighbour, whose frame is this
-                    // one shifted by a cell along the axis; a patch decides
-                    // without the crossing time
+                if (int(out0) + int(out1) + int(out2) == 1 && fmaxf(fabsf(e0), fmaxf(fabsf(e1), fabsf(e2))) <= 1.5f) {
+                    // through one face and no further than the neighbour: into
+                    // the neighbour, whose frame is this one shifted by a cell
+                    // along the axis; a patch decides without the crossing
+                    // time.  A longer step along one axis takes the loop below.
                     const int ax = out0 ? 0 : out1 ? 1 : 2;
                     const float ea = out0 ? e0 : out1 ? e1 : e2;
                     const int nb = __ldg(P.m.nbr + 6 * s.cell + 2 * ax + (ea > 0.f ? 1 : 0));
@@ -694,7 +747,7 @@ __global__ void __launch_bounds__(256, 5) move_cell_kernel_fp32(MoveParams P, in
                         const int kind = kind_s[patch];
                         fate = 1;
                         if (kind == PICGPU_PATCH_FLOATING || (kind == PICGPU_PATCH_CIRCUIT && P.q != 0.0))
-                            atomicAdd(P.qconv + patch, P.weight * P.q);
+                            atomicAdd(P.qconv + patch, parcel_charge(P, s));
                         else if (kind != PICGPU_PATCH_ABSORB)
                             fate = 2;
                     }
@@ -737,7 +790,7 @@ __global__ void __launch_bounds__(256, 5) move_cell_kernel_fp32(MoveParams P, in
                             const int kind = kind_s[patch];
                             fate = 1;
                             if (kind == PICGPU_PATCH_FLOATING || (kind == PICGPU_PATCH_CIRCUIT && P.q != 0.0))
-                                atomicAdd(P.qconv + patch, P.weight * P.q);
+                                atomicAdd(P.qconv + patch, parcel_charge(P, s));
                             else if (kind != PICGPU_PATCH_ABSORB)
                                 fate = 2;
                             break;
@@ -807,24 +860,14 @@ __global__ void __launch_bounds__(256, 5) move_cell_kernel_fp32(MoveParams P, in
 // Charge deposit straight into the global accumulators.
 __device__ __forceinline__ void deposit_global32(const MoveParams& P, const unsigned* tri_of, const S32& s) {
     if (!P.has_value) return;
-    constexpr float kScale = float(1u << kDepositBits);
-    unsigned long long* g = P.acc9 + 9 * size_t(s.cell);
-    if (P.charge_distribution == PICGPU_WEIGHTING_CELL_AVERAGE) {
-        atomicAdd(g, (unsigned long long)(1u << kDepositBits));
-        return;
-    }
-    const unsigned tri = tri_of[s.tet];
-    atomicAdd(g, (unsigned long long)__float2uint_rn(s.y[0] * kScale));
-    atomicAdd(g + 1 + (tri & 15u), (unsigned long long)__float2uint_rn(s.y[1] * kScale));
-    atomicAdd(g + 1 + ((tri >> 4) & 15u), (unsigned long long)__float2uint_rn(s.y[2] * kScale));
-    atomicAdd(g + 1 + ((tri >> 8) & 15u), (unsigned long long)__float2uint_rn(s.y[3] * kScale));
+    deposit_heavy32(P, tri_of, s);
 }
 
 // The particles the in-cell mover queued, block b of this grid taking block
 // b's segment: barycentric tracking from the start position with the pushed
 // velocity (PICParcel::moveForward: cell faces, patches, velocity sync),
 // then store and deposit.
-template <int PUSHER>
+template <int PUSHER, bool ATTRS>
 __global__ void __launch_bounds__(256) track_queue_kernel_fp32(MoveParams P) {
     __shared__ Tables32 T;
     const int cnt = P.xq.count[blockIdx.x];
@@ -850,6 +893,7 @@ __global__ void __launch_bounds__(256) track_queue_kernel_fp32(MoveParams P) {
         s.U[0] = r.u0;
         s.U[1] = r.u1;
         s.U[2] = r.u2;
+        load_attributes32<ATTRS>(P, i, s);
         Tally td{0u, 0u, 0u, true};
         track32<PUSHER>(P, T, s, td);
         ts += td.tet_steps;
@@ -869,18 +913,25 @@ __global__ void __launch_bounds__(256) track_queue_kernel_fp32(MoveParams P) {
     warp_add_counter<float>(&P.counters->absorbed, ab);
 }
 
-template <int PUSHER>
-int launch_pusher(const MoveParams& P, int blocks, int chunk, bool cell, cudaStream_t s) {
+template <int PUSHER, bool ATTRS>
+int launch_kernels(const MoveParams& P, int blocks, int chunk, bool cell, cudaStream_t s) {
     const size_t smem = size_t(kWindow) * 9 * sizeof(unsigned);
     if (!cell) {
-        move_kernel_fp32<PUSHER><<<blocks, 256, smem, s>>>(P, chunk);
+        move_kernel_fp32<PUSHER, ATTRS><<<blocks, 256, smem, s>>>(P, chunk);
         return 1;
     }
     const size_t cell_smem = size_t(kCellWindow) * kCellSlots * sizeof(unsigned);
-    move_cell_kernel_fp32<PUSHER><<<blocks, 256, cell_smem, s>>>(P, chunk);
+    move_cell_kernel_fp32<PUSHER, ATTRS><<<blocks, 256, cell_smem, s>>>(P, chunk);
     if (!P.solve_movement || !P.reflecting) return 1;
-    track_queue_kernel_fp32<PUSHER><<<blocks, 256, 0, s>>>(P);
+    track_queue_kernel_fp32<PUSHER, ATTRS><<<blocks, 256, 0, s>>>(P);
     return 2;
+}
+
+// Stores with per-parcel attributes take the kernels that read them.
+template <int PUSHER>
+int launch_pusher(const MoveParams& P, int blocks, int chunk, bool cell, cudaStream_t s) {
+    return P.p.nw ? launch_kernels<PUSHER, true>(P, blocks, chunk, cell, s)
+                  : launch_kernels<PUSHER, false>(P, blocks, chunk, cell, s);
 }
 
 }  // namespace

@@ -45,6 +45,7 @@ __global__ void __launch_bounds__(256) push_only_kernel(MoveParams P, Real tt) {
         s.U[0] = ubuf<Real>(P.p, 0)[i];
         s.U[1] = ubuf<Real>(P.p, 1)[i];
         s.U[2] = ubuf<Real>(P.p, 2)[i];
+        load_attributes(P, i, s);
         push<Real>(P, c_tet64, s, tt);
         ubuf<Real>(P.p, 0)[i] = s.U[0];
         ubuf<Real>(P.p, 1)[i] = s.U[1];

@@ -31,8 +31,10 @@ template <class Real> struct PC;
 template <> struct PC<double> {
     static __device__ __forceinline__ double dt(const MoveParams& P) { return P.dt; }
     static __device__ __forceinline__ double B(const MoveParams& P, int a) { return P.B[a]; }
-    static __device__ __forceinline__ double qdm(const MoveParams& P, double half_dt) {
-        return P.q * half_dt / P.mass;
+    // the parcel's charge is the species charge times its charge modifier zf
+    // (PICCloud.C:368); zf = 1 leaves q dt/2 / m as it is
+    static __device__ __forceinline__ double qdm(const MoveParams& P, double half_dt, double zf) {
+        return P.q * zf * half_dt / P.mass;
     }
     static __device__ __forceinline__ double centre(const MoveParams& P, int a) { return P.m.mesh_centre[a]; }
     static __device__ __forceinline__ double cc(const MoveParams& P, int c, int a) {
@@ -42,7 +44,9 @@ template <> struct PC<double> {
 template <> struct PC<float> {
     static __device__ __forceinline__ float dt(const MoveParams& P) { return P.dt_f; }
     static __device__ __forceinline__ float B(const MoveParams& P, int a) { return P.B_f[a]; }
-    static __device__ __forceinline__ float qdm(const MoveParams& P, float half_dt) { return P.qm_f * half_dt; }
+    static __device__ __forceinline__ float qdm(const MoveParams& P, float half_dt, float zf) {
+        return P.qm_f * zf * half_dt;
+    }
     static __device__ __forceinline__ float centre(const MoveParams& P, int a) { return P.centre_f[a]; }
     static __device__ __forceinline__ float cc(const MoveParams& P, int c, int a) {
         return P.m.cc32[3 * size_t(c) + a];
@@ -65,7 +69,22 @@ struct PState {
     int cell, tet;
     Real y[4];
     Real U[3];
+    Real zf;      // charge modifier (1 without per-parcel attributes)
+    double nw;    // nParticle (the species weight without per-parcel attributes)
 };
+
+// The parcel's charge modifier and weight: per parcel when the store has
+// the arrays, else 1 and the species weight.
+template <class Real>
+__device__ __forceinline__ void load_attributes(const MoveParams& P, int i, PState<Real>& s) {
+    if (P.p.nw) {
+        s.zf = Real(P.p.zq[i]);
+        s.nw = P.p.nw[i];
+    } else {
+        s.zf = Real(1);
+        s.nw = P.weight;
+    }
+}
 
 template <class Real> __device__ __forceinline__ const Real* e_cell(const MoveParams& P);
 template <> __device__ __forceinline__ const double* e_cell<double>(const MoveParams& P) { return P.E; }
@@ -106,14 +125,15 @@ __device__ __forceinline__ void field_at(const MoveParams& P, const TetConst& T,
 
 // BorisPusher::updateVelocity (submodels/ParticlePusher/BorisPusher/BorisPusher.C:69-112)
 template <class Real>
-__device__ __forceinline__ void push_boris(const MoveParams& P, const Real* E, const Real* Bv, Real* U, Real tt) {
+__device__ __forceinline__ void push_boris(const MoveParams& P, const Real* E, const Real* Bv, Real* U, Real tt,
+                                      Real zf) {
     const Real c = Real(kC);
     const Real dt2 = Real(0.5) * tt;
     const Real mU = sqrt(dot3(U, U)) / c;
     const Real g0 = sqrt(Real(1) - mU * mU);
     Real rU[3] = {U[0] / g0, U[1] / g0, U[2] / g0};
     const Real oldrU[3] = {rU[0], rU[1], rU[2]};
-    const Real qdm = PC<Real>::qdm(P, dt2);
+    const Real qdm = PC<Real>::qdm(P, dt2, zf);
     const Real rUsm[3] = {qdm * E[0], qdm * E[1], qdm * E[2]};
     rU[0] = rU[0] + rUsm[0]; rU[1] = rU[1] + rUsm[1]; rU[2] = rU[2] + rUsm[2];
     if (P.rotation) {
@@ -136,9 +156,10 @@ __device__ __forceinline__ void push_boris(const MoveParams& P, const Real* E, c
 
 // BorisNRPusher::updateVelocity (BorisNRPusher.C:69-99)
 template <class Real>
-__device__ __forceinline__ void push_boris_nr(const MoveParams& P, const Real* E, const Real* Bv, Real* U, Real tt) {
+__device__ __forceinline__ void push_boris_nr(const MoveParams& P, const Real* E, const Real* Bv, Real* U, Real tt,
+                                      Real zf) {
     const Real dt2 = Real(0.5) * tt;
-    const Real alpha = PC<Real>::qdm(P, dt2);
+    const Real alpha = PC<Real>::qdm(P, dt2, zf);
     Real W[3] = {U[0] + alpha * E[0], U[1] + alpha * E[1], U[2] + alpha * E[2]};
     if (P.rotation) {
         const Real t[3] = {alpha * Bv[0], alpha * Bv[1], alpha * Bv[2]};
@@ -155,15 +176,16 @@ __device__ __forceinline__ void push_boris_nr(const MoveParams& P, const Real* E
 
 // VayPusher::updateVelocity (VayPusher.C:54-100); U x T uses v (VayPusher.C:81).
 template <class Real>
-__device__ __forceinline__ void push_vay(const MoveParams& P, const Real* E, const Real* Bv, Real* U, Real tt) {
+__device__ __forceinline__ void push_vay(const MoveParams& P, const Real* E, const Real* Bv, Real* U, Real tt,
+                                      Real zf) {
     const Real c = Real(kC);
     const Real dt2 = Real(0.5) * tt;
     const Real mU = sqrt(dot3(U, U)) / c;
     const Real lF = Real(1) / sqrt(Real(1) - mU * mU);
     const Real rU0[3] = {lF * U[0], lF * U[1], lF * U[2]};
-    const Real qe = PC<Real>::qdm(P, tt);
+    const Real qe = PC<Real>::qdm(P, tt, zf);
     Real Ud[3] = {rU0[0] + qe * E[0], rU0[1] + qe * E[1], rU0[2] + qe * E[2]};
-    const Real qb = PC<Real>::qdm(P, dt2);
+    const Real qb = PC<Real>::qdm(P, dt2, zf);
     Real T[3] = {qb * Bv[0], qb * Bv[1], qb * Bv[2]};
     Real cr[3];
     cross3(U, T, cr);
@@ -189,13 +211,14 @@ __device__ __forceinline__ void push_vay(const MoveParams& P, const Real* E, con
 
 // HigueraCaryPusher::updateVelocity (HigueraCary.C:69-115)
 template <class Real>
-__device__ __forceinline__ void push_hc(const MoveParams& P, const Real* E, const Real* Bv, Real* U, Real tt) {
+__device__ __forceinline__ void push_hc(const MoveParams& P, const Real* E, const Real* Bv, Real* U, Real tt,
+                                      Real zf) {
     const Real c = Real(kC);
     const Real dt2 = Real(0.5) * tt;
     const Real mU = sqrt(dot3(U, U)) / c;
     const Real g0 = sqrt(Real(1) - mU * mU);
     Real rU[3] = {U[0] / g0, U[1] / g0, U[2] / g0};
-    const Real qdm = PC<Real>::qdm(P, dt2);
+    const Real qdm = PC<Real>::qdm(P, dt2, zf);
     const Real rUsm[3] = {qdm * E[0], qdm * E[1], qdm * E[2]};
     rU[0] = rU[0] + rUsm[0]; rU[1] = rU[1] + rUsm[1]; rU[2] = rU[2] + rUsm[2];
     if (P.rotation) {
@@ -242,10 +265,10 @@ __device__ __forceinline__ void push(const MoveParams& P, const TetConst& T, PSt
     field_at(P, T, s, E);
     cell_B(P, s.cell, Bv);
     switch (P.pusher) {
-        case PICGPU_PUSHER_BORIS: push_boris(P, E, Bv, s.U, tt); break;
-        case PICGPU_PUSHER_BORIS_NR: push_boris_nr(P, E, Bv, s.U, tt); break;
-        case PICGPU_PUSHER_VAY: push_vay(P, E, Bv, s.U, tt); break;
-        default: push_hc(P, E, Bv, s.U, tt); break;
+        case PICGPU_PUSHER_BORIS: push_boris(P, E, Bv, s.U, tt, s.zf); break;
+        case PICGPU_PUSHER_BORIS_NR: push_boris_nr(P, E, Bv, s.U, tt, s.zf); break;
+        case PICGPU_PUSHER_VAY: push_vay(P, E, Bv, s.U, tt, s.zf); break;
+        default: push_hc(P, E, Bv, s.U, tt, s.zf); break;
     }
 }
 
@@ -288,7 +311,7 @@ __device__ __forceinline__ int tet_step(const MoveParams& P, PState<Real>& s, co
 template <class Real>
 __device__ __forceinline__ void sync_velocity(const MoveParams& P, const TetConst& T, PState<Real>& s,
                                               Real fraction) {
-    if (P.sync && P.charged) push(P, T, s, fraction * PC<Real>::dt(P));
+    if (P.sync && P.charged && s.zf != Real(0)) push(P, T, s, fraction * PC<Real>::dt(P));
 }
 
 struct TrackTally {
@@ -306,7 +329,7 @@ __device__ __forceinline__ void hit_patch(const MoveParams& P, const TetConst& T
     // (circuitRLC.C:268-288) deletes charged parcels and reflects neutral ones
     if (kind == PICGPU_PATCH_FLOATING || (kind == PICGPU_PATCH_CIRCUIT && P.q != 0.0)) {
         td.keep = false;
-        atomicAdd(P.qconv + patch, P.weight * P.q);
+        atomicAdd(P.qconv + patch, P.p.nw ? s.nw * (P.q * double(s.zf)) : P.weight * P.q);
         return;
     }
     const int f = s.tet / 2;
@@ -401,7 +424,8 @@ __device__ __forceinline__ void deposit_add(const MoveParams& P, double* dst64, 
 
 // ChargeDistribution::add for one particle at its end-of-step position.
 __device__ __forceinline__ void deposit(const MoveParams& P, const TetConst& T, const PState<double>& s) {
-    const double value = P.value;
+    // charge x nParticle of the parcel (VolumeWeighting.C:114)
+    const double value = P.p.nw ? P.q * s.zf * s.nw : P.value;
     if (value == 0.0) return;
     if (P.charge_distribution == PICGPU_WEIGHTING_CELL_AVERAGE) {
         deposit_add(P, P.cc_data, P.cc_fix, s.cell, value);
@@ -439,9 +463,11 @@ __device__ __forceinline__ void move_one(const MoveParams& P, const TetConst& T,
     s.U[0] = ubuf<Real>(P.p, 0)[i];
     s.U[1] = ubuf<Real>(P.p, 1)[i];
     s.U[2] = ubuf<Real>(P.p, 2)[i];
+    load_attributes(P, i, s);
     if (P.solve_movement) {
         const Real dt = PC<Real>::dt(P);
-        if (P.charged) push(P, T, s, dt);
+        // PICParcel::move pushes charged parcels only (PICParcel.C:55)
+        if (P.charged && s.zf != Real(0)) push(P, T, s, dt);
         const Real c = Real(kC);
         if (!(sqrt(dot3(s.U, s.U)) < c)) {
             td.keep = false;

@@ -72,7 +72,9 @@ __global__ void scatter_kernel(const int32_t* __restrict__ tet, const R* __restr
                                const R* __restrict__ u1, const R* __restrict__ u2, int32_t* __restrict__ otet,
                                R* __restrict__ oy0, R* __restrict__ oy1, R* __restrict__ oy2,
                                R* __restrict__ ou0, R* __restrict__ ou1, R* __restrict__ ou2, long n,
-                               const int* __restrict__ offsets) {
+                               const int* __restrict__ offsets, const double* __restrict__ nw,
+                               const int32_t* __restrict__ zq, double* __restrict__ onw,
+                               int32_t* __restrict__ ozq) {
     __shared__ int ws[kBlock / 32];
     const long base = long(blockIdx.x) * kTile + long(threadIdx.x) * kItems;
     bool f[kItems];
@@ -100,6 +102,10 @@ __global__ void scatter_kernel(const int32_t* __restrict__ tet, const R* __restr
         otet[pos] = tet[i];
         oy0[pos] = y0[i]; oy1[pos] = y1[i]; oy2[pos] = y2[i];
         ou0[pos] = u0[i]; ou1[pos] = u1[i]; ou2[pos] = u2[i];
+        if (nw) {
+            onw[pos] = nw[i];
+            ozq[pos] = zq[i];
+        }
         ++pos;
     }
 }
@@ -150,7 +156,21 @@ __global__ void gather_rows_kernel(DSpecies src, long n, int32_t* __restrict__ t
     }
 }
 
+__global__ void fill_attributes_kernel(double* __restrict__ nw, int32_t* __restrict__ zq, long from, long to,
+                                       double weight) {
+    for (long i = from + blockIdx.x * long(blockDim.x) + threadIdx.x; i < to; i += long(gridDim.x) * blockDim.x) {
+        nw[i] = weight;
+        zq[i] = 1;
+    }
+}
+
 }  // namespace
+
+void launch_fill_attributes(const DSpecies& d, long from, long to, double weight, cudaStream_t s) {
+    if (!d.nw || to <= from) return;
+    const int g = int(std::min<long>((to - from + 255) / 256, 152 * 16));
+    fill_attributes_kernel<<<g, 256, 0, s>>>(d.nw, d.zq, from, to, weight);
+}
 
 void launch_check_tets(const int32_t* tet, long n, long long ntet, int* bad, cudaStream_t s) {
     if (n > 0) check_tets_kernel<<<int(std::min<long>((n + 255) / 256, 152 * 16)), 256, 0, s>>>(tet, n, ntet, bad);
@@ -181,11 +201,11 @@ cudaError_t compact_species(const DSpecies& src, const DSpecies& dst, long n, bo
     if (mixed)
         scatter_kernel<float><<<unsigned(nblk), kBlock, 0, s>>>(
             src.tet, src.y32[0], src.y32[1], src.y32[2], src.u32[0], src.u32[1], src.u32[2], dst.tet, dst.y32[0],
-            dst.y32[1], dst.y32[2], dst.u32[0], dst.u32[1], dst.u32[2], n, scan);
+            dst.y32[1], dst.y32[2], dst.u32[0], dst.u32[1], dst.u32[2], n, scan, src.nw, src.zq, dst.nw, dst.zq);
     else
         scatter_kernel<double><<<unsigned(nblk), kBlock, 0, s>>>(
             src.tet, src.y64[0], src.y64[1], src.y64[2], src.u64[0], src.u64[1], src.u64[2], dst.tet, dst.y64[0],
-            dst.y64[1], dst.y64[2], dst.u64[0], dst.u64[1], dst.u64[2], n, scan);
+            dst.y64[1], dst.y64[2], dst.u64[0], dst.u64[1], dst.u64[2], n, scan, src.nw, src.zq, dst.nw, dst.zq);
     int total = 0;
     cudaError_t e = cudaMemcpyAsync(&total, scan + nblk, sizeof(int), cudaMemcpyDeviceToHost, s);
     if (e != cudaSuccess) return e;

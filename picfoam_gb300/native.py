@@ -37,6 +37,8 @@ def declare(lib, prefix, ctx_api=True):
     f("set_particles", i, [P, i, C.c_size_t, I32P, F64P, F64P])
     f("count_particles", i, [P, i, SZP])
     f("get_particles", i, [P, i, C.c_size_t, I32P, F64P, F64P, SZP])
+    f("set_parcel_attributes", i, [P, i, C.c_size_t, F64P, I32P])
+    f("get_parcel_attributes", i, [P, i, C.c_size_t, F64P, I32P, SZP])
     f("initialise_fields", i, [P])
     f("initialise", i, [P, C.POINTER(abi.Init), C.POINTER(abi.InitStats)])
     f("set_injection", i, [P, i, C.POINTER(abi.Injection)])
@@ -48,6 +50,7 @@ def declare(lib, prefix, ctx_api=True):
     f("get_field", i, [P, i, F64P, C.c_size_t])
     f("set_field", i, [P, i, F64P, C.c_size_t])
     f("set_step_index", i, [P, C.c_int64])
+    f("compute_field", i, [P])
 
 
 def load():

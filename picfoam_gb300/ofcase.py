@@ -218,9 +218,11 @@ def _species_values(d, names, default=0.0):
     return [float(d.number(n, default)) if isinstance(d, foam.Dict) else default for n in names]
 
 
-def load_case(path, allow_unsupported=False, precision=abi.PREC_FP64, seed=1234):
+def load_case(path, allow_unsupported=False, precision=abi.PREC_FP64, seed=1234, ionization_model=None):
     """Map a picFoam case directory onto the picgpu configuration (see the
-    module docstring for what is read)."""
+    module docstring for what is read).  ionization_model overrides the
+    Coulomb model's IonizationModel entry (e.g. "Perez" to switch on the
+    coefficients a case carries)."""
     bad = _Unsupported(allow_unsupported)
     n, origin, length, cell_order, patch_sides, patch_types = _block(path)
     zero = os.path.join(path, "0") if os.path.isdir(os.path.join(path, "0")) else os.path.join(path, "0.org")
@@ -427,9 +429,12 @@ def load_case(path, allow_unsupported=False, precision=abi.PREC_FP64, seed=1234)
 
     init_dict = _read_optional(os.path.join(path, "system", "picInitialiseDict"))
     keep = []
-    _collisions(props.sub("CollisionModels"), cfg, names, mol, bad, init_dict, keep)
-    if props.word("ParticleMerging", "none") != "none":
-        bad(f"ParticleMerging {props.word('ParticleMerging')}")
+    _collisions(props.sub("CollisionModels"), cfg, names, mol, bad, init_dict, keep, ionization_model)
+    merging = props.word("ParticleMerging", "none")
+    if merging == "PairMerging":
+        _merging(props.sub("PairMergingCoeffs"), cfg, names)
+    elif merging != "none":
+        bad(f"ParticleMerging {merging}")
 
     plist = []
     init = _init(init_dict, names, cfg, seed, bad, plist)
@@ -508,7 +513,55 @@ def _electron_neutral(cm, cfg, names, mol, init_dict, bad, keep):
         bad("ionization_nEquivalentParticles (one weight per species)")
 
 
-def _collisions(cm, cfg, names, mol, bad, init_dict=None, keep=None):
+def _merging(co, cfg, names):
+    """PairMergingCoeffs (PairMerging.C:35-68): species in merge order with
+    nDeviation per species, reductionFactor, cellParcelsMax, maxChecks,
+    nCheckNeighbors, angleDifference [deg], velocityRatio,
+    mergeMaximumPerCell."""
+    species = [str(x) for x in co.get("species", [])]
+    dev = [float(x) for x in co.get("nDeviation", [])]
+    if not species or len(dev) != len(species) or any(s not in names for s in species):
+        raise UnsupportedCase("PairMerging: species must be defined and nDeviation give one value per species")
+    cases.set_merging(cfg, [names.index(s) for s in species],
+                      cell_parcels_max=int(co.number("cellParcelsMax")), reduction_factor=co.number("reductionFactor"),
+                      max_checks=int(co.number("maxChecks")), n_check_neighbors=int(co.number("nCheckNeighbors")),
+                      angle_difference=co.number("angleDifference"), velocity_ratio=co.number("velocityRatio"),
+                      n_deviation=dev, merge_maximum_per_cell=int(co.number("mergeMaximumPerCell")))
+
+
+def _perez(coeffs, cfg, names):
+    """PerezIonizationCoeffs (PerezIonizationModel.C:50-116): one entry per
+    ion species with atomicNumber, the optional ionizationLimit and the
+    bindingEnergy / ionizationEnergy lists [eV]."""
+    pz = cfg.perez
+    pz.enabled = 1
+    k = 0
+    for _, d in coeffs.items():
+        if not isinstance(d, foam.Dict):
+            continue
+        ion = str(d.word("ionSpecies"))
+        if ion not in names:
+            raise UnsupportedCase(f"PerezIonization: ionSpecies {ion} is not defined")
+        if k >= abi.PEREZ_MAX_IONS:
+            raise UnsupportedCase(f"PerezIonization: more than {abi.PEREZ_MAX_IONS} ion species")
+        A = int(d.number("atomicNumber"))
+        binding = [float(x) for x in d.get("bindingEnergy", [])]
+        energy = [float(x) for x in d.get("ionizationEnergy", [])]
+        if not 1 <= A <= abi.PEREZ_MAX_Z or len(binding) != A or len(energy) != A:
+            raise UnsupportedCase("PerezIonization: bindingEnergy and ionizationEnergy need atomicNumber entries")
+        e = pz.ion[k]
+        e.species = names.index(ion)
+        e.atomic_number = A
+        limit = d.number("ionizationLimit", None)
+        e.ionization_limit = -1 if limit is None else int(limit)
+        for i in range(A):
+            e.binding_energy[i] = binding[i]
+            e.ionization_energy[i] = energy[i]
+        k += 1
+    pz.n_ions = k
+
+
+def _collisions(cm, cfg, names, mol, bad, init_dict=None, keep=None, ionization_model=None):
     """CollisionModels: electron-neutral collisions with neutral parcels
     (FixedValue cross sections), Coulomb (fixed or computed coulombLog) and
     binary IsotropicScattering map; background-gas MCC and ion-neutral
@@ -541,8 +594,11 @@ def _collisions(cm, cfg, names, mol, bad, init_dict=None, keep=None):
         if len(logs) > 1:
             bad("CoulombCollisionCoeffs: different coulombLog per pair (one value is used)")
         c.coulomb_log = max(logs) if logs else 0.0
-        if co.word("IonizationModel", "none") != "none":
-            bad(f"IonizationModel {co.word('IonizationModel')}")
+        model = ionization_model or co.word("IonizationModel", "none")
+        if model == "Perez":
+            _perez(co.sub("PerezIonizationCoeffs"), cfg, names)
+        elif model != "none":
+            bad(f"IonizationModel {model}")
     binary = cm.word("BinaryCollisionModel", "none")
     if binary != "none":
         if binary != "IsotropicScattering":
@@ -721,25 +777,27 @@ def write_fields(sim, case, t, cloud="pic", step_index=None):
     _write_vol(os.path.join(d, "rhoCharge"), "rhoCharge", _RHO_DIM, rho, False, case)
     from .simulation import Mesh
     m = Mesh(case.mesh)
-    U, tid, npart, pos, tets, barys = [], [], [], [], [], []
+    U, tid, npart, pos, tets, barys, zq = [], [], [], [], [], [], []
     for s in range(len(case.species)):
         tet, bary, u = sim.get_particles(s)
+        w, z = sim.get_parcel_attributes(s)
         if len(tet) == 0:
             continue
         U.append(u)
         tid.append(np.full(len(tet), s, dtype=np.int64))
-        npart.append(np.full(len(tet), case.cfg.species[s].weight))
+        npart.append(w)
+        zq.append(z.astype(np.int64))
         pos.append(m.position(tet, bary))
         tets.append(tet.astype(np.int64))
         barys.append(bary)
     if U:
         ld = os.path.join(d, "lagrangian", cloud)
         os.makedirs(ld, exist_ok=True)
-        U, tid, npart, pos, tets, barys = (np.concatenate(x) for x in (U, tid, npart, pos, tets, barys))
+        U, tid, npart, pos, tets, barys, zq = (np.concatenate(x) for x in (U, tid, npart, pos, tets, barys, zq))
         loc = os.path.join(time_name(t), "lagrangian", cloud)
         for name, cls, body in (("U", "vectorField", foam.format_vectors(U)),
                                 ("typeId", "labelField", foam.format_labels(tid)),
-                                ("chargeModifier", "labelField", foam.format_labels(np.ones_like(tid))),
+                                ("chargeModifier", "labelField", foam.format_labels(zq)),
                                 ("nParticle", "scalarField", foam.format_scalars(npart)),
                                 ("cartesianPositions", "vectorField", foam.format_vectors(pos)),
                                 ("picgpuTet", "labelField", foam.format_labels(tets)),
@@ -791,11 +849,11 @@ def restart(sim, case, t=None, cloud="pic"):
     startFrom latestTime of picFoam (PICParcelIO.C:83-120 reads the parcels
     back): particles from picgpuTet / picgpuBarycentric / U / typeId (the
     state this library writes; without them the cartesianPositions are
-    located again, which rounds the coordinates), the potential phiE, the
-    step index and the floating patches' surface charge.  The charge density
-    and E are recomputed from them: with the written potential as the start
-    guess the Poisson solve is already converged, so a FP64 run continues
-    bit for bit.  Not restored: the remainders of injection, emission and
+    located again, which rounds the coordinates), their nParticle and
+    chargeModifier where they differ from the species', the potential phiE,
+    the step index and the floating patches' surface charge.  E is computed
+    from the written potential (no Poisson solve; the next step deposits the
+    charge again), so a FP64 run continues bit for bit.  Not restored: the remainders of injection, emission and
     collision models, MCC (sigma v)_max and circuit states.  Returns t."""
     if t is None:
         t = latest_time(case)
@@ -810,9 +868,17 @@ def restart(sim, case, t=None, cloud="pic"):
         else:
             from .simulation import Mesh
             tet, bary = Mesh(case.mesh).locate(read_list(os.path.join(ld, "cartesianPositions")).reshape(-1, 3))
+        w = read_list(os.path.join(ld, "nParticle")) if os.path.exists(os.path.join(ld, "nParticle")) else None
+        z = (read_list(os.path.join(ld, "chargeModifier")).astype(np.int32)
+             if os.path.exists(os.path.join(ld, "chargeModifier")) else None)
         for s in range(len(case.species)):
             sel = tid == s
             sim.set_particles(s, tet[sel], bary[sel], U[sel])
+            # per-parcel weights and charge states where they differ from
+            # the species' (PICParcelIO.C:98-113)
+            if w is not None and z is not None and np.any(sel) and (
+                    np.any(w[sel] != case.cfg.species[s].weight) or np.any(z[sel] != 1)):
+                sim.set_parcel_attributes(s, w[sel], z[sel])
     phi_case = read_field(os.path.join(d, "phiE"))
     phi = np.empty_like(phi_case)
     phi[case.cell_order] = phi_case
@@ -824,7 +890,10 @@ def restart(sim, case, t=None, cloud="pic"):
         sim.set_field(abi.FIELD_PATCH_SIGMA, foam.numeric_list(st["patchSigma"]))
     sim.set_step_index(step_index)
     sim.set_field(abi.FIELD_PHI, phi)
-    sim.initialise_fields()
+    # E from the written potential: the charge density of that step was
+    # deposited before the step's last changes to the parcels (PairMerging
+    # runs after the field solve), so it is not deposited again here
+    sim.compute_field()
     return t
 
 

@@ -131,6 +131,30 @@ class Simulation:
         k = n.value
         return tet[:k], bary[:k], U[:k]
 
+    def set_parcel_attributes(self, species, nParticle, chargeModifier):
+        """Per-parcel nParticle and chargeModifier of one species, in the
+        order of get_particles (picgpu_set_parcel_attributes)."""
+        w, wp = _f64(nParticle)
+        z = np.ascontiguousarray(chargeModifier, dtype=np.int32)
+        assert w.shape[0] == z.shape[0]
+        self._check(self._fn("set_parcel_attributes")(self._h, species, w.shape[0], wp,
+                                                      z.ctypes.data_as(C.POINTER(C.c_int32))))
+
+    def get_parcel_attributes(self, species):
+        """(nParticle, chargeModifier) of one species, in the order of get_particles."""
+        n = C.c_size_t()
+        self._check(self._fn("get_parcel_attributes")(self._h, species, 0, None, None, C.byref(n)))
+        w = np.zeros(n.value)
+        z = np.zeros(n.value, np.int32)
+        self._check(self._fn("get_parcel_attributes")(
+            self._h, species, n.value, w.ctypes.data_as(C.POINTER(C.c_double)),
+            z.ctypes.data_as(C.POINTER(C.c_int32)), C.byref(n)))
+        return w[:n.value], z[:n.value]
+
+    def compute_field(self):
+        """E from the current potential, no Poisson solve (picgpu_compute_field)."""
+        self._check(self._fn("compute_field")(self._h))
+
     # ---------------------------------------------------------------- step
     def initialise_fields(self):
         self._check(self._fn("initialise_fields")(self._h))

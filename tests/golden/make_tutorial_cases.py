@@ -20,6 +20,10 @@ TUTORIALS = {"plasmaOscillation": False, "thermalization": False, "thermalizatio
              "electricAcceleration": True}
 
 
+# fixture -> (tutorial, IonizationModel override)
+VARIANTS = {"thermalization_perez": ("thermalization", "Perez")}
+
+
 def main():
     root = os.environ.get("PICFOAM_TUTORIALS") or (sys.argv[1] if len(sys.argv) > 1 else None)
     if not root or not os.path.isdir(root):
@@ -28,6 +32,13 @@ def main():
     os.makedirs(out, exist_ok=True)
     for name, allow in TUTORIALS.items():
         case = ofcase.load_case(os.path.join(root, name), allow_unsupported=allow)
+        with open(os.path.join(out, name + ".json"), "w") as f:
+            json.dump(tutorial_cases.dump(case), f, indent=1)
+        print(name, "unmapped:", case.unsupported)
+    # the thermalization tutorial carries PerezIonizationCoeffs for argon with
+    # the model switched off; this fixture switches it on
+    for name, (src, model) in VARIANTS.items():
+        case = ofcase.load_case(os.path.join(root, src), ionization_model=model)
         with open(os.path.join(out, name + ".json"), "w") as f:
             json.dump(tutorial_cases.dump(case), f, indent=1)
         print(name, "unmapped:", case.unsupported)

@@ -52,7 +52,8 @@ MIRRORS = {
     "Mcc": "picgpu_mcc", "IonMcc": "picgpu_ion_mcc", "Coulomb": "picgpu_coulomb", "Learned": "picgpu_learned",
     "Multigrid": "picgpu_multigrid", "Config": "picgpu_config", "StepStats": "picgpu_step_stats",
     "MeshInfo": "picgpu_mesh_info", "Diagnostics": "picgpu_diagnostics",
-    "Binary": "picgpu_binary", "Circuit": "picgpu_circuit", "FreeStream": "picgpu_freestream",
+    "Binary": "picgpu_binary", "Circuit": "picgpu_circuit", "Merging": "picgpu_merging", "Perez": "picgpu_perez", "PerezIon": "picgpu_perez_ion",
+    "FreeStream": "picgpu_freestream",
     "Injection": "picgpu_injection", "Emission": "picgpu_emission", "ParticlesSoa": "picgpu_particles_soa",
 }
 

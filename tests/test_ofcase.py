@@ -51,9 +51,14 @@ def write(path, rel, text):
         fh.write(HEADER % os.path.basename(rel) + text)
 
 
-def make_case(path, pusher="Boris", injection=True):
+def make_case(path, pusher="Boris", injection=True, merging=False):
     """A 6 x 4 x 5 block whose local axes are x1 = -y, x2 = -z, x3 = +x
-    (injection=False leaves the SimpleInjection of the source patch out)."""
+    (injection=False leaves the SimpleInjection of the source patch out;
+    merging=True merges both species' parcels in cells of more than 900)."""
+    merge = ("""PairMerging;
+PairMergingCoeffs { species (e Ar+); nDeviation (5e3 5e3); reductionFactor 0.9; cellParcelsMax 900; maxChecks 300;
+                    nCheckNeighbors 6; angleDifference 20; velocityRatio 0.6; mergeMaximumPerCell 40; }"""
+             if merging else "none;")
     source = ("""source { type SimpleInjection; SimpleInjectionCoeffs { frequencies (1e15 2e14); injectionEndTime 1;
                      eV (2 0.1); injectionTypeIds (e Ar+); velocityModel halfMaxwellianFlux;
                      interactions { e { type deletion; } Ar+ { type deletion; } } } }"""
@@ -110,7 +115,7 @@ MaxwellSolver ElectroStatic;
 ParticlePusher {pusher};
 CollisionModels {{ BackgroundGasModel none; ElectronNeutralCollisionModel none; BinaryCollisionModel none;
                   CoulombCollisionModel none; IonNeutralCollisionModel none; }}
-ParticleMerging none;
+ParticleMerging {merge}
 """)
     write(path, "system/controlDict", "deltaT 1e-12;\nendTime 4e-12;\nwriteInterval 2e-12;\n")
     write(path, "system/fvSolution", "solvers { phiE { solver PCG; preconditioner DIC; tolerance 1e-9; relTol 0; } }\n")
@@ -286,6 +291,29 @@ def test_reference_magnetic_rotation_gyrates(oracle_backend):
         x = m.position(t, b)
         assert np.linalg.norm(x[0, :2]) == pytest.approx(r0, rel=1e-7)
         assert np.linalg.norm(U[0]) == pytest.approx(29979246.0, rel=1e-12)
+
+
+def test_merging_maps_and_restarts_bit_for_bit(oracle_backend, tmp_path):
+    """PairMergingCoeffs map onto picgpu_merging, and a run with merging
+    written at step 2 and continued from that time directory reproduces the
+    uninterrupted run: nParticle and chargeModifier are written per parcel
+    and read back (PICParcelIO.C:98-160)."""
+    from picfoam_gb300 import run
+    a, b = str(tmp_path / "a"), str(tmp_path / "b")
+    make_case(a, injection=False, merging=True)
+    make_case(b, injection=False, merging=True)
+    mg = ofcase.load_case(a).cfg.merging
+    assert mg.enabled == 1 and mg.n_species == 2 and list(mg.species[:2]) == [0, 1]
+    assert (mg.cell_parcels_max, mg.n_check_neighbors, mg.merge_maximum_per_cell) == (900, 6, 40)
+    assert mg.reduction_factor == 0.9 and mg.angle_difference == 20 and list(mg.n_deviation[:2]) == [5e3, 5e3]
+    assert run.main([a, "--oracle", "--steps", "4"]) == 0
+    assert run.main([b, "--oracle", "--steps", "2"]) == 0
+    assert run.main([b, "--oracle", "--restart", "--steps", "2"]) == 0
+    la, lb = (os.path.join(p, "4e-12", "lagrangian", "pic") for p in (a, b))
+    for name in ("picgpuTet", "picgpuBarycentric", "U", "typeId", "nParticle", "chargeModifier"):
+        np.testing.assert_array_equal(ofcase.read_list(os.path.join(la, name)),
+                                      ofcase.read_list(os.path.join(lb, name)))
+    assert ofcase.read_list(os.path.join(la, "nParticle")).max() > 1e3      # merged parcels
 
 
 def test_restart_continues_bit_for_bit(oracle_backend, tmp_path):
