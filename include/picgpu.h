@@ -529,7 +529,11 @@ picgpu_status picgpu_get_particles(picgpu_ctx* ctx, int species, size_t cap,
  * nParticle in (0, 4096 x species weight], chargeModifier in [0, 1024];
  * the store is compacted first.  Parcels created later (injection,
  * collisions, picInitialise) get the defaults (PICCloud::addNewParcel,
- * PICCloud.C:707-723).  Get works with or without per-parcel arrays. */
+ * PICCloud.C:707-723).  Get works with or without per-parcel arrays.
+ * Species that a background or parcel MCC, ion-neutral or binary collision
+ * model uses cannot have per-parcel arrays (those models take one weight per
+ * species): PICGPU_NOT_SUPPORTED, also for PairMerging and Perez
+ * ionisation on such species at context creation. */
 picgpu_status picgpu_set_parcel_attributes(picgpu_ctx* ctx, int species, size_t n,
                                            const double* nParticle, const int32_t* chargeModifier);
 picgpu_status picgpu_get_parcel_attributes(picgpu_ctx* ctx, int species, size_t cap,

@@ -533,12 +533,29 @@ pgd::DSpecies view(const picgpu_ctx* c, int s, int k) {
     return v;
 }
 
+// Whether a collision model that takes its weights per species (background
+// and parcel MCC, ion-neutral MCC, binary collisions) uses species s.
+bool species_weight_models(const picgpu_config& cfg, int s) {
+    const picgpu_mcc& m = cfg.mcc;
+    const picgpu_ion_mcc& im = cfg.ion_mcc;
+    if (m.enabled && (s == cfg.electron_species || (m.create_ion && s == m.ion_species) ||
+                      (m.neutral_parcels && s == m.neutral_species)))
+        return true;
+    if (im.enabled && (s == im.ion_species || (im.neutral_parcels && s == im.neutral_species))) return true;
+    if (cfg.binary.enabled && cfg.species[s].charge == 0.0) return true;
+    return false;
+}
+
 // Per-parcel attributes for species s: both halves of the store get the
 // arrays, the parcels stored so far the defaults (species weight, charge
 // modifier 1).
 picgpu_status enable_attributes(picgpu_ctx* c, int s) {
     SpeciesBuf& b = c->sp[s];
     if (b.attrs) return PICGPU_OK;
+    if (species_weight_models(c->cfg, s))
+        return bad(c, PICGPU_NOT_SUPPORTED,
+                   "per-parcel weights: the MCC, ion-neutral and binary collision models of this library take one "
+                   "weight per species");
     if (c->n_cases > 1 || !c->graphs.empty())
         return bad(c, PICGPU_NOT_SUPPORTED, "per-parcel attributes are not supported with ensembles or graph steps");
     picgpu_status st;
