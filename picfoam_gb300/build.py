@@ -17,6 +17,7 @@ ROOT = os.path.dirname(HERE)
 SRC = os.path.join(HERE, "csrc")
 OUT = os.path.join(HERE, "_build")
 LIB = os.path.join(OUT, "libpicgpu.so")
+DRIVER = os.path.join(OUT, "picgpu_rts_driver")
 INCLUDE = os.path.join(ROOT, "include")
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
@@ -84,6 +85,15 @@ def build(verbose=False):
         r = subprocess.run(cmd, capture_output=True, text=True)
         if r.returncode != 0:
             raise RuntimeError(f"link failed:\n{' '.join(cmd)}\n{r.stdout}\n{r.stderr}")
+    # the C++ host driver over the run-time selection header (picgpu_rts.hpp)
+    drv_src = os.path.join(HERE, "host", "rts_driver.cpp")
+    if os.path.exists(drv_src) and _stale(DRIVER, [drv_src, LIB] + HEADERS):
+        cxx = shutil.which("g++") or "g++"
+        cmd = [cxx, "-O2", "-std=c++17", "-I", INCLUDE, drv_src, "-o", DRIVER, "-L", OUT, "-lpicgpu",
+               "-Wl,-rpath,$ORIGIN"]
+        r = subprocess.run(cmd, capture_output=True, text=True)
+        if r.returncode != 0:
+            raise RuntimeError(f"driver build failed:\n{' '.join(cmd)}\n{r.stdout}\n{r.stderr}")
     if verbose:
         print(LIB)
     return LIB

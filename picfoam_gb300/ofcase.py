@@ -615,8 +615,8 @@ def _collisions(cm, cfg, names, mol, bad, init_dict=None, keep=None, ionization_
         if wc is None:
             raise UnsupportedCase(f"WeightCorrection {co.word('WeightCorrection')}")
         b.weight_correction = wc
-        if co.flag("handleChargeExchange", False):
-            bad("IsotropicScattering handleChargeExchange")
+        # IsotropicScatteringCoeffs handleChargeExchange (a tutorial entry)
+        # is read by none of picFoam's collision code, so it is ignored here
         vhs = cm.sub("VariableHardSphereCoeffs")
         b.tref = vhs.number("Tref", 273.0)
         b.background_species = -1
