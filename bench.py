@@ -66,7 +66,7 @@ def parse():
     p.add_argument("--ens-steps", type=int, default=100)
     p.add_argument("--ens-graph", type=int, default=10)
     p.add_argument("--ens-seq-steps", type=int, default=20)
-    p.add_argument("--only", default=None, choices=["electrode", "unet", "ensemble", "init"],
+    p.add_argument("--only", default=None, choices=["electrode", "unet", "ensemble", "init", "coulomb", "learned"],
                    help="profiling drivers: run one workload briefly and print a short summary "
                         "(electrode: electrode_box steps; unet: one forward + train steps; "
                         "ensemble: two graph replays)")
@@ -779,6 +779,20 @@ def run_only(args):
         assert lib.picgpu_unet_train(h, p(x), p(t), p(m), args.only_steps, 1e-3, C.byref(loss)) == 0
         lib.picgpu_unet_destroy(h)
         print(json.dumps({"only": "unet", "grid": n, "loss": loss.value}))
+    elif args.only == "learned":
+        # the learned warm start against the previous-potential start on the
+        # electrode geometry with the --ws-* settings (BASELINE config 4 as
+        # stated: --ws-ppc 30 --ws-train 500 --ws-measure 2000)
+        print(json.dumps({"only": "learned", "poisson_learned_vs_plain": learned_vs_plain(args)}))
+    elif args.only == "coulomb":
+        # the Coulomb thermalisation of the swarm workload (16^3 cells, 400
+        # electrons per cell, NanbuYonemura + Nanbu), FP32 store
+        from picfoam_gb300 import abi
+        case = cases.coulomb_thermalisation(n_cells=16, per_cell=400, precision=abi.PREC_MIXED)
+        sim = cases.build(case)
+        for _ in range(args.only_steps):
+            st = sim.step(1)
+        print(json.dumps({"only": "coulomb", "electrons": sim.count(0), "pairs": st.coulomb_pairs}))
     elif args.only == "init":
         from picfoam_gb300 import abi
         L, n = 0.05, 1e15
