@@ -81,11 +81,11 @@ __global__ void charge_update_mixed_kernel(DMesh m, int volume_weighting, Specie
     const double V = m.vol[c];
     double ccv = 0.0;
     for (int s = 0; s < sv.n; ++s) ccv += sv.v[s] * double(acc9[s * stride + 9 * size_t(c)]);
-    double r = ccv / V;
+    // one division per cell: the FP32 form's density is compared with the
+    // oracle within its tolerance, and FP64 divisions are the cost here
     if (volume_weighting)
-        for (int q = 0; q < 8; ++q)
-            r += (m.vw_weight[8 * size_t(c) + q] * vtx[m.cell_pt[8 * size_t(c) + q]]) / V;
-    rho[c] = r + space_charge;
+        for (int q = 0; q < 8; ++q) ccv += m.vw_weight[8 * size_t(c) + q] * vtx[m.cell_pt[8 * size_t(c) + q]];
+    rho[c] = ccv / V + space_charge;
 }
 
 void launch_charge_update_mixed(const DMesh& m, int vw, const SpeciesValues& sv, const unsigned long long* acc9,

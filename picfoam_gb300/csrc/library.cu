@@ -1111,7 +1111,20 @@ picgpu_status one_step(picgpu_ctx* c, picgpu_step_stats* stats, bool fields) {
     if ((!c->injectors.empty() || !c->freestreams.empty() || !c->emitters.empty()) && (s = inject(c))) return s;
     if ((s = zero_accumulators(c))) return s;
     if ((s = move_species(c, false))) return s;
-    if ((s = read_counters(c))) return s;
+    // Without collisions the charge update needs nothing the host decides
+    // from the move counters (it reads the deposit accumulators only), so it
+    // is queued before the counters are read: one wait per step.
+    const bool colliding = c->cfg.mcc.enabled || c->cfg.coulomb.enabled || c->cfg.ion_mcc.enabled ||
+                           c->cfg.binary.enabled;
+    if (!colliding) {
+        CK(cudaMemcpyAsync(c->counters_host, c->counters, sizeof(pgd::MoveCounters) * c->cfg.n_species,
+                           cudaMemcpyDeviceToHost, c->stream));
+        if ((s = charge_update(c))) return s;
+        CK(cudaStreamSynchronize(c->stream));
+        if (c->profiling) harvest_events(c);
+    } else if ((s = read_counters(c))) {
+        return s;
+    }
     int err = 0;
     for (int k = 0; k < c->cfg.n_species; ++k) err = std::max(err, c->counters_host[k].error);
     if (err)
@@ -1147,10 +1160,10 @@ picgpu_status one_step(picgpu_ctx* c, picgpu_step_stats* stats, bool fields) {
     // collision secondaries of this step come after them
     long n_occ[PICGPU_MAX_SPECIES] = {};
     for (int k = 0; k < c->cfg.n_species; ++k) n_occ[k] = c->sp[k].n;
-    if (c->cfg.mcc.enabled || c->cfg.coulomb.enabled || c->cfg.ion_mcc.enabled || c->cfg.binary.enabled) {
+    if (colliding) {
         if ((s = pgd_collisions(c, stats))) return s;
+        if ((s = charge_update(c))) return s;
     }
-    if ((s = charge_update(c))) return s;
     if (!fields) return PICGPU_OK;
     pgd::launch_floating_update(c->qconv, c->sigma, c->grad_bc, c->stream);
     c->launches++;
