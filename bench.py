@@ -33,11 +33,11 @@ METRIC = "particle-steps/s (push+track+deposit)"
 UNIT = "particle-steps/s"
 BYTES_FP32 = 56   # int32 tet + 3 x f32 barycentric + 3 x f32 velocity, read + write
 BYTES_FP64 = 104  # int32 tet + 3 x f64 barycentric + 3 x f64 velocity, read + write
-# DRAM bytes (read + write) per particle-step of move_kernel_fp32 measured by
-# ncu (dram__bytes_read.sum + dram__bytes_write.sum) on the 40^3 case of this
-# workload; profiles/move_kernel_fp32_two_species_40cube.md.  The traffic is
-# per particle, so a full launch scales by its particles.
-TRAFFIC_FP32_PER_PARTICLE = 44.3
+# DRAM bytes (read + write) per particle-step of move_cell_kernel_fp32 measured
+# by ncu (dram__bytes_read.sum + dram__bytes_write.sum) on this workload at
+# full size (64^3 cells, 50 per cell and species: one electron and one ion
+# launch, 1559 MB for 26.1M particles); profiles/move_cell_kernel_fp32_two_species.md.
+TRAFFIC_FP32_PER_PARTICLE = 59.7
 
 
 def parse():
@@ -699,11 +699,12 @@ def run_ours(args, rank, ws):
                          "frac": achieved / peak,
                          "traffic": (TRAFFIC_FP32_PER_PARTICLE * n_steps_particles / max(move_launches, 1)
                                      if prec == abi.PREC_MIXED else None),
-                         "traffic_source": "ncu dram__bytes_read.sum + dram__bytes_write.sum, 40^3 capture "
-                                           "scaled by particles per launch (profiles/move_kernel_fp32_two_species_40cube.md)",
+                         "traffic_source": "ncu dram__bytes_read.sum + dram__bytes_write.sum of one electron and "
+                                           "one ion launch of this workload, per particle "
+                                           "(profiles/move_cell_kernel_fp32_two_species.md)",
                          "peak_source": f"{peak_kind} (MEASURED_PEAKS.json hbm_gbs)" if peak_kind == "measured"
                          else "fallback 6.8 TB/s",
-                         "kernel": "move_kernel_fp32" if prec == abi.PREC_MIXED else "move_kernel_fp64",
+                         "kernel": "move_cell_kernel_fp32" if prec == abi.PREC_MIXED else "move_kernel_fp64",
                          "bytes_per_particle_step": bytes_pp,
                          "kernel_ms_per_launch": move_ms / max(move_launches, 1),
                          "launches": move_launches},
