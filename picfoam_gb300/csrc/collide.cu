@@ -310,17 +310,25 @@ __device__ __forceinline__ void electron_scatter(int relativistic, double eV, V3
 }
 
 // List cross section, linear between bracketing nodes, end values held
-// (ListCrossSection.C:33-88).
-__device__ double interp_xs(double x, const double* e, const double* v, int n) {
-    if (x <= e[0]) return v[0];
-    if (x >= e[n - 1]) return v[n - 1];
+// (ListCrossSection.C:33-88).  The tables of a collision model share one
+// energy axis, so the bracket is searched once and every table read at it.
+struct XsBracket {
+    int lo, hi;
+    int exact;   // -1 inside the bracket, else the node whose value is returned
+};
+__device__ XsBracket xs_bracket(double x, const double* e, int n) {
+    if (x <= e[0]) return {0, 0, 0};
+    if (x >= e[n - 1]) return {n - 1, n - 1, n - 1};
     int lo = 0, hi = n - 1;
     while (hi - lo > 1) {
         const int mid = (lo + hi) >> 1;
         if (e[mid] <= x) lo = mid; else hi = mid;
     }
-    if (e[lo] == x) return v[lo];
-    return v[lo] + ((x - e[lo]) / (e[hi] - e[lo])) * (v[hi] - v[lo]);
+    return {lo, hi, e[lo] == x ? lo : -1};
+}
+__device__ __forceinline__ double xs_at(const XsBracket& b, double x, const double* e, const double* v) {
+    if (b.exact >= 0) return v[b.exact];
+    return v[b.lo] + ((x - e[b.lo]) / (e[b.hi] - e[b.lo])) * (v[b.hi] - v[b.lo]);
 }
 
 struct MccParams {
@@ -398,9 +406,10 @@ __global__ void mcc_kernel(MccParams M, DSpecies el, Secondary* __restrict__ sta
         const double gamma = 1.0 / sqrt(1.0 - (cR * cR) / (kC * kC));
         double eV = (gamma - 1.0) * M.me * kC * kC / kEch;
         const double sigmaT = sv / cR;
-        const double Qel = interp_xs(eV, E, EL, M.n_xs);
-        const double Qex = interp_xs(eV, E, EX, M.n_xs);
-        const double Qiz = interp_xs(eV, E, IZ, M.n_xs);
+        const XsBracket xb = xs_bracket(eV, E, M.n_xs);
+        const double Qel = xs_at(xb, eV, E, EL);
+        const double Qex = xs_at(xb, eV, E, EX);
+        const double Qiz = xs_at(xb, eV, E, IZ);
         const double Qt = Qel + Qex + Qiz;
         if (Qt * cR > M.svmax[c]) M.svmax[c] = Qt * cR;
         const double Ru = r.uniform();
@@ -558,9 +567,10 @@ __global__ void mcc_parcel_kernel(MccParcelParams M, DSpecies el, DSpecies neu, 
         const double cR = magd(d);
         const double gamma = 1.0 / sqrt(1.0 - (cR * cR) / (kC * kC));
         double eV = (gamma - 1.0) * M.me * kC * kC / kEch;
-        const double Qel = interp_xs(eV, E, EL, M.n_xs);
-        const double Qex = interp_xs(eV, E, EX, M.n_xs);
-        const double Qiz = interp_xs(eV, E, IZ, M.n_xs);
+        const XsBracket xb = xs_bracket(eV, E, M.n_xs);
+        const double Qel = xs_at(xb, eV, E, EL);
+        const double Qex = xs_at(xb, eV, E, EX);
+        const double Qiz = xs_at(xb, eV, E, IZ);
         const double Qt = Qel + Qex + Qiz;
         if (Qt * cR > M.svmax[c]) M.svmax[c] = Qt * cR;
         const double rndU = r.uniform();
@@ -732,8 +742,9 @@ __global__ void ion_parcel_kernel(IonParcelParams M, DSpecies ions, DSpecies neu
         const double cR = magd(d);
         const double gamma = 1.0 / sqrt(1.0 - (cR * cR) / (kC * kC));
         const double eV = (gamma - 1.0) * M.mi * kC * kC / kEch;
-        const double Qel = interp_xs(eV, E, EL, M.n_xs);
-        const double Qcx = interp_xs(eV, E, CX, M.n_xs);
+        const XsBracket xb = xs_bracket(eV, E, M.n_xs);
+        const double Qel = xs_at(xb, eV, E, EL);
+        const double Qcx = xs_at(xb, eV, E, CX);
         const double Qt = Qel + Qcx;
         if (Qt * cR > M.svmax[c]) M.svmax[c] = Qt * cR;
         const double rndU = r.uniform();
@@ -822,8 +833,9 @@ __global__ void ion_mcc_kernel(IonMccParams M, DSpecies ions) {
         const double gamma = 1.0 / sqrt(1.0 - (cR * cR) / (kC * kC));
         const double eV = (gamma - 1.0) * M.mi * kC * kC / kEch;
         const double sigmaT = sv / cR;
-        const double Qel = interp_xs(eV, E, EL, M.n_xs);
-        const double Qcx = interp_xs(eV, E, CX, M.n_xs);
+        const XsBracket xb = xs_bracket(eV, E, M.n_xs);
+        const double Qel = xs_at(xb, eV, E, EL);
+        const double Qcx = xs_at(xb, eV, E, CX);
         const double Qt = Qel + Qcx;
         if (Qt * cR > M.svmax[c]) M.svmax[c] = Qt * cR;
         const double Ru = r.uniform();
