@@ -30,6 +30,7 @@ UNITS = {
     "fields.cu": ["--fmad=false"],
     "particles.cu": [],
     "collide.cu": ["--fmad=false"],
+    "mcc_fp32.cu": ["--use_fast_math"],
     "library.cu": [],
     "pcg_static.cu": ["--fmad=false"],
     "unet_conv.cu": [],

@@ -331,29 +331,6 @@ __device__ __forceinline__ double xs_at(const XsBracket& b, double x, const doub
     return v[b.lo] + ((x - e[b.lo]) / (e[b.hi] - e[b.lo])) * (v[b.hi] - v[b.lo]);
 }
 
-struct MccParams {
-    int n_cells;
-    const int* e_start;   // n_cells + 1
-    const int* e_idx;
-    double* svmax;
-    double* rem;
-    const double* xs;     // 4 x n_xs
-    int n_xs;
-    double n_gas, vth_gas, mg, me, dt;
-    double drift[3];
-    double ex_th, iz_th;
-    double wEwN, wNwE;
-    int create_e, create_i;
-    int relativistic;     // RelativisticElectronNeutral scattering
-    uint64_t seed;
-    uint32_t step;
-    const int* cand_off;  // n_cells + 1
-    unsigned long long* counts;
-    long stage_cap;       // staging slots; a cell whose candidates do not fit drops its secondaries
-    int* overflow;        // raised when that happens
-    unsigned long long* iz_cell;  // optional ionisations per cell
-    const unsigned* step_dev;     // optional: the step index read on the device (graph replays)
-};
 
 __device__ __forceinline__ long mcc_candidates(const MccParams& M, int c, double* coll_out) {
     const int eC = M.e_start[c + 1] - M.e_start[c];
@@ -2156,6 +2133,13 @@ int collide_init(CollideState& st, const picgpu_config& cfg, const DMesh& m, cud
         // remainders seeded U(0,1) (ElectronNeutralCollisionModel.C:286-296)
         const int e = upload_mcc(&st.svmax, &st.remainder, &st.xs, xs, sv, cfg.seed, kStreamRemainder, nc, s, msg);
         if (e) return e;
+        // the FP32 copy the FP32 store's MCC kernel reads
+        const std::vector<float> xs32(xs.begin(), xs.end());
+        if (dmalloc(&st.xs32, xs32.size()) ||
+            cudaMemcpy(st.xs32, xs32.data(), xs32.size() * sizeof(float), cudaMemcpyHostToDevice) != cudaSuccess) {
+            *msg = "MCC tables: device allocation failed";
+            return PICGPU_OOM;
+        }
         if (dmalloc(&st.ncand, nc + 1) || dmalloc(&st.cand_off, nc + 2)) {
             *msg = "MCC state: device allocation failed";
             return PICGPU_OOM;
@@ -2295,7 +2279,7 @@ int collide_init(CollideState& st, const picgpu_config& cfg, const DMesh& m, cud
 }
 
 void collide_free(CollideState& st) {
-    void* ptrs[] = {st.svmax,      st.remainder,   st.xs,     st.isvmax,   st.iremainder, st.ixs,
+    void* ptrs[] = {st.svmax,      st.remainder,   st.xs,     st.xs32,     st.isvmax,   st.iremainder, st.ixs,
                     st.cell_start, st.cell_count,  st.cell_cursor, st.counts, st.scan_tmp, st.ncand,
                     st.cand_off,   st.stage,       st.flags,  st.pos,      st.stage_tmp, st.overflow,
                     st.iz_cell,    st.bsmax,       st.brem,   st.bbgrem,   st.blist,      st.boct,
@@ -2478,11 +2462,13 @@ MccParams mcc_setup(const CollideState& st, const CollideArgs& a) {
     M.svmax = st.svmax;
     M.rem = st.remainder;
     M.xs = st.xs;
+    M.xs32 = st.xs32;
     M.n_xs = st.n_xs;
     M.n_gas = mc.gas_density;
     M.mg = mc.gas_mass;
     M.vth_gas = std::sqrt(kKb * mc.gas_temperature / mc.gas_mass);
     M.me = cfg.species[es].mass;
+    M.me_c2_eV = float(M.me * kC * kC / 1.602176634e-19);
     M.dt = cfg.dt;
     for (int k = 0; k < 3; ++k) M.drift[k] = mc.gas_velocity[k];
     M.ex_th = mc.ex_threshold;
@@ -2824,7 +2810,8 @@ int run_collisions(CollideState& st, const CollideArgs& a, int64_t counts[kColli
         M.stage_cap = st.stage_cap;
         M.overflow = st.overflow;
         M.iz_cell = st.iz_cell;
-        if (a.mixed) mcc_kernel<float><<<(nc + st.mcc_block - 1) / st.mcc_block, st.mcc_block, 0, a.stream>>>(M, a.sp[es], st.stage);
+        if (a.mixed && !M.relativistic && M.xs32) launch_mcc_fp32(M, a.sp[es], st.stage, st.mcc_block, a.stream);
+        else if (a.mixed) mcc_kernel<float><<<(nc + st.mcc_block - 1) / st.mcc_block, st.mcc_block, 0, a.stream>>>(M, a.sp[es], st.stage);
         else mcc_kernel<double><<<(nc + st.mcc_block - 1) / st.mcc_block, st.mcc_block, 0, a.stream>>>(M, a.sp[es], st.stage);
         *launches += 2;
         // append secondaries in (cell, candidate) order
@@ -2991,7 +2978,8 @@ int run_collisions_device(CollideState& st, const CollideArgs& a, int* n_dev, in
         const long scap = st.stage_cap;
         mcc_count_kernel<<<(nc + 255) / 256, 256, 0, a.stream>>>(M, st.ncand);
         exclusive_scan(st.ncand, st.cand_off, nc, st.scan_tmp, a.stream, launches);
-        if (a.mixed) mcc_kernel<float><<<(nc + st.mcc_block - 1) / st.mcc_block, st.mcc_block, 0, a.stream>>>(M, a.sp[es], st.stage);
+        if (a.mixed && !M.relativistic && M.xs32) launch_mcc_fp32(M, a.sp[es], st.stage, st.mcc_block, a.stream);
+        else if (a.mixed) mcc_kernel<float><<<(nc + st.mcc_block - 1) / st.mcc_block, st.mcc_block, 0, a.stream>>>(M, a.sp[es], st.stage);
         else mcc_kernel<double><<<(nc + st.mcc_block - 1) / st.mcc_block, st.mcc_block, 0, a.stream>>>(M, a.sp[es], st.stage);
         *launches += 2;
         for (int bit = 1; bit <= 2; bit <<= 1) {

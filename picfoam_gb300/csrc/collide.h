@@ -22,6 +22,36 @@ struct Secondary {
     double y_i[3];
 };
 
+// Electron-neutral null-collision MCC against the background gas
+// (ElectronNeutralCollisionModel.C:703-829) for one step: the per-cell
+// candidate counts, remainders, (sigma v)_max, tables and the staging of
+// secondaries.
+struct MccParams {
+    int n_cells;
+    const int* e_start;   // n_cells + 1
+    const int* e_idx;
+    double* svmax;
+    double* rem;
+    const double* xs;     // 4 x n_xs
+    const float* xs32;    // the same tables in FP32 (FP32 store), or null
+    float me_c2_eV;       // electron rest energy m c^2 / e [eV] (FP32 kernel)
+    int n_xs;
+    double n_gas, vth_gas, mg, me, dt;
+    double drift[3];
+    double ex_th, iz_th;
+    double wEwN, wNwE;
+    int create_e, create_i;
+    int relativistic;     // RelativisticElectronNeutral scattering
+    uint64_t seed;
+    uint32_t step;
+    const int* cand_off;  // n_cells + 1
+    unsigned long long* counts;
+    long stage_cap;       // staging slots; a cell whose candidates do not fit drops its secondaries
+    int* overflow;        // raised when that happens
+    unsigned long long* iz_cell;  // optional ionisations per cell
+    const unsigned* step_dev;     // optional: the step index read on the device (graph replays)
+};
+
 // A parcel made by PairMerging, staged per cell until it is appended.
 struct MergedParcel {
     int32_t tet;
@@ -61,6 +91,7 @@ struct CollideState {
     double* svmax = nullptr;      // (sigma v)_max per cell
     double* remainder = nullptr;  // collision remainder per cell
     double* xs = nullptr;         // 4 x n_xs: energy, elastic, excitation, ionisation
+    float* xs32 = nullptr;        // the same in FP32 (FP32 store)
     int n_xs = 0;
     double* isvmax = nullptr;     // ion-neutral (sigma v)_max per cell
     double* iremainder = nullptr; // ion-neutral collision remainder per cell
@@ -171,5 +202,11 @@ int merge_append(CollideState& st, const CollideArgs& a, int s, long first, long
 // Merged parcels, candidates checked and the kinetic-energy change of the
 // merges since the last call (and resets them).
 int merge_counters(CollideState& st, cudaStream_t s, long long* merged, long long* checked, double* kin_err);
+
+// The background MCC of the FP32 store in FP32 arithmetic with Nanbu
+// scattering (mcc_fp32.cu): one thread per cell as mcc_kernel, the same
+// candidate count, staging and counters; collisions and secondaries agree
+// with the FP64 kernel statistically.
+void launch_mcc_fp32(const MccParams& M, const DSpecies& el, Secondary* stage, int block, cudaStream_t s);
 
 }  // namespace pgd
