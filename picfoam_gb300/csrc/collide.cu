@@ -127,40 +127,62 @@ void exclusive_scan(const int* in, int* out, long n, int* tmp, cudaStream_t s, i
 }
 
 // ---------------------------------------------------- cell occupancy -----
+// The store is kept in cell order, so the lanes of a warp mostly share a
+// cell: each group of lanes with one cell adds once (its leader), and in the
+// scatter the lanes of a group take consecutive slots in lane order.  The
+// warps step through the store together (whole warps in the loop).
 __global__ void count_cells_kernel(const int32_t* __restrict__ tet, int n, int* __restrict__ count,
                                    const int* n_dev = nullptr) {
     if (n_dev) n = *n_dev;
-    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
-        const int t = tet[i];
-        if (t >= 0) atomicAdd(count + t / 12, 1);
+    const int lane = threadIdx.x & 31;
+    const long stride = long(gridDim.x) * blockDim.x;
+    for (long w = long(blockIdx.x) * blockDim.x + (threadIdx.x & ~31); w < n; w += stride) {
+        const long i = w + lane;
+        const int t = i < n ? tet[i] : -1;
+        const int c = t >= 0 ? t / 12 : -1;
+        const unsigned grp = __match_any_sync(0xffffffffu, c);
+        if (c >= 0 && lane == __ffs(grp) - 1) atomicAdd(count + c, __popc(grp));
     }
 }
 
 __global__ void scatter_cells_kernel(const int32_t* __restrict__ tet, int n, const int* __restrict__ start,
                                      int* __restrict__ cursor, int* __restrict__ idx, const int* n_dev = nullptr) {
     if (n_dev) n = *n_dev;
-    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
-        const int t = tet[i];
-        if (t >= 0) {
-            const int c = t / 12;
-            idx[start[c] + atomicAdd(cursor + c, 1)] = i;
-        }
+    const int lane = threadIdx.x & 31;
+    const long stride = long(gridDim.x) * blockDim.x;
+    for (long w = long(blockIdx.x) * blockDim.x + (threadIdx.x & ~31); w < n; w += stride) {
+        const long i = w + lane;
+        const int t = i < n ? tet[i] : -1;
+        const int c = t >= 0 ? t / 12 : -1;
+        const unsigned grp = __match_any_sync(0xffffffffu, c);
+        const int leader = __ffs(grp) - 1;
+        int b = 0;
+        if (c >= 0 && lane == leader) b = atomicAdd(cursor + c, __popc(grp));
+        b = __shfl_sync(0xffffffffu, b, leader);
+        if (c >= 0) idx[start[c] + b + __popc(grp & ((1u << lane) - 1u))] = int(i);
     }
 }
 
 // Order every cell's list by particle index: one warp per cell; each lane
 // ranks its element against the whole list through shuffles (indices are
 // distinct), writes it to its rank in tmp, and the warp copies the list back.
+// With `need`, only the cells whose need is non-zero (the background MCC's
+// candidate counts, when nothing else reads the lists).
 __global__ void order_cells_kernel(int n_cells, const int* __restrict__ start, int* __restrict__ idx,
-                                   int* __restrict__ tmp) {
+                                   int* __restrict__ tmp, const int* __restrict__ need = nullptr) {
     const int cell = int((long(blockIdx.x) * blockDim.x + threadIdx.x) >> 5);
     const int lane = threadIdx.x & 31;
     if (cell >= n_cells) return;
+    if (need && need[cell] == 0) return;
     const int s0 = start[cell];
     const int L = start[cell + 1] - s0;
     if (L <= 1) return;
     int* a = idx + s0;
     int* t = tmp + s0;
+    // lists whose groups arrived in order are sorted already
+    bool sorted = true;
+    for (int i = lane + 1; i < L; i += 32) sorted = sorted && a[i - 1] < a[i];
+    if (__all_sync(0xffffffffu, sorted)) return;
     for (int base = 0; base < L; base += 32) {
         const int i = base + lane;
         const int v = i < L ? a[i] : 0x7fffffff;
@@ -2749,6 +2771,12 @@ int perez_append(CollideState& st, const CollideArgs& a, long newn[], long long*
     return cudaGetLastError() == cudaSuccess ? PICGPU_OK : PICGPU_CUDA_ERROR;
 }
 
+// The background MCC is the only reader of the cell lists this step.
+bool mcc_lists_only(const picgpu_config& cfg) {
+    return cfg.mcc.enabled && !cfg.mcc.neutral_parcels && !cfg.coulomb.enabled && !cfg.ion_mcc.enabled &&
+           !cfg.binary.enabled;
+}
+
 int run_collisions(CollideState& st, const CollideArgs& a, int64_t counts[kCollideCounts], long newn[], int swapped[],
                    std::string* msg, int64_t* launches, double* phase_ms) {
     (void)phase_ms;
@@ -2757,9 +2785,12 @@ int run_collisions(CollideState& st, const CollideArgs& a, int64_t counts[kColli
     for (int s = 0; s < a.n_species; ++s) { newn[s] = a.n[s]; swapped[s] = 0; }
     cudaMemsetAsync(st.counts, 0, kCollideCounts * sizeof(unsigned long long), a.stream);
     long long perez_electrons = 0;
-    // cell occupancy of every species (PICCloud::buildCellOccupancy)
+    // cell occupancy of every species (PICCloud::buildCellOccupancy); when
+    // the background MCC alone reads the lists, only the cells with
+    // candidates are put in index order (after the candidate count)
+    const bool mcc_only = mcc_lists_only(cfg);
     for (int s = 0; s < a.n_species; ++s) {
-        const int e = occupancy(st, a, s, msg, launches);
+        const int e = occupancy(st, a, s, msg, launches, !mcc_only);
         if (e) return e;
     }
     // Coulomb, electron-neutral, then ion-neutral (PICCloud::collisions,
@@ -2788,6 +2819,11 @@ int run_collisions(CollideState& st, const CollideArgs& a, int64_t counts[kColli
         MccParams M = mcc_setup(st, a);
         // candidates per cell and their staging offsets
         mcc_count_kernel<<<(nc + 255) / 256, 256, 0, a.stream>>>(M, st.ncand);
+        if (mcc_only) {
+            order_cells_kernel<<<order_blocks(nc), 256, 0, a.stream>>>(nc, M.e_start, st.idx[es], st.sel[es],
+                                                                       st.ncand);
+            *launches += 1;
+        }
         exclusive_scan(st.ncand, st.cand_off, nc, st.scan_tmp, a.stream, launches);
         int total = 0;
         cudaMemcpyAsync(&total, st.cand_off + nc, sizeof(int), cudaMemcpyDeviceToHost, a.stream);
@@ -2957,8 +2993,11 @@ int run_collisions_device(CollideState& st, const CollideArgs& a, int* n_dev, in
         exclusive_scan(cnt, start, nc, st.scan_tmp, a.stream, launches);
         scatter_cells_kernel<<<grid_of(cap, 256), 256, 0, a.stream>>>(a.sp[s].tet, int(cap), start, st.cell_cursor,
                                                                       st.idx[s], n_dev + s);
-        order_cells_kernel<<<order_blocks(nc), 256, 0, a.stream>>>(nc, start, st.idx[s], st.sel[s]);
-        *launches += 3;
+        *launches += 2;
+        if (!mcc_lists_only(cfg)) {
+            order_cells_kernel<<<order_blocks(nc), 256, 0, a.stream>>>(nc, start, st.idx[s], st.sel[s]);
+            *launches += 1;
+        }
     }
     if (cfg.coulomb.enabled) {
         CoulombSpecies C;
@@ -2977,6 +3016,11 @@ int run_collisions_device(CollideState& st, const CollideArgs& a, int* n_dev, in
         M.step_dev = step_dev;
         const long scap = st.stage_cap;
         mcc_count_kernel<<<(nc + 255) / 256, 256, 0, a.stream>>>(M, st.ncand);
+        if (mcc_lists_only(cfg)) {
+            order_cells_kernel<<<order_blocks(nc), 256, 0, a.stream>>>(nc, M.e_start, st.idx[es], st.sel[es],
+                                                                       st.ncand);
+            *launches += 1;
+        }
         exclusive_scan(st.ncand, st.cand_off, nc, st.scan_tmp, a.stream, launches);
         if (a.mixed && !M.relativistic && M.xs32) launch_mcc_fp32(M, a.sp[es], st.stage, st.mcc_block, a.stream);
         else if (a.mixed) mcc_kernel<float><<<(nc + st.mcc_block - 1) / st.mcc_block, st.mcc_block, 0, a.stream>>>(M, a.sp[es], st.stage);
