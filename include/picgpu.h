@@ -510,6 +510,15 @@ picgpu_status picgpu_mesh_position(const picgpu_mesh* mesh, size_t n, const int3
 /* Cell centres (n_cells x 3) and volumes (n_cells). */
 picgpu_status picgpu_mesh_cells(const picgpu_mesh* mesh, double* centres, double* volumes);
 
+/* Page-locked host memory for particle and field transfers.  Arrays passed
+ * to picgpu_set_particles / picgpu_get_particles (and the other host-buffer
+ * calls) that lie in such memory go straight to the DMA engine; pageable
+ * arrays are staged through the context's pinned ring by host threads.
+ * picFoam has no counterpart (its parcels live in host memory only).
+ * Free with picgpu_host_free. */
+picgpu_status picgpu_host_alloc(size_t bytes, void** ptr);
+picgpu_status picgpu_host_free(void* ptr);
+
 /* Replace the particles of one species (host buffers, row-major n x 3). */
 picgpu_status picgpu_set_particles(picgpu_ctx* ctx, int species, size_t n,
                                    const int32_t* tet, const double* bary,

@@ -183,6 +183,33 @@ __global__ void order_cells_kernel(int n_cells, const int* __restrict__ start, i
     bool sorted = true;
     for (int i = lane + 1; i < L; i += 32) sorted = sorted && a[i - 1] < a[i];
     if (__all_sync(0xffffffffu, sorted)) return;
+    if (L <= 64) {
+        // bitonic network over 64 slots, element e = lane + 32 r in v[r]
+        // (padding sorts last); pairs (e, e ^ j) hold (min, max) where
+        // e & k == 0, (max, min) elsewhere
+        int v[2] = {lane < L ? a[lane] : 0x7fffffff, lane + 32 < L ? a[lane + 32] : 0x7fffffff};
+        for (int k = 2; k <= 64; k <<= 1) {
+            for (int j = k >> 1; j > 0; j >>= 1) {
+                if (j == 32) {
+                    const int lo = min(v[0], v[1]), hi = max(v[0], v[1]);
+                    const bool up = (lane & k) == 0;
+                    v[0] = up ? lo : hi;
+                    v[1] = up ? hi : lo;
+                } else {
+#pragma unroll
+                    for (int r = 0; r < 2; ++r) {
+                        const int e = lane + 32 * r;
+                        const int w = __shfl_xor_sync(0xffffffffu, v[r], j);
+                        const bool keep_min = ((e & j) == 0) == ((e & k) == 0);
+                        v[r] = keep_min ? min(v[r], w) : max(v[r], w);
+                    }
+                }
+            }
+        }
+        if (lane < L) a[lane] = v[0];
+        if (lane + 32 < L) a[lane + 32] = v[1];
+        return;
+    }
     for (int base = 0; base < L; base += 32) {
         const int i = base + lane;
         const int v = i < L ? a[i] : 0x7fffffff;

@@ -169,8 +169,18 @@ struct HostStager {
         ready = false;
     }
     void par_copy(char* dst, const char* src, size_t n) { pool.copy(dst, src, n); }
+    // page-locked caller memory (picgpu_host_alloc, cudaHostRegister ...)
+    static bool pinned_host(const void* p) {
+        cudaPointerAttributes a{};
+        if (cudaPointerGetAttributes(&a, p) != cudaSuccess) {
+            cudaGetLastError();
+            return false;
+        }
+        return a.type == cudaMemoryTypeHost;
+    }
     cudaError_t upload(void* dev, const void* host, size_t n, cudaStream_t s) {
-        if (n < (size_t(8) << 20) || !init()) return cudaMemcpyAsync(dev, host, n, cudaMemcpyHostToDevice, s);
+        if (n < (size_t(8) << 20) || pinned_host(host) || !init())
+            return cudaMemcpyAsync(dev, host, n, cudaMemcpyHostToDevice, s);
         const char* src = static_cast<const char*>(host);
         char* dst = static_cast<char*>(dev);
         int k = 0;
@@ -185,7 +195,7 @@ struct HostStager {
         return cudaSuccess;
     }
     cudaError_t download(void* host, const void* dev, size_t n, cudaStream_t s) {
-        if (n < (size_t(8) << 20) || !init()) {
+        if (n < (size_t(8) << 20) || pinned_host(host) || !init()) {
             cudaError_t e = cudaMemcpyAsync(host, dev, n, cudaMemcpyDeviceToHost, s);
             return e ? e : cudaStreamSynchronize(s);
         }
@@ -2627,6 +2637,26 @@ picgpu_status picgpu_move(picgpu_ctx* c, picgpu_step_stats* stats) {
     CK(cudaStreamSynchronize(c->stream));
     if (c->profiling) harvest_events(c);
     fill_counts(c, stats);
+    return PICGPU_OK;
+}
+
+picgpu_status picgpu_host_alloc(size_t bytes, void** ptr) {
+    if (!ptr) return PICGPU_INVALID_ARG;
+    *ptr = nullptr;
+    if (bytes == 0) return PICGPU_OK;
+    if (cudaMallocHost(ptr, bytes) != cudaSuccess) {
+        cudaGetLastError();
+        *ptr = nullptr;
+        return PICGPU_OOM;
+    }
+    return PICGPU_OK;
+}
+
+picgpu_status picgpu_host_free(void* ptr) {
+    if (ptr && cudaFreeHost(ptr) != cudaSuccess) {
+        cudaGetLastError();
+        return PICGPU_INVALID_ARG;
+    }
     return PICGPU_OK;
 }
 

@@ -128,5 +128,9 @@ def load():
     lib.picgpu_unet_gradients.argtypes = [P, F32P, F32P, F32P, F32P, F64P]
     lib.picgpu_unet_train.restype = i
     lib.picgpu_unet_train.argtypes = [P, F32P, F32P, F32P, i, C.c_double, F64P]
+    lib.picgpu_host_alloc.restype = i
+    lib.picgpu_host_alloc.argtypes = [C.c_size_t, PP]
+    lib.picgpu_host_free.restype = i
+    lib.picgpu_host_free.argtypes = [P]
     _lib = lib
     return lib

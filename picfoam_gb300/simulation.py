@@ -7,6 +7,7 @@ particle access.  It talks to a backend: the CUDA library by default; the
 test suite plugs the CPU oracle in through the same interface.
 """
 import ctypes as C
+import weakref
 
 import numpy as np
 
@@ -56,6 +57,21 @@ def _f64(a):
 def _i32(a):
     a = np.ascontiguousarray(a, dtype=np.int32)
     return a, a.ctypes.data_as(C.POINTER(C.c_int32))
+
+
+def pinned_empty(shape, dtype):
+    """An uninitialised numpy array in page-locked host memory
+    (picgpu_host_alloc), freed with the array: transfers from and to it go
+    straight to the DMA engine."""
+    lib = native.load()
+    dtype = np.dtype(dtype)
+    nbytes = max(int(np.prod(shape)) * dtype.itemsize, 1)
+    ptr = C.c_void_p()
+    if lib.picgpu_host_alloc(nbytes, C.byref(ptr)) != abi.OK:
+        raise MemoryError(f"picgpu_host_alloc({nbytes}) failed")
+    buf = (C.c_char * nbytes).from_address(ptr.value)
+    weakref.finalize(buf, lib.picgpu_host_free, ptr.value)
+    return np.frombuffer(buf, dtype=dtype, count=int(np.prod(shape))).reshape(shape)
 
 
 class Simulation:
@@ -118,11 +134,20 @@ class Simulation:
         self._check(self._fn("count_particles")(self._h, species, C.byref(n)))
         return n.value
 
-    def get_particles(self, species):
+    def get_particles(self, species, out=None):
+        """(tet, bary, U) of one species in storage order; `out` = three
+        arrays to fill (int32 n, float64 n x 3, float64 n x 3, e.g. from
+        pinned_empty), of at least the species' count."""
         cap = self.count(species)
-        tet = np.zeros(cap, np.int32)
-        bary = np.zeros((cap, 3))
-        U = np.zeros((cap, 3))
+        if out is None:
+            tet = np.zeros(cap, np.int32)
+            bary = np.zeros((cap, 3))
+            U = np.zeros((cap, 3))
+        else:
+            tet, bary, U = out
+            assert tet.dtype == np.int32 and bary.dtype == U.dtype == np.float64
+            assert tet.flags.c_contiguous and bary.flags.c_contiguous and U.flags.c_contiguous
+            cap = min(len(tet), len(bary), len(U))
         n = C.c_size_t()
         self._check(self._fn("get_particles")(
             self._h, species, cap, tet.ctypes.data_as(C.POINTER(C.c_int32)),
