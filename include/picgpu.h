@@ -137,7 +137,7 @@ typedef struct {
     double  charge;         /* [C] per real particle */
     double  weight;         /* nEquivalentParticles */
     int32_t solve_movement; /* solveMovement */
-    int32_t capacity_hint;  /* optional storage capacity (0: automatic) */
+    int32_t capacity_hint;  /* optional storage capacity, allocated with the context with the staging of host arrays (0: automatic) */
 } picgpu_species;
 
 /* Background gas (uniformBackground.C:36-127) and null-collision MCC

@@ -1616,6 +1616,22 @@ picgpu_status picgpu_mesh_cells(const picgpu_mesh* mesh, double* centres, double
 
 static picgpu_status create_with_mesh(picgpu_ctx* c, const picgpu_config* cfg);
 
+// Device staging of row-major host arrays (n tets, n x 3 bary, n x 3 U).
+static picgpu_status ensure_rows(picgpu_ctx* c, size_t n) {
+    if (c->rows_cap >= n) return PICGPU_OK;
+    dfree(c, c->rows_tet);
+    dfree(c, c->rows_y);
+    dfree(c, c->rows_u);
+    c->rows_cap = 0;
+    const size_t cap = std::max<size_t>(n, 1024);
+    picgpu_status s;
+    if ((s = dalloc(c, &c->rows_tet, cap)) || (s = dalloc(c, &c->rows_y, 3 * cap)) ||
+        (s = dalloc(c, &c->rows_u, 3 * cap)))
+        return s;
+    c->rows_cap = cap;
+    return PICGPU_OK;
+}
+
 picgpu_status picgpu_create(const picgpu_mesh_desc* mesh, const picgpu_config* cfg, picgpu_ctx** out) {
     if (!mesh || !cfg || !out) return PICGPU_INVALID_ARG;
     auto* c = new picgpu_ctx();
@@ -1886,10 +1902,15 @@ static picgpu_status create_with_mesh(picgpu_ctx* c, const picgpu_config* cfg) {
     CK(cudaMallocHost(&c->counters_host, sizeof(pgd::MoveCounters) * PICGPU_MAX_SPECIES));
     std::memset(c->st_host, 0, sizeof(pgd::PcgState));
     std::memset(c->counters_host, 0, sizeof(pgd::MoveCounters) * PICGPU_MAX_SPECIES);
+    long max_hint = 0;
     for (int sp = 0; sp < cfg->n_species; ++sp) {
         const long cap = std::max<long>(cfg->species[sp].capacity_hint, 1024);
         if ((s = alloc_species(c, sp, cap))) return s;
+        max_hint = std::max<long>(max_hint, cfg->species[sp].capacity_hint);
     }
+    // with a capacity hint, the staging of host arrays is sized here too, so
+    // that the first picgpu_set_particles allocates nothing
+    if (max_hint > 0 && (s = ensure_rows(c, size_t(max_hint)))) return s;
     if (cfg->maxwell_solver != PICGPU_MAXWELL_ELECTROSTATIC)
         if ((s = set_applied_field(c))) return s;
     std::string msg;
@@ -1969,21 +1990,6 @@ picgpu_status picgpu_mesh_query(const picgpu_ctx* c, picgpu_mesh_info* info) {
     return PICGPU_OK;
 }
 
-// Device staging of row-major host arrays (n tets, n x 3 bary, n x 3 U).
-static picgpu_status ensure_rows(picgpu_ctx* c, size_t n) {
-    if (c->rows_cap >= n) return PICGPU_OK;
-    dfree(c, c->rows_tet);
-    dfree(c, c->rows_y);
-    dfree(c, c->rows_u);
-    c->rows_cap = 0;
-    const size_t cap = std::max<size_t>(n, 1024);
-    picgpu_status s;
-    if ((s = dalloc(c, &c->rows_tet, cap)) || (s = dalloc(c, &c->rows_y, 3 * cap)) ||
-        (s = dalloc(c, &c->rows_u, 3 * cap)))
-        return s;
-    c->rows_cap = cap;
-    return PICGPU_OK;
-}
 
 picgpu_status picgpu_set_particles(picgpu_ctx* c, int species, size_t n, const int32_t* tet,
                                    const double* bary, const double* U) {
