@@ -66,7 +66,8 @@ def parse():
     p.add_argument("--ens-steps", type=int, default=100)
     p.add_argument("--ens-graph", type=int, default=10)
     p.add_argument("--ens-seq-steps", type=int, default=20)
-    p.add_argument("--only", default=None, choices=["electrode", "unet", "ensemble", "init", "coulomb", "learned"],
+    p.add_argument("--only", default=None, choices=["electrode", "unet", "ensemble", "init", "coulomb", "learned",
+                                                   "swarm"],
                    help="profiling drivers: run one workload briefly and print a short summary "
                         "(electrode: electrode_box steps; unet: one forward + train steps; "
                         "ensemble: two graph replays)")
@@ -815,6 +816,14 @@ def run_only(args):
         # electrode geometry with the --ws-* settings (BASELINE config 4 as
         # stated: --ws-ppc 30 --ws-train 500 --ws-measure 2000)
         print(json.dumps({"only": "learned", "poisson_learned_vs_plain": learned_vs_plain(args)}))
+    elif args.only == "swarm":
+        # the electron swarm of the collision benchmark (32x32x256 cells,
+        # 10M electrons, background MCC with the FP32 store)
+        case = cases.electron_swarm()
+        sim = cases.build(case)
+        for _ in range(args.only_steps):
+            st = sim.step(1)
+        print(json.dumps({"only": "swarm", "electrons": sim.count(0), "mcc_candidates": st.mcc_candidates}))
     elif args.only == "coulomb":
         # the Coulomb thermalisation of the swarm workload (16^3 cells, 400
         # electrons per cell, NanbuYonemura + Nanbu), FP32 store

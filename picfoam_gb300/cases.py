@@ -256,6 +256,9 @@ def electron_swarm(nx=32, ny=32, nz=256, N=10_000_000, Ez=1e4, gas_density=1e21,
     u = np.sort(rng.random((N, 3)), axis=1)
     bary = np.stack([u[:, 0], u[:, 1] - u[:, 0], u[:, 2] - u[:, 1]], axis=1)
     U = maxwellian(rng, N, T_e, M_E)
+    # the store in cell order, as picInitialise's per-cell placement leaves it
+    o = np.argsort(tet, kind="stable")
+    tet, bary, U = tet[o], bary[o], U[o]
     parts = {0: (tet, bary, U)}
     if ion_species:
         parts[1] = (np.zeros(0, np.int32), np.zeros((0, 3)), np.zeros((0, 3)))
